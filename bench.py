@@ -1,0 +1,371 @@
+"""Benchmark: FP64 SpGEMM GFLOPS (2 * nnzCub / time) of C = A*A on the
+3D 27-point stencil 96^3 (the workload whose HBM-roofline target the
+project is measured on), through the library's C ABI.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload st27-96|lap256|rmat16-aat] [--cpu-seconds S]
+
+One step = one full SpGEMM: CSR A in device memory -> tile conversion ->
+step 1 -> step 2 -> numeric -> CSR C in device memory (C is freed after the
+step, back into the context's pool).  `value` is timed with CUDA events on
+the library's stream; `e2e` repeats the step through the same C ABI with
+host operands (pinned) and a host C, the copies inside the timed region.
+Under torchrun each rank runs its own replica of the workload (weak scaling)
+and rank 0 prints one JSON line with the max time over ranks.
+
+--impl reference times the reference's own CPU algorithm for the path
+(thmkl_dcsrmultcsr, restated in oracle/tsg_oracle.c) on the host cores, on a
+bounded sample of rows of the same workload per step.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "FP64 SpGEMM GFLOPS (2*nnzCub/s)"
+UNIT = "GFLOP/s"
+
+
+def make_workload(name: str):
+    from tilespgemm_gb300 import matrices as M
+    if name == "st27-96":
+        return M.stencil_27(96, seed=1), "AA", ("3D 27-point stencil 96^3 (n=884,736), values U[0.5,1.5], "
+                                                 "diagonal = row sum, C = A*A")
+    if name == "lap256":
+        return M.laplacian_2d(256), "AA", "2D 5-point Laplacian 256x256 (n=65,536), diag 4, off -1, C = A*A"
+    if name == "rmat16-aat":
+        return M.rmat(16, 16, seed=1), "AAT", "R-MAT 2^16 x 16/row (0.57,0.19,0.19,0.05), values U[-1,1], C = A*A^T"
+    raise SystemExit(f"unknown workload {name}")
+
+
+def operand_b(A, op):
+    if op == "AA":
+        return A
+    from tilespgemm_gb300 import matrices as M
+    return M.transpose(A)
+
+
+def nnzcub(A, B) -> int:
+    rp = np.asarray(B.rowptr, np.int64)
+    lens = rp[1:] - rp[:-1]
+    return int(lens[np.asarray(A.col)].sum())
+
+
+def algorithmic_bytes(A, B, nnz_c: int) -> dict:
+    """Compulsory traffic with int32 indices and FP64 values; B counted even
+    when it aliases A; C's row pointer 4 bytes when nnzC < 2^31, else 8."""
+    a = 4 * (A.m + 1) + 12 * A.nnz
+    b = 4 * (B.m + 1) + 12 * B.nnz
+    c = (4 if nnz_c < 2 ** 31 else 8) * (A.m + 1) + 12 * nnz_c
+    # the numeric step reads A and B and writes C's columns and values
+    return {"total": a + b + c, "numeric": a + b + 12 * nnz_c}
+
+
+def load_peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text())
+        except Exception:
+            pass
+    return {}
+
+
+def load_traffic(workload: str):
+    p = ROOT / "profiles" / "traffic.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text()).get(workload)
+        except Exception:
+            return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi sampling during the timed region (clocks and throttle reasons)."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.f = None
+
+    def __enter__(self):
+        try:
+            self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        if self.proc is None or self.f is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.f.flush()
+        rows = []
+        for line in Path(self.f.name).read_text().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for nm, v in zip(names, r[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def cpu_thmkl_sample(A, B, seconds: float) -> dict:
+    """The reference CPU algorithm (thmkl_dcsrmultcsr restated, all host
+    threads) on a contiguous block of rows from the middle of the matrix,
+    grown until it takes about `seconds`."""
+    from oracle import oracle as O
+    rp = np.asarray(A.rowptr, np.int64)
+    brp = np.asarray(B.rowptr, np.int64)
+    blen = brp[1:] - brp[:-1]
+    mid = A.m // 2
+    rows = 32
+    while True:
+        r0 = max(0, mid - rows // 2)
+        r1 = min(A.m, r0 + rows)
+        t0 = time.perf_counter()
+        O.thmkl_rows(A, B, r0, r1)
+        dt = time.perf_counter() - t0
+        if dt >= seconds * 0.5 or r1 - r0 >= A.m:
+            break
+        rows = int(rows * min(8.0, max(2.0, seconds * 0.6 / max(dt, 1e-3))))
+    cub = int(blen[np.asarray(A.col)[rp[r0]:rp[r1]]].sum())
+    return {"value": 2.0 * cub / dt / 1e9, "unit": UNIT, "cores": O.max_threads(), "kind": "port",
+            "sample": f"rows [{r0},{r1}) of {A.m} ({r1 - r0} rows, {cub} intermediate products, {dt:.2f} s), "
+                      "symbolic + numeric as in thmkl_dcsrmultcsr.c:190-210",
+            "seconds": dt, "rows": r1 - r0, "r0": r0}
+
+
+def run_reference(args) -> None:
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    A, op, desc = make_workload(args.workload)
+    B = operand_b(A, op)
+    from oracle import oracle as O
+    cal = cpu_thmkl_sample(A, B, min(args.cpu_seconds, 4.0))
+    r0, r1 = cal["r0"], cal["r0"] + cal["rows"]
+    rp = np.asarray(A.rowptr, np.int64)
+    blen = np.diff(np.asarray(B.rowptr, np.int64))
+    cub = int(blen[np.asarray(A.col)[rp[r0]:rp[r1]]].sum())
+    for _ in range(args.warmup):
+        O.thmkl_rows(A, B, r0, r1)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        O.thmkl_rows(A, B, r0, r1)
+    dt = (time.perf_counter() - t0) / args.steps
+    val = 2.0 * cub / dt / 1e9
+    out = {
+        "impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"{args.workload}: {desc}", "sample_rows": [r0, r1], "nnz_cub_sample": cub},
+        "cpu_baseline": {"value": val, "unit": UNIT, "cores": O.max_threads(), "kind": "port",
+                         "sample": cal["sample"]},
+        "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out))
+
+
+def run_ours(args) -> None:
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    from tilespgemm_gb300 import Context
+    from tilespgemm_gb300 import _abi
+    from tilespgemm_gb300.api import CSR
+
+    A, op, desc = make_workload(args.workload)
+    B = operand_b(A, op)
+    cub = nnzcub(A, B)
+    ctx = Context(local, phase_times=1)
+    lib = _abi.lib()
+    stream = torch.cuda.ExternalStream(lib.tsg_get_stream(ctx.handle), device=torch.device("cuda", local))
+
+    Ad = A.to_device(local)
+    Ad.rowptr = Ad.rowptr.to(torch.int32)          # the reference's int row pointers
+    for _ in range(args.warmup):
+        oc, st = ctx.spgemm_raw(Ad, op=op, out="device", stats=True)
+        oc.free()
+    nnz_c = st["nnz_c"]
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # ---- device-resident value ----
+    phases = []
+    barrier()
+    l0 = lib.tsg_launch_count()
+    with ClockSampler(local) as clk:
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for _ in range(args.steps):
+            oc, st = ctx.spgemm_raw(Ad, op=op, out="device", stats=True)
+            phases.append(st)
+            oc.free()
+        ev1.record(stream)
+        ev1.synchronize()
+    launches = lib.tsg_launch_count() - l0
+    barrier()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    if dist is not None:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * 2.0 * cub / (ms * 1e6)
+
+    # ---- e2e through the ABI with host operands ----
+    Ah = CSR(A.m, A.n, torch.from_numpy(np.asarray(A.rowptr, np.int32)).pin_memory(),
+             torch.from_numpy(np.asarray(A.col, np.int32)).pin_memory(),
+             torch.from_numpy(np.asarray(A.val, np.float64)).pin_memory())
+    oc, _ = ctx.spgemm_raw(Ah, op=op, out="host")
+    c_rowptr_bytes = 4 * (A.m + 1) if oc.rowptr_bits == 32 else 8 * (A.m + 1)
+    oc.free()
+    barrier()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        oc, _ = ctx.spgemm_raw(Ah, op=op, out="host")
+        oc.free()
+    e1.record(stream)
+    e1.synchronize()
+    barrier()
+    ms_e2e = e0.elapsed_time(e1) / args.steps
+    if dist is not None:
+        t = torch.tensor([ms_e2e], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_e2e = float(t.item())
+    h2d = 4 * (A.m + 1) + 12 * A.nnz
+    d2h = c_rowptr_bytes + 12 * nnz_c
+
+    if rank != 0:
+        ctx.close()
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+
+    peaks = load_peaks()
+    hbm_peak = peaks.get("hbm_gbs")
+    import ctypes
+    fp64 = ctypes.c_double(0.0)
+    _abi.check(lib.tsg_measure_fp64_peak(ctx.handle, ctypes.byref(fp64)))
+    ms_num = statistics.mean(p["ms_step3"] for p in phases)
+    ab = algorithmic_bytes(A, B, nnz_c)
+    achieved = ab["numeric"] / (ms_num * 1e6)
+    traffic = load_traffic(args.workload)
+    roofline = {
+        "kernel": "k_numeric_smem (step 3: FP64 accumulation + CSR write)",
+        "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+        "frac": (achieved / hbm_peak) if hbm_peak else None,
+        "peak_source": "of measured (MEASURED_PEAKS.json hbm_gbs)" if hbm_peak else "of fallback 6800 GB/s",
+        "traffic": traffic,
+        "algorithmic_bytes_per_launch": ab["numeric"], "ms_per_launch": ms_num,
+        "fp64": {"achieved_gflops": 2.0 * cub / (ms_num * 1e6), "peak_gflops": fp64.value,
+                 "frac": 2.0 * cub / (ms_num * 1e6) / fp64.value if fp64.value else None,
+                 "peak_source": "measured live (tsg_measure_fp64_peak, DFMA-only kernel)"},
+        "whole_step": {"achieved_gbs": ab["total"] / (ms * 1e6),
+                       "frac": ab["total"] / (ms * 1e6) / hbm_peak if hbm_peak else None,
+                       "algorithmic_bytes": ab["total"]},
+    }
+    if hbm_peak is None:
+        roofline["peak"] = 6800.0
+        roofline["frac"] = achieved / 6800.0
+    cpu = None
+    if world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_thmkl_sample(A, B, args.cpu_seconds)
+        for k in ("seconds", "rows", "r0"):
+            cpu.pop(k, None)
+    mean = lambda k: statistics.mean(p[k] for p in phases)  # noqa: E731
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator, shapes of the named workload)",
+        "config": {"workload": f"{args.workload}: {desc}", "n": A.m, "nnz_a": A.nnz, "nnz_cub": cub,
+                   "nnz_c": nnz_c, "tiles_a": phases[-1]["tiles_a"], "tiles_c": phases[-1]["tiles_c"],
+                   "l2": "inputs larger than L2: A is %.0f MB and C %.0f MB against a 129 MB L2" % (
+                       (12 * A.nnz + 4 * A.m) / 1e6, 12 * nnz_c / 1e6),
+                   "parallelism": f"one replica per GPU ({world})"},
+        "phases_ms": {"convert": mean("ms_convert"), "step1": mean("ms_step1"), "step2": mean("ms_step2"),
+                      "step3": mean("ms_step3")},
+        "host_waits_per_step": phases[-1]["n_syncs"],
+        "roofline": roofline,
+        "cpu_baseline": cpu,
+        "e2e": {"value": world * 2.0 * cub / (ms_e2e * 1e6), "unit": UNIT, "ms_per_step": ms_e2e,
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": int(launches),
+        "gpu_launches_per_step": launches / args.steps,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(out))
+    ctx.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", default="st27-96")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

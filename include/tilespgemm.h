@@ -1,0 +1,225 @@
+/*
+ * tilespgemm.h -- C ABI of the GB300-native tiled FP64 SpGEMM library
+ * (libtilespgemm.so).  Plain C types only: no C++ or torch types cross it.
+ *
+ * It replaces the SpGEMM call of YuyaoNiu/TileSpGEMM.  In the reference that
+ * call is the CLI driver main_spgemm-col.cu:4821-5577, which loads a Matrix
+ * Market file (mmio_allinone, mmio_highlevel.h:593-759), converts CSR to
+ * 16x16 tiles on the host (main_spgemm-col.cu:4968-5360) and runs the timed
+ * device pipeline stepall_cuda_new (main_spgemm-col.cu:4431-4819), which
+ * discards C.  Here the whole path -- CSR in, tile conversion, tile symbolic,
+ * per-tile masks, numeric, CSR out -- runs on the GPU behind one call.
+ *
+ * Conventions
+ *   - Every entry point returns tsg_status (0 = success).  Nothing exits or
+ *     traps.  tsg_last_error() gives a one-line description of the last
+ *     failure on the calling thread.
+ *   - A context (tsg_ctx) owns one CUDA stream and one stream-ordered memory
+ *     pool on one device.  Calls on one context are not re-entrant; use one
+ *     context per host thread.
+ *   - Values are FP64, column indices int32, row pointers int32 or int64
+ *     (tsg_csr.rowptr_bits).  C's row pointer is int64 whenever its nnz does
+ *     not fit int32, or when the caller asks for 64 bits.
+ */
+#ifndef TILESPGEMM_H
+#define TILESPGEMM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    TSG_OK = 0,
+    TSG_ERR_INVALID_ARG = 1,     /* NULL pointer, bad enum, negative size */
+    TSG_ERR_CUDA = 2,            /* a CUDA runtime call failed */
+    TSG_ERR_OOM = 3,             /* device or pinned host allocation failed */
+    TSG_ERR_INT32_OVERFLOW = 4,  /* result needs int64 row pointers but the caller asked for int32 */
+    TSG_ERR_BAD_MTX = 5,         /* Matrix Market file could not be opened or parsed */
+    TSG_ERR_DEVICE_TIMEOUT = 6,  /* a bounded device-side wait gave up */
+    TSG_ERR_SHAPE = 7,           /* A.n != B.m, or A*A on a non-square A */
+    TSG_ERR_BAD_INPUT = 8,       /* row pointer not monotone / out of range, or column out of range */
+    TSG_ERR_NOT_SUPPORTED = 9,   /* input larger than the supported index ranges */
+    TSG_ERR_BUDGET = 10          /* request does not fit the memory budget it was admitted under */
+} tsg_status;
+
+typedef enum {
+    TSG_OP_AB = 0,   /* C = A * B */
+    TSG_OP_AA = 1,   /* C = A * A   (A square; the reference's default, AAT == 0) */
+    TSG_OP_AAT = 2   /* C = A * A^T (the reference's AAT == 1 build) */
+} tsg_op;
+
+typedef enum {
+    TSG_MEM_HOST = 0,    /* pointers are host memory (pageable or pinned) */
+    TSG_MEM_DEVICE = 1   /* pointers are device memory on the context's device */
+} tsg_mem;
+
+/*
+ * A CSR matrix.  The reference's SMatrix (main_spgemm-col.cu:34-39) plus the
+ * shape and the location of the arrays.
+ *   row_ptr: m+1 entries, int32 or int64 per rowptr_bits (32 or 64)
+ *   col:     nnz int32 column indices (any order inside a row; duplicates are
+ *            summed like the reference's CPU path does)
+ *   val:     nnz doubles
+ * For outputs, set all pointers to NULL: the library allocates them (device
+ * pool or pinned host memory, per `where`) and tsg_csr_free releases them.
+ */
+typedef struct {
+    int32_t m, n;
+    int64_t nnz;
+    int32_t rowptr_bits;   /* 32 or 64 */
+    int32_t where;         /* tsg_mem */
+    void *row_ptr;
+    int32_t *col;
+    double *val;
+    void *owner;           /* library bookkeeping for outputs; NULL for caller-owned input */
+} tsg_csr;
+
+/* Options; tsg_opts_default fills the defaults. */
+typedef struct {
+    int32_t validate;        /* check row pointers and column ranges (default 1) */
+    int32_t phase_times;     /* record per-phase CUDA-event times into tsg_stats (default 0) */
+    int32_t out_rowptr_bits; /* 32, 64, or 0 = 32 when it fits, else 64 (default 0) */
+    int32_t dense_tile_min;  /* C tile-rows whose mean tile nnz is >= this use the dense
+                                16x16 accumulator (default 160; 257 = never) */
+    int32_t smem_acc_max;    /* largest C tile-row (in entries) accumulated in shared memory (default 24576) */
+    int32_t threads_numeric; /* threads per CTA of the numeric kernels: 128, 256 or 512 (default 256) */
+} tsg_opts;
+
+/* Per-call statistics.  Sizes are always filled; times only with phase_times. */
+typedef struct {
+    int64_t nnz_a, nnz_b, nnz_c;
+    int64_t nnz_cub;           /* intermediate products, sum over A(i,k) of nnz(B row k) */
+    int64_t tiles_a, tiles_b, tiles_c;
+    double ms_total;           /* host wall time of the call */
+    double ms_convert;         /* CSR -> tiles for A and B (and B = A^T for AAT) */
+    double ms_step1;           /* tile-level symbolic: C tile structure */
+    double ms_step2;           /* C tile masks, row counts, row pointer scan */
+    double ms_step3;           /* numeric + CSR write */
+    double ms_h2d, ms_d2h;     /* host <-> device copies (host operands only) */
+    int32_t n_syncs;           /* host waits on the device inside the call */
+    int32_t bins[4];           /* C tile-rows per numeric bin: empty, shared sparse, shared dense, global */
+} tsg_stats;
+
+typedef struct tsg_ctx tsg_ctx;
+
+/* ---- context ----------------------------------------------------------- */
+
+/* Fill *o with the defaults listed in tsg_opts. */
+void tsg_opts_default(tsg_opts *o);
+
+/* Create a context on `device`; opts may be NULL (defaults).  Replaces the
+ * reference's cudaSetDevice + per-run stream and cudaMalloc setup
+ * (main_spgemm-col.cu:4856-4862, :4509-4512, spgemm_nsparse_kernel.h:45-90). */
+tsg_status tsg_create(tsg_ctx **ctx, int device, const tsg_opts *opts);
+tsg_status tsg_destroy(tsg_ctx *ctx);
+
+/* Description of the last failure on this thread ("" if none). */
+const char *tsg_last_error(void);
+
+/* Library version string. */
+const char *tsg_version(void);
+
+/* Diagnostics (no counterpart in the reference).  tsg_launch_count: kernel
+ * launches this library has issued in this process.  tsg_get_stream: the
+ * context's cudaStream_t, for ordering caller work or recording CUDA events
+ * around the library's kernels.  tsg_measure_fp64_peak: the device's FP64
+ * FMA throughput in GFLOP/s (2 FLOP per FMA), measured by a short kernel. */
+int64_t tsg_launch_count(void);
+void *tsg_get_stream(tsg_ctx *ctx);
+tsg_status tsg_measure_fp64_peak(tsg_ctx *ctx, double *gflops);
+
+/* ---- matrix market load path ------------------------------------------- */
+
+/*
+ * Load a Matrix Market coordinate file into a host CSR with the semantics of
+ * the reference's mmio_allinone (mmio_highlevel.h:593-759): 1-based indices
+ * become 0-based; symmetric and hermitian files are mirrored with the same
+ * value (the diagonal once); skew-symmetric files are not mirrored; pattern
+ * entries are 1.0; integer values are converted to double; complex files
+ * keep the real part; entries are neither sorted nor merged (file order per
+ * row).  *is_symmetric (may be NULL) is 1 for symmetric/hermitian files.
+ * The arrays are malloc'd host memory with int32 row pointers (the
+ * reference's int); release them with tsg_csr_free(NULL, out).
+ * The reference returns -1 (open), -2 (banner) or -4 (size line); all three
+ * map to TSG_ERR_BAD_MTX here, as do truncated data lines and 'array' files.
+ */
+tsg_status tsg_load_mtx(const char *path, tsg_csr *out, int32_t *is_symmetric);
+
+/* Release arrays that the library allocated into *m (C outputs or a loaded
+ * matrix).  ctx may be NULL for host matrices from tsg_load_mtx. */
+tsg_status tsg_csr_free(tsg_ctx *ctx, tsg_csr *m);
+
+/* ---- SpGEMM -------------------------------------------------------------- */
+
+/*
+ * C = op(A, B) on the context's device.  Replaces stepall_cuda_new
+ * (main_spgemm-col.cu:4431-4819) together with the host tile conversion in
+ * main (main_spgemm-col.cu:4968-5360) and adds the tile -> CSR output the
+ * reference lacks.
+ *   op == TSG_OP_AB : B must be given, A.n == B.m
+ *   op == TSG_OP_AA : B ignored (may be NULL), A.m == A.n
+ *   op == TSG_OP_AAT: B ignored (may be NULL)
+ * A and B may live on host or device (independently).  C is allocated by the
+ * library where C->where says (host: pinned memory; device: the context's
+ * pool) and released with tsg_csr_free.  C's rows list columns in ascending
+ * order, one entry per structural nonzero (an entry whose products cancel to
+ * 0.0 is kept, as in the reference).  stats may be NULL.
+ */
+tsg_status tsg_spgemm(tsg_ctx *ctx, tsg_op op, const tsg_csr *A, const tsg_csr *B,
+                      tsg_csr *C, tsg_stats *stats);
+
+/* ---- tile form (the reference's device format) --------------------------- */
+
+/*
+ * C in the reference's 16x16 tile format, as stepall_cuda_new leaves it on the
+ * device (main_spgemm-col.cu:4567-4658): tile-row pointer, sorted tile
+ * columns, per-tile nnz prefix, 16 uint8 row starts per tile, uint8 local
+ * columns, FP64 values and 16 uint16 row masks (bit 15-c for local column c).
+ * The tile list includes tiles whose element-level product is empty (nnz 0,
+ * mask 0, row starts 0), as the reference's does.  Arrays are device memory
+ * from the context's pool; free with tsg_tiles_free.
+ */
+typedef struct {
+    int32_t m, n;            /* shape of the matrix */
+    int32_t blkm, blkn;      /* ceil(m/16), ceil(n/16) */
+    int64_t numblk;          /* number of tiles */
+    int64_t nnz;
+    int64_t *blkrowptr;      /* blkm+1 */
+    int32_t *blkcolidx;      /* numblk */
+    int64_t *nnzb;           /* numblk+1, exclusive prefix of per-tile nnz */
+    uint8_t *ptr;            /* 16*numblk */
+    uint8_t *col;            /* nnz, local column */
+    double *val;             /* nnz */
+    uint16_t *mask;          /* 16*numblk */
+    void *owner;
+} tsg_tiles;
+
+/* A CSR matrix (any location) -> tile form on the device, in the layout of
+ * the reference's host conversion for A (main_spgemm-col.cu:4968-5240). */
+tsg_status tsg_csr_to_tiles(tsg_ctx *ctx, const tsg_csr *A, tsg_tiles *T);
+
+/* C = op(A, B) returned in tile form (the reference's stepall_cuda_new output). */
+tsg_status tsg_spgemm_tiles(tsg_ctx *ctx, tsg_op op, const tsg_csr *A, const tsg_csr *B,
+                            tsg_tiles *C, tsg_stats *stats);
+
+/* Tile form -> CSR (device), the tile -> CSR output step. */
+tsg_status tsg_tiles_to_csr(tsg_ctx *ctx, const tsg_tiles *T, tsg_csr *C);
+
+tsg_status tsg_tiles_free(tsg_ctx *ctx, tsg_tiles *T);
+
+/* Copy a tile matrix's arrays to caller-provided host buffers (sizes from T). */
+tsg_status tsg_tiles_download(tsg_ctx *ctx, const tsg_tiles *T, int64_t *blkrowptr, int32_t *blkcolidx,
+                              int64_t *nnzb, uint8_t *ptr, uint8_t *col, double *val, uint16_t *mask);
+
+/* Copy a CSR's arrays (any location) to caller-provided host buffers.
+ * row_ptr receives int64 values whatever the source width. */
+tsg_status tsg_csr_download(tsg_ctx *ctx, const tsg_csr *M, int64_t *row_ptr, int32_t *col, double *val);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TILESPGEMM_H */

@@ -1,0 +1,222 @@
+"""GPU parity: the CUDA path (through the C ABI) against the oracle and the
+reference goldens.  Structure is compared bit for bit; values bit for bit
+against the oracle (same accumulation order, same FMA rounding) and within
+1e-12 * sum|a||b| per entry against the reference CPU path."""
+import numpy as np
+import pytest
+
+from conftest import assert_values_close, golden_names, load_case
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+CASES = golden_names()
+
+
+def check_against_oracle(C, A, B, exact=True):
+    rp, col, val, bnd = O.spgemm(A, B, with_bound=True)
+    assert C.m == A.m and C.n == B.n
+    assert np.array_equal(np.asarray(C.rowptr, np.int64), rp)
+    assert np.array_equal(C.col, col)
+    if exact:
+        assert np.array_equal(C.val, val), np.max(np.abs(C.val - val)) if val.size else 0
+    else:
+        assert_values_close(C.val, val, bnd)
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_csr_matches_golden(ctx, name):
+    d = load_case(name)
+    C = ctx.spgemm(d["A"], op=d["op"])
+    assert np.array_equal(np.asarray(C.rowptr, np.int64), d["c_rowptr"])
+    assert np.array_equal(C.col, d["c_col"])
+    if d["exact"]:
+        assert np.array_equal(C.val, d["c_val"])
+    else:
+        _, _, _, bnd = O.spgemm(d["A"], d["B"], with_bound=True)
+        assert_values_close(C.val, d["c_val"], bnd)
+    check_against_oracle(C, d["A"], d["B"])
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_tiles_match_reference_steps(ctx, name):
+    """C's tile form equals the reference's step1..step4 output, including the
+    structurally empty tiles (nnz 0, mask 0, row starts 0)."""
+    d = load_case(name)
+    T = ctx.spgemm_tiles(d["A"], op=d["op"])
+    assert np.array_equal(T.blkrowptr, d["blkrowptrC"].astype(np.int64))
+    assert np.array_equal(T.blkcolidx, d["blkcolidxC"])
+    assert np.array_equal(T.nnzb, d["nnzbC"].astype(np.int64))
+    assert np.array_equal(T.ptr, d["ptrC"])
+    assert np.array_equal(T.col, d["colC"])
+    if d["exact"]:
+        assert np.array_equal(T.val, d["valC"])
+    else:
+        assert np.allclose(T.val, d["valC"], rtol=1e-12, atol=1e-13)
+    ref_mask = O.tile_spgemm(d["A"], d["B"])["mask"]
+    assert np.array_equal(T.mask, ref_mask)
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_csr_to_tiles_matches_oracle(ctx, name):
+    d = load_case(name)
+    T = ctx.csr_to_tiles(d["A"])
+    t = O.tile_csr(d["A"])
+    assert np.array_equal(T.blkrowptr, t["blkrowptr"].astype(np.int64))
+    assert np.array_equal(T.blkcolidx, t["blkcolidx"])
+    assert np.array_equal(T.nnzb, t["nnzb"].astype(np.int64))
+    assert np.array_equal(T.ptr, t["ptr"])
+    assert np.array_equal(T.col, t["lcol"])
+    assert np.array_equal(T.val, t["val"])
+    assert np.array_equal(T.mask, t["mask"])
+    assert np.array_equal(T.blkcolidx, d["a_blkcolidx"])
+
+
+@pytest.mark.parametrize("name", [n for n in CASES if "unsorted" not in n])
+def test_tiles_roundtrip(ctx, name):
+    d = load_case(name)
+    A = d["A"]
+    R = ctx.tiles_roundtrip(A)
+    assert np.array_equal(R.rowptr, A.rowptr)
+    assert np.array_equal(R.col, A.col)
+    assert np.array_equal(R.val, A.val)
+
+
+def _mats():
+    from tilespgemm_gb300 import matrices as M
+    return {
+        "lap64": (M.laplacian_2d(64), "AA"),
+        "lap256": (M.laplacian_2d(256), "AA"),
+        "st27_20": (M.stencil_27(20, seed=3), "AA"),
+        "rand5000": (M.random_sparse(5000, 5000, 10, seed=12), "AA"),
+        "band4000": (M.random_sparse(4000, 4000, 24, seed=13, band=100), "AA"),
+        "rmat12_aat": (M.rmat(12, 16, seed=5), "AAT"),
+        "rmat12_aa": (M.rmat(12, 8, seed=6), "AA"),
+        "rect_aat": (M.random_sparse(700, 2500, 12, seed=14), "AAT"),
+        "dups": (M.random_sparse(1000, 1000, 20, seed=15, dup=True, unsorted=True), "AA"),
+        "empty_rows": (M.random_sparse(3000, 3000, 6, seed=16, empty_rows=0.5), "AA"),
+        "long_rows": (M.random_sparse(64, 64, 60, seed=17), "AA"),
+    }
+
+
+@pytest.mark.parametrize("key", list(_mats().keys()))
+def test_random_matrices_bit_exact(ctx, key):
+    A, op = _mats()[key]
+    B = A if op == "AA" else O_transpose_csr(A)
+    C = ctx.spgemm(A, op=op)
+    check_against_oracle(C, A, B)
+
+
+def O_transpose_csr(A):
+    from tilespgemm_gb300.api import CSR
+    tp, tr, tv = O.transpose(A)
+    return CSR(A.n, A.m, tp, tr, tv)
+
+
+def test_general_ab_rectangular(ctx):
+    from tilespgemm_gb300 import matrices as M
+    A = M.random_sparse(300, 500, 9, seed=21)
+    B = M.random_sparse(500, 170, 7, seed=22)
+    C = ctx.spgemm(A, B, op="AB")
+    check_against_oracle(C, A, B)
+
+
+@pytest.mark.parametrize("opts", [dict(smem_acc_max=0), dict(dense_tile_min=1), dict(threads_numeric=128),
+                                  dict(threads_numeric=512), dict(out_rowptr_bits=64)])
+def test_numeric_bins_agree(opts, built_lib):
+    """Every accumulator path (shared sparse, shared dense, global) gives the
+    same bits."""
+    from tilespgemm_gb300 import Context
+    from tilespgemm_gb300 import matrices as M
+    A = M.stencil_27(12, seed=4)
+    B2 = M.random_sparse(2000, 2000, 15, seed=23, dup=True)
+    with Context(0, **opts) as c:
+        for X in (A, B2):
+            C, st = c.spgemm(X, op="AA", stats=True)
+            check_against_oracle(C, X, X)
+            if opts.get("smem_acc_max") == 0:
+                assert st["bins"][3] > 0
+            if opts.get("dense_tile_min") == 1:
+                assert st["bins"][2] > 0
+            if opts.get("out_rowptr_bits") == 64:
+                assert C.rowptr.dtype == np.int64
+
+
+def test_device_inputs_and_outputs(ctx):
+    import torch
+    from tilespgemm_gb300 import matrices as M
+    A = M.random_sparse(2000, 2000, 8, seed=24)
+    Ad = A.to_device(0)
+    oc, st = ctx.spgemm_raw(Ad, op="AA", out="device", stats=True)
+    assert oc.where == "device"
+    C = oc.download()
+    oc.free()
+    check_against_oracle(C, A, A)
+    assert st["nnz_cub"] == O.nnzcub(A, A)
+    A32 = A.to_device(0)
+    A32.rowptr = A32.rowptr.to(torch.int32)
+    C2 = ctx.spgemm(A32, op="AA")
+    assert np.array_equal(C2.col, C.col) and np.array_equal(C2.val, C.val)
+
+
+def test_stats_and_syncs(ctx):
+    from tilespgemm_gb300 import matrices as M
+    A = M.laplacian_2d(100)
+    C, st = ctx.spgemm(A, op="AA", stats=True)
+    assert st["nnz_c"] == C.nnz and st["nnz_a"] == A.nnz
+    assert st["nnz_cub"] == O.nnzcub(A, A)
+    assert st["n_syncs"] <= 3
+    assert st["tiles_a"] == O.tile_csr(A)["numblk"]
+
+
+def test_empty_and_tiny(ctx):
+    from tilespgemm_gb300.api import CSR
+    Z = CSR(40, 40, np.zeros(41, np.int64), np.zeros(0, np.int32), np.zeros(0))
+    C = ctx.spgemm(Z, op="AA")
+    assert C.nnz == 0 and np.all(C.rowptr == 0)
+    one = CSR(1, 1, np.array([0, 1]), np.array([0], np.int32), np.array([3.0]))
+    C = ctx.spgemm(one, op="AA")
+    assert C.nnz == 1 and C.val[0] == 9.0
+    E = CSR(0, 0, np.zeros(1, np.int64), np.zeros(0, np.int32), np.zeros(0))
+    C = ctx.spgemm(E, op="AA")
+    assert C.m == 0 and C.nnz == 0
+
+
+def test_cancellation_keeps_structural_zero(ctx):
+    """An entry whose products cancel to 0.0 stays in C (the reference's flag
+    is structural, thmkl_dcsrmultcsr.c:63-72)."""
+    from tilespgemm_gb300.api import CSR
+    A = CSR(2, 2, np.array([0, 2, 3]), np.array([0, 1, 0], np.int32), np.array([1.0, 1.0, 1.0]))
+    B = CSR(2, 2, np.array([0, 1, 2]), np.array([0, 0], np.int32), np.array([1.0, -1.0]))
+    C = ctx.spgemm(A, B, op="AB")
+    assert np.array_equal(C.rowptr, [0, 1, 2]) and np.array_equal(C.col, [0, 0])
+    assert C.val[0] == 0.0 and C.val[1] == 1.0
+
+
+def test_invalid_inputs_are_reported(ctx):
+    from tilespgemm_gb300 import TSGError
+    from tilespgemm_gb300.api import CSR
+    bad_col = CSR(3, 3, np.array([0, 1, 2, 3]), np.array([0, 5, 1], np.int32), np.ones(3))
+    with pytest.raises(TSGError) as e:
+        ctx.spgemm(bad_col, op="AA")
+    assert e.value.status == 8
+    bad_rp = CSR(3, 3, np.array([0, 2, 1, 3]), np.array([0, 1, 2], np.int32), np.ones(3))
+    with pytest.raises(TSGError) as e:
+        ctx.spgemm(bad_rp, op="AA")
+    assert e.value.status == 8
+    rect = CSR(2, 3, np.array([0, 1, 2]), np.array([0, 2], np.int32), np.ones(2))
+    with pytest.raises(TSGError) as e:
+        ctx.spgemm(rect, op="AA")
+    assert e.value.status == 7
+    # the context stays usable after errors
+    ok = CSR(2, 2, np.array([0, 1, 2]), np.array([1, 0], np.int32), np.array([2.0, 3.0]))
+    C = ctx.spgemm(ok, op="AA")
+    assert np.array_equal(C.val, [6.0, 6.0])
+
+
+def test_repeat_calls_reuse_pool(ctx):
+    from tilespgemm_gb300 import matrices as M
+    A = M.stencil_27(16, seed=9)
+    first = ctx.spgemm(A, op="AA")
+    for _ in range(3):
+        again = ctx.spgemm(A, op="AA")
+        assert np.array_equal(again.val, first.val) and np.array_equal(again.col, first.col)

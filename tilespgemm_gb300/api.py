@@ -1,0 +1,293 @@
+"""Python host-side mirror of the reference's SpGEMM call, over the C ABI.
+
+The reference (YuyaoNiu/TileSpGEMM) exposes its SpGEMM only through its CLI
+driver (main_spgemm-col.cu:4821-5577): ``mmio_allinone`` loads a Matrix
+Market file into CSR, ``AAT`` (a compile-time switch, :24) selects A*A or
+A*A^T, and ``stepall_cuda_new`` runs the device pipeline and reports nnzC,
+time and GFLOPS = 2*nnzCub/time (:4787).  This module offers the same
+operations as calls:
+
+    A = load_mtx("x.mtx")                       # mmio_allinone semantics
+    with Context(device=0) as ctx:
+        C = ctx.spgemm(A, op="AA")              # CSR in, CSR out (host)
+        C, st = ctx.spgemm(A, op="AAT", stats=True)
+        T = ctx.spgemm_tiles(A, op="AA")        # C in the reference's tile form
+
+Every call goes through libtilespgemm.so; errors raise TSGError with the
+library's status (the reference has no error reporting at all).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+from typing import Any
+
+import numpy as np
+
+from . import _abi
+from ._abi import TSGError, check, lib
+
+_OPS = {"AB": _abi.OP_AB, "AA": _abi.OP_AA, "AAT": _abi.OP_AAT}
+
+
+@dataclass
+class CSR:
+    """A CSR matrix on the host (numpy) or the device (torch CUDA tensors)."""
+    m: int
+    n: int
+    rowptr: Any          # int32 or int64, m+1
+    col: Any             # int32, nnz
+    val: Any             # float64, nnz
+
+    @property
+    def nnz(self) -> int:
+        return int(self.col.shape[0])
+
+    @property
+    def on_device(self) -> bool:
+        return hasattr(self.col, "is_cuda") and bool(self.col.is_cuda)
+
+    @classmethod
+    def from_scipy(cls, s) -> "CSR":
+        s = s.tocsr()
+        return cls(s.shape[0], s.shape[1], np.ascontiguousarray(s.indptr.astype(np.int64)),
+                   np.ascontiguousarray(s.indices.astype(np.int32)),
+                   np.ascontiguousarray(s.data.astype(np.float64)))
+
+    def to_scipy(self):
+        import scipy.sparse as sp
+        return sp.csr_matrix((np.asarray(self.val), np.asarray(self.col), np.asarray(self.rowptr)),
+                             shape=(self.m, self.n))
+
+    def to_device(self, device: int = 0) -> "CSR":
+        import torch
+        dev = torch.device("cuda", device)
+        return CSR(self.m, self.n, torch.as_tensor(np.asarray(self.rowptr)).to(dev),
+                   torch.as_tensor(np.asarray(self.col)).to(dev), torch.as_tensor(np.asarray(self.val)).to(dev))
+
+    def _tsg(self) -> tuple[_abi.tsg_csr, list]:
+        """tsg_csr view of this matrix plus the objects that must stay alive."""
+        s = _abi.tsg_csr()
+        s.m, s.n = int(self.m), int(self.n)
+        keep: list = []
+        if self.on_device:
+            import torch
+            rp, col, val = self.rowptr, self.col, self.val
+            if rp.dtype not in (torch.int32, torch.int64) or col.dtype != torch.int32 or val.dtype != torch.float64:
+                raise TypeError("device CSR needs int32/int64 row pointers, int32 columns, float64 values")
+            rp, col, val = rp.contiguous(), col.contiguous(), val.contiguous()
+            keep += [rp, col, val]
+            s.rowptr_bits = 64 if rp.dtype == torch.int64 else 32
+            s.where = _abi.MEM_DEVICE
+            s.row_ptr, s.col, s.val = rp.data_ptr(), col.data_ptr(), val.data_ptr()
+            s.nnz = int(col.numel())
+            torch.cuda.current_stream(rp.device).synchronize()
+        else:
+            rp = np.asarray(self.rowptr)
+            if rp.dtype not in (np.int32, np.int64):
+                rp = rp.astype(np.int64)
+            rp = np.ascontiguousarray(rp)
+            col = np.ascontiguousarray(np.asarray(self.col), dtype=np.int32)
+            val = np.ascontiguousarray(np.asarray(self.val), dtype=np.float64)
+            keep += [rp, col, val]
+            s.rowptr_bits = 64 if rp.dtype == np.int64 else 32
+            s.where = _abi.MEM_HOST
+            s.row_ptr = rp.ctypes.data
+            s.col = col.ctypes.data if col.size else None
+            s.val = val.ctypes.data if val.size else None
+            s.nnz = int(col.size)
+        s.owner = None
+        return s, keep
+
+
+def _download(ctx_handle, s: _abi.tsg_csr) -> CSR:
+    rp = np.empty(s.m + 1, dtype=np.int64)
+    col = np.empty(s.nnz, dtype=np.int32)
+    val = np.empty(s.nnz, dtype=np.float64)
+    check(lib().tsg_csr_download(ctx_handle, C.byref(s), rp.ctypes.data, col.ctypes.data if s.nnz else None,
+                                 val.ctypes.data if s.nnz else None))
+    return CSR(s.m, s.n, rp, col, val)
+
+
+class OwnedCSR:
+    """A C produced by the library (device pool memory or pinned host memory).
+
+    Valid until ``free()`` (or garbage collection); ``download()`` copies it
+    into plain numpy arrays."""
+
+    def __init__(self, ctx: "Context", s: _abi.tsg_csr):
+        self._ctx = ctx
+        self.s = s
+
+    m = property(lambda self: self.s.m)
+    n = property(lambda self: self.s.n)
+    nnz = property(lambda self: self.s.nnz)
+    rowptr_bits = property(lambda self: self.s.rowptr_bits)
+    where = property(lambda self: "device" if self.s.where == _abi.MEM_DEVICE else "host")
+
+    def download(self) -> CSR:
+        return _download(self._ctx.handle, self.s)
+
+    def free(self) -> None:
+        if self.s.owner:
+            lib().tsg_csr_free(self._ctx.handle, C.byref(self.s))
+
+    def __del__(self):
+        try:
+            if self._ctx.handle:
+                self.free()
+        except Exception:
+            pass
+
+
+@dataclass
+class Tiles:
+    """The reference's 16x16 tile form of a matrix (host copies)."""
+    m: int
+    n: int
+    blkm: int
+    blkn: int
+    blkrowptr: np.ndarray   # int64, blkm+1
+    blkcolidx: np.ndarray   # int32, numblk
+    nnzb: np.ndarray        # int64, numblk+1
+    ptr: np.ndarray         # uint8, 16*numblk
+    col: np.ndarray         # uint8, nnz (local column)
+    val: np.ndarray         # float64, nnz
+    mask: np.ndarray        # uint16, 16*numblk
+
+    @property
+    def numblk(self) -> int:
+        return int(self.blkcolidx.shape[0])
+
+
+def _download_tiles(ctx_handle, t: _abi.tsg_tiles) -> Tiles:
+    nb, nnz = int(t.numblk), int(t.nnz)
+    out = Tiles(t.m, t.n, t.blkm, t.blkn,
+                np.empty(t.blkm + 1, np.int64), np.empty(nb, np.int32), np.empty(nb + 1, np.int64),
+                np.empty(nb * 16, np.uint8), np.empty(nnz, np.uint8), np.empty(nnz, np.float64),
+                np.empty(nb * 16, np.uint16))
+
+    def p(a):
+        return a.ctypes.data if a.size else None
+    check(lib().tsg_tiles_download(ctx_handle, C.byref(t), p(out.blkrowptr), p(out.blkcolidx), p(out.nnzb),
+                                   p(out.ptr), p(out.col), p(out.val), p(out.mask)))
+    return out
+
+
+class Context:
+    """One device, one stream, one memory pool (tsg_create / tsg_destroy)."""
+
+    def __init__(self, device: int = 0, **opts):
+        o = _abi.tsg_opts()
+        lib().tsg_opts_default(C.byref(o))
+        for k, v in opts.items():
+            if not hasattr(o, k):
+                raise TypeError(f"unknown option {k}")
+            setattr(o, k, int(v))
+        self.opts = o
+        h = C.c_void_p()
+        check(lib().tsg_create(C.byref(h), int(device), C.byref(o)))
+        self.handle = h
+        self.device = device
+
+    def close(self) -> None:
+        if self.handle:
+            lib().tsg_destroy(self.handle)
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def spgemm_raw(self, A: CSR, B: CSR | None = None, op: str = "AA", out: str = "host",
+                   stats: bool = False) -> tuple[OwnedCSR, dict | None]:
+        """C = op(A, B) left in library-owned memory (`out` = "host" pinned or "device")."""
+        a, keep_a = A._tsg()
+        b_ptr = None
+        keep_b: list = []
+        if B is not None:
+            b, keep_b = B._tsg()
+            b_ptr = C.byref(b)
+        c = _abi.tsg_csr()
+        c.where = _abi.MEM_DEVICE if out == "device" else _abi.MEM_HOST
+        st = _abi.tsg_stats() if stats else None
+        check(lib().tsg_spgemm(self.handle, _OPS[op], C.byref(a), b_ptr, C.byref(c),
+                               C.byref(st) if st is not None else None))
+        del keep_a, keep_b
+        return OwnedCSR(self, c), (st.as_dict() if st is not None else None)
+
+    def spgemm(self, A: CSR, B: CSR | None = None, op: str = "AA", stats: bool = False):
+        """C = op(A, B) as a host CSR (numpy).  op: "AA", "AAT" or "AB"."""
+        oc, st = self.spgemm_raw(A, B, op, out="host", stats=stats)
+        res = oc.download()
+        oc.free()
+        return (res, st) if stats else res
+
+    def spgemm_tiles(self, A: CSR, B: CSR | None = None, op: str = "AA") -> Tiles:
+        """C = op(A, B) in the reference's tile form (tsg_spgemm_tiles)."""
+        a, keep_a = A._tsg()
+        b_ptr = None
+        keep_b: list = []
+        if B is not None:
+            b, keep_b = B._tsg()
+            b_ptr = C.byref(b)
+        t = _abi.tsg_tiles()
+        check(lib().tsg_spgemm_tiles(self.handle, _OPS[op], C.byref(a), b_ptr, C.byref(t), None))
+        try:
+            return _download_tiles(self.handle, t)
+        finally:
+            lib().tsg_tiles_free(self.handle, C.byref(t))
+            del keep_a, keep_b
+
+    def csr_to_tiles(self, A: CSR) -> Tiles:
+        a, keep = A._tsg()
+        t = _abi.tsg_tiles()
+        check(lib().tsg_csr_to_tiles(self.handle, C.byref(a), C.byref(t)))
+        try:
+            return _download_tiles(self.handle, t)
+        finally:
+            lib().tsg_tiles_free(self.handle, C.byref(t))
+            del keep
+
+    def tiles_roundtrip(self, A: CSR) -> CSR:
+        """CSR -> tiles -> CSR entirely on the device (tsg_csr_to_tiles + tsg_tiles_to_csr)."""
+        a, keep = A._tsg()
+        t = _abi.tsg_tiles()
+        check(lib().tsg_csr_to_tiles(self.handle, C.byref(a), C.byref(t)))
+        c = _abi.tsg_csr()
+        try:
+            check(lib().tsg_tiles_to_csr(self.handle, C.byref(t), C.byref(c)))
+            res = _download(self.handle, c)
+            lib().tsg_csr_free(self.handle, C.byref(c))
+            return res
+        finally:
+            lib().tsg_tiles_free(self.handle, C.byref(t))
+            del keep
+
+
+def load_mtx(path: str) -> tuple[CSR, bool]:
+    """Matrix Market file -> host CSR with mmio_allinone semantics; returns (A, is_symmetric)."""
+    s = _abi.tsg_csr()
+    sym = C.c_int32(0)
+    check(lib().tsg_load_mtx(str(path).encode(), C.byref(s), C.byref(sym)))
+    try:
+        out = _download(None, s)
+        out.rowptr = out.rowptr.astype(np.int32)
+        return out, bool(sym.value)
+    finally:
+        lib().tsg_csr_free(None, C.byref(s))
+
+
+def version() -> str:
+    return lib().tsg_version().decode()
+
+
+__all__ = ["CSR", "Context", "OwnedCSR", "Tiles", "TSGError", "load_mtx", "version"]

@@ -1,0 +1,865 @@
+// tsg_api.cu -- the C ABI (include/tilespgemm.h): contexts, memory, and the
+// device pipeline CSR -> tiles -> step 1 -> step 2 -> step 3 -> CSR.
+//
+// The reference's timed pipeline (stepall_cuda_new, main_spgemm-col.cu:4431-4819)
+// does about 20 cudaMalloc/cudaFree calls, creates streams and makes about 8
+// blocking device->host copies per SpGEMM.  Here a call makes two host waits
+// (after step 1 for C's tile count, after step 2 for C's nnz; both copies
+// also carry the bin sizes and the device error flags), allocates from a
+// stream-ordered pool that keeps its memory cached, and runs everything on
+// one stream.
+#include "tilespgemm.h"
+#include "tsg_internal.cuh"
+#include "tsg_numeric.cuh"
+
+#include <atomic>
+#include <chrono>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+namespace tsg {
+cudaError_t tiles_init_attributes();
+cudaError_t prepare_csr(Pool &pool, const void *rp, int rp_bits, const int *col, int m, int n, long long nnz,
+                        long long *rp_out, int *flags, bool check_cols);
+cudaError_t csr_to_tile_structure(Pool &pool, const long long *rp, const int *col, TileCSR &T, bool masks,
+                                  int *flags, int *stat_max);
+cudaError_t tile_symbolic(Pool &pool, const TileCSR &A, const TileCSR &B, long long *crp, int *ccol, int *cnt,
+                          int *flags, int *stat_max);
+cudaError_t csr_transpose(Pool &pool, const long long *rp, const int *col, const double *val, int m, int n,
+                          long long nnz, long long *tp, int *tcol, double *tval, int *flags);
+cudaError_t aux_nnzcub(Pool &pool, const long long *rpA, const int *colA, int m, const long long *rpB, int kB,
+                       unsigned long long *out);
+cudaError_t aux_mask_popc(Pool &pool, const int *trp, int blkm, const uint16_t *mask, unsigned long long *out);
+cudaError_t aux_copy_scalars(Pool &pool, const long long *a, long long *da, const int *b, long long *db,
+                             const int *c, long long *dc);
+cudaError_t aux_rowptr_narrow(Pool &pool, const long long *in, int *out, long long n);
+cudaError_t tiles_from_csr_c(Pool &pool, int m, int blkm, long long numblk, const long long *crp, const int *ccol,
+                             const uint16_t *cmask, const long long *rowptr, const int *col, const double *val,
+                             long long *nnzb, uint8_t *ptr, uint8_t *lcol, double *tval, int *flags);
+cudaError_t tiles_payload_a(Pool &pool, int m, int n, const long long *rp, const int *col, const double *val,
+                            const TileCSR &T, long long numblk, long long *nnzb, uint8_t *ptr, uint8_t *lcol,
+                            double *tval, int *flags);
+cudaError_t fp64_peak(cudaStream_t s, cudaEvent_t e0, cudaEvent_t e1, double *gflops);
+cudaError_t csr_from_tiles(Pool &pool, int m, const long long *brp, const int *bcol, const long long *nnzb,
+                           const uint8_t *ptr, const uint8_t *lcol, const double *tval, long long *rowptr, int *col,
+                           double *val, int *flags, bool fill);
+}  // namespace tsg
+
+using namespace tsg;
+
+static thread_local std::string g_err;
+static std::atomic<long long> g_launches{0};
+
+void tsg::count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+namespace tsg {
+void set_last_error(const char *msg) { g_err = msg; }
+}
+
+static tsg_status fail(tsg_status st, const char *fmt, ...) __attribute__((format(printf, 2, 3)));
+static tsg_status fail(tsg_status st, const char *fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return st;
+}
+
+#define CUDA_OK(call)                                                                                  \
+    do {                                                                                               \
+        cudaError_t e_ = (call);                                                                       \
+        if (e_ != cudaSuccess) {                                                                       \
+            return fail(e_ == cudaErrorMemoryAllocation ? TSG_ERR_OOM : TSG_ERR_CUDA, "%s: %s (%s:%d)", \
+                        #call, cudaGetErrorString(e_), __FILE__, __LINE__);                            \
+        }                                                                                              \
+    } while (0)
+
+struct tsg_ctx {
+    int device = 0;
+    tsg_opts opts{};
+    cudaStream_t stream = nullptr;
+    cudaMemPool_t pool = nullptr;
+    int *dflags = nullptr;           // FLAG_COUNT ints
+    long long *dstat = nullptr;      // 64 slots
+    long long *hstat = nullptr;      // pinned mirror: 64 stat slots + FLAG_COUNT flags (as long long)
+    std::mutex mu;
+    std::multimap<size_t, void *> pinned_cache;
+    cudaEvent_t ev[8] = {};
+};
+
+namespace {
+
+enum StatSlot {
+    ST_NUMBLKC = 0, ST_MAXS = 1, ST_TILESA = 2, ST_TILESB = 3, ST_NNZCUB = 4, ST_POPCB = 5, ST_NNZC = 6,
+    ST_BINS = 8,                 // NBIN counts, then NBIN max shared-memory sizes
+    ST_HFLAGS = 40,              // host mirror only: device flags
+    ST_SLOTS = 64
+};
+
+struct OutOwner {
+    int where = TSG_MEM_DEVICE;
+    tsg_ctx *ctx = nullptr;
+    std::vector<std::pair<void *, size_t>> blocks;
+};
+
+void *pinned_get(tsg_ctx *ctx, size_t bytes)
+{
+    if (bytes == 0) bytes = 16;
+    {
+        std::lock_guard<std::mutex> lk(ctx->mu);
+        auto it = ctx->pinned_cache.lower_bound(bytes);
+        if (it != ctx->pinned_cache.end() && it->first <= bytes + bytes / 4 + (1 << 20)) {
+            void *p = it->second;
+            ctx->pinned_cache.erase(it);
+            return p;
+        }
+    }
+    void *p = nullptr;
+    if (cudaMallocHost(&p, bytes) != cudaSuccess) { cudaGetLastError(); return nullptr; }
+    return p;
+}
+
+void pinned_put(tsg_ctx *ctx, void *p, size_t bytes)
+{
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    ctx->pinned_cache.emplace(bytes == 0 ? 16 : bytes, p);
+}
+
+// device-side view of a CSR operand (after upload and preparation)
+struct DevCSR {
+    int m = 0, n = 0;
+    long long nnz = 0;
+    long long *rp = nullptr;   // int64, clamped
+    const int *col = nullptr;
+    const double *val = nullptr;
+};
+
+// Everything one call allocates from the pool; released together.
+struct Scratch {
+    Pool &pool;
+    std::vector<void *> ptrs;
+    explicit Scratch(Pool &p) : pool(p) {}
+    template <class T> T *get(long long n) {
+        T *p = pool.alloc_n<T>(n);
+        if (p) ptrs.push_back(p);
+        return p;
+    }
+    ~Scratch() { for (void *p : ptrs) pool.free(p); }
+};
+
+tsg_status check_csr(const tsg_csr *M, const char *name)
+{
+    if (!M) return fail(TSG_ERR_INVALID_ARG, "%s is NULL", name);
+    if (M->m < 0 || M->n < 0 || M->nnz < 0) return fail(TSG_ERR_INVALID_ARG, "%s has a negative size", name);
+    if (M->rowptr_bits != 32 && M->rowptr_bits != 64) return fail(TSG_ERR_INVALID_ARG, "%s.rowptr_bits must be 32 or 64", name);
+    if (M->where != TSG_MEM_HOST && M->where != TSG_MEM_DEVICE) return fail(TSG_ERR_INVALID_ARG, "%s.where is not a tsg_mem", name);
+    if (!M->row_ptr) return fail(TSG_ERR_INVALID_ARG, "%s.row_ptr is NULL", name);
+    if (M->nnz > 0 && (!M->col || !M->val)) return fail(TSG_ERR_INVALID_ARG, "%s.col/val is NULL", name);
+    if (M->nnz >= (1ll << 31)) return fail(TSG_ERR_NOT_SUPPORTED, "%s has %lld entries; operands are limited to 2^31-1", name, (long long)M->nnz);
+    if (M->m > (1 << 30) || M->n > (1 << 30)) return fail(TSG_ERR_NOT_SUPPORTED, "%s is larger than 2^30 rows or columns", name);
+    return TSG_OK;
+}
+
+// Upload (if on the host) and prepare one operand.
+tsg_status stage_operand(tsg_ctx *ctx, Pool &pool, Scratch &sc, const tsg_csr *M, bool validate, DevCSR &D)
+{
+    D.m = M->m; D.n = M->n; D.nnz = M->nnz;
+    const void *rp = M->row_ptr;
+    const int *col = M->col;
+    const double *val = M->val;
+    const size_t rpb = (size_t)(M->m + 1) * (M->rowptr_bits == 64 ? 8 : 4);
+    if (M->where == TSG_MEM_HOST) {
+        void *drp = sc.get<char>((long long)rpb);
+        int *dcol = sc.get<int>(M->nnz);
+        double *dval = sc.get<double>(M->nnz);
+        if (!drp || !dcol || !dval) return fail(TSG_ERR_OOM, "device pool allocation failed for an operand");
+        CUDA_OK(cudaMemcpyAsync(drp, rp, rpb, cudaMemcpyHostToDevice, ctx->stream));
+        if (M->nnz > 0) {
+            CUDA_OK(cudaMemcpyAsync(dcol, col, sizeof(int) * (size_t)M->nnz, cudaMemcpyHostToDevice, ctx->stream));
+            CUDA_OK(cudaMemcpyAsync(dval, val, sizeof(double) * (size_t)M->nnz, cudaMemcpyHostToDevice, ctx->stream));
+        }
+        rp = drp; col = dcol; val = dval;
+    }
+    D.rp = sc.get<long long>(M->m + 1);
+    if (!D.rp) return fail(TSG_ERR_OOM, "device pool allocation failed");
+    CUDA_OK(prepare_csr(pool, rp, M->rowptr_bits, col, M->m, M->n, M->nnz, D.rp, ctx->dflags, validate));
+    D.col = col; D.val = val;
+    return TSG_OK;
+}
+
+tsg_status build_tiles(Pool &pool, Scratch &sc, const DevCSR &D, TileCSR &T, tsg_ctx *ctx)
+{
+    T.m = D.m; T.n = D.n;
+    T.blkm = ceil_div_i(D.m, TILE);
+    T.blkn = ceil_div_i(D.n, TILE);
+    long long cap = D.nnz;
+    if ((long long)T.blkm * T.blkn < cap) cap = (long long)T.blkm * T.blkn;
+    T.cap = cap;
+    T.trp = sc.get<int>(T.blkm + 1);
+    T.tcol = sc.get<int>(cap);
+    T.mask = sc.get<uint16_t>(cap * TILE + 2);
+    if (!T.trp || !T.tcol || !T.mask) return fail(TSG_ERR_OOM, "device pool allocation failed for tiles");
+    CUDA_OK(csr_to_tile_structure(pool, D.rp, D.col, T, true, ctx->dflags, nullptr));
+    return TSG_OK;
+}
+
+tsg_status read_flags(tsg_ctx *ctx)
+{
+    long long *hf = ctx->hstat + ST_HFLAGS;
+    if (hf[FLAG_BAD_INPUT]) return fail(TSG_ERR_BAD_INPUT, "row pointer not monotone/in range or column index out of range");
+    if (hf[FLAG_TIMEOUT]) return fail(TSG_ERR_DEVICE_TIMEOUT, "a bounded device wait gave up");
+    if (hf[FLAG_OVERFLOW]) return fail(TSG_ERR_NOT_SUPPORTED, "an index count overflowed its type");
+    if (hf[FLAG_INTERNAL]) return fail(TSG_ERR_CUDA, "internal bound check failed on the device");
+    return TSG_OK;
+}
+
+// device -> pinned mirror of stats and flags, then wait
+tsg_status host_wait(tsg_ctx *ctx, int *nsync)
+{
+    CUDA_OK(cudaMemcpyAsync(ctx->hstat, ctx->dstat, sizeof(long long) * ST_HFLAGS, cudaMemcpyDeviceToHost, ctx->stream));
+    static_assert(FLAG_COUNT <= ST_SLOTS - ST_HFLAGS, "flag mirror");
+    int hflags[FLAG_COUNT];
+    CUDA_OK(cudaMemcpyAsync(ctx->hstat + ST_HFLAGS + 16, ctx->dflags, sizeof(int) * FLAG_COUNT, cudaMemcpyDeviceToHost, ctx->stream));
+    CUDA_OK(cudaStreamSynchronize(ctx->stream));
+    memcpy(hflags, ctx->hstat + ST_HFLAGS + 16, sizeof(hflags));
+    for (int f = 0; f < FLAG_COUNT; ++f) ctx->hstat[ST_HFLAGS + f] = hflags[f];
+    if (nsync) ++*nsync;
+    return read_flags(ctx);
+}
+
+double ms_since(std::chrono::steady_clock::time_point t0)
+{
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+struct PhaseTimer {
+    tsg_ctx *ctx;
+    bool on;
+    int n = 0;
+    PhaseTimer(tsg_ctx *c, bool enable) : ctx(c), on(enable) {}
+    void mark() { if (on && n < 8) cudaEventRecord(ctx->ev[n++], ctx->stream); }
+    double between(int a, int b) {
+        if (!on || b >= n) return 0.0;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ctx->ev[a], ctx->ev[b]);
+        return ms;
+    }
+};
+
+// The pipeline.  Produces C's CSR on the device (rowptr int64, col, val, all
+// owned by the caller of this function) plus C's tile structure when
+// `keep_tiles` is non-null.
+struct CTiles {
+    int blkm = 0;
+    long long numblk = 0;
+    long long *crp = nullptr;
+    int *ccol = nullptr;
+    uint16_t *cmask = nullptr;
+};
+
+tsg_status run_pipeline(tsg_ctx *ctx, Pool &pool, Scratch &sc, tsg_op op, const tsg_csr *A, const tsg_csr *B,
+                        long long **rowptrC, int **colC, double **valC, long long *nnzC_out, int *mC, int *nC,
+                        tsg_stats *st, CTiles *keep_tiles)
+{
+    const bool validate = ctx->opts.validate != 0;
+    PhaseTimer tm(ctx, st && ctx->opts.phase_times);
+    int nsync = 0;
+    auto t_begin = std::chrono::steady_clock::now();
+
+    tsg_status r = check_csr(A, "A");
+    if (r) return r;
+    if (op == TSG_OP_AB) {
+        r = check_csr(B, "B");
+        if (r) return r;
+        if (A->n != B->m) return fail(TSG_ERR_SHAPE, "A is %d x %d but B is %d x %d", A->m, A->n, B->m, B->n);
+    } else if (op == TSG_OP_AA) {
+        if (A->m != A->n) return fail(TSG_ERR_SHAPE, "A*A needs a square A (got %d x %d)", A->m, A->n);
+    } else if (op != TSG_OP_AAT) {
+        return fail(TSG_ERR_INVALID_ARG, "unknown op %d", (int)op);
+    }
+
+    CUDA_OK(cudaMemsetAsync(ctx->dflags, 0, sizeof(int) * FLAG_COUNT, ctx->stream));
+    CUDA_OK(cudaMemsetAsync(ctx->dstat, 0, sizeof(long long) * ST_SLOTS, ctx->stream));
+    tm.mark();  // 0
+
+    DevCSR dA, dB;
+    r = stage_operand(ctx, pool, sc, A, validate, dA);
+    if (r) return r;
+    if (op == TSG_OP_AB) {
+        r = stage_operand(ctx, pool, sc, B, validate, dB);
+        if (r) return r;
+    } else if (op == TSG_OP_AA) {
+        dB = dA;
+    } else {
+        dB.m = dA.n; dB.n = dA.m; dB.nnz = dA.nnz;
+        long long *tp = sc.get<long long>(dA.n + 1);
+        int *tc = sc.get<int>(dA.nnz);
+        double *tv = sc.get<double>(dA.nnz);
+        if (!tp || !tc || !tv) return fail(TSG_ERR_OOM, "device pool allocation failed for A^T");
+        CUDA_OK(csr_transpose(pool, dA.rp, dA.col, dA.val, dA.m, dA.n, dA.nnz, tp, tc, tv, ctx->dflags));
+        dB.rp = tp; dB.col = tc; dB.val = tv;
+    }
+    const int m = dA.m, n = dB.n;
+    *mC = m; *nC = n;
+
+    TileCSR TA, TB;
+    r = build_tiles(pool, sc, dA, TA, ctx);
+    if (r) return r;
+    if (op == TSG_OP_AA) TB = TA;
+    else {
+        r = build_tiles(pool, sc, dB, TB, ctx);
+        if (r) return r;
+    }
+    tm.mark();  // 1
+
+    // step 1, count: C's tile-row pointer
+    const int blkm = TA.blkm;
+    long long *crp = sc.get<long long>(blkm + 1);
+    int *cnt = sc.get<int>(blkm + 1);
+    if (!crp || !cnt) return fail(TSG_ERR_OOM, "device pool allocation failed (step 1)");
+    CUDA_OK(tile_symbolic(pool, TA, TB, crp, nullptr, cnt, ctx->dflags, (int *)(ctx->dstat + ST_MAXS)));
+    CUDA_OK(aux_copy_scalars(pool, crp + blkm, ctx->dstat + ST_NUMBLKC, TA.trp + TA.blkm, ctx->dstat + ST_TILESA,
+                             TB.trp + TB.blkm, ctx->dstat + ST_TILESB));
+    CUDA_OK(aux_mask_popc(pool, TB.trp, TB.blkm, TB.mask, (unsigned long long *)(ctx->dstat + ST_POPCB)));
+    if (st) CUDA_OK(aux_nnzcub(pool, dA.rp, dA.col, m, dB.rp, dB.m, (unsigned long long *)(ctx->dstat + ST_NNZCUB)));
+    r = host_wait(ctx, &nsync);
+    if (r) return r;
+    const long long numblkC = ctx->hstat[ST_NUMBLKC];
+    const int maxS = (int)(ctx->hstat[ST_MAXS] & 0xffffffff);
+    const long long tilesA = ctx->hstat[ST_TILESA], tilesB = ctx->hstat[ST_TILESB];
+    const bool dupsafe = ctx->hstat[ST_POPCB] != dB.nnz;
+    const long long nnzcub = ctx->hstat[ST_NNZCUB];
+    if (numblkC >= (1ll << 31)) return fail(TSG_ERR_NOT_SUPPORTED, "C has %lld tiles; the limit is 2^31-1", numblkC);
+
+    // step 1, fill: C's sorted tile columns
+    int *ccol = keep_tiles ? pool.alloc_n<int>(numblkC) : sc.get<int>(numblkC);
+    uint16_t *cmask = keep_tiles ? pool.alloc_n<uint16_t>(numblkC * TILE + 2) : sc.get<uint16_t>(numblkC * TILE + 2);
+    if (keep_tiles) {
+        keep_tiles->ccol = ccol; keep_tiles->cmask = cmask;
+    }
+    if (!ccol || !cmask) return fail(TSG_ERR_OOM, "device pool allocation failed for C tiles");
+    CUDA_OK(tile_symbolic(pool, TA, TB, crp, ccol, cnt, ctx->dflags, nullptr));
+    tm.mark();  // 2
+
+    // step 2: masks, row counts, row pointer, bins
+    int *rowcnt = sc.get<int>(m + 1);
+    unsigned char *bin = sc.get<unsigned char>(blkm + 1);
+    long long *rowptr = pool.alloc_n<long long>(m + 1);
+    if (!rowcnt || !bin || !rowptr) { pool.free(rowptr); return fail(TSG_ERR_OOM, "device pool allocation failed (step 2)"); }
+    *rowptrC = rowptr;
+    NumericBinParams bp{ctx->opts.dense_tile_min, ctx->opts.smem_acc_max};
+    CUDA_OK(step2_masks(pool, TA, TB, m, blkm, crp, ccol, cmask, rowcnt, maxS, bp, bin, ctx->dstat + ST_BINS,
+                        ctx->dflags));
+    CUDA_OK(scan_i32_to_i64(pool, rowcnt, rowptr, m, ctx->dflags));
+    CUDA_OK(cudaMemcpyAsync(ctx->dstat + ST_NNZC, rowptr + m, sizeof(long long), cudaMemcpyDeviceToDevice, ctx->stream));
+    r = host_wait(ctx, &nsync);
+    if (r) return r;
+    const long long nnzC = ctx->hstat[ST_NNZC];
+    long long counts[NBIN], req[NBIN];
+    for (int b = 0; b < NBIN; ++b) { counts[b] = ctx->hstat[ST_BINS + b]; req[b] = ctx->hstat[ST_BINS + NBIN + b]; }
+    tm.mark();  // 3
+
+    // step 3: numeric
+    int *col = pool.alloc_n<int>(nnzC);
+    double *val = pool.alloc_n<double>(nnzC);
+    *colC = col; *valC = val;
+    if (!col || !val) return fail(TSG_ERR_OOM, "device pool allocation failed for C (%lld entries)", nnzC);
+    NumericArgs na{};
+    na.m = m; na.blkm = blkm;
+    na.rpA = dA.rp; na.colA = dA.col; na.valA = dA.val;
+    na.rpB = dB.rp; na.colB = dB.col; na.valB = dB.val;
+    na.crp = crp; na.ccol = ccol; na.cmask = cmask;
+    na.rowptrC = rowptr; na.colC = col; na.valC = val;
+    na.bin = bin; na.flags = ctx->dflags;
+    if (counts[BIN_GLOBAL] > 0) {
+        na.offC = sc.get<int>(numblkC * TILE);
+        if (!na.offC) return fail(TSG_ERR_OOM, "device pool allocation failed (global bin offsets)");
+    }
+    CUDA_OK(numeric_run(pool, na, counts, req, dupsafe, ctx->opts.threads_numeric));
+    tm.mark();  // 4
+    *nnzC_out = nnzC;
+
+    if (keep_tiles) {
+        keep_tiles->blkm = blkm;
+        keep_tiles->numblk = numblkC;
+        keep_tiles->crp = crp;
+        // crp belongs to the scratch set; hand the caller its own copy
+        long long *crp2 = pool.alloc_n<long long>(blkm + 1);
+        if (!crp2) return fail(TSG_ERR_OOM, "device pool allocation failed");
+        CUDA_OK(cudaMemcpyAsync(crp2, crp, sizeof(long long) * (blkm + 1), cudaMemcpyDeviceToDevice, ctx->stream));
+        keep_tiles->crp = crp2;
+    }
+
+    if (st) {
+        st->nnz_a = dA.nnz; st->nnz_b = dB.nnz; st->nnz_c = nnzC;
+        st->nnz_cub = nnzcub;
+        st->tiles_a = tilesA; st->tiles_b = tilesB; st->tiles_c = numblkC;
+        st->n_syncs = nsync;
+        st->bins[0] = (int)counts[BIN_EMPTY];
+        st->bins[1] = (int)(counts[BIN_SPARSE_S] + counts[BIN_SPARSE_L]);
+        st->bins[2] = (int)(counts[BIN_DENSE_S] + counts[BIN_DENSE_L]);
+        st->bins[3] = (int)counts[BIN_GLOBAL];
+    }
+    (void)t_begin;
+    return TSG_OK;
+}
+
+tsg_status finish_stats(tsg_ctx *ctx, tsg_stats *st, PhaseTimer *tm)
+{
+    (void)ctx; (void)st; (void)tm;
+    return TSG_OK;
+}
+
+}  // namespace
+
+// ============================================================================
+// C ABI
+// ============================================================================
+
+extern "C" {
+
+void tsg_opts_default(tsg_opts *o)
+{
+    if (!o) return;
+    o->validate = 1;
+    o->phase_times = 0;
+    o->out_rowptr_bits = 0;
+    o->dense_tile_min = 160;
+    o->smem_acc_max = 24576;
+    o->threads_numeric = 256;
+}
+
+const char *tsg_last_error(void) { return g_err.c_str(); }
+
+const char *tsg_version(void) { return "tilespgemm-gb300 0.1 (sm_103a)"; }
+
+int64_t tsg_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
+
+void *tsg_get_stream(tsg_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
+
+tsg_status tsg_measure_fp64_peak(tsg_ctx *ctx, double *gflops)
+{
+    if (!ctx || !gflops) return fail(TSG_ERR_INVALID_ARG, "ctx/gflops is NULL");
+    CUDA_OK(cudaSetDevice(ctx->device));
+    double best = 0.0;
+    CUDA_OK(tsg::fp64_peak(ctx->stream, ctx->ev[6], ctx->ev[7], &best));
+    *gflops = best;
+    return TSG_OK;
+}
+
+tsg_status tsg_create(tsg_ctx **out, int device, const tsg_opts *opts)
+{
+    if (!out) return fail(TSG_ERR_INVALID_ARG, "ctx out-pointer is NULL");
+    *out = nullptr;
+    int ndev = 0;
+    CUDA_OK(cudaGetDeviceCount(&ndev));
+    if (device < 0 || device >= ndev) return fail(TSG_ERR_INVALID_ARG, "device %d out of range (%d devices)", device, ndev);
+    CUDA_OK(cudaSetDevice(device));
+    int major = 0, minor = 0;
+    CUDA_OK(cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, device));
+    CUDA_OK(cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, device));
+    if (major * 10 + minor != 103)
+        return fail(TSG_ERR_NOT_SUPPORTED, "device %d is sm_%d%d; this library is built for sm_103a (GB300) only", device, major, minor);
+    tsg_ctx *c = new tsg_ctx();
+    c->device = device;
+    tsg_opts_default(&c->opts);
+    if (opts) c->opts = *opts;
+    if (c->opts.threads_numeric != 128 && c->opts.threads_numeric != 256 && c->opts.threads_numeric != 512)
+        c->opts.threads_numeric = 256;
+    auto cleanup = [&](tsg_status st) { tsg_destroy(c); return st; };
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess)
+        return cleanup(fail(TSG_ERR_CUDA, "cudaStreamCreate failed"));
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.handleTypes = cudaMemHandleTypeNone;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = device;
+    if (cudaMemPoolCreate(&c->pool, &props) != cudaSuccess)
+        return cleanup(fail(TSG_ERR_CUDA, "cudaMemPoolCreate failed"));
+    unsigned long long thr = ~0ull;
+    cudaMemPoolSetAttribute(c->pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    if (cudaMalloc(&c->dflags, sizeof(int) * FLAG_COUNT) != cudaSuccess ||
+        cudaMalloc(&c->dstat, sizeof(long long) * ST_SLOTS) != cudaSuccess ||
+        cudaMallocHost(&c->hstat, sizeof(long long) * ST_SLOTS) != cudaSuccess)
+        return cleanup(fail(TSG_ERR_OOM, "context buffers"));
+    for (auto &e : c->ev)
+        if (cudaEventCreate(&e) != cudaSuccess) return cleanup(fail(TSG_ERR_CUDA, "cudaEventCreate failed"));
+    cudaError_t e = tiles_init_attributes();
+    if (e == cudaSuccess) e = symbolic_init_attributes();
+    if (e == cudaSuccess) e = numeric_init_attributes();
+    if (e != cudaSuccess) return cleanup(fail(TSG_ERR_CUDA, "kernel attributes: %s", cudaGetErrorString(e)));
+    *out = c;
+    return TSG_OK;
+}
+
+tsg_status tsg_destroy(tsg_ctx *c)
+{
+    if (!c) return TSG_OK;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    for (auto &kv : c->pinned_cache) cudaFreeHost(kv.second);
+    c->pinned_cache.clear();
+    for (auto &e : c->ev) if (e) cudaEventDestroy(e);
+    if (c->dflags) cudaFree(c->dflags);
+    if (c->dstat) cudaFree(c->dstat);
+    if (c->hstat) cudaFreeHost(c->hstat);
+    if (c->pool) cudaMemPoolDestroy(c->pool);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return TSG_OK;
+}
+
+tsg_status tsg_csr_free(tsg_ctx *ctx, tsg_csr *M)
+{
+    if (!M) return TSG_OK;
+    OutOwner *o = static_cast<OutOwner *>(M->owner);
+    if (!o) {
+        // a loaded host matrix (plain malloc)
+        free(M->row_ptr); free(M->col); free(M->val);
+    } else {
+        tsg_ctx *c = o->ctx ? o->ctx : ctx;
+        if (o->where == TSG_MEM_DEVICE) {
+            if (c) {
+                cudaSetDevice(c->device);
+                for (auto &b : o->blocks) cudaFreeAsync(b.first, c->stream);
+                cudaStreamSynchronize(c->stream);
+            }
+        } else {
+            for (auto &b : o->blocks) {
+                if (c) pinned_put(c, b.first, b.second);
+                else cudaFreeHost(b.first);
+            }
+        }
+        delete o;
+    }
+    M->row_ptr = nullptr; M->col = nullptr; M->val = nullptr; M->owner = nullptr;
+    M->nnz = 0;
+    return TSG_OK;
+}
+
+tsg_status tsg_spgemm(tsg_ctx *ctx, tsg_op op, const tsg_csr *A, const tsg_csr *B, tsg_csr *C, tsg_stats *st)
+{
+    if (!ctx) return fail(TSG_ERR_INVALID_ARG, "ctx is NULL");
+    if (!C) return fail(TSG_ERR_INVALID_ARG, "C is NULL");
+    if (C->where != TSG_MEM_HOST && C->where != TSG_MEM_DEVICE) return fail(TSG_ERR_INVALID_ARG, "C->where is not a tsg_mem");
+    auto t0 = std::chrono::steady_clock::now();
+    CUDA_OK(cudaSetDevice(ctx->device));
+    if (st) memset(st, 0, sizeof(*st));
+    Pool pool{ctx->pool, ctx->stream};
+    long long *rowptr = nullptr;
+    int *col = nullptr;
+    double *val = nullptr;
+    long long nnzC = 0;
+    int m = 0, n = 0;
+    tsg_status r;
+    {
+        Scratch sc(pool);
+        r = run_pipeline(ctx, pool, sc, op, A, B, &rowptr, &col, &val, &nnzC, &m, &n, st, nullptr);
+    }
+    auto release = [&]() { pool.free(rowptr); pool.free(col); pool.free(val); };
+    if (r) { release(); cudaStreamSynchronize(ctx->stream); cudaGetLastError(); return r; }
+
+    int bits = ctx->opts.out_rowptr_bits;
+    if (bits == 0) bits = nnzC < (1ll << 31) ? 32 : 64;
+    if (bits == 32 && nnzC >= (1ll << 31)) {
+        release();
+        cudaStreamSynchronize(ctx->stream);
+        return fail(TSG_ERR_INT32_OVERFLOW, "C has %lld entries; int32 row pointers cannot hold them", nnzC);
+    }
+    OutOwner *o = new OutOwner();
+    o->ctx = ctx;
+    o->where = C->where;
+    C->m = m; C->n = n; C->nnz = nnzC; C->rowptr_bits = bits;
+    cudaError_t e = cudaSuccess;
+    if (C->where == TSG_MEM_DEVICE) {
+        void *rp_out = rowptr;
+        if (bits == 32) {
+            int *rp32 = pool.alloc_n<int>(m + 1);
+            if (!rp32) e = cudaErrorMemoryAllocation;
+            else { e = aux_rowptr_narrow(pool, rowptr, rp32, m + 1); pool.free(rowptr); rowptr = nullptr; rp_out = rp32; }
+        }
+        o->blocks.push_back({rp_out, 0});
+        o->blocks.push_back({col, 0});
+        o->blocks.push_back({val, 0});
+        C->row_ptr = rp_out; C->col = col; C->val = val;
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    } else {
+        auto t_d2h = std::chrono::steady_clock::now();
+        const size_t rpb = (size_t)(m + 1) * (bits == 64 ? 8 : 4);
+        const size_t cb = sizeof(int) * (size_t)nnzC, vb = sizeof(double) * (size_t)nnzC;
+        void *hrp = pinned_get(ctx, rpb), *hcol = pinned_get(ctx, cb), *hval = pinned_get(ctx, vb);
+        if (!hrp || !hcol || !hval) e = cudaErrorMemoryAllocation;
+        void *src_rp = rowptr;
+        int *rp32 = nullptr;
+        if (e == cudaSuccess && bits == 32) {
+            rp32 = pool.alloc_n<int>(m + 1);
+            if (!rp32) e = cudaErrorMemoryAllocation;
+            else { e = aux_rowptr_narrow(pool, rowptr, rp32, m + 1); src_rp = rp32; }
+        }
+        if (e == cudaSuccess) e = cudaMemcpyAsync(hrp, src_rp, rpb, cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess && nnzC > 0) e = cudaMemcpyAsync(hcol, col, cb, cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess && nnzC > 0) e = cudaMemcpyAsync(hval, val, vb, cudaMemcpyDeviceToHost, ctx->stream);
+        pool.free(rp32);
+        release();
+        rowptr = nullptr; col = nullptr; val = nullptr;
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (hrp) o->blocks.push_back({hrp, rpb});
+        if (hcol) o->blocks.push_back({hcol, cb});
+        if (hval) o->blocks.push_back({hval, vb});
+        C->row_ptr = hrp; C->col = (int *)hcol; C->val = (double *)hval;
+        if (st) st->ms_d2h = ms_since(t_d2h);
+    }
+    C->owner = o;
+    if (e != cudaSuccess) {
+        tsg_csr_free(ctx, C);
+        cudaGetLastError();
+        return fail(e == cudaErrorMemoryAllocation ? TSG_ERR_OOM : TSG_ERR_CUDA, "output: %s", cudaGetErrorString(e));
+    }
+    // the final wait also surfaces errors of the numeric kernels
+    e = cudaGetLastError();
+    if (e != cudaSuccess) { tsg_csr_free(ctx, C); return fail(TSG_ERR_CUDA, "kernel: %s", cudaGetErrorString(e)); }
+    if (st) {
+        st->ms_total = ms_since(t0);
+        if (ctx->opts.phase_times) {
+            float a = 0, b = 0, c1 = 0, d = 0;
+            cudaEventElapsedTime(&a, ctx->ev[0], ctx->ev[1]);
+            cudaEventElapsedTime(&b, ctx->ev[1], ctx->ev[2]);
+            cudaEventElapsedTime(&c1, ctx->ev[2], ctx->ev[3]);
+            cudaEventElapsedTime(&d, ctx->ev[3], ctx->ev[4]);
+            st->ms_convert = a; st->ms_step1 = b; st->ms_step2 = c1; st->ms_step3 = d;
+        }
+        st->n_syncs += 1;
+    }
+    return TSG_OK;
+}
+
+tsg_status tsg_csr_download(tsg_ctx *ctx, const tsg_csr *M, int64_t *row_ptr, int32_t *col, double *val)
+{
+    if (!M) return fail(TSG_ERR_INVALID_ARG, "M is NULL");
+    const int kind = M->where == TSG_MEM_DEVICE ? 1 : 0;
+    if (kind && !ctx) return fail(TSG_ERR_INVALID_ARG, "device matrix needs a context");
+    if (ctx) CUDA_OK(cudaSetDevice(ctx->device));
+    const size_t rpb = (size_t)(M->m + 1) * (M->rowptr_bits == 64 ? 8 : 4);
+    std::vector<char> tmp;
+    const void *rp_src = M->row_ptr;
+    if (row_ptr) {
+        if (M->rowptr_bits == 64) {
+            if (kind) CUDA_OK(cudaMemcpy(row_ptr, rp_src, rpb, cudaMemcpyDeviceToHost));
+            else memcpy(row_ptr, rp_src, rpb);
+        } else {
+            tmp.resize(rpb);
+            if (kind) CUDA_OK(cudaMemcpy(tmp.data(), rp_src, rpb, cudaMemcpyDeviceToHost));
+            else memcpy(tmp.data(), rp_src, rpb);
+            const int *p32 = reinterpret_cast<const int *>(tmp.data());
+            for (int i = 0; i <= M->m; ++i) row_ptr[i] = p32[i];
+        }
+    }
+    if (M->nnz > 0) {
+        if (col) {
+            if (kind) CUDA_OK(cudaMemcpy(col, M->col, sizeof(int) * (size_t)M->nnz, cudaMemcpyDeviceToHost));
+            else memcpy(col, M->col, sizeof(int) * (size_t)M->nnz);
+        }
+        if (val) {
+            if (kind) CUDA_OK(cudaMemcpy(val, M->val, sizeof(double) * (size_t)M->nnz, cudaMemcpyDeviceToHost));
+            else memcpy(val, M->val, sizeof(double) * (size_t)M->nnz);
+        }
+    }
+    return TSG_OK;
+}
+
+
+}  // extern "C"
+
+// ---- tile form --------------------------------------------------------------
+
+namespace {
+struct TilesOwner {
+    tsg_ctx *ctx = nullptr;
+    std::vector<void *> blocks;
+};
+
+void reset_dev_state(tsg_ctx *ctx)
+{
+    cudaMemsetAsync(ctx->dflags, 0, sizeof(int) * FLAG_COUNT, ctx->stream);
+    cudaMemsetAsync(ctx->dstat, 0, sizeof(long long) * ST_SLOTS, ctx->stream);
+}
+
+__global__ void k_widen_i32(const int *in, long long *out, long long n)
+{
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i < n) out[i] = in[i];
+}
+}  // namespace
+
+extern "C" {
+
+tsg_status tsg_tiles_free(tsg_ctx *ctx, tsg_tiles *T)
+{
+    if (!T) return TSG_OK;
+    TilesOwner *o = static_cast<TilesOwner *>(T->owner);
+    if (o) {
+        tsg_ctx *c = o->ctx ? o->ctx : ctx;
+        if (c) {
+            cudaSetDevice(c->device);
+            for (void *b : o->blocks) cudaFreeAsync(b, c->stream);
+            cudaStreamSynchronize(c->stream);
+        }
+        delete o;
+    }
+    memset(T, 0, sizeof(*T));
+    return TSG_OK;
+}
+
+tsg_status tsg_csr_to_tiles(tsg_ctx *ctx, const tsg_csr *A, tsg_tiles *T)
+{
+    if (!ctx || !T) return fail(TSG_ERR_INVALID_ARG, "ctx/T is NULL");
+    tsg_status r = check_csr(A, "A");
+    if (r) return r;
+    CUDA_OK(cudaSetDevice(ctx->device));
+    memset(T, 0, sizeof(*T));
+    Pool pool{ctx->pool, ctx->stream};
+    TilesOwner *o = new TilesOwner();
+    o->ctx = ctx;
+    T->owner = o;
+    {
+        Scratch sc(pool);
+        reset_dev_state(ctx);
+        DevCSR dA;
+        r = stage_operand(ctx, pool, sc, A, ctx->opts.validate != 0, dA);
+        TileCSR TA;
+        if (!r) r = build_tiles(pool, sc, dA, TA, ctx);
+        if (!r) {
+            // dstat was zeroed, so the int32 count lands as a valid int64 (little-endian)
+            cudaMemcpyAsync(ctx->dstat + ST_TILESB, TA.trp + TA.blkm, sizeof(int), cudaMemcpyDeviceToDevice, ctx->stream);
+            r = host_wait(ctx, nullptr);
+        }
+        if (!r) {
+            const long long nb = ctx->hstat[ST_TILESB];
+            T->m = dA.m; T->n = dA.n; T->blkm = TA.blkm; T->blkn = TA.blkn; T->numblk = nb; T->nnz = dA.nnz;
+            auto get = [&](size_t bytes) { void *p = pool.alloc(bytes); if (p) o->blocks.push_back(p); return p; };
+            T->blkrowptr = (int64_t *)get(sizeof(int64_t) * (TA.blkm + 1));
+            T->blkcolidx = (int32_t *)get(sizeof(int32_t) * (size_t)(nb + 1));
+            T->mask = (uint16_t *)get(sizeof(uint16_t) * (size_t)(nb * TILE + 2));
+            T->nnzb = (int64_t *)get(sizeof(int64_t) * (size_t)(nb + 1));
+            T->ptr = (uint8_t *)get((size_t)(nb * TILE + 16));
+            T->col = (uint8_t *)get((size_t)(dA.nnz + 16));
+            T->val = (double *)get(sizeof(double) * (size_t)(dA.nnz + 1));
+            if (o->blocks.size() != 7) r = fail(TSG_ERR_OOM, "device pool allocation failed for tiles");
+            if (!r) {
+                { k_widen_i32<<<(unsigned)((TA.blkm + 1 + 255) / 256), 256, 0, ctx->stream>>>(TA.trp, (long long *)T->blkrowptr, TA.blkm + 1); ::tsg::count_launch(); }
+                cudaMemcpyAsync(T->blkcolidx, TA.tcol, sizeof(int) * (size_t)nb, cudaMemcpyDeviceToDevice, ctx->stream);
+                cudaMemcpyAsync(T->mask, TA.mask, sizeof(uint16_t) * (size_t)nb * TILE, cudaMemcpyDeviceToDevice, ctx->stream);
+                cudaError_t e = tiles_payload_a(pool, dA.m, dA.n, dA.rp, dA.col, dA.val, TA, nb, (long long *)T->nnzb,
+                                                T->ptr, T->col, T->val, ctx->dflags);
+                if (e != cudaSuccess) r = fail(TSG_ERR_CUDA, "tile payload: %s", cudaGetErrorString(e));
+            }
+            if (!r) r = host_wait(ctx, nullptr);
+        }
+    }
+    if (r) { tsg_tiles_free(ctx, T); cudaGetLastError(); }
+    return r;
+}
+
+tsg_status tsg_spgemm_tiles(tsg_ctx *ctx, tsg_op op, const tsg_csr *A, const tsg_csr *B, tsg_tiles *C, tsg_stats *st)
+{
+    if (!ctx || !C) return fail(TSG_ERR_INVALID_ARG, "ctx/C is NULL");
+    CUDA_OK(cudaSetDevice(ctx->device));
+    memset(C, 0, sizeof(*C));
+    if (st) memset(st, 0, sizeof(*st));
+    Pool pool{ctx->pool, ctx->stream};
+    long long *rowptr = nullptr;
+    int *col = nullptr;
+    double *val = nullptr;
+    long long nnzC = 0;
+    int m = 0, n = 0;
+    CTiles ct;
+    tsg_status r;
+    {
+        Scratch sc(pool);
+        r = run_pipeline(ctx, pool, sc, op, A, B, &rowptr, &col, &val, &nnzC, &m, &n, st, &ct);
+    }
+    TilesOwner *o = new TilesOwner();
+    o->ctx = ctx;
+    C->owner = o;
+    if (ct.crp) o->blocks.push_back(ct.crp);
+    if (ct.ccol) o->blocks.push_back(ct.ccol);
+    if (ct.cmask) o->blocks.push_back(ct.cmask);
+    if (!r) {
+        const long long nb = ct.numblk;
+        C->m = m; C->n = n; C->blkm = ct.blkm; C->blkn = ceil_div_i(n, TILE); C->numblk = nb; C->nnz = nnzC;
+        C->blkrowptr = (int64_t *)ct.crp; C->blkcolidx = ct.ccol; C->mask = ct.cmask;
+        auto get = [&](size_t bytes) { void *p = pool.alloc(bytes); if (p) o->blocks.push_back(p); return p; };
+        C->nnzb = (int64_t *)get(sizeof(int64_t) * (size_t)(nb + 1));
+        C->ptr = (uint8_t *)get((size_t)(nb * TILE + 16));
+        C->col = (uint8_t *)get((size_t)(nnzC + 16));
+        C->val = (double *)get(sizeof(double) * (size_t)(nnzC + 1));
+        if (!C->nnzb || !C->ptr || !C->col || !C->val) r = fail(TSG_ERR_OOM, "device pool allocation failed for C tiles");
+        if (!r) {
+            cudaError_t e = tiles_from_csr_c(pool, m, ct.blkm, nb, ct.crp, ct.ccol, ct.cmask, rowptr, col, val,
+                                             (long long *)C->nnzb, C->ptr, C->col, C->val, ctx->dflags);
+            if (e != cudaSuccess) r = fail(TSG_ERR_CUDA, "tile payload of C: %s", cudaGetErrorString(e));
+        }
+        if (!r) r = host_wait(ctx, nullptr);
+    }
+    pool.free(rowptr); pool.free(col); pool.free(val);
+    if (r) { tsg_tiles_free(ctx, C); cudaGetLastError(); }
+    else cudaStreamSynchronize(ctx->stream);
+    return r;
+}
+
+tsg_status tsg_tiles_to_csr(tsg_ctx *ctx, const tsg_tiles *T, tsg_csr *C)
+{
+    if (!ctx || !T || !C) return fail(TSG_ERR_INVALID_ARG, "ctx/T/C is NULL");
+    CUDA_OK(cudaSetDevice(ctx->device));
+    Pool pool{ctx->pool, ctx->stream};
+    reset_dev_state(ctx);
+    long long *rowptr = pool.alloc_n<long long>(T->m + 1);
+    if (!rowptr) return fail(TSG_ERR_OOM, "device pool allocation failed");
+    CUDA_OK(csr_from_tiles(pool, T->m, (const long long *)T->blkrowptr, T->blkcolidx, (const long long *)T->nnzb,
+                           T->ptr, T->col, T->val, rowptr, nullptr, nullptr, ctx->dflags, false));
+    CUDA_OK(cudaMemcpyAsync(ctx->dstat + ST_NNZC, rowptr + T->m, sizeof(long long), cudaMemcpyDeviceToDevice, ctx->stream));
+    tsg_status r = host_wait(ctx, nullptr);
+    if (r) { pool.free(rowptr); return r; }
+    const long long nnz = ctx->hstat[ST_NNZC];
+    int *col = pool.alloc_n<int>(nnz);
+    double *val = pool.alloc_n<double>(nnz);
+    if (!col || !val) { pool.free(rowptr); pool.free(col); pool.free(val); return fail(TSG_ERR_OOM, "device pool allocation failed"); }
+    CUDA_OK(csr_from_tiles(pool, T->m, (const long long *)T->blkrowptr, T->blkcolidx, (const long long *)T->nnzb,
+                           T->ptr, T->col, T->val, rowptr, col, val, ctx->dflags, true));
+    CUDA_OK(cudaStreamSynchronize(ctx->stream));
+    OutOwner *o = new OutOwner();
+    o->ctx = ctx;
+    o->where = TSG_MEM_DEVICE;
+    o->blocks = {{rowptr, 0}, {col, 0}, {val, 0}};
+    C->m = T->m; C->n = T->n; C->nnz = nnz; C->rowptr_bits = 64; C->where = TSG_MEM_DEVICE;
+    C->row_ptr = rowptr; C->col = col; C->val = val; C->owner = o;
+    return TSG_OK;
+}
+
+tsg_status tsg_tiles_download(tsg_ctx *ctx, const tsg_tiles *T, int64_t *blkrowptr, int32_t *blkcolidx,
+                              int64_t *nnzb, uint8_t *ptr, uint8_t *col, double *val, uint16_t *mask)
+{
+    if (!ctx || !T) return fail(TSG_ERR_INVALID_ARG, "ctx/T is NULL");
+    CUDA_OK(cudaSetDevice(ctx->device));
+    CUDA_OK(cudaStreamSynchronize(ctx->stream));
+    const size_t nb = (size_t)T->numblk;
+    if (blkrowptr) CUDA_OK(cudaMemcpy(blkrowptr, T->blkrowptr, sizeof(int64_t) * (size_t)(T->blkm + 1), cudaMemcpyDeviceToHost));
+    if (nb && blkcolidx) CUDA_OK(cudaMemcpy(blkcolidx, T->blkcolidx, sizeof(int32_t) * nb, cudaMemcpyDeviceToHost));
+    if (nnzb) CUDA_OK(cudaMemcpy(nnzb, T->nnzb, sizeof(int64_t) * (nb + 1), cudaMemcpyDeviceToHost));
+    if (nb && ptr) CUDA_OK(cudaMemcpy(ptr, T->ptr, nb * TILE, cudaMemcpyDeviceToHost));
+    if (nb && mask) CUDA_OK(cudaMemcpy(mask, T->mask, sizeof(uint16_t) * nb * TILE, cudaMemcpyDeviceToHost));
+    if (T->nnz && col) CUDA_OK(cudaMemcpy(col, T->col, (size_t)T->nnz, cudaMemcpyDeviceToHost));
+    if (T->nnz && val) CUDA_OK(cudaMemcpy(val, T->val, sizeof(double) * (size_t)T->nnz, cudaMemcpyDeviceToHost));
+    return TSG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,360 @@
+// tsg_aux.cu -- small reductions used by the pipeline, and the conversions
+// between CSR and the reference's tile format:
+//   tiles_payload_a   CSR -> tile payload (nnz offsets, uint8 row starts,
+//                     local columns, values) in the layout of the reference's
+//                     host conversion main_spgemm-col.cu:5055-5240
+//   tiles_from_csr_c  C's CSR + tile masks -> C's tile payload, the layout
+//                     stepall_cuda_new leaves on the device (:4586-4735)
+//   csr_from_tiles    any tile matrix -> CSR (the tile -> CSR output)
+// Roofline: all HBM-bound copies/gathers (read once, write once).
+#include "tsg_internal.cuh"
+
+namespace tsg {
+
+namespace {
+
+__device__ __forceinline__ int lower_bound_aux(const int *a, int n, int key) {
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (a[mid] < key) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+
+__global__ void k_nnzcub(const long long *__restrict__ rpA, const int *__restrict__ colA, int m,
+                         const long long *__restrict__ rpB, int kB, unsigned long long *out)
+{
+    __shared__ unsigned long long s[8];
+    unsigned long long acc = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x)
+        for (long long p = rpA[i]; p < rpA[i + 1]; ++p) {
+            int k = colA[p];
+            if ((unsigned)k < (unsigned)kB) acc += (unsigned long long)(rpB[k + 1] - rpB[k]);
+        }
+    acc = (unsigned long long)warp_sum_ll((long long)acc);
+    if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long t = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += s[w];
+        atomicAdd(out, t);
+    }
+}
+
+__global__ void k_mask_popc(const int *__restrict__ trp, int blkm, const uint16_t *__restrict__ mask,
+                            unsigned long long *out)
+{
+    const long long nt = trp[blkm];
+    const unsigned *mw = reinterpret_cast<const unsigned *>(mask);
+    unsigned long long acc = 0;
+    for (long long w = blockIdx.x * (long long)blockDim.x + threadIdx.x; w < nt * 8; w += (long long)gridDim.x * blockDim.x)
+        acc += __popc(mw[w]);
+    acc = (unsigned long long)warp_sum_ll((long long)acc);
+    if ((threadIdx.x & 31) == 0 && acc) atomicAdd(out, acc);
+}
+
+__global__ void k_copy_scalars(const long long *a, long long *da, const int *b, long long *db, const int *c, long long *dc)
+{
+    if (threadIdx.x == 0) { *da = *a; *db = *b; *dc = *c; }
+}
+
+__global__ void k_rowptr_narrow(const long long *in, int *out, long long n)
+{
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i < n) out[i] = (int)in[i];
+}
+
+// ---- C tiles from C's CSR ------------------------------------------------
+
+__global__ void k_tile_nnz_from_mask(const uint16_t *__restrict__ mask, long long numblk, int *tn)
+{
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < numblk; t += (long long)gridDim.x * blockDim.x) {
+        const uint4 *q = reinterpret_cast<const uint4 *>(mask + t * TILE);
+        uint4 a = q[0], b = q[1];
+        tn[t] = __popc(a.x) + __popc(a.y) + __popc(a.z) + __popc(a.w) + __popc(b.x) + __popc(b.y) + __popc(b.z) + __popc(b.w);
+    }
+}
+
+// one CTA per C tile-row; warp per row, lanes over the tile-row's tiles
+__global__ void __launch_bounds__(256)
+k_tile_payload_c(int m, const long long *__restrict__ crp, const int *__restrict__ ccol,
+                 const uint16_t *__restrict__ cmask, const long long *__restrict__ rowptr,
+                 const int *__restrict__ col, const double *__restrict__ val, const long long *__restrict__ nnzb,
+                 uint8_t *ptr, uint8_t *lcol, double *tval)
+{
+    const int i = blockIdx.x, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int r0 = i * TILE, rows = min(TILE, m - r0);
+    const long long c0 = crp[i];
+    const int S = (int)(crp[i + 1] - c0);
+    // row starts inside each tile
+    for (int s = threadIdx.x; s < S; s += blockDim.x) {
+        int run = 0;
+        for (int r = 0; r < TILE; ++r) {
+            ptr[(c0 + s) * TILE + r] = (uint8_t)run;
+            run += __popc((unsigned)cmask[(c0 + s) * TILE + r]);
+        }
+    }
+    for (int r = warp; r < rows; r += 8) {
+        const long long Rb = rowptr[r0 + r];
+        int run = 0;
+        for (int sb = 0; sb < S; sb += 32) {
+            const int s = sb + lane;
+            unsigned mk = (s < S) ? (unsigned)cmask[(c0 + s) * TILE + r] : 0u;
+            int c = __popc(mk);
+            int incl = warp_incl_scan(c, lane);
+            if (s < S && c) {
+                int before = 0;
+                for (int q = 0; q < r; ++q) before += __popc((unsigned)cmask[(c0 + s) * TILE + q]);
+                const long long src = Rb + run + incl - c;
+                const long long dst = nnzb[c0 + s] + before;
+                for (int x = 0; x < c; ++x) {
+                    lcol[dst + x] = (uint8_t)(col[src + x] & 15);
+                    tval[dst + x] = val[src + x];
+                }
+            }
+            run += __shfl_sync(0xffffffffu, incl, 31);
+        }
+    }
+}
+
+// ---- A's tile payload ------------------------------------------------------
+
+// per (tile, local row) entry counts; warp per CSR row
+__global__ void k_a_counts(int m, const long long *__restrict__ rp, const int *__restrict__ col, int n,
+                           const int *__restrict__ trp, const int *__restrict__ tcol, int *cnt16)
+{
+    const int R = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (R >= m) return;
+    const int i = R / TILE, r = R - i * TILE;
+    const int t0 = trp[i], S = trp[i + 1] - t0;
+    for (long long p = rp[R] + lane; p < rp[R + 1]; p += 32) {
+        int c = col[p];
+        if ((unsigned)c >= (unsigned)n) continue;
+        int s = lower_bound_aux(tcol + t0, S, c >> 4);
+        atomicAdd(&cnt16[(long long)(t0 + s) * TILE + r], 1);
+    }
+}
+
+__global__ void k_a_ptr(long long numblk, int blkm, const int *__restrict__ trp, const int *__restrict__ cnt16,
+                        int *tn, uint8_t *ptr, int m, int *flags)
+{
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < numblk; t += (long long)gridDim.x * blockDim.x) {
+        int run = 0;
+        for (int r = 0; r < TILE; ++r) {
+            if (run > 255) set_flag(flags, FLAG_OVERFLOW);
+            ptr[t * TILE + r] = (uint8_t)run;
+            run += cnt16[t * TILE + r];
+        }
+        tn[t] = run;
+    }
+    (void)blkm; (void)trp; (void)m;
+}
+
+// scatter in CSR order; a warp owns a row, so per-(tile,row) cursors advance
+// deterministically
+__global__ void k_a_scatter(int m, const long long *__restrict__ rp, const int *__restrict__ col,
+                            const double *__restrict__ val, int n, const int *__restrict__ trp,
+                            const int *__restrict__ tcol, const long long *__restrict__ nnzb,
+                            const uint8_t *__restrict__ ptr, int *cur16, uint8_t *lcol, double *tval)
+{
+    const int R = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (R >= m) return;
+    const int i = R / TILE, r = R - i * TILE;
+    const int t0 = trp[i], S = trp[i + 1] - t0;
+    for (long long pb = rp[R]; pb < rp[R + 1]; pb += 32) {
+        const long long p = pb + lane;
+        const bool ok = p < rp[R + 1];
+        int c = ok ? col[p] : -1;
+        const bool valid = ok && (unsigned)c < (unsigned)n;
+        int t = valid ? t0 + lower_bound_aux(tcol + t0, S, c >> 4) : -1 - lane;
+        unsigned peers = __match_any_sync(0xffffffffu, t);
+        int rank = __popc(peers & lanemask_lt());
+        int before = valid ? cur16[(long long)t * TILE + r] : 0;
+        __syncwarp();
+        if (valid) {
+            long long dst = nnzb[t] + ptr[(long long)t * TILE + r] + before + rank;
+            lcol[dst] = (uint8_t)(c & 15);
+            tval[dst] = val[p];
+            if (lane == __ffs(peers) - 1) cur16[(long long)t * TILE + r] = before + __popc(peers);
+        }
+        __syncwarp();
+    }
+}
+
+// ---- tiles -> CSR ----------------------------------------------------------
+
+__device__ __forceinline__ int tile_row_len(const uint8_t *ptr, const long long *nnzb, long long t, int r) {
+    int s = ptr[t * TILE + r];
+    int e = (r == TILE - 1) ? (int)(nnzb[t + 1] - nnzb[t]) : ptr[t * TILE + r + 1];
+    return e > s ? e - s : 0;
+}
+
+__global__ void k_csr_rowcnt_from_tiles(int m, const long long *__restrict__ brp, const long long *__restrict__ nnzb,
+                                        const uint8_t *__restrict__ ptr, int *rowcnt)
+{
+    const int R = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (R >= m) return;
+    const int i = R / TILE, r = R - i * TILE;
+    int c = 0;
+    for (long long t = brp[i] + lane; t < brp[i + 1]; t += 32) c += tile_row_len(ptr, nnzb, t, r);
+    c = warp_sum_int(c);
+    if (lane == 0) rowcnt[R] = c;
+}
+
+__global__ void k_csr_fill_from_tiles(int m, const long long *__restrict__ brp, const int *__restrict__ bcol,
+                                      const long long *__restrict__ nnzb, const uint8_t *__restrict__ ptr,
+                                      const uint8_t *__restrict__ lcol, const double *__restrict__ tval,
+                                      const long long *__restrict__ rowptr, int *col, double *val)
+{
+    const int R = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (R >= m) return;
+    const int i = R / TILE, r = R - i * TILE;
+    long long run = rowptr[R];
+    for (long long tb = brp[i]; tb < brp[i + 1]; tb += 32) {
+        const long long t = tb + lane;
+        int len = (t < brp[i + 1]) ? tile_row_len(ptr, nnzb, t, r) : 0;
+        int incl = warp_incl_scan(len, lane);
+        if (len) {
+            const long long src = nnzb[t] + ptr[t * TILE + r];
+            const long long dst = run + incl - len;
+            const int jb = bcol[t] * TILE;
+            for (int x = 0; x < len; ++x) {
+                col[dst + x] = jb + lcol[src + x];
+                val[dst + x] = tval[src + x];
+            }
+        }
+        run += __shfl_sync(0xffffffffu, incl, 31);
+    }
+}
+
+// FP64 FMA throughput probe: 8 independent FMA chains per thread (the
+// operands keep the values finite); nothing but DFMA in the loop.
+__global__ void __launch_bounds__(256) k_fp64_peak(double *out, int iters, double a, double b)
+{
+    double x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+    for (int i = 0; i < iters; ++i) {
+        x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+        x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+    }
+    out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+
+inline unsigned g256(long long n) {
+    long long g = (n + 255) / 256;
+    if (g < 1) g = 1;
+    if (g > 152ll * 64) g = 152ll * 64;
+    return (unsigned)g;
+}
+
+}  // namespace
+
+cudaError_t fp64_peak(cudaStream_t s, cudaEvent_t e0, cudaEvent_t e1, double *gflops)
+{
+    int dev = 0, sms = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    const int blocks = sms * 8, threads = 256, iters = 2000;
+    double *out = nullptr;
+    e = cudaMallocAsync(&out, sizeof(double) * blocks * threads, s);
+    if (e != cudaSuccess) return e;
+    double best = 0.0;
+    for (int rep = 0; rep < 4 && e == cudaSuccess; ++rep) {
+        cudaEventRecord(e0, s);
+        { k_fp64_peak<<<blocks, threads, 0, s>>>(out, iters, 1.0000001, 1e-9); ::tsg::count_launch(); }
+        cudaEventRecord(e1, s);
+        e = cudaEventSynchronize(e1);
+        float ms = 0.f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+        const double flop = 2.0 * 8.0 * iters * (double)blocks * threads;
+        if (rep > 0 && ms > 0.f) best = best > flop / (ms * 1e6) ? best : flop / (ms * 1e6);
+    }
+    cudaFreeAsync(out, s);
+    cudaStreamSynchronize(s);
+    *gflops = best;
+    return e;
+}
+
+cudaError_t aux_nnzcub(Pool &pool, const long long *rpA, const int *colA, int m, const long long *rpB, int kB,
+                       unsigned long long *out)
+{
+    if (m <= 0) return cudaSuccess;
+    { k_nnzcub<<<g256(m), 256, 0, pool.stream>>>(rpA, colA, m, rpB, kB, out); ::tsg::count_launch(); }
+    return cudaGetLastError();
+}
+
+cudaError_t aux_mask_popc(Pool &pool, const int *trp, int blkm, const uint16_t *mask, unsigned long long *out)
+{
+    { k_mask_popc<<<152 * 4, 256, 0, pool.stream>>>(trp, blkm, mask, out); ::tsg::count_launch(); }
+    return cudaGetLastError();
+}
+
+cudaError_t aux_copy_scalars(Pool &pool, const long long *a, long long *da, const int *b, long long *db,
+                             const int *c, long long *dc)
+{
+    { k_copy_scalars<<<1, 32, 0, pool.stream>>>(a, da, b, db, c, dc); ::tsg::count_launch(); }
+    return cudaGetLastError();
+}
+
+cudaError_t aux_rowptr_narrow(Pool &pool, const long long *in, int *out, long long n)
+{
+    if (n <= 0) return cudaSuccess;
+    { k_rowptr_narrow<<<(unsigned)((n + 255) / 256), 256, 0, pool.stream>>>(in, out, n); ::tsg::count_launch(); }
+    return cudaGetLastError();
+}
+
+cudaError_t tiles_from_csr_c(Pool &pool, int m, int blkm, long long numblk, const long long *crp, const int *ccol,
+                             const uint16_t *cmask, const long long *rowptr, const int *col, const double *val,
+                             long long *nnzb, uint8_t *ptr, uint8_t *lcol, double *tval, int *flags)
+{
+    int *tn = pool.alloc_n<int>(numblk + 1);
+    if (!tn) return pool.err;
+    if (numblk > 0) { k_tile_nnz_from_mask<<<g256(numblk), 256, 0, pool.stream>>>(cmask, numblk, tn); ::tsg::count_launch(); }
+    cudaError_t e = scan_i32_to_i64(pool, tn, nnzb, numblk, flags);
+    if (e == cudaSuccess && blkm > 0)
+        { k_tile_payload_c<<<blkm, 256, 0, pool.stream>>>(m, crp, ccol, cmask, rowptr, col, val, nnzb, ptr, lcol, tval); ::tsg::count_launch(); }
+    if (e == cudaSuccess) e = cudaGetLastError();
+    pool.free(tn);
+    return e;
+}
+
+cudaError_t tiles_payload_a(Pool &pool, int m, int n, const long long *rp, const int *col, const double *val,
+                            const TileCSR &T, long long numblk, long long *nnzb, uint8_t *ptr, uint8_t *lcol,
+                            double *tval, int *flags)
+{
+    int *cnt16 = pool.alloc_n<int>(numblk * TILE + 1);
+    int *cur16 = pool.alloc_n<int>(numblk * TILE + 1);
+    int *tn = pool.alloc_n<int>(numblk + 1);
+    cudaError_t e = (cnt16 && cur16 && tn) ? cudaSuccess : pool.err;
+    if (e == cudaSuccess) e = cudaMemsetAsync(cnt16, 0, sizeof(int) * (size_t)(numblk * TILE + 1), pool.stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(cur16, 0, sizeof(int) * (size_t)(numblk * TILE + 1), pool.stream);
+    const unsigned gr = (unsigned)((m + 7) / 8);
+    if (e == cudaSuccess && m > 0) { k_a_counts<<<gr, 256, 0, pool.stream>>>(m, rp, col, n, T.trp, T.tcol, cnt16); ::tsg::count_launch(); }
+    if (e == cudaSuccess && numblk > 0) { k_a_ptr<<<g256(numblk), 256, 0, pool.stream>>>(numblk, T.blkm, T.trp, cnt16, tn, ptr, m, flags); ::tsg::count_launch(); }
+    if (e == cudaSuccess) e = scan_i32_to_i64(pool, tn, nnzb, numblk, flags);
+    if (e == cudaSuccess && m > 0)
+        { k_a_scatter<<<gr, 256, 0, pool.stream>>>(m, rp, col, val, n, T.trp, T.tcol, nnzb, ptr, cur16, lcol, tval); ::tsg::count_launch(); }
+    if (e == cudaSuccess) e = cudaGetLastError();
+    pool.free(cnt16); pool.free(cur16); pool.free(tn);
+    return e;
+}
+
+cudaError_t csr_from_tiles(Pool &pool, int m, const long long *brp, const int *bcol, const long long *nnzb,
+                           const uint8_t *ptr, const uint8_t *lcol, const double *tval, long long *rowptr, int *col,
+                           double *val, int *flags, bool fill)
+{
+    const unsigned gr = (unsigned)((m + 7) / 8);
+    if (!fill) {
+        int *rowcnt = pool.alloc_n<int>(m + 1);
+        if (!rowcnt) return pool.err;
+        if (m > 0) { k_csr_rowcnt_from_tiles<<<gr, 256, 0, pool.stream>>>(m, brp, nnzb, ptr, rowcnt); ::tsg::count_launch(); }
+        cudaError_t e = scan_i32_to_i64(pool, rowcnt, rowptr, m, flags);
+        pool.free(rowcnt);
+        return e;
+    }
+    if (m > 0) { k_csr_fill_from_tiles<<<gr, 256, 0, pool.stream>>>(m, brp, bcol, nnzb, ptr, lcol, tval, rowptr, col, val); ::tsg::count_launch(); }
+    return cudaGetLastError();
+}
+
+}  // namespace tsg

@@ -1,0 +1,127 @@
+// tsg_internal.cuh -- shared definitions of the GB300 tiled SpGEMM kernels.
+//
+// Layout in HBM (all device arrays come from the context's stream-ordered pool):
+//   CSR operand   rp (int64, m+1, clamped copy of the caller's int32/int64
+//                 pointer), col (int32, nnz), val (f64, nnz)
+//   tile-CSR      trp (int32, blkm+1), tcol (int32, numblk, sorted per
+//                 tile-row), mask (uint16, 16 per tile, bit 15-c for local
+//                 column c -- main_spgemm-col.cu:5215)
+//   C tiles       crp (int64, blkm+1), ccol (int32), cmask (uint16, 16 per tile)
+//   C CSR         rowptr (int64, m+1), col (int32), val (f64)
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace tsg {
+
+constexpr int TILE = 16;
+
+// Device error flags (one int32 array per context, read back at the host
+// waits).  Kernels never trap: they record and return.
+enum DevFlag : int {
+    FLAG_BAD_INPUT = 0,    // row pointer or column index out of range
+    FLAG_TIMEOUT = 1,      // a bounded wait in the scan gave up
+    FLAG_INTERNAL = 2,     // an internal bound check failed (a library bug)
+    FLAG_OVERFLOW = 3,     // a count did not fit its index type
+    FLAG_COUNT = 8
+};
+
+// Bounded-wait limit for the decoupled-lookback scan (spins with nanosleep;
+// about a quarter second before giving up).
+constexpr int SPIN_LIMIT = 1 << 22;
+
+__device__ __forceinline__ unsigned lanemask_lt() {
+    unsigned r;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(r));
+    return r;
+}
+
+__device__ __forceinline__ int warp_sum_int(int v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ long long warp_sum_ll(long long v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ int warp_min_int(int v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+__device__ __forceinline__ int warp_max_int(int v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// Inclusive warp scan.
+__device__ __forceinline__ int warp_incl_scan(int v, int lane) {
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int t = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += t;
+    }
+    return v;
+}
+
+// OR a 16-bit row mask into the uint16 array viewed as 32-bit words (the
+// arrays hold 16 masks per tile, so the word view is always in bounds).
+__device__ __forceinline__ void atomic_or_mask16(uint16_t *mask, long long idx, unsigned bits) {
+    unsigned *w = reinterpret_cast<unsigned *>(mask) + (idx >> 1);
+    atomicOr(w, bits << ((idx & 1) * 16));
+}
+
+__device__ __forceinline__ void set_flag(int *flags, int which) {
+    atomicOr(flags + which, 1);
+}
+
+}  // namespace tsg
+
+// ---- host-side helpers shared by the .cu files --------------------------------
+namespace tsg {
+
+// Every kernel launch site calls this (process-wide counter behind
+// tsg_launch_count), so benchmarks count launches instead of estimating them.
+void count_launch();
+
+// Stream-ordered allocations from the context's memory pool.  The pool keeps
+// freed memory cached (release threshold = max), so steady-state calls do no
+// cudaMalloc.  alloc() returns nullptr and sets `err` on failure.
+struct Pool {
+    cudaMemPool_t pool = nullptr;
+    cudaStream_t stream = nullptr;
+    cudaError_t err = cudaSuccess;
+    void *alloc(size_t bytes) {
+        if (bytes == 0) bytes = 16;
+        void *p = nullptr;
+        cudaError_t e = cudaMallocFromPoolAsync(&p, bytes, pool, stream);
+        if (e != cudaSuccess) { err = e; cudaGetLastError(); return nullptr; }
+        return p;
+    }
+    template <class T> T *alloc_n(long long n) { return static_cast<T *>(alloc(sizeof(T) * (size_t)(n > 0 ? n : 1))); }
+    void free(void *p) { if (p) cudaFreeAsync(p, stream); }
+};
+
+struct TileCSR {
+    int m = 0, n = 0, blkm = 0, blkn = 0;
+    long long cap = 0;          // allocated tile capacity (an upper bound of numblk)
+    int *trp = nullptr;         // blkm+1 tile-row pointer
+    int *tcol = nullptr;        // cap sorted tile columns
+    uint16_t *mask = nullptr;   // 16*cap row masks
+};
+
+// Exclusive scans (decoupled look-back, one pass): out[i] = sum_{j<i} in[j]
+// and out[n] = total.  The int32-output form flags FLAG_OVERFLOW on overflow.
+cudaError_t scan_i32_to_i64(Pool &pool, const int *in, long long *out, long long n, int *flags);
+cudaError_t scan_i32_to_i32(Pool &pool, const int *in, int *out, long long n, int *flags);
+cudaError_t scan_i64_to_i64(Pool &pool, const long long *in, long long *out, long long n, int *flags);
+
+inline int ceil_div_i(long long a, long long b) { return (int)((a + b - 1) / b); }
+
+}  // namespace tsg

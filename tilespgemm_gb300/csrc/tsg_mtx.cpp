@@ -1,0 +1,183 @@
+// tsg_mtx.cpp -- Matrix Market load path (tsg_load_mtx).
+//
+// Restates the semantics of the reference's loader mmio_allinone
+// (mmio_highlevel.h:593-759, using mm_read_banner mmio.h:400-496 and
+// mm_read_mtx_crd_size mmio.h:561-590):
+//   - banner "%%MatrixMarket matrix coordinate <real|complex|integer|pattern>
+//     <general|symmetric|hermitian|skew-symmetric>" (tokens after the first
+//     are case-insensitive);
+//   - comment lines start with '%'; the size line holds M N NNZ;
+//   - entries are 1-based; pattern -> 1.0, integer -> double, complex -> real
+//     part;
+//   - symmetric and hermitian files are mirrored with the same value (the
+//     diagonal once), skew-symmetric files are not mirrored;
+//   - per row, entries keep file order (a mirrored entry (j,i) lands in row
+//     j at the file position of its source); nothing is sorted or merged.
+// Differences, all of which the reference turns into undefined behaviour:
+// 'array' files, indices outside [1,M]x[1,N], and truncated data lines are
+// rejected with TSG_ERR_BAD_MTX.
+#include "tilespgemm.h"
+
+#include <cctype>
+#include <cerrno>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+namespace tsg {
+void set_last_error(const char *msg);
+}
+
+namespace {
+
+bool read_file(const char *path, std::string &out)
+{
+    FILE *f = fopen(path, "rb");
+    if (!f) return false;
+    std::vector<char> buf(1 << 20);
+    size_t got;
+    while ((got = fread(buf.data(), 1, buf.size(), f)) > 0) out.append(buf.data(), got);
+    fclose(f);
+    return true;
+}
+
+std::string lower(std::string s)
+{
+    for (auto &ch : s) ch = (char)tolower((unsigned char)ch);
+    return s;
+}
+
+struct Cursor {
+    const char *p, *end;
+    void skip_ws() { while (p < end && (*p == ' ' || *p == '\t' || *p == '\r' || *p == '\n')) ++p; }
+    bool read_long(long long &v) {
+        skip_ws();
+        if (p >= end) return false;
+        char *e = nullptr;
+        errno = 0;
+        v = strtoll(p, &e, 10);
+        if (e == p || errno) return false;
+        p = e;
+        return true;
+    }
+    bool read_double(double &v) {
+        skip_ws();
+        if (p >= end) return false;
+        char *e = nullptr;
+        v = strtod(p, &e);
+        if (e == p) return false;
+        p = e;
+        return true;
+    }
+};
+
+tsg_status bad(const char *msg)
+{
+    tsg::set_last_error(msg);
+    return TSG_ERR_BAD_MTX;
+}
+
+}  // namespace
+
+extern "C" tsg_status tsg_load_mtx(const char *path, tsg_csr *out, int32_t *is_symmetric)
+{
+    if (!path || !out) {
+        tsg::set_last_error("path/out is NULL");
+        return TSG_ERR_INVALID_ARG;
+    }
+    memset(out, 0, sizeof(*out));
+    std::string text;
+    if (!read_file(path, text)) return bad("could not open the Matrix Market file");
+    // make sure strtod/strtoll stop at the end of the buffer
+    text.push_back('\n');
+    const char *p = text.data(), *end = text.data() + text.size();
+    // banner line
+    const char *nl = (const char *)memchr(p, '\n', (size_t)(end - p));
+    std::string line(p, nl ? (size_t)(nl - p) : (size_t)(end - p));
+    char tok[5][1025];
+    if (line.size() > 1024 || sscanf(line.c_str(), "%1024s %1024s %1024s %1024s %1024s", tok[0], tok[1], tok[2], tok[3], tok[4]) != 5)
+        return bad("premature end of the banner line");
+    if (strncmp(tok[0], "%%MatrixMarket", 14) != 0) return bad("no %%MatrixMarket banner");
+    const std::string mtx = lower(tok[1]), crd = lower(tok[2]), type = lower(tok[3]), sym = lower(tok[4]);
+    if (mtx != "matrix") return bad("unsupported object (not 'matrix')");
+    if (crd == "array") return bad("'array' (dense) Matrix Market files are not supported");
+    if (crd != "coordinate") return bad("unsupported storage (not 'coordinate')");
+    const bool is_real = type == "real", is_complex = type == "complex", is_int = type == "integer", is_pat = type == "pattern";
+    if (!is_real && !is_complex && !is_int && !is_pat) return bad("unsupported data type");
+    const bool symm = (sym == "symmetric" || sym == "hermitian");
+    if (!symm && sym != "general" && sym != "skew-symmetric") return bad("unsupported symmetry");
+    p = nl ? nl + 1 : end;
+    // skip comment lines, then blank lines, to the size line
+    while (p < end && *p == '%') {
+        const char *e = (const char *)memchr(p, '\n', (size_t)(end - p));
+        p = e ? e + 1 : end;
+    }
+    Cursor cur{p, end};
+    long long M = 0, N = 0, NZ = 0;
+    if (!cur.read_long(M) || !cur.read_long(N) || !cur.read_long(NZ)) return bad("bad size line");
+    if (M < 0 || N < 0 || NZ < 0 || M > INT32_MAX - 1 || N > INT32_MAX - 1 || NZ > INT32_MAX) return bad("sizes out of range");
+    std::vector<int> ri((size_t)NZ), ci((size_t)NZ);
+    std::vector<double> vv((size_t)NZ);
+    for (long long t = 0; t < NZ; ++t) {
+        long long i = 0, j = 0;
+        double v = 1.0, vim = 0.0;
+        if (!cur.read_long(i) || !cur.read_long(j)) return bad("truncated data line");
+        if (is_real) { if (!cur.read_double(v)) return bad("truncated data line"); }
+        else if (is_complex) { if (!cur.read_double(v) || !cur.read_double(vim)) return bad("truncated data line"); }
+        else if (is_int) { long long iv; if (!cur.read_long(iv)) return bad("truncated data line"); v = (double)(int)iv; }
+        if (i < 1 || i > M || j < 1 || j > N) return bad("entry index outside the matrix");
+        ri[(size_t)t] = (int)(i - 1);
+        ci[(size_t)t] = (int)(j - 1);
+        vv[(size_t)t] = v;
+    }
+    // counts, then fill in file order (mirrors right after their source)
+    std::vector<long long> cnt((size_t)M + 1, 0);
+    for (long long t = 0; t < NZ; ++t) {
+        cnt[(size_t)ri[(size_t)t]]++;
+        if (symm && ri[(size_t)t] != ci[(size_t)t]) {
+            if (ci[(size_t)t] >= M) return bad("symmetric entry mirrored outside the matrix");
+            cnt[(size_t)ci[(size_t)t]]++;
+        }
+    }
+    long long total = 0;
+    for (long long r = 0; r < M; ++r) { long long c = cnt[(size_t)r]; cnt[(size_t)r] = total; total += c; }
+    cnt[(size_t)M] = total;
+    if (total > INT32_MAX) {
+        tsg::set_last_error("more than 2^31-1 entries after mirroring");
+        return TSG_ERR_NOT_SUPPORTED;
+    }
+    int *rp = (int *)malloc(sizeof(int) * (size_t)(M + 1));
+    int *col = (int *)malloc(sizeof(int) * (size_t)(total > 0 ? total : 1));
+    double *val = (double *)malloc(sizeof(double) * (size_t)(total > 0 ? total : 1));
+    if (!rp || !col || !val) {
+        free(rp); free(col); free(val);
+        tsg::set_last_error("host allocation failed");
+        return TSG_ERR_OOM;
+    }
+    for (long long r = 0; r <= M; ++r) rp[r] = (int)cnt[(size_t)r];
+    std::vector<long long> pos(cnt.begin(), cnt.end() - 1);
+    for (long long t = 0; t < NZ; ++t) {
+        const int i = ri[(size_t)t], j = ci[(size_t)t];
+        long long d = pos[(size_t)i]++;
+        col[d] = j;
+        val[d] = vv[(size_t)t];
+        if (symm && i != j) {
+            d = pos[(size_t)j]++;
+            col[d] = i;
+            val[d] = vv[(size_t)t];
+        }
+    }
+    out->m = (int32_t)M;
+    out->n = (int32_t)N;
+    out->nnz = total;
+    out->rowptr_bits = 32;
+    out->where = TSG_MEM_HOST;
+    out->row_ptr = rp;
+    out->col = col;
+    out->val = val;
+    out->owner = nullptr;
+    if (is_symmetric) *is_symmetric = symm ? 1 : 0;
+    return TSG_OK;
+}

@@ -1,0 +1,337 @@
+// tsg_numeric.cu -- step 3: FP64 numeric accumulation and the CSR write of C.
+//
+// Reference: stir_spgemm_step4_cuda_kernel_smem_v3 (main_spgemm-col.cu:2094-2397,
+// sparse tiles: warp per C tile, products added into the tile's sorted local
+// column list found by linear search, shared-memory atomicAdd(double)) and
+// stir_spgemm_step4_cuda_kernel_dns_noatomic_halfwarp (:3386-3755, dense
+// tiles: 16x16 FP64 shared accumulator).  The reference writes C in tile form
+// and stops; this step writes CSR directly.
+//
+// GB300 design.  On this part FP64 FMA issue is the ceiling (about 0.6 T
+// FMA/s, and an FMA warp instruction costs the same with idle lanes), so each
+// intermediate product is exactly one DFMA, with no other FP64 instruction in
+// the loop.  One CTA owns a C tile-row (16 rows); step 2 already fixed every
+// output's position: for C tile (i,j) and local row r, the row's entries are
+// the set bits of mask[j][r], and an output column c of that row sits at
+//     offset(j, r) + popc(mask[j][r] >> (16 - c))
+// inside the tile-row's CSR segment (a perfect hash keyed by the masks).  The
+// CTA keeps the tile-row's whole CSR segment of values in shared memory,
+// each warp owns C rows (so no two warps touch one output), and for every
+// A entry (R,k) the warp's lanes take B row k's entries, which have distinct
+// columns, so one DFMA instruction updates distinct outputs (rows with
+// duplicate column indices in B take the DUPSAFE variant, which serialises
+// equal targets in B's entry order).  Per output the products are applied in
+// A's row order, then B's row order: the same order as the CPU reference
+// (thmkl_dcsrmultcsr.c:52-91), so with FMA rounding the two agree bit for bit.
+// The epilogue streams the segment's values out coalesced and expands the
+// masks into column indices.  Dense tile-rows (mean tile nnz >= a threshold)
+// use 16x16 dense accumulators instead (position = slot*256 + r*16 + c).
+// Tile-rows too large for shared memory accumulate in C's value array.
+//
+// Roofline: the DFMA issue rate bounds the loop (2 FLOP per intermediate
+// product); HBM traffic is A and B once (B rows are re-read from L2) plus
+// 12 bytes per C entry written.
+#include "tsg_numeric.cuh"
+
+namespace tsg {
+
+namespace {
+
+__device__ __forceinline__ int lower_bound_dev(const int *a, int n, int key) {
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (a[mid] < key) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+
+// row-segment offset within the row for C tile s, local row r is packed in
+// the top 16 bits of word[s*16+r], the row mask in the low 16 bits
+__device__ __forceinline__ int rank_in_row(unsigned w, int c) {
+    return (int)(w >> 16) + __popc((w & 0xffffu) >> (TILE - c));
+}
+
+template <int NT, bool DENSE, bool DUPSAFE>
+__global__ void __launch_bounds__(NT, 1024 / NT)
+k_numeric_smem(NumericArgs g, int mybin)
+{
+    constexpr int NWARP = NT / 32;
+    extern __shared__ __align__(16) unsigned char s_raw[];
+    const int i = blockIdx.x;
+    if (g.bin[i] != mybin) return;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int r0 = i * TILE;
+    const int rows = min(TILE, g.m - r0);
+    const long long c0 = g.crp[i];
+    const int S = (int)(g.crp[i + 1] - c0);
+    const long long R0 = g.rowptrC[r0];
+    const int nnz_tr = (int)(g.rowptrC[r0 + rows] - R0);
+    const int jbase = g.ccol[c0];
+    const int span = g.ccol[c0 + S - 1] - jbase + 1;
+    const bool use_map = span <= MAP_MAX;
+
+    int *scol = reinterpret_cast<int *>(s_raw);
+    unsigned *word = reinterpret_cast<unsigned *>(s_raw + align16((long long)S * 4));
+    unsigned short *map = reinterpret_cast<unsigned short *>(s_raw + align16((long long)S * 4) + align16((long long)S * TILE * 4));
+    double *acc = reinterpret_cast<double *>(s_raw + align16((long long)S * 4) + align16((long long)S * TILE * 4) +
+                                             (use_map ? align16((long long)span * 2) : 0));
+
+    for (int s = tid; s < S; s += NT) {
+        int j = g.ccol[c0 + s];
+        scol[s] = j;
+        if (use_map) map[j - jbase] = (unsigned short)s;
+    }
+    // packed words: per row, exclusive scan of popc over the tile-row's tiles
+    for (int r = warp; r < TILE; r += NWARP) {
+        int run = (r < rows) ? (int)(g.rowptrC[r0 + r] - R0) : 0;
+        for (int sb = 0; sb < S; sb += 32) {
+            const int s = sb + lane;
+            unsigned mk = (s < S) ? (unsigned)g.cmask[(c0 + s) * TILE + r] : 0u;
+            int c = __popc(mk);
+            int incl = warp_incl_scan(c, lane);
+            if (s < S) word[s * TILE + r] = ((unsigned)(run + incl - c) << 16) | mk;
+            run += __shfl_sync(0xffffffffu, incl, 31);
+        }
+    }
+    {
+        const long long nacc = DENSE ? (long long)S * 256 : (long long)nnz_tr;
+        unsigned long long *z = reinterpret_cast<unsigned long long *>(acc);
+        for (long long t = tid; t < nacc; t += NT) z[t] = 0ull;
+    }
+    __syncthreads();
+
+    for (int r = warp; r < rows; r += NWARP) {
+        const int R = r0 + r;
+        const int pa0 = (int)g.rpA[R], pa1 = (int)g.rpA[R + 1];
+        for (int pb = pa0; pb < pa1; pb += 32) {
+            const int na = min(32, pa1 - pb);
+            int bs = 0, be = 0;
+            double av = 0.0;
+            if (lane < na) {
+                const int k = g.colA[pb + lane];
+                av = g.valA[pb + lane];
+                bs = (int)g.rpB[k];
+                be = (int)g.rpB[k + 1];
+            }
+            for (int t = 0; t < na; ++t) {
+                const double a = __shfl_sync(0xffffffffu, av, t);
+                const int b0 = __shfl_sync(0xffffffffu, bs, t);
+                const int b1 = __shfl_sync(0xffffffffu, be, t);
+                if (!DUPSAFE) {
+                    for (int e = b0 + lane; e < b1; e += 32) {
+                        const int col = g.colB[e];
+                        const double b = g.valB[e];
+                        const int j = col >> 4, c = col & 15;
+                        const int s = use_map ? (int)map[j - jbase] : lower_bound_dev(scol, S, j);
+                        int pos;
+                        if (DENSE) pos = s * 256 + r * TILE + c;
+                        else pos = rank_in_row(word[s * TILE + r], c);
+                        acc[pos] = fma(a, b, acc[pos]);
+                    }
+                } else {
+                    for (int eb = b0; eb < b1; eb += 32) {
+                        const int e = eb + lane;
+                        const bool ok = e < b1;
+                        const unsigned act = __ballot_sync(0xffffffffu, ok);
+                        if (ok) {
+                            const int col = g.colB[e];
+                            const double b = g.valB[e];
+                            const int j = col >> 4, c = col & 15;
+                            const int s = use_map ? (int)map[j - jbase] : lower_bound_dev(scol, S, j);
+                            int pos;
+                            if (DENSE) pos = s * 256 + r * TILE + c;
+                            else pos = rank_in_row(word[s * TILE + r], c);
+                            const unsigned peers = __match_any_sync(act, pos);
+                            const int rank = __popc(peers & lanemask_lt());
+                            const int rounds = __reduce_max_sync(act, __popc(peers));
+                            for (int q = 0; q < rounds; ++q) {
+                                if (q == rank) acc[pos] = fma(a, b, acc[pos]);
+                                __syncwarp(act);
+                            }
+                        }
+                    }
+                }
+            }
+        }
+    }
+    __syncthreads();
+
+    // epilogue: values (coalesced for the sparse layout) and column indices
+    if (!DENSE) {
+        for (int p = tid; p < nnz_tr; p += NT) g.valC[R0 + p] = acc[p];
+    }
+    for (int t = tid; t < S * TILE; t += NT) {
+        const int s = t / TILE, r = t - s * TILE;
+        if (r >= rows) continue;
+        const unsigned w = word[t];
+        unsigned mk = w & 0xffffu;
+        long long dst = R0 + (w >> 16);
+        const int jb = scol[s] * TILE;
+        while (mk) {
+            const int b = 31 - __clz(mk);   // highest bit = smallest local column
+            const int c = TILE - 1 - b;
+            g.colC[dst] = jb + c;
+            if (DENSE) g.valC[dst] = acc[s * 256 + r * TILE + c];
+            ++dst;
+            mk &= ~(1u << b);
+        }
+    }
+}
+
+// ---- tile-rows too large for shared memory ----------------------------------
+
+// per C tile and row: offset of its segment inside the C row; column indices;
+// zeroed values
+__global__ void __launch_bounds__(256)
+k_global_prep(NumericArgs g)
+{
+    const int i = blockIdx.x;
+    if (g.bin[i] != BIN_GLOBAL) return;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int r0 = i * TILE, rows = min(TILE, g.m - r0);
+    const long long c0 = g.crp[i];
+    const int S = (int)(g.crp[i + 1] - c0);
+    for (int r = warp; r < rows; r += 8) {
+        const long long Rb = g.rowptrC[r0 + r];
+        int run = 0;
+        for (int sb = 0; sb < S; sb += 32) {
+            const int s = sb + lane;
+            unsigned mk = (s < S) ? (unsigned)g.cmask[(c0 + s) * TILE + r] : 0u;
+            int c = __popc(mk);
+            int incl = warp_incl_scan(c, lane);
+            if (s < S) {
+                int off = run + incl - c;
+                g.offC[(c0 + s) * TILE + r] = off;
+                long long dst = Rb + off;
+                const int jb = g.ccol[c0 + s] * TILE;
+                while (mk) {
+                    const int b = 31 - __clz(mk);
+                    g.colC[dst] = jb + (TILE - 1 - b);
+                    g.valC[dst] = 0.0;
+                    ++dst;
+                    mk &= ~(1u << b);
+                }
+            }
+            run += __shfl_sync(0xffffffffu, incl, 31);
+        }
+    }
+}
+
+// one warp per C row of a global-bin tile-row; accumulates in place
+template <bool DUPSAFE>
+__global__ void __launch_bounds__(256)
+k_numeric_global(NumericArgs g)
+{
+    const int R = blockIdx.x * 8 + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (R >= g.m) return;
+    const int i = R / TILE, r = R - i * TILE;
+    if (g.bin[i] != BIN_GLOBAL) return;
+    const long long c0 = g.crp[i];
+    const int S = (int)(g.crp[i + 1] - c0);
+    const int *tc = g.ccol + c0;
+    const long long Rb = g.rowptrC[R];
+    const int pa0 = (int)g.rpA[R], pa1 = (int)g.rpA[R + 1];
+    for (int pb = pa0; pb < pa1; pb += 32) {
+        const int na = min(32, pa1 - pb);
+        int bs = 0, be = 0;
+        double av = 0.0;
+        if (lane < na) {
+            const int k = g.colA[pb + lane];
+            av = g.valA[pb + lane];
+            bs = (int)g.rpB[k];
+            be = (int)g.rpB[k + 1];
+        }
+        for (int t = 0; t < na; ++t) {
+            const double a = __shfl_sync(0xffffffffu, av, t);
+            const int b0 = __shfl_sync(0xffffffffu, bs, t);
+            const int b1 = __shfl_sync(0xffffffffu, be, t);
+            for (int eb = b0; eb < b1; eb += 32) {
+                const int e = eb + lane;
+                const bool ok = e < b1;
+                const unsigned act = __ballot_sync(0xffffffffu, ok);
+                if (ok) {
+                    const int col = g.colB[e];
+                    const double b = g.valB[e];
+                    const int j = col >> 4, c = col & 15;
+                    const int s = lower_bound_dev(tc, S, j);
+                    const unsigned mk = g.cmask[(c0 + s) * TILE + r];
+                    const long long pos = Rb + g.offC[(c0 + s) * TILE + r] + __popc(mk >> (TILE - c));
+                    if (!DUPSAFE) {
+                        g.valC[pos] = fma(a, b, g.valC[pos]);
+                    } else {
+                        const unsigned peers = __match_any_sync(act, (unsigned)(pos & 0xffffffff));
+                        const int rank = __popc(peers & lanemask_lt());
+                        const int rounds = __reduce_max_sync(act, __popc(peers));
+                        for (int q = 0; q < rounds; ++q) {
+                            if (q == rank) g.valC[pos] = fma(a, b, g.valC[pos]);
+                            __syncwarp(act);
+                        }
+                    }
+                }
+            }
+        }
+    }
+}
+
+template <int NT, bool DENSE, bool DUPSAFE>
+cudaError_t set_smem_attr() {
+    return cudaFuncSetAttribute(k_numeric_smem<NT, DENSE, DUPSAFE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)SMEM_LARGE);
+}
+
+template <int NT>
+cudaError_t launch_smem(const NumericArgs &a, int bin, long long smem, bool dense, bool dup, cudaStream_t s) {
+    const unsigned grid = (unsigned)a.blkm;
+    if (dense) {
+        if (dup) { k_numeric_smem<NT, true, true><<<grid, NT, smem, s>>>(a, bin); ::tsg::count_launch(); }
+        else { k_numeric_smem<NT, true, false><<<grid, NT, smem, s>>>(a, bin); ::tsg::count_launch(); }
+    } else {
+        if (dup) { k_numeric_smem<NT, false, true><<<grid, NT, smem, s>>>(a, bin); ::tsg::count_launch(); }
+        else { k_numeric_smem<NT, false, false><<<grid, NT, smem, s>>>(a, bin); ::tsg::count_launch(); }
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t numeric_init_attributes()
+{
+    cudaError_t e = cudaSuccess;
+#define TSG_SET(NT)                                                    \
+    if (e == cudaSuccess) e = set_smem_attr<NT, false, false>();       \
+    if (e == cudaSuccess) e = set_smem_attr<NT, false, true>();        \
+    if (e == cudaSuccess) e = set_smem_attr<NT, true, false>();        \
+    if (e == cudaSuccess) e = set_smem_attr<NT, true, true>();
+    TSG_SET(128)
+    TSG_SET(256)
+    TSG_SET(512)
+#undef TSG_SET
+    return e;
+}
+
+cudaError_t numeric_run(Pool &pool, const NumericArgs &a, const long long *counts, const long long *req,
+                        bool dupsafe, int threads)
+{
+    cudaStream_t s = pool.stream;
+    cudaError_t e = cudaSuccess;
+    for (int b = BIN_SPARSE_S; b <= BIN_DENSE_L && e == cudaSuccess; ++b) {
+        if (counts[b] == 0) continue;
+        const bool dense = (b == BIN_DENSE_S || b == BIN_DENSE_L);
+        const long long smem = req[b];
+        if (threads == 128) e = launch_smem<128>(a, b, smem, dense, dupsafe, s);
+        else if (threads == 512) e = launch_smem<512>(a, b, smem, dense, dupsafe, s);
+        else e = launch_smem<256>(a, b, smem, dense, dupsafe, s);
+    }
+    if (e == cudaSuccess && counts[BIN_GLOBAL] > 0) {
+        { k_global_prep<<<(unsigned)a.blkm, 256, 0, s>>>(a); ::tsg::count_launch(); }
+        const unsigned g = (unsigned)((a.m + 7) / 8);
+        if (dupsafe) { k_numeric_global<true><<<g, 256, 0, s>>>(a); ::tsg::count_launch(); }
+        else { k_numeric_global<false><<<g, 256, 0, s>>>(a); ::tsg::count_launch(); }
+        e = cudaGetLastError();
+    }
+    return e;
+}
+
+}  // namespace tsg

@@ -1,0 +1,82 @@
+// tsg_numeric.cuh -- numeric-step bins shared by step 2 (which classifies
+// C's tile-rows) and the numeric kernels.
+#pragma once
+#include "tsg_internal.cuh"
+
+namespace tsg {
+
+// Numeric bins of C's tile-rows (the nsparse-style binning of
+// spgemm_nsparse_kernel.h:4-14 / the reference's tile bins at
+// main_spgemm-col.cu:26-29, here chosen per tile-row by accumulator size):
+enum NumericBin : int {
+    BIN_EMPTY = 0,      // no entries
+    BIN_SPARSE_S = 1,   // mask-rank accumulator in shared memory, <= SMEM_SMALL bytes
+    BIN_SPARSE_L = 2,   // same, <= SMEM_LARGE bytes (one CTA per SM)
+    BIN_DENSE_S = 3,    // dense 16x16 tile accumulators in shared memory, <= SMEM_SMALL
+    BIN_DENSE_L = 4,    // same, <= SMEM_LARGE
+    BIN_GLOBAL = 5,     // accumulator in C's value array (any size)
+    NBIN = 6
+};
+
+constexpr long long SMEM_SMALL = 48 * 1024;
+constexpr long long SMEM_LARGE = 200 * 1024;
+constexpr long long MAP_MAX = 8192;   // direct tile-column -> slot map when the window is this narrow
+
+struct NumericBinParams {
+    int dense_tile_min;   // mean C-tile nnz at which a tile-row uses dense accumulators
+    int smem_acc_max;     // largest tile-row (entries) accumulated in shared memory
+};
+
+__host__ __device__ inline long long align16(long long x) { return (x + 15) & ~15ll; }
+
+// Shared-memory layout of a tile-row in the numeric kernels:
+//   int   scol[S]       C tile columns
+//   u32   word[S*16]    (offset of the tile's row segment inside the tile-row << 16) | row mask
+//   u16   map[span]     tile column - scol[0] -> slot (only when span <= MAP_MAX)
+//   f64   acc[...]      nnz_tr entries (sparse) or S*256 (dense)
+__host__ __device__ inline long long numeric_smem_bytes(long long S, long long nnz_tr, long long span, bool dense) {
+    long long b = align16(S * 4) + align16(S * TILE * 4) + (span <= MAP_MAX ? align16(span * 2) : 0);
+    return b + (dense ? S * 256 * 8 : nnz_tr * 8);
+}
+
+__host__ __device__ inline void numeric_classify(const NumericBinParams &bp, long long S, long long nnz_tr, long long span,
+                                                 int &bin, long long &req) {
+    req = 0;
+    if (nnz_tr == 0) { bin = BIN_EMPTY; return; }
+    const long long dreq = numeric_smem_bytes(S, nnz_tr, span, true);
+    const long long sreq = numeric_smem_bytes(S, nnz_tr, span, false);
+    if (nnz_tr >= (long long)bp.dense_tile_min * S && dreq <= SMEM_LARGE && nnz_tr < 65536) {
+        bin = dreq <= SMEM_SMALL ? BIN_DENSE_S : BIN_DENSE_L;
+        req = dreq;
+    } else if (nnz_tr <= bp.smem_acc_max && sreq <= SMEM_LARGE && nnz_tr < 65536) {
+        bin = sreq <= SMEM_SMALL ? BIN_SPARSE_S : BIN_SPARSE_L;
+        req = sreq;
+    } else {
+        bin = BIN_GLOBAL;
+    }
+}
+
+struct NumericArgs {
+    int m, blkm;
+    const long long *rpA; const int *colA; const double *valA;
+    const long long *rpB; const int *colB; const double *valB;
+    const long long *crp; const int *ccol; const uint16_t *cmask;
+    const long long *rowptrC; int *colC; double *valC;
+    const unsigned char *bin;
+    int *offC;      // 16 int32 per C tile (global bin only)
+    int *flags;
+};
+
+cudaError_t step2_masks(Pool &pool, const TileCSR &A, const TileCSR &B, int m, int blkm, const long long *crp,
+                        const int *ccol, uint16_t *cmask, int *rowcnt, int max_tiles_per_row,
+                        const NumericBinParams &bp, unsigned char *bin, long long *binstat, int *flags);
+
+// Launch the numeric kernels of every non-empty bin.  counts/req are the
+// per-bin tile-row counts and maximum shared-memory sizes from step 2.
+cudaError_t numeric_run(Pool &pool, const NumericArgs &a, const long long *counts, const long long *req,
+                        bool dupsafe, int threads);
+
+cudaError_t symbolic_init_attributes();
+cudaError_t numeric_init_attributes();
+
+}  // namespace tsg

@@ -1,0 +1,596 @@
+// tsg_tiles.cu -- CSR preparation, CSR -> 16x16 tile structure, the
+// tile-level symbolic product (step 1), and the stable CSR transpose used
+// for A*A^T.
+//
+// Both the conversion and step 1 are "sorted union of small integer keys per
+// tile-row": the tile columns touched by 16 CSR rows (conversion,
+// main_spgemm-col.cu:44-120 + :4976-4985), or the union over A's tiles (i,k)
+// of B's tile-row k (step 1, main_spgemm-col.cu:122-188 and :572-627; the
+// reference runs nsparse hash SpGEMM on the tile pattern for it,
+// spgemm_nsparse_kernel.h:221-311, 1171-1438).  Here one warp owns a
+// tile-row and sets bits in a shared-memory bitmap over the row's key window
+// [min, max]; popc gives the count, a warp scan of per-word popc gives each
+// key its rank, so the list comes out sorted with no sort and no hash.  Rows
+// whose window exceeds 4096 keys go to a CTA-wide kernel that walks the
+// window in 262,144-key chunks (any width).
+//
+// Roofline: HBM-bound; the conversion reads each CSR column index twice
+// (count pass, fill pass) and writes 36 bytes per tile.
+#include "tsg_internal.cuh"
+#include <climits>
+
+namespace tsg {
+
+namespace {
+
+constexpr int NW = 128;                 // narrow bitmap: 128 words = 4096 keys per warp
+constexpr int WPC = 8;                  // warps per CTA in the narrow kernels
+constexpr int WIDE_WORDS = 8192;        // wide bitmap chunk: 262,144 keys
+constexpr int WIDE_THREADS = 256;
+constexpr int WIDE_SMEM = WIDE_WORDS * 4 * 2;  // bitmap + word prefix
+
+// ---- key sources --------------------------------------------------------
+
+// Tile columns of the entries of one tile-row of a CSR matrix.
+struct CsrKeys {
+    struct Params { const long long *rp; const int *col; int m, n; };
+    const long long *rp; const int *col; int n, r0, r1;
+    __device__ CsrKeys(const Params &p, int row)
+        : rp(p.rp), col(p.col), n(p.n), r0(row * TILE), r1(min(p.m, row * TILE + TILE)) {}
+    __device__ void bounds(int start, int stride, int &kmin, int &kmax) const {
+        for (long long q = rp[r0] + start; q < rp[r1]; q += stride) {
+            int c = col[q];
+            if ((unsigned)c < (unsigned)n) { kmin = min(kmin, c >> 4); kmax = max(kmax, c >> 4); }
+        }
+    }
+    template <class F> __device__ void each(int start, int stride, F &&f) const {
+        for (int r = r0; r < r1; ++r) {
+            const long long e = rp[r + 1];
+            for (long long q = rp[r] + start; q < e; q += stride) {
+                int c = col[q];
+                if ((unsigned)c < (unsigned)n) f(c >> 4, r - r0, c & 15);
+            }
+        }
+    }
+};
+
+// Tile columns of C's tile-row i: union over A's tiles (i,k) of B's tile-row k.
+struct UnionKeys {
+    struct Params { const int *arp; const int *acol; const int *brp; const int *bcol; };
+    const int *arp, *acol, *brp, *bcol; int i;
+    __device__ UnionKeys(const Params &p, int row) : arp(p.arp), acol(p.acol), brp(p.brp), bcol(p.bcol), i(row) {}
+    __device__ void bounds(int start, int stride, int &kmin, int &kmax) const {
+        for (int a = arp[i] + start; a < arp[i + 1]; a += stride) {
+            int k = acol[a];
+            int q0 = brp[k], q1 = brp[k + 1];
+            if (q1 > q0) { kmin = min(kmin, bcol[q0]); kmax = max(kmax, bcol[q1 - 1]); }
+        }
+    }
+    template <class F> __device__ void each(int start, int stride, F &&f) const {
+        for (int a = arp[i]; a < arp[i + 1]; ++a) {
+            int k = acol[a];
+            const int q1 = brp[k + 1];
+            for (int q = brp[k] + start; q < q1; q += stride) f(bcol[q], 0, 0);
+        }
+    }
+};
+
+// ---- narrow path: one warp per tile-row ----------------------------------
+
+template <class KS>
+__global__ void __launch_bounds__(WPC * 32)
+k_union_count(typename KS::Params P, int nrows, int *cnt, int *wide_list, int *wide_n, int *stat_max)
+{
+    __shared__ unsigned s_bm[WPC][NW];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int row = blockIdx.x * WPC + warp;
+    if (row >= nrows) return;
+    KS ks(P, row);
+    int kmin = INT_MAX, kmax = -1;
+    ks.bounds(lane, 32, kmin, kmax);
+    kmin = warp_min_int(kmin);
+    kmax = warp_max_int(kmax);
+    if (kmax < kmin) { if (lane == 0) cnt[row] = 0; return; }
+    const long long span = (long long)kmax - kmin + 1;
+    if (span > NW * 32) {
+        if (lane == 0) { cnt[row] = 0; wide_list[atomicAdd(wide_n, 1)] = row; }
+        return;
+    }
+    unsigned *bm = s_bm[warp];
+    const int nwords = (int)((span + 31) >> 5);
+    for (int w = lane; w < nwords; w += 32) bm[w] = 0;
+    __syncwarp();
+    ks.each(lane, 32, [&](int key, int, int) {
+        int o = key - kmin;
+        atomicOr(&bm[o >> 5], 1u << (o & 31));
+    });
+    __syncwarp();
+    int c = 0;
+    for (int w = lane; w < nwords; w += 32) c += __popc(bm[w]);
+    c = warp_sum_int(c);
+    if (lane == 0) {
+        cnt[row] = c;
+        if (stat_max) atomicMax(stat_max, c);
+    }
+}
+
+template <class KS, bool MASK, typename TP>
+__global__ void __launch_bounds__(WPC * 32)
+k_union_fill(typename KS::Params P, int nrows, const TP *rowptr, int *out, uint16_t *mask)
+{
+    __shared__ unsigned s_bm[WPC][NW];
+    __shared__ unsigned short s_pref[WPC][NW];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int row = blockIdx.x * WPC + warp;
+    if (row >= nrows) return;
+    KS ks(P, row);
+    int kmin = INT_MAX, kmax = -1;
+    ks.bounds(lane, 32, kmin, kmax);
+    kmin = warp_min_int(kmin);
+    kmax = warp_max_int(kmax);
+    if (kmax < kmin) return;
+    const long long span = (long long)kmax - kmin + 1;
+    if (span > NW * 32) return;  // handled by the wide kernel
+    unsigned *bm = s_bm[warp];
+    unsigned short *pref = s_pref[warp];
+    const int nwords = (int)((span + 31) >> 5);
+    for (int w = lane; w < nwords; w += 32) bm[w] = 0;
+    __syncwarp();
+    ks.each(lane, 32, [&](int key, int, int) {
+        int o = key - kmin;
+        atomicOr(&bm[o >> 5], 1u << (o & 31));
+    });
+    __syncwarp();
+    const int wpl = (nwords + 31) >> 5;
+    const int w0 = min(nwords, lane * wpl), w1 = min(nwords, w0 + wpl);
+    int lc = 0;
+    for (int w = w0; w < w1; ++w) lc += __popc(bm[w]);
+    const int incl = warp_incl_scan(lc, lane);
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    const long long base = (long long)rowptr[row];
+    int run = incl - lc;
+    for (int w = w0; w < w1; ++w) {
+        unsigned x = bm[w];
+        pref[w] = (unsigned short)run;
+        while (x) {
+            int b = __ffs(x) - 1;
+            out[base + run] = kmin + w * 32 + b;
+            ++run;
+            x &= x - 1;
+        }
+    }
+    if (MASK) {
+        // zero this tile-row's masks, then OR the entries in
+        unsigned *mw = reinterpret_cast<unsigned *>(mask) + base * 8;
+        for (int t = lane; t < total * 8; t += 32) mw[t] = 0u;
+        __syncwarp();
+        ks.each(lane, 32, [&](int key, int r, int c) {
+            int o = key - kmin, w = o >> 5;
+            int slot = pref[w] + __popc(bm[w] & ((1u << (o & 31)) - 1u));
+            atomic_or_mask16(mask, (base + slot) * TILE + r, 1u << (TILE - 1 - c));
+        });
+    }
+}
+
+// ---- wide path: one CTA per tile-row, chunked window ----------------------
+
+__device__ __forceinline__ int block_reduce_min(int v, int *sred) {
+    v = warp_min_int(v);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) sred[warp] = v;
+    __syncthreads();
+    int r = INT_MAX;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r = min(r, sred[w]);
+    __syncthreads();
+    return r;
+}
+__device__ __forceinline__ int block_reduce_max(int v, int *sred) {
+    v = warp_max_int(v);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) sred[warp] = v;
+    __syncthreads();
+    int r = -1;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r = max(r, sred[w]);
+    __syncthreads();
+    return r;
+}
+__device__ __forceinline__ long long block_reduce_sum_ll(long long v, long long *sred) {
+    v = warp_sum_ll(v);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) sred[warp] = v;
+    __syncthreads();
+    long long r = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r += sred[w];
+    __syncthreads();
+    return r;
+}
+
+// FILL=false: count (cnt[row]); FILL=true: sorted list + optional masks.
+template <class KS, bool FILL, bool MASK, typename TP>
+__global__ void __launch_bounds__(WIDE_THREADS)
+k_union_wide(typename KS::Params P, const int *wide_list, const int *wide_n, int *cnt, int *stat_max,
+             const TP *rowptr, int *out, uint16_t *mask)
+{
+    extern __shared__ unsigned s_dyn[];
+    unsigned *bm = s_dyn;
+    int *pref = reinterpret_cast<int *>(s_dyn + WIDE_WORDS);
+    __shared__ int s_red[WIDE_THREADS / 32];
+    __shared__ long long s_redll[WIDE_THREADS / 32];
+    __shared__ int s_wsum[WIDE_THREADS / 32];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int nw = *wide_n;
+    for (int wi = blockIdx.x; wi < nw; wi += gridDim.x) {
+        const int row = wide_list[wi];
+        KS ks(P, row);
+        int kmin = INT_MAX, kmax = -1;
+        ks.bounds(tid, WIDE_THREADS, kmin, kmax);
+        kmin = block_reduce_min(kmin, s_red);
+        kmax = block_reduce_max(kmax, s_red);
+        long long base = 0;
+        if (FILL) {
+            base = (long long)rowptr[row];
+            if (MASK) {
+                const long long ntiles = (long long)rowptr[row + 1] - base;
+                unsigned *mw = reinterpret_cast<unsigned *>(mask) + base * 8;
+                for (long long t = tid; t < ntiles * 8; t += WIDE_THREADS) mw[t] = 0u;
+                __syncthreads();
+            }
+        }
+        long long run = 0;
+        for (long long c0 = kmin; c0 <= kmax; c0 += (long long)WIDE_WORDS * 32) {
+            const long long span = min((long long)WIDE_WORDS * 32, (long long)kmax - c0 + 1);
+            const int nwords = (int)((span + 31) >> 5);
+            for (int w = tid; w < nwords; w += WIDE_THREADS) bm[w] = 0;
+            __syncthreads();
+            ks.each(tid, WIDE_THREADS, [&](int key, int, int) {
+                long long o = (long long)key - c0;
+                if (o >= 0 && o < span) atomicOr(&bm[o >> 5], 1u << (o & 31));
+            });
+            __syncthreads();
+            const int wpt = (nwords + WIDE_THREADS - 1) / WIDE_THREADS;
+            const int w0 = min(nwords, tid * wpt), w1 = min(nwords, w0 + wpt);
+            int lc = 0;
+            for (int w = w0; w < w1; ++w) lc += __popc(bm[w]);
+            if (!FILL) {
+                run += block_reduce_sum_ll(lc, s_redll);
+                continue;
+            }
+            // block exclusive scan of lc
+            int incl = warp_incl_scan(lc, lane);
+            if (lane == 31) s_wsum[warp] = incl;
+            __syncthreads();
+            int woff = 0, chunk_total = 0;
+            for (int w = 0; w < WIDE_THREADS / 32; ++w) {
+                if (w < warp) woff += s_wsum[w];
+                chunk_total += s_wsum[w];
+            }
+            int r2 = woff + incl - lc;
+            for (int w = w0; w < w1; ++w) {
+                unsigned x = bm[w];
+                pref[w] = r2;
+                while (x) {
+                    int b = __ffs(x) - 1;
+                    out[base + run + r2] = (int)(c0 + w * 32 + b);
+                    ++r2;
+                    x &= x - 1;
+                }
+            }
+            __syncthreads();
+            if (MASK) {
+                ks.each(tid, WIDE_THREADS, [&](int key, int r, int c) {
+                    long long o = (long long)key - c0;
+                    if (o >= 0 && o < span) {
+                        int w = (int)(o >> 5);
+                        long long slot = run + pref[w] + __popc(bm[w] & ((1u << (o & 31)) - 1u));
+                        atomic_or_mask16(mask, (base + slot) * TILE + r, 1u << (TILE - 1 - c));
+                    }
+                });
+            }
+            run += chunk_total;
+            __syncthreads();
+        }
+        if (!FILL && tid == 0) {
+            cnt[row] = (int)run;
+            if ((long long)(int)run != run) set_flag(stat_max, 0);  // cannot happen for int keys
+            if (stat_max) atomicMax(stat_max, (int)run);
+        }
+        __syncthreads();
+    }
+}
+
+// ---- preparation ----------------------------------------------------------
+
+template <typename Tr>
+__global__ void k_prepare_rowptr(const Tr *__restrict__ rp, long long m, long long nnz, long long *out, int *flags)
+{
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i > m) return;
+    long long v = (long long)rp[i];
+    bool bad = (v < 0 || v > nnz) || (i == 0 && v != 0) || (i == m && v != nnz);
+    if (i < m && (long long)rp[i + 1] < v) bad = true;
+    if (bad) set_flag(flags, FLAG_BAD_INPUT);
+    out[i] = v < 0 ? 0 : (v > nnz ? nnz : v);
+}
+
+__global__ void k_check_cols(const int *__restrict__ col, long long nnz, int n, int *flags)
+{
+    bool bad = false;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < nnz; q += (long long)gridDim.x * blockDim.x)
+        bad |= ((unsigned)col[q] >= (unsigned)n);
+    if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) set_flag(flags, FLAG_BAD_INPUT);
+}
+
+// ---- stable transpose (CSR of A^T), LSD radix sort of (column, position) --
+
+constexpr int RADIX_THREADS = 256;
+constexpr int RADIX_ITEMS = 8;
+constexpr int RADIX_CHUNK = RADIX_THREADS * RADIX_ITEMS;
+constexpr int RADIX_BITS = 8;
+constexpr int RADIX_BINS = 1 << RADIX_BITS;
+
+// per-chunk digit histogram; counts laid out digit-major (digit * nchunks + chunk)
+__global__ void __launch_bounds__(RADIX_THREADS)
+k_radix_hist(const int *__restrict__ keys, long long n, int shift, int nchunks, int *counts)
+{
+    __shared__ int s_h[RADIX_BINS];
+    for (int d = threadIdx.x; d < RADIX_BINS; d += RADIX_THREADS) s_h[d] = 0;
+    __syncthreads();
+    const long long base = (long long)blockIdx.x * RADIX_CHUNK;
+    for (int j = threadIdx.x; j < RADIX_CHUNK; j += RADIX_THREADS) {
+        long long q = base + j;
+        if (q < n) atomicAdd(&s_h[((unsigned)keys[q] >> shift) & (RADIX_BINS - 1)], 1);
+    }
+    __syncthreads();
+    for (int d = threadIdx.x; d < RADIX_BINS; d += RADIX_THREADS)
+        counts[(long long)d * nchunks + blockIdx.x] = s_h[d];
+}
+
+// stable scatter: items are ranked in input order within the chunk
+// (warp-contiguous sub-chunks, lanes striped inside each 32-item step)
+__global__ void __launch_bounds__(RADIX_THREADS)
+k_radix_scatter(const int *__restrict__ kin, const int *__restrict__ vin, int *kout, int *vout,
+                long long n, int shift, int nchunks, const int *__restrict__ offsets)
+{
+    constexpr int NWARP = RADIX_THREADS / 32;
+    __shared__ int s_cnt[NWARP][RADIX_BINS];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int d = threadIdx.x; d < NWARP * RADIX_BINS; d += RADIX_THREADS) (&s_cnt[0][0])[d] = 0;
+    __syncthreads();
+    const long long wbase = (long long)blockIdx.x * RADIX_CHUNK + (long long)warp * (RADIX_ITEMS * 32);
+    int key[RADIX_ITEMS], val[RADIX_ITEMS], dig[RADIX_ITEMS], loc[RADIX_ITEMS];
+#pragma unroll
+    for (int it = 0; it < RADIX_ITEMS; ++it) {
+        long long q = wbase + it * 32 + lane;
+        bool ok = q < n;
+        key[it] = ok ? kin[q] : 0;
+        val[it] = ok ? vin[q] : 0;
+        int d = ok ? (int)(((unsigned)key[it] >> shift) & (RADIX_BINS - 1)) : RADIX_BINS;  // RADIX_BINS = none
+        dig[it] = d;
+        unsigned peers = __match_any_sync(0xffffffffu, d);
+        int rank = __popc(peers & lanemask_lt());
+        int leader = __ffs(peers) - 1;
+        int before = 0;
+        if (ok) before = s_cnt[warp][d];
+        __syncwarp();
+        loc[it] = before + rank;
+        if (ok && lane == leader) s_cnt[warp][d] = before + __popc(peers);
+        __syncwarp();
+    }
+    __syncthreads();
+    // exclusive scan over warps, per digit
+    for (int d = threadIdx.x; d < RADIX_BINS; d += RADIX_THREADS) {
+        int run = 0;
+        for (int w = 0; w < NWARP; ++w) { int c = s_cnt[w][d]; s_cnt[w][d] = run; run += c; }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int it = 0; it < RADIX_ITEMS; ++it) {
+        long long q = wbase + it * 32 + lane;
+        if (q < n) {
+            int d = dig[it];
+            long long dst = (long long)offsets[(long long)d * nchunks + blockIdx.x] + s_cnt[warp][d] + loc[it];
+            kout[dst] = key[it];
+            vout[dst] = val[it];
+        }
+    }
+}
+
+__global__ void k_iota_and_keys(const int *__restrict__ col, long long nnz, int n, int *keys, int *vals)
+{
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < nnz; q += (long long)gridDim.x * blockDim.x) {
+        int c = col[q];
+        keys[q] = ((unsigned)c < (unsigned)n) ? c : n - 1;  // invalid input is flagged elsewhere
+        vals[q] = (int)q;
+    }
+}
+
+// row index of every entry (warp per row)
+__global__ void k_expand_rows(const long long *__restrict__ rp, int m, int *rowof)
+{
+    const int row = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (row >= m) return;
+    for (long long q = rp[row] + lane; q < rp[row + 1]; q += 32) rowof[q] = row;
+}
+
+// column histogram -> transposed row lengths
+__global__ void k_col_hist(const int *__restrict__ keys_sorted, long long nnz, int *len)
+{
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < nnz; q += (long long)gridDim.x * blockDim.x)
+        atomicAdd(&len[keys_sorted[q]], 1);
+}
+
+__global__ void k_gather_transposed(const int *__restrict__ perm, const int *__restrict__ rowof,
+                                    const double *__restrict__ val, long long nnz, int *tcol, double *tval)
+{
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < nnz; q += (long long)gridDim.x * blockDim.x) {
+        int p = perm[q];
+        tcol[q] = rowof[p];
+        tval[q] = val[p];
+    }
+}
+
+__global__ void k_i32_to_i64(const int *in, long long *out, long long n)
+{
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i < n) out[i] = in[i];
+}
+
+inline unsigned grid_for(long long n, int threads, long long cap = 152ll * 32) {
+    long long g = (n + threads - 1) / threads;
+    if (g < 1) g = 1;
+    if (g > cap) g = cap;
+    return (unsigned)g;
+}
+
+template <class KS, typename TP>
+cudaError_t union_structure(Pool &pool, typename KS::Params P, int nrows, int *cnt_scratch,
+                            TP *rowptr_out, int *out_cols, uint16_t *mask, int *flags, int *stat_max,
+                            cudaError_t (*scan)(Pool &, const int *, TP *, long long, int *))
+{
+    cudaStream_t s = pool.stream;
+    int *wide = pool.alloc_n<int>(nrows + 1);
+    if (!wide) return pool.err;
+    int *wide_n = wide + nrows;
+    cudaError_t e = cudaMemsetAsync(wide_n, 0, sizeof(int), s);
+    if (e != cudaSuccess) { pool.free(wide); return e; }
+    const unsigned g = (unsigned)((nrows + WPC - 1) / WPC);
+    if (nrows > 0) {
+        { k_union_count<KS><<<g, WPC * 32, 0, s>>>(P, nrows, cnt_scratch, wide, wide_n, stat_max); ::tsg::count_launch(); }
+        { k_union_wide<KS, false, false, TP><<<304, WIDE_THREADS, WIDE_SMEM, s>>>(
+            P, wide, wide_n, cnt_scratch, stat_max, nullptr, nullptr, nullptr); ::tsg::count_launch(); }
+    }
+    e = scan(pool, cnt_scratch, rowptr_out, nrows, flags);
+    if (e == cudaSuccess && nrows > 0 && out_cols) {
+        if (mask) {
+            { k_union_fill<KS, true, TP><<<g, WPC * 32, 0, s>>>(P, nrows, rowptr_out, out_cols, mask); ::tsg::count_launch(); }
+            { k_union_wide<KS, true, true, TP><<<304, WIDE_THREADS, WIDE_SMEM, s>>>(
+                P, wide, wide_n, nullptr, nullptr, rowptr_out, out_cols, mask); ::tsg::count_launch(); }
+        } else {
+            { k_union_fill<KS, false, TP><<<g, WPC * 32, 0, s>>>(P, nrows, rowptr_out, out_cols, nullptr); ::tsg::count_launch(); }
+            { k_union_wide<KS, true, false, TP><<<304, WIDE_THREADS, WIDE_SMEM, s>>>(
+                P, wide, wide_n, nullptr, nullptr, rowptr_out, out_cols, nullptr); ::tsg::count_launch(); }
+        }
+    }
+    if (e == cudaSuccess) e = cudaGetLastError();
+    pool.free(wide);
+    return e;
+}
+
+template <class KS, bool FILL, bool MASK, typename TP>
+cudaError_t set_wide_smem() {
+    return cudaFuncSetAttribute(k_union_wide<KS, FILL, MASK, TP>, cudaFuncAttributeMaxDynamicSharedMemorySize, WIDE_SMEM);
+}
+
+}  // namespace
+
+cudaError_t tiles_init_attributes()
+{
+    cudaError_t e = cudaSuccess;
+    if (e == cudaSuccess) e = set_wide_smem<CsrKeys, false, false, int>();
+    if (e == cudaSuccess) e = set_wide_smem<CsrKeys, true, true, int>();
+    if (e == cudaSuccess) e = set_wide_smem<CsrKeys, true, false, int>();
+    if (e == cudaSuccess) e = set_wide_smem<UnionKeys, false, false, long long>();
+    if (e == cudaSuccess) e = set_wide_smem<UnionKeys, true, false, long long>();
+    if (e == cudaSuccess) e = set_wide_smem<UnionKeys, true, true, long long>();
+    return e;
+}
+
+cudaError_t prepare_csr(Pool &pool, const void *rp, int rp_bits, const int *col, int m, int n, long long nnz,
+                        long long *rp_out, int *flags, bool check_cols)
+{
+    cudaStream_t s = pool.stream;
+    unsigned g = (unsigned)((m + 1 + 255) / 256);
+    if (rp_bits == 64) { k_prepare_rowptr<long long><<<g, 256, 0, s>>>((const long long *)rp, m, nnz, rp_out, flags); ::tsg::count_launch(); }
+    else { k_prepare_rowptr<int><<<g, 256, 0, s>>>((const int *)rp, m, nnz, rp_out, flags); ::tsg::count_launch(); }
+    if (check_cols && nnz > 0) { k_check_cols<<<grid_for(nnz, 256), 256, 0, s>>>(col, nnz, n, flags); ::tsg::count_launch(); }
+    return cudaGetLastError();
+}
+
+// CSR -> tile structure (tile-row pointer, sorted tile columns, masks).
+// T.trp/tcol/mask must be allocated by the caller (tcol, mask with an upper
+// bound of the tile count: min(nnz, blkm*blkn)).
+cudaError_t csr_to_tile_structure(Pool &pool, const long long *rp, const int *col, TileCSR &T, bool masks,
+                                  int *flags, int *stat_max)
+{
+    int *cnt = pool.alloc_n<int>(T.blkm + 1);
+    if (!cnt) return pool.err;
+    CsrKeys::Params P{rp, col, T.m, T.n};
+    cudaError_t e = union_structure<CsrKeys, int>(pool, P, T.blkm, cnt, T.trp, T.tcol, masks ? T.mask : nullptr,
+                                                  flags, stat_max, scan_i32_to_i32);
+    pool.free(cnt);
+    return e;
+}
+
+// Step 1: C's tile-row pointer (crp, int64) and, when ccol != nullptr, the
+// sorted tile columns.  Call once with ccol == nullptr to size C.
+cudaError_t tile_symbolic(Pool &pool, const TileCSR &A, const TileCSR &B, long long *crp, int *ccol, int *cnt,
+                          int *flags, int *stat_max)
+{
+    UnionKeys::Params P{A.trp, A.tcol, B.trp, B.tcol};
+    return union_structure<UnionKeys, long long>(pool, P, A.blkm, cnt, crp, ccol, nullptr, flags, stat_max,
+                                                 scan_i32_to_i64);
+}
+
+// Stable CSR transpose: (tp, tcol, tval) = CSR of A^T (n x m).
+cudaError_t csr_transpose(Pool &pool, const long long *rp, const int *col, const double *val, int m, int n,
+                          long long nnz, long long *tp, int *tcol, double *tval, int *flags)
+{
+    cudaStream_t s = pool.stream;
+    cudaError_t e = cudaSuccess;
+    int *len = pool.alloc_n<int>(n + 1);
+    if (!len) return pool.err;
+    if (nnz == 0) {
+        e = cudaMemsetAsync(len, 0, sizeof(int) * (size_t)(n + 1), s);
+        if (e == cudaSuccess) e = scan_i32_to_i64(pool, len, tp, n, flags);
+        pool.free(len);
+        return e;
+    }
+    int *k0 = pool.alloc_n<int>(nnz), *v0 = pool.alloc_n<int>(nnz);
+    int *k1 = pool.alloc_n<int>(nnz), *v1 = pool.alloc_n<int>(nnz);
+    int *rowof = pool.alloc_n<int>(nnz);
+    const int nchunks = (int)((nnz + RADIX_CHUNK - 1) / RADIX_CHUNK);
+    int *counts = pool.alloc_n<int>((long long)RADIX_BINS * nchunks + 1);
+    if (!k0 || !v0 || !k1 || !v1 || !rowof || !counts) {
+        e = pool.err ? pool.err : cudaErrorMemoryAllocation;
+    } else {
+        { k_iota_and_keys<<<grid_for(nnz, 256), 256, 0, s>>>(col, nnz, n, k0, v0); ::tsg::count_launch(); }
+        int bits = 1;
+        while (bits < 31 && (1ll << bits) < (long long)n) ++bits;
+        for (int shift = 0; shift < bits && e == cudaSuccess; shift += RADIX_BITS) {
+            { k_radix_hist<<<nchunks, RADIX_THREADS, 0, s>>>(k0, nnz, shift, nchunks, counts); ::tsg::count_launch(); }
+            e = scan_i32_to_i32(pool, counts, counts, (long long)RADIX_BINS * nchunks, flags);
+            if (e != cudaSuccess) break;
+            { k_radix_scatter<<<nchunks, RADIX_THREADS, 0, s>>>(k0, v0, k1, v1, nnz, shift, nchunks, counts); ::tsg::count_launch(); }
+            int *t = k0; k0 = k1; k1 = t;
+            t = v0; v0 = v1; v1 = t;
+        }
+        if (e == cudaSuccess) {
+            { k_expand_rows<<<(unsigned)((m + 7) / 8), 256, 0, s>>>(rp, m, rowof); ::tsg::count_launch(); }
+            e = cudaMemsetAsync(len, 0, sizeof(int) * (size_t)(n + 1), s);
+        }
+        if (e == cudaSuccess) {
+            { k_col_hist<<<grid_for(nnz, 256), 256, 0, s>>>(k0, nnz, len); ::tsg::count_launch(); }
+            e = scan_i32_to_i64(pool, len, tp, n, flags);
+        }
+        if (e == cudaSuccess) {
+            { k_gather_transposed<<<grid_for(nnz, 256), 256, 0, s>>>(v0, rowof, val, nnz, tcol, tval); ::tsg::count_launch(); }
+            e = cudaGetLastError();
+        }
+    }
+    pool.free(k0); pool.free(v0); pool.free(k1); pool.free(v1);
+    pool.free(rowof); pool.free(counts); pool.free(len);
+    return e;
+}
+
+cudaError_t i32_to_i64(Pool &pool, const int *in, long long *out, long long n)
+{
+    if (n <= 0) return cudaSuccess;
+    { k_i32_to_i64<<<(unsigned)((n + 255) / 256), 256, 0, pool.stream>>>(in, out, n); ::tsg::count_launch(); }
+    return cudaGetLastError();
+}
+
+}  // namespace tsg
