@@ -43,6 +43,9 @@ def make_workload(name: str):
     if name == "st27-96":
         return M.stencil_27(96, seed=1), "AA", ("3D 27-point stencil 96^3 (n=884,736), values U[0.5,1.5], "
                                                  "diagonal = row sum, C = A*A")
+    if name.startswith("st27-") and name[5:].isdigit() and name != "st27-96":
+        side = int(name[5:])
+        return M.stencil_27(side, seed=1), "AA", f"3D 27-point stencil {side}^3, values U[0.5,1.5], diagonal = row sum, C = A*A"
     if name == "lap256":
         return M.laplacian_2d(256), "AA", "2D 5-point Laplacian 256x256 (n=65,536), diag 4, off -1, C = A*A"
     if name == "rmat16-aat":
@@ -108,7 +111,7 @@ class ClockSampler:
         try:
             self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                          "--format=csv,noheader,nounits", "-lms", "20"],
                                          stdout=self.f, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None

@@ -52,6 +52,15 @@ __device__ __forceinline__ int rank_in_row(unsigned w, int c) {
     return (int)(w >> 16) + __popc((w & 0xffffu) >> (TILE - c));
 }
 
+// slot of tile column j in the tile-row (-1 if it is not one of its tiles)
+__device__ __forceinline__ int slot_of(int j, int jbase, int span, bool use_map, const unsigned short *map,
+                                       const int *scol, int S) {
+    const unsigned off = (unsigned)(j - jbase);
+    if (off >= (unsigned)span) return -1;
+    const int s = use_map ? (int)map[off] : lower_bound_dev(scol, S, j);
+    return (s < S && scol[s] == j) ? s : -1;
+}
+
 template <int NT, bool DENSE, bool DUPSAFE>
 __global__ void __launch_bounds__(NT, 1024 / NT)
 k_numeric_smem(NumericArgs g, int mybin)
@@ -94,10 +103,10 @@ k_numeric_smem(NumericArgs g, int mybin)
             run += __shfl_sync(0xffffffffu, incl, 31);
         }
     }
+    const int nacc = DENSE ? S * 256 : nnz_tr;
     {
-        const long long nacc = DENSE ? (long long)S * 256 : (long long)nnz_tr;
         unsigned long long *z = reinterpret_cast<unsigned long long *>(acc);
-        for (long long t = tid; t < nacc; t += NT) z[t] = 0ull;
+        for (int t = tid; t < nacc; t += NT) z[t] = 0ull;
     }
     __syncthreads();
 
@@ -123,10 +132,10 @@ k_numeric_smem(NumericArgs g, int mybin)
                         const int col = g.colB[e];
                         const double b = g.valB[e];
                         const int j = col >> 4, c = col & 15;
-                        const int s = use_map ? (int)map[j - jbase] : lower_bound_dev(scol, S, j);
-                        int pos;
-                        if (DENSE) pos = s * 256 + r * TILE + c;
-                        else pos = rank_in_row(word[s * TILE + r], c);
+                        const int s = slot_of(j, jbase, span, use_map, map, scol, S);
+                        int pos = -1;
+                        if (s >= 0) pos = DENSE ? s * 256 + r * TILE + c : rank_in_row(word[s * TILE + r], c);
+                        if ((unsigned)pos >= (unsigned)nacc) { set_flag(g.flags, FLAG_INTERNAL); continue; }
                         acc[pos] = fma(a, b, acc[pos]);
                     }
                 } else {
@@ -138,15 +147,16 @@ k_numeric_smem(NumericArgs g, int mybin)
                             const int col = g.colB[e];
                             const double b = g.valB[e];
                             const int j = col >> 4, c = col & 15;
-                            const int s = use_map ? (int)map[j - jbase] : lower_bound_dev(scol, S, j);
-                            int pos;
-                            if (DENSE) pos = s * 256 + r * TILE + c;
-                            else pos = rank_in_row(word[s * TILE + r], c);
+                            const int s = slot_of(j, jbase, span, use_map, map, scol, S);
+                            int pos = -1;
+                            if (s >= 0) pos = DENSE ? s * 256 + r * TILE + c : rank_in_row(word[s * TILE + r], c);
+                            const bool okpos = (unsigned)pos < (unsigned)nacc;
+                            if (!okpos) { set_flag(g.flags, FLAG_INTERNAL); pos = -1 - lane; }
                             const unsigned peers = __match_any_sync(act, pos);
                             const int rank = __popc(peers & lanemask_lt());
                             const int rounds = __reduce_max_sync(act, __popc(peers));
                             for (int q = 0; q < rounds; ++q) {
-                                if (q == rank) acc[pos] = fma(a, b, acc[pos]);
+                                if (q == rank && okpos) acc[pos] = fma(a, b, acc[pos]);
                                 __syncwarp(act);
                             }
                         }
@@ -255,17 +265,19 @@ k_numeric_global(NumericArgs g)
                     const int col = g.colB[e];
                     const double b = g.valB[e];
                     const int j = col >> 4, c = col & 15;
-                    const int s = lower_bound_dev(tc, S, j);
+                    int s = lower_bound_dev(tc, S, j);
+                    const bool found = s < S && tc[s] == j;
+                    if (!found) { set_flag(g.flags, FLAG_INTERNAL); s = 0; }
                     const unsigned mk = g.cmask[(c0 + s) * TILE + r];
                     const long long pos = Rb + g.offC[(c0 + s) * TILE + r] + __popc(mk >> (TILE - c));
                     if (!DUPSAFE) {
-                        g.valC[pos] = fma(a, b, g.valC[pos]);
+                        if (found) g.valC[pos] = fma(a, b, g.valC[pos]);
                     } else {
-                        const unsigned peers = __match_any_sync(act, (unsigned)(pos & 0xffffffff));
+                        const unsigned peers = __match_any_sync(act, found ? (unsigned)(pos & 0xffffffff) : ~0u - lane);
                         const int rank = __popc(peers & lanemask_lt());
                         const int rounds = __reduce_max_sync(act, __popc(peers));
                         for (int q = 0; q < rounds; ++q) {
-                            if (q == rank) g.valC[pos] = fma(a, b, g.valC[pos]);
+                            if (q == rank && found) g.valC[pos] = fma(a, b, g.valC[pos]);
                             __syncwarp(act);
                         }
                     }

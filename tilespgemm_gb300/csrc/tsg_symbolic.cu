@@ -54,7 +54,7 @@ k_step2(int blkm, int m, const int *__restrict__ arp, const int *__restrict__ ac
         const uint16_t *__restrict__ amask, const int *__restrict__ brp, const int *__restrict__ bcol,
         const uint16_t *__restrict__ bmask, const long long *__restrict__ crp, const int *__restrict__ ccol,
         uint16_t *cmask, int *rowcnt, int smax, NumericBinParams bp, unsigned char *bin,
-        long long *binstat)
+        long long *binstat, int *flags)
 {
     extern __shared__ unsigned s_dyn[];
     __shared__ int s_rows[S2_WARPS][TILE];
@@ -100,7 +100,9 @@ k_step2(int blkm, int m, const int *__restrict__ arp, const int *__restrict__ ac
             const int r = s_rows[warp][t];
             unsigned acc = or_rows(s_rmask[warp][t], bmask, q);
             if (acc) {
-                const int s = lower_bound_i(scol, S, bcol[q]);
+                const int key = bcol[q];
+                const int s = lower_bound_i(scol, S, key);
+                if (s >= S || scol[s] != key) { set_flag(flags, FLAG_INTERNAL); continue; }
                 if (GLOBAL) atomic_or_mask16(cmask, (c0 + s) * TILE + r, acc);
                 else atomicOr(&smask[s * TILE + r], acc);
             }
@@ -154,7 +156,6 @@ cudaError_t step2_masks(Pool &pool, const TileCSR &A, const TileCSR &B, int m, i
                         const int *ccol, uint16_t *cmask, int *rowcnt, int max_tiles_per_row,
                         const NumericBinParams &bp, unsigned char *bin, long long *binstat, int *flags)
 {
-    (void)flags;
     cudaStream_t s = pool.stream;
     if (blkm <= 0) return cudaSuccess;
     // shared path: up to `smax` tiles per tile-row, (16*4 + 4) bytes per tile
@@ -162,10 +163,10 @@ cudaError_t step2_masks(Pool &pool, const TileCSR &A, const TileCSR &B, int m, i
     const int s_used = max_tiles_per_row < smax ? max_tiles_per_row : smax;
     const size_t smem = (size_t)s_used * (TILE * 4 + 4) + 16;
     { k_step2<false><<<blkm, S2_THREADS, smem, s>>>(blkm, m, A.trp, A.tcol, A.mask, B.trp, B.tcol, B.mask, crp, ccol,
-                                                   cmask, rowcnt, smax, bp, bin, binstat); ::tsg::count_launch(); }
+                                                   cmask, rowcnt, smax, bp, bin, binstat, flags); ::tsg::count_launch(); }
     if (max_tiles_per_row > smax)
         { k_step2<true><<<blkm, S2_THREADS, 0, s>>>(blkm, m, A.trp, A.tcol, A.mask, B.trp, B.tcol, B.mask, crp, ccol,
-                                                   cmask, rowcnt, smax, bp, bin, binstat); ::tsg::count_launch(); }
+                                                   cmask, rowcnt, smax, bp, bin, binstat, flags); ::tsg::count_launch(); }
     return cudaGetLastError();
 }
 
