@@ -171,6 +171,33 @@ tsg_status tsg_csr_free(tsg_ctx *ctx, tsg_csr *m);
 tsg_status tsg_spgemm(tsg_ctx *ctx, tsg_op op, const tsg_csr *A, const tsg_csr *B,
                       tsg_csr *C, tsg_stats *stats);
 
+/* ---- plans: symbolic once, numeric many times ----------------------------- */
+
+/*
+ * The reference recomputes everything for every product (stepall_cuda_new
+ * runs its four steps per call, main_spgemm-col.cu:4529-4747).  A plan keeps
+ * the result of the symbolic phase -- A's and B's structure, C's tile
+ * structure, row masks, row pointer and numeric bins -- resident on the
+ * device, so products that repeat a pattern with new values run only the
+ * numeric step.
+ *
+ * tsg_plan_create: symbolic phase of op(A, B) (A's and B's values are not
+ *   needed; device operands are copied, so the caller may free them).
+ * tsg_plan_execute: C = op(A, B) with new values: valA holds A's nnz values
+ *   in A's CSR order, valB B's (used for TSG_OP_AB only; for A*A and A*A^T
+ *   B's values come from valA).  `where` says whether the value arrays are
+ *   host or device memory.  C is returned like tsg_spgemm's.
+ * tsg_plan_nnz: nnz of C.  tsg_plan_device_bytes: device memory the plan holds.
+ */
+typedef struct tsg_plan tsg_plan;
+tsg_status tsg_plan_create(tsg_ctx *ctx, tsg_op op, const tsg_csr *A, const tsg_csr *B, tsg_plan **plan,
+                           tsg_stats *stats);
+tsg_status tsg_plan_execute(tsg_ctx *ctx, tsg_plan *plan, const double *valA, const double *valB, int32_t where,
+                            tsg_csr *C, tsg_stats *stats);
+int64_t tsg_plan_nnz(const tsg_plan *plan);
+int64_t tsg_plan_device_bytes(const tsg_plan *plan);
+tsg_status tsg_plan_destroy(tsg_ctx *ctx, tsg_plan *plan);
+
 /* ---- tile form (the reference's device format) --------------------------- */
 
 /*

@@ -1,0 +1,75 @@
+"""Numeric-only repeats through plans (tsg_plan_*): the same bits as a full
+SpGEMM with the new values, for A*A, A*A^T and A*B, host and device values."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def _newvals(A, seed):
+    rng = np.random.default_rng(seed)
+    return rng.uniform(-1.0, 1.0, A.nnz)
+
+
+def _with(A, vals):
+    from tilespgemm_gb300.api import CSR
+    return CSR(A.m, A.n, A.rowptr, A.col, vals)
+
+
+@pytest.mark.parametrize("op", ["AA", "AAT"])
+def test_plan_matches_full_call(ctx, op):
+    from tilespgemm_gb300 import matrices as M
+    A = M.random_sparse(1500, 1500, 9, seed=31) if op == "AA" else M.random_sparse(900, 1300, 8, seed=32)
+    plan = ctx.plan(A, op=op)
+    assert plan.nnz > 0 and plan.device_bytes > 0
+    for seed in range(3):
+        v = _newvals(A, seed)
+        Av = _with(A, v)
+        C1 = plan.execute(v)
+        C2 = ctx.spgemm(Av, op=op)
+        assert np.array_equal(C1.rowptr, C2.rowptr) and np.array_equal(C1.col, C2.col)
+        assert np.array_equal(C1.val, C2.val)
+        B = Av if op == "AA" else _with(A, v)  # structure of B built by the oracle below
+        if op == "AAT":
+            from tilespgemm_gb300.api import CSR
+            tp, tr, tv = O.transpose(Av)
+            B = CSR(A.n, A.m, tp, tr, tv)
+        rp, col, val = O.spgemm(Av, B)
+        assert np.array_equal(C1.val, val)
+    plan.close()
+
+
+def test_plan_ab_and_device_values(ctx):
+    import torch
+    from tilespgemm_gb300 import matrices as M
+    A = M.random_sparse(600, 800, 7, seed=33)
+    B = M.random_sparse(800, 500, 6, seed=34)
+    plan = ctx.plan(A, B, op="AB")
+    va, vb = _newvals(A, 5), _newvals(B, 6)
+    C1 = plan.execute(va, vb)
+    oc, _ = plan.execute_raw(torch.from_numpy(va).cuda(), torch.from_numpy(vb).cuda(), out="device")
+    C2 = oc.download()
+    oc.free()
+    rp, col, val = O.spgemm(_with(A, va), _with(B, vb))
+    for C in (C1, C2):
+        assert np.array_equal(np.asarray(C.rowptr, np.int64), rp) and np.array_equal(C.col, col)
+        assert np.array_equal(C.val, val)
+    plan.close()
+
+
+def test_plan_outlives_device_operands(ctx):
+    """A plan built from device tensors copies them: freeing them is safe."""
+    import torch
+    from tilespgemm_gb300 import matrices as M
+    A = M.stencil_27(10, seed=2)
+    Ad = A.to_device(0)
+    plan = ctx.plan(Ad, op="AA")
+    del Ad
+    torch.cuda.empty_cache()
+    v = _newvals(A, 9)
+    C = plan.execute(v)
+    rp, col, val = O.spgemm(_with(A, v), _with(A, v))
+    assert np.array_equal(C.col, col) and np.array_equal(C.val, val)
+    plan.close()

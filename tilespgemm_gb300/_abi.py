@@ -91,6 +91,13 @@ SIGNATURES = {
     "tsg_csr_free": (C.c_int, [C.c_void_p, C.POINTER(tsg_csr)]),
     "tsg_spgemm": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(tsg_csr), C.POINTER(tsg_csr),
                              C.POINTER(tsg_csr), C.POINTER(tsg_stats)]),
+    "tsg_plan_create": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(tsg_csr), C.POINTER(tsg_csr),
+                                  C.POINTER(C.c_void_p), C.POINTER(tsg_stats)]),
+    "tsg_plan_execute": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
+                                   C.POINTER(tsg_csr), C.POINTER(tsg_stats)]),
+    "tsg_plan_nnz": (C.c_int64, [C.c_void_p]),
+    "tsg_plan_device_bytes": (C.c_int64, [C.c_void_p]),
+    "tsg_plan_destroy": (C.c_int, [C.c_void_p, C.c_void_p]),
     "tsg_csr_to_tiles": (C.c_int, [C.c_void_p, C.POINTER(tsg_csr), C.POINTER(tsg_tiles)]),
     "tsg_spgemm_tiles": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(tsg_csr), C.POINTER(tsg_csr),
                                    C.POINTER(tsg_tiles), C.POINTER(tsg_stats)]),

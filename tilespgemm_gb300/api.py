@@ -174,6 +174,80 @@ def _download_tiles(ctx_handle, t: _abi.tsg_tiles) -> Tiles:
     return out
 
 
+class Plan:
+    """The symbolic phase of op(A, B) kept on the device (tsg_plan_*): later
+    products with the same patterns and new values run only the numeric step."""
+
+    def __init__(self, ctx: "Context", A: CSR, B: CSR | None, op: str):
+        a, keep_a = A._tsg()
+        b_ptr = None
+        keep_b: list = []
+        if B is not None:
+            b, keep_b = B._tsg()
+            b_ptr = C.byref(b)
+        h = C.c_void_p()
+        st = _abi.tsg_stats()
+        check(lib().tsg_plan_create(ctx.handle, _OPS[op], C.byref(a), b_ptr, C.byref(h), C.byref(st)))
+        del keep_a, keep_b
+        self._ctx, self.handle, self.op, self.stats = ctx, h, op, st.as_dict()
+        self.m, self.n = A.m, (B.n if B is not None else (A.n if op == "AA" else A.m))
+
+    @property
+    def nnz(self) -> int:
+        return int(lib().tsg_plan_nnz(self.handle))
+
+    @property
+    def device_bytes(self) -> int:
+        return int(lib().tsg_plan_device_bytes(self.handle))
+
+    def execute_raw(self, valA, valB=None, out: str = "host", stats: bool = False):
+        """C with new values (numpy arrays on the host, or torch CUDA tensors)."""
+        keep = []
+
+        def ptr(v):
+            if v is None:
+                return None, _abi.MEM_HOST
+            if hasattr(v, "is_cuda") and v.is_cuda:
+                import torch
+                v = v.contiguous()
+                keep.append(v)
+                torch.cuda.current_stream(v.device).synchronize()
+                return v.data_ptr(), _abi.MEM_DEVICE
+            a = np.ascontiguousarray(np.asarray(v), dtype=np.float64)
+            keep.append(a)
+            return (a.ctypes.data if a.size else None), _abi.MEM_HOST
+        pa, wa = ptr(valA)
+        pb, wb = ptr(valB)
+        where = wa if valA is not None else wb
+        if valB is not None and wb != where:
+            raise ValueError("valA and valB must both be host or both be device arrays")
+        c = _abi.tsg_csr()
+        c.where = _abi.MEM_DEVICE if out == "device" else _abi.MEM_HOST
+        st = _abi.tsg_stats() if stats else None
+        check(lib().tsg_plan_execute(self._ctx.handle, self.handle, pa, pb, where, C.byref(c),
+                                     C.byref(st) if st is not None else None))
+        del keep
+        return OwnedCSR(self._ctx, c), (st.as_dict() if st is not None else None)
+
+    def execute(self, valA, valB=None) -> CSR:
+        oc, _ = self.execute_raw(valA, valB, out="host")
+        res = oc.download()
+        oc.free()
+        return res
+
+    def close(self) -> None:
+        if self.handle:
+            lib().tsg_plan_destroy(self._ctx.handle, self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            if self._ctx.handle:
+                self.close()
+        except Exception:
+            pass
+
+
 class Context:
     """One device, one stream, one memory pool (tsg_create / tsg_destroy)."""
 
@@ -230,6 +304,10 @@ class Context:
         res = oc.download()
         oc.free()
         return (res, st) if stats else res
+
+    def plan(self, A: CSR, B: CSR | None = None, op: str = "AA") -> Plan:
+        """Symbolic phase of op(A, B), kept for numeric-only repeats."""
+        return Plan(self, A, B, op)
 
     def spgemm_tiles(self, A: CSR, B: CSR | None = None, op: str = "AA") -> Tiles:
         """C = op(A, B) in the reference's tile form (tsg_spgemm_tiles)."""
@@ -290,4 +368,4 @@ def version() -> str:
     return lib().tsg_version().decode()
 
 
-__all__ = ["CSR", "Context", "OwnedCSR", "Tiles", "TSGError", "load_mtx", "version"]
+__all__ = ["CSR", "Context", "OwnedCSR", "Plan", "Tiles", "TSGError", "load_mtx", "version"]

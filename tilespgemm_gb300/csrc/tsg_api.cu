@@ -30,9 +30,10 @@ cudaError_t prepare_csr(Pool &pool, const void *rp, int rp_bits, const int *col,
 cudaError_t csr_to_tile_structure(Pool &pool, const long long *rp, const int *col, TileCSR &T, bool masks,
                                   int *flags, int *stat_max);
 cudaError_t tile_symbolic(Pool &pool, const TileCSR &A, const TileCSR &B, long long *crp, int *ccol, int *cnt,
-                          int *flags, int *stat_max);
+                          int *wide, int *flags, int *stat, bool count_pass);
 cudaError_t csr_transpose(Pool &pool, const long long *rp, const int *col, const double *val, int m, int n,
-                          long long nnz, long long *tp, int *tcol, double *tval, int *flags);
+                          long long nnz, long long *tp, int *tcol, double *tval, int *perm, int *flags);
+cudaError_t aux_gather(Pool &pool, const int *perm, const double *src, double *dst, long long n);
 cudaError_t aux_nnzcub(Pool &pool, const long long *rpA, const int *colA, int m, const long long *rpB, int kB,
                        unsigned long long *out);
 cudaError_t aux_mask_popc(Pool &pool, const int *trp, int blkm, const uint16_t *mask, unsigned long long *out);
@@ -255,26 +256,48 @@ struct PhaseTimer {
     }
 };
 
-// The pipeline.  Produces C's CSR on the device (rowptr int64, col, val, all
-// owned by the caller of this function) plus C's tile structure when
-// `keep_tiles` is non-null.
-struct CTiles {
-    int blkm = 0;
-    long long numblk = 0;
+// Everything the numeric step needs for one op(A, B), produced by the
+// symbolic phase (conversion + steps 1-2).  A plan (tsg_plan) keeps one alive;
+// tsg_spgemm builds one, runs the numeric step once and drops it.
+struct PlanData {
+    tsg_op op = TSG_OP_AA;
+    int m = 0, k = 0, n = 0, blkm = 0;
+    long long nnzA = 0, nnzB = 0, numblkC = 0, nnzC = 0, nnzcub = 0, tilesA = 0, tilesB = 0;
+    long long *rpA = nullptr, *rpB = nullptr;      // int64 row pointers
+    const int *colA = nullptr, *colB = nullptr;
+    const double *valA = nullptr, *valB = nullptr; // values of the operands as staged
+    double *valA_buf = nullptr, *valB_buf = nullptr; // plan-owned value buffers for later executions
+    int *perm = nullptr;                           // A*A^T: B's entry q is A's entry perm[q]
     long long *crp = nullptr;
     int *ccol = nullptr;
     uint16_t *cmask = nullptr;
+    long long *rowptrC = nullptr;
+    unsigned char *bin = nullptr;
+    int *offC = nullptr;
+    long long counts[NBIN] = {}, req[NBIN] = {};
+    bool dupsafe = false;
+    int nsync = 0;
+    std::vector<void *> owned;
+    template <class T> T *own(Pool &pool, long long n) {
+        T *p = pool.alloc_n<T>(n);
+        if (p) owned.push_back(p);
+        return p;
+    }
+    void disown(void *p) {
+        for (auto &q : owned) if (q == p) q = nullptr;
+    }
+    void release(Pool &pool) {
+        for (void *p : owned) pool.free(p);
+        owned.clear();
+    }
+    long long device_bytes() const {
+        return 8ll * (m + 1) * 2 + 4ll * (nnzA + nnzB) + 8ll * (nnzA + nnzB) + 8ll * (blkm + 1) +
+               36ll * numblkC + 8ll * (m + 1) + (counts[BIN_GLOBAL] ? 64ll * numblkC : 0);
+    }
 };
 
-tsg_status run_pipeline(tsg_ctx *ctx, Pool &pool, Scratch &sc, tsg_op op, const tsg_csr *A, const tsg_csr *B,
-                        long long **rowptrC, int **colC, double **valC, long long *nnzC_out, int *mC, int *nC,
-                        tsg_stats *st, CTiles *keep_tiles)
+tsg_status check_op(tsg_op op, const tsg_csr *A, const tsg_csr *B)
 {
-    const bool validate = ctx->opts.validate != 0;
-    PhaseTimer tm(ctx, st && ctx->opts.phase_times);
-    int nsync = 0;
-    auto t_begin = std::chrono::steady_clock::now();
-
     tsg_status r = check_csr(A, "A");
     if (r) return r;
     if (op == TSG_OP_AB) {
@@ -286,30 +309,86 @@ tsg_status run_pipeline(tsg_ctx *ctx, Pool &pool, Scratch &sc, tsg_op op, const 
     } else if (op != TSG_OP_AAT) {
         return fail(TSG_ERR_INVALID_ARG, "unknown op %d", (int)op);
     }
+    return TSG_OK;
+}
 
+// Stage one operand into the plan: row pointer (int64, validated), columns
+// and values on the device.  Device operands are used in place unless
+// `copy` (a plan must not keep the caller's device buffers).
+tsg_status stage_into_plan(tsg_ctx *ctx, Pool &pool, PlanData &P, const tsg_csr *M, bool validate, bool copy,
+                           long long *&rp64, const int *&col, const double *&val, double *&valbuf)
+{
+    const size_t rpb = (size_t)(M->m + 1) * (M->rowptr_bits == 64 ? 8 : 4);
+    const void *rp = M->row_ptr;
+    const int *c = M->col;
+    const double *v = M->val;
+    valbuf = nullptr;
+    if (M->where == TSG_MEM_HOST || copy) {
+        const cudaMemcpyKind kind = M->where == TSG_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+        void *drp = P.own<char>(pool, (long long)rpb);
+        int *dcol = P.own<int>(pool, M->nnz);
+        double *dval = P.own<double>(pool, M->nnz);
+        if (!drp || !dcol || !dval) return fail(TSG_ERR_OOM, "device pool allocation failed for an operand");
+        CUDA_OK(cudaMemcpyAsync(drp, rp, rpb, kind, ctx->stream));
+        if (M->nnz > 0) {
+            CUDA_OK(cudaMemcpyAsync(dcol, c, sizeof(int) * (size_t)M->nnz, kind, ctx->stream));
+            if (v) CUDA_OK(cudaMemcpyAsync(dval, v, sizeof(double) * (size_t)M->nnz, kind, ctx->stream));
+        }
+        rp = drp; c = dcol; v = dval;
+        valbuf = dval;
+    }
+    rp64 = P.own<long long>(pool, M->m + 1);
+    if (!rp64) return fail(TSG_ERR_OOM, "device pool allocation failed");
+    CUDA_OK(prepare_csr(pool, rp, M->rowptr_bits, c, M->m, M->n, M->nnz, rp64, ctx->dflags, validate));
+    col = c;
+    val = v;
+    return TSG_OK;
+}
+
+// Symbolic phase: staging, A^T for A*A^T, tiles, step 1, step 2 (two host waits).
+// `keep` = the plan outlives the call (device operands are copied).
+tsg_status plan_symbolic(tsg_ctx *ctx, Pool &pool, Scratch &sc, tsg_op op, const tsg_csr *A, const tsg_csr *B,
+                         PlanData &P, bool keep, bool want_cub, PhaseTimer &tm)
+{
+    const bool validate = ctx->opts.validate != 0;
+    tsg_status r = check_op(op, A, B);
+    if (r) return r;
     CUDA_OK(cudaMemsetAsync(ctx->dflags, 0, sizeof(int) * FLAG_COUNT, ctx->stream));
     CUDA_OK(cudaMemsetAsync(ctx->dstat, 0, sizeof(long long) * ST_SLOTS, ctx->stream));
     tm.mark();  // 0
-
-    DevCSR dA, dB;
-    r = stage_operand(ctx, pool, sc, A, validate, dA);
+    P.op = op;
+    P.m = A->m;
+    P.k = A->n;
+    P.nnzA = A->nnz;
+    r = stage_into_plan(ctx, pool, P, A, validate, keep, P.rpA, P.colA, P.valA, P.valA_buf);
     if (r) return r;
     if (op == TSG_OP_AB) {
-        r = stage_operand(ctx, pool, sc, B, validate, dB);
+        P.n = B->n;
+        P.nnzB = B->nnz;
+        r = stage_into_plan(ctx, pool, P, B, validate, keep, P.rpB, P.colB, P.valB, P.valB_buf);
         if (r) return r;
     } else if (op == TSG_OP_AA) {
-        dB = dA;
+        P.n = A->n;
+        P.nnzB = A->nnz;
+        P.rpB = P.rpA; P.colB = P.colA; P.valB = P.valA;
     } else {
-        dB.m = dA.n; dB.n = dA.m; dB.nnz = dA.nnz;
-        long long *tp = sc.get<long long>(dA.n + 1);
-        int *tc = sc.get<int>(dA.nnz);
-        double *tv = sc.get<double>(dA.nnz);
-        if (!tp || !tc || !tv) return fail(TSG_ERR_OOM, "device pool allocation failed for A^T");
-        CUDA_OK(csr_transpose(pool, dA.rp, dA.col, dA.val, dA.m, dA.n, dA.nnz, tp, tc, tv, ctx->dflags));
-        dB.rp = tp; dB.col = tc; dB.val = tv;
+        P.n = A->m;
+        P.nnzB = A->nnz;
+        long long *tp = P.own<long long>(pool, P.k + 1);
+        int *tc = P.own<int>(pool, P.nnzA);
+        double *tv = P.own<double>(pool, P.nnzA);
+        P.perm = P.own<int>(pool, P.nnzA);
+        if (!tp || !tc || !tv || !P.perm) return fail(TSG_ERR_OOM, "device pool allocation failed for A^T");
+        CUDA_OK(csr_transpose(pool, P.rpA, P.colA, P.valA, P.m, P.k, P.nnzA, tp, tc, tv, P.perm, ctx->dflags));
+        P.rpB = tp; P.colB = tc; P.valB = tv; P.valB_buf = tv;
     }
-    const int m = dA.m, n = dB.n;
-    *mC = m; *nC = n;
+    if (keep && !P.valA_buf) {   // AA/AAT plans built from device operands still need a value buffer
+        P.valA_buf = P.own<double>(pool, P.nnzA);
+        if (!P.valA_buf) return fail(TSG_ERR_OOM, "device pool allocation failed");
+    }
+    DevCSR dA, dB;
+    dA.m = P.m; dA.n = P.k; dA.nnz = P.nnzA; dA.rp = P.rpA; dA.col = P.colA;
+    dB.m = P.k; dB.n = P.n; dB.nnz = P.nnzB; dB.rp = P.rpB; dB.col = P.colB;
 
     TileCSR TA, TB;
     r = build_tiles(pool, sc, dA, TA, ctx);
@@ -322,101 +401,160 @@ tsg_status run_pipeline(tsg_ctx *ctx, Pool &pool, Scratch &sc, tsg_op op, const 
     tm.mark();  // 1
 
     // step 1, count: C's tile-row pointer
-    const int blkm = TA.blkm;
-    long long *crp = sc.get<long long>(blkm + 1);
-    int *cnt = sc.get<int>(blkm + 1);
-    if (!crp || !cnt) return fail(TSG_ERR_OOM, "device pool allocation failed (step 1)");
-    CUDA_OK(tile_symbolic(pool, TA, TB, crp, nullptr, cnt, ctx->dflags, (int *)(ctx->dstat + ST_MAXS)));
-    CUDA_OK(aux_copy_scalars(pool, crp + blkm, ctx->dstat + ST_NUMBLKC, TA.trp + TA.blkm, ctx->dstat + ST_TILESA,
+    P.blkm = TA.blkm;
+    P.crp = P.own<long long>(pool, P.blkm + 1);
+    int *cnt = sc.get<int>(P.blkm + 1);
+    int *wide = sc.get<int>(P.blkm + 1);
+    if (!P.crp || !cnt || !wide) return fail(TSG_ERR_OOM, "device pool allocation failed (step 1)");
+    CUDA_OK(tile_symbolic(pool, TA, TB, P.crp, nullptr, cnt, wide, ctx->dflags, (int *)(ctx->dstat + ST_MAXS), true));
+    CUDA_OK(aux_copy_scalars(pool, P.crp + P.blkm, ctx->dstat + ST_NUMBLKC, TA.trp + TA.blkm, ctx->dstat + ST_TILESA,
                              TB.trp + TB.blkm, ctx->dstat + ST_TILESB));
     CUDA_OK(aux_mask_popc(pool, TB.trp, TB.blkm, TB.mask, (unsigned long long *)(ctx->dstat + ST_POPCB)));
-    if (st) CUDA_OK(aux_nnzcub(pool, dA.rp, dA.col, m, dB.rp, dB.m, (unsigned long long *)(ctx->dstat + ST_NNZCUB)));
-    r = host_wait(ctx, &nsync);
+    if (want_cub)
+        CUDA_OK(aux_nnzcub(pool, P.rpA, P.colA, P.m, P.rpB, P.k, (unsigned long long *)(ctx->dstat + ST_NNZCUB)));
+    r = host_wait(ctx, &P.nsync);
     if (r) return r;
-    const long long numblkC = ctx->hstat[ST_NUMBLKC];
-    const int maxS = (int)(ctx->hstat[ST_MAXS] & 0xffffffff);
-    const long long tilesA = ctx->hstat[ST_TILESA], tilesB = ctx->hstat[ST_TILESB];
-    const bool dupsafe = ctx->hstat[ST_POPCB] != dB.nnz;
-    const long long nnzcub = ctx->hstat[ST_NNZCUB];
-    if (numblkC >= (1ll << 31)) return fail(TSG_ERR_NOT_SUPPORTED, "C has %lld tiles; the limit is 2^31-1", numblkC);
+    P.numblkC = ctx->hstat[ST_NUMBLKC];
+    const int maxS = (int)(ctx->hstat[ST_MAXS] & 0xffffffff);        // stat[0]: max C tiles per tile-row
+    const int maxSpan = (int)(ctx->hstat[ST_MAXS] >> 32);              // stat[1]: max tile-column window
+    P.tilesA = ctx->hstat[ST_TILESA];
+    P.tilesB = ctx->hstat[ST_TILESB];
+    P.dupsafe = ctx->hstat[ST_POPCB] != P.nnzB;
+    P.nnzcub = ctx->hstat[ST_NNZCUB];
+    if (P.numblkC >= (1ll << 31)) return fail(TSG_ERR_NOT_SUPPORTED, "C has %lld tiles; the limit is 2^31-1", P.numblkC);
 
     // step 1, fill: C's sorted tile columns
-    int *ccol = keep_tiles ? pool.alloc_n<int>(numblkC) : sc.get<int>(numblkC);
-    uint16_t *cmask = keep_tiles ? pool.alloc_n<uint16_t>(numblkC * TILE + 2) : sc.get<uint16_t>(numblkC * TILE + 2);
-    if (keep_tiles) {
-        keep_tiles->ccol = ccol; keep_tiles->cmask = cmask;
-    }
-    if (!ccol || !cmask) return fail(TSG_ERR_OOM, "device pool allocation failed for C tiles");
-    CUDA_OK(tile_symbolic(pool, TA, TB, crp, ccol, cnt, ctx->dflags, nullptr));
+    P.ccol = P.own<int>(pool, P.numblkC);
+    P.cmask = P.own<uint16_t>(pool, P.numblkC * TILE + 2);
+    if (!P.ccol || !P.cmask) return fail(TSG_ERR_OOM, "device pool allocation failed for C tiles");
+    CUDA_OK(tile_symbolic(pool, TA, TB, P.crp, P.ccol, cnt, wide, ctx->dflags, nullptr, false));
     tm.mark();  // 2
 
     // step 2: masks, row counts, row pointer, bins
-    int *rowcnt = sc.get<int>(m + 1);
-    unsigned char *bin = sc.get<unsigned char>(blkm + 1);
-    long long *rowptr = pool.alloc_n<long long>(m + 1);
-    if (!rowcnt || !bin || !rowptr) { pool.free(rowptr); return fail(TSG_ERR_OOM, "device pool allocation failed (step 2)"); }
-    *rowptrC = rowptr;
+    int *rowcnt = sc.get<int>(P.m + 1);
+    P.bin = P.own<unsigned char>(pool, P.blkm + 1);
+    P.rowptrC = P.own<long long>(pool, P.m + 1);
+    if (!rowcnt || !P.bin || !P.rowptrC) return fail(TSG_ERR_OOM, "device pool allocation failed (step 2)");
     NumericBinParams bp{ctx->opts.dense_tile_min, ctx->opts.smem_acc_max};
-    CUDA_OK(step2_masks(pool, TA, TB, m, blkm, crp, ccol, cmask, rowcnt, maxS, bp, bin, ctx->dstat + ST_BINS,
-                        ctx->dflags));
-    CUDA_OK(scan_i32_to_i64(pool, rowcnt, rowptr, m, ctx->dflags));
-    CUDA_OK(cudaMemcpyAsync(ctx->dstat + ST_NNZC, rowptr + m, sizeof(long long), cudaMemcpyDeviceToDevice, ctx->stream));
-    r = host_wait(ctx, &nsync);
+    CUDA_OK(step2_masks(pool, TA, TB, P.m, P.blkm, P.crp, P.ccol, P.cmask, rowcnt, maxS, maxSpan, bp, P.bin,
+                        ctx->dstat + ST_BINS, ctx->dflags));
+    CUDA_OK(scan_i32_to_i64(pool, rowcnt, P.rowptrC, P.m, ctx->dflags));
+    CUDA_OK(cudaMemcpyAsync(ctx->dstat + ST_NNZC, P.rowptrC + P.m, sizeof(long long), cudaMemcpyDeviceToDevice,
+                            ctx->stream));
+    r = host_wait(ctx, &P.nsync);
     if (r) return r;
-    const long long nnzC = ctx->hstat[ST_NNZC];
-    long long counts[NBIN], req[NBIN];
-    for (int b = 0; b < NBIN; ++b) { counts[b] = ctx->hstat[ST_BINS + b]; req[b] = ctx->hstat[ST_BINS + NBIN + b]; }
+    P.nnzC = ctx->hstat[ST_NNZC];
+    for (int b = 0; b < NBIN; ++b) {
+        P.counts[b] = ctx->hstat[ST_BINS + b];
+        P.req[b] = ctx->hstat[ST_BINS + NBIN + b];
+    }
+    if (P.counts[BIN_GLOBAL] > 0) {
+        P.offC = P.own<int>(pool, P.numblkC * TILE);
+        if (!P.offC) return fail(TSG_ERR_OOM, "device pool allocation failed (global bin offsets)");
+    }
     tm.mark();  // 3
-
-    // step 3: numeric
-    int *col = pool.alloc_n<int>(nnzC);
-    double *val = pool.alloc_n<double>(nnzC);
-    *colC = col; *valC = val;
-    if (!col || !val) return fail(TSG_ERR_OOM, "device pool allocation failed for C (%lld entries)", nnzC);
-    NumericArgs na{};
-    na.m = m; na.blkm = blkm;
-    na.rpA = dA.rp; na.colA = dA.col; na.valA = dA.val;
-    na.rpB = dB.rp; na.colB = dB.col; na.valB = dB.val;
-    na.crp = crp; na.ccol = ccol; na.cmask = cmask;
-    na.rowptrC = rowptr; na.colC = col; na.valC = val;
-    na.bin = bin; na.flags = ctx->dflags;
-    if (counts[BIN_GLOBAL] > 0) {
-        na.offC = sc.get<int>(numblkC * TILE);
-        if (!na.offC) return fail(TSG_ERR_OOM, "device pool allocation failed (global bin offsets)");
-    }
-    CUDA_OK(numeric_run(pool, na, counts, req, dupsafe, ctx->opts.threads_numeric));
-    tm.mark();  // 4
-    *nnzC_out = nnzC;
-
-    if (keep_tiles) {
-        keep_tiles->blkm = blkm;
-        keep_tiles->numblk = numblkC;
-        keep_tiles->crp = crp;
-        // crp belongs to the scratch set; hand the caller its own copy
-        long long *crp2 = pool.alloc_n<long long>(blkm + 1);
-        if (!crp2) return fail(TSG_ERR_OOM, "device pool allocation failed");
-        CUDA_OK(cudaMemcpyAsync(crp2, crp, sizeof(long long) * (blkm + 1), cudaMemcpyDeviceToDevice, ctx->stream));
-        keep_tiles->crp = crp2;
-    }
-
-    if (st) {
-        st->nnz_a = dA.nnz; st->nnz_b = dB.nnz; st->nnz_c = nnzC;
-        st->nnz_cub = nnzcub;
-        st->tiles_a = tilesA; st->tiles_b = tilesB; st->tiles_c = numblkC;
-        st->n_syncs = nsync;
-        st->bins[0] = (int)counts[BIN_EMPTY];
-        st->bins[1] = (int)(counts[BIN_SPARSE_S] + counts[BIN_SPARSE_L]);
-        st->bins[2] = (int)(counts[BIN_DENSE_S] + counts[BIN_DENSE_L]);
-        st->bins[3] = (int)counts[BIN_GLOBAL];
-    }
-    (void)t_begin;
     return TSG_OK;
 }
 
-tsg_status finish_stats(tsg_ctx *ctx, tsg_stats *st, PhaseTimer *tm)
+// Numeric phase into caller-provided col/val (nnzC each).
+tsg_status plan_numeric(tsg_ctx *ctx, Pool &pool, PlanData &P, const double *valA, const double *valB, int *col,
+                        double *val)
 {
-    (void)ctx; (void)st; (void)tm;
+    NumericArgs na{};
+    na.m = P.m; na.blkm = P.blkm;
+    na.rpA = P.rpA; na.colA = P.colA; na.valA = valA;
+    na.rpB = P.rpB; na.colB = P.colB; na.valB = valB;
+    na.crp = P.crp; na.ccol = P.ccol; na.cmask = P.cmask;
+    na.rowptrC = P.rowptrC; na.colC = col; na.valC = val;
+    na.bin = P.bin; na.offC = P.offC; na.flags = ctx->dflags;
+    CUDA_OK(numeric_run(pool, na, P.counts, P.req, P.dupsafe, ctx->opts.threads_numeric));
     return TSG_OK;
+}
+
+void fill_stats(const PlanData &P, tsg_stats *st)
+{
+    if (!st) return;
+    st->nnz_a = P.nnzA; st->nnz_b = P.nnzB; st->nnz_c = P.nnzC;
+    st->nnz_cub = P.nnzcub;
+    st->tiles_a = P.tilesA; st->tiles_b = P.tilesB; st->tiles_c = P.numblkC;
+    st->n_syncs = P.nsync;
+    st->bins[0] = (int)P.counts[BIN_EMPTY];
+    st->bins[1] = (int)(P.counts[BIN_SPARSE_S] + P.counts[BIN_SPARSE_L]);
+    st->bins[2] = (int)(P.counts[BIN_DENSE_S] + P.counts[BIN_DENSE_L]);
+    st->bins[3] = (int)P.counts[BIN_GLOBAL];
+}
+
+// Hand C (rowptr copied/narrowed from `rowptr`, col/val adopted) to the
+// caller per C->where; frees col/val on failure.
+tsg_status emit_output(tsg_ctx *ctx, Pool &pool, int m, int n, long long nnzC, const long long *rowptr, int *col,
+                       double *val, tsg_csr *C, tsg_stats *st)
+{
+    int bits = ctx->opts.out_rowptr_bits;
+    if (bits == 0) bits = nnzC < (1ll << 31) ? 32 : 64;
+    if (bits == 32 && nnzC >= (1ll << 31)) {
+        pool.free(col); pool.free(val);
+        cudaStreamSynchronize(ctx->stream);
+        return fail(TSG_ERR_INT32_OVERFLOW, "C has %lld entries; int32 row pointers cannot hold them", nnzC);
+    }
+    OutOwner *o = new OutOwner();
+    o->ctx = ctx;
+    o->where = C->where;
+    C->m = m; C->n = n; C->nnz = nnzC; C->rowptr_bits = bits;
+    cudaError_t e = cudaSuccess;
+    void *rp_dev = nullptr;
+    if (bits == 32) {
+        int *rp32 = pool.alloc_n<int>(m + 1);
+        if (!rp32) e = cudaErrorMemoryAllocation;
+        else e = aux_rowptr_narrow(pool, rowptr, rp32, m + 1);
+        rp_dev = rp32;
+    } else {
+        long long *rp64 = pool.alloc_n<long long>(m + 1);
+        if (!rp64) e = cudaErrorMemoryAllocation;
+        else e = cudaMemcpyAsync(rp64, rowptr, sizeof(long long) * (size_t)(m + 1), cudaMemcpyDeviceToDevice, ctx->stream);
+        rp_dev = rp64;
+    }
+    if (C->where == TSG_MEM_DEVICE) {
+        o->blocks.push_back({rp_dev, 0});
+        o->blocks.push_back({col, 0});
+        o->blocks.push_back({val, 0});
+        C->row_ptr = rp_dev; C->col = col; C->val = val;
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    } else {
+        auto t_d2h = std::chrono::steady_clock::now();
+        const size_t rpb = (size_t)(m + 1) * (bits == 64 ? 8 : 4);
+        const size_t cb = sizeof(int) * (size_t)nnzC, vb = sizeof(double) * (size_t)nnzC;
+        void *hrp = pinned_get(ctx, rpb), *hcol = pinned_get(ctx, cb), *hval = pinned_get(ctx, vb);
+        if (!hrp || !hcol || !hval) e = cudaErrorMemoryAllocation;
+        if (e == cudaSuccess) e = cudaMemcpyAsync(hrp, rp_dev, rpb, cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess && nnzC > 0) e = cudaMemcpyAsync(hcol, col, cb, cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess && nnzC > 0) e = cudaMemcpyAsync(hval, val, vb, cudaMemcpyDeviceToHost, ctx->stream);
+        pool.free(rp_dev); pool.free(col); pool.free(val);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (hrp) o->blocks.push_back({hrp, rpb});
+        if (hcol) o->blocks.push_back({hcol, cb});
+        if (hval) o->blocks.push_back({hval, vb});
+        C->row_ptr = hrp; C->col = (int *)hcol; C->val = (double *)hval;
+        if (st) st->ms_d2h = ms_since(t_d2h);
+    }
+    C->owner = o;
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        tsg_csr_free(ctx, C);
+        cudaGetLastError();
+        return fail(e == cudaErrorMemoryAllocation ? TSG_ERR_OOM : TSG_ERR_CUDA, "output: %s", cudaGetErrorString(e));
+    }
+    return TSG_OK;
+}
+
+void phase_times(tsg_ctx *ctx, tsg_stats *st, const PhaseTimer &tm)
+{
+    if (!st || !tm.on || tm.n < 5) return;
+    float a = 0, b = 0, c1 = 0, d = 0;
+    cudaEventElapsedTime(&a, ctx->ev[0], ctx->ev[1]);
+    cudaEventElapsedTime(&b, ctx->ev[1], ctx->ev[2]);
+    cudaEventElapsedTime(&c1, ctx->ev[2], ctx->ev[3]);
+    cudaEventElapsedTime(&d, ctx->ev[3], ctx->ev[4]);
+    st->ms_convert = a; st->ms_step1 = b; st->ms_step2 = c1; st->ms_step3 = d;
 }
 
 }  // namespace
@@ -555,90 +693,148 @@ tsg_status tsg_spgemm(tsg_ctx *ctx, tsg_op op, const tsg_csr *A, const tsg_csr *
     CUDA_OK(cudaSetDevice(ctx->device));
     if (st) memset(st, 0, sizeof(*st));
     Pool pool{ctx->pool, ctx->stream};
-    long long *rowptr = nullptr;
+    PlanData P;
+    PhaseTimer tm(ctx, st && ctx->opts.phase_times);
     int *col = nullptr;
     double *val = nullptr;
-    long long nnzC = 0;
-    int m = 0, n = 0;
     tsg_status r;
     {
         Scratch sc(pool);
-        r = run_pipeline(ctx, pool, sc, op, A, B, &rowptr, &col, &val, &nnzC, &m, &n, st, nullptr);
+        r = plan_symbolic(ctx, pool, sc, op, A, B, P, false, st != nullptr, tm);
+        if (!r) {
+            col = pool.alloc_n<int>(P.nnzC);
+            val = pool.alloc_n<double>(P.nnzC);
+            if (!col || !val) r = fail(TSG_ERR_OOM, "device pool allocation failed for C (%lld entries)", P.nnzC);
+        }
+        if (!r) r = plan_numeric(ctx, pool, P, P.valA, P.valB, col, val);
+        tm.mark();  // 4
     }
-    auto release = [&]() { pool.free(rowptr); pool.free(col); pool.free(val); };
-    if (r) { release(); cudaStreamSynchronize(ctx->stream); cudaGetLastError(); return r; }
-
-    int bits = ctx->opts.out_rowptr_bits;
-    if (bits == 0) bits = nnzC < (1ll << 31) ? 32 : 64;
-    if (bits == 32 && nnzC >= (1ll << 31)) {
-        release();
+    if (r) {
+        pool.free(col); pool.free(val);
+        P.release(pool);
         cudaStreamSynchronize(ctx->stream);
-        return fail(TSG_ERR_INT32_OVERFLOW, "C has %lld entries; int32 row pointers cannot hold them", nnzC);
-    }
-    OutOwner *o = new OutOwner();
-    o->ctx = ctx;
-    o->where = C->where;
-    C->m = m; C->n = n; C->nnz = nnzC; C->rowptr_bits = bits;
-    cudaError_t e = cudaSuccess;
-    if (C->where == TSG_MEM_DEVICE) {
-        void *rp_out = rowptr;
-        if (bits == 32) {
-            int *rp32 = pool.alloc_n<int>(m + 1);
-            if (!rp32) e = cudaErrorMemoryAllocation;
-            else { e = aux_rowptr_narrow(pool, rowptr, rp32, m + 1); pool.free(rowptr); rowptr = nullptr; rp_out = rp32; }
-        }
-        o->blocks.push_back({rp_out, 0});
-        o->blocks.push_back({col, 0});
-        o->blocks.push_back({val, 0});
-        C->row_ptr = rp_out; C->col = col; C->val = val;
-        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
-    } else {
-        auto t_d2h = std::chrono::steady_clock::now();
-        const size_t rpb = (size_t)(m + 1) * (bits == 64 ? 8 : 4);
-        const size_t cb = sizeof(int) * (size_t)nnzC, vb = sizeof(double) * (size_t)nnzC;
-        void *hrp = pinned_get(ctx, rpb), *hcol = pinned_get(ctx, cb), *hval = pinned_get(ctx, vb);
-        if (!hrp || !hcol || !hval) e = cudaErrorMemoryAllocation;
-        void *src_rp = rowptr;
-        int *rp32 = nullptr;
-        if (e == cudaSuccess && bits == 32) {
-            rp32 = pool.alloc_n<int>(m + 1);
-            if (!rp32) e = cudaErrorMemoryAllocation;
-            else { e = aux_rowptr_narrow(pool, rowptr, rp32, m + 1); src_rp = rp32; }
-        }
-        if (e == cudaSuccess) e = cudaMemcpyAsync(hrp, src_rp, rpb, cudaMemcpyDeviceToHost, ctx->stream);
-        if (e == cudaSuccess && nnzC > 0) e = cudaMemcpyAsync(hcol, col, cb, cudaMemcpyDeviceToHost, ctx->stream);
-        if (e == cudaSuccess && nnzC > 0) e = cudaMemcpyAsync(hval, val, vb, cudaMemcpyDeviceToHost, ctx->stream);
-        pool.free(rp32);
-        release();
-        rowptr = nullptr; col = nullptr; val = nullptr;
-        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
-        if (hrp) o->blocks.push_back({hrp, rpb});
-        if (hcol) o->blocks.push_back({hcol, cb});
-        if (hval) o->blocks.push_back({hval, vb});
-        C->row_ptr = hrp; C->col = (int *)hcol; C->val = (double *)hval;
-        if (st) st->ms_d2h = ms_since(t_d2h);
-    }
-    C->owner = o;
-    if (e != cudaSuccess) {
-        tsg_csr_free(ctx, C);
         cudaGetLastError();
-        return fail(e == cudaErrorMemoryAllocation ? TSG_ERR_OOM : TSG_ERR_CUDA, "output: %s", cudaGetErrorString(e));
+        return r;
     }
-    // the final wait also surfaces errors of the numeric kernels
-    e = cudaGetLastError();
-    if (e != cudaSuccess) { tsg_csr_free(ctx, C); return fail(TSG_ERR_CUDA, "kernel: %s", cudaGetErrorString(e)); }
+    fill_stats(P, st);
+    r = emit_output(ctx, pool, P.m, P.n, P.nnzC, P.rowptrC, col, val, C, st);
+    P.release(pool);
+    if (r) return r;
     if (st) {
         st->ms_total = ms_since(t0);
-        if (ctx->opts.phase_times) {
-            float a = 0, b = 0, c1 = 0, d = 0;
-            cudaEventElapsedTime(&a, ctx->ev[0], ctx->ev[1]);
-            cudaEventElapsedTime(&b, ctx->ev[1], ctx->ev[2]);
-            cudaEventElapsedTime(&c1, ctx->ev[2], ctx->ev[3]);
-            cudaEventElapsedTime(&d, ctx->ev[3], ctx->ev[4]);
-            st->ms_convert = a; st->ms_step1 = b; st->ms_step2 = c1; st->ms_step3 = d;
-        }
-        st->n_syncs += 1;
+        phase_times(ctx, st, tm);
+        st->n_syncs = P.nsync + 1;
     }
+    return TSG_OK;
+}
+
+// ---- plans: symbolic once, numeric many times ------------------------------
+
+}  // extern "C"
+
+struct tsg_plan {
+    tsg_ctx *ctx = nullptr;
+    PlanData P;
+};
+
+extern "C" {
+
+tsg_status tsg_plan_create(tsg_ctx *ctx, tsg_op op, const tsg_csr *A, const tsg_csr *B, tsg_plan **plan,
+                           tsg_stats *st)
+{
+    if (!ctx || !plan) return fail(TSG_ERR_INVALID_ARG, "ctx/plan is NULL");
+    *plan = nullptr;
+    CUDA_OK(cudaSetDevice(ctx->device));
+    if (st) memset(st, 0, sizeof(*st));
+    auto t0 = std::chrono::steady_clock::now();
+    Pool pool{ctx->pool, ctx->stream};
+    tsg_plan *pl = new tsg_plan();
+    pl->ctx = ctx;
+    PhaseTimer tm(ctx, false);
+    tsg_status r;
+    {
+        Scratch sc(pool);
+        r = plan_symbolic(ctx, pool, sc, op, A, B, pl->P, true, true, tm);
+    }
+    if (r == TSG_OK && cudaStreamSynchronize(ctx->stream) != cudaSuccess) r = fail(TSG_ERR_CUDA, "plan build failed");
+    if (r) {
+        pl->P.release(pool);
+        cudaStreamSynchronize(ctx->stream);
+        cudaGetLastError();
+        delete pl;
+        return r;
+    }
+    fill_stats(pl->P, st);
+    if (st) st->ms_total = ms_since(t0);
+    *plan = pl;
+    return TSG_OK;
+}
+
+tsg_status tsg_plan_execute(tsg_ctx *ctx, tsg_plan *plan, const double *valA, const double *valB, int32_t where,
+                            tsg_csr *C, tsg_stats *st)
+{
+    if (!ctx || !plan || !C) return fail(TSG_ERR_INVALID_ARG, "ctx/plan/C is NULL");
+    if (plan->ctx != ctx) return fail(TSG_ERR_INVALID_ARG, "plan belongs to another context");
+    if (where != TSG_MEM_HOST && where != TSG_MEM_DEVICE) return fail(TSG_ERR_INVALID_ARG, "where is not a tsg_mem");
+    if (C->where != TSG_MEM_HOST && C->where != TSG_MEM_DEVICE) return fail(TSG_ERR_INVALID_ARG, "C->where is not a tsg_mem");
+    PlanData &P = plan->P;
+    if (P.nnzA > 0 && !valA) return fail(TSG_ERR_INVALID_ARG, "valA is NULL");
+    if (P.op == TSG_OP_AB && P.nnzB > 0 && !valB) return fail(TSG_ERR_INVALID_ARG, "valB is NULL for A*B");
+    auto t0 = std::chrono::steady_clock::now();
+    CUDA_OK(cudaSetDevice(ctx->device));
+    if (st) memset(st, 0, sizeof(*st));
+    Pool pool{ctx->pool, ctx->stream};
+    CUDA_OK(cudaMemsetAsync(ctx->dflags, 0, sizeof(int) * FLAG_COUNT, ctx->stream));
+    const double *va = valA, *vb = valB;
+    if (where == TSG_MEM_HOST && P.nnzA > 0) {
+        CUDA_OK(cudaMemcpyAsync(P.valA_buf, valA, sizeof(double) * (size_t)P.nnzA, cudaMemcpyHostToDevice, ctx->stream));
+        va = P.valA_buf;
+    }
+    if (P.op == TSG_OP_AB) {
+        if (where == TSG_MEM_HOST && P.nnzB > 0) {
+            CUDA_OK(cudaMemcpyAsync(P.valB_buf, valB, sizeof(double) * (size_t)P.nnzB, cudaMemcpyHostToDevice, ctx->stream));
+            vb = P.valB_buf;
+        }
+    } else if (P.op == TSG_OP_AA) {
+        vb = va;
+    } else {
+        CUDA_OK(aux_gather(pool, P.perm, va, P.valB_buf, P.nnzA));
+        vb = P.valB_buf;
+    }
+    int *col = pool.alloc_n<int>(P.nnzC);
+    double *val = pool.alloc_n<double>(P.nnzC);
+    if (!col || !val) {
+        pool.free(col); pool.free(val);
+        return fail(TSG_ERR_OOM, "device pool allocation failed for C (%lld entries)", P.nnzC);
+    }
+    tsg_status r = plan_numeric(ctx, pool, P, va, vb, col, val);
+    if (r) { pool.free(col); pool.free(val); cudaStreamSynchronize(ctx->stream); return r; }
+    fill_stats(P, st);
+    r = emit_output(ctx, pool, P.m, P.n, P.nnzC, P.rowptrC, col, val, C, st);
+    if (r) return r;
+    // numeric kernels report an internal bound failure through the flags
+    int hflags[FLAG_COUNT];
+    CUDA_OK(cudaMemcpy(hflags, ctx->dflags, sizeof(hflags), cudaMemcpyDeviceToHost));
+    if (hflags[FLAG_INTERNAL]) { tsg_csr_free(ctx, C); return fail(TSG_ERR_CUDA, "internal bound check failed on the device"); }
+    if (st) { st->ms_total = ms_since(t0); st->n_syncs = 1; }
+    return TSG_OK;
+}
+
+int64_t tsg_plan_nnz(const tsg_plan *plan) { return plan ? plan->P.nnzC : -1; }
+
+int64_t tsg_plan_device_bytes(const tsg_plan *plan) { return plan ? plan->P.device_bytes() : -1; }
+
+tsg_status tsg_plan_destroy(tsg_ctx *ctx, tsg_plan *plan)
+{
+    if (!plan) return TSG_OK;
+    tsg_ctx *c = plan->ctx ? plan->ctx : ctx;
+    if (c) {
+        cudaSetDevice(c->device);
+        Pool pool{c->pool, c->stream};
+        plan->P.release(pool);
+        cudaStreamSynchronize(c->stream);
+    }
+    delete plan;
     return TSG_OK;
 }
 
@@ -776,41 +972,46 @@ tsg_status tsg_spgemm_tiles(tsg_ctx *ctx, tsg_op op, const tsg_csr *A, const tsg
     memset(C, 0, sizeof(*C));
     if (st) memset(st, 0, sizeof(*st));
     Pool pool{ctx->pool, ctx->stream};
-    long long *rowptr = nullptr;
+    PlanData P;
+    PhaseTimer tm(ctx, false);
     int *col = nullptr;
     double *val = nullptr;
-    long long nnzC = 0;
-    int m = 0, n = 0;
-    CTiles ct;
     tsg_status r;
     {
         Scratch sc(pool);
-        r = run_pipeline(ctx, pool, sc, op, A, B, &rowptr, &col, &val, &nnzC, &m, &n, st, &ct);
+        r = plan_symbolic(ctx, pool, sc, op, A, B, P, false, st != nullptr, tm);
+        if (!r) {
+            col = pool.alloc_n<int>(P.nnzC);
+            val = pool.alloc_n<double>(P.nnzC);
+            if (!col || !val) r = fail(TSG_ERR_OOM, "device pool allocation failed for C (%lld entries)", P.nnzC);
+        }
+        if (!r) r = plan_numeric(ctx, pool, P, P.valA, P.valB, col, val);
     }
     TilesOwner *o = new TilesOwner();
     o->ctx = ctx;
     C->owner = o;
-    if (ct.crp) o->blocks.push_back(ct.crp);
-    if (ct.ccol) o->blocks.push_back(ct.ccol);
-    if (ct.cmask) o->blocks.push_back(ct.cmask);
     if (!r) {
-        const long long nb = ct.numblk;
-        C->m = m; C->n = n; C->blkm = ct.blkm; C->blkn = ceil_div_i(n, TILE); C->numblk = nb; C->nnz = nnzC;
-        C->blkrowptr = (int64_t *)ct.crp; C->blkcolidx = ct.ccol; C->mask = ct.cmask;
+        // hand C's tile structure over from the plan
+        for (void *p : {(void *)P.crp, (void *)P.ccol, (void *)P.cmask}) { P.disown(p); o->blocks.push_back(p); }
+        const long long nb = P.numblkC;
+        C->m = P.m; C->n = P.n; C->blkm = P.blkm; C->blkn = ceil_div_i(P.n, TILE); C->numblk = nb; C->nnz = P.nnzC;
+        C->blkrowptr = (int64_t *)P.crp; C->blkcolidx = P.ccol; C->mask = P.cmask;
         auto get = [&](size_t bytes) { void *p = pool.alloc(bytes); if (p) o->blocks.push_back(p); return p; };
         C->nnzb = (int64_t *)get(sizeof(int64_t) * (size_t)(nb + 1));
         C->ptr = (uint8_t *)get((size_t)(nb * TILE + 16));
-        C->col = (uint8_t *)get((size_t)(nnzC + 16));
-        C->val = (double *)get(sizeof(double) * (size_t)(nnzC + 1));
+        C->col = (uint8_t *)get((size_t)(P.nnzC + 16));
+        C->val = (double *)get(sizeof(double) * (size_t)(P.nnzC + 1));
         if (!C->nnzb || !C->ptr || !C->col || !C->val) r = fail(TSG_ERR_OOM, "device pool allocation failed for C tiles");
         if (!r) {
-            cudaError_t e = tiles_from_csr_c(pool, m, ct.blkm, nb, ct.crp, ct.ccol, ct.cmask, rowptr, col, val,
+            cudaError_t e = tiles_from_csr_c(pool, P.m, P.blkm, nb, P.crp, P.ccol, P.cmask, P.rowptrC, col, val,
                                              (long long *)C->nnzb, C->ptr, C->col, C->val, ctx->dflags);
             if (e != cudaSuccess) r = fail(TSG_ERR_CUDA, "tile payload of C: %s", cudaGetErrorString(e));
         }
         if (!r) r = host_wait(ctx, nullptr);
+        fill_stats(P, st);
     }
-    pool.free(rowptr); pool.free(col); pool.free(val);
+    pool.free(col); pool.free(val);
+    P.release(pool);
     if (r) { tsg_tiles_free(ctx, C); cudaGetLastError(); }
     else cudaStreamSynchronize(ctx->stream);
     return r;

@@ -240,6 +240,12 @@ __global__ void __launch_bounds__(256) k_fp64_peak(double *out, int iters, doubl
     out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
 }
 
+__global__ void k_gather(const int *__restrict__ perm, const double *__restrict__ src, double *dst, long long n)
+{
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x)
+        dst[q] = src[perm[q]];
+}
+
 inline unsigned g256(long long n) {
     long long g = (n + 255) / 256;
     if (g < 1) g = 1;
@@ -294,6 +300,13 @@ cudaError_t aux_copy_scalars(Pool &pool, const long long *a, long long *da, cons
                              const int *c, long long *dc)
 {
     { k_copy_scalars<<<1, 32, 0, pool.stream>>>(a, da, b, db, c, dc); ::tsg::count_launch(); }
+    return cudaGetLastError();
+}
+
+cudaError_t aux_gather(Pool &pool, const int *perm, const double *src, double *dst, long long n)
+{
+    if (n <= 0) return cudaSuccess;
+    { k_gather<<<g256(n), 256, 0, pool.stream>>>(perm, src, dst, n); ::tsg::count_launch(); }
     return cudaGetLastError();
 }
 

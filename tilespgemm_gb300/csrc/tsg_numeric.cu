@@ -46,8 +46,22 @@ __device__ __forceinline__ int lower_bound_dev(const int *a, int n, int key) {
     return lo;
 }
 
-// row-segment offset within the row for C tile s, local row r is packed in
-// the top 16 bits of word[s*16+r], the row mask in the low 16 bits
+// dense accumulators: 16 doubles per (row, tile) padded to 17, so lanes on
+// different tiles with the same local column use different banks
+constexpr int DPAD = 17;
+
+// word[r*S + s] packs, for C tile s and local row r, the offset of the
+// tile's row segment inside the tile-row's CSR segment (top 16 bits) and the
+// row mask (low 16 bits)
+// Bank swizzles.  The accumulator index p is permuted inside aligned groups
+// of 16 (p ^ ((p >> 4) & 15)): regular column strides (stencils put a B
+// row's outputs 16 apart) would otherwise land on one bank.  The map index
+// is permuted inside groups of 64 halfwords for the same reason (tile
+// columns of neighbouring planes sit 2^k apart).  Both are bijections that
+// keep the index inside its group, so the arrays are rounded up to 16 / 64.
+__device__ __forceinline__ int acc_swz(int p) { return p ^ ((p >> 4) & 15); }
+__device__ __forceinline__ unsigned map_swz(unsigned o) { return o ^ (((o >> 6) & 31u) << 1); }
+
 __device__ __forceinline__ int rank_in_row(unsigned w, int c) {
     return (int)(w >> 16) + __popc((w & 0xffffu) >> (TILE - c));
 }
@@ -57,12 +71,76 @@ __device__ __forceinline__ int slot_of(int j, int jbase, int span, bool use_map,
                                        const int *scol, int S) {
     const unsigned off = (unsigned)(j - jbase);
     if (off >= (unsigned)span) return -1;
-    const int s = use_map ? (int)map[off] : lower_bound_dev(scol, S, j);
+    if (use_map) {
+        const int s = (int)map[map_swz(off)];          // 0xffff marks a column with no C tile
+        return s < S ? s : -1;
+    }
+    const int s = lower_bound_dev(scol, S, j);
     return (s < S && scol[s] == j) ? s : -1;
 }
 
+struct TileRowSmem {
+    const int *scol;
+    const unsigned *word;
+    const unsigned short *map;
+    double *acc;
+    int S, jbase, span, nacc;
+};
+
+template <bool DENSE, bool MAP>
+__device__ __forceinline__ int out_pos(const TileRowSmem &t, const unsigned *wrow, int r, int col) {
+    const unsigned off = (unsigned)((col >> 4) - t.jbase);
+    if (off >= (unsigned)t.span) return -1;
+    int s;
+    if (MAP) {
+        s = (int)t.map[map_swz(off)];          // 0xffff marks a column with no C tile
+        if (s >= t.S) return -1;
+    } else {
+        s = lower_bound_dev(t.scol, t.S, col >> 4);
+        if (s >= t.S || t.scol[s] != (col >> 4)) return -1;
+    }
+    const int p = DENSE ? (r * t.S + s) * DPAD + (col & 15) : acc_swz(rank_in_row(wrow[s], col & 15));
+    return (unsigned)p < (unsigned)t.nacc ? p : -1;
+}
+
+// One C row: the warp walks A's row in order; for each A entry its lanes
+// take the B row's entries (distinct columns, so distinct outputs).
+template <bool DENSE, bool MAP>
+__device__ __forceinline__ void numeric_row(const NumericArgs &g, const TileRowSmem &t, int r0, int r, int lane)
+{
+    const int R = r0 + r;
+    const unsigned *wrow = t.word + r * t.S;
+    const int pa0 = (int)g.rpA[R], pa1 = (int)g.rpA[R + 1];
+    double *acc = t.acc;
+    bool bad = false;
+    for (int pb = pa0; pb < pa1; pb += 32) {
+        const int na = min(32, pa1 - pb);
+        int bs = 0, be = 0;
+        double av = 0.0;
+        if (lane < na) {
+            const int k = g.colA[pb + lane];
+            av = g.valA[pb + lane];
+            bs = (int)g.rpB[k];
+            be = (int)g.rpB[k + 1];
+        }
+        for (int q = 0; q < na; ++q) {
+            const double a = __shfl_sync(0xffffffffu, av, q);
+            const int b0 = __shfl_sync(0xffffffffu, bs, q);
+            const int b1 = __shfl_sync(0xffffffffu, be, q);
+            for (int e = b0 + lane; e < b1; e += 32) {
+                const int col = g.colB[e];
+                const double b = g.valB[e];
+                const int pos = out_pos<DENSE, MAP>(t, wrow, r, col);
+                if (pos < 0) { bad = true; continue; }
+                acc[pos] = fma(a, b, acc[pos]);
+            }
+        }
+    }
+    if (bad) set_flag(g.flags, FLAG_INTERNAL);
+}
+
 template <int NT, bool DENSE, bool DUPSAFE>
-__global__ void __launch_bounds__(NT, 1024 / NT)
+__global__ void __launch_bounds__(NT, 2048 / NT)
 k_numeric_smem(NumericArgs g, int mybin)
 {
     constexpr int NWARP = NT / 32;
@@ -84,14 +162,21 @@ k_numeric_smem(NumericArgs g, int mybin)
     unsigned *word = reinterpret_cast<unsigned *>(s_raw + align16((long long)S * 4));
     unsigned short *map = reinterpret_cast<unsigned short *>(s_raw + align16((long long)S * 4) + align16((long long)S * TILE * 4));
     double *acc = reinterpret_cast<double *>(s_raw + align16((long long)S * 4) + align16((long long)S * TILE * 4) +
-                                             (use_map ? align16((long long)span * 2) : 0));
+                                             (use_map ? map_bytes(span) : 0));
 
+    if (use_map) {
+        const int span64 = (span + 63) & ~63;
+        for (int t = tid; t < span64; t += NT) map[t] = 0xffffu;
+        __syncthreads();
+    }
     for (int s = tid; s < S; s += NT) {
         int j = g.ccol[c0 + s];
         scol[s] = j;
-        if (use_map) map[j - jbase] = (unsigned short)s;
+        if (use_map) map[map_swz((unsigned)(j - jbase))] = (unsigned short)s;
     }
-    // packed words: per row, exclusive scan of popc over the tile-row's tiles
+    // packed words, row-major (word[r*S + s]) so that lanes on different
+    // tiles of one row hit different banks: per row, exclusive scan of popc
+    // over the tile-row's tiles
     for (int r = warp; r < TILE; r += NWARP) {
         int run = (r < rows) ? (int)(g.rowptrC[r0 + r] - R0) : 0;
         for (int sb = 0; sb < S; sb += 32) {
@@ -99,46 +184,45 @@ k_numeric_smem(NumericArgs g, int mybin)
             unsigned mk = (s < S) ? (unsigned)g.cmask[(c0 + s) * TILE + r] : 0u;
             int c = __popc(mk);
             int incl = warp_incl_scan(c, lane);
-            if (s < S) word[s * TILE + r] = ((unsigned)(run + incl - c) << 16) | mk;
+            if (s < S) word[r * S + s] = ((unsigned)(run + incl - c) << 16) | mk;
             run += __shfl_sync(0xffffffffu, incl, 31);
         }
     }
-    const int nacc = DENSE ? S * 256 : nnz_tr;
+    const int nacc = DENSE ? S * TILE * DPAD : (nnz_tr + 15) & ~15;
     {
         unsigned long long *z = reinterpret_cast<unsigned long long *>(acc);
         for (int t = tid; t < nacc; t += NT) z[t] = 0ull;
     }
     __syncthreads();
 
-    for (int r = warp; r < rows; r += NWARP) {
-        const int R = r0 + r;
-        const int pa0 = (int)g.rpA[R], pa1 = (int)g.rpA[R + 1];
-        for (int pb = pa0; pb < pa1; pb += 32) {
-            const int na = min(32, pa1 - pb);
-            int bs = 0, be = 0;
-            double av = 0.0;
-            if (lane < na) {
-                const int k = g.colA[pb + lane];
-                av = g.valA[pb + lane];
-                bs = (int)g.rpB[k];
-                be = (int)g.rpB[k + 1];
-            }
-            for (int t = 0; t < na; ++t) {
-                const double a = __shfl_sync(0xffffffffu, av, t);
-                const int b0 = __shfl_sync(0xffffffffu, bs, t);
-                const int b1 = __shfl_sync(0xffffffffu, be, t);
-                if (!DUPSAFE) {
-                    for (int e = b0 + lane; e < b1; e += 32) {
-                        const int col = g.colB[e];
-                        const double b = g.valB[e];
-                        const int j = col >> 4, c = col & 15;
-                        const int s = slot_of(j, jbase, span, use_map, map, scol, S);
-                        int pos = -1;
-                        if (s >= 0) pos = DENSE ? s * 256 + r * TILE + c : rank_in_row(word[s * TILE + r], c);
-                        if ((unsigned)pos >= (unsigned)nacc) { set_flag(g.flags, FLAG_INTERNAL); continue; }
-                        acc[pos] = fma(a, b, acc[pos]);
-                    }
-                } else {
+    if (!DUPSAFE) {
+        // warp w owns rows w, w+NWARP, ...
+        TileRowSmem t{scol, word, map, acc, S, jbase, span, nacc};
+        for (int r = warp; r < rows; r += NWARP) {
+            if (use_map) numeric_row<DENSE, true>(g, t, r0, r, lane);
+            else numeric_row<DENSE, false>(g, t, r0, r, lane);
+        }
+    } else {
+        // B has rows with repeated columns: lanes that would update the same
+        // output are serialised in B's entry order
+        for (int r = warp; r < rows; r += NWARP) {
+            const int R = r0 + r;
+            const unsigned *wrow = word + r * S;
+            const int pa0 = (int)g.rpA[R], pa1 = (int)g.rpA[R + 1];
+            for (int pb = pa0; pb < pa1; pb += 32) {
+                const int na = min(32, pa1 - pb);
+                int bs = 0, be = 0;
+                double av = 0.0;
+                if (lane < na) {
+                    const int k = g.colA[pb + lane];
+                    av = g.valA[pb + lane];
+                    bs = (int)g.rpB[k];
+                    be = (int)g.rpB[k + 1];
+                }
+                for (int t = 0; t < na; ++t) {
+                    const double a = __shfl_sync(0xffffffffu, av, t);
+                    const int b0 = __shfl_sync(0xffffffffu, bs, t);
+                    const int b1 = __shfl_sync(0xffffffffu, be, t);
                     for (int eb = b0; eb < b1; eb += 32) {
                         const int e = eb + lane;
                         const bool ok = e < b1;
@@ -149,7 +233,7 @@ k_numeric_smem(NumericArgs g, int mybin)
                             const int j = col >> 4, c = col & 15;
                             const int s = slot_of(j, jbase, span, use_map, map, scol, S);
                             int pos = -1;
-                            if (s >= 0) pos = DENSE ? s * 256 + r * TILE + c : rank_in_row(word[s * TILE + r], c);
+                            if (s >= 0) pos = DENSE ? (r * S + s) * DPAD + c : acc_swz(rank_in_row(wrow[s], c));
                             const bool okpos = (unsigned)pos < (unsigned)nacc;
                             if (!okpos) { set_flag(g.flags, FLAG_INTERNAL); pos = -1 - lane; }
                             const unsigned peers = __match_any_sync(act, pos);
@@ -169,22 +253,22 @@ k_numeric_smem(NumericArgs g, int mybin)
 
     // epilogue: values (coalesced for the sparse layout) and column indices
     if (!DENSE) {
-        for (int p = tid; p < nnz_tr; p += NT) g.valC[R0 + p] = acc[p];
+        for (int p = tid; p < nnz_tr; p += NT) g.valC[R0 + p] = acc[acc_swz(p)];
     }
-    for (int t = tid; t < S * TILE; t += NT) {
-        const int s = t / TILE, r = t - s * TILE;
-        if (r >= rows) continue;
-        const unsigned w = word[t];
-        unsigned mk = w & 0xffffu;
-        long long dst = R0 + (w >> 16);
-        const int jb = scol[s] * TILE;
-        while (mk) {
-            const int b = 31 - __clz(mk);   // highest bit = smallest local column
-            const int c = TILE - 1 - b;
-            g.colC[dst] = jb + c;
-            if (DENSE) g.valC[dst] = acc[s * 256 + r * TILE + c];
-            ++dst;
-            mk &= ~(1u << b);
+    for (int r = warp; r < rows; r += NWARP) {
+        for (int s = lane; s < S; s += 32) {
+            const unsigned w = word[r * S + s];
+            unsigned mk = w & 0xffffu;
+            long long dst = R0 + (w >> 16);
+            const int jb = scol[s] * TILE;
+            while (mk) {
+                const int b = 31 - __clz(mk);   // highest bit = smallest local column
+                const int c = TILE - 1 - b;
+                g.colC[dst] = jb + c;
+                if (DENSE) g.valC[dst] = acc[(r * S + s) * DPAD + c];
+                ++dst;
+                mk &= ~(1u << b);
+            }
         }
     }
 }
@@ -230,7 +314,7 @@ k_global_prep(NumericArgs g)
 
 // one warp per C row of a global-bin tile-row; accumulates in place
 template <bool DUPSAFE>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 4)
 k_numeric_global(NumericArgs g)
 {
     const int R = blockIdx.x * 8 + (threadIdx.x >> 5);
@@ -289,8 +373,14 @@ k_numeric_global(NumericArgs g)
 
 template <int NT, bool DENSE, bool DUPSAFE>
 cudaError_t set_smem_attr() {
-    return cudaFuncSetAttribute(k_numeric_smem<NT, DENSE, DUPSAFE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)SMEM_LARGE);
+    cudaError_t e = cudaFuncSetAttribute(k_numeric_smem<NT, DENSE, DUPSAFE>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_LARGE);
+    // the whole unified L1 as shared memory, so occupancy is set by the
+    // tile-row's actual request, not by a smaller carveout
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_numeric_smem<NT, DENSE, DUPSAFE>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 (int)cudaSharedmemCarveoutMaxShared);
+    return e;
 }
 
 template <int NT>

@@ -29,14 +29,18 @@ struct NumericBinParams {
 
 __host__ __device__ inline long long align16(long long x) { return (x + 15) & ~15ll; }
 
+// bytes of the tile-column -> slot map (uint16 entries, window rounded up to
+// the 64-entry swizzle groups)
+__host__ __device__ inline long long map_bytes(long long span) { return align16(((span + 63) & ~63ll) * 2); }
+
 // Shared-memory layout of a tile-row in the numeric kernels:
 //   int   scol[S]       C tile columns
 //   u32   word[S*16]    (offset of the tile's row segment inside the tile-row << 16) | row mask
-//   u16   map[span]     tile column - scol[0] -> slot (only when span <= MAP_MAX)
-//   f64   acc[...]      nnz_tr entries (sparse) or S*256 (dense)
+//   u16   map[span64]   tile column - scol[0] -> slot, swizzled (only when span <= MAP_MAX)
+//   f64   acc[...]      nnz_tr entries rounded to 16, swizzled (sparse) or S*16*17 (dense, rows padded to 17)
 __host__ __device__ inline long long numeric_smem_bytes(long long S, long long nnz_tr, long long span, bool dense) {
-    long long b = align16(S * 4) + align16(S * TILE * 4) + (span <= MAP_MAX ? align16(span * 2) : 0);
-    return b + (dense ? S * 256 * 8 : nnz_tr * 8);
+    long long b = align16(S * 4) + align16(S * TILE * 4) + (span <= MAP_MAX ? map_bytes(span) : 0);
+    return b + (dense ? S * TILE * 17 * 8 : ((nnz_tr + 15) & ~15ll) * 8);
 }
 
 __host__ __device__ inline void numeric_classify(const NumericBinParams &bp, long long S, long long nnz_tr, long long span,
@@ -68,7 +72,7 @@ struct NumericArgs {
 };
 
 cudaError_t step2_masks(Pool &pool, const TileCSR &A, const TileCSR &B, int m, int blkm, const long long *crp,
-                        const int *ccol, uint16_t *cmask, int *rowcnt, int max_tiles_per_row,
+                        const int *ccol, uint16_t *cmask, int *rowcnt, int max_tiles_per_row, int max_span,
                         const NumericBinParams &bp, unsigned char *bin, long long *binstat, int *flags);
 
 // Launch the numeric kernels of every non-empty bin.  counts/req are the

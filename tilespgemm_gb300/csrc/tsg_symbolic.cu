@@ -46,19 +46,34 @@ __device__ __forceinline__ unsigned or_rows(unsigned ma, const uint16_t *__restr
     return acc;
 }
 
+constexpr int STG = 64;   // B tiles staged per warp at a time
+
+// slot of tile column j in C's tile-row: direct map over the row's window
+// when it is narrow, binary search otherwise; -1 if j is not one of its tiles
+__device__ __forceinline__ int c_slot(int j, int jbase, int span, const unsigned short *map, const int *scol, int S) {
+    const unsigned off = (unsigned)(j - jbase);
+    if (off >= (unsigned)span) return -1;
+    const int s = map ? (int)map[off] : lower_bound_i(scol, S, j);
+    return (s < S && scol[s] == j) ? s : -1;
+}
+
 // GLOBAL = false: masks accumulate in shared memory (tile-rows with at most
 // `smax` tiles); GLOBAL = true: in cmask with global atomics (the rest).
+// Work split: a warp takes one A tile (i,k) at a time and its lanes the B
+// tiles of B's tile-row k.  The A tile is transposed once (16 ballots give,
+// for every local column c, the set of rows that use it); then for each c,
+// uniformly across the warp, every lane ORs its B tile's row c into the
+// rows of that set -- one shared atomicOr per A entry and B tile, no search,
+// no per-element branching on the B side.
 template <bool GLOBAL>
 __global__ void __launch_bounds__(S2_THREADS)
 k_step2(int blkm, int m, const int *__restrict__ arp, const int *__restrict__ acol,
         const uint16_t *__restrict__ amask, const int *__restrict__ brp, const int *__restrict__ bcol,
         const uint16_t *__restrict__ bmask, const long long *__restrict__ crp, const int *__restrict__ ccol,
-        uint16_t *cmask, int *rowcnt, int smax, NumericBinParams bp, unsigned char *bin,
+        uint16_t *cmask, int *rowcnt, int smax, int map_cap, NumericBinParams bp, unsigned char *bin,
         long long *binstat, int *flags)
 {
-    extern __shared__ unsigned s_dyn[];
-    __shared__ int s_rows[S2_WARPS][TILE];
-    __shared__ unsigned s_rmask[S2_WARPS][TILE];
+    extern __shared__ __align__(16) unsigned char s_raw[];
     __shared__ long long s_rowtot[TILE];
     const int i = blockIdx.x;
     if (i >= blkm) return;
@@ -66,12 +81,22 @@ k_step2(int blkm, int m, const int *__restrict__ arp, const int *__restrict__ ac
     const int S = (int)(crp[i + 1] - c0);
     if (GLOBAL ? (S <= smax) : (S > smax)) return;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    unsigned *smask = s_dyn;                                   // S*16 (shared path)
-    const int *scol = GLOBAL ? (ccol + c0) : reinterpret_cast<const int *>(s_dyn + S * TILE);
+    const int jbase = S > 0 ? ccol[c0] : 0;
+    const int span = S > 0 ? ccol[c0 + S - 1] - jbase + 1 : 0;
+    unsigned *smask = reinterpret_cast<unsigned *>(s_raw);                        // [16][S] (shared path)
+    int *wcol = reinterpret_cast<int *>(s_raw + (GLOBAL ? 0 : align16((long long)S * TILE * 4)));
+    unsigned short *map = nullptr;
+    if (!GLOBAL && span <= map_cap)
+        map = reinterpret_cast<unsigned short *>(s_raw + align16((long long)S * TILE * 4) + align16((long long)S * 4));
+    const int *scol = GLOBAL ? (ccol + c0) : wcol;
     if (!GLOBAL) {
-        int *wcol = reinterpret_cast<int *>(s_dyn + S * TILE);
         for (int t = tid; t < S * TILE; t += S2_THREADS) smask[t] = 0u;
         for (int t = tid; t < S; t += S2_THREADS) wcol[t] = ccol[c0 + t];
+        if (map) {
+            for (int t = tid; t < span; t += S2_THREADS) map[t] = 0xffffu;
+            __syncthreads();
+            for (int t = tid; t < S; t += S2_THREADS) map[ccol[c0 + t] - jbase] = (unsigned short)t;
+        }
     } else {
         unsigned *mw = reinterpret_cast<unsigned *>(cmask) + c0 * 8;
         for (long long t = tid; t < (long long)S * 8; t += S2_THREADS) mw[t] = 0u;
@@ -80,49 +105,60 @@ k_step2(int blkm, int m, const int *__restrict__ arp, const int *__restrict__ ac
     __syncthreads();
 
     const int a0 = arp[i], a1 = arp[i + 1];
+    bool bad = false;
     for (int a = a0 + warp; a < a1; a += S2_WARPS) {
         const int kt = acol[a];
         const int q0 = brp[kt], nq = brp[kt + 1] - q0;
-        // compact the nonzero rows of A tile a
-        unsigned ma = (lane < TILE) ? amask[(long long)a * TILE + lane] : 0u;
-        unsigned nzr = __ballot_sync(0xffffffffu, ma != 0u);
-        if (ma) {
-            int pos = __popc(nzr & lanemask_lt());
-            s_rows[warp][pos] = lane;
-            s_rmask[warp][pos] = ma;
-        }
-        __syncwarp();
-        const int nrow = __popc(nzr);
-        const int total = nrow * nq;
-        for (int idx = lane; idx < total; idx += 32) {
-            const int t = idx / nq;
-            const long long q = q0 + (idx - t * nq);
-            const int r = s_rows[warp][t];
-            unsigned acc = or_rows(s_rmask[warp][t], bmask, q);
-            if (acc) {
-                const int key = bcol[q];
-                const int s = lower_bound_i(scol, S, key);
-                if (s >= S || scol[s] != key) { set_flag(flags, FLAG_INTERNAL); continue; }
-                if (GLOBAL) atomic_or_mask16(cmask, (c0 + s) * TILE + r, acc);
-                else atomicOr(&smask[s * TILE + r], acc);
+        // transpose the A tile: colrows[c] = rows r whose mask has local column c
+        const unsigned ma = (lane < TILE) ? (unsigned)amask[(long long)a * TILE + lane] : 0u;
+        unsigned colrows[TILE];
+#pragma unroll
+        for (int c = 0; c < TILE; ++c) colrows[c] = __ballot_sync(0xffffffffu, (ma >> (TILE - 1 - c)) & 1u) & 0xffffu;
+        for (int qb = 0; qb < nq; qb += 32) {
+            const int q = qb + lane;
+            const bool ok = q < nq;
+            uint4 blo = make_uint4(0, 0, 0, 0), bhi = make_uint4(0, 0, 0, 0);
+            int sl = -1;
+            if (ok) {
+                const uint4 *bq = reinterpret_cast<const uint4 *>(bmask + (long long)(q0 + q) * TILE);
+                blo = bq[0];
+                bhi = bq[1];
+                sl = c_slot(bcol[q0 + q], jbase, span, map, scol, S);
+                if (sl < 0) bad = true;
+            }
+            const unsigned bw[8] = {blo.x, blo.y, blo.z, blo.w, bhi.x, bhi.y, bhi.z, bhi.w};
+#pragma unroll
+            for (int c = 0; c < TILE; ++c) {
+                unsigned rowsc = colrows[c];
+                if (rowsc == 0u) continue;                       // uniform across the warp
+                const unsigned brow = (bw[c >> 1] >> ((c & 1) * 16)) & 0xffffu;   // B tile row c
+                if (sl < 0 || brow == 0u) continue;
+                while (rowsc) {
+                    const int r = __ffs(rowsc) - 1;
+                    if (GLOBAL) atomic_or_mask16(cmask, (c0 + sl) * TILE + r, brow);
+                    else atomicOr(&smask[r * S + sl], brow);
+                    rowsc &= rowsc - 1;
+                }
             }
         }
-        __syncwarp();
     }
+    if (bad) set_flag(flags, FLAG_INTERNAL);
     __syncthreads();
     if (GLOBAL) __threadfence();
 
     const int rows = min(TILE, m - i * TILE);
-    // write masks (shared path) and count rows
     if (!GLOBAL) {
+        // smask is row-major ([r][s]); cmask is tile-major (16 rows per tile)
         unsigned *mw = reinterpret_cast<unsigned *>(cmask) + c0 * 8;
-        for (int t = tid; t < S * 8; t += S2_THREADS)
-            mw[t] = (smask[2 * t] & 0xffffu) | (smask[2 * t + 1] << 16);
+        for (int t = tid; t < S * 8; t += S2_THREADS) {
+            const int sl = t >> 3, r = (t & 7) * 2;
+            mw[t] = (smask[r * S + sl] & 0xffffu) | (smask[(r + 1) * S + sl] << 16);
+        }
     }
     for (int r = warp; r < TILE; r += S2_WARPS) {
         int c = 0;
         for (int s = lane; s < S; s += 32) {
-            unsigned mk = GLOBAL ? (unsigned)__ldcg(cmask + (c0 + s) * TILE + r) : smask[s * TILE + r];
+            unsigned mk = GLOBAL ? (unsigned)__ldcg(cmask + (c0 + s) * TILE + r) : smask[r * S + s];
             c += __popc(mk & 0xffffu);
         }
         c = warp_sum_int(c);
@@ -135,7 +171,6 @@ k_step2(int blkm, int m, const int *__restrict__ arp, const int *__restrict__ ac
     if (tid == 0) {
         long long nnz_tr = 0;
         for (int r = 0; r < TILE; ++r) nnz_tr += s_rowtot[r];
-        const long long span = S > 0 ? (long long)scol[S - 1] - scol[0] + 1 : 0;
         int b;
         long long req = 0;
         numeric_classify(bp, S, nnz_tr, span, b, req);
@@ -147,26 +182,32 @@ k_step2(int blkm, int m, const int *__restrict__ arp, const int *__restrict__ ac
 
 }  // namespace
 
+constexpr int S2_SMAX = 2048;   // tiles per tile-row handled with shared-memory masks
+
 cudaError_t symbolic_init_attributes()
 {
-    return cudaFuncSetAttribute(k_step2<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 2048 * (TILE * 4 + 4) + 16);
+    cudaError_t e = cudaFuncSetAttribute(k_step2<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)(align16(S2_SMAX * TILE * 4) + align16(S2_SMAX * 4) + align16(MAP_MAX * 2)));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_step2<false>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 (int)cudaSharedmemCarveoutMaxShared);
+    return e;
 }
 
 cudaError_t step2_masks(Pool &pool, const TileCSR &A, const TileCSR &B, int m, int blkm, const long long *crp,
-                        const int *ccol, uint16_t *cmask, int *rowcnt, int max_tiles_per_row,
+                        const int *ccol, uint16_t *cmask, int *rowcnt, int max_tiles_per_row, int max_span,
                         const NumericBinParams &bp, unsigned char *bin, long long *binstat, int *flags)
 {
     cudaStream_t s = pool.stream;
     if (blkm <= 0) return cudaSuccess;
-    // shared path: up to `smax` tiles per tile-row, (16*4 + 4) bytes per tile
-    const int smax = 2048;
-    const int s_used = max_tiles_per_row < smax ? max_tiles_per_row : smax;
-    const size_t smem = (size_t)s_used * (TILE * 4 + 4) + 16;
+    const int s_used = max_tiles_per_row < S2_SMAX ? max_tiles_per_row : S2_SMAX;
+    const int map_cap = max_span < (int)MAP_MAX ? max_span : (int)MAP_MAX;
+    const size_t smem = (size_t)(align16((long long)s_used * TILE * 4) + align16((long long)s_used * 4) + align16((long long)map_cap * 2));
     { k_step2<false><<<blkm, S2_THREADS, smem, s>>>(blkm, m, A.trp, A.tcol, A.mask, B.trp, B.tcol, B.mask, crp, ccol,
-                                                   cmask, rowcnt, smax, bp, bin, binstat, flags); ::tsg::count_launch(); }
-    if (max_tiles_per_row > smax)
+                                                   cmask, rowcnt, S2_SMAX, map_cap, bp, bin, binstat, flags); ::tsg::count_launch(); }
+    if (max_tiles_per_row > S2_SMAX)
         { k_step2<true><<<blkm, S2_THREADS, 0, s>>>(blkm, m, A.trp, A.tcol, A.mask, B.trp, B.tcol, B.mask, crp, ccol,
-                                                   cmask, rowcnt, smax, bp, bin, binstat, flags); ::tsg::count_launch(); }
+                                                   cmask, rowcnt, S2_SMAX, 0, bp, bin, binstat, flags); ::tsg::count_launch(); }
     return cudaGetLastError();
 }
 

@@ -79,7 +79,7 @@ struct UnionKeys {
 
 template <class KS>
 __global__ void __launch_bounds__(WPC * 32)
-k_union_count(typename KS::Params P, int nrows, int *cnt, int *wide_list, int *wide_n, int *stat_max)
+k_union_count(typename KS::Params P, int nrows, int *cnt, int *wide_list, int *wide_n, int *stat)
 {
     __shared__ unsigned s_bm[WPC][NW];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -92,6 +92,7 @@ k_union_count(typename KS::Params P, int nrows, int *cnt, int *wide_list, int *w
     kmax = warp_max_int(kmax);
     if (kmax < kmin) { if (lane == 0) cnt[row] = 0; return; }
     const long long span = (long long)kmax - kmin + 1;
+    if (stat && lane == 0) atomicMax(stat + 1, (int)span);
     if (span > NW * 32) {
         if (lane == 0) { cnt[row] = 0; wide_list[atomicAdd(wide_n, 1)] = row; }
         return;
@@ -110,7 +111,7 @@ k_union_count(typename KS::Params P, int nrows, int *cnt, int *wide_list, int *w
     c = warp_sum_int(c);
     if (lane == 0) {
         cnt[row] = c;
-        if (stat_max) atomicMax(stat_max, c);
+        if (stat) atomicMax(stat, c);
     }
 }
 
@@ -294,8 +295,7 @@ k_union_wide(typename KS::Params P, const int *wide_list, const int *wide_n, int
         }
         if (!FILL && tid == 0) {
             cnt[row] = (int)run;
-            if ((long long)(int)run != run) set_flag(stat_max, 0);  // cannot happen for int keys
-            if (stat_max) atomicMax(stat_max, (int)run);
+            if (stat_max) { atomicMax(stat_max, (int)run); atomicMax(stat_max + 1, kmax - kmin + 1); }
         }
         __syncthreads();
     }
@@ -446,25 +446,30 @@ inline unsigned grid_for(long long n, int threads, long long cap = 152ll * 32) {
     return (unsigned)g;
 }
 
+// Count (+ scan into rowptr_out) and/or fill.  `wide` (nrows+1 ints: the
+// list of rows too wide for one warp, then its length) is written by the
+// count pass and read by the fill pass, so the two may be separate calls.
 template <class KS, typename TP>
-cudaError_t union_structure(Pool &pool, typename KS::Params P, int nrows, int *cnt_scratch,
-                            TP *rowptr_out, int *out_cols, uint16_t *mask, int *flags, int *stat_max,
-                            cudaError_t (*scan)(Pool &, const int *, TP *, long long, int *))
+cudaError_t union_structure(Pool &pool, typename KS::Params P, int nrows, int *cnt_scratch, int *wide,
+                            TP *rowptr_out, int *out_cols, uint16_t *mask, int *flags, int *stat,
+                            cudaError_t (*scan)(Pool &, const int *, TP *, long long, int *),
+                            bool do_count, bool do_fill)
 {
     cudaStream_t s = pool.stream;
-    int *wide = pool.alloc_n<int>(nrows + 1);
-    if (!wide) return pool.err;
     int *wide_n = wide + nrows;
-    cudaError_t e = cudaMemsetAsync(wide_n, 0, sizeof(int), s);
-    if (e != cudaSuccess) { pool.free(wide); return e; }
+    cudaError_t e = cudaSuccess;
     const unsigned g = (unsigned)((nrows + WPC - 1) / WPC);
-    if (nrows > 0) {
-        { k_union_count<KS><<<g, WPC * 32, 0, s>>>(P, nrows, cnt_scratch, wide, wide_n, stat_max); ::tsg::count_launch(); }
-        { k_union_wide<KS, false, false, TP><<<304, WIDE_THREADS, WIDE_SMEM, s>>>(
-            P, wide, wide_n, cnt_scratch, stat_max, nullptr, nullptr, nullptr); ::tsg::count_launch(); }
+    if (do_count) {
+        e = cudaMemsetAsync(wide_n, 0, sizeof(int), s);
+        if (e != cudaSuccess) return e;
+        if (nrows > 0) {
+            { k_union_count<KS><<<g, WPC * 32, 0, s>>>(P, nrows, cnt_scratch, wide, wide_n, stat); ::tsg::count_launch(); }
+            { k_union_wide<KS, false, false, TP><<<304, WIDE_THREADS, WIDE_SMEM, s>>>(
+                P, wide, wide_n, cnt_scratch, stat, nullptr, nullptr, nullptr); ::tsg::count_launch(); }
+        }
+        e = scan(pool, cnt_scratch, rowptr_out, nrows, flags);
     }
-    e = scan(pool, cnt_scratch, rowptr_out, nrows, flags);
-    if (e == cudaSuccess && nrows > 0 && out_cols) {
+    if (e == cudaSuccess && do_fill && nrows > 0 && out_cols) {
         if (mask) {
             { k_union_fill<KS, true, TP><<<g, WPC * 32, 0, s>>>(P, nrows, rowptr_out, out_cols, mask); ::tsg::count_launch(); }
             { k_union_wide<KS, true, true, TP><<<304, WIDE_THREADS, WIDE_SMEM, s>>>(
@@ -476,7 +481,6 @@ cudaError_t union_structure(Pool &pool, typename KS::Params P, int nrows, int *c
         }
     }
     if (e == cudaSuccess) e = cudaGetLastError();
-    pool.free(wide);
     return e;
 }
 
@@ -514,30 +518,35 @@ cudaError_t prepare_csr(Pool &pool, const void *rp, int rp_bits, const int *col,
 // T.trp/tcol/mask must be allocated by the caller (tcol, mask with an upper
 // bound of the tile count: min(nnz, blkm*blkn)).
 cudaError_t csr_to_tile_structure(Pool &pool, const long long *rp, const int *col, TileCSR &T, bool masks,
-                                  int *flags, int *stat_max)
+                                  int *flags, int *stat)
 {
     int *cnt = pool.alloc_n<int>(T.blkm + 1);
-    if (!cnt) return pool.err;
+    int *wide = pool.alloc_n<int>(T.blkm + 1);
+    cudaError_t e = (cnt && wide) ? cudaSuccess : pool.err;
     CsrKeys::Params P{rp, col, T.m, T.n};
-    cudaError_t e = union_structure<CsrKeys, int>(pool, P, T.blkm, cnt, T.trp, T.tcol, masks ? T.mask : nullptr,
-                                                  flags, stat_max, scan_i32_to_i32);
+    if (e == cudaSuccess)
+        e = union_structure<CsrKeys, int>(pool, P, T.blkm, cnt, wide, T.trp, T.tcol, masks ? T.mask : nullptr,
+                                          flags, stat, scan_i32_to_i32, true, true);
     pool.free(cnt);
+    pool.free(wide);
     return e;
 }
 
-// Step 1: C's tile-row pointer (crp, int64) and, when ccol != nullptr, the
-// sorted tile columns.  Call once with ccol == nullptr to size C.
+// Step 1: C's tile-row pointer (crp, int64; count pass) and C's sorted tile
+// columns (fill pass, ccol).  cnt and wide (blkm+1 ints each) carry state
+// from the count pass to the fill pass; stat[0] gets the largest tile count
+// of a tile-row and stat[1] the widest tile-column window.
 cudaError_t tile_symbolic(Pool &pool, const TileCSR &A, const TileCSR &B, long long *crp, int *ccol, int *cnt,
-                          int *flags, int *stat_max)
+                          int *wide, int *flags, int *stat, bool count_pass)
 {
     UnionKeys::Params P{A.trp, A.tcol, B.trp, B.tcol};
-    return union_structure<UnionKeys, long long>(pool, P, A.blkm, cnt, crp, ccol, nullptr, flags, stat_max,
-                                                 scan_i32_to_i64);
+    return union_structure<UnionKeys, long long>(pool, P, A.blkm, cnt, wide, crp, ccol, nullptr, flags, stat,
+                                                 scan_i32_to_i64, count_pass, !count_pass);
 }
 
 // Stable CSR transpose: (tp, tcol, tval) = CSR of A^T (n x m).
 cudaError_t csr_transpose(Pool &pool, const long long *rp, const int *col, const double *val, int m, int n,
-                          long long nnz, long long *tp, int *tcol, double *tval, int *flags)
+                          long long nnz, long long *tp, int *tcol, double *tval, int *perm, int *flags)
 {
     cudaStream_t s = pool.stream;
     cudaError_t e = cudaSuccess;
@@ -580,6 +589,8 @@ cudaError_t csr_transpose(Pool &pool, const long long *rp, const int *col, const
             { k_gather_transposed<<<grid_for(nnz, 256), 256, 0, s>>>(v0, rowof, val, nnz, tcol, tval); ::tsg::count_launch(); }
             e = cudaGetLastError();
         }
+        if (e == cudaSuccess && perm)   // entry q of A^T is entry perm[q] of A
+            e = cudaMemcpyAsync(perm, v0, sizeof(int) * (size_t)nnz, cudaMemcpyDeviceToDevice, s);
     }
     pool.free(k0); pool.free(v0); pool.free(k1); pool.free(v1);
     pool.free(rowof); pool.free(counts); pool.free(len);
