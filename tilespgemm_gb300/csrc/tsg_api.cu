@@ -30,7 +30,7 @@ cudaError_t prepare_csr(Pool &pool, const void *rp, int rp_bits, const int *col,
 cudaError_t csr_to_tile_structure(Pool &pool, const long long *rp, const int *col, TileCSR &T, bool masks,
                                   int *flags, int *stat_max);
 cudaError_t tile_symbolic(Pool &pool, const TileCSR &A, const TileCSR &B, long long *crp, int *ccol, int *cnt,
-                          int *wide, int *flags, int *stat, bool count_pass);
+                          int *wide, int *flags, int *stat, bool count_pass, int *defer);
 cudaError_t csr_transpose(Pool &pool, const long long *rp, const int *col, const double *val, int m, int n,
                           long long nnz, long long *tp, int *tcol, double *tval, int *perm, int *flags);
 cudaError_t aux_gather(Pool &pool, const int *perm, const double *src, double *dst, long long n);
@@ -101,6 +101,7 @@ namespace {
 
 enum StatSlot {
     ST_NUMBLKC = 0, ST_MAXS = 1, ST_TILESA = 2, ST_TILESB = 3, ST_NNZCUB = 4, ST_POPCB = 5, ST_NNZC = 6,
+    ST_NDEFER = 7,               // tile-rows left to the CTA step-2 kernel
     ST_BINS = 8,                 // NBIN counts, then NBIN max shared-memory sizes
     ST_HFLAGS = 40,              // host mirror only: device flags
     ST_SLOTS = 64
@@ -405,8 +406,12 @@ tsg_status plan_symbolic(tsg_ctx *ctx, Pool &pool, Scratch &sc, tsg_op op, const
     P.crp = P.own<long long>(pool, P.blkm + 1);
     int *cnt = sc.get<int>(P.blkm + 1);
     int *wide = sc.get<int>(P.blkm + 1);
-    if (!P.crp || !cnt || !wide) return fail(TSG_ERR_OOM, "device pool allocation failed (step 1)");
-    CUDA_OK(tile_symbolic(pool, TA, TB, P.crp, nullptr, cnt, wide, ctx->dflags, (int *)(ctx->dstat + ST_MAXS), true));
+    int *defer = sc.get<int>(P.blkm + 1);
+    if (!P.crp || !cnt || !wide || !defer) return fail(TSG_ERR_OOM, "device pool allocation failed (step 1)");
+    CUDA_OK(cudaMemsetAsync(defer + P.blkm, 0, sizeof(int), ctx->stream));
+    CUDA_OK(tile_symbolic(pool, TA, TB, P.crp, nullptr, cnt, wide, ctx->dflags, (int *)(ctx->dstat + ST_MAXS), true,
+                          defer));
+    CUDA_OK(cudaMemcpyAsync(ctx->dstat + ST_NDEFER, defer + P.blkm, sizeof(int), cudaMemcpyDeviceToDevice, ctx->stream));
     CUDA_OK(aux_copy_scalars(pool, P.crp + P.blkm, ctx->dstat + ST_NUMBLKC, TA.trp + TA.blkm, ctx->dstat + ST_TILESA,
                              TB.trp + TB.blkm, ctx->dstat + ST_TILESB));
     CUDA_OK(aux_mask_popc(pool, TB.trp, TB.blkm, TB.mask, (unsigned long long *)(ctx->dstat + ST_POPCB)));
@@ -417,27 +422,28 @@ tsg_status plan_symbolic(tsg_ctx *ctx, Pool &pool, Scratch &sc, tsg_op op, const
     P.numblkC = ctx->hstat[ST_NUMBLKC];
     const int maxS = (int)(ctx->hstat[ST_MAXS] & 0xffffffff);        // stat[0]: max C tiles per tile-row
     const int maxSpan = (int)(ctx->hstat[ST_MAXS] >> 32);              // stat[1]: max tile-column window
+    const int ndefer = (int)(ctx->hstat[ST_NDEFER] & 0xffffffff);
     P.tilesA = ctx->hstat[ST_TILESA];
     P.tilesB = ctx->hstat[ST_TILESB];
     P.dupsafe = ctx->hstat[ST_POPCB] != P.nnzB;
     P.nnzcub = ctx->hstat[ST_NNZCUB];
     if (P.numblkC >= (1ll << 31)) return fail(TSG_ERR_NOT_SUPPORTED, "C has %lld tiles; the limit is 2^31-1", P.numblkC);
 
-    // step 1, fill: C's sorted tile columns
+    // step 1 fill + step 2: C's sorted tile columns, row masks, row counts,
+    // numeric bins (one warp per tile-row where it fits, CTA kernels for the rest)
     P.ccol = P.own<int>(pool, P.numblkC);
     P.cmask = P.own<uint16_t>(pool, P.numblkC * TILE + 2);
-    if (!P.ccol || !P.cmask) return fail(TSG_ERR_OOM, "device pool allocation failed for C tiles");
-    CUDA_OK(tile_symbolic(pool, TA, TB, P.crp, P.ccol, cnt, wide, ctx->dflags, nullptr, false));
-    tm.mark();  // 2
-
-    // step 2: masks, row counts, row pointer, bins
     int *rowcnt = sc.get<int>(P.m + 1);
     P.bin = P.own<unsigned char>(pool, P.blkm + 1);
     P.rowptrC = P.own<long long>(pool, P.m + 1);
-    if (!rowcnt || !P.bin || !P.rowptrC) return fail(TSG_ERR_OOM, "device pool allocation failed (step 2)");
+    if (!P.ccol || !P.cmask || !rowcnt || !P.bin || !P.rowptrC)
+        return fail(TSG_ERR_OOM, "device pool allocation failed for C tiles");
     NumericBinParams bp{ctx->opts.dense_tile_min, ctx->opts.smem_acc_max};
+    CUDA_OK(symbolic_fill_fused(pool, TA, TB, P.m, P.crp, P.ccol, P.cmask, rowcnt, P.bin, bp, ctx->dstat + ST_BINS,
+                                cnt, wide, ctx->dflags));
+    tm.mark();  // 2
     CUDA_OK(step2_masks(pool, TA, TB, P.m, P.blkm, P.crp, P.ccol, P.cmask, rowcnt, maxS, maxSpan, bp, P.bin,
-                        ctx->dstat + ST_BINS, ctx->dflags));
+                        ctx->dstat + ST_BINS, ctx->dflags, defer, ndefer));
     CUDA_OK(scan_i32_to_i64(pool, rowcnt, P.rowptrC, P.m, ctx->dflags));
     CUDA_OK(cudaMemcpyAsync(ctx->dstat + ST_NNZC, P.rowptrC + P.m, sizeof(long long), cudaMemcpyDeviceToDevice,
                             ctx->stream));
@@ -953,7 +959,7 @@ tsg_status tsg_csr_to_tiles(tsg_ctx *ctx, const tsg_csr *A, tsg_tiles *T)
             if (!r) {
                 { k_widen_i32<<<(unsigned)((TA.blkm + 1 + 255) / 256), 256, 0, ctx->stream>>>(TA.trp, (long long *)T->blkrowptr, TA.blkm + 1); ::tsg::count_launch(); }
                 cudaMemcpyAsync(T->blkcolidx, TA.tcol, sizeof(int) * (size_t)nb, cudaMemcpyDeviceToDevice, ctx->stream);
-                cudaMemcpyAsync(T->mask, TA.mask, sizeof(uint16_t) * (size_t)nb * TILE, cudaMemcpyDeviceToDevice, ctx->stream);
+                masks_to_tile_major_i32(pool, TA.blkm, TA.trp, TA.mask, T->mask);
                 cudaError_t e = tiles_payload_a(pool, dA.m, dA.n, dA.rp, dA.col, dA.val, TA, nb, (long long *)T->nnzb,
                                                 T->ptr, T->col, T->val, ctx->dflags);
                 if (e != cudaSuccess) r = fail(TSG_ERR_CUDA, "tile payload: %s", cudaGetErrorString(e));
@@ -992,16 +998,18 @@ tsg_status tsg_spgemm_tiles(tsg_ctx *ctx, tsg_op op, const tsg_csr *A, const tsg
     C->owner = o;
     if (!r) {
         // hand C's tile structure over from the plan
-        for (void *p : {(void *)P.crp, (void *)P.ccol, (void *)P.cmask}) { P.disown(p); o->blocks.push_back(p); }
+        for (void *p : {(void *)P.crp, (void *)P.ccol}) { P.disown(p); o->blocks.push_back(p); }
         const long long nb = P.numblkC;
         C->m = P.m; C->n = P.n; C->blkm = P.blkm; C->blkn = ceil_div_i(P.n, TILE); C->numblk = nb; C->nnz = P.nnzC;
-        C->blkrowptr = (int64_t *)P.crp; C->blkcolidx = P.ccol; C->mask = P.cmask;
+        C->blkrowptr = (int64_t *)P.crp; C->blkcolidx = P.ccol;
         auto get = [&](size_t bytes) { void *p = pool.alloc(bytes); if (p) o->blocks.push_back(p); return p; };
+        C->mask = (uint16_t *)get(sizeof(uint16_t) * (size_t)(nb * TILE + 2));
+        if (C->mask) masks_to_tile_major_i64(pool, P.blkm, P.crp, P.cmask, C->mask);
         C->nnzb = (int64_t *)get(sizeof(int64_t) * (size_t)(nb + 1));
         C->ptr = (uint8_t *)get((size_t)(nb * TILE + 16));
         C->col = (uint8_t *)get((size_t)(P.nnzC + 16));
         C->val = (double *)get(sizeof(double) * (size_t)(P.nnzC + 1));
-        if (!C->nnzb || !C->ptr || !C->col || !C->val) r = fail(TSG_ERR_OOM, "device pool allocation failed for C tiles");
+        if (!C->mask || !C->nnzb || !C->ptr || !C->col || !C->val) r = fail(TSG_ERR_OOM, "device pool allocation failed for C tiles");
         if (!r) {
             cudaError_t e = tiles_from_csr_c(pool, P.m, P.blkm, nb, P.crp, P.ccol, P.cmask, P.rowptrC, col, val,
                                              (long long *)C->nnzb, C->ptr, C->col, C->val, ctx->dflags);

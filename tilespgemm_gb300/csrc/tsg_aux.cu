@@ -67,12 +67,17 @@ __global__ void k_rowptr_narrow(const long long *in, int *out, long long n)
 
 // ---- C tiles from C's CSR ------------------------------------------------
 
-__global__ void k_tile_nnz_from_mask(const uint16_t *__restrict__ mask, long long numblk, int *tn)
+// per-tile nnz of C from its row-major masks (warp per tile-row)
+__global__ void k_tile_nnz_rm(int blkm, const long long *__restrict__ crp, const uint16_t *__restrict__ cmask, int *tn)
 {
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < numblk; t += (long long)gridDim.x * blockDim.x) {
-        const uint4 *q = reinterpret_cast<const uint4 *>(mask + t * TILE);
-        uint4 a = q[0], b = q[1];
-        tn[t] = __popc(a.x) + __popc(a.y) + __popc(a.z) + __popc(a.w) + __popc(b.x) + __popc(b.y) + __popc(b.z) + __popc(b.w);
+    const int i = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (i >= blkm) return;
+    const long long c0 = crp[i];
+    const int S = (int)(crp[i + 1] - c0);
+    for (int s = lane; s < S; s += 32) {
+        int c = 0;
+        for (int r = 0; r < TILE; ++r) c += __popc((unsigned)cmask[c0 * TILE + (long long)r * S + s]);
+        tn[c0 + s] = c;
     }
 }
 
@@ -87,12 +92,13 @@ k_tile_payload_c(int m, const long long *__restrict__ crp, const int *__restrict
     const int r0 = i * TILE, rows = min(TILE, m - r0);
     const long long c0 = crp[i];
     const int S = (int)(crp[i + 1] - c0);
+    const uint16_t *mk_rm = cmask + c0 * TILE;     // row r of tile s at mk_rm[r*S + s]
     // row starts inside each tile
     for (int s = threadIdx.x; s < S; s += blockDim.x) {
         int run = 0;
         for (int r = 0; r < TILE; ++r) {
             ptr[(c0 + s) * TILE + r] = (uint8_t)run;
-            run += __popc((unsigned)cmask[(c0 + s) * TILE + r]);
+            run += __popc((unsigned)mk_rm[r * S + s]);
         }
     }
     for (int r = warp; r < rows; r += 8) {
@@ -100,12 +106,12 @@ k_tile_payload_c(int m, const long long *__restrict__ crp, const int *__restrict
         int run = 0;
         for (int sb = 0; sb < S; sb += 32) {
             const int s = sb + lane;
-            unsigned mk = (s < S) ? (unsigned)cmask[(c0 + s) * TILE + r] : 0u;
+            unsigned mk = (s < S) ? (unsigned)mk_rm[r * S + s] : 0u;
             int c = __popc(mk);
             int incl = warp_incl_scan(c, lane);
             if (s < S && c) {
                 int before = 0;
-                for (int q = 0; q < r; ++q) before += __popc((unsigned)cmask[(c0 + s) * TILE + q]);
+                for (int q = 0; q < r; ++q) before += __popc((unsigned)mk_rm[q * S + s]);
                 const long long src = Rb + run + incl - c;
                 const long long dst = nnzb[c0 + s] + before;
                 for (int x = 0; x < c; ++x) {
@@ -323,7 +329,7 @@ cudaError_t tiles_from_csr_c(Pool &pool, int m, int blkm, long long numblk, cons
 {
     int *tn = pool.alloc_n<int>(numblk + 1);
     if (!tn) return pool.err;
-    if (numblk > 0) { k_tile_nnz_from_mask<<<g256(numblk), 256, 0, pool.stream>>>(cmask, numblk, tn); ::tsg::count_launch(); }
+    if (blkm > 0) { k_tile_nnz_rm<<<(unsigned)((blkm + 7) / 8), 256, 0, pool.stream>>>(blkm, crp, cmask, tn); ::tsg::count_launch(); }
     cudaError_t e = scan_i32_to_i64(pool, tn, nnzb, numblk, flags);
     if (e == cudaSuccess && blkm > 0)
         { k_tile_payload_c<<<blkm, 256, 0, pool.stream>>>(m, crp, ccol, cmask, rowptr, col, val, nnzb, ptr, lcol, tval); ::tsg::count_launch(); }

@@ -181,7 +181,7 @@ k_numeric_smem(NumericArgs g, int mybin)
         int run = (r < rows) ? (int)(g.rowptrC[r0 + r] - R0) : 0;
         for (int sb = 0; sb < S; sb += 32) {
             const int s = sb + lane;
-            unsigned mk = (s < S) ? (unsigned)g.cmask[(c0 + s) * TILE + r] : 0u;
+            unsigned mk = (s < S) ? (unsigned)g.cmask[c0 * TILE + (long long)r * S + s] : 0u;
             int c = __popc(mk);
             int incl = warp_incl_scan(c, lane);
             if (s < S) word[r * S + s] = ((unsigned)(run + incl - c) << 16) | mk;
@@ -291,7 +291,7 @@ k_global_prep(NumericArgs g)
         int run = 0;
         for (int sb = 0; sb < S; sb += 32) {
             const int s = sb + lane;
-            unsigned mk = (s < S) ? (unsigned)g.cmask[(c0 + s) * TILE + r] : 0u;
+            unsigned mk = (s < S) ? (unsigned)g.cmask[c0 * TILE + (long long)r * S + s] : 0u;
             int c = __popc(mk);
             int incl = warp_incl_scan(c, lane);
             if (s < S) {
@@ -352,7 +352,7 @@ k_numeric_global(NumericArgs g)
                     int s = lower_bound_dev(tc, S, j);
                     const bool found = s < S && tc[s] == j;
                     if (!found) { set_flag(g.flags, FLAG_INTERNAL); s = 0; }
-                    const unsigned mk = g.cmask[(c0 + s) * TILE + r];
+                    const unsigned mk = g.cmask[c0 * TILE + (long long)r * S + s];
                     const long long pos = Rb + g.offC[(c0 + s) * TILE + r] + __popc(mk >> (TILE - c));
                     if (!DUPSAFE) {
                         if (found) g.valC[pos] = fma(a, b, g.valC[pos]);

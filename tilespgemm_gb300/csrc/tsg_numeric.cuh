@@ -18,6 +18,15 @@ enum NumericBin : int {
     NBIN = 6
 };
 
+// C tile-rows whose masks the fused warp kernel builds (step 1 fill + step 2
+// in one warp): tile-column window at most FUSED_MAX_SPAN, at most
+// FUSED_MAX_TILES tiles.  The rest go to the CTA step-2 kernel.
+constexpr int FUSED_MAX_SPAN = 4096;
+constexpr int FUSED_MAX_TILES = 160;
+__host__ __device__ inline bool fused_handles(long long span, long long S) {
+    return span <= FUSED_MAX_SPAN && S <= FUSED_MAX_TILES;
+}
+
 constexpr long long SMEM_SMALL = 48 * 1024;
 constexpr long long SMEM_LARGE = 200 * 1024;
 constexpr long long MAP_MAX = 8192;   // direct tile-column -> slot map when the window is this narrow
@@ -73,12 +82,19 @@ struct NumericArgs {
 
 cudaError_t step2_masks(Pool &pool, const TileCSR &A, const TileCSR &B, int m, int blkm, const long long *crp,
                         const int *ccol, uint16_t *cmask, int *rowcnt, int max_tiles_per_row, int max_span,
-                        const NumericBinParams &bp, unsigned char *bin, long long *binstat, int *flags);
+                        const NumericBinParams &bp, unsigned char *bin, long long *binstat, int *flags,
+                        const int *defer_list, int ndefer);
 
 // Launch the numeric kernels of every non-empty bin.  counts/req are the
 // per-bin tile-row counts and maximum shared-memory sizes from step 2.
 cudaError_t numeric_run(Pool &pool, const NumericArgs &a, const long long *counts, const long long *req,
                         bool dupsafe, int threads);
+
+cudaError_t symbolic_fill_fused(Pool &pool, const TileCSR &A, const TileCSR &B, int m, const long long *crp,
+                                int *ccol, uint16_t *cmask, int *rowcnt, unsigned char *bin,
+                                const NumericBinParams &bp, long long *binstat, int *cnt, int *wide, int *flags);
+cudaError_t masks_to_tile_major_i32(Pool &pool, int blkm, const int *rowptr, const uint16_t *src, uint16_t *dst);
+cudaError_t masks_to_tile_major_i64(Pool &pool, int blkm, const long long *rowptr, const uint16_t *src, uint16_t *dst);
 
 cudaError_t symbolic_init_attributes();
 cudaError_t numeric_init_attributes();

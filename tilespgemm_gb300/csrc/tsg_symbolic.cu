@@ -71,11 +71,11 @@ k_step2(int blkm, int m, const int *__restrict__ arp, const int *__restrict__ ac
         const uint16_t *__restrict__ amask, const int *__restrict__ brp, const int *__restrict__ bcol,
         const uint16_t *__restrict__ bmask, const long long *__restrict__ crp, const int *__restrict__ ccol,
         uint16_t *cmask, int *rowcnt, int smax, int map_cap, NumericBinParams bp, unsigned char *bin,
-        long long *binstat, int *flags)
+        long long *binstat, int *flags, const int *__restrict__ rows_list)
 {
     extern __shared__ __align__(16) unsigned char s_raw[];
     __shared__ long long s_rowtot[TILE];
-    const int i = blockIdx.x;
+    const int i = rows_list[blockIdx.x];
     if (i >= blkm) return;
     const long long c0 = crp[i];
     const int S = (int)(crp[i + 1] - c0);
@@ -83,6 +83,7 @@ k_step2(int blkm, int m, const int *__restrict__ arp, const int *__restrict__ ac
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int jbase = S > 0 ? ccol[c0] : 0;
     const int span = S > 0 ? ccol[c0 + S - 1] - jbase + 1 : 0;
+    if (fused_handles(span, S)) return;     // done by the fused warp kernel
     unsigned *smask = reinterpret_cast<unsigned *>(s_raw);                        // [16][S] (shared path)
     int *wcol = reinterpret_cast<int *>(s_raw + (GLOBAL ? 0 : align16((long long)S * TILE * 4)));
     unsigned short *map = nullptr;
@@ -104,40 +105,38 @@ k_step2(int blkm, int m, const int *__restrict__ arp, const int *__restrict__ ac
     if (tid < TILE) s_rowtot[tid] = 0;
     __syncthreads();
 
-    const int a0 = arp[i], a1 = arp[i + 1];
+    const int a0 = arp[i], a1 = arp[i + 1], na = a1 - a0;
     bool bad = false;
     for (int a = a0 + warp; a < a1; a += S2_WARPS) {
         const int kt = acol[a];
         const int q0 = brp[kt], nq = brp[kt + 1] - q0;
         // transpose the A tile: colrows[c] = rows r whose mask has local column c
-        const unsigned ma = (lane < TILE) ? (unsigned)amask[(long long)a * TILE + lane] : 0u;
+        const unsigned ma = (lane < TILE) ? (unsigned)amask[(long long)a0 * TILE + (long long)lane * na + (a - a0)] : 0u;
         unsigned colrows[TILE];
 #pragma unroll
         for (int c = 0; c < TILE; ++c) colrows[c] = __ballot_sync(0xffffffffu, (ma >> (TILE - 1 - c)) & 1u) & 0xffffu;
         for (int qb = 0; qb < nq; qb += 32) {
             const int q = qb + lane;
             const bool ok = q < nq;
-            uint4 blo = make_uint4(0, 0, 0, 0), bhi = make_uint4(0, 0, 0, 0);
             int sl = -1;
             if (ok) {
-                const uint4 *bq = reinterpret_cast<const uint4 *>(bmask + (long long)(q0 + q) * TILE);
-                blo = bq[0];
-                bhi = bq[1];
                 sl = c_slot(bcol[q0 + q], jbase, span, map, scol, S);
                 if (sl < 0) bad = true;
             }
-            const unsigned bw[8] = {blo.x, blo.y, blo.z, blo.w, bhi.x, bhi.y, bhi.z, bhi.w};
+            const uint16_t *bq = bmask + (long long)q0 * TILE + q;   // row c of B tile q at bq[c*nq]
+            unsigned brow[TILE];
+#pragma unroll
+            for (int c = 0; c < TILE; ++c) brow[c] = (colrows[c] != 0u && sl >= 0) ? (unsigned)bq[c * nq] : 0u;
 #pragma unroll
             for (int c = 0; c < TILE; ++c) {
                 unsigned rowsc = colrows[c];
-                if (rowsc == 0u) continue;                       // uniform across the warp
-                const unsigned brow = (bw[c >> 1] >> ((c & 1) * 16)) & 0xffffu;   // B tile row c
-                if (sl < 0 || brow == 0u) continue;
+                const unsigned b = brow[c];
                 while (rowsc) {
                     const int r = __ffs(rowsc) - 1;
-                    if (GLOBAL) atomic_or_mask16(cmask, (c0 + sl) * TILE + r, brow);
-                    else atomicOr(&smask[r * S + sl], brow);
                     rowsc &= rowsc - 1;
+                    if (!b) continue;
+                    if (GLOBAL) atomic_or_mask16(cmask, c0 * TILE + (long long)r * S + sl, b);
+                    else atomicOr(&smask[r * S + sl], b);
                 }
             }
         }
@@ -148,17 +147,13 @@ k_step2(int blkm, int m, const int *__restrict__ arp, const int *__restrict__ ac
 
     const int rows = min(TILE, m - i * TILE);
     if (!GLOBAL) {
-        // smask is row-major ([r][s]); cmask is tile-major (16 rows per tile)
-        unsigned *mw = reinterpret_cast<unsigned *>(cmask) + c0 * 8;
-        for (int t = tid; t < S * 8; t += S2_THREADS) {
-            const int sl = t >> 3, r = (t & 7) * 2;
-            mw[t] = (smask[r * S + sl] & 0xffffu) | (smask[(r + 1) * S + sl] << 16);
-        }
+        // both smask and cmask are row-major ([r][s]) within the tile-row
+        for (int t = tid; t < S * TILE; t += S2_THREADS) cmask[c0 * TILE + t] = (uint16_t)smask[t];
     }
     for (int r = warp; r < TILE; r += S2_WARPS) {
         int c = 0;
         for (int s = lane; s < S; s += 32) {
-            unsigned mk = GLOBAL ? (unsigned)__ldcg(cmask + (c0 + s) * TILE + r) : smask[r * S + s];
+            unsigned mk = GLOBAL ? (unsigned)__ldcg(cmask + c0 * TILE + (long long)r * S + s) : smask[r * S + s];
             c += __popc(mk & 0xffffu);
         }
         c = warp_sum_int(c);
@@ -196,18 +191,19 @@ cudaError_t symbolic_init_attributes()
 
 cudaError_t step2_masks(Pool &pool, const TileCSR &A, const TileCSR &B, int m, int blkm, const long long *crp,
                         const int *ccol, uint16_t *cmask, int *rowcnt, int max_tiles_per_row, int max_span,
-                        const NumericBinParams &bp, unsigned char *bin, long long *binstat, int *flags)
+                        const NumericBinParams &bp, unsigned char *bin, long long *binstat, int *flags,
+                        const int *defer_list, int ndefer)
 {
     cudaStream_t s = pool.stream;
-    if (blkm <= 0) return cudaSuccess;
+    if (blkm <= 0 || ndefer <= 0) return cudaSuccess;
     const int s_used = max_tiles_per_row < S2_SMAX ? max_tiles_per_row : S2_SMAX;
     const int map_cap = max_span < (int)MAP_MAX ? max_span : (int)MAP_MAX;
     const size_t smem = (size_t)(align16((long long)s_used * TILE * 4) + align16((long long)s_used * 4) + align16((long long)map_cap * 2));
-    { k_step2<false><<<blkm, S2_THREADS, smem, s>>>(blkm, m, A.trp, A.tcol, A.mask, B.trp, B.tcol, B.mask, crp, ccol,
-                                                   cmask, rowcnt, S2_SMAX, map_cap, bp, bin, binstat, flags); ::tsg::count_launch(); }
+    { k_step2<false><<<ndefer, S2_THREADS, smem, s>>>(blkm, m, A.trp, A.tcol, A.mask, B.trp, B.tcol, B.mask, crp, ccol,
+                                                   cmask, rowcnt, S2_SMAX, map_cap, bp, bin, binstat, flags, defer_list); ::tsg::count_launch(); }
     if (max_tiles_per_row > S2_SMAX)
-        { k_step2<true><<<blkm, S2_THREADS, 0, s>>>(blkm, m, A.trp, A.tcol, A.mask, B.trp, B.tcol, B.mask, crp, ccol,
-                                                   cmask, rowcnt, S2_SMAX, 0, bp, bin, binstat, flags); ::tsg::count_launch(); }
+        { k_step2<true><<<ndefer, S2_THREADS, 0, s>>>(blkm, m, A.trp, A.tcol, A.mask, B.trp, B.tcol, B.mask, crp, ccol,
+                                                   cmask, rowcnt, S2_SMAX, 0, bp, bin, binstat, flags, defer_list); ::tsg::count_launch(); }
     return cudaGetLastError();
 }
 

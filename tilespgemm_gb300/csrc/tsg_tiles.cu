@@ -14,9 +14,16 @@
 // whose window exceeds 4096 keys go to a CTA-wide kernel that walks the
 // window in 262,144-key chunks (any width).
 //
+// Row masks are stored per tile-row in row-major order: the masks of the
+// tile-row whose tiles are t0..t1-1 occupy [16*t0, 16*t1), local row r of
+// tile t at 16*t0 + r*(t1-t0) + (t-t0), so lanes that walk a tile-row's
+// tiles read one row's masks contiguously.  (The reference's tile format,
+// 16 masks per tile, is produced only when a caller asks for tile form.)
+//
 // Roofline: HBM-bound; the conversion reads each CSR column index twice
 // (count pass, fill pass) and writes 36 bytes per tile.
 #include "tsg_internal.cuh"
+#include "tsg_numeric.cuh"
 #include <climits>
 
 namespace tsg {
@@ -79,7 +86,8 @@ struct UnionKeys {
 
 template <class KS>
 __global__ void __launch_bounds__(WPC * 32)
-k_union_count(typename KS::Params P, int nrows, int *cnt, int *wide_list, int *wide_n, int *stat)
+k_union_count(typename KS::Params P, int nrows, int *cnt, int *wide_list, int *wide_n, int *stat, int *defer_list,
+              int *defer_n, int defer_S)
 {
     __shared__ unsigned s_bm[WPC][NW];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -94,7 +102,11 @@ k_union_count(typename KS::Params P, int nrows, int *cnt, int *wide_list, int *w
     const long long span = (long long)kmax - kmin + 1;
     if (stat && lane == 0) atomicMax(stat + 1, (int)span);
     if (span > NW * 32) {
-        if (lane == 0) { cnt[row] = 0; wide_list[atomicAdd(wide_n, 1)] = row; }
+        if (lane == 0) {
+            cnt[row] = 0;
+            wide_list[atomicAdd(wide_n, 1)] = row;
+            if (defer_list) defer_list[atomicAdd(defer_n, 1)] = row;
+        }
         return;
     }
     unsigned *bm = s_bm[warp];
@@ -112,6 +124,7 @@ k_union_count(typename KS::Params P, int nrows, int *cnt, int *wide_list, int *w
     if (lane == 0) {
         cnt[row] = c;
         if (stat) atomicMax(stat, c);
+        if (defer_list && c > defer_S) defer_list[atomicAdd(defer_n, 1)] = row;
     }
 }
 
@@ -168,8 +181,162 @@ k_union_fill(typename KS::Params P, int nrows, const TP *rowptr, int *out, uint1
         ks.each(lane, 32, [&](int key, int r, int c) {
             int o = key - kmin, w = o >> 5;
             int slot = pref[w] + __popc(bm[w] & ((1u << (o & 31)) - 1u));
-            atomic_or_mask16(mask, (base + slot) * TILE + r, 1u << (TILE - 1 - c));
+            atomic_or_mask16(mask, base * TILE + (long long)r * total + slot, 1u << (TILE - 1 - c));
         });
+    }
+}
+
+// ---- fused step-1 fill + step 2 (narrow tile-rows) -------------------------
+
+constexpr int FWPC = 4;                 // warps per CTA
+constexpr int FSW = FUSED_MAX_TILES;    // most C tiles per tile-row handled here
+static_assert(NW * 32 == FUSED_MAX_SPAN, "fused window");
+
+// One warp per C tile-row whose tile-column window is at most 4096 wide and
+// which has at most FSW tiles: it writes the row's sorted tile columns (step
+// 1) and then, in the same warp, its row masks (step 2): for each A tile
+// (i,k), lanes take B's tiles (k,j) -- the bitmap rank of j is its slot --
+// and for every nonzero row r of the A tile OR together the B rows named by
+// A's row mask (masks read coalesced from the row-major layout).  Lanes hold
+// distinct slots, so the accumulation in shared memory needs no atomics.
+// Then per-row popcounts give C's row counts and the numeric bin.
+__global__ void __launch_bounds__(FWPC * 32)
+k_sym_fused(UnionKeys::Params P, int blkm, int m, const long long *__restrict__ crp, int *ccol,
+            const uint16_t *__restrict__ amask, const uint16_t *__restrict__ bmask, uint16_t *cmask, int *rowcnt,
+            unsigned char *bin, NumericBinParams bp, long long *binstat, int *flags)
+{
+    __shared__ unsigned s_bm[FWPC][NW];
+    __shared__ unsigned short s_pref[FWPC][NW];
+    __shared__ unsigned short s_msk[FWPC][TILE * FSW];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int row = blockIdx.x * FWPC + warp;
+    if (row >= blkm) return;
+    UnionKeys ks(P, row);
+    int kmin = INT_MAX, kmax = -1;
+    ks.bounds(lane, 32, kmin, kmax);
+    kmin = warp_min_int(kmin);
+    kmax = warp_max_int(kmax);
+    const long long c0 = crp[row];
+    const int S = (int)(crp[row + 1] - c0);
+    const long long span = kmax >= kmin ? (long long)kmax - kmin + 1 : 0;
+    if (span > NW * 32) return;   // wide: the wide fill writes its columns, the CTA step-2 kernel its masks
+    const int rows = min(TILE, m - row * TILE);
+    unsigned *bm = s_bm[warp];
+    unsigned short *pref = s_pref[warp];
+    unsigned short *msk = s_msk[warp];
+    const int nwords = (int)((span + 31) >> 5);
+    for (int w = lane; w < nwords; w += 32) bm[w] = 0;
+    if (S <= FSW)
+        for (int t = lane; t < S * TILE; t += 32) msk[t] = 0;
+    __syncwarp();
+    ks.each(lane, 32, [&](int key, int, int) {
+        int o = key - kmin;
+        atomicOr(&bm[o >> 5], 1u << (o & 31));
+    });
+    __syncwarp();
+    {   // sorted tile columns + per-word ranks
+        const int wpl = (nwords + 31) >> 5;
+        const int w0 = min(nwords, lane * wpl), w1 = min(nwords, w0 + wpl);
+        int lc = 0;
+        for (int w = w0; w < w1; ++w) lc += __popc(bm[w]);
+        const int incl = warp_incl_scan(lc, lane);
+        int run = incl - lc;
+        for (int w = w0; w < w1; ++w) {
+            unsigned x = bm[w];
+            pref[w] = (unsigned short)run;
+            while (x) {
+                const int b = __ffs(x) - 1;
+                ccol[c0 + run] = kmin + w * 32 + b;
+                ++run;
+                x &= x - 1;
+            }
+        }
+    }
+    __syncwarp();
+    if (S > FSW) return;          // masks and counts of this tile-row: CTA step-2 kernel
+    const int a0 = P.arp[row], a1 = P.arp[row + 1], na = a1 - a0;
+    bool bad = false;
+    for (int ab = a0; ab < a1; ab += 32) {
+        // B tile-row of up to 32 A tiles, fetched by the lanes at once
+        const int nac = min(32, a1 - ab);
+        int q0l = 0, nql = 0;
+        if (lane < nac) {
+            const int kt = P.acol[ab + lane];
+            q0l = P.brp[kt];
+            nql = P.brp[kt + 1] - q0l;
+        }
+        for (int t = 0; t < nac; ++t) {
+            const int q0 = __shfl_sync(0xffffffffu, q0l, t), nq = __shfl_sync(0xffffffffu, nql, t);
+            const int a = ab + t;
+            const unsigned ma = (lane < TILE) ? (unsigned)amask[(long long)a0 * TILE + (long long)lane * na + (a - a0)] : 0u;
+            // transpose the A tile: colrows[c] = rows that use local column c (uniform)
+            unsigned colrows[TILE];
+#pragma unroll
+            for (int c = 0; c < TILE; ++c) colrows[c] = __ballot_sync(0xffffffffu, (ma >> (TILE - 1 - c)) & 1u) & 0xffffu;
+            const uint16_t *bq = bmask + (long long)q0 * TILE;
+            for (int qb = 0; qb < nq; qb += 32) {
+                const int q = qb + lane;
+                int slot = -1;
+                if (q < nq) {
+                    const int o = P.bcol[q0 + q] - kmin;
+                    if (o >= 0 && o < span) {
+                        const int w = o >> 5;
+                        slot = pref[w] + __popc(bm[w] & ((1u << (o & 31)) - 1u));
+                    }
+                    if (slot < 0 || slot >= S) { bad = true; slot = -1; }
+                }
+                // the B tile's rows this A tile uses: independent loads, issued together
+                unsigned brow[TILE];
+#pragma unroll
+                for (int c = 0; c < TILE; ++c)
+                    brow[c] = (colrows[c] != 0u && slot >= 0) ? (unsigned)bq[c * nq + q] : 0u;
+#pragma unroll
+                for (int c = 0; c < TILE; ++c) {
+                    unsigned rws = colrows[c];
+                    const unsigned b = brow[c];
+                    while (rws) {
+                        const int r = __ffs(rws) - 1;
+                        rws &= rws - 1;
+                        if (b) msk[r * S + slot] |= (unsigned short)b;
+                    }
+                }
+            }
+        }
+    }
+    __syncwarp();
+    for (int t = lane; t < S * TILE; t += 32) cmask[c0 * TILE + t] = msk[t];
+    long long nnz_tr = 0;
+    for (int r = 0; r < TILE; ++r) {
+        int c = 0;
+        for (int sl = lane; sl < S; sl += 32) c += __popc((unsigned)msk[r * S + sl]);
+        c = warp_sum_int(c);
+        if (lane == 0 && r < rows) rowcnt[row * TILE + r] = c;
+        nnz_tr += c;
+    }
+    if (bad) set_flag(flags, FLAG_INTERNAL);
+    if (lane == 0) {
+        int b;
+        long long req = 0;
+        numeric_classify(bp, S, nnz_tr, span, b, req);
+        bin[row] = (unsigned char)b;
+        atomicAdd((unsigned long long *)&binstat[b], 1ull);
+        atomicMax((long long *)&binstat[NBIN + b], req);
+    }
+}
+
+// Row-major masks of each tile-row -> 16 consecutive masks per tile (the
+// reference's layout).  One warp per tile-row.
+template <typename TP>
+__global__ void k_masks_to_tile_major(int blkm, const TP *__restrict__ rowptr, const uint16_t *__restrict__ src,
+                                      uint16_t *dst)
+{
+    const int row = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (row >= blkm) return;
+    const long long b = (long long)rowptr[row];
+    const long long nt = (long long)rowptr[row + 1] - b;
+    for (long long t = lane; t < nt * TILE; t += 32) {
+        const long long r = t / nt, sl = t - r * nt;
+        dst[(b + sl) * TILE + r] = src[b * TILE + t];
     }
 }
 
@@ -230,11 +397,11 @@ k_union_wide(typename KS::Params P, const int *wide_list, const int *wide_n, int
         ks.bounds(tid, WIDE_THREADS, kmin, kmax);
         kmin = block_reduce_min(kmin, s_red);
         kmax = block_reduce_max(kmax, s_red);
-        long long base = 0;
+        long long base = 0, ntiles = 0;
         if (FILL) {
             base = (long long)rowptr[row];
+            ntiles = (long long)rowptr[row + 1] - base;
             if (MASK) {
-                const long long ntiles = (long long)rowptr[row + 1] - base;
                 unsigned *mw = reinterpret_cast<unsigned *>(mask) + base * 8;
                 for (long long t = tid; t < ntiles * 8; t += WIDE_THREADS) mw[t] = 0u;
                 __syncthreads();
@@ -286,7 +453,7 @@ k_union_wide(typename KS::Params P, const int *wide_list, const int *wide_n, int
                     if (o >= 0 && o < span) {
                         int w = (int)(o >> 5);
                         long long slot = run + pref[w] + __popc(bm[w] & ((1u << (o & 31)) - 1u));
-                        atomic_or_mask16(mask, (base + slot) * TILE + r, 1u << (TILE - 1 - c));
+                        atomic_or_mask16(mask, base * TILE + r * ntiles + slot, 1u << (TILE - 1 - c));
                     }
                 });
             }
@@ -453,7 +620,7 @@ template <class KS, typename TP>
 cudaError_t union_structure(Pool &pool, typename KS::Params P, int nrows, int *cnt_scratch, int *wide,
                             TP *rowptr_out, int *out_cols, uint16_t *mask, int *flags, int *stat,
                             cudaError_t (*scan)(Pool &, const int *, TP *, long long, int *),
-                            bool do_count, bool do_fill)
+                            bool do_count, bool do_fill, int *defer = nullptr, int defer_S = 0)
 {
     cudaStream_t s = pool.stream;
     int *wide_n = wide + nrows;
@@ -463,7 +630,8 @@ cudaError_t union_structure(Pool &pool, typename KS::Params P, int nrows, int *c
         e = cudaMemsetAsync(wide_n, 0, sizeof(int), s);
         if (e != cudaSuccess) return e;
         if (nrows > 0) {
-            { k_union_count<KS><<<g, WPC * 32, 0, s>>>(P, nrows, cnt_scratch, wide, wide_n, stat); ::tsg::count_launch(); }
+            { k_union_count<KS><<<g, WPC * 32, 0, s>>>(P, nrows, cnt_scratch, wide, wide_n, stat, defer,
+                                                      defer ? defer + nrows : nullptr, defer_S); ::tsg::count_launch(); }
             { k_union_wide<KS, false, false, TP><<<304, WIDE_THREADS, WIDE_SMEM, s>>>(
                 P, wide, wide_n, cnt_scratch, stat, nullptr, nullptr, nullptr); ::tsg::count_launch(); }
         }
@@ -536,12 +704,47 @@ cudaError_t csr_to_tile_structure(Pool &pool, const long long *rp, const int *co
 // columns (fill pass, ccol).  cnt and wide (blkm+1 ints each) carry state
 // from the count pass to the fill pass; stat[0] gets the largest tile count
 // of a tile-row and stat[1] the widest tile-column window.
+// defer (blkm+1 ints, count pass only): the tile-rows the fused warp kernel
+// leaves to the CTA step-2 kernel (too wide, or more than FUSED_MAX_TILES
+// tiles), then their number; the caller zeroes defer[blkm] first.
 cudaError_t tile_symbolic(Pool &pool, const TileCSR &A, const TileCSR &B, long long *crp, int *ccol, int *cnt,
-                          int *wide, int *flags, int *stat, bool count_pass)
+                          int *wide, int *flags, int *stat, bool count_pass, int *defer)
 {
     UnionKeys::Params P{A.trp, A.tcol, B.trp, B.tcol};
     return union_structure<UnionKeys, long long>(pool, P, A.blkm, cnt, wide, crp, ccol, nullptr, flags, stat,
-                                                 scan_i32_to_i64, count_pass, !count_pass);
+                                                 scan_i32_to_i64, count_pass, !count_pass, defer, FUSED_MAX_TILES);
+}
+
+// Step 1 fill and step 2 for the tile-rows one warp can hold (k_sym_fused),
+// then the sorted tile columns of the wide tile-rows (their masks and counts
+// come from step2_masks's CTA kernel).
+cudaError_t symbolic_fill_fused(Pool &pool, const TileCSR &A, const TileCSR &B, int m, const long long *crp,
+                                int *ccol, uint16_t *cmask, int *rowcnt, unsigned char *bin,
+                                const NumericBinParams &bp, long long *binstat, int *cnt, int *wide, int *flags)
+{
+    cudaStream_t s = pool.stream;
+    if (A.blkm <= 0) return cudaSuccess;
+    UnionKeys::Params P{A.trp, A.tcol, B.trp, B.tcol};
+    { k_sym_fused<<<(unsigned)((A.blkm + FWPC - 1) / FWPC), FWPC * 32, 0, s>>>(P, A.blkm, m, crp, ccol, A.mask, B.mask,
+                                                                         cmask, rowcnt, bin, bp, binstat, flags); ::tsg::count_launch(); }
+    (void)cnt;
+    { k_union_wide<UnionKeys, true, false, long long><<<304, WIDE_THREADS, WIDE_SMEM, s>>>(
+        P, wide, wide + A.blkm, nullptr, nullptr, crp, ccol, nullptr); ::tsg::count_launch(); }
+    return cudaGetLastError();
+}
+
+cudaError_t masks_to_tile_major_i32(Pool &pool, int blkm, const int *rowptr, const uint16_t *src, uint16_t *dst)
+{
+    if (blkm <= 0) return cudaSuccess;
+    { k_masks_to_tile_major<int><<<(unsigned)((blkm + 7) / 8), 256, 0, pool.stream>>>(blkm, rowptr, src, dst); ::tsg::count_launch(); }
+    return cudaGetLastError();
+}
+
+cudaError_t masks_to_tile_major_i64(Pool &pool, int blkm, const long long *rowptr, const uint16_t *src, uint16_t *dst)
+{
+    if (blkm <= 0) return cudaSuccess;
+    { k_masks_to_tile_major<long long><<<(unsigned)((blkm + 7) / 8), 256, 0, pool.stream>>>(blkm, rowptr, src, dst); ::tsg::count_launch(); }
+    return cudaGetLastError();
 }
 
 // Stable CSR transpose: (tp, tcol, tval) = CSR of A^T (n x m).
