@@ -149,7 +149,9 @@ tsg_status tsg_measure_fp64_peak(tsg_ctx *ctx, double *gflops);
 tsg_status tsg_load_mtx(const char *path, tsg_csr *out, int32_t *is_symmetric);
 
 /* Release arrays that the library allocated into *m (C outputs or a loaded
- * matrix).  ctx may be NULL for host matrices from tsg_load_mtx. */
+ * matrix); a matrix whose owner is NULL belongs to the caller and is left
+ * alone.  ctx may be NULL for host matrices from tsg_load_mtx.  Outputs of
+ * one batched call share memory that is released with the last of them. */
 tsg_status tsg_csr_free(tsg_ctx *ctx, tsg_csr *m);
 
 /* ---- SpGEMM -------------------------------------------------------------- */
@@ -170,6 +172,22 @@ tsg_status tsg_csr_free(tsg_ctx *ctx, tsg_csr *m);
  */
 tsg_status tsg_spgemm(tsg_ctx *ctx, tsg_op op, const tsg_csr *A, const tsg_csr *B,
                       tsg_csr *C, tsg_stats *stats);
+
+/* ---- batched products ------------------------------------------------------ */
+
+/*
+ * C[i] = op(A[i], B[i]) for i < count (B used for TSG_OP_AB only), computed
+ * as ONE SpGEMM over the block-diagonal stacking of the instances: each
+ * instance's rows and columns start on a multiple of 16, so no tile
+ * straddles two instances and the tile-rows of the stack form an
+ * (instance, tile-row) work list that one symbolic pass and one numeric
+ * launch per bin cover.  Operands must be all host or all device memory;
+ * C[0].where chooses where all outputs go.  C[i] are views into one
+ * allocation; release each with tsg_csr_free (the memory goes with the last).
+ * No counterpart in the reference, which runs one product per process.
+ */
+tsg_status tsg_spgemm_batched(tsg_ctx *ctx, tsg_op op, int32_t count, const tsg_csr *A, const tsg_csr *B,
+                              tsg_csr *C, tsg_stats *stats);
 
 /* ---- plans: symbolic once, numeric many times ----------------------------- */
 
@@ -197,6 +215,49 @@ tsg_status tsg_plan_execute(tsg_ctx *ctx, tsg_plan *plan, const double *valA, co
 int64_t tsg_plan_nnz(const tsg_plan *plan);
 int64_t tsg_plan_device_bytes(const tsg_plan *plan);
 tsg_status tsg_plan_destroy(tsg_ctx *ctx, tsg_plan *plan);
+
+/* ---- serving: continuous batching of requests ------------------------------ */
+
+/*
+ * A request loop on one GPU (no counterpart in the reference).  Requests are
+ * admitted while the device memory they may need fits budget_bytes (operands
+ * plus an upper bound of C from the intermediate-product count); `workers`
+ * slots, each with its own CUDA stream and memory pool, run admitted
+ * requests concurrently, taking up to max_batch at a time.  A request with a
+ * nonzero pattern_key keeps its symbolic result (a plan) in its worker's
+ * cache (plan_cache_bytes, least recently used first out): a later request
+ * with the same key and new values runs only the numeric step.  Keyless
+ * requests of one op taken together run as one batched product.
+ * Operands are host memory and must stay valid until tsg_server_wait returns
+ * the request.  Results are host CSRs (pinned); release them with
+ * tsg_csr_free before destroying the server.
+ */
+typedef struct {
+    int32_t device;
+    int32_t workers;           /* concurrent slots (default 4) */
+    int32_t max_batch;         /* requests a slot takes at once (default 32) */
+    int64_t budget_bytes;      /* device memory admission budget (default 64 GiB) */
+    int64_t plan_cache_bytes;  /* per-slot plan cache for numeric-only repeats (default 8 GiB) */
+} tsg_server_opts;
+
+typedef struct {
+    double latency_ms;         /* submit -> result */
+    double queue_ms;           /* submit -> taken by a slot */
+    double run_ms;             /* taken -> result (the slot's whole group) */
+    int32_t numeric_only;      /* 1 when a cached plan skipped the symbolic steps */
+    int32_t batched_with;      /* requests computed in the same batched product */
+    int32_t worker;            /* slot that ran it */
+} tsg_server_result;
+
+typedef struct tsg_server tsg_server;
+void tsg_server_opts_default(tsg_server_opts *o);
+tsg_status tsg_server_create(const tsg_server_opts *opts, tsg_server **server);
+/* TSG_ERR_BUDGET: the request alone exceeds the budget. */
+tsg_status tsg_server_submit(tsg_server *server, tsg_op op, const tsg_csr *A, const tsg_csr *B, uint64_t pattern_key,
+                             int64_t *request_id);
+/* Blocks until the request is done; C receives the result. */
+tsg_status tsg_server_wait(tsg_server *server, int64_t request_id, tsg_csr *C, tsg_server_result *info);
+tsg_status tsg_server_destroy(tsg_server *server);
 
 /* ---- tile form (the reference's device format) --------------------------- */
 

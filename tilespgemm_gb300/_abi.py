@@ -77,6 +77,19 @@ class tsg_tiles(C.Structure):
     ]
 
 
+class tsg_server_opts(C.Structure):
+    _fields_ = [("device", C.c_int32), ("workers", C.c_int32), ("max_batch", C.c_int32),
+                ("budget_bytes", C.c_int64), ("plan_cache_bytes", C.c_int64)]
+
+
+class tsg_server_result(C.Structure):
+    _fields_ = [("latency_ms", C.c_double), ("queue_ms", C.c_double), ("run_ms", C.c_double),
+                ("numeric_only", C.c_int32), ("batched_with", C.c_int32), ("worker", C.c_int32)]
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
 # name -> (restype, argtypes); the list every consumer of the ABI checks against
 SIGNATURES = {
     "tsg_opts_default": (None, [C.POINTER(tsg_opts)]),
@@ -91,6 +104,8 @@ SIGNATURES = {
     "tsg_csr_free": (C.c_int, [C.c_void_p, C.POINTER(tsg_csr)]),
     "tsg_spgemm": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(tsg_csr), C.POINTER(tsg_csr),
                              C.POINTER(tsg_csr), C.POINTER(tsg_stats)]),
+    "tsg_spgemm_batched": (C.c_int, [C.c_void_p, C.c_int, C.c_int32, C.POINTER(tsg_csr), C.POINTER(tsg_csr),
+                                     C.POINTER(tsg_csr), C.POINTER(tsg_stats)]),
     "tsg_plan_create": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(tsg_csr), C.POINTER(tsg_csr),
                                   C.POINTER(C.c_void_p), C.POINTER(tsg_stats)]),
     "tsg_plan_execute": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
@@ -98,6 +113,12 @@ SIGNATURES = {
     "tsg_plan_nnz": (C.c_int64, [C.c_void_p]),
     "tsg_plan_device_bytes": (C.c_int64, [C.c_void_p]),
     "tsg_plan_destroy": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "tsg_server_opts_default": (None, [C.POINTER(tsg_server_opts)]),
+    "tsg_server_create": (C.c_int, [C.POINTER(tsg_server_opts), C.POINTER(C.c_void_p)]),
+    "tsg_server_submit": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(tsg_csr), C.POINTER(tsg_csr), C.c_uint64,
+                                    C.POINTER(C.c_int64)]),
+    "tsg_server_wait": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(tsg_csr), C.POINTER(tsg_server_result)]),
+    "tsg_server_destroy": (C.c_int, [C.c_void_p]),
     "tsg_csr_to_tiles": (C.c_int, [C.c_void_p, C.POINTER(tsg_csr), C.POINTER(tsg_tiles)]),
     "tsg_spgemm_tiles": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(tsg_csr), C.POINTER(tsg_csr),
                                    C.POINTER(tsg_tiles), C.POINTER(tsg_stats)]),

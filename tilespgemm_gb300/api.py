@@ -305,6 +305,45 @@ class Context:
         oc.free()
         return (res, st) if stats else res
 
+    def spgemm_batched_raw(self, As: list, Bs: list | None = None, op: str = "AA", out: str = "host",
+                           stats: bool = False):
+        """C_i = op(A_i, B_i) for all instances in one pipeline pass (tsg_spgemm_batched);
+        returns OwnedCSR views that share one allocation."""
+        n = len(As)
+        a = (_abi.tsg_csr * max(n, 1))()
+        keep: list = []
+        for i, A in enumerate(As):
+            s_, k_ = A._tsg()
+            a[i] = s_
+            keep.append(k_)
+        b_ptr = None
+        if Bs is not None:
+            b = (_abi.tsg_csr * max(n, 1))()
+            for i, B in enumerate(Bs):
+                s_, k_ = B._tsg()
+                b[i] = s_
+                keep.append(k_)
+            b_ptr = b
+        c = (_abi.tsg_csr * max(n, 1))()
+        c[0].where = _abi.MEM_DEVICE if out == "device" else _abi.MEM_HOST
+        st = _abi.tsg_stats() if stats else None
+        check(lib().tsg_spgemm_batched(self.handle, _OPS[op], n, a, b_ptr, c, C.byref(st) if st is not None else None))
+        del keep
+        outs = []
+        for i in range(n):
+            cs = _abi.tsg_csr()
+            C.memmove(C.byref(cs), C.byref(c[i]), C.sizeof(_abi.tsg_csr))
+            outs.append(OwnedCSR(self, cs))
+        return outs, (st.as_dict() if st is not None else None)
+
+    def spgemm_batched(self, As: list, Bs: list | None = None, op: str = "AA") -> list:
+        """Host CSRs C_i = op(A_i, B_i), computed as one batched SpGEMM."""
+        outs, _ = self.spgemm_batched_raw(As, Bs, op, out="host")
+        res = [o.download() for o in outs]
+        for o in outs:
+            o.free()
+        return res
+
     def plan(self, A: CSR, B: CSR | None = None, op: str = "AA") -> Plan:
         """Symbolic phase of op(A, B), kept for numeric-only repeats."""
         return Plan(self, A, B, op)

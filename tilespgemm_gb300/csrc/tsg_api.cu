@@ -61,6 +61,7 @@ void tsg::count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
 namespace tsg {
 void set_last_error(const char *msg) { g_err = msg; }
+void *make_malloc_owner(void *a, void *b, void *c);
 }
 
 static tsg_status fail(tsg_status st, const char *fmt, ...) __attribute__((format(printf, 2, 3)));
@@ -107,11 +108,15 @@ enum StatSlot {
     ST_SLOTS = 64
 };
 
+// Owner of library-allocated arrays handed to a caller (tsg_csr.owner).
+// Batched outputs share one owner; it is released when its last view is.
 struct OutOwner {
-    int where = TSG_MEM_DEVICE;
+    int where = TSG_MEM_DEVICE;   // TSG_MEM_DEVICE: pool memory; TSG_MEM_HOST: pinned; OWN_MALLOC: malloc
     tsg_ctx *ctx = nullptr;
+    int refs = 1;
     std::vector<std::pair<void *, size_t>> blocks;
 };
+constexpr int OWN_MALLOC = 2;
 
 void *pinned_get(tsg_ctx *ctx, size_t bytes)
 {
@@ -349,12 +354,12 @@ tsg_status stage_into_plan(tsg_ctx *ctx, Pool &pool, PlanData &P, const tsg_csr 
 // Symbolic phase: staging, A^T for A*A^T, tiles, step 1, step 2 (two host waits).
 // `keep` = the plan outlives the call (device operands are copied).
 tsg_status plan_symbolic(tsg_ctx *ctx, Pool &pool, Scratch &sc, tsg_op op, const tsg_csr *A, const tsg_csr *B,
-                         PlanData &P, bool keep, bool want_cub, PhaseTimer &tm)
+                         PlanData &P, bool keep, bool want_cub, PhaseTimer &tm, bool reset_flags = true)
 {
     const bool validate = ctx->opts.validate != 0;
     tsg_status r = check_op(op, A, B);
     if (r) return r;
-    CUDA_OK(cudaMemsetAsync(ctx->dflags, 0, sizeof(int) * FLAG_COUNT, ctx->stream));
+    if (reset_flags) CUDA_OK(cudaMemsetAsync(ctx->dflags, 0, sizeof(int) * FLAG_COUNT, ctx->stream));
     CUDA_OK(cudaMemsetAsync(ctx->dstat, 0, sizeof(long long) * ST_SLOTS, ctx->stream));
     tm.mark();  // 0
     P.op = op;
@@ -565,6 +570,14 @@ void phase_times(tsg_ctx *ctx, tsg_stats *st, const PhaseTimer &tm)
 
 }  // namespace
 
+void *tsg::make_malloc_owner(void *a, void *b, void *c)
+{
+    OutOwner *o = new OutOwner();
+    o->where = OWN_MALLOC;
+    for (void *p : {a, b, c}) if (p) o->blocks.push_back({p, 0});
+    return o;
+}
+
 // ============================================================================
 // C ABI
 // ============================================================================
@@ -666,10 +679,7 @@ tsg_status tsg_csr_free(tsg_ctx *ctx, tsg_csr *M)
 {
     if (!M) return TSG_OK;
     OutOwner *o = static_cast<OutOwner *>(M->owner);
-    if (!o) {
-        // a loaded host matrix (plain malloc)
-        free(M->row_ptr); free(M->col); free(M->val);
-    } else {
+    if (o && --o->refs <= 0) {
         tsg_ctx *c = o->ctx ? o->ctx : ctx;
         if (o->where == TSG_MEM_DEVICE) {
             if (c) {
@@ -677,16 +687,21 @@ tsg_status tsg_csr_free(tsg_ctx *ctx, tsg_csr *M)
                 for (auto &b : o->blocks) cudaFreeAsync(b.first, c->stream);
                 cudaStreamSynchronize(c->stream);
             }
-        } else {
+        } else if (o->where == TSG_MEM_HOST) {
             for (auto &b : o->blocks) {
                 if (c) pinned_put(c, b.first, b.second);
                 else cudaFreeHost(b.first);
             }
+        } else {
+            for (auto &b : o->blocks) free(b.first);
         }
         delete o;
     }
-    M->row_ptr = nullptr; M->col = nullptr; M->val = nullptr; M->owner = nullptr;
-    M->nnz = 0;
+    // caller-owned arrays (owner NULL) are left alone
+    if (o) {
+        M->row_ptr = nullptr; M->col = nullptr; M->val = nullptr; M->owner = nullptr;
+        M->nnz = 0;
+    }
     return TSG_OK;
 }
 
@@ -1068,6 +1083,251 @@ tsg_status tsg_tiles_download(tsg_ctx *ctx, const tsg_tiles *T, int64_t *blkrowp
     if (nb && mask) CUDA_OK(cudaMemcpy(mask, T->mask, sizeof(uint16_t) * nb * TILE, cudaMemcpyDeviceToHost));
     if (T->nnz && col) CUDA_OK(cudaMemcpy(col, T->col, (size_t)T->nnz, cudaMemcpyDeviceToHost));
     if (T->nnz && val) CUDA_OK(cudaMemcpy(val, T->val, sizeof(double) * (size_t)T->nnz, cudaMemcpyDeviceToHost));
+    return TSG_OK;
+}
+
+}  // extern "C"
+
+// ---- batched products ------------------------------------------------------
+
+namespace {
+
+inline long long round16(long long x) { return (x + 15) & ~15ll; }
+
+// Stack `count` operands block-diagonally into one device CSR (rows and
+// columns of every instance start on a multiple of 16).  rowoff/coloff give
+// each instance's first packed row/column.
+tsg_status pack_operands(tsg_ctx *ctx, Pool &pool, Scratch &sc, int count, const tsg_csr *M,
+                         const std::vector<long long> &rowoff, const std::vector<long long> &coloff,
+                         long long rows_total, long long cols_total, tsg_csr &packed)
+{
+    long long nnz = 0;
+    std::vector<long long> nnzoff(count);
+    for (int i = 0; i < count; ++i) { nnzoff[i] = nnz; nnz += M[i].nnz; }
+    if (nnz >= (1ll << 31)) return fail(TSG_ERR_NOT_SUPPORTED, "batch operands hold %lld entries; the limit is 2^31-1", nnz);
+    if (rows_total >= (1ll << 30) || cols_total >= (1ll << 30))
+        return fail(TSG_ERR_NOT_SUPPORTED, "batch is larger than 2^30 rows or columns");
+    long long *rp = sc.get<long long>(rows_total + 1);
+    int *col = sc.get<int>(nnz);
+    double *val = sc.get<double>(nnz);
+    if (!rp || !col || !val) return fail(TSG_ERR_OOM, "device pool allocation failed for the packed batch");
+    const bool host = M[0].where == TSG_MEM_HOST;
+    if (host) {
+        // pack on the host into pinned staging, then one copy per array
+        const size_t rpb = sizeof(long long) * (size_t)(rows_total + 1);
+        long long *hrp = (long long *)pinned_get(ctx, rpb);
+        int *hcol = (int *)pinned_get(ctx, sizeof(int) * (size_t)(nnz > 0 ? nnz : 1));
+        double *hval = (double *)pinned_get(ctx, sizeof(double) * (size_t)(nnz > 0 ? nnz : 1));
+        if (!hrp || !hcol || !hval) return fail(TSG_ERR_OOM, "pinned staging for the batch");
+        bool bad = false;
+        for (int i = 0; i < count; ++i) {
+            const tsg_csr &X = M[i];
+            const long long pad = (i + 1 < count ? rowoff[i + 1] : rows_total) - rowoff[i];
+            auto rp_at = [&](long long r) -> long long {
+                return X.rowptr_bits == 64 ? ((const long long *)X.row_ptr)[r] : (long long)((const int *)X.row_ptr)[r];
+            };
+            if (rp_at(X.m) != X.nnz) bad = true;
+            for (long long r = 0; r < pad; ++r) {
+                long long v = X.nnz;                      // padding rows repeat the end
+                if (r < X.m) {
+                    v = rp_at(r);
+                    if (v < 0 || v > X.nnz || (r == 0 && v != 0)) { bad = true; v = v < 0 ? 0 : (v > X.nnz ? X.nnz : v); }
+                }
+                hrp[rowoff[i] + r] = nnzoff[i] + v;
+            }
+            for (long long q = 0; q < X.nnz; ++q) {
+                int c = X.col[q];
+                if ((unsigned)c >= (unsigned)X.n) { bad = true; c = 0; }
+                hcol[nnzoff[i] + q] = (int)(c + coloff[i]);
+            }
+            if (X.nnz > 0) memcpy(hval + nnzoff[i], X.val, sizeof(double) * (size_t)X.nnz);
+        }
+        hrp[rows_total] = nnz;
+        for (long long r = 1; r <= rows_total && !bad; ++r) if (hrp[r] < hrp[r - 1]) bad = true;
+        cudaError_t e = cudaMemcpyAsync(rp, hrp, rpb, cudaMemcpyHostToDevice, ctx->stream);
+        if (e == cudaSuccess && nnz > 0) e = cudaMemcpyAsync(col, hcol, sizeof(int) * (size_t)nnz, cudaMemcpyHostToDevice, ctx->stream);
+        if (e == cudaSuccess && nnz > 0) e = cudaMemcpyAsync(val, hval, sizeof(double) * (size_t)nnz, cudaMemcpyHostToDevice, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        pinned_put(ctx, hrp, rpb);
+        pinned_put(ctx, hcol, sizeof(int) * (size_t)(nnz > 0 ? nnz : 1));
+        pinned_put(ctx, hval, sizeof(double) * (size_t)(nnz > 0 ? nnz : 1));
+        if (e != cudaSuccess) return fail(TSG_ERR_CUDA, "batch upload: %s", cudaGetErrorString(e));
+        if (bad) return fail(TSG_ERR_BAD_INPUT, "an instance's row pointer or column index is out of range");
+    } else {
+        std::vector<PackDesc> d(count);
+        for (int i = 0; i < count; ++i) {
+            const tsg_csr &X = M[i];
+            d[i].rp = X.row_ptr; d[i].col = X.col; d[i].val = X.val; d[i].rp_bits = X.rowptr_bits;
+            d[i].m = X.m; d[i].n = X.n; d[i].nnz = X.nnz; d[i].rowoff = rowoff[i];
+            d[i].rowpad = (i + 1 < count ? rowoff[i + 1] : rows_total) - rowoff[i];
+            d[i].coloff = coloff[i]; d[i].nnzoff = nnzoff[i];
+        }
+        PackDesc *dd = sc.get<PackDesc>(count);
+        if (!dd) return fail(TSG_ERR_OOM, "device pool allocation failed");
+        CUDA_OK(cudaMemcpyAsync(dd, d.data(), sizeof(PackDesc) * (size_t)count, cudaMemcpyHostToDevice, ctx->stream));
+        CUDA_OK(batch_pack(pool, dd, count, rp, col, val, ctx->dflags));
+        CUDA_OK(cudaMemcpyAsync(rp + rows_total, &nnz, sizeof(long long), cudaMemcpyHostToDevice, ctx->stream));
+        CUDA_OK(cudaStreamSynchronize(ctx->stream));   // the descriptor and the end value are host stack memory
+    }
+    packed = tsg_csr{};
+    packed.m = (int)rows_total; packed.n = (int)cols_total; packed.nnz = nnz;
+    packed.rowptr_bits = 64; packed.where = TSG_MEM_DEVICE;
+    packed.row_ptr = rp; packed.col = col; packed.val = val;
+    return TSG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+tsg_status tsg_spgemm_batched(tsg_ctx *ctx, tsg_op op, int32_t count, const tsg_csr *A, const tsg_csr *B,
+                              tsg_csr *C, tsg_stats *st)
+{
+    if (!ctx || !C || (count > 0 && !A)) return fail(TSG_ERR_INVALID_ARG, "ctx/A/C is NULL");
+    if (count < 0) return fail(TSG_ERR_INVALID_ARG, "negative count");
+    if (op == TSG_OP_AB && count > 0 && !B) return fail(TSG_ERR_INVALID_ARG, "B is NULL for A*B");
+    if (C[0].where != TSG_MEM_HOST && C[0].where != TSG_MEM_DEVICE) return fail(TSG_ERR_INVALID_ARG, "C[0].where is not a tsg_mem");
+    if (st) memset(st, 0, sizeof(*st));
+    if (count == 0) return TSG_OK;
+    auto t0 = std::chrono::steady_clock::now();
+    CUDA_OK(cudaSetDevice(ctx->device));
+    for (int i = 0; i < count; ++i) {
+        tsg_status r = check_op(op, &A[i], op == TSG_OP_AB ? &B[i] : nullptr);
+        if (r) return r;
+        if (A[i].where != A[0].where || (op == TSG_OP_AB && B[i].where != A[0].where))
+            return fail(TSG_ERR_INVALID_ARG, "all batch operands must be host, or all device");
+        if (A[i].nnz > 0 && !A[i].val) return fail(TSG_ERR_INVALID_ARG, "instance %d has no values", i);
+    }
+    // layout: rows of A (and C), columns of A (= rows of B), columns of B (and C)
+    std::vector<long long> roff(count), koff(count), noff(count);
+    long long M = 0, K = 0, N = 0;
+    for (int i = 0; i < count; ++i) {
+        roff[i] = M; M += round16(A[i].m);
+        koff[i] = K; K += round16(A[i].n);
+        const int ni = op == TSG_OP_AB ? B[i].n : (op == TSG_OP_AA ? A[i].n : A[i].m);
+        noff[i] = N; N += round16(ni);
+    }
+    Pool pool{ctx->pool, ctx->stream};
+    PlanData P;
+    PhaseTimer tm(ctx, st && ctx->opts.phase_times);
+    int *col = nullptr;
+    double *val = nullptr;
+    tsg_status r;
+    {
+        Scratch sc(pool);
+        CUDA_OK(cudaMemsetAsync(ctx->dflags, 0, sizeof(int) * FLAG_COUNT, ctx->stream));
+        tsg_csr pA{}, pB{};
+        r = pack_operands(ctx, pool, sc, count, A, roff, op == TSG_OP_AAT ? koff : (op == TSG_OP_AA ? roff : koff),
+                          M, op == TSG_OP_AA ? M : K, pA);
+        if (!r && op == TSG_OP_AB) r = pack_operands(ctx, pool, sc, count, B, koff, noff, K, N, pB);
+        if (!r) r = plan_symbolic(ctx, pool, sc, op, &pA, op == TSG_OP_AB ? &pB : nullptr, P, false, st != nullptr, tm,
+                                  false);
+        if (!r) {
+            col = pool.alloc_n<int>(P.nnzC);
+            val = pool.alloc_n<double>(P.nnzC);
+            if (!col || !val) r = fail(TSG_ERR_OOM, "device pool allocation failed for C (%lld entries)", P.nnzC);
+        }
+        if (!r) r = plan_numeric(ctx, pool, P, P.valA, P.valB, col, val);
+        tm.mark();  // 4
+        // unpack: per-instance row pointers (rebased) and columns (rebased in place)
+        long long rpn = 0;
+        std::vector<UnpackDesc> ud(count);
+        for (int i = 0; i < count; ++i) {
+            ud[i].rowoff = roff[i]; ud[i].m = A[i].m;
+            ud[i].coloff = op == TSG_OP_AAT ? roff[i] : noff[i];
+            ud[i].rpoff = rpn; rpn += A[i].m + 1;
+        }
+        int bits = ctx->opts.out_rowptr_bits;
+        if (bits == 0) bits = P.nnzC < (1ll << 31) ? 32 : 64;
+        if (!r && bits == 32 && P.nnzC >= (1ll << 31)) r = fail(TSG_ERR_INT32_OVERFLOW, "batch C needs int64 row pointers");
+        void *rp_out = nullptr;
+        long long *ebase = nullptr;
+        if (!r) {
+            rp_out = pool.alloc((size_t)rpn * (bits == 64 ? 8 : 4));
+            ebase = sc.get<long long>(count);
+            UnpackDesc *dud = sc.get<UnpackDesc>(count);
+            if (!rp_out || !ebase || !dud) r = fail(TSG_ERR_OOM, "device pool allocation failed (batch outputs)");
+            if (!r) {
+                CUDA_OK(cudaMemcpyAsync(dud, ud.data(), sizeof(UnpackDesc) * (size_t)count, cudaMemcpyHostToDevice, ctx->stream));
+                CUDA_OK(batch_unpack(pool, dud, count, P.rowptrC, col, rp_out, bits, ebase));
+            }
+        }
+        std::vector<long long> eb(count);
+        if (!r) {
+            CUDA_OK(cudaMemcpyAsync(eb.data(), ebase, sizeof(long long) * (size_t)count, cudaMemcpyDeviceToHost, ctx->stream));
+            CUDA_OK(cudaStreamSynchronize(ctx->stream));
+            int hflags[FLAG_COUNT];
+            CUDA_OK(cudaMemcpy(hflags, ctx->dflags, sizeof(hflags), cudaMemcpyDeviceToHost));
+            if (hflags[FLAG_BAD_INPUT]) r = fail(TSG_ERR_BAD_INPUT, "an instance's row pointer or column index is out of range");
+            else if (hflags[FLAG_INTERNAL]) r = fail(TSG_ERR_CUDA, "internal bound check failed on the device");
+        }
+        if (!r) {
+            OutOwner *o = new OutOwner();
+            o->ctx = ctx;
+            o->refs = count;
+            o->where = C[0].where;
+            const int w = bits == 64 ? 8 : 4;
+            char *hrp = nullptr;
+            int *hcol = nullptr;
+            double *hval = nullptr;
+            if (C[0].where == TSG_MEM_DEVICE) {
+                o->blocks = {{rp_out, 0}, {col, 0}, {val, 0}};
+            } else {
+                const size_t rpb = (size_t)rpn * w, cb = sizeof(int) * (size_t)P.nnzC, vb = sizeof(double) * (size_t)P.nnzC;
+                hrp = (char *)pinned_get(ctx, rpb);
+                hcol = (int *)pinned_get(ctx, cb);
+                hval = (double *)pinned_get(ctx, vb);
+                cudaError_t e = (hrp && hcol && hval) ? cudaSuccess : cudaErrorMemoryAllocation;
+                if (e == cudaSuccess) e = cudaMemcpyAsync(hrp, rp_out, rpb, cudaMemcpyDeviceToHost, ctx->stream);
+                if (e == cudaSuccess && P.nnzC) e = cudaMemcpyAsync(hcol, col, cb, cudaMemcpyDeviceToHost, ctx->stream);
+                if (e == cudaSuccess && P.nnzC) e = cudaMemcpyAsync(hval, val, vb, cudaMemcpyDeviceToHost, ctx->stream);
+                if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+                pool.free(rp_out); pool.free(col); pool.free(val);
+                col = nullptr; val = nullptr; rp_out = nullptr;
+                if (hrp) o->blocks.push_back({hrp, rpb});
+                if (hcol) o->blocks.push_back({hcol, cb});
+                if (hval) o->blocks.push_back({hval, vb});
+                if (e != cudaSuccess) {
+                    o->refs = 1;
+                    tsg_csr tmp{};
+                    tmp.owner = o;
+                    tsg_csr_free(ctx, &tmp);
+                    r = fail(TSG_ERR_CUDA, "batch output copy: %s", cudaGetErrorString(e));
+                }
+            }
+            if (!r) {
+                char *rpbase = C[0].where == TSG_MEM_DEVICE ? (char *)rp_out : hrp;
+                int *colbase = C[0].where == TSG_MEM_DEVICE ? col : hcol;
+                double *valbase = C[0].where == TSG_MEM_DEVICE ? val : hval;
+                for (int i = 0; i < count; ++i) {
+                    const int ni = op == TSG_OP_AB ? B[i].n : (op == TSG_OP_AA ? A[i].n : A[i].m);
+                    const long long nz_i = (i + 1 < count ? eb[i + 1] : P.nnzC) - eb[i];
+                    C[i].m = A[i].m; C[i].n = ni; C[i].nnz = nz_i; C[i].rowptr_bits = bits; C[i].where = C[0].where;
+                    C[i].row_ptr = rpbase + ud[i].rpoff * w;
+                    C[i].col = colbase + eb[i];
+                    C[i].val = valbase + eb[i];
+                    C[i].owner = o;
+                }
+                col = nullptr; val = nullptr;
+            }
+        } else {
+            pool.free(rp_out);
+        }
+    }
+    if (r) {
+        pool.free(col); pool.free(val);
+        P.release(pool);
+        cudaStreamSynchronize(ctx->stream);
+        cudaGetLastError();
+        return r;
+    }
+    fill_stats(P, st);
+    P.release(pool);
+    cudaStreamSynchronize(ctx->stream);
+    if (st) {
+        st->ms_total = ms_since(t0);
+        phase_times(ctx, st, tm);
+    }
     return TSG_OK;
 }
 

@@ -252,6 +252,54 @@ __global__ void k_gather(const int *__restrict__ perm, const double *__restrict_
         dst[q] = src[perm[q]];
 }
 
+// ---- batched products: block-diagonal packing -----------------------------
+
+// one CTA per instance: shifted row pointer (padding rows repeat the end),
+// shifted columns, copied values; row pointers and columns are validated
+__global__ void __launch_bounds__(256)
+k_batch_pack(const PackDesc *__restrict__ descs, long long *rp, int *col, double *val, int *flags)
+{
+    const PackDesc d = descs[blockIdx.x];
+    bool bad = false;
+    for (long long r = threadIdx.x; r < d.rowpad; r += blockDim.x) {
+        long long v;
+        if (r < d.m) {
+            v = d.rp_bits == 64 ? ((const long long *)d.rp)[r] : (long long)((const int *)d.rp)[r];
+            const long long nx = d.rp_bits == 64 ? ((const long long *)d.rp)[r + 1] : (long long)((const int *)d.rp)[r + 1];
+            if (v < 0 || nx < v || nx > d.nnz || (r == 0 && v != 0)) bad = true;
+            v = v < 0 ? 0 : (v > d.nnz ? d.nnz : v);
+        } else {
+            v = d.nnz;
+        }
+        rp[d.rowoff + r] = d.nnzoff + v;
+    }
+    if (threadIdx.x == 0 && d.m > 0) {
+        const long long last = d.rp_bits == 64 ? ((const long long *)d.rp)[d.m] : (long long)((const int *)d.rp)[d.m];
+        if (last != d.nnz) bad = true;
+    }
+    for (long long q = threadIdx.x; q < d.nnz; q += blockDim.x) {
+        int c = d.col[q];
+        if ((unsigned)c >= (unsigned)d.n) { bad = true; c = 0; }
+        col[d.nnzoff + q] = (int)(c + d.coloff);
+        if (d.val) val[d.nnzoff + q] = d.val[q];
+    }
+    if (__syncthreads_or(bad) && threadIdx.x == 0) set_flag(flags, FLAG_BAD_INPUT);
+}
+
+// one CTA per instance: C_i's row pointer rebased to 0, its columns rebased
+template <typename TR>
+__global__ void __launch_bounds__(256)
+k_batch_unpack(const UnpackDesc *__restrict__ descs, const long long *__restrict__ rowptrC, int *col, TR *rp_out,
+               long long *ebase)
+{
+    const UnpackDesc d = descs[blockIdx.x];
+    const long long e0 = rowptrC[d.rowoff];
+    if (threadIdx.x == 0) ebase[blockIdx.x] = e0;
+    for (long long r = threadIdx.x; r <= d.m; r += blockDim.x) rp_out[d.rpoff + r] = (TR)(rowptrC[d.rowoff + r] - e0);
+    const long long e1 = rowptrC[d.rowoff + d.m];
+    for (long long q = e0 + threadIdx.x; q < e1; q += blockDim.x) col[q] = (int)(col[q] - d.coloff);
+}
+
 inline unsigned g256(long long n) {
     long long g = (n + 255) / 256;
     if (g < 1) g = 1;
@@ -313,6 +361,22 @@ cudaError_t aux_gather(Pool &pool, const int *perm, const double *src, double *d
 {
     if (n <= 0) return cudaSuccess;
     { k_gather<<<g256(n), 256, 0, pool.stream>>>(perm, src, dst, n); ::tsg::count_launch(); }
+    return cudaGetLastError();
+}
+
+cudaError_t batch_pack(Pool &pool, const PackDesc *d_desc, int count, long long *rp, int *col, double *val, int *flags)
+{
+    if (count <= 0) return cudaSuccess;
+    { k_batch_pack<<<count, 256, 0, pool.stream>>>(d_desc, rp, col, val, flags); ::tsg::count_launch(); }
+    return cudaGetLastError();
+}
+
+cudaError_t batch_unpack(Pool &pool, const UnpackDesc *d_desc, int count, const long long *rowptrC, int *col,
+                         void *rp_out, int rp_bits, long long *ebase)
+{
+    if (count <= 0) return cudaSuccess;
+    if (rp_bits == 64) { k_batch_unpack<long long><<<count, 256, 0, pool.stream>>>(d_desc, rowptrC, col, (long long *)rp_out, ebase); ::tsg::count_launch(); }
+    else { k_batch_unpack<int><<<count, 256, 0, pool.stream>>>(d_desc, rowptrC, col, (int *)rp_out, ebase); ::tsg::count_launch(); }
     return cudaGetLastError();
 }
 

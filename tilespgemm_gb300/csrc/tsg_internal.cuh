@@ -124,4 +124,29 @@ cudaError_t scan_i64_to_i64(Pool &pool, const long long *in, long long *out, lon
 
 inline int ceil_div_i(long long a, long long b) { return (int)((a + b - 1) / b); }
 
+// One instance of a batched product, as the pack/unpack kernels see it.
+struct PackDesc {
+    const void *rp;          // instance row pointer (int32 or int64), device
+    const int *col;          // instance columns, device
+    const double *val;       // instance values, device (may be null)
+    int rp_bits;
+    int m, n;                // instance shape (n: column bound for validation)
+    long long nnz;
+    long long rowoff;        // first packed row (multiple of 16)
+    long long rowpad;        // packed rows reserved (m rounded up to 16)
+    long long coloff;        // added to the instance's column indices
+    long long nnzoff;        // first packed entry
+};
+
+struct UnpackDesc {
+    long long rowoff;        // first packed row of C_i
+    int m;                   // rows of C_i
+    long long coloff;        // subtracted from C's packed column indices
+    long long rpoff;         // first entry of C_i's row pointer in the output array
+};
+
+cudaError_t batch_pack(Pool &pool, const PackDesc *d_desc, int count, long long *rp, int *col, double *val, int *flags);
+cudaError_t batch_unpack(Pool &pool, const UnpackDesc *d_desc, int count, const long long *rowptrC, int *col,
+                         void *rp_out, int rp_bits, long long *ebase);
+
 }  // namespace tsg

@@ -28,6 +28,7 @@
 
 namespace tsg {
 void set_last_error(const char *msg);
+void *make_malloc_owner(void *a, void *b, void *c);
 }
 
 namespace {
@@ -177,7 +178,7 @@ extern "C" tsg_status tsg_load_mtx(const char *path, tsg_csr *out, int32_t *is_s
     out->row_ptr = rp;
     out->col = col;
     out->val = val;
-    out->owner = nullptr;
+    out->owner = tsg::make_malloc_owner(rp, col, val);
     if (is_symmetric) *is_symmetric = symm ? 1 : 0;
     return TSG_OK;
 }
