@@ -352,6 +352,100 @@ def run_ours(args) -> None:
         dist.destroy_process_group()
 
 
+def run_batched(args) -> None:
+    """Batched instances/s (tsg_spgemm_batched, in waves) against the same
+    instances computed one call at a time (tsg_spgemm), device operands and
+    device results, CUDA events on the library's stream."""
+    import torch
+    from tilespgemm_gb300 import Context, _abi
+    from tilespgemm_gb300 import matrices as M
+    count, waves = args.batch_count, max(1, args.batch_waves)
+    As = [M.batch_instance(i, seed=1) for i in range(count)]
+    cub = sum(int(np.diff(np.asarray(A.rowptr))[np.asarray(A.col)].sum()) for A in As)
+    Ad = [A.to_device(0) for A in As]
+    ctx = Context(0)
+    lib = _abi.lib()
+    stream = torch.cuda.ExternalStream(lib.tsg_get_stream(ctx.handle), device=torch.device("cuda", 0))
+    per = (count + waves - 1) // waves
+    groups = [Ad[w * per:(w + 1) * per] for w in range(waves) if Ad[w * per:(w + 1) * per]]
+
+    def batched_pass():
+        nnz = 0
+        for g in groups:
+            outs, _ = ctx.spgemm_batched_raw(g, op="AA", out="device")
+            nnz += sum(o.nnz for o in outs)
+            for o in outs:
+                o.free()
+        return nnz
+
+    def single_pass():
+        for A in Ad:
+            oc, _ = ctx.spgemm_raw(A, op="AA", out="device")
+            oc.free()
+
+    def timed(fn, reps):
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    for _ in range(args.warmup):
+        nnz_c = batched_pass()
+    single_pass()
+    l0 = lib.tsg_launch_count()
+    with ClockSampler(0) as clk:
+        ms_b = timed(batched_pass, args.steps)
+    launches_b = (lib.tsg_launch_count() - l0) / args.steps
+    ms_s = timed(single_pass, 1)
+    out = {
+        "metric": "batched SpGEMM instances/s", "value": count / (ms_b / 1e3), "unit": "instances/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_b, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded, batched workload shapes)",
+        "config": {"workload": f"batched: {count} x A*A, n log-uniform [64,16384], nnz/row U[2,64], "
+                               f"banded (n/8) for even instances, uniform for odd", "waves": len(groups),
+                   "nnz_a": int(sum(A.nnz for A in As)), "nnz_cub": cub, "nnz_c": int(nnz_c)},
+        "one_at_a_time": {"instances_per_s": count / (ms_s / 1e3), "ms": ms_s},
+        "speedup_vs_one_at_a_time": ms_s / ms_b,
+        "gflops_batched": 2.0 * cub / (ms_b * 1e6),
+        "gpu_launches_per_step": launches_b,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(out))
+    ctx.close()
+
+
+def run_served(args) -> None:
+    """Served stream: p50/p99 latency and throughput (tsg_server_*)."""
+    from tilespgemm_gb300.serving import Server, make_stream, run_stream
+    procs = max(1, min(16, (os.cpu_count() or 1)))
+    reqs = make_stream(args.serve_requests, seed=1, rate=args.serve_rate,
+                       rmat_scale=(12, args.serve_max_scale), procs=procs)
+    warm = make_stream(16, seed=99, rate=args.serve_rate, rmat_scale=(12, 13), lap_side=(32, 64))
+    with Server(workers=args.serve_workers, budget_gb=64.0) as srv:
+        run_stream(srv, warm, realtime=False, download=False)
+        st = run_stream(srv, reqs, realtime=True, download=False)
+    done = [r for r in st["results"] if r is not None]
+    lat = [r[1]["latency_ms"] for r in done]
+    out_nnz = sum(r[1]["nnz"] for r in done)
+    out = {
+        "metric": "served SpGEMM requests/s with p50/p99 latency", "value": st["throughput_rps"], "unit": "requests/s",
+        "n_gpus": 1, "steps": 1, "warmup": 1, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded Poisson stream)",
+        "config": {"workload": f"served: {len(reqs)} requests, Poisson {args.serve_rate:.0f}/s, 50/50 Laplacian "
+                               f"(side 32-512) / R-MAT (2^12-2^{args.serve_max_scale}, 8-32/row), 50/50 A*A / A*A^T, "
+                               "30% numeric-only repeats, 64 GB budget", "workers": args.serve_workers},
+        "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "mean_ms": st["mean_ms"],
+        "max_ms": float(max(lat)) if lat else None, "completed": st["completed"],
+        "refused_over_budget": st["refused"], "numeric_only_requests": st["numeric_only"],
+        "c_entries_returned": int(out_nnz), "wall_s": st["wall_s"],
+    }
+    print(json.dumps(out))
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -361,11 +455,21 @@ def main() -> None:
     ap.add_argument("--workload", default="st27-96")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--batch-count", type=int, default=4096)
+    ap.add_argument("--batch-waves", type=int, default=8)
+    ap.add_argument("--serve-requests", type=int, default=400)
+    ap.add_argument("--serve-rate", type=float, default=2000.0)
+    ap.add_argument("--serve-max-scale", type=int, default=18)
+    ap.add_argument("--serve-workers", type=int, default=4)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "batched":
+        run_batched(args)
+    elif args.workload == "served":
+        run_served(args)
     else:
         run_ours(args)
 

@@ -77,32 +77,35 @@ int64_t rowptr_at(const tsg_csr &M, int64_t i)
     return M.rowptr_bits == 64 ? ((const int64_t *)M.row_ptr)[i] : ((const int32_t *)M.row_ptr)[i];
 }
 
-// Device bytes a request may need: operands, C's upper bound (12 bytes per
-// intermediate product, capped by the dense size), tiles.
+// Device bytes a request may need: operands, C's upper bound (per row, the
+// row's intermediate-product count capped by C's column count; 12 bytes per
+// entry), tiles.
 int64_t estimate_bytes(tsg_op op, const tsg_csr &A, const tsg_csr *B)
 {
-    int64_t cub = 0;
+    const int64_t n = (op == TSG_OP_AB && B) ? B->n : (op == TSG_OP_AA ? A.n : A.m);
+    int64_t cmax = 0;
+    std::vector<int32_t> colcnt;
     if (op == TSG_OP_AAT) {
         // B = A^T: B row k has as many entries as A column k
-        std::vector<int32_t> colcnt((size_t)(A.n > 0 ? A.n : 1), 0);
+        colcnt.assign((size_t)(A.n > 0 ? A.n : 1), 0);
         for (int64_t p = 0; p < A.nnz; ++p) {
             const int c = A.col[p];
             if ((unsigned)c < (unsigned)A.n) colcnt[(size_t)c]++;
         }
-        for (int64_t p = 0; p < A.nnz; ++p) {
-            const int c = A.col[p];
-            if ((unsigned)c < (unsigned)A.n) cub += colcnt[(size_t)c];
-        }
-    } else {
-        const tsg_csr &Bm = (op == TSG_OP_AB && B) ? *B : A;
-        for (int64_t p = 0; p < A.nnz; ++p) {
-            const int c = A.col[p];
-            if ((unsigned)c < (unsigned)Bm.m) cub += rowptr_at(Bm, c + 1) - rowptr_at(Bm, c);
-        }
     }
-    const int64_t n = (op == TSG_OP_AB && B) ? B->n : (op == TSG_OP_AA ? A.n : A.m);
-    const int64_t dense = (int64_t)A.m * (n > 0 ? n : 1);
-    const int64_t cmax = cub < dense ? cub : dense;
+    const tsg_csr &Bm = (op == TSG_OP_AB && B) ? *B : A;
+    for (int i = 0; i < A.m; ++i) {
+        int64_t row = 0;
+        for (int64_t p = rowptr_at(A, i); p < rowptr_at(A, i + 1); ++p) {
+            const int c = A.col[p];
+            if (op == TSG_OP_AAT) {
+                if ((unsigned)c < (unsigned)A.n) row += colcnt[(size_t)c];
+            } else if ((unsigned)c < (unsigned)Bm.m) {
+                row += rowptr_at(Bm, c + 1) - rowptr_at(Bm, c);
+            }
+        }
+        cmax += row < n ? row : n;
+    }
     const int64_t opnd = 24 * (A.nnz + ((op == TSG_OP_AB && B) ? B->nnz : A.nnz)) + 32ll * (A.m + A.n + 2);
     return opnd + 12 * cmax + 48 * cmax / 8 + 16ll * (A.m + 1) + (1 << 20);
 }

@@ -139,3 +139,31 @@ def transpose(A: CSR) -> CSR:
     import scipy.sparse as sp
     s = sp.csr_matrix((A.val, A.col, A.rowptr), shape=(A.m, A.n)).T.tocsr()
     return CSR.from_scipy(s)
+
+
+def batch_instance(i: int, seed: int = 1, n_range=(64, 16384), nnz_range=(2, 64)) -> CSR:
+    """Instance i of the batched workload: n log-uniform in n_range, nnz/row
+    uniform in nnz_range (drawn once per instance), columns banded
+    (|i-j| <= n/16, bandwidth n/8) for even i and uniform for odd i,
+    duplicates merged, values uniform in [-1, 1]."""
+    rng = _rng(seed * 1_000_003 + i)
+    n = int(round(np.exp(rng.uniform(np.log(n_range[0]), np.log(n_range[1])))))
+    k = int(rng.integers(nnz_range[0], nnz_range[1] + 1))
+    k = min(k, n)
+    rows = np.arange(n, dtype=np.int64)[:, None]
+    if i % 2 == 0:
+        half = max(1, n // 16)
+        lo = np.maximum(rows - half, 0)
+        hi = np.minimum(rows + half, n - 1)
+        cols = lo + np.floor(rng.random((n, k)) * (hi - lo + 1)).astype(np.int64)
+    else:
+        cols = rng.integers(0, n, size=(n, k))
+    cols.sort(axis=1)
+    keep = np.ones_like(cols, dtype=bool)
+    keep[:, 1:] = cols[:, 1:] != cols[:, :-1]
+    counts = keep.sum(axis=1)
+    rp = np.zeros(n + 1, dtype=np.int64)
+    np.cumsum(counts, out=rp[1:])
+    col = cols[keep].astype(np.int32)
+    val = rng.uniform(-1.0, 1.0, size=col.size)
+    return CSR(n, n, rp, col, val)

@@ -20,7 +20,7 @@ import time
 import numpy as np
 
 from . import _abi
-from ._abi import check, lib
+from ._abi import TSGError, check, lib
 from .api import CSR, _download
 
 _OPS = {"AB": _abi.OP_AB, "AA": _abi.OP_AA, "AAT": _abi.OP_AAT}
@@ -52,16 +52,20 @@ class Server:
             self._keep[rid.value] = [ka, kb]       # operands must outlive the request
         return rid.value
 
-    def wait(self, rid: int) -> tuple[CSR, dict]:
+    def wait(self, rid: int, download: bool = True) -> tuple[CSR | None, dict]:
+        """Result of request `rid` (a host CSR; None with download=False,
+        which only releases it) and its timing record."""
         c = _abi.tsg_csr()
         info = _abi.tsg_server_result()
         st = lib().tsg_server_wait(self.handle, C.c_int64(rid), C.byref(c), C.byref(info))
         with self._lock:
             self._keep.pop(rid, None)
         check(st)
-        res = _download(None, c)
+        d = info.as_dict()
+        d["nnz"] = int(c.nnz)
+        res = _download(None, c) if download else None
         lib().tsg_csr_free(None, C.byref(c))
-        return res, info.as_dict()
+        return res, d
 
     def close(self) -> None:
         if self.handle:
@@ -75,61 +79,101 @@ class Server:
         self.close()
 
 
-def make_stream(n_requests: int, seed: int = 1, rate: float = 2000.0, repeat_frac: float = 0.3,
-                lap_side=(32, 512), rmat_scale=(12, 18), rmat_edge=(8, 32)):
-    """The seeded request stream: list of dicts (t_arrival, A, op, key, kind)."""
+def _build_request(spec: dict) -> CSR:
+    """Matrix of one stream request from its drawn spec (runs in a worker process)."""
     from . import matrices as M
+    vr = np.random.Generator(np.random.Philox(spec["vseed"]))
+    if spec["kind"].startswith("lap"):
+        A = M.laplacian_2d(spec["side"])
+    else:
+        A = M.rmat(spec["scale"], spec["ef"], seed=spec["mseed"])
+    return CSR(A.m, A.n, A.rowptr, A.col, vr.uniform(-1.0, 1.0, A.nnz))
+
+
+def make_stream(n_requests: int, seed: int = 1, rate: float = 2000.0, repeat_frac: float = 0.3,
+                lap_side=(32, 512), rmat_scale=(12, 18), rmat_edge=(8, 32), procs: int = 0):
+    """The seeded request stream: list of dicts (t, A, op, key, kind).
+
+    Arrival gaps are exponential (Poisson arrivals at `rate`/s).  With
+    probability `repeat_frac` a request repeats an earlier request's pattern
+    (same key) with new values; otherwise it is a fresh 2D Laplacian or R-MAT
+    operand, A*A or A*A^T with equal odds.  All draws are made first, in one
+    sequential pass; the operands are then built, in `procs` spawned worker
+    processes when procs > 1 (start those before the first GPU call)."""
     rng = np.random.Generator(np.random.Philox(seed))
     t = 0.0
-    reqs = []
+    specs = []
     for i in range(n_requests):
         t += rng.exponential(1.0 / rate)
-        if reqs and rng.random() < repeat_frac:
-            base = reqs[int(rng.integers(0, len(reqs)))]
-            A0 = base["A"]
-            A = CSR(A0.m, A0.n, A0.rowptr, A0.col, rng.uniform(-1.0, 1.0, A0.nnz))
-            reqs.append(dict(t=t, A=A, op=base["op"], key=base["key"], kind=base["kind"] + "-repeat"))
+        vseed = int(rng.integers(1, 2 ** 62))
+        if specs and rng.random() < repeat_frac:
+            base = specs[int(rng.integers(0, len(specs)))]
+            specs.append(dict(base, t=t, vseed=vseed, kind=base["kind"].replace("-repeat", "") + "-repeat"))
             continue
         op = "AA" if rng.random() < 0.5 else "AAT"
         if rng.random() < 0.5:
             side = int(rng.integers(lap_side[0], lap_side[1] + 1))
-            A = M.laplacian_2d(side)
-            A = CSR(A.m, A.n, A.rowptr, A.col, rng.uniform(-1.0, 1.0, A.nnz))
-            kind = f"lap{side}"
+            specs.append(dict(t=t, vseed=vseed, op=op, key=i + 1, kind=f"lap{side}", side=side))
         else:
             scale = int(rng.integers(rmat_scale[0], rmat_scale[1] + 1))
             ef = int(rng.integers(rmat_edge[0], rmat_edge[1] + 1))
-            A = M.rmat(scale, ef, seed=int(rng.integers(1, 2 ** 31)))
-            kind = f"rmat{scale}x{ef}"
-        reqs.append(dict(t=t, A=A, op=op, key=i + 1, kind=kind))
-    return reqs
+            specs.append(dict(t=t, vseed=vseed, op=op, key=i + 1, kind=f"rmat{scale}x{ef}", scale=scale, ef=ef,
+                              mseed=int(rng.integers(1, 2 ** 31))))
+    if procs > 1 and len(specs) > 1:
+        import multiprocessing as mp
+        with mp.get_context("spawn").Pool(procs) as pool:
+            mats = pool.map(_build_request, specs, chunksize=1)
+    else:
+        mats = [_build_request(sp) for sp in specs]
+    return [dict(t=sp["t"], A=A, op=sp["op"], key=sp["key"], kind=sp["kind"]) for sp, A in zip(specs, mats)]
 
 
-def run_stream(srv: Server, reqs: list, realtime: bool = True) -> dict:
-    """Submit the stream at its arrival times; collect results and latencies."""
+def run_stream(srv: Server, reqs: list, realtime: bool = True, download: bool = True) -> dict:
+    """Submit the stream at its arrival times; collect results and latencies.
+
+    A request the budget refuses at submission (TSG_ERR_BUDGET) is counted
+    in `refused` and has no latency; other errors propagate."""
     ids = [None] * len(reqs)
     results = [None] * len(reqs)
+    errors: list = []
     t0 = time.perf_counter()
 
     def collector():
-        for i in range(len(reqs)):
-            while ids[i] is None:
-                time.sleep(0.0001)
-            C_, info = srv.wait(ids[i])
-            results[i] = (C_, info)
+        try:
+            for i in range(len(reqs)):
+                while ids[i] is None:
+                    time.sleep(0.0001)
+                if ids[i] < 0:
+                    continue
+                results[i] = srv.wait(ids[i], download=download)
+        except BaseException as e:   # surfaced after join
+            errors.append(e)
 
     th = threading.Thread(target=collector)
     th.start()
-    for i, r in enumerate(reqs):
-        if realtime:
-            dt = r["t"] - (time.perf_counter() - t0)
-            if dt > 0:
-                time.sleep(dt)
-        ids[i] = srv.submit(r["A"], op=r["op"], key=r["key"])
-    th.join()
+    try:
+        for i, r in enumerate(reqs):
+            if realtime:
+                dt = r["t"] - (time.perf_counter() - t0)
+                if dt > 0:
+                    time.sleep(dt)
+            try:
+                ids[i] = srv.submit(r["A"], op=r["op"], key=r["key"])
+            except TSGError as e:
+                if e.status != _abi.ERR_BUDGET:
+                    raise
+                ids[i] = -1
+    finally:
+        for i in range(len(ids)):
+            if ids[i] is None:
+                ids[i] = -1
+        th.join()
+    if errors:
+        raise errors[0]
     wall = time.perf_counter() - t0
-    lat = np.array([res[1]["latency_ms"] for res in results])
-    flops = 0.0
-    return dict(n=len(reqs), wall_s=wall, throughput_rps=len(reqs) / wall, p50_ms=float(np.percentile(lat, 50)),
+    done = [res for res in results if res is not None]
+    lat = np.array([res[1]["latency_ms"] for res in done]) if done else np.zeros(1)
+    return dict(n=len(reqs), completed=len(done), refused=sum(1 for x in ids if x < 0), wall_s=wall,
+                throughput_rps=len(done) / wall, p50_ms=float(np.percentile(lat, 50)),
                 p99_ms=float(np.percentile(lat, 99)), mean_ms=float(lat.mean()),
-                numeric_only=int(sum(res[1]["numeric_only"] for res in results)), flops=flops, results=results)
+                numeric_only=int(sum(res[1]["numeric_only"] for res in done)), results=results)
