@@ -296,6 +296,25 @@ tsg_status tsg_spgemm_tiles(tsg_ctx *ctx, tsg_op op, const tsg_csr *A, const tsg
 /* Tile form -> CSR (device), the tile -> CSR output step. */
 tsg_status tsg_tiles_to_csr(tsg_ctx *ctx, const tsg_tiles *T, tsg_csr *C);
 
+/* Largest row count tsg_tiles_to_csr_noalloc accepts (its static scratch is
+ * about 4 MiB per device). */
+#define TSG_NOALLOC_MAX_ROWS 1048576
+
+/* tsg_tiles_to_csr for callers that cannot allocate: no counterpart in the
+ * reference.  T is device tile form (from tsg_csr_to_tiles or
+ * tsg_spgemm_tiles); row_ptr (m+1 int64), col and val (T->nnz each) are
+ * caller-provided device memory of ctx's device, and the result is the one
+ * tsg_tiles_to_csr gives.  The call allocates no device or pinned memory: its
+ * scratch (row counts, scan look-back state, error flags) is one static
+ * device array, cleared at the start of every call.  T->m above
+ * TSG_NOALLOC_MAX_ROWS is refused with TSG_ERR_NOT_SUPPORTED.  The first call
+ * on a device looks up the array's address (cudaGetSymbolAddress); make it
+ * before any stream capture.  All contexts of a device share the array, so
+ * calls that overlap in time (other threads or streams) race: serialize them.
+ * Returns after the result is complete (it waits on ctx's stream). */
+tsg_status tsg_tiles_to_csr_noalloc(tsg_ctx *ctx, const tsg_tiles *T, int64_t *row_ptr, int32_t *col,
+                                    double *val);
+
 tsg_status tsg_tiles_free(tsg_ctx *ctx, tsg_tiles *T);
 
 /* Copy a tile matrix's arrays to caller-provided host buffers (sizes from T). */

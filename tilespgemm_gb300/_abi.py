@@ -24,6 +24,9 @@ ERR_BAD_INPUT = 8
 ERR_NOT_SUPPORTED = 9
 ERR_BUDGET = 10
 
+# largest row count of tsg_tiles_to_csr_noalloc
+NOALLOC_MAX_ROWS = 1 << 20
+
 STATUS_NAMES = {
     0: "TSG_OK", 1: "TSG_ERR_INVALID_ARG", 2: "TSG_ERR_CUDA", 3: "TSG_ERR_OOM",
     4: "TSG_ERR_INT32_OVERFLOW", 5: "TSG_ERR_BAD_MTX", 6: "TSG_ERR_DEVICE_TIMEOUT",
@@ -124,6 +127,7 @@ SIGNATURES = {
                                    C.POINTER(tsg_tiles), C.POINTER(tsg_stats)]),
     "tsg_tiles_to_csr": (C.c_int, [C.c_void_p, C.POINTER(tsg_tiles), C.POINTER(tsg_csr)]),
     "tsg_tiles_free": (C.c_int, [C.c_void_p, C.POINTER(tsg_tiles)]),
+    "tsg_tiles_to_csr_noalloc": (C.c_int, [C.c_void_p, C.POINTER(tsg_tiles), C.c_void_p, C.c_void_p, C.c_void_p]),
     "tsg_tiles_download": (C.c_int, [C.c_void_p, C.POINTER(tsg_tiles), C.c_void_p, C.c_void_p, C.c_void_p,
                                      C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "tsg_csr_download": (C.c_int, [C.c_void_p, C.POINTER(tsg_csr), C.c_void_p, C.c_void_p, C.c_void_p]),

@@ -50,6 +50,14 @@ cudaError_t fp64_peak(cudaStream_t s, cudaEvent_t e0, cudaEvent_t e1, double *gf
 cudaError_t csr_from_tiles(Pool &pool, int m, const long long *brp, const int *bcol, const long long *nnzb,
                            const uint8_t *ptr, const uint8_t *lcol, const double *tval, long long *rowptr, int *col,
                            double *val, int *flags, bool fill);
+cudaError_t csr_rowcnt_from_tiles(cudaStream_t s, int m, const long long *brp, const long long *nnzb,
+                                  const uint8_t *ptr, int *rowcnt);
+cudaError_t csr_fill_from_tiles(cudaStream_t s, int m, const long long *brp, const int *bcol, const long long *nnzb,
+                                const uint8_t *ptr, const uint8_t *lcol, const double *tval, const long long *rowptr,
+                                int *col, double *val);
+long long scan_status_words(long long n);
+cudaError_t scan_i32_to_i64_in(cudaStream_t s, const int *in, long long *out, long long n, int *flags,
+                               unsigned *ticket, unsigned long long *status);
 }  // namespace tsg
 
 using namespace tsg;
@@ -1328,6 +1336,117 @@ tsg_status tsg_spgemm_batched(tsg_ctx *ctx, tsg_op op, int32_t count, const tsg_
         st->ms_total = ms_since(t0);
         phase_times(ctx, st, tm);
     }
+    return TSG_OK;
+}
+
+}  // extern "C"
+
+// ---- tile form -> CSR without allocation -----------------------------------
+//
+// tsg_tiles_to_csr_noalloc runs the two passes of tsg_tiles_to_csr (row counts
+// and their scan, then the fill) with its scratch in one file-scope device
+// array instead of the context's pool, and writes into caller buffers.
+// Scratch layout (bytes), sized for TSG_NOALLOC_MAX_ROWS rows:
+//   [0, 32)        device error flags (FLAG_COUNT int32)
+//   [128, 132)     scan ticket
+//   [256, 4352)    scan look-back status, one uint64 per 2048 rows
+//   [4352, ...)    row counts, int32, one per row
+namespace {
+
+constexpr long long NA_FLAGS_OFF = 0;
+constexpr long long NA_TICKET_OFF = 128;
+constexpr long long NA_STATUS_OFF = 256;
+constexpr long long NA_STATUS_BYTES = 8ll * ((TSG_NOALLOC_MAX_ROWS + 2047) / 2048);
+constexpr long long NA_ROWCNT_OFF = NA_STATUS_OFF + NA_STATUS_BYTES;
+constexpr long long NA_SCRATCH_BYTES = (NA_ROWCNT_OFF + 4ll * (TSG_NOALLOC_MAX_ROWS + 1) + 255) / 256 * 256;
+static_assert(NA_ROWCNT_OFF % 256 == 0, "row counts start on a 256-byte boundary");
+static_assert(FLAG_COUNT * 4 <= NA_TICKET_OFF, "flags fit before the ticket");
+
+constexpr int NA_MAX_DEVICES = 64;
+std::mutex g_na_mu;
+char *g_na_addr[NA_MAX_DEVICES] = {};
+
+}  // namespace
+
+static __device__ __align__(256) unsigned char tsg_noalloc_scratch[NA_SCRATCH_BYTES];
+
+namespace {
+
+// Device address of the scratch array on `device` (current), resolved once
+// per device with cudaGetSymbolAddress and kept.
+tsg_status noalloc_scratch(int device, char **out)
+{
+    if (device < 0 || device >= NA_MAX_DEVICES) return fail(TSG_ERR_NOT_SUPPORTED, "device %d: no-alloc scratch covers devices 0-%d", device, NA_MAX_DEVICES - 1);
+    std::lock_guard<std::mutex> lk(g_na_mu);
+    if (!g_na_addr[device]) {
+        void *p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, tsg_noalloc_scratch);
+        if (e != cudaSuccess || !p) {
+            cudaGetLastError();
+            return fail(TSG_ERR_CUDA, "cudaGetSymbolAddress(no-alloc scratch) on device %d: %s", device,
+                        cudaGetErrorString(e));
+        }
+        g_na_addr[device] = static_cast<char *>(p);
+    }
+    *out = g_na_addr[device];
+    return TSG_OK;
+}
+
+bool is_device_pointer(const void *p)
+{
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) { cudaGetLastError(); return false; }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+}  // namespace
+
+extern "C" {
+
+tsg_status tsg_tiles_to_csr_noalloc(tsg_ctx *ctx, const tsg_tiles *T, int64_t *row_ptr, int32_t *col, double *val)
+{
+    if (!ctx || !T || !row_ptr) return fail(TSG_ERR_INVALID_ARG, "ctx/T/row_ptr is NULL");
+    if (T->m < 0 || T->n < 0 || T->nnz < 0 || T->numblk < 0) return fail(TSG_ERR_INVALID_ARG, "T has a negative size");
+    if (T->m > TSG_NOALLOC_MAX_ROWS)
+        return fail(TSG_ERR_NOT_SUPPORTED,
+                    "tsg_tiles_to_csr_noalloc: T has %d rows, more than its static scratch holds "
+                    "(TSG_NOALLOC_MAX_ROWS = %d); use tsg_tiles_to_csr", T->m, TSG_NOALLOC_MAX_ROWS);
+    if (T->blkm != (T->m + TILE - 1) / TILE) return fail(TSG_ERR_INVALID_ARG, "T->blkm is not ceil(m/16)");
+    if (T->m > 0 && (!T->blkrowptr || !T->nnzb || !T->ptr)) return fail(TSG_ERR_INVALID_ARG, "T's tile arrays are NULL");
+    if (T->nnz > 0 && (!T->blkcolidx || !T->col || !T->val)) return fail(TSG_ERR_INVALID_ARG, "T's entry arrays are NULL");
+    if (T->nnz > 0 && (!col || !val)) return fail(TSG_ERR_INVALID_ARG, "col/val is NULL for %lld entries", (long long)T->nnz);
+    CUDA_OK(cudaSetDevice(ctx->device));
+    if (!is_device_pointer(row_ptr) || (T->nnz > 0 && (!is_device_pointer(col) || !is_device_pointer(val))))
+        return fail(TSG_ERR_INVALID_ARG, "row_ptr/col/val must be device memory");
+    char *scr = nullptr;
+    tsg_status r = noalloc_scratch(ctx->device, &scr);
+    if (r) return r;
+    const long long words = scan_status_words(T->m);
+    if (8 * words > NA_STATUS_BYTES) return fail(TSG_ERR_CUDA, "no-alloc scan status does not fit its scratch");
+    int *flags = reinterpret_cast<int *>(scr + NA_FLAGS_OFF);
+    unsigned *ticket = reinterpret_cast<unsigned *>(scr + NA_TICKET_OFF);
+    unsigned long long *status = reinterpret_cast<unsigned long long *>(scr + NA_STATUS_OFF);
+    int *rowcnt = reinterpret_cast<int *>(scr + NA_ROWCNT_OFF);
+    cudaStream_t s = ctx->stream;
+    // flags, ticket and look-back status start at zero; the count pass writes every row count
+    CUDA_OK(cudaMemsetAsync(scr, 0, (size_t)(NA_STATUS_OFF + 8 * words), s));
+    const long long *brp = reinterpret_cast<const long long *>(T->blkrowptr);
+    const long long *nnzb = reinterpret_cast<const long long *>(T->nnzb);
+    long long *rp = reinterpret_cast<long long *>(row_ptr);
+    CUDA_OK(csr_rowcnt_from_tiles(s, T->m, brp, nnzb, T->ptr, rowcnt));
+    CUDA_OK(scan_i32_to_i64_in(s, rowcnt, rp, T->m, flags, ticket, status));
+    long long total = 0;
+    int hflags[FLAG_COUNT];
+    CUDA_OK(cudaMemcpyAsync(&total, rp + T->m, sizeof(total), cudaMemcpyDeviceToHost, s));
+    CUDA_OK(cudaMemcpyAsync(hflags, flags, sizeof(hflags), cudaMemcpyDeviceToHost, s));
+    CUDA_OK(cudaStreamSynchronize(s));
+    if (hflags[FLAG_TIMEOUT]) return fail(TSG_ERR_DEVICE_TIMEOUT, "a bounded device wait gave up");
+    if (hflags[FLAG_INTERNAL] || hflags[FLAG_OVERFLOW]) return fail(TSG_ERR_CUDA, "internal bound check failed on the device");
+    // the fill writes exactly `total` entries: it must be the size of the caller's col/val
+    if (total != T->nnz)
+        return fail(TSG_ERR_BAD_INPUT, "T's tiles hold %lld entries but T->nnz is %lld", total, (long long)T->nnz);
+    CUDA_OK(csr_fill_from_tiles(s, T->m, brp, T->blkcolidx, nnzb, T->ptr, T->col, T->val, rp, col, val));
+    CUDA_OK(cudaStreamSynchronize(s));
     return TSG_OK;
 }
 

@@ -423,6 +423,23 @@ cudaError_t tiles_payload_a(Pool &pool, int m, int n, const long long *rp, const
     return e;
 }
 
+// The two passes of csr_from_tiles as separate launches on `s`, into
+// caller-provided row counts (m entries) and outputs; they allocate nothing.
+cudaError_t csr_rowcnt_from_tiles(cudaStream_t s, int m, const long long *brp, const long long *nnzb,
+                                  const uint8_t *ptr, int *rowcnt)
+{
+    if (m > 0) { k_csr_rowcnt_from_tiles<<<(unsigned)((m + 7) / 8), 256, 0, s>>>(m, brp, nnzb, ptr, rowcnt); ::tsg::count_launch(); }
+    return cudaGetLastError();
+}
+
+cudaError_t csr_fill_from_tiles(cudaStream_t s, int m, const long long *brp, const int *bcol, const long long *nnzb,
+                                const uint8_t *ptr, const uint8_t *lcol, const double *tval, const long long *rowptr,
+                                int *col, double *val)
+{
+    if (m > 0) { k_csr_fill_from_tiles<<<(unsigned)((m + 7) / 8), 256, 0, s>>>(m, brp, bcol, nnzb, ptr, lcol, tval, rowptr, col, val); ::tsg::count_launch(); }
+    return cudaGetLastError();
+}
+
 cudaError_t csr_from_tiles(Pool &pool, int m, const long long *brp, const int *bcol, const long long *nnzb,
                            const uint8_t *ptr, const uint8_t *lcol, const double *tval, long long *rowptr, int *col,
                            double *val, int *flags, bool fill)

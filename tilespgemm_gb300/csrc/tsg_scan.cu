@@ -152,4 +152,22 @@ cudaError_t scan_i32_to_i32(Pool &pool, const int *in, int *out, long long n, in
 cudaError_t scan_i64_to_i64(Pool &pool, const long long *in, long long *out, long long n, int *flags)
 { return scan_impl<long long, long long>(pool, in, out, n, flags); }
 
+long long scan_status_words(long long n) { return n > 0 ? (n + SCAN_TILE - 1) / SCAN_TILE : 0; }
+
+// The same scan with its look-back state in caller-provided device memory:
+// `ticket` (one word) and `status` (scan_status_words(n) words), both zero on
+// entry.  Allocates nothing.
+cudaError_t scan_i32_to_i64_in(cudaStream_t s, const int *in, long long *out, long long n, int *flags,
+                               unsigned *ticket, unsigned long long *status)
+{
+    if (n <= 0) {
+        { k_scan_empty<long long><<<1, 1, 0, s>>>(out); ::tsg::count_launch(); }
+        return cudaGetLastError();
+    }
+    const long long tiles = scan_status_words(n);
+    if (tiles > (1ll << 30)) return cudaErrorInvalidValue;
+    { k_scan<int, long long><<<(unsigned)tiles, SCAN_THREADS, 0, s>>>(in, out, n, status, ticket, flags); ::tsg::count_launch(); }
+    return cudaGetLastError();
+}
+
 }  // namespace tsg
