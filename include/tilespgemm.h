@@ -86,6 +86,8 @@ typedef struct {
                                 16x16 accumulator (default 160; 257 = never) */
     int32_t smem_acc_max;    /* largest C tile-row (in entries) accumulated in shared memory (default 24576) */
     int32_t threads_numeric; /* threads per CTA of the numeric kernels: 128, 256 or 512 (default 256) */
+    int32_t row_acc_max;     /* larger tile-rows: largest C row (entries) accumulated in shared memory by the
+                                one-row-per-CTA kernel; longer rows accumulate in C's value array (default 65535) */
 } tsg_opts;
 
 /* Per-call statistics.  Sizes are always filled; times only with phase_times. */
@@ -100,7 +102,7 @@ typedef struct {
     double ms_step3;           /* numeric + CSR write */
     double ms_h2d, ms_d2h;     /* host <-> device copies (host operands only) */
     int32_t n_syncs;           /* host waits on the device inside the call */
-    int32_t bins[4];           /* C tile-rows per numeric bin: empty, shared sparse, shared dense, global */
+    int32_t bins[4];           /* C tile-rows per numeric bin: empty, shared sparse, shared dense, per-row or global */
 } tsg_stats;
 
 typedef struct tsg_ctx tsg_ctx;

@@ -120,11 +120,11 @@ def test_general_ab_rectangular(ctx):
     check_against_oracle(C, A, B)
 
 
-@pytest.mark.parametrize("opts", [dict(smem_acc_max=0), dict(dense_tile_min=1), dict(threads_numeric=128),
-                                  dict(threads_numeric=512), dict(out_rowptr_bits=64)])
+@pytest.mark.parametrize("opts", [dict(smem_acc_max=0), dict(smem_acc_max=0, row_acc_max=0), dict(dense_tile_min=1),
+                                  dict(threads_numeric=128), dict(threads_numeric=512), dict(out_rowptr_bits=64)])
 def test_numeric_bins_agree(opts, built_lib):
-    """Every accumulator path (shared sparse, shared dense, global) gives the
-    same bits."""
+    """Every accumulator path (shared sparse, shared dense, one row per CTA,
+    global) gives the same bits."""
     from tilespgemm_gb300 import Context
     from tilespgemm_gb300 import matrices as M
     A = M.stencil_27(12, seed=4)
@@ -140,6 +140,20 @@ def test_numeric_bins_agree(opts, built_lib):
                 assert st["bins"][2] > 0
             if opts.get("out_rowptr_bits") == 64:
                 assert C.rowptr.dtype == np.int64
+
+
+@pytest.mark.parametrize("opts", [dict(), dict(row_acc_max=0)])
+def test_long_rows(opts, built_lib):
+    """C rows of ~3,900 and ~8,400 entries: the medium and large size classes
+    of the one-row-per-CTA kernel (and, with row_acc_max=0, the global
+    accumulator), bit-exact against the oracle."""
+    from tilespgemm_gb300 import Context
+    from tilespgemm_gb300 import matrices as M
+    with Context(0, **opts) as c:
+        for X in (M.random_sparse(6000, 6000, 80, seed=31), M.random_sparse(12000, 12000, 120, seed=32)):
+            C, st = c.spgemm(X, op="AA", stats=True)
+            assert st["bins"][3] > 0
+            check_against_oracle(C, X, X)
 
 
 def test_device_inputs_and_outputs(ctx):

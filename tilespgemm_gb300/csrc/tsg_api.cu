@@ -287,6 +287,7 @@ struct PlanData {
     uint16_t *cmask = nullptr;
     long long *rowptrC = nullptr;
     unsigned char *bin = nullptr;
+    int *binlist = nullptr;                        // tile-rows of each bin, NBIN * blkm
     int *offC = nullptr;
     long long counts[NBIN] = {}, req[NBIN] = {};
     bool dupsafe = false;
@@ -306,7 +307,7 @@ struct PlanData {
     }
     long long device_bytes() const {
         return 8ll * (m + 1) * 2 + 4ll * (nnzA + nnzB) + 8ll * (nnzA + nnzB) + 8ll * (blkm + 1) +
-               36ll * numblkC + 8ll * (m + 1) + (counts[BIN_GLOBAL] ? 64ll * numblkC : 0);
+               36ll * numblkC + 8ll * (m + 1) + 4ll * NBIN * blkm + (counts[BIN_GLOBAL] ? 64ll * numblkC : 0);
     }
 };
 
@@ -448,15 +449,16 @@ tsg_status plan_symbolic(tsg_ctx *ctx, Pool &pool, Scratch &sc, tsg_op op, const
     P.cmask = P.own<uint16_t>(pool, P.numblkC * TILE + 2);
     int *rowcnt = sc.get<int>(P.m + 1);
     P.bin = P.own<unsigned char>(pool, P.blkm + 1);
+    P.binlist = P.own<int>(pool, (long long)NBIN * P.blkm);
     P.rowptrC = P.own<long long>(pool, P.m + 1);
-    if (!P.ccol || !P.cmask || !rowcnt || !P.bin || !P.rowptrC)
+    if (!P.ccol || !P.cmask || !rowcnt || !P.bin || !P.binlist || !P.rowptrC)
         return fail(TSG_ERR_OOM, "device pool allocation failed for C tiles");
-    NumericBinParams bp{ctx->opts.dense_tile_min, ctx->opts.smem_acc_max};
+    NumericBinParams bp{ctx->opts.dense_tile_min, ctx->opts.smem_acc_max, ctx->opts.row_acc_max};
     CUDA_OK(symbolic_fill_fused(pool, TA, TB, P.m, P.crp, P.ccol, P.cmask, rowcnt, P.bin, bp, ctx->dstat + ST_BINS,
-                                cnt, wide, ctx->dflags));
+                                P.binlist, cnt, wide, ctx->dflags, P.rpB, P.colB));
     tm.mark();  // 2
     CUDA_OK(step2_masks(pool, TA, TB, P.m, P.blkm, P.crp, P.ccol, P.cmask, rowcnt, maxS, maxSpan, bp, P.bin,
-                        ctx->dstat + ST_BINS, ctx->dflags, defer, ndefer));
+                        ctx->dstat + ST_BINS, P.binlist, ctx->dflags, defer, ndefer, P.rpB, P.colB));
     CUDA_OK(scan_i32_to_i64(pool, rowcnt, P.rowptrC, P.m, ctx->dflags));
     CUDA_OK(cudaMemcpyAsync(ctx->dstat + ST_NNZC, P.rowptrC + P.m, sizeof(long long), cudaMemcpyDeviceToDevice,
                             ctx->stream));
@@ -477,7 +479,7 @@ tsg_status plan_symbolic(tsg_ctx *ctx, Pool &pool, Scratch &sc, tsg_op op, const
 
 // Numeric phase into caller-provided col/val (nnzC each).
 tsg_status plan_numeric(tsg_ctx *ctx, Pool &pool, PlanData &P, const double *valA, const double *valB, int *col,
-                        double *val)
+                        double *val, const int *tr_coloff = nullptr)
 {
     NumericArgs na{};
     na.m = P.m; na.blkm = P.blkm;
@@ -485,7 +487,7 @@ tsg_status plan_numeric(tsg_ctx *ctx, Pool &pool, PlanData &P, const double *val
     na.rpB = P.rpB; na.colB = P.colB; na.valB = valB;
     na.crp = P.crp; na.ccol = P.ccol; na.cmask = P.cmask;
     na.rowptrC = P.rowptrC; na.colC = col; na.valC = val;
-    na.bin = P.bin; na.offC = P.offC; na.flags = ctx->dflags;
+    na.bin = P.bin; na.binlist = P.binlist; na.tr_coloff = tr_coloff; na.offC = P.offC; na.flags = ctx->dflags;
     CUDA_OK(numeric_run(pool, na, P.counts, P.req, P.dupsafe, ctx->opts.threads_numeric));
     return TSG_OK;
 }
@@ -500,7 +502,7 @@ void fill_stats(const PlanData &P, tsg_stats *st)
     st->bins[0] = (int)P.counts[BIN_EMPTY];
     st->bins[1] = (int)(P.counts[BIN_SPARSE_S] + P.counts[BIN_SPARSE_L]);
     st->bins[2] = (int)(P.counts[BIN_DENSE_S] + P.counts[BIN_DENSE_L]);
-    st->bins[3] = (int)P.counts[BIN_GLOBAL];
+    st->bins[3] = (int)(P.counts[BIN_ROWS_S] + P.counts[BIN_ROWS_M] + P.counts[BIN_ROWS_L] + P.counts[BIN_GLOBAL]);
 }
 
 // Hand C (rowptr copied/narrowed from `rowptr`, col/val adopted) to the
@@ -601,6 +603,7 @@ void tsg_opts_default(tsg_opts *o)
     o->dense_tile_min = 160;
     o->smem_acc_max = 24576;
     o->threads_numeric = 256;
+    o->row_acc_max = 65535;
 }
 
 const char *tsg_last_error(void) { return g_err.c_str(); }
@@ -1230,21 +1233,30 @@ tsg_status tsg_spgemm_batched(tsg_ctx *ctx, tsg_op op, int32_t count, const tsg_
         if (!r && op == TSG_OP_AB) r = pack_operands(ctx, pool, sc, count, B, koff, noff, K, N, pB);
         if (!r) r = plan_symbolic(ctx, pool, sc, op, &pA, op == TSG_OP_AB ? &pB : nullptr, P, false, st != nullptr, tm,
                                   false);
-        if (!r) {
-            col = pool.alloc_n<int>(P.nnzC);
-            val = pool.alloc_n<double>(P.nnzC);
-            if (!col || !val) r = fail(TSG_ERR_OOM, "device pool allocation failed for C (%lld entries)", P.nnzC);
-        }
-        if (!r) r = plan_numeric(ctx, pool, P, P.valA, P.valB, col, val);
-        tm.mark();  // 4
-        // unpack: per-instance row pointers (rebased) and columns (rebased in place)
+        // C's column offset of each packed tile-row's instance: the numeric
+        // step writes C_i's columns already rebased
         long long rpn = 0;
         std::vector<UnpackDesc> ud(count);
+        std::vector<int> trc((size_t)(M / TILE) + 1, 0);
         for (int i = 0; i < count; ++i) {
             ud[i].rowoff = roff[i]; ud[i].m = A[i].m;
             ud[i].coloff = op == TSG_OP_AAT ? roff[i] : noff[i];
             ud[i].rpoff = rpn; rpn += A[i].m + 1;
+            for (long long t = roff[i] / TILE; t < (roff[i] + round16(A[i].m)) / TILE; ++t) trc[(size_t)t] = (int)ud[i].coloff;
         }
+        int *d_trc = nullptr;
+        if (!r) {
+            col = pool.alloc_n<int>(P.nnzC);
+            val = pool.alloc_n<double>(P.nnzC);
+            d_trc = sc.get<int>((long long)trc.size());
+            if (!col || !val || !d_trc) r = fail(TSG_ERR_OOM, "device pool allocation failed for C (%lld entries)", P.nnzC);
+        }
+        if (!r) {
+            CUDA_OK(cudaMemcpyAsync(d_trc, trc.data(), sizeof(int) * trc.size(), cudaMemcpyHostToDevice, ctx->stream));
+            r = plan_numeric(ctx, pool, P, P.valA, P.valB, col, val, d_trc);
+        }
+        tm.mark();  // 4
+        // unpack: per-instance row pointers, rebased
         int bits = ctx->opts.out_rowptr_bits;
         if (bits == 0) bits = P.nnzC < (1ll << 31) ? 32 : 64;
         if (!r && bits == 32 && P.nnzC >= (1ll << 31)) r = fail(TSG_ERR_INT32_OVERFLOW, "batch C needs int64 row pointers");
@@ -1257,7 +1269,7 @@ tsg_status tsg_spgemm_batched(tsg_ctx *ctx, tsg_op op, int32_t count, const tsg_
             if (!rp_out || !ebase || !dud) r = fail(TSG_ERR_OOM, "device pool allocation failed (batch outputs)");
             if (!r) {
                 CUDA_OK(cudaMemcpyAsync(dud, ud.data(), sizeof(UnpackDesc) * (size_t)count, cudaMemcpyHostToDevice, ctx->stream));
-                CUDA_OK(batch_unpack(pool, dud, count, P.rowptrC, col, rp_out, bits, ebase));
+                CUDA_OK(batch_unpack(pool, dud, count, P.rowptrC, rp_out, bits, ebase));
             }
         }
         std::vector<long long> eb(count);

@@ -286,18 +286,16 @@ k_batch_pack(const PackDesc *__restrict__ descs, long long *rp, int *col, double
     if (__syncthreads_or(bad) && threadIdx.x == 0) set_flag(flags, FLAG_BAD_INPUT);
 }
 
-// one CTA per instance: C_i's row pointer rebased to 0, its columns rebased
+// one CTA per instance: C_i's row pointer rebased to 0 and its first entry
 template <typename TR>
 __global__ void __launch_bounds__(256)
-k_batch_unpack(const UnpackDesc *__restrict__ descs, const long long *__restrict__ rowptrC, int *col, TR *rp_out,
+k_batch_unpack(const UnpackDesc *__restrict__ descs, const long long *__restrict__ rowptrC, TR *rp_out,
                long long *ebase)
 {
     const UnpackDesc d = descs[blockIdx.x];
     const long long e0 = rowptrC[d.rowoff];
     if (threadIdx.x == 0) ebase[blockIdx.x] = e0;
     for (long long r = threadIdx.x; r <= d.m; r += blockDim.x) rp_out[d.rpoff + r] = (TR)(rowptrC[d.rowoff + r] - e0);
-    const long long e1 = rowptrC[d.rowoff + d.m];
-    for (long long q = e0 + threadIdx.x; q < e1; q += blockDim.x) col[q] = (int)(col[q] - d.coloff);
 }
 
 inline unsigned g256(long long n) {
@@ -371,12 +369,12 @@ cudaError_t batch_pack(Pool &pool, const PackDesc *d_desc, int count, long long 
     return cudaGetLastError();
 }
 
-cudaError_t batch_unpack(Pool &pool, const UnpackDesc *d_desc, int count, const long long *rowptrC, int *col,
-                         void *rp_out, int rp_bits, long long *ebase)
+cudaError_t batch_unpack(Pool &pool, const UnpackDesc *d_desc, int count, const long long *rowptrC, void *rp_out,
+                         int rp_bits, long long *ebase)
 {
     if (count <= 0) return cudaSuccess;
-    if (rp_bits == 64) { k_batch_unpack<long long><<<count, 256, 0, pool.stream>>>(d_desc, rowptrC, col, (long long *)rp_out, ebase); ::tsg::count_launch(); }
-    else { k_batch_unpack<int><<<count, 256, 0, pool.stream>>>(d_desc, rowptrC, col, (int *)rp_out, ebase); ::tsg::count_launch(); }
+    if (rp_bits == 64) { k_batch_unpack<long long><<<count, 256, 0, pool.stream>>>(d_desc, rowptrC, (long long *)rp_out, ebase); ::tsg::count_launch(); }
+    else { k_batch_unpack<int><<<count, 256, 0, pool.stream>>>(d_desc, rowptrC, (int *)rp_out, ebase); ::tsg::count_launch(); }
     return cudaGetLastError();
 }
 

@@ -141,12 +141,12 @@ struct PackDesc {
 struct UnpackDesc {
     long long rowoff;        // first packed row of C_i
     int m;                   // rows of C_i
-    long long coloff;        // subtracted from C's packed column indices
+    long long coloff;        // C_i's first packed column (the numeric step subtracts it)
     long long rpoff;         // first entry of C_i's row pointer in the output array
 };
 
 cudaError_t batch_pack(Pool &pool, const PackDesc *d_desc, int count, long long *rp, int *col, double *val, int *flags);
-cudaError_t batch_unpack(Pool &pool, const UnpackDesc *d_desc, int count, const long long *rowptrC, int *col,
-                         void *rp_out, int rp_bits, long long *ebase);
+cudaError_t batch_unpack(Pool &pool, const UnpackDesc *d_desc, int count, const long long *rowptrC, void *rp_out,
+                         int rp_bits, long long *ebase);
 
 }  // namespace tsg

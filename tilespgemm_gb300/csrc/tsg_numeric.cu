@@ -139,14 +139,62 @@ __device__ __forceinline__ void numeric_row(const NumericArgs &g, const TileRowS
     if (bad) set_flag(g.flags, FLAG_INTERNAL);
 }
 
+// numeric_row for B operands with repeated columns in a row: lanes that
+// would update the same output are serialised in B's entry order.
+template <bool DENSE>
+__device__ __forceinline__ void numeric_row_dupsafe(const NumericArgs &g, const TileRowSmem &t, bool use_map, int r0,
+                                                    int r, int lane)
+{
+    const int R = r0 + r;
+    const unsigned *wrow = t.word + r * t.S;
+    const int pa0 = (int)g.rpA[R], pa1 = (int)g.rpA[R + 1];
+    for (int pb = pa0; pb < pa1; pb += 32) {
+        const int na = min(32, pa1 - pb);
+        int bs = 0, be = 0;
+        double av = 0.0;
+        if (lane < na) {
+            const int k = g.colA[pb + lane];
+            av = g.valA[pb + lane];
+            bs = (int)g.rpB[k];
+            be = (int)g.rpB[k + 1];
+        }
+        for (int q0 = 0; q0 < na; ++q0) {
+            const double a = __shfl_sync(0xffffffffu, av, q0);
+            const int b0 = __shfl_sync(0xffffffffu, bs, q0);
+            const int b1 = __shfl_sync(0xffffffffu, be, q0);
+            for (int eb = b0; eb < b1; eb += 32) {
+                const int e = eb + lane;
+                const bool ok = e < b1;
+                const unsigned act = __ballot_sync(0xffffffffu, ok);
+                if (ok) {
+                    const int col = g.colB[e];
+                    const double b = g.valB[e];
+                    const int j = col >> 4, c = col & 15;
+                    const int s = slot_of(j, t.jbase, t.span, use_map, t.map, t.scol, t.S);
+                    int pos = -1;
+                    if (s >= 0) pos = DENSE ? (r * t.S + s) * DPAD + c : acc_swz(rank_in_row(wrow[s], c));
+                    const bool okpos = (unsigned)pos < (unsigned)t.nacc;
+                    if (!okpos) { set_flag(g.flags, FLAG_INTERNAL); pos = -1 - lane; }
+                    const unsigned peers = __match_any_sync(act, pos);
+                    const int rank = __popc(peers & lanemask_lt());
+                    const int rounds = __reduce_max_sync(act, __popc(peers));
+                    for (int q = 0; q < rounds; ++q) {
+                        if (q == rank && okpos) t.acc[pos] = fma(a, b, t.acc[pos]);
+                        __syncwarp(act);
+                    }
+                }
+            }
+        }
+    }
+}
+
 template <int NT, bool DENSE, bool DUPSAFE>
 __global__ void __launch_bounds__(NT, 2048 / NT)
 k_numeric_smem(NumericArgs g, int mybin)
 {
     constexpr int NWARP = NT / 32;
     extern __shared__ __align__(16) unsigned char s_raw[];
-    const int i = blockIdx.x;
-    if (g.bin[i] != mybin) return;
+    const int i = g.binlist[(long long)mybin * g.blkm + blockIdx.x];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int r0 = i * TILE;
     const int rows = min(TILE, g.m - r0);
@@ -195,59 +243,12 @@ k_numeric_smem(NumericArgs g, int mybin)
     }
     __syncthreads();
 
-    if (!DUPSAFE) {
-        // warp w owns rows w, w+NWARP, ...
-        TileRowSmem t{scol, word, map, acc, S, jbase, span, nacc};
-        for (int r = warp; r < rows; r += NWARP) {
-            if (use_map) numeric_row<DENSE, true>(g, t, r0, r, lane);
-            else numeric_row<DENSE, false>(g, t, r0, r, lane);
-        }
-    } else {
-        // B has rows with repeated columns: lanes that would update the same
-        // output are serialised in B's entry order
-        for (int r = warp; r < rows; r += NWARP) {
-            const int R = r0 + r;
-            const unsigned *wrow = word + r * S;
-            const int pa0 = (int)g.rpA[R], pa1 = (int)g.rpA[R + 1];
-            for (int pb = pa0; pb < pa1; pb += 32) {
-                const int na = min(32, pa1 - pb);
-                int bs = 0, be = 0;
-                double av = 0.0;
-                if (lane < na) {
-                    const int k = g.colA[pb + lane];
-                    av = g.valA[pb + lane];
-                    bs = (int)g.rpB[k];
-                    be = (int)g.rpB[k + 1];
-                }
-                for (int t = 0; t < na; ++t) {
-                    const double a = __shfl_sync(0xffffffffu, av, t);
-                    const int b0 = __shfl_sync(0xffffffffu, bs, t);
-                    const int b1 = __shfl_sync(0xffffffffu, be, t);
-                    for (int eb = b0; eb < b1; eb += 32) {
-                        const int e = eb + lane;
-                        const bool ok = e < b1;
-                        const unsigned act = __ballot_sync(0xffffffffu, ok);
-                        if (ok) {
-                            const int col = g.colB[e];
-                            const double b = g.valB[e];
-                            const int j = col >> 4, c = col & 15;
-                            const int s = slot_of(j, jbase, span, use_map, map, scol, S);
-                            int pos = -1;
-                            if (s >= 0) pos = DENSE ? (r * S + s) * DPAD + c : acc_swz(rank_in_row(wrow[s], c));
-                            const bool okpos = (unsigned)pos < (unsigned)nacc;
-                            if (!okpos) { set_flag(g.flags, FLAG_INTERNAL); pos = -1 - lane; }
-                            const unsigned peers = __match_any_sync(act, pos);
-                            const int rank = __popc(peers & lanemask_lt());
-                            const int rounds = __reduce_max_sync(act, __popc(peers));
-                            for (int q = 0; q < rounds; ++q) {
-                                if (q == rank && okpos) acc[pos] = fma(a, b, acc[pos]);
-                                __syncwarp(act);
-                            }
-                        }
-                    }
-                }
-            }
-        }
+    // warp w owns rows w, w+NWARP, ...
+    TileRowSmem t{scol, word, map, acc, S, jbase, span, nacc};
+    for (int r = warp; r < rows; r += NWARP) {
+        if (DUPSAFE) numeric_row_dupsafe<DENSE>(g, t, use_map, r0, r, lane);
+        else if (use_map) numeric_row<DENSE, true>(g, t, r0, r, lane);
+        else numeric_row<DENSE, false>(g, t, r0, r, lane);
     }
     __syncthreads();
 
@@ -255,12 +256,13 @@ k_numeric_smem(NumericArgs g, int mybin)
     if (!DENSE) {
         for (int p = tid; p < nnz_tr; p += NT) g.valC[R0 + p] = acc[acc_swz(p)];
     }
+    const int cshift = g.tr_coloff ? g.tr_coloff[i] : 0;
     for (int r = warp; r < rows; r += NWARP) {
         for (int s = lane; s < S; s += 32) {
             const unsigned w = word[r * S + s];
             unsigned mk = w & 0xffffu;
             long long dst = R0 + (w >> 16);
-            const int jb = scol[s] * TILE;
+            const int jb = scol[s] * TILE - cshift;
             while (mk) {
                 const int b = 31 - __clz(mk);   // highest bit = smallest local column
                 const int c = TILE - 1 - b;
@@ -273,6 +275,144 @@ k_numeric_smem(NumericArgs g, int mybin)
     }
 }
 
+// ---- tile-rows whose rows fit shared memory one at a time -------------------
+
+// numeric_row for the row kernel, with B's entries loaded one step ahead:
+// the warp walks the (A entry, 32-entry chunk of its B row) pairs in order
+// and issues the next pair's loads before the current pair's shared-memory
+// update, so the L2 latency of B overlaps the accumulator work.  Order of the
+// updates per output is unchanged (A's row order, then B's row order).
+template <bool MAP>
+__device__ __forceinline__ void numeric_row_prefetch(const NumericArgs &g, const TileRowSmem &t, int R, int lane)
+{
+    const unsigned *wrow = t.word;
+    const int pa0 = (int)g.rpA[R], pa1 = (int)g.rpA[R + 1];
+    double *acc = t.acc;
+    bool bad = false;
+    for (int pb = pa0; pb < pa1; pb += 32) {
+        const int na = min(32, pa1 - pb);
+        int bs = 0, be = 0;
+        double av = 0.0;
+        if (lane < na) {
+            const int k = g.colA[pb + lane];
+            av = g.valA[pb + lane];
+            bs = (int)g.rpB[k];
+            be = (int)g.rpB[k + 1];
+        }
+        // first non-empty pair
+        int q = 0, eb = __shfl_sync(0xffffffffu, bs, 0), ee = __shfl_sync(0xffffffffu, be, 0);
+        double a = __shfl_sync(0xffffffffu, av, 0);
+        while (eb >= ee && ++q < na) {
+            eb = __shfl_sync(0xffffffffu, bs, q);
+            ee = __shfl_sync(0xffffffffu, be, q);
+            a = __shfl_sync(0xffffffffu, av, q);
+        }
+        int col = 0;
+        double b = 0.0;
+        bool ok = false;
+        if (q < na && eb + lane < ee) { ok = true; col = g.colB[eb + lane]; b = g.valB[eb + lane]; }
+        while (q < na) {
+            // next pair (uniform across the warp)
+            int nq = q, neb = eb + 32, nee = ee;
+            double na_ = a;
+            while (neb >= nee && ++nq < na) {
+                neb = __shfl_sync(0xffffffffu, bs, nq);
+                nee = __shfl_sync(0xffffffffu, be, nq);
+                na_ = __shfl_sync(0xffffffffu, av, nq);
+            }
+            int ncol = 0;
+            double nb = 0.0;
+            bool nok = false;
+            if (nq < na && neb + lane < nee) { nok = true; ncol = g.colB[neb + lane]; nb = g.valB[neb + lane]; }
+            if (ok) {
+                const int pos = out_pos<false, MAP>(t, wrow, 0, col);
+                if (pos < 0) bad = true;
+                else acc[pos] = fma(a, b, acc[pos]);
+            }
+            q = nq; eb = neb; ee = nee; a = na_;
+            col = ncol; b = nb; ok = nok;
+        }
+    }
+    if (bad) set_flag(g.flags, FLAG_INTERNAL);
+}
+
+// One single-warp CTA per C row of a tile-row in bin `mybin` (a BIN_ROWS_*
+// size class): the row's CSR segment of values in shared memory, addressed
+// as in the tile-row kernel (slot map + this row's packed words), then
+// streamed out.  Used where the whole tile-row's segment does not fit: each
+// CTA holds one row, so the shared memory in use scales with the row, and
+// the rows of one tile-row run on different SMs.
+template <bool DUPSAFE>
+__global__ void __launch_bounds__(32, 32)
+k_numeric_rows(NumericArgs g, int mybin)
+{
+    extern __shared__ __align__(16) unsigned char s_raw[];
+    const int i = g.binlist[(long long)mybin * g.blkm + (blockIdx.x >> 4)];
+    const int r = blockIdx.x & (TILE - 1);
+    const int R = i * TILE + r;
+    if (R >= g.m) return;
+    const int lane = threadIdx.x;
+    const long long c0 = g.crp[i];
+    const int S = (int)(g.crp[i + 1] - c0);
+    const long long Rb = g.rowptrC[R];
+    const int nnz_r = (int)(g.rowptrC[R + 1] - Rb);
+    if (nnz_r == 0) return;
+    const int jbase = g.ccol[c0];
+    const int span = g.ccol[c0 + S - 1] - jbase + 1;
+    const bool use_map = span <= MAP_MAX;
+
+    unsigned *word = reinterpret_cast<unsigned *>(s_raw);
+    unsigned char *p1 = s_raw + align16((long long)S * 4);
+    unsigned short *map = use_map ? reinterpret_cast<unsigned short *>(p1) : nullptr;
+    int *scol = use_map ? nullptr : reinterpret_cast<int *>(p1);
+    double *acc = reinterpret_cast<double *>(p1 + (use_map ? map_bytes(span) : align16((long long)S * 4)));
+
+    if (use_map) {
+        const int span64 = (span + 63) & ~63;
+        for (int t = lane; t < span64; t += 32) map[t] = 0xffffu;
+        __syncwarp();
+    }
+    for (int s = lane; s < S; s += 32) {
+        const int j = g.ccol[c0 + s];
+        if (use_map) map[map_swz((unsigned)(j - jbase))] = (unsigned short)s;
+        else scol[s] = j;
+    }
+    int run = 0;
+    for (int sb = 0; sb < S; sb += 32) {
+        const int s = sb + lane;
+        const unsigned mk = (s < S) ? (unsigned)g.cmask[c0 * TILE + (long long)r * S + s] : 0u;
+        const int c = __popc(mk);
+        const int incl = warp_incl_scan(c, lane);
+        if (s < S) word[s] = ((unsigned)(run + incl - c) << 16) | mk;
+        run += __shfl_sync(0xffffffffu, incl, 31);
+    }
+    const int nacc = (nnz_r + 15) & ~15;
+    {
+        unsigned long long *z = reinterpret_cast<unsigned long long *>(acc);
+        for (int t = lane; t < nacc; t += 32) z[t] = 0ull;
+    }
+    __syncwarp();
+    TileRowSmem t{scol, word, map, acc, S, jbase, span, nacc};
+    if (DUPSAFE) numeric_row_dupsafe<false>(g, t, use_map, R, 0, lane);
+    else if (use_map) numeric_row_prefetch<true>(g, t, R, lane);
+    else numeric_row_prefetch<false>(g, t, R, lane);
+    __syncwarp();
+    for (int p = lane; p < nnz_r; p += 32) g.valC[Rb + p] = acc[acc_swz(p)];
+    const int cshift = g.tr_coloff ? g.tr_coloff[i] : 0;
+    for (int s = lane; s < S; s += 32) {
+        const unsigned w = word[s];
+        unsigned mk = w & 0xffffu;
+        long long dst = Rb + (w >> 16);
+        const int jb = (use_map ? g.ccol[c0 + s] : scol[s]) * TILE - cshift;
+        while (mk) {
+            const int b = 31 - __clz(mk);   // highest bit = smallest local column
+            g.colC[dst] = jb + (TILE - 1 - b);
+            ++dst;
+            mk &= ~(1u << b);
+        }
+    }
+}
+
 // ---- tile-rows too large for shared memory ----------------------------------
 
 // per C tile and row: offset of its segment inside the C row; column indices;
@@ -280,8 +420,8 @@ k_numeric_smem(NumericArgs g, int mybin)
 __global__ void __launch_bounds__(256)
 k_global_prep(NumericArgs g)
 {
-    const int i = blockIdx.x;
-    if (g.bin[i] != BIN_GLOBAL) return;
+    const int i = g.binlist[(long long)BIN_GLOBAL * g.blkm + blockIdx.x];
+    const int cshift = g.tr_coloff ? g.tr_coloff[i] : 0;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int r0 = i * TILE, rows = min(TILE, g.m - r0);
     const long long c0 = g.crp[i];
@@ -298,7 +438,7 @@ k_global_prep(NumericArgs g)
                 int off = run + incl - c;
                 g.offC[(c0 + s) * TILE + r] = off;
                 long long dst = Rb + off;
-                const int jb = g.ccol[c0 + s] * TILE;
+                const int jb = g.ccol[c0 + s] * TILE - cshift;
                 while (mk) {
                     const int b = 31 - __clz(mk);
                     g.colC[dst] = jb + (TILE - 1 - b);
@@ -317,11 +457,11 @@ template <bool DUPSAFE>
 __global__ void __launch_bounds__(256, 4)
 k_numeric_global(NumericArgs g)
 {
-    const int R = blockIdx.x * 8 + (threadIdx.x >> 5);
+    const int i = g.binlist[(long long)BIN_GLOBAL * g.blkm + (blockIdx.x >> 1)];
+    const int r = (blockIdx.x & 1) * 8 + (threadIdx.x >> 5);
+    const int R = i * TILE + r;
     const int lane = threadIdx.x & 31;
     if (R >= g.m) return;
-    const int i = R / TILE, r = R - i * TILE;
-    if (g.bin[i] != BIN_GLOBAL) return;
     const long long c0 = g.crp[i];
     const int S = (int)(g.crp[i + 1] - c0);
     const int *tc = g.ccol + c0;
@@ -384,8 +524,9 @@ cudaError_t set_smem_attr() {
 }
 
 template <int NT>
-cudaError_t launch_smem(const NumericArgs &a, int bin, long long smem, bool dense, bool dup, cudaStream_t s) {
-    const unsigned grid = (unsigned)a.blkm;
+cudaError_t launch_smem(const NumericArgs &a, int bin, long long nrows, long long smem, bool dense, bool dup,
+                        cudaStream_t s) {
+    const unsigned grid = (unsigned)nrows;
     if (dense) {
         if (dup) { k_numeric_smem<NT, true, true><<<grid, NT, smem, s>>>(a, bin); ::tsg::count_launch(); }
         else { k_numeric_smem<NT, true, false><<<grid, NT, smem, s>>>(a, bin); ::tsg::count_launch(); }
@@ -410,6 +551,12 @@ cudaError_t numeric_init_attributes()
     TSG_SET(256)
     TSG_SET(512)
 #undef TSG_SET
+    for (int d = 0; d < 2 && e == cudaSuccess; ++d) {
+        const void *f = d ? (const void *)k_numeric_rows<true> : (const void *)k_numeric_rows<false>;
+        e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_LARGE);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
+    }
     return e;
 }
 
@@ -422,13 +569,21 @@ cudaError_t numeric_run(Pool &pool, const NumericArgs &a, const long long *count
         if (counts[b] == 0) continue;
         const bool dense = (b == BIN_DENSE_S || b == BIN_DENSE_L);
         const long long smem = req[b];
-        if (threads == 128) e = launch_smem<128>(a, b, smem, dense, dupsafe, s);
-        else if (threads == 512) e = launch_smem<512>(a, b, smem, dense, dupsafe, s);
-        else e = launch_smem<256>(a, b, smem, dense, dupsafe, s);
+        if (threads == 128) e = launch_smem<128>(a, b, counts[b], smem, dense, dupsafe, s);
+        else if (threads == 512) e = launch_smem<512>(a, b, counts[b], smem, dense, dupsafe, s);
+        else e = launch_smem<256>(a, b, counts[b], smem, dense, dupsafe, s);
+    }
+    for (int b = BIN_ROWS_S; b <= BIN_ROWS_L && e == cudaSuccess; ++b) {
+        if (counts[b] == 0) continue;
+        const unsigned g = (unsigned)(counts[b] * TILE);
+        const size_t smem = (size_t)req[b];
+        if (dupsafe) { k_numeric_rows<true><<<g, 32, smem, s>>>(a, b); ::tsg::count_launch(); }
+        else { k_numeric_rows<false><<<g, 32, smem, s>>>(a, b); ::tsg::count_launch(); }
+        e = cudaGetLastError();
     }
     if (e == cudaSuccess && counts[BIN_GLOBAL] > 0) {
-        { k_global_prep<<<(unsigned)a.blkm, 256, 0, s>>>(a); ::tsg::count_launch(); }
-        const unsigned g = (unsigned)((a.m + 7) / 8);
+        { k_global_prep<<<(unsigned)counts[BIN_GLOBAL], 256, 0, s>>>(a); ::tsg::count_launch(); }
+        const unsigned g = (unsigned)(counts[BIN_GLOBAL] * 2);
         if (dupsafe) { k_numeric_global<true><<<g, 256, 0, s>>>(a); ::tsg::count_launch(); }
         else { k_numeric_global<false><<<g, 256, 0, s>>>(a); ::tsg::count_launch(); }
         e = cudaGetLastError();

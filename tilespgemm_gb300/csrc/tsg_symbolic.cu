@@ -71,7 +71,8 @@ k_step2(int blkm, int m, const int *__restrict__ arp, const int *__restrict__ ac
         const uint16_t *__restrict__ amask, const int *__restrict__ brp, const int *__restrict__ bcol,
         const uint16_t *__restrict__ bmask, const long long *__restrict__ crp, const int *__restrict__ ccol,
         uint16_t *cmask, int *rowcnt, int smax, int map_cap, NumericBinParams bp, unsigned char *bin,
-        long long *binstat, int *flags, const int *__restrict__ rows_list)
+        long long *binstat, int *binlist, int *flags, const int *__restrict__ rows_list,
+        const long long *__restrict__ erpB, const int *__restrict__ ecolB)
 {
     extern __shared__ __align__(16) unsigned char s_raw[];
     __shared__ long long s_rowtot[TILE];
@@ -115,6 +116,33 @@ k_step2(int blkm, int m, const int *__restrict__ arp, const int *__restrict__ ac
         unsigned colrows[TILE];
 #pragma unroll
         for (int c = 0; c < TILE; ++c) colrows[c] = __ballot_sync(0xffffffffu, (ma >> (TILE - 1 - c)) & 1u) & 0xffffu;
+        // A tiles with few entries: visit the B rows of the A tile's local
+        // columns element by element (an entry (kt*16+c, col) sets bit
+        // 15-(col&15) of C's tile col>>4 in the rows that use c) instead of
+        // all nq B tiles; the masks are the same either way
+        const unsigned acols = __brev(__reduce_or_sync(0xffffffffu, ma)) >> 16;   // bit c: local column c used
+        int eb0 = 0, eb1 = 0;   // operands hold < 2^31 entries
+        if (lane < TILE && ((acols >> lane) & 1u)) { eb0 = (int)erpB[kt * TILE + lane]; eb1 = (int)erpB[kt * TILE + lane + 1]; }
+        const int elem_iters = warp_sum_int((eb1 - eb0 + 31) >> 5);
+        if (elem_iters <= 3 * ((nq + 31) >> 5)) {
+            for (unsigned cs = acols; cs; cs &= cs - 1) {
+                const int c = __ffs(cs) - 1;
+                const int e0 = __shfl_sync(0xffffffffu, eb0, c), e1 = __shfl_sync(0xffffffffu, eb1, c);
+                const unsigned rowsc = __ballot_sync(0xffffffffu, (ma >> (TILE - 1 - c)) & 1u) & 0xffffu;
+                for (int e = e0 + lane; e < e1; e += 32) {
+                    const int col = ecolB[e];
+                    const int sl = c_slot(col >> 4, jbase, span, map, scol, S);
+                    if (sl < 0) { bad = true; continue; }
+                    const unsigned bit = 0x8000u >> (col & 15);
+                    for (unsigned rs = rowsc; rs; rs &= rs - 1) {
+                        const int r = __ffs(rs) - 1;
+                        if (GLOBAL) atomic_or_mask16(cmask, c0 * TILE + (long long)r * S + sl, bit);
+                        else atomicOr(&smask[r * S + sl], bit);
+                    }
+                }
+            }
+            continue;
+        }
         for (int qb = 0; qb < nq; qb += 32) {
             const int q = qb + lane;
             const bool ok = q < nq;
@@ -164,13 +192,14 @@ k_step2(int blkm, int m, const int *__restrict__ arp, const int *__restrict__ ac
     }
     __syncthreads();
     if (tid == 0) {
-        long long nnz_tr = 0;
-        for (int r = 0; r < TILE; ++r) nnz_tr += s_rowtot[r];
+        long long nnz_tr = 0, max_row = 0;
+        for (int r = 0; r < TILE; ++r) { nnz_tr += s_rowtot[r]; max_row = max(max_row, s_rowtot[r]); }
         int b;
         long long req = 0;
-        numeric_classify(bp, S, nnz_tr, span, b, req);
+        numeric_classify(bp, S, nnz_tr, span, max_row, b, req);
         bin[i] = (unsigned char)b;
-        atomicAdd((unsigned long long *)&binstat[b], 1ull);
+        const unsigned long long pos = atomicAdd((unsigned long long *)&binstat[b], 1ull);
+        binlist[(long long)b * blkm + (long long)pos] = i;
         atomicMax((long long *)&binstat[NBIN + b], req);
     }
 }
@@ -191,8 +220,8 @@ cudaError_t symbolic_init_attributes()
 
 cudaError_t step2_masks(Pool &pool, const TileCSR &A, const TileCSR &B, int m, int blkm, const long long *crp,
                         const int *ccol, uint16_t *cmask, int *rowcnt, int max_tiles_per_row, int max_span,
-                        const NumericBinParams &bp, unsigned char *bin, long long *binstat, int *flags,
-                        const int *defer_list, int ndefer)
+                        const NumericBinParams &bp, unsigned char *bin, long long *binstat, int *binlist,
+                        int *flags, const int *defer_list, int ndefer, const long long *erpB, const int *ecolB)
 {
     cudaStream_t s = pool.stream;
     if (blkm <= 0 || ndefer <= 0) return cudaSuccess;
@@ -200,10 +229,12 @@ cudaError_t step2_masks(Pool &pool, const TileCSR &A, const TileCSR &B, int m, i
     const int map_cap = max_span < (int)MAP_MAX ? max_span : (int)MAP_MAX;
     const size_t smem = (size_t)(align16((long long)s_used * TILE * 4) + align16((long long)s_used * 4) + align16((long long)map_cap * 2));
     { k_step2<false><<<ndefer, S2_THREADS, smem, s>>>(blkm, m, A.trp, A.tcol, A.mask, B.trp, B.tcol, B.mask, crp, ccol,
-                                                   cmask, rowcnt, S2_SMAX, map_cap, bp, bin, binstat, flags, defer_list); ::tsg::count_launch(); }
+                                                   cmask, rowcnt, S2_SMAX, map_cap, bp, bin, binstat, binlist, flags, defer_list,
+                                                   erpB, ecolB); ::tsg::count_launch(); }
     if (max_tiles_per_row > S2_SMAX)
         { k_step2<true><<<ndefer, S2_THREADS, 0, s>>>(blkm, m, A.trp, A.tcol, A.mask, B.trp, B.tcol, B.mask, crp, ccol,
-                                                   cmask, rowcnt, S2_SMAX, 0, bp, bin, binstat, flags, defer_list); ::tsg::count_launch(); }
+                                                   cmask, rowcnt, S2_SMAX, 0, bp, bin, binstat, binlist, flags, defer_list,
+                                                   erpB, ecolB); ::tsg::count_launch(); }
     return cudaGetLastError();
 }
 

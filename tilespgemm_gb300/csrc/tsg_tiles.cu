@@ -203,7 +203,8 @@ static_assert(NW * 32 == FUSED_MAX_SPAN, "fused window");
 __global__ void __launch_bounds__(FWPC * 32)
 k_sym_fused(UnionKeys::Params P, int blkm, int m, const long long *__restrict__ crp, int *ccol,
             const uint16_t *__restrict__ amask, const uint16_t *__restrict__ bmask, uint16_t *cmask, int *rowcnt,
-            unsigned char *bin, NumericBinParams bp, long long *binstat, int *flags)
+            unsigned char *bin, NumericBinParams bp, long long *binstat, int *binlist, int *flags,
+            const long long *__restrict__ erpB, const int *__restrict__ ecolB)
 {
     __shared__ unsigned s_bm[FWPC][NW];
     __shared__ unsigned short s_pref[FWPC][NW];
@@ -273,6 +274,38 @@ k_sym_fused(UnionKeys::Params P, int blkm, int m, const long long *__restrict__ 
             unsigned colrows[TILE];
 #pragma unroll
             for (int c = 0; c < TILE; ++c) colrows[c] = __ballot_sync(0xffffffffu, (ma >> (TILE - 1 - c)) & 1u) & 0xffffu;
+            // A tiles with few entries: B's rows element by element (as in the
+            // CTA step-2 kernel); lanes may then share a slot, so word atomics
+            const unsigned acols = __brev(__reduce_or_sync(0xffffffffu, ma)) >> 16;
+            const int kt = P.acol[a];
+            int eb0 = 0, eb1 = 0;   // operands hold < 2^31 entries
+            if (lane < TILE && ((acols >> lane) & 1u)) { eb0 = (int)erpB[kt * TILE + lane]; eb1 = (int)erpB[kt * TILE + lane + 1]; }
+            const int elem_iters = warp_sum_int((eb1 - eb0 + 31) >> 5);
+            if (elem_iters <= 3 * ((nq + 31) >> 5)) {
+                unsigned *mw = reinterpret_cast<unsigned *>(msk);
+                __syncwarp();
+                for (unsigned cs = acols; cs; cs &= cs - 1) {
+                    const int c = __ffs(cs) - 1;
+                    const int e0 = __shfl_sync(0xffffffffu, eb0, c), e1 = __shfl_sync(0xffffffffu, eb1, c);
+                    const unsigned rowsc = __ballot_sync(0xffffffffu, (ma >> (TILE - 1 - c)) & 1u) & 0xffffu;
+                    for (int e = e0 + lane; e < e1; e += 32) {
+                        const int o = (ecolB[e] >> 4) - kmin;
+                        int slot = -1;
+                        if (o >= 0 && o < span) {
+                            const int w = o >> 5;
+                            slot = pref[w] + __popc(bm[w] & ((1u << (o & 31)) - 1u));
+                        }
+                        if (slot < 0 || slot >= S) { bad = true; continue; }
+                        const unsigned bit = 0x8000u >> (ecolB[e] & 15);
+                        for (unsigned rs = rowsc; rs; rs &= rs - 1) {
+                            const int idx = (__ffs(rs) - 1) * S + slot;
+                            atomicOr(mw + (idx >> 1), bit << ((idx & 1) * 16));
+                        }
+                    }
+                }
+                __syncwarp();
+                continue;
+            }
             const uint16_t *bq = bmask + (long long)q0 * TILE;
             for (int qb = 0; qb < nq; qb += 32) {
                 const int q = qb + lane;
@@ -306,20 +339,23 @@ k_sym_fused(UnionKeys::Params P, int blkm, int m, const long long *__restrict__ 
     __syncwarp();
     for (int t = lane; t < S * TILE; t += 32) cmask[c0 * TILE + t] = msk[t];
     long long nnz_tr = 0;
+    int max_row = 0;
     for (int r = 0; r < TILE; ++r) {
         int c = 0;
         for (int sl = lane; sl < S; sl += 32) c += __popc((unsigned)msk[r * S + sl]);
         c = warp_sum_int(c);
         if (lane == 0 && r < rows) rowcnt[row * TILE + r] = c;
         nnz_tr += c;
+        max_row = max(max_row, c);
     }
     if (bad) set_flag(flags, FLAG_INTERNAL);
     if (lane == 0) {
         int b;
         long long req = 0;
-        numeric_classify(bp, S, nnz_tr, span, b, req);
+        numeric_classify(bp, S, nnz_tr, span, max_row, b, req);
         bin[row] = (unsigned char)b;
-        atomicAdd((unsigned long long *)&binstat[b], 1ull);
+        const unsigned long long pos = atomicAdd((unsigned long long *)&binstat[b], 1ull);
+        binlist[(long long)b * blkm + (long long)pos] = row;
         atomicMax((long long *)&binstat[NBIN + b], req);
     }
 }
@@ -720,13 +756,15 @@ cudaError_t tile_symbolic(Pool &pool, const TileCSR &A, const TileCSR &B, long l
 // come from step2_masks's CTA kernel).
 cudaError_t symbolic_fill_fused(Pool &pool, const TileCSR &A, const TileCSR &B, int m, const long long *crp,
                                 int *ccol, uint16_t *cmask, int *rowcnt, unsigned char *bin,
-                                const NumericBinParams &bp, long long *binstat, int *cnt, int *wide, int *flags)
+                                const NumericBinParams &bp, long long *binstat, int *binlist, int *cnt, int *wide,
+                                int *flags, const long long *erpB, const int *ecolB)
 {
     cudaStream_t s = pool.stream;
     if (A.blkm <= 0) return cudaSuccess;
     UnionKeys::Params P{A.trp, A.tcol, B.trp, B.tcol};
     { k_sym_fused<<<(unsigned)((A.blkm + FWPC - 1) / FWPC), FWPC * 32, 0, s>>>(P, A.blkm, m, crp, ccol, A.mask, B.mask,
-                                                                         cmask, rowcnt, bin, bp, binstat, flags); ::tsg::count_launch(); }
+                                                                         cmask, rowcnt, bin, bp, binstat, binlist, flags,
+                                                                         erpB, ecolB); ::tsg::count_launch(); }
     (void)cnt;
     { k_union_wide<UnionKeys, true, false, long long><<<304, WIDE_THREADS, WIDE_SMEM, s>>>(
         P, wide, wide + A.blkm, nullptr, nullptr, crp, ccol, nullptr); ::tsg::count_launch(); }
