@@ -150,6 +150,13 @@ tsg_status tsg_measure_fp64_peak(tsg_ctx *ctx, double *gflops);
  */
 tsg_status tsg_load_mtx(const char *path, tsg_csr *out, int32_t *is_symmetric);
 
+/* Write a host CSR (for example C) as a Matrix Market coordinate real
+ * general file in the format of the reference's mm_write_mtx_crd
+ * (mmio.h:780-850): 1-based "i j value" lines in CSR order, values as
+ * "%20.16g"; exact != 0 writes 17 significant digits instead, so the file
+ * loads back bit for bit. */
+tsg_status tsg_write_mtx(const char *path, const tsg_csr *M, int32_t exact);
+
 /* Release arrays that the library allocated into *m (C outputs or a loaded
  * matrix); a matrix whose owner is NULL belongs to the caller and is left
  * alone.  ctx may be NULL for host matrices from tsg_load_mtx.  Outputs of

@@ -60,3 +60,25 @@ def test_roundtrip_generated(built_lib, tmp_path):
     B, sym = load_mtx(tmp_path / "g.mtx")
     assert not sym
     assert np.array_equal(B.rowptr, A.rowptr) and np.array_equal(B.col, A.col) and np.array_equal(B.val, A.val)
+
+
+def test_write_then_load_round_trip(built_lib, tmp_path):
+    """tsg_write_mtx: the reference writer's format (banner, size line,
+    1-based 'i j %20.16g' lines in CSR order); exact mode loads back bit for
+    bit."""
+    from tilespgemm_gb300 import load_mtx, write_mtx
+    from tilespgemm_gb300 import matrices as M
+    A = M.random_sparse(37, 23, 4, seed=3)
+    p = tmp_path / "a.mtx"
+    write_mtx(p, A)
+    lines = p.read_text().splitlines()
+    assert lines[0] == "%%MatrixMarket matrix coordinate real general"
+    assert lines[1] == f"{A.m} {A.n} {A.nnz}"
+    r0 = int(np.searchsorted(A.rowptr, 0, side="right")) - 1
+    assert lines[2] == "%d %d %20.16g" % (r0 + 1, A.col[0] + 1, A.val[0])
+    B, sym = load_mtx(p)
+    assert not sym and np.array_equal(B.rowptr, A.rowptr) and np.array_equal(B.col, A.col)
+    assert np.allclose(B.val, A.val, rtol=1e-15, atol=0)
+    write_mtx(p, A, exact=True)
+    B, _ = load_mtx(p)
+    assert np.array_equal(B.val, A.val)

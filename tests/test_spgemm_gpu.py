@@ -156,6 +156,36 @@ def test_long_rows(opts, built_lib):
             check_against_oracle(C, X, X)
 
 
+def _runs_matrix(m, n, runs, seed):
+    """Row k holds the column runs given by runs(k) -> list of (start, length),
+    values uniform in [-1, 1]."""
+    from tilespgemm_gb300.api import CSR
+    rng = np.random.default_rng(seed)
+    rp, cols = [0], []
+    for k in range(m):
+        c = np.unique(np.concatenate([np.arange(s0, min(s0 + ln, n)) for s0, ln in runs(k)]))
+        cols.append(c)
+        rp.append(rp[-1] + c.size)
+    col = np.concatenate(cols).astype(np.int32)
+    return CSR(m, n, np.array(rp, np.int64), col, rng.uniform(-1, 1, col.size))
+
+
+@pytest.mark.parametrize("opts", [dict(), dict(dense_tile_min=257)])
+def test_wide_tile_rows(ctx, opts, built_lib):
+    """C tile-rows with more than 2,048 tiles (windowed step 2) and rows
+    spanning more than 4,096 tile columns (windowed global accumulator):
+    dense tiles (tile path) and scattered entries (element path)."""
+    from tilespgemm_gb300 import Context
+    A = _runs_matrix(32, 120, lambda k: [(0, 120)], seed=41)                       # dense rows
+    B1 = _runs_matrix(120, 120000, lambda k: [(k * 1000, 300)], seed=42)            # dense tiles
+    B2 = _runs_matrix(120, 120000, lambda k: [(k * 997 + 16 * t, 1) for t in range(300)], seed=43)  # 1 per tile
+    with Context(0, **opts) as c:
+        for B in (B1, B2):
+            C, st = c.spgemm(A, B, op="AB", stats=True)
+            assert st["bins"][3] > 0
+            check_against_oracle(C, A, B)
+
+
 def test_device_inputs_and_outputs(ctx):
     import torch
     from tilespgemm_gb300 import matrices as M

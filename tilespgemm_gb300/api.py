@@ -403,8 +403,18 @@ def load_mtx(path: str) -> tuple[CSR, bool]:
         lib().tsg_csr_free(None, C.byref(s))
 
 
+def write_mtx(path: str, A: CSR, exact: bool = False) -> None:
+    """Host CSR -> Matrix Market coordinate file in the reference's writer
+    format (mm_write_mtx_crd); exact=True keeps every bit of the values."""
+    if A.on_device:
+        raise ValueError("write_mtx takes a host matrix")
+    a, keep = A._tsg()
+    check(lib().tsg_write_mtx(str(path).encode(), C.byref(a), int(bool(exact))))
+    del keep
+
+
 def version() -> str:
     return lib().tsg_version().decode()
 
 
-__all__ = ["CSR", "Context", "OwnedCSR", "Plan", "Tiles", "TSGError", "load_mtx", "version"]
+__all__ = ["CSR", "Context", "OwnedCSR", "Plan", "Tiles", "TSGError", "load_mtx", "write_mtx", "version"]

@@ -288,7 +288,6 @@ struct PlanData {
     long long *rowptrC = nullptr;
     unsigned char *bin = nullptr;
     int *binlist = nullptr;                        // tile-rows of each bin, NBIN * blkm
-    int *offC = nullptr;
     long long counts[NBIN] = {}, req[NBIN] = {};
     bool dupsafe = false;
     int nsync = 0;
@@ -307,7 +306,7 @@ struct PlanData {
     }
     long long device_bytes() const {
         return 8ll * (m + 1) * 2 + 4ll * (nnzA + nnzB) + 8ll * (nnzA + nnzB) + 8ll * (blkm + 1) +
-               36ll * numblkC + 8ll * (m + 1) + 4ll * NBIN * blkm + (counts[BIN_GLOBAL] ? 64ll * numblkC : 0);
+               36ll * numblkC + 8ll * (m + 1) + 4ll * NBIN * blkm;
     }
 };
 
@@ -469,10 +468,6 @@ tsg_status plan_symbolic(tsg_ctx *ctx, Pool &pool, Scratch &sc, tsg_op op, const
         P.counts[b] = ctx->hstat[ST_BINS + b];
         P.req[b] = ctx->hstat[ST_BINS + NBIN + b];
     }
-    if (P.counts[BIN_GLOBAL] > 0) {
-        P.offC = P.own<int>(pool, P.numblkC * TILE);
-        if (!P.offC) return fail(TSG_ERR_OOM, "device pool allocation failed (global bin offsets)");
-    }
     tm.mark();  // 3
     return TSG_OK;
 }
@@ -487,7 +482,7 @@ tsg_status plan_numeric(tsg_ctx *ctx, Pool &pool, PlanData &P, const double *val
     na.rpB = P.rpB; na.colB = P.colB; na.valB = valB;
     na.crp = P.crp; na.ccol = P.ccol; na.cmask = P.cmask;
     na.rowptrC = P.rowptrC; na.colC = col; na.valC = val;
-    na.bin = P.bin; na.binlist = P.binlist; na.tr_coloff = tr_coloff; na.offC = P.offC; na.flags = ctx->dflags;
+    na.bin = P.bin; na.binlist = P.binlist; na.tr_coloff = tr_coloff; na.flags = ctx->dflags;
     CUDA_OK(numeric_run(pool, na, P.counts, P.req, P.dupsafe, ctx->opts.threads_numeric));
     return TSG_OK;
 }

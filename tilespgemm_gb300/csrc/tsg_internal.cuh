@@ -77,6 +77,24 @@ __device__ __forceinline__ void atomic_or_mask16(uint16_t *mask, long long idx, 
     atomicOr(w, bits << ((idx & 1) * 16));
 }
 
+// First index in [lo, hi) whose value is >= key (hi if none), by a 32-way
+// search of the warp: each round every lane probes one point.
+__device__ __forceinline__ int warp_lower_bound(const int *__restrict__ a, int lo, int hi, int key, int lane)
+{
+    while (hi - lo > 32) {
+        const int step = (hi - lo + 31) >> 5;
+        const int idx = lo + lane * step;
+        const unsigned m = __ballot_sync(0xffffffffu, idx >= hi || a[idx] >= key);
+        const int f = m ? __ffs(m) - 1 : 32;
+        const int nlo = f == 0 ? lo : lo + (f - 1) * step + 1;
+        hi = min(hi, lo + f * step);
+        lo = nlo;
+    }
+    const int idx = lo + lane;
+    const unsigned m = __ballot_sync(0xffffffffu, idx < hi && a[idx] >= key);
+    return m ? lo + __ffs(m) - 1 : hi;
+}
+
 __device__ __forceinline__ void set_flag(int *flags, int which) {
     atomicOr(flags + which, 1);
 }

@@ -182,3 +182,47 @@ extern "C" tsg_status tsg_load_mtx(const char *path, tsg_csr *out, int32_t *is_s
     if (is_symmetric) *is_symmetric = symm ? 1 : 0;
     return TSG_OK;
 }
+
+// Write a host CSR as a Matrix Market coordinate file, in the format of the
+// reference's writer mm_write_mtx_crd (mmio.h:780-850): banner
+// "%%MatrixMarket matrix coordinate real general", the size line "M N NNZ",
+// then one "i j value" line per entry with 1-based indices, in CSR order.
+// Values use the reference's "%20.16g" unless `exact`, which writes 17
+// significant digits so that the file loads back to the same doubles.
+extern "C" tsg_status tsg_write_mtx(const char *path, const tsg_csr *M, int32_t exact)
+{
+    if (!path || !M) { tsg::set_last_error("path/M is NULL"); return TSG_ERR_INVALID_ARG; }
+    if (M->where != TSG_MEM_HOST) { tsg::set_last_error("tsg_write_mtx takes a host matrix"); return TSG_ERR_INVALID_ARG; }
+    if (M->m < 0 || M->n < 0 || M->nnz < 0 || (M->rowptr_bits != 32 && M->rowptr_bits != 64) || !M->row_ptr ||
+        (M->nnz > 0 && (!M->col || !M->val))) {
+        tsg::set_last_error("M is not a valid CSR");
+        return TSG_ERR_INVALID_ARG;
+    }
+    FILE *f = fopen(path, "wb");
+    if (!f) { tsg::set_last_error("cannot open the output file"); return TSG_ERR_INVALID_ARG; }
+    std::string buf;
+    buf.reserve(1 << 20);
+    char line[128];
+    int len = snprintf(line, sizeof line, "%%%%MatrixMarket matrix coordinate real general\n%d %d %lld\n", M->m, M->n,
+                       (long long)M->nnz);
+    buf.append(line, (size_t)len);
+    const char *fmt = exact ? "%d %d %.17g\n" : "%d %d %20.16g\n";
+    bool ok = true;
+    for (int i = 0; i < M->m && ok; ++i) {
+        const long long p0 = M->rowptr_bits == 64 ? ((const long long *)M->row_ptr)[i] : ((const int *)M->row_ptr)[i];
+        const long long p1 = M->rowptr_bits == 64 ? ((const long long *)M->row_ptr)[i + 1] : ((const int *)M->row_ptr)[i + 1];
+        if (p0 < 0 || p1 < p0 || p1 > M->nnz) { ok = false; break; }
+        for (long long p = p0; p < p1; ++p) {
+            len = snprintf(line, sizeof line, fmt, i + 1, M->col[p] + 1, M->val[p]);
+            buf.append(line, (size_t)len);
+        }
+        if (buf.size() > (1u << 20)) {
+            ok = fwrite(buf.data(), 1, buf.size(), f) == buf.size();
+            buf.clear();
+        }
+    }
+    if (ok && !buf.empty()) ok = fwrite(buf.data(), 1, buf.size(), f) == buf.size();
+    if (fclose(f) != 0) ok = false;
+    if (!ok) { tsg::set_last_error("writing the Matrix Market file failed (or the row pointer is invalid)"); return TSG_ERR_INVALID_ARG; }
+    return TSG_OK;
+}

@@ -33,6 +33,8 @@
 // 12 bytes per C entry written.
 #include "tsg_numeric.cuh"
 
+#include <climits>
+
 namespace tsg {
 
 namespace {
@@ -413,10 +415,9 @@ k_numeric_rows(NumericArgs g, int mybin)
     }
 }
 
-// ---- tile-rows too large for shared memory ----------------------------------
+// ---- rows too large for a shared-memory accumulator ----------------------
 
-// per C tile and row: offset of its segment inside the C row; column indices;
-// zeroed values
+// per row of a global-bin tile-row: column indices and zeroed values
 __global__ void __launch_bounds__(256)
 k_global_prep(NumericArgs g)
 {
@@ -428,87 +429,137 @@ k_global_prep(NumericArgs g)
     const int S = (int)(g.crp[i + 1] - c0);
     for (int r = warp; r < rows; r += 8) {
         const long long Rb = g.rowptrC[r0 + r];
-        int run = 0;
+        long long run = 0;
         for (int sb = 0; sb < S; sb += 32) {
             const int s = sb + lane;
             unsigned mk = (s < S) ? (unsigned)g.cmask[c0 * TILE + (long long)r * S + s] : 0u;
-            int c = __popc(mk);
-            int incl = warp_incl_scan(c, lane);
-            if (s < S) {
-                int off = run + incl - c;
-                g.offC[(c0 + s) * TILE + r] = off;
-                long long dst = Rb + off;
-                const int jb = g.ccol[c0 + s] * TILE - cshift;
-                while (mk) {
-                    const int b = 31 - __clz(mk);
-                    g.colC[dst] = jb + (TILE - 1 - b);
-                    g.valC[dst] = 0.0;
-                    ++dst;
-                    mk &= ~(1u << b);
-                }
+            const int c = __popc(mk);
+            const int incl = warp_incl_scan(c, lane);
+            long long dst = Rb + run + incl - c;
+            const int jb = (s < S) ? g.ccol[c0 + s] * TILE - cshift : 0;
+            while (mk) {
+                const int b = 31 - __clz(mk);
+                g.colC[dst] = jb + (TILE - 1 - b);
+                g.valC[dst] = 0.0;
+                ++dst;
+                mk &= ~(1u << b);
             }
             run += __shfl_sync(0xffffffffu, incl, 31);
         }
     }
 }
 
-// one warp per C row of a global-bin tile-row; accumulates in place
+constexpr int WIDE_W = 4096;   // tile columns per window of the wide-row kernel
+
+// One single-warp CTA per C row of a global-bin tile-row; the values
+// accumulate in place in C (zeroed by k_global_prep).  The row's tile
+// columns are walked in windows of WIDE_W tile columns: for a window the
+// CTA tabulates, by tile column, the row's mask and the offset of its
+// segment in the row (shared memory, 24 KB), then applies A's row in order,
+// each A entry's B row restricted to the window's columns (found by a warp
+// search, then scanned until it leaves the window).  Per output the
+// products still come in A's row order.
 template <bool DUPSAFE>
-__global__ void __launch_bounds__(256, 4)
-k_numeric_global(NumericArgs g)
+__global__ void __launch_bounds__(32, 16)
+k_numeric_wide(NumericArgs g)
 {
-    const int i = g.binlist[(long long)BIN_GLOBAL * g.blkm + (blockIdx.x >> 1)];
-    const int r = (blockIdx.x & 1) * 8 + (threadIdx.x >> 5);
+    __shared__ unsigned s_off[WIDE_W];
+    __shared__ unsigned short s_msk[WIDE_W];
+    const int i = g.binlist[(long long)BIN_GLOBAL * g.blkm + (blockIdx.x >> 4)];
+    const int r = blockIdx.x & (TILE - 1);
     const int R = i * TILE + r;
-    const int lane = threadIdx.x & 31;
     if (R >= g.m) return;
+    const int lane = threadIdx.x;
     const long long c0 = g.crp[i];
     const int S = (int)(g.crp[i + 1] - c0);
-    const int *tc = g.ccol + c0;
     const long long Rb = g.rowptrC[R];
+    if (g.rowptrC[R + 1] == Rb) return;
+    for (int t = lane; t < WIDE_W; t += 32) s_msk[t] = 0;
+    __syncwarp();
+    const uint16_t *mrow = g.cmask + c0 * TILE + (long long)r * S;
+    const int *tcol = g.ccol + c0;
     const int pa0 = (int)g.rpA[R], pa1 = (int)g.rpA[R + 1];
-    for (int pb = pa0; pb < pa1; pb += 32) {
-        const int na = min(32, pa1 - pb);
-        int bs = 0, be = 0;
-        double av = 0.0;
-        if (lane < na) {
-            const int k = g.colA[pb + lane];
-            av = g.valA[pb + lane];
-            bs = (int)g.rpB[k];
-            be = (int)g.rpB[k + 1];
+    unsigned run = 0;     // entries of the row before tile slot s
+    bool bad = false;
+    int s = 0;
+    while (s < S) {
+        // the window starts at the row's next tile with entries
+        {
+            int f = -1;
+            while (s < S) {
+                const int ss = s + lane;
+                const unsigned nz = __ballot_sync(0xffffffffu, ss < S && mrow[ss] != 0);
+                if (nz) { f = __ffs(nz) - 1; break; }
+                s += 32;
+            }
+            if (f < 0) break;
+            s += f;
         }
-        for (int t = 0; t < na; ++t) {
-            const double a = __shfl_sync(0xffffffffu, av, t);
-            const int b0 = __shfl_sync(0xffffffffu, bs, t);
-            const int b1 = __shfl_sync(0xffffffffu, be, t);
-            for (int eb = b0; eb < b1; eb += 32) {
-                const int e = eb + lane;
-                const bool ok = e < b1;
-                const unsigned act = __ballot_sync(0xffffffffu, ok);
-                if (ok) {
-                    const int col = g.colB[e];
-                    const double b = g.valB[e];
-                    const int j = col >> 4, c = col & 15;
-                    int s = lower_bound_dev(tc, S, j);
-                    const bool found = s < S && tc[s] == j;
-                    if (!found) { set_flag(g.flags, FLAG_INTERNAL); s = 0; }
-                    const unsigned mk = g.cmask[c0 * TILE + (long long)r * S + s];
-                    const long long pos = Rb + g.offC[(c0 + s) * TILE + r] + __popc(mk >> (TILE - c));
+        const int j0 = tcol[s];
+        int se = s;
+        for (;;) {
+            const int ss = se + lane;
+            const bool in = ss < S && tcol[ss] < j0 + WIDE_W;
+            const unsigned mk = in ? (unsigned)mrow[ss] : 0u;
+            const int c = __popc(mk);
+            const int incl = warp_incl_scan(c, lane);
+            if (mk) { const int t = tcol[ss] - j0; s_off[t] = run + incl - c; s_msk[t] = (unsigned short)mk; }
+            run += __shfl_sync(0xffffffffu, incl, 31);
+            const int cnt = __popc(__ballot_sync(0xffffffffu, in));   // in-window slots are a prefix
+            se += cnt;
+            if (cnt < 32) break;
+        }
+        __syncwarp();
+        const int lo = j0 * TILE, hi = (j0 + WIDE_W) * TILE;
+        for (int pb = pa0; pb < pa1; pb += 32) {
+            const int na = min(32, pa1 - pb);
+            int bs = 0, be = 0;
+            double av = 0.0;
+            if (lane < na) {
+                const int k = g.colA[pb + lane];
+                av = g.valA[pb + lane];
+                bs = (int)g.rpB[k];
+                be = (int)g.rpB[k + 1];
+            }
+            for (int q = 0; q < na; ++q) {
+                const double a = __shfl_sync(0xffffffffu, av, q);
+                const int b1 = __shfl_sync(0xffffffffu, be, q);
+                const int b0 = warp_lower_bound(g.colB, __shfl_sync(0xffffffffu, bs, q), b1, lo, lane);
+                for (int eb = b0; eb < b1; eb += 32) {
+                    const int e = eb + lane;
+                    const int col = e < b1 ? g.colB[e] : INT_MAX;
+                    const bool ok = col < hi;
+                    long long pos = -1;
+                    double b = 0.0;
+                    if (ok) {
+                        b = g.valB[e];
+                        const int t = (col >> 4) - j0, cc = col & 15;
+                        const unsigned mk = s_msk[t];
+                        if ((mk >> (TILE - 1 - cc)) & 1u) pos = Rb + s_off[t] + __popc(mk >> (TILE - cc));
+                        else bad = true;
+                    }
                     if (!DUPSAFE) {
-                        if (found) g.valC[pos] = fma(a, b, g.valC[pos]);
+                        if (pos >= 0) g.valC[pos] = fma(a, b, g.valC[pos]);
                     } else {
-                        const unsigned peers = __match_any_sync(act, found ? (unsigned)(pos & 0xffffffff) : ~0u - lane);
+                        const unsigned act = __activemask();
+                        const unsigned peers = __match_any_sync(act, pos >= 0 ? pos : -1 - lane);
                         const int rank = __popc(peers & lanemask_lt());
                         const int rounds = __reduce_max_sync(act, __popc(peers));
-                        for (int q = 0; q < rounds; ++q) {
-                            if (q == rank && found) g.valC[pos] = fma(a, b, g.valC[pos]);
+                        for (int q2 = 0; q2 < rounds; ++q2) {
+                            if (q2 == rank && pos >= 0) g.valC[pos] = fma(a, b, g.valC[pos]);
                             __syncwarp(act);
                         }
                     }
+                    if (__ballot_sync(0xffffffffu, !ok)) break;   // the rest of B's row is past the window
                 }
+                __syncwarp();
             }
         }
+        for (int ss = s + lane; ss < se; ss += 32) s_msk[tcol[ss] - j0] = 0;
+        __syncwarp();
+        s = se;
     }
+    if (bad) set_flag(g.flags, FLAG_INTERNAL);
 }
 
 template <int NT, bool DENSE, bool DUPSAFE>
@@ -583,9 +634,9 @@ cudaError_t numeric_run(Pool &pool, const NumericArgs &a, const long long *count
     }
     if (e == cudaSuccess && counts[BIN_GLOBAL] > 0) {
         { k_global_prep<<<(unsigned)counts[BIN_GLOBAL], 256, 0, s>>>(a); ::tsg::count_launch(); }
-        const unsigned g = (unsigned)(counts[BIN_GLOBAL] * 2);
-        if (dupsafe) { k_numeric_global<true><<<g, 256, 0, s>>>(a); ::tsg::count_launch(); }
-        else { k_numeric_global<false><<<g, 256, 0, s>>>(a); ::tsg::count_launch(); }
+        const unsigned g = (unsigned)(counts[BIN_GLOBAL] * TILE);
+        if (dupsafe) { k_numeric_wide<true><<<g, 32, 0, s>>>(a); ::tsg::count_launch(); }
+        else { k_numeric_wide<false><<<g, 32, 0, s>>>(a); ::tsg::count_launch(); }
         e = cudaGetLastError();
     }
     return e;

@@ -99,7 +99,6 @@ struct NumericArgs {
     const unsigned char *bin;
     const int *binlist;   // tile-rows of bin b at binlist[b * blkm + 0 .. counts[b])
     const int *tr_coloff; // per tile-row, subtracted from the column indices written (batched products); may be null
-    int *offC;      // 16 int32 per C tile (global bin only)
     int *flags;
 };
 

@@ -19,6 +19,8 @@
 #include "tsg_internal.cuh"
 #include "tsg_numeric.cuh"
 
+#include <climits>
+
 namespace tsg {
 
 namespace {
@@ -204,16 +206,157 @@ k_step2(int blkm, int m, const int *__restrict__ arp, const int *__restrict__ ac
     }
 }
 
+// Tile-rows with more than `smax` C tiles: the tile slots are taken in
+// windows of `smax`; per window the row masks accumulate in shared memory
+// (OR does not depend on order) and are then written out.  Every window
+// walks the tile-row's A tiles again, with each B tile-row (tile path) or
+// B row (element path) restricted to the window's tile columns by a warp
+// search.
+__global__ void __launch_bounds__(S2_THREADS)
+k_step2_win(int blkm, int m, const int *__restrict__ arp, const int *__restrict__ acol,
+            const uint16_t *__restrict__ amask, const int *__restrict__ brp, const int *__restrict__ bcol,
+            const uint16_t *__restrict__ bmask, const long long *__restrict__ crp, const int *__restrict__ ccol,
+            uint16_t *cmask, int *rowcnt, int smax, NumericBinParams bp, unsigned char *bin,
+            long long *binstat, int *binlist, int *flags, const int *__restrict__ rows_list,
+            const long long *__restrict__ erpB, const int *__restrict__ ecolB)
+{
+    extern __shared__ __align__(16) unsigned char s_raw[];
+    __shared__ long long s_rowtot[TILE];
+    const int i = rows_list[blockIdx.x];
+    if (i >= blkm) return;
+    const long long c0 = crp[i];
+    const int S = (int)(crp[i + 1] - c0);
+    if (S <= smax) return;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int span = ccol[c0 + S - 1] - ccol[c0] + 1;
+    unsigned *smask = reinterpret_cast<unsigned *>(s_raw);                                   // [16][smax]
+    int *wcol = reinterpret_cast<int *>(s_raw + align16((long long)smax * TILE * 4));        // [smax]
+    unsigned short *map = reinterpret_cast<unsigned short *>(s_raw + align16((long long)smax * TILE * 4) +
+                                                              align16((long long)smax * 4));  // [MAP_MAX]
+    if (tid < TILE) s_rowtot[tid] = 0;
+    const int a0 = arp[i], a1 = arp[i + 1], na = a1 - a0;
+    bool bad = false;
+    for (int s0 = 0; s0 < S; s0 += smax) {
+        const int SW = min(smax, S - s0);
+        for (int t = tid; t < SW * TILE; t += S2_THREADS) smask[t] = 0u;
+        for (int t = tid; t < SW; t += S2_THREADS) wcol[t] = ccol[c0 + s0 + t];
+        __syncthreads();
+        const int jlo = wcol[0], jhi = wcol[SW - 1];
+        const bool use_map = jhi - jlo + 1 <= (int)MAP_MAX;
+        if (use_map) {
+            for (int t = tid; t < jhi - jlo + 1; t += S2_THREADS) map[t] = 0xffffu;
+            __syncthreads();
+            for (int t = tid; t < SW; t += S2_THREADS) map[wcol[t] - jlo] = (unsigned short)t;
+        }
+        __syncthreads();
+        const int wspan = jhi - jlo + 1;
+        for (int a = a0 + warp; a < a1; a += S2_WARPS) {
+            const int kt = acol[a];
+            const int q0 = brp[kt], nq = brp[kt + 1] - q0;
+            const unsigned ma = (lane < TILE) ? (unsigned)amask[(long long)a0 * TILE + (long long)lane * na + (a - a0)] : 0u;
+            const unsigned acols = __brev(__reduce_or_sync(0xffffffffu, ma)) >> 16;
+            int eb0 = 0, eb1 = 0;
+            if (lane < TILE && ((acols >> lane) & 1u)) { eb0 = (int)erpB[kt * TILE + lane]; eb1 = (int)erpB[kt * TILE + lane + 1]; }
+            const int elem_iters = warp_sum_int((eb1 - eb0 + 31) >> 5);
+            if (elem_iters <= 3 * ((nq + 31) >> 5)) {
+                for (unsigned cs = acols; cs; cs &= cs - 1) {
+                    const int c = __ffs(cs) - 1;
+                    const int e1 = __shfl_sync(0xffffffffu, eb1, c);
+                    const int e0 = warp_lower_bound(ecolB, __shfl_sync(0xffffffffu, eb0, c), e1, jlo * TILE, lane);
+                    const unsigned rowsc = __ballot_sync(0xffffffffu, (ma >> (TILE - 1 - c)) & 1u) & 0xffffu;
+                    for (int eb = e0; eb < e1; eb += 32) {
+                        const int e = eb + lane;
+                        const int col = e < e1 ? ecolB[e] : INT_MAX;
+                        const bool ok = (col >> 4) <= jhi;
+                        if (ok) {
+                            const int sl = c_slot(col >> 4, jlo, wspan, use_map ? map : nullptr, wcol, SW);
+                            if (sl < 0) bad = true;
+                            else {
+                                const unsigned bit = 0x8000u >> (col & 15);
+                                for (unsigned rs = rowsc; rs; rs &= rs - 1) atomicOr(&smask[(__ffs(rs) - 1) * SW + sl], bit);
+                            }
+                        }
+                        if (__ballot_sync(0xffffffffu, !ok)) break;
+                    }
+                }
+                continue;
+            }
+            unsigned colrows[TILE];
+#pragma unroll
+            for (int c = 0; c < TILE; ++c) colrows[c] = __ballot_sync(0xffffffffu, (ma >> (TILE - 1 - c)) & 1u) & 0xffffu;
+            const int qs = warp_lower_bound(bcol, q0, q0 + nq, jlo, lane) - q0;
+            for (int qb = qs; qb < nq; qb += 32) {
+                const int q = qb + lane;
+                const int j = q < nq ? bcol[q0 + q] : INT_MAX;
+                const bool ok = j <= jhi;
+                int sl = -1;
+                if (ok) {
+                    sl = c_slot(j, jlo, wspan, use_map ? map : nullptr, wcol, SW);
+                    if (sl < 0) bad = true;
+                }
+                const uint16_t *bq = bmask + (long long)q0 * TILE + q;   // row c of B tile q at bq[c*nq]
+                unsigned brow[TILE];
+#pragma unroll
+                for (int c = 0; c < TILE; ++c) brow[c] = (colrows[c] != 0u && sl >= 0) ? (unsigned)bq[c * nq] : 0u;
+#pragma unroll
+                for (int c = 0; c < TILE; ++c) {
+                    unsigned rowsc = colrows[c];
+                    const unsigned b = brow[c];
+                    while (rowsc) {
+                        const int r = __ffs(rowsc) - 1;
+                        rowsc &= rowsc - 1;
+                        if (b) atomicOr(&smask[r * SW + sl], b);
+                    }
+                }
+                if (__ballot_sync(0xffffffffu, !ok)) break;
+            }
+        }
+        __syncthreads();
+        for (int t = tid; t < SW * TILE; t += S2_THREADS) {
+            const int r = t / SW, sl = t - r * SW;
+            cmask[c0 * TILE + (long long)r * S + s0 + sl] = (uint16_t)smask[t];
+        }
+        for (int r = warp; r < TILE; r += S2_WARPS) {
+            int c = 0;
+            for (int sl = lane; sl < SW; sl += 32) c += __popc(smask[r * SW + sl] & 0xffffu);
+            c = warp_sum_int(c);
+            if (lane == 0) s_rowtot[r] += c;
+        }
+        __syncthreads();
+    }
+    if (bad) set_flag(flags, FLAG_INTERNAL);
+    const int rows = min(TILE, m - i * TILE);
+    if (tid == 0) {
+        long long nnz_tr = 0, max_row = 0;
+        for (int r = 0; r < TILE; ++r) {
+            if (r < rows) rowcnt[i * TILE + r] = (int)s_rowtot[r];
+            nnz_tr += s_rowtot[r];
+            max_row = max(max_row, s_rowtot[r]);
+        }
+        int b;
+        long long req = 0;
+        numeric_classify(bp, S, nnz_tr, span, max_row, b, req);
+        bin[i] = (unsigned char)b;
+        const unsigned long long pos = atomicAdd((unsigned long long *)&binstat[b], 1ull);
+        binlist[(long long)b * blkm + (long long)pos] = i;
+        atomicMax((long long *)&binstat[NBIN + b], req);
+    }
+}
+
 }  // namespace
 
 constexpr int S2_SMAX = 2048;   // tiles per tile-row handled with shared-memory masks
 
 cudaError_t symbolic_init_attributes()
 {
-    cudaError_t e = cudaFuncSetAttribute(k_step2<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)(align16(S2_SMAX * TILE * 4) + align16(S2_SMAX * 4) + align16(MAP_MAX * 2)));
+    const int smem = (int)(align16(S2_SMAX * TILE * 4) + align16(S2_SMAX * 4) + align16(MAP_MAX * 2));
+    cudaError_t e = cudaFuncSetAttribute(k_step2<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(k_step2<false>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 (int)cudaSharedmemCarveoutMaxShared);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_step2_win, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_step2_win, cudaFuncAttributePreferredSharedMemoryCarveout,
                                  (int)cudaSharedmemCarveoutMaxShared);
     return e;
 }
@@ -231,10 +374,12 @@ cudaError_t step2_masks(Pool &pool, const TileCSR &A, const TileCSR &B, int m, i
     { k_step2<false><<<ndefer, S2_THREADS, smem, s>>>(blkm, m, A.trp, A.tcol, A.mask, B.trp, B.tcol, B.mask, crp, ccol,
                                                    cmask, rowcnt, S2_SMAX, map_cap, bp, bin, binstat, binlist, flags, defer_list,
                                                    erpB, ecolB); ::tsg::count_launch(); }
-    if (max_tiles_per_row > S2_SMAX)
-        { k_step2<true><<<ndefer, S2_THREADS, 0, s>>>(blkm, m, A.trp, A.tcol, A.mask, B.trp, B.tcol, B.mask, crp, ccol,
-                                                   cmask, rowcnt, S2_SMAX, 0, bp, bin, binstat, binlist, flags, defer_list,
-                                                   erpB, ecolB); ::tsg::count_launch(); }
+    if (max_tiles_per_row > S2_SMAX) {
+        const size_t wsmem = (size_t)(align16(S2_SMAX * TILE * 4) + align16(S2_SMAX * 4) + align16(MAP_MAX * 2));
+        { k_step2_win<<<ndefer, S2_THREADS, wsmem, s>>>(blkm, m, A.trp, A.tcol, A.mask, B.trp, B.tcol, B.mask, crp, ccol,
+                                                      cmask, rowcnt, S2_SMAX, bp, bin, binstat, binlist, flags, defer_list,
+                                                      erpB, ecolB); ::tsg::count_launch(); }
+    }
     return cudaGetLastError();
 }
 
