@@ -88,6 +88,9 @@ typedef struct {
     int32_t threads_numeric; /* threads per CTA of the numeric kernels: 128, 256 or 512 (default 256) */
     int32_t row_acc_max;     /* larger tile-rows: largest C row (entries) accumulated in shared memory by the
                                 one-row-per-CTA kernel; longer rows accumulate in C's value array (default 65535) */
+    int32_t numeric_walk;    /* 0 = auto; 1 = lanes over one B row per A entry; 2 = packed (lanes over the row's
+                                flattened (A entry, B entry) pairs).  Auto packs only when a B row repeats a
+                                column. */
 } tsg_opts;
 
 /* Per-call statistics.  Sizes are always filled; times only with phase_times. */
@@ -224,6 +227,38 @@ tsg_status tsg_plan_execute(tsg_ctx *ctx, tsg_plan *plan, const double *valA, co
 int64_t tsg_plan_nnz(const tsg_plan *plan);
 int64_t tsg_plan_device_bytes(const tsg_plan *plan);
 tsg_status tsg_plan_destroy(tsg_ctx *ctx, tsg_plan *plan);
+
+/*
+ * Device-resident numeric step (no counterpart in the reference).
+ *
+ * tsg_plan_create_batched: the symbolic phase of `count` independent
+ *   products op(A[i], B[i]), packed as in tsg_spgemm_batched; such a plan
+ *   runs only through the calls below.  tsg_plan_count: its instance count
+ *   (1 for a plain plan).
+ * tsg_plan_set_values: new operand values into the plan's resident
+ *   buffers: valA holds every instance's A values one after the other
+ *   (instance i from a_offsets[i], tsg_plan_value_offsets), valB likewise
+ *   for A*B.  Host arrays are copied before the call returns; device
+ *   arrays are copied in stream order on the context's stream.
+ * tsg_plan_replay: the numeric step on the resident values into the plan's
+ *   resident C, launched as one CUDA graph (captured at the first replay;
+ *   the first call must not itself be inside a stream capture).
+ *   Asynchronous on the context's stream.
+ * tsg_plan_result: waits for the stream and returns a device view of
+ *   instance `instance` of the resident C (int64 row pointer; owner NULL:
+ *   the memory stays the plan's until the next replay or its destruction).
+ * tsg_plan_tune: times the numeric step's variants (threads per tile-row
+ *   CTA, row walk) on the resident values and keeps the fastest for later
+ *   replays; every variant gives the same bits.
+ */
+tsg_status tsg_plan_create_batched(tsg_ctx *ctx, tsg_op op, int32_t count, const tsg_csr *A, const tsg_csr *B,
+                                   tsg_plan **plan, tsg_stats *stats);
+int32_t tsg_plan_count(const tsg_plan *plan);
+tsg_status tsg_plan_value_offsets(const tsg_plan *plan, int64_t *a_offsets, int64_t *b_offsets);
+tsg_status tsg_plan_set_values(tsg_ctx *ctx, tsg_plan *plan, const double *valA, const double *valB, int32_t where);
+tsg_status tsg_plan_replay(tsg_ctx *ctx, tsg_plan *plan);
+tsg_status tsg_plan_result(tsg_ctx *ctx, tsg_plan *plan, int32_t instance, tsg_csr *C);
+tsg_status tsg_plan_tune(tsg_ctx *ctx, tsg_plan *plan, double *best_ms);
 
 /* ---- serving: continuous batching of requests ------------------------------ */
 

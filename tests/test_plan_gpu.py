@@ -73,3 +73,54 @@ def test_plan_outlives_device_operands(ctx):
     rp, col, val = O.spgemm(_with(A, v), _with(A, v))
     assert np.array_equal(C.col, col) and np.array_equal(C.val, val)
     plan.close()
+
+
+@pytest.mark.parametrize("op", ["AA", "AAT", "AB"])
+def test_batched_plan_replay(ctx, op):
+    """Batched plan: new values, graph replays (before and after tuning)
+    give each instance the bits of its own full product."""
+    from tilespgemm_gb300 import matrices as M
+    sizes = [(40, 40), (300, 300), (17, 17), (1200, 1200), (64, 64)]
+    if op == "AA":
+        As = [M.random_sparse(m, m, 6, seed=60 + i) for i, (m, _) in enumerate(sizes)]
+        Bs = None
+    elif op == "AAT":
+        As = [M.random_sparse(m, m + 37, 5, seed=70 + i) for i, (m, _) in enumerate(sizes)]
+        Bs = None
+    else:
+        As = [M.random_sparse(m, m + 11, 5, seed=80 + i) for i, (m, _) in enumerate(sizes)]
+        Bs = [M.random_sparse(m + 11, 200 + 13 * i, 4, seed=90 + i) for i, (m, _) in enumerate(sizes)]
+    plan = ctx.plan_batched(As, Bs, op=op)
+    assert plan.count == len(As)
+    ao, bo = plan.value_offsets()
+    assert ao[-1] == sum(A.nnz for A in As)
+    for rnd in range(3):
+        va = np.concatenate([_newvals(A, 100 * rnd + i) for i, A in enumerate(As)])
+        vb = np.concatenate([_newvals(B, 200 * rnd + i) for i, B in enumerate(Bs)]) if Bs else None
+        plan.set_values(va, vb)
+        if rnd == 1:
+            assert plan.tune() > 0.0
+        plan.replay()
+        plan.replay()   # idempotent on the same values
+        for i, A in enumerate(As):
+            Ai = _with(A, va[ao[i]:ao[i + 1]])
+            Bi = _with(Bs[i], vb[bo[i]:bo[i + 1]]) if Bs else None
+            ref = ctx.spgemm(Ai, Bi, op=op)
+            got = plan.result(i)
+            assert np.array_equal(got.rowptr, np.asarray(ref.rowptr, np.int64))
+            assert np.array_equal(got.col, ref.col)
+            assert np.array_equal(got.val, ref.val)
+    plan.close()
+
+
+def test_plain_plan_replay(ctx):
+    from tilespgemm_gb300 import matrices as M
+    A = M.random_sparse(2500, 2500, 11, seed=99)
+    plan = ctx.plan(A, op="AA")
+    v = _newvals(A, 5)
+    plan.set_values(v)
+    plan.replay()
+    ref = ctx.spgemm(_with(A, v), op="AA")
+    got = plan.result(0)
+    assert np.array_equal(got.col, ref.col) and np.array_equal(got.val, ref.val)
+    plan.close()

@@ -52,7 +52,7 @@ class tsg_opts(C.Structure):
     _fields_ = [
         ("validate", C.c_int32), ("phase_times", C.c_int32), ("out_rowptr_bits", C.c_int32),
         ("dense_tile_min", C.c_int32), ("smem_acc_max", C.c_int32), ("threads_numeric", C.c_int32),
-        ("row_acc_max", C.c_int32),
+        ("row_acc_max", C.c_int32), ("numeric_walk", C.c_int32),
     ]
 
 
@@ -118,6 +118,14 @@ SIGNATURES = {
     "tsg_plan_nnz": (C.c_int64, [C.c_void_p]),
     "tsg_plan_device_bytes": (C.c_int64, [C.c_void_p]),
     "tsg_plan_destroy": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "tsg_plan_create_batched": (C.c_int, [C.c_void_p, C.c_int, C.c_int32, C.POINTER(tsg_csr), C.POINTER(tsg_csr),
+                                          C.POINTER(C.c_void_p), C.POINTER(tsg_stats)]),
+    "tsg_plan_count": (C.c_int32, [C.c_void_p]),
+    "tsg_plan_value_offsets": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "tsg_plan_set_values": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32]),
+    "tsg_plan_replay": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "tsg_plan_result": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(tsg_csr)]),
+    "tsg_plan_tune": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_double)]),
     "tsg_server_opts_default": (None, [C.POINTER(tsg_server_opts)]),
     "tsg_server_create": (C.c_int, [C.POINTER(tsg_server_opts), C.POINTER(C.c_void_p)]),
     "tsg_server_submit": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(tsg_csr), C.POINTER(tsg_csr), C.c_uint64,

@@ -178,19 +178,76 @@ class Plan:
     """The symbolic phase of op(A, B) kept on the device (tsg_plan_*): later
     products with the same patterns and new values run only the numeric step."""
 
-    def __init__(self, ctx: "Context", A: CSR, B: CSR | None, op: str):
-        a, keep_a = A._tsg()
-        b_ptr = None
-        keep_b: list = []
-        if B is not None:
-            b, keep_b = B._tsg()
-            b_ptr = C.byref(b)
+    def __init__(self, ctx: "Context", A, B, op: str, batched: bool = False):
+        """A plain plan of op(A, B), or with batched=True a batched plan of the
+        lists A[i], B[i] (tsg_plan_create_batched)."""
         h = C.c_void_p()
         st = _abi.tsg_stats()
-        check(lib().tsg_plan_create(ctx.handle, _OPS[op], C.byref(a), b_ptr, C.byref(h), C.byref(st)))
-        del keep_a, keep_b
+        if batched:
+            n = len(A)
+            a = (_abi.tsg_csr * n)()
+            keep: list = []
+            for i, X in enumerate(A):
+                s_, k_ = X._tsg()
+                a[i] = s_
+                keep.append(k_)
+            b_ptr = None
+            if B is not None:
+                b = (_abi.tsg_csr * n)()
+                for i, X in enumerate(B):
+                    s_, k_ = X._tsg()
+                    b[i] = s_
+                    keep.append(k_)
+                b_ptr = b
+            check(lib().tsg_plan_create_batched(ctx.handle, _OPS[op], n, a, b_ptr, C.byref(h), C.byref(st)))
+            del keep
+            self.m = self.n = None
+        else:
+            a, keep_a = A._tsg()
+            b_ptr = None
+            keep_b: list = []
+            if B is not None:
+                b, keep_b = B._tsg()
+                b_ptr = C.byref(b)
+            check(lib().tsg_plan_create(ctx.handle, _OPS[op], C.byref(a), b_ptr, C.byref(h), C.byref(st)))
+            del keep_a, keep_b
+            self.m, self.n = A.m, (B.n if B is not None else (A.n if op == "AA" else A.m))
         self._ctx, self.handle, self.op, self.stats = ctx, h, op, st.as_dict()
-        self.m, self.n = A.m, (B.n if B is not None else (A.n if op == "AA" else A.m))
+
+    @property
+    def count(self) -> int:
+        return int(lib().tsg_plan_count(self.handle))
+
+    def value_offsets(self) -> tuple[np.ndarray, np.ndarray]:
+        """Where each instance's values start in set_values' arrays (count+1 each)."""
+        n = self.count
+        ao = np.zeros(n + 1, np.int64)
+        bo = np.zeros(n + 1, np.int64)
+        check(lib().tsg_plan_value_offsets(self.handle, ao.ctypes.data, bo.ctypes.data))
+        return ao, bo
+
+    def set_values(self, valA, valB=None) -> None:
+        """New values (host numpy) for the resident numeric step."""
+        a = np.ascontiguousarray(np.asarray(valA), dtype=np.float64)
+        b = None if valB is None else np.ascontiguousarray(np.asarray(valB), dtype=np.float64)
+        check(lib().tsg_plan_set_values(self._ctx.handle, self.handle, a.ctypes.data if a.size else None,
+                                        (b.ctypes.data if b.size else None) if b is not None else None, _abi.MEM_HOST))
+
+    def replay(self) -> None:
+        """Numeric step on the resident values as one CUDA graph (asynchronous)."""
+        check(lib().tsg_plan_replay(self._ctx.handle, self.handle))
+
+    def tune(self) -> float:
+        """Pick the fastest numeric variant for this plan; returns its time in ms."""
+        ms = C.c_double()
+        check(lib().tsg_plan_tune(self._ctx.handle, self.handle, C.byref(ms)))
+        return ms.value
+
+    def result(self, instance: int = 0) -> CSR:
+        """Host copy of instance `instance` of the resident C (after replay)."""
+        c = _abi.tsg_csr()
+        check(lib().tsg_plan_result(self._ctx.handle, self.handle, int(instance), C.byref(c)))
+        return _download(self._ctx.handle, c)
 
     @property
     def nnz(self) -> int:
@@ -347,6 +404,10 @@ class Context:
     def plan(self, A: CSR, B: CSR | None = None, op: str = "AA") -> Plan:
         """Symbolic phase of op(A, B), kept for numeric-only repeats."""
         return Plan(self, A, B, op)
+
+    def plan_batched(self, As: list, Bs: list | None = None, op: str = "AA") -> Plan:
+        """Symbolic phase of op(A_i, B_i) for all instances, packed (tsg_plan_create_batched)."""
+        return Plan(self, As, Bs, op, batched=True)
 
     def spgemm_tiles(self, A: CSR, B: CSR | None = None, op: str = "AA") -> Tiles:
         """C = op(A, B) in the reference's tile form (tsg_spgemm_tiles)."""

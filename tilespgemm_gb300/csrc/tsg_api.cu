@@ -37,6 +37,7 @@ cudaError_t aux_gather(Pool &pool, const int *perm, const double *src, double *d
 cudaError_t aux_nnzcub(Pool &pool, const long long *rpA, const int *colA, int m, const long long *rpB, int kB,
                        unsigned long long *out);
 cudaError_t aux_mask_popc(Pool &pool, const int *trp, int blkm, const uint16_t *mask, unsigned long long *out);
+cudaError_t aux_rows_increasing(Pool &pool, const long long *rp, const int *col, int m, unsigned long long *out);
 cudaError_t aux_copy_scalars(Pool &pool, const long long *a, long long *da, const int *b, long long *db,
                              const int *c, long long *dc);
 cudaError_t aux_rowptr_narrow(Pool &pool, const long long *in, int *out, long long n);
@@ -111,7 +112,8 @@ namespace {
 enum StatSlot {
     ST_NUMBLKC = 0, ST_MAXS = 1, ST_TILESA = 2, ST_TILESB = 3, ST_NNZCUB = 4, ST_POPCB = 5, ST_NNZC = 6,
     ST_NDEFER = 7,               // tile-rows left to the CTA step-2 kernel
-    ST_BINS = 8,                 // NBIN counts, then NBIN max shared-memory sizes
+    ST_BINS = 8,                 // step 2's bin statistics, BS_SLOTS slots (tsg_numeric.cuh)
+    ST_BUNSORTED = 36,           // B rows whose columns are not strictly increasing
     ST_HFLAGS = 40,              // host mirror only: device flags
     ST_SLOTS = 64
 };
@@ -242,6 +244,7 @@ tsg_status host_wait(tsg_ctx *ctx, int *nsync)
 {
     CUDA_OK(cudaMemcpyAsync(ctx->hstat, ctx->dstat, sizeof(long long) * ST_HFLAGS, cudaMemcpyDeviceToHost, ctx->stream));
     static_assert(FLAG_COUNT <= ST_SLOTS - ST_HFLAGS, "flag mirror");
+    static_assert(ST_BINS + BS_SLOTS <= ST_BUNSORTED && ST_BUNSORTED < ST_HFLAGS, "statistics slots");
     int hflags[FLAG_COUNT];
     CUDA_OK(cudaMemcpyAsync(ctx->hstat + ST_HFLAGS + 16, ctx->dflags, sizeof(int) * FLAG_COUNT, cudaMemcpyDeviceToHost, ctx->stream));
     CUDA_OK(cudaStreamSynchronize(ctx->stream));
@@ -288,8 +291,10 @@ struct PlanData {
     long long *rowptrC = nullptr;
     unsigned char *bin = nullptr;
     int *binlist = nullptr;                        // tile-rows of each bin, NBIN * blkm
-    long long counts[NBIN] = {}, req[NBIN] = {};
+    long long bstat[BS_SLOTS] = {};                // step 2's bin statistics (counts, shared-memory sizes)
+    int *rowlist = nullptr;                        // rows of each row class, NROWCLS * m
     bool dupsafe = false;
+    bool b_increasing = true;                      // every B row's columns strictly increase
     int nsync = 0;
     std::vector<void *> owned;
     template <class T> T *own(Pool &pool, long long n) {
@@ -306,7 +311,7 @@ struct PlanData {
     }
     long long device_bytes() const {
         return 8ll * (m + 1) * 2 + 4ll * (nnzA + nnzB) + 8ll * (nnzA + nnzB) + 8ll * (blkm + 1) +
-               36ll * numblkC + 8ll * (m + 1) + 4ll * NBIN * blkm;
+               36ll * numblkC + 8ll * (m + 1) + 4ll * NBIN * blkm + 4ll * NROWCLS * m;
     }
 };
 
@@ -412,6 +417,13 @@ tsg_status plan_symbolic(tsg_ctx *ctx, Pool &pool, Scratch &sc, tsg_op op, const
         r = build_tiles(pool, sc, dB, TB, ctx);
         if (r) return r;
     }
+    {   // bitmaps of B's tile-rows for step 1's bitmap path
+        TB.bmoff = sc.get<long long>(TB.blkm + 1);
+        TB.bmw = sc.get<unsigned>(tile_bitmap_words_bound(TB));
+        long long *wcount = sc.get<long long>(TB.blkm + 1);
+        if (!TB.bmoff || !TB.bmw || !wcount) return fail(TSG_ERR_OOM, "device pool allocation failed (tile bitmaps)");
+        CUDA_OK(tile_bitmaps(pool, TB, wcount, ctx->dflags));
+    }
     tm.mark();  // 1
 
     // step 1, count: C's tile-row pointer
@@ -428,6 +440,7 @@ tsg_status plan_symbolic(tsg_ctx *ctx, Pool &pool, Scratch &sc, tsg_op op, const
     CUDA_OK(aux_copy_scalars(pool, P.crp + P.blkm, ctx->dstat + ST_NUMBLKC, TA.trp + TA.blkm, ctx->dstat + ST_TILESA,
                              TB.trp + TB.blkm, ctx->dstat + ST_TILESB));
     CUDA_OK(aux_mask_popc(pool, TB.trp, TB.blkm, TB.mask, (unsigned long long *)(ctx->dstat + ST_POPCB)));
+    CUDA_OK(aux_rows_increasing(pool, P.rpB, P.colB, P.k, (unsigned long long *)(ctx->dstat + ST_BUNSORTED)));
     if (want_cub)
         CUDA_OK(aux_nnzcub(pool, P.rpA, P.colA, P.m, P.rpB, P.k, (unsigned long long *)(ctx->dstat + ST_NNZCUB)));
     r = host_wait(ctx, &P.nsync);
@@ -439,6 +452,7 @@ tsg_status plan_symbolic(tsg_ctx *ctx, Pool &pool, Scratch &sc, tsg_op op, const
     P.tilesA = ctx->hstat[ST_TILESA];
     P.tilesB = ctx->hstat[ST_TILESB];
     P.dupsafe = ctx->hstat[ST_POPCB] != P.nnzB;
+    P.b_increasing = ctx->hstat[ST_BUNSORTED] == 0;
     P.nnzcub = ctx->hstat[ST_NNZCUB];
     if (P.numblkC >= (1ll << 31)) return fail(TSG_ERR_NOT_SUPPORTED, "C has %lld tiles; the limit is 2^31-1", P.numblkC);
 
@@ -449,24 +463,24 @@ tsg_status plan_symbolic(tsg_ctx *ctx, Pool &pool, Scratch &sc, tsg_op op, const
     int *rowcnt = sc.get<int>(P.m + 1);
     P.bin = P.own<unsigned char>(pool, P.blkm + 1);
     P.binlist = P.own<int>(pool, (long long)NBIN * P.blkm);
+    P.rowlist = P.own<int>(pool, (long long)NROWCLS * P.m);
     P.rowptrC = P.own<long long>(pool, P.m + 1);
-    if (!P.ccol || !P.cmask || !rowcnt || !P.bin || !P.binlist || !P.rowptrC)
+    if (!P.ccol || !P.cmask || !rowcnt || !P.bin || !P.binlist || !P.rowlist || !P.rowptrC)
         return fail(TSG_ERR_OOM, "device pool allocation failed for C tiles");
     NumericBinParams bp{ctx->opts.dense_tile_min, ctx->opts.smem_acc_max, ctx->opts.row_acc_max};
     CUDA_OK(symbolic_fill_fused(pool, TA, TB, P.m, P.crp, P.ccol, P.cmask, rowcnt, P.bin, bp, ctx->dstat + ST_BINS,
-                                P.binlist, cnt, wide, ctx->dflags, P.rpB, P.colB));
+                                P.binlist, P.rowlist, cnt, wide, ctx->dflags, P.rpB, P.colB));
     tm.mark();  // 2
     CUDA_OK(step2_masks(pool, TA, TB, P.m, P.blkm, P.crp, P.ccol, P.cmask, rowcnt, maxS, maxSpan, bp, P.bin,
-                        ctx->dstat + ST_BINS, P.binlist, ctx->dflags, defer, ndefer, P.rpB, P.colB));
+                        ctx->dstat + ST_BINS, P.binlist, P.rowlist, ctx->dflags, defer, ndefer, P.rpB, P.colB));
     CUDA_OK(scan_i32_to_i64(pool, rowcnt, P.rowptrC, P.m, ctx->dflags));
     CUDA_OK(cudaMemcpyAsync(ctx->dstat + ST_NNZC, P.rowptrC + P.m, sizeof(long long), cudaMemcpyDeviceToDevice,
                             ctx->stream));
     r = host_wait(ctx, &P.nsync);
     if (r) return r;
     P.nnzC = ctx->hstat[ST_NNZC];
-    for (int b = 0; b < NBIN; ++b) {
-        P.counts[b] = ctx->hstat[ST_BINS + b];
-        P.req[b] = ctx->hstat[ST_BINS + NBIN + b];
+    for (int b = 0; b < BS_SLOTS; ++b) {
+        P.bstat[b] = ctx->hstat[ST_BINS + b];
     }
     tm.mark();  // 3
     return TSG_OK;
@@ -474,7 +488,7 @@ tsg_status plan_symbolic(tsg_ctx *ctx, Pool &pool, Scratch &sc, tsg_op op, const
 
 // Numeric phase into caller-provided col/val (nnzC each).
 tsg_status plan_numeric(tsg_ctx *ctx, Pool &pool, PlanData &P, const double *valA, const double *valB, int *col,
-                        double *val, const int *tr_coloff = nullptr)
+                        double *val, const int *tr_coloff = nullptr, int threads = 0, int walk = -1)
 {
     NumericArgs na{};
     na.m = P.m; na.blkm = P.blkm;
@@ -482,8 +496,11 @@ tsg_status plan_numeric(tsg_ctx *ctx, Pool &pool, PlanData &P, const double *val
     na.rpB = P.rpB; na.colB = P.colB; na.valB = valB;
     na.crp = P.crp; na.ccol = P.ccol; na.cmask = P.cmask;
     na.rowptrC = P.rowptrC; na.colC = col; na.valC = val;
-    na.bin = P.bin; na.binlist = P.binlist; na.tr_coloff = tr_coloff; na.flags = ctx->dflags;
-    CUDA_OK(numeric_run(pool, na, P.counts, P.req, P.dupsafe, ctx->opts.threads_numeric));
+    na.bin = P.bin; na.binlist = P.binlist; na.rowlist = P.rowlist; na.b_sorted = P.b_increasing; na.tr_coloff = tr_coloff; na.flags = ctx->dflags;
+    if (walk < 0) walk = ctx->opts.numeric_walk;
+    if (threads <= 0) threads = ctx->opts.threads_numeric;
+    const bool packed = P.dupsafe || walk == 2;
+    CUDA_OK(numeric_run(pool, na, P.bstat, packed, threads));
     return TSG_OK;
 }
 
@@ -494,10 +511,10 @@ void fill_stats(const PlanData &P, tsg_stats *st)
     st->nnz_cub = P.nnzcub;
     st->tiles_a = P.tilesA; st->tiles_b = P.tilesB; st->tiles_c = P.numblkC;
     st->n_syncs = P.nsync;
-    st->bins[0] = (int)P.counts[BIN_EMPTY];
-    st->bins[1] = (int)(P.counts[BIN_SPARSE_S] + P.counts[BIN_SPARSE_L]);
-    st->bins[2] = (int)(P.counts[BIN_DENSE_S] + P.counts[BIN_DENSE_L]);
-    st->bins[3] = (int)(P.counts[BIN_ROWS_S] + P.counts[BIN_ROWS_M] + P.counts[BIN_ROWS_L] + P.counts[BIN_GLOBAL]);
+    st->bins[0] = (int)P.bstat[BIN_EMPTY];
+    st->bins[1] = (int)(P.bstat[BIN_SPARSE_S] + P.bstat[BIN_SPARSE_L]);
+    st->bins[2] = (int)(P.bstat[BIN_DENSE_S] + P.bstat[BIN_DENSE_L]);
+    st->bins[3] = (int)P.bstat[BIN_ROWS];
 }
 
 // Hand C (rowptr copied/narrowed from `rowptr`, col/val adopted) to the
@@ -599,6 +616,7 @@ void tsg_opts_default(tsg_opts *o)
     o->smem_acc_max = 24576;
     o->threads_numeric = 256;
     o->row_acc_max = 65535;
+    o->numeric_walk = 0;
 }
 
 const char *tsg_last_error(void) { return g_err.c_str(); }
@@ -762,6 +780,21 @@ tsg_status tsg_spgemm(tsg_ctx *ctx, tsg_op op, const tsg_csr *A, const tsg_csr *
 struct tsg_plan {
     tsg_ctx *ctx = nullptr;
     PlanData P;
+    // batched plans (count > 0): layout of the packed instances
+    int count = 0;
+    std::vector<int> mi, ni;
+    std::vector<long long> aoff, boff;   // first packed value of each instance (A, and B for A*B), count+1
+    std::vector<long long> ebase, rpoff; // first C entry, first row-pointer entry of each instance
+    int *d_trc = nullptr;                // per tile-row C column offset
+    UnpackDesc *d_ud = nullptr;
+    long long *rp_out = nullptr;         // instances' row pointers, rebased
+    long long *d_ebase = nullptr;
+    // resident result of tsg_plan_replay and its CUDA graph
+    int *rcol = nullptr;
+    double *rval = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    long long glaunches = 0;             // kernel launches in the graph
+    int threads = 0, walk = -1;          // numeric settings picked by tsg_plan_tune (0 / -1: the context's)
 };
 
 extern "C" {
@@ -804,6 +837,7 @@ tsg_status tsg_plan_execute(tsg_ctx *ctx, tsg_plan *plan, const double *valA, co
     if (plan->ctx != ctx) return fail(TSG_ERR_INVALID_ARG, "plan belongs to another context");
     if (where != TSG_MEM_HOST && where != TSG_MEM_DEVICE) return fail(TSG_ERR_INVALID_ARG, "where is not a tsg_mem");
     if (C->where != TSG_MEM_HOST && C->where != TSG_MEM_DEVICE) return fail(TSG_ERR_INVALID_ARG, "C->where is not a tsg_mem");
+    if (plan->count > 0) return fail(TSG_ERR_NOT_SUPPORTED, "a batched plan runs with tsg_plan_set_values + tsg_plan_replay");
     PlanData &P = plan->P;
     if (P.nnzA > 0 && !valA) return fail(TSG_ERR_INVALID_ARG, "valA is NULL");
     if (P.op == TSG_OP_AB && P.nnzB > 0 && !valB) return fail(TSG_ERR_INVALID_ARG, "valB is NULL for A*B");
@@ -857,6 +891,8 @@ tsg_status tsg_plan_destroy(tsg_ctx *ctx, tsg_plan *plan)
     tsg_ctx *c = plan->ctx ? plan->ctx : ctx;
     if (c) {
         cudaSetDevice(c->device);
+        cudaStreamSynchronize(c->stream);
+        if (plan->gexec) cudaGraphExecDestroy(plan->gexec);
         Pool pool{c->pool, c->stream};
         plan->P.release(pool);
         cudaStreamSynchronize(c->stream);
@@ -1454,6 +1490,285 @@ tsg_status tsg_tiles_to_csr_noalloc(tsg_ctx *ctx, const tsg_tiles *T, int64_t *r
         return fail(TSG_ERR_BAD_INPUT, "T's tiles hold %lld entries but T->nnz is %lld", total, (long long)T->nnz);
     CUDA_OK(csr_fill_from_tiles(s, T->m, brp, T->blkcolidx, nnzb, T->ptr, T->col, T->val, rp, col, val));
     CUDA_OK(cudaStreamSynchronize(s));
+    return TSG_OK;
+}
+
+}  // extern "C"
+
+// ---- plans: batched plans, resident results, tuning, graph replay ------------
+//
+// A plan's numeric step can run entirely on the device: tsg_plan_set_values
+// puts new operand values into the plan's resident buffers, tsg_plan_replay
+// launches the numeric step (for A*A^T also the gather of A^T's values, for a
+// batched plan also the per-instance row pointers) into the plan's resident
+// C as one CUDA graph, captured at the first replay, and tsg_plan_result
+// hands out device views of C.  tsg_plan_tune times the numeric step's
+// variants (threads per tile-row CTA, row walk) on the plan and keeps the
+// fastest; all variants give the same bits.
+
+namespace {
+
+// the numeric step of a plan on its resident values into its resident C;
+// stream-ordered, no allocation and no host wait (so it can be captured)
+tsg_status plan_enqueue_numeric(tsg_ctx *ctx, Pool &pool, tsg_plan *pl, int threads, int walk)
+{
+    PlanData &P = pl->P;
+    const double *va = P.valA_buf, *vb = nullptr;
+    if (P.op == TSG_OP_AB) vb = P.valB_buf;
+    else if (P.op == TSG_OP_AA) vb = va;
+    else {
+        CUDA_OK(aux_gather(pool, P.perm, va, P.valB_buf, P.nnzA));
+        vb = P.valB_buf;
+    }
+    tsg_status r = plan_numeric(ctx, pool, P, va, vb, pl->rcol, pl->rval, pl->d_trc, threads, walk);
+    if (r) return r;
+    if (pl->count > 0) {
+        CUDA_OK(batch_unpack(pool, pl->d_ud, pl->count, P.rowptrC, pl->rp_out, 64, pl->d_ebase));
+    }
+    return TSG_OK;
+}
+
+tsg_status plan_resident(tsg_plan *pl, Pool &pool)
+{
+    if (pl->rcol) return TSG_OK;
+    pl->rcol = pl->P.own<int>(pool, pl->P.nnzC);
+    pl->rval = pl->P.own<double>(pool, pl->P.nnzC);
+    if (!pl->rcol || !pl->rval) return fail(TSG_ERR_OOM, "device pool allocation failed for the plan's C");
+    return TSG_OK;
+}
+
+tsg_status plan_check_flags(tsg_ctx *ctx)
+{
+    int hflags[FLAG_COUNT];
+    CUDA_OK(cudaMemcpy(hflags, ctx->dflags, sizeof(hflags), cudaMemcpyDeviceToHost));
+    if (hflags[FLAG_INTERNAL]) return fail(TSG_ERR_CUDA, "internal bound check failed on the device");
+    if (hflags[FLAG_BAD_INPUT]) return fail(TSG_ERR_BAD_INPUT, "an operand was out of range");
+    return TSG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+tsg_status tsg_plan_create_batched(tsg_ctx *ctx, tsg_op op, int32_t count, const tsg_csr *A, const tsg_csr *B,
+                                   tsg_plan **plan, tsg_stats *st)
+{
+    if (!ctx || !plan || (count > 0 && !A)) return fail(TSG_ERR_INVALID_ARG, "ctx/A/plan is NULL");
+    *plan = nullptr;
+    if (count <= 0) return fail(TSG_ERR_INVALID_ARG, "a batched plan needs at least one instance");
+    if (op == TSG_OP_AB && !B) return fail(TSG_ERR_INVALID_ARG, "B is NULL for A*B");
+    if (st) memset(st, 0, sizeof(*st));
+    auto t0 = std::chrono::steady_clock::now();
+    CUDA_OK(cudaSetDevice(ctx->device));
+    for (int i = 0; i < count; ++i) {
+        tsg_status r = check_op(op, &A[i], op == TSG_OP_AB ? &B[i] : nullptr);
+        if (r) return r;
+        if (A[i].where != A[0].where || (op == TSG_OP_AB && B[i].where != A[0].where))
+            return fail(TSG_ERR_INVALID_ARG, "all batch operands must be host, or all device");
+        if (A[i].nnz > 0 && !A[i].val) return fail(TSG_ERR_INVALID_ARG, "instance %d has no values", i);
+    }
+    std::vector<long long> roff(count), koff(count), noff(count);
+    long long M = 0, K = 0, N = 0;
+    for (int i = 0; i < count; ++i) {
+        roff[i] = M; M += round16(A[i].m);
+        koff[i] = K; K += round16(A[i].n);
+        const int ni = op == TSG_OP_AB ? B[i].n : (op == TSG_OP_AA ? A[i].n : A[i].m);
+        noff[i] = N; N += round16(ni);
+    }
+    Pool pool{ctx->pool, ctx->stream};
+    tsg_plan *pl = new tsg_plan();
+    pl->ctx = ctx;
+    pl->count = count;
+    PlanData &P = pl->P;
+    PhaseTimer tm(ctx, false);
+    tsg_status r;
+    {
+        Scratch sc(pool);
+        CUDA_OK(cudaMemsetAsync(ctx->dflags, 0, sizeof(int) * FLAG_COUNT, ctx->stream));
+        tsg_csr pA{}, pB{};
+        r = pack_operands(ctx, pool, sc, count, A, roff, op == TSG_OP_AAT ? koff : (op == TSG_OP_AA ? roff : koff),
+                          M, op == TSG_OP_AA ? M : K, pA);
+        if (!r && op == TSG_OP_AB) r = pack_operands(ctx, pool, sc, count, B, koff, noff, K, N, pB);
+        if (!r) r = plan_symbolic(ctx, pool, sc, op, &pA, op == TSG_OP_AB ? &pB : nullptr, P, true, st != nullptr, tm,
+                                  false);
+        if (!r) r = cudaStreamSynchronize(ctx->stream) == cudaSuccess ? TSG_OK : fail(TSG_ERR_CUDA, "plan build failed");
+    }
+    if (!r) {
+        pl->mi.resize(count); pl->ni.resize(count);
+        pl->aoff.assign(count + 1, 0); pl->boff.assign(count + 1, 0);
+        pl->rpoff.resize(count);
+        std::vector<UnpackDesc> ud(count);
+        std::vector<int> trc((size_t)(M / TILE) + 1, 0);
+        long long rpn = 0;
+        for (int i = 0; i < count; ++i) {
+            pl->mi[i] = A[i].m;
+            pl->ni[i] = op == TSG_OP_AB ? B[i].n : (op == TSG_OP_AA ? A[i].n : A[i].m);
+            pl->aoff[i + 1] = pl->aoff[i] + A[i].nnz;
+            pl->boff[i + 1] = pl->boff[i] + (op == TSG_OP_AB ? B[i].nnz : 0);
+            ud[i].rowoff = roff[i]; ud[i].m = A[i].m;
+            ud[i].coloff = op == TSG_OP_AAT ? roff[i] : noff[i];
+            ud[i].rpoff = rpn;
+            pl->rpoff[i] = rpn;
+            rpn += A[i].m + 1;
+            for (long long t = roff[i] / TILE; t < (roff[i] + round16(A[i].m)) / TILE; ++t) trc[(size_t)t] = (int)ud[i].coloff;
+        }
+        pl->d_trc = P.own<int>(pool, (long long)trc.size());
+        pl->d_ud = P.own<UnpackDesc>(pool, count);
+        pl->rp_out = P.own<long long>(pool, rpn);
+        pl->d_ebase = P.own<long long>(pool, count);
+        if (!pl->d_trc || !pl->d_ud || !pl->rp_out || !pl->d_ebase) r = fail(TSG_ERR_OOM, "device pool allocation failed (batched plan)");
+        if (!r) {
+            CUDA_OK(cudaMemcpyAsync(pl->d_trc, trc.data(), sizeof(int) * trc.size(), cudaMemcpyHostToDevice, ctx->stream));
+            CUDA_OK(cudaMemcpyAsync(pl->d_ud, ud.data(), sizeof(UnpackDesc) * (size_t)count, cudaMemcpyHostToDevice, ctx->stream));
+            CUDA_OK(batch_unpack(pool, pl->d_ud, count, P.rowptrC, pl->rp_out, 64, pl->d_ebase));
+            pl->ebase.resize(count);
+            CUDA_OK(cudaMemcpyAsync(pl->ebase.data(), pl->d_ebase, sizeof(long long) * (size_t)count, cudaMemcpyDeviceToHost, ctx->stream));
+            CUDA_OK(cudaStreamSynchronize(ctx->stream));
+            r = plan_check_flags(ctx);
+        }
+    }
+    if (r) {
+        P.release(pool);
+        cudaStreamSynchronize(ctx->stream);
+        cudaGetLastError();
+        delete pl;
+        return r;
+    }
+    fill_stats(P, st);
+    if (st) st->ms_total = ms_since(t0);
+    *plan = pl;
+    return TSG_OK;
+}
+
+int32_t tsg_plan_count(const tsg_plan *plan) { return plan ? (plan->count > 0 ? plan->count : 1) : 0; }
+
+tsg_status tsg_plan_set_values(tsg_ctx *ctx, tsg_plan *plan, const double *valA, const double *valB, int32_t where)
+{
+    if (!ctx || !plan) return fail(TSG_ERR_INVALID_ARG, "ctx/plan is NULL");
+    if (plan->ctx != ctx) return fail(TSG_ERR_INVALID_ARG, "plan belongs to another context");
+    if (where != TSG_MEM_HOST && where != TSG_MEM_DEVICE) return fail(TSG_ERR_INVALID_ARG, "where is not a tsg_mem");
+    PlanData &P = plan->P;
+    if (P.nnzA > 0 && !valA) return fail(TSG_ERR_INVALID_ARG, "valA is NULL");
+    if (P.op == TSG_OP_AB && P.nnzB > 0 && !valB) return fail(TSG_ERR_INVALID_ARG, "valB is NULL for A*B");
+    CUDA_OK(cudaSetDevice(ctx->device));
+    const cudaMemcpyKind kind = where == TSG_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+    if (P.nnzA > 0) CUDA_OK(cudaMemcpyAsync(P.valA_buf, valA, sizeof(double) * (size_t)P.nnzA, kind, ctx->stream));
+    if (P.op == TSG_OP_AB && P.nnzB > 0)
+        CUDA_OK(cudaMemcpyAsync(P.valB_buf, valB, sizeof(double) * (size_t)P.nnzB, kind, ctx->stream));
+    if (where == TSG_MEM_HOST) CUDA_OK(cudaStreamSynchronize(ctx->stream));   // the caller may reuse host memory
+    return TSG_OK;
+}
+
+tsg_status tsg_plan_replay(tsg_ctx *ctx, tsg_plan *plan)
+{
+    if (!ctx || !plan) return fail(TSG_ERR_INVALID_ARG, "ctx/plan is NULL");
+    if (plan->ctx != ctx) return fail(TSG_ERR_INVALID_ARG, "plan belongs to another context");
+    CUDA_OK(cudaSetDevice(ctx->device));
+    Pool pool{ctx->pool, ctx->stream};
+    if (!plan->gexec) {
+        tsg_status r = plan_resident(plan, pool);
+        if (r) return r;
+        CUDA_OK(cudaStreamSynchronize(ctx->stream));
+        CUDA_OK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+        const long long l0 = g_launches.load(std::memory_order_relaxed);
+        cudaError_t me = cudaMemsetAsync(ctx->dflags, 0, sizeof(int) * FLAG_COUNT, ctx->stream);
+        r = me == cudaSuccess ? plan_enqueue_numeric(ctx, pool, plan, plan->threads, plan->walk)
+                              : fail(TSG_ERR_CUDA, "%s", cudaGetErrorString(me));
+        cudaGraph_t graph = nullptr;
+        const cudaError_t ce = cudaStreamEndCapture(ctx->stream, &graph);
+        // launches issued while capturing run at each replay instead
+        plan->glaunches = g_launches.load(std::memory_order_relaxed) - l0;
+        g_launches.fetch_sub(plan->glaunches, std::memory_order_relaxed);
+        if (!r && ce != cudaSuccess) r = fail(TSG_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
+        if (!r) {
+            const cudaError_t ie = cudaGraphInstantiate(&plan->gexec, graph, 0);
+            if (ie != cudaSuccess) { plan->gexec = nullptr; r = fail(TSG_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ie)); }
+        }
+        if (graph) cudaGraphDestroy(graph);
+        if (r) { cudaGetLastError(); return r; }
+    }
+    CUDA_OK(cudaGraphLaunch(plan->gexec, ctx->stream));
+    g_launches.fetch_add(plan->glaunches, std::memory_order_relaxed);
+    return TSG_OK;
+}
+
+tsg_status tsg_plan_result(tsg_ctx *ctx, tsg_plan *plan, int32_t instance, tsg_csr *C)
+{
+    if (!ctx || !plan || !C) return fail(TSG_ERR_INVALID_ARG, "ctx/plan/C is NULL");
+    if (plan->ctx != ctx) return fail(TSG_ERR_INVALID_ARG, "plan belongs to another context");
+    const int n = plan->count > 0 ? plan->count : 1;
+    if (instance < 0 || instance >= n) return fail(TSG_ERR_INVALID_ARG, "instance %d out of range (%d)", instance, n);
+    if (!plan->rcol) return fail(TSG_ERR_INVALID_ARG, "the plan has no result yet: call tsg_plan_replay");
+    CUDA_OK(cudaSetDevice(ctx->device));
+    CUDA_OK(cudaStreamSynchronize(ctx->stream));
+    tsg_status r = plan_check_flags(ctx);
+    if (r) return r;
+    const PlanData &P = plan->P;
+    *C = tsg_csr{};
+    C->rowptr_bits = 64;
+    C->where = TSG_MEM_DEVICE;
+    C->owner = nullptr;   // a view of the plan's memory
+    if (plan->count == 0) {
+        C->m = P.m; C->n = P.n; C->nnz = P.nnzC;
+        C->row_ptr = P.rowptrC; C->col = plan->rcol; C->val = plan->rval;
+    } else {
+        const long long e0 = plan->ebase[instance];
+        const long long e1 = instance + 1 < plan->count ? plan->ebase[instance + 1] : P.nnzC;
+        C->m = plan->mi[instance]; C->n = plan->ni[instance]; C->nnz = e1 - e0;
+        C->row_ptr = plan->rp_out + plan->rpoff[instance];
+        C->col = plan->rcol + e0; C->val = plan->rval + e0;
+    }
+    return TSG_OK;
+}
+
+tsg_status tsg_plan_value_offsets(const tsg_plan *plan, int64_t *a_offsets, int64_t *b_offsets)
+{
+    if (!plan) return fail(TSG_ERR_INVALID_ARG, "plan is NULL");
+    const int n = plan->count > 0 ? plan->count : 1;
+    for (int i = 0; i <= n; ++i) {
+        if (a_offsets) a_offsets[i] = plan->count > 0 ? plan->aoff[i] : (i ? plan->P.nnzA : 0);
+        if (b_offsets) b_offsets[i] = plan->count > 0 ? plan->boff[i] : (i ? (plan->P.op == TSG_OP_AB ? plan->P.nnzB : 0) : 0);
+    }
+    return TSG_OK;
+}
+
+tsg_status tsg_plan_tune(tsg_ctx *ctx, tsg_plan *plan, double *best_ms)
+{
+    if (!ctx || !plan) return fail(TSG_ERR_INVALID_ARG, "ctx/plan is NULL");
+    if (plan->ctx != ctx) return fail(TSG_ERR_INVALID_ARG, "plan belongs to another context");
+    CUDA_OK(cudaSetDevice(ctx->device));
+    Pool pool{ctx->pool, ctx->stream};
+    tsg_status r = plan_resident(plan, pool);
+    if (r) return r;
+    const int cand_threads[3] = {128, 256, 512};
+    const int cand_walk[2] = {1, 2};
+    float best = 1e30f;
+    int bt = plan->threads, bw = plan->walk;
+    for (int t : cand_threads) {
+        for (int w : cand_walk) {
+            if (w == 1 && plan->P.dupsafe) continue;   // repeated B columns always take the packed walk
+            float tot = 0.f;
+            for (int rep = 0; rep < 4; ++rep) {
+                CUDA_OK(cudaEventRecord(ctx->ev[6], ctx->stream));
+                r = plan_enqueue_numeric(ctx, pool, plan, t, w);
+                if (r) return r;
+                CUDA_OK(cudaEventRecord(ctx->ev[7], ctx->stream));
+                CUDA_OK(cudaEventSynchronize(ctx->ev[7]));
+                float ms = 0.f;
+                CUDA_OK(cudaEventElapsedTime(&ms, ctx->ev[6], ctx->ev[7]));
+                if (rep > 0) tot += ms;   // the first run warms up
+            }
+            if (tot / 3 < best) { best = tot / 3; bt = t; bw = w; }
+        }
+    }
+    r = plan_check_flags(ctx);
+    if (r) return r;
+    if (bt != plan->threads || bw != plan->walk) {
+        plan->threads = bt;
+        plan->walk = bw;
+        if (plan->gexec) { cudaGraphExecDestroy(plan->gexec); plan->gexec = nullptr; }
+    }
+    if (best_ms) *best_ms = best;
     return TSG_OK;
 }
 

@@ -54,6 +54,23 @@ __global__ void k_mask_popc(const int *__restrict__ trp, int blkm, const uint16_
     if ((threadIdx.x & 31) == 0 && acc) atomicAdd(out, acc);
 }
 
+// rows whose columns are not strictly increasing (unsorted or repeated);
+// one warp per row, lanes compare neighbours
+__global__ void k_rows_increasing(const long long *__restrict__ rp, const int *__restrict__ col, int m,
+                                  unsigned long long *out)
+{
+    const int lane = threadIdx.x & 31;
+    unsigned long long cnt = 0;
+    for (long long R = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5; R < m;
+         R += ((long long)gridDim.x * blockDim.x) >> 5) {
+        const long long p0 = rp[R], p1 = rp[R + 1];
+        bool bad = false;
+        for (long long q = p0 + lane; q + 1 < p1; q += 32) bad |= col[q] >= col[q + 1];
+        if (__any_sync(0xffffffffu, bad)) ++cnt;
+    }
+    if (lane == 0 && cnt) atomicAdd(out, cnt);
+}
+
 __global__ void k_copy_scalars(const long long *a, long long *da, const int *b, long long *db, const int *c, long long *dc)
 {
     if (threadIdx.x == 0) { *da = *a; *db = *b; *dc = *c; }
@@ -339,6 +356,15 @@ cudaError_t aux_nnzcub(Pool &pool, const long long *rpA, const int *colA, int m,
 {
     if (m <= 0) return cudaSuccess;
     { k_nnzcub<<<g256(m), 256, 0, pool.stream>>>(rpA, colA, m, rpB, kB, out); ::tsg::count_launch(); }
+    return cudaGetLastError();
+}
+
+cudaError_t aux_rows_increasing(Pool &pool, const long long *rp, const int *col, int m, unsigned long long *out)
+{
+    if (m <= 0) return cudaSuccess;
+    long long g = ((long long)m * 32 + 255) / 256;
+    if (g > 152ll * 16) g = 152ll * 16;
+    { k_rows_increasing<<<(unsigned)g, 256, 0, pool.stream>>>(rp, col, m, out); ::tsg::count_launch(); }
     return cudaGetLastError();
 }
 

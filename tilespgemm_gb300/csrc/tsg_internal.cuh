@@ -132,7 +132,17 @@ struct TileCSR {
     int *trp = nullptr;         // blkm+1 tile-row pointer
     int *tcol = nullptr;        // cap sorted tile columns
     uint16_t *mask = nullptr;   // 16*cap row masks
+    // optional bitmap of each tile-row's tile columns (step 1's bitmap path):
+    // tile-row k's words cover [tcol_first & ~31, tcol_last] at bmw[bmoff[k], bmoff[k+1]);
+    // tile-rows wider than 4,096 tile columns have none
+    long long *bmoff = nullptr; // blkm+1
+    unsigned *bmw = nullptr;
 };
+
+// Bitmaps of T's tile-rows (T.bmoff / T.bmw, allocated by the caller:
+// blkm+1 offsets and tile_bitmap_words_bound(T) words).
+long long tile_bitmap_words_bound(const TileCSR &T);
+cudaError_t tile_bitmaps(Pool &pool, TileCSR &T, long long *wcount, int *flags);
 
 // Exclusive scans (decoupled look-back, one pass): out[i] = sum_{j<i} in[j]
 // and out[n] = total.  The int32-output form flags FLAG_OVERFLOW on overflow.

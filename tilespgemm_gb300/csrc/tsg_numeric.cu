@@ -18,15 +18,19 @@
 // CTA keeps the tile-row's whole CSR segment of values in shared memory,
 // each warp owns C rows (so no two warps touch one output), and for every
 // A entry (R,k) the warp's lanes take B row k's entries, which have distinct
-// columns, so one DFMA instruction updates distinct outputs (rows with
-// duplicate column indices in B take the DUPSAFE variant, which serialises
-// equal targets in B's entry order).  Per output the products are applied in
+// columns, so one DFMA instruction updates distinct outputs.  When B's rows
+// repeat columns the packed walk instead gives each lane one (A entry, B
+// entry) pair of the row's flattened pair sequence and orders lanes that
+// meet in one output (it fills the lanes when B's rows are short too, but
+// measured slower there: these loops are latency-bound, not DFMA-bound).  Per output the products are applied in
 // A's row order, then B's row order: the same order as the CPU reference
 // (thmkl_dcsrmultcsr.c:52-91), so with FMA rounding the two agree bit for bit.
 // The epilogue streams the segment's values out coalesced and expands the
 // masks into column indices.  Dense tile-rows (mean tile nnz >= a threshold)
 // use 16x16 dense accumulators instead (position = slot*256 + r*16 + c).
-// Tile-rows too large for shared memory accumulate in C's value array.
+// Tile-rows too large for one CTA's shared memory take one CTA per row
+// (k_numeric_rows), and rows too large for that accumulate in C's value
+// array (k_numeric_wide).
 //
 // Roofline: the DFMA issue rate bounds the loop (2 FLOP per intermediate
 // product); HBM traffic is A and B once (B rows are re-read from L2) plus
@@ -66,19 +70,6 @@ __device__ __forceinline__ unsigned map_swz(unsigned o) { return o ^ (((o >> 6) 
 
 __device__ __forceinline__ int rank_in_row(unsigned w, int c) {
     return (int)(w >> 16) + __popc((w & 0xffffu) >> (TILE - c));
-}
-
-// slot of tile column j in the tile-row (-1 if it is not one of its tiles)
-__device__ __forceinline__ int slot_of(int j, int jbase, int span, bool use_map, const unsigned short *map,
-                                       const int *scol, int S) {
-    const unsigned off = (unsigned)(j - jbase);
-    if (off >= (unsigned)span) return -1;
-    if (use_map) {
-        const int s = (int)map[map_swz(off)];          // 0xffff marks a column with no C tile
-        return s < S ? s : -1;
-    }
-    const int s = lower_bound_dev(scol, S, j);
-    return (s < S && scol[s] == j) ? s : -1;
 }
 
 struct TileRowSmem {
@@ -141,15 +132,78 @@ __device__ __forceinline__ void numeric_row(const NumericArgs &g, const TileRowS
     if (bad) set_flag(g.flags, FLAG_INTERNAL);
 }
 
-// numeric_row for B operands with repeated columns in a row: lanes that
-// would update the same output are serialised in B's entry order.
-template <bool DENSE>
-__device__ __forceinline__ void numeric_row_dupsafe(const NumericArgs &g, const TileRowSmem &t, bool use_map, int r0,
-                                                    int r, int lane)
+// Packed walk of one C row: the row's (A entry, B entry) pairs, in A's row
+// order then B's row order, are taken 32 at a time, one per lane, whatever
+// the lengths of the B rows.  Lanes whose pairs hit the same output --
+// repeated columns in a B row, or different A entries meeting in one column
+// -- apply their products in lane order, which is pair order, so each
+// output still sees A's row order, then B's.  This is the walk for B
+// operands with repeated columns.  pos_of(col) gives the accumulator index
+// of column col: -1 flags an error (not in C's pattern), other negative
+// values skip the pair (a column outside the caller's range).
+template <class Acc, class PosFn>
+__device__ __forceinline__ void row_walk_packed(const NumericArgs &g, int R, int lane, Acc *acc, PosFn pos_of)
 {
-    const int R = r0 + r;
-    const unsigned *wrow = t.word + r * t.S;
     const int pa0 = (int)g.rpA[R], pa1 = (int)g.rpA[R + 1];
+    bool bad = false;
+    for (int pb = pa0; pb < pa1; pb += 32) {
+        const int na = min(32, pa1 - pb);
+        int bs = 0, len = 0;
+        double av = 0.0;
+        if (lane < na) {
+            const int k = g.colA[pb + lane];
+            av = g.valA[pb + lane];
+            bs = (int)g.rpB[k];
+            len = (int)g.rpB[k + 1] - bs;
+        }
+        const int incl = warp_incl_scan(len, lane);
+        const int off = incl - len;
+        const int T = __shfl_sync(0xffffffffu, incl, 31);
+        for (int base = 0; base < T; base += 32) {
+            const int tt = base + lane;
+            // q = last lane whose pair range starts at or before tt (non-empty when tt < T)
+            int q = 0;
+#pragma unroll
+            for (int step = 16; step > 0; step >>= 1) {
+                const int oc = __shfl_sync(0xffffffffu, off, q + step);
+                if (oc <= tt) q += step;
+            }
+            const int e = __shfl_sync(0xffffffffu, bs, q) + tt - __shfl_sync(0xffffffffu, off, q);
+            const double a = __shfl_sync(0xffffffffu, av, q);
+            long long pos = -2;
+            double b = 0.0;
+            if (tt < T) {
+                b = g.valB[e];
+                pos = pos_of(g.colB[e]);
+                if (pos == -1) bad = true;
+            }
+            const unsigned peers = __match_any_sync(0xffffffffu, pos >= 0 ? pos : -3ll - lane);
+            const int rank = __popc(peers & lanemask_lt());
+            if (!__any_sync(0xffffffffu, rank > 0)) {
+                if (pos >= 0) acc[pos] = fma(a, b, acc[pos]);
+            } else {
+                const int rounds = __reduce_max_sync(0xffffffffu, __popc(peers));
+                for (int q2 = 0; q2 < rounds; ++q2) {
+                    if (q2 == rank && pos >= 0) acc[pos] = fma(a, b, acc[pos]);
+                    __syncwarp();
+                }
+            }
+            __syncwarp();
+        }
+    }
+    if (bad) set_flag(g.flags, FLAG_INTERNAL);
+}
+
+// One warp applies row R's products whose column lies in [lo, hi), in A's
+// row order then B's (lanes over one B row; B rows without repeated
+// columns).  With sorted B rows the B row is entered by a warp search and
+// left at the first column >= hi; otherwise every entry is tested.
+template <class Acc, class PosFn>
+__device__ __forceinline__ void row_walk_range(const NumericArgs &g, int R, int lane, int lo, int hi, Acc *acc,
+                                               PosFn pos_of)
+{
+    const int pa0 = (int)g.rpA[R], pa1 = (int)g.rpA[R + 1];
+    bool bad = false;
     for (int pb = pa0; pb < pa1; pb += 32) {
         const int na = min(32, pa1 - pb);
         int bs = 0, be = 0;
@@ -160,38 +214,29 @@ __device__ __forceinline__ void numeric_row_dupsafe(const NumericArgs &g, const 
             bs = (int)g.rpB[k];
             be = (int)g.rpB[k + 1];
         }
-        for (int q0 = 0; q0 < na; ++q0) {
-            const double a = __shfl_sync(0xffffffffu, av, q0);
-            const int b0 = __shfl_sync(0xffffffffu, bs, q0);
-            const int b1 = __shfl_sync(0xffffffffu, be, q0);
+        for (int q = 0; q < na; ++q) {
+            const double a = __shfl_sync(0xffffffffu, av, q);
+            const int b1 = __shfl_sync(0xffffffffu, be, q);
+            int b0 = __shfl_sync(0xffffffffu, bs, q);
+            if (g.b_sorted) b0 = warp_lower_bound(g.colB, b0, b1, lo, lane);
             for (int eb = b0; eb < b1; eb += 32) {
                 const int e = eb + lane;
-                const bool ok = e < b1;
-                const unsigned act = __ballot_sync(0xffffffffu, ok);
-                if (ok) {
-                    const int col = g.colB[e];
-                    const double b = g.valB[e];
-                    const int j = col >> 4, c = col & 15;
-                    const int s = slot_of(j, t.jbase, t.span, use_map, t.map, t.scol, t.S);
-                    int pos = -1;
-                    if (s >= 0) pos = DENSE ? (r * t.S + s) * DPAD + c : acc_swz(rank_in_row(wrow[s], c));
-                    const bool okpos = (unsigned)pos < (unsigned)t.nacc;
-                    if (!okpos) { set_flag(g.flags, FLAG_INTERNAL); pos = -1 - lane; }
-                    const unsigned peers = __match_any_sync(act, pos);
-                    const int rank = __popc(peers & lanemask_lt());
-                    const int rounds = __reduce_max_sync(act, __popc(peers));
-                    for (int q = 0; q < rounds; ++q) {
-                        if (q == rank && okpos) t.acc[pos] = fma(a, b, t.acc[pos]);
-                        __syncwarp(act);
-                    }
+                const int col = e < b1 ? g.colB[e] : INT_MAX;
+                if (col >= lo && col < hi) {
+                    const long long pos = pos_of(col);
+                    if (pos < 0) bad = true;
+                    else acc[pos] = fma(a, g.valB[e], acc[pos]);
                 }
+                if (g.b_sorted && __ballot_sync(0xffffffffu, col >= hi)) break;
             }
+            __syncwarp();
         }
     }
+    if (bad) set_flag(g.flags, FLAG_INTERNAL);
 }
 
-template <int NT, bool DENSE, bool DUPSAFE>
-__global__ void __launch_bounds__(NT, 2048 / NT)
+template <int NT, bool DENSE, bool PACKED>
+__global__ void __launch_bounds__(NT, (PACKED ? 1024 : 2048) / NT)
 k_numeric_smem(NumericArgs g, int mybin)
 {
     constexpr int NWARP = NT / 32;
@@ -248,9 +293,17 @@ k_numeric_smem(NumericArgs g, int mybin)
     // warp w owns rows w, w+NWARP, ...
     TileRowSmem t{scol, word, map, acc, S, jbase, span, nacc};
     for (int r = warp; r < rows; r += NWARP) {
-        if (DUPSAFE) numeric_row_dupsafe<DENSE>(g, t, use_map, r0, r, lane);
-        else if (use_map) numeric_row<DENSE, true>(g, t, r0, r, lane);
-        else numeric_row<DENSE, false>(g, t, r0, r, lane);
+        if (PACKED) {
+            const unsigned *wrow = word + r * S;
+            if (use_map)
+                row_walk_packed(g, r0 + r, lane, acc, [&](int col) -> long long { return out_pos<DENSE, true>(t, wrow, r, col); });
+            else
+                row_walk_packed(g, r0 + r, lane, acc, [&](int col) -> long long { return out_pos<DENSE, false>(t, wrow, r, col); });
+        } else if (use_map) {
+            numeric_row<DENSE, true>(g, t, r0, r, lane);
+        } else {
+            numeric_row<DENSE, false>(g, t, r0, r, lane);
+        }
     }
     __syncthreads();
 
@@ -276,8 +329,6 @@ k_numeric_smem(NumericArgs g, int mybin)
         }
     }
 }
-
-// ---- tile-rows whose rows fit shared memory one at a time -------------------
 
 // numeric_row for the row kernel, with B's entries loaded one step ahead:
 // the warp walks the (A entry, 32-entry chunk of its B row) pairs in order
@@ -338,74 +389,106 @@ __device__ __forceinline__ void numeric_row_prefetch(const NumericArgs &g, const
     if (bad) set_flag(g.flags, FLAG_INTERNAL);
 }
 
-// One single-warp CTA per C row of a tile-row in bin `mybin` (a BIN_ROWS_*
-// size class): the row's CSR segment of values in shared memory, addressed
-// as in the tile-row kernel (slot map + this row's packed words), then
-// streamed out.  Used where the whole tile-row's segment does not fit: each
-// CTA holds one row, so the shared memory in use scales with the row, and
-// the rows of one tile-row run on different SMs.
-template <bool DUPSAFE>
-__global__ void __launch_bounds__(32, 32)
-k_numeric_rows(NumericArgs g, int mybin)
+// ---- rows of tile-rows too large for one CTA (BIN_ROWS) --------------------
+
+// Shared-memory view of one C row (row r of tile-row i): the row's packed
+// words word[S] ((offset in the row << 16) | mask), the slot map or the
+// tile columns, and the accumulator.  Built by the CTA's nthr threads.
+struct RowSmem {
+    unsigned *word;
+    unsigned short *map;
+    int *scol;
+    double *acc;
+    int S, jbase, span, nacc;
+    bool use_map;
+};
+
+__device__ __forceinline__ RowSmem row_smem_build(const NumericArgs &g, unsigned char *s_raw, int i, int r,
+                                                  int nnz_r, int tid, int nthr, int *s_part)
 {
-    extern __shared__ __align__(16) unsigned char s_raw[];
-    const int i = g.binlist[(long long)mybin * g.blkm + (blockIdx.x >> 4)];
-    const int r = blockIdx.x & (TILE - 1);
-    const int R = i * TILE + r;
-    if (R >= g.m) return;
-    const int lane = threadIdx.x;
+    RowSmem w;
     const long long c0 = g.crp[i];
-    const int S = (int)(g.crp[i + 1] - c0);
-    const long long Rb = g.rowptrC[R];
-    const int nnz_r = (int)(g.rowptrC[R + 1] - Rb);
-    if (nnz_r == 0) return;
-    const int jbase = g.ccol[c0];
-    const int span = g.ccol[c0 + S - 1] - jbase + 1;
-    const bool use_map = span <= MAP_MAX;
-
-    unsigned *word = reinterpret_cast<unsigned *>(s_raw);
-    unsigned char *p1 = s_raw + align16((long long)S * 4);
-    unsigned short *map = use_map ? reinterpret_cast<unsigned short *>(p1) : nullptr;
-    int *scol = use_map ? nullptr : reinterpret_cast<int *>(p1);
-    double *acc = reinterpret_cast<double *>(p1 + (use_map ? map_bytes(span) : align16((long long)S * 4)));
-
-    if (use_map) {
-        const int span64 = (span + 63) & ~63;
-        for (int t = lane; t < span64; t += 32) map[t] = 0xffffu;
-        __syncwarp();
+    w.S = (int)(g.crp[i + 1] - c0);
+    w.jbase = g.ccol[c0];
+    w.span = g.ccol[c0 + w.S - 1] - w.jbase + 1;
+    w.use_map = w.span <= MAP_MAX;
+    w.word = reinterpret_cast<unsigned *>(s_raw);
+    unsigned char *p1 = s_raw + align16((long long)w.S * 4);
+    w.map = w.use_map ? reinterpret_cast<unsigned short *>(p1) : nullptr;
+    w.scol = w.use_map ? nullptr : reinterpret_cast<int *>(p1);
+    w.acc = reinterpret_cast<double *>(p1 + (w.use_map ? map_bytes(w.span) : align16((long long)w.S * 4)));
+    w.nacc = (nnz_r + 15) & ~15;
+    const int lane = tid & 31, warp = tid >> 5, nw = nthr >> 5;
+    if (w.use_map) {
+        const int span64 = (w.span + 63) & ~63;
+        for (int t = tid; t < span64; t += nthr) w.map[t] = 0xffffu;
+        if (nw > 1) __syncthreads(); else __syncwarp();
     }
-    for (int s = lane; s < S; s += 32) {
+    for (int s = tid; s < w.S; s += nthr) {
         const int j = g.ccol[c0 + s];
-        if (use_map) map[map_swz((unsigned)(j - jbase))] = (unsigned short)s;
-        else scol[s] = j;
+        if (w.use_map) w.map[map_swz((unsigned)(j - w.jbase))] = (unsigned short)s;
+        else w.scol[s] = j;
     }
+    // packed words: warp k scans slots [k*seg, (k+1)*seg); a prefix over the
+    // warps' totals (s_part) gives each segment's start offset
+    const uint16_t *mrow = g.cmask + c0 * TILE + (long long)r * w.S;
+    const int seg = (((w.S + nw - 1) / nw) + 31) & ~31;
+    const int s0 = min(w.S, warp * seg), s1 = min(w.S, s0 + seg);
+    int tot = 0;
+    for (int s = s0 + lane; s < s1; s += 32) tot += __popc((unsigned)mrow[s]);
+    tot = warp_sum_int(tot);
     int run = 0;
-    for (int sb = 0; sb < S; sb += 32) {
+    if (nw > 1) {
+        if (lane == 0) s_part[warp] = tot;
+        __syncthreads();
+        for (int k = 0; k < warp; ++k) run += s_part[k];
+    }
+    for (int sb = s0; sb < s1; sb += 32) {
         const int s = sb + lane;
-        const unsigned mk = (s < S) ? (unsigned)g.cmask[c0 * TILE + (long long)r * S + s] : 0u;
+        const unsigned mk = (s < s1) ? (unsigned)mrow[s] : 0u;
         const int c = __popc(mk);
         const int incl = warp_incl_scan(c, lane);
-        if (s < S) word[s] = ((unsigned)(run + incl - c) << 16) | mk;
+        if (s < s1) w.word[s] = ((unsigned)(run + incl - c) << 16) | mk;
         run += __shfl_sync(0xffffffffu, incl, 31);
     }
-    const int nacc = (nnz_r + 15) & ~15;
     {
-        unsigned long long *z = reinterpret_cast<unsigned long long *>(acc);
-        for (int t = lane; t < nacc; t += 32) z[t] = 0ull;
+        unsigned long long *z = reinterpret_cast<unsigned long long *>(w.acc);
+        for (int t = tid; t < w.nacc; t += nthr) z[t] = 0ull;
     }
-    __syncwarp();
-    TileRowSmem t{scol, word, map, acc, S, jbase, span, nacc};
-    if (DUPSAFE) numeric_row_dupsafe<false>(g, t, use_map, R, 0, lane);
-    else if (use_map) numeric_row_prefetch<true>(g, t, R, lane);
-    else numeric_row_prefetch<false>(g, t, R, lane);
-    __syncwarp();
-    for (int p = lane; p < nnz_r; p += 32) g.valC[Rb + p] = acc[acc_swz(p)];
+    if (nw > 1) __syncthreads(); else __syncwarp();
+    return w;
+}
+
+__device__ __forceinline__ long long row_pos(const RowSmem &w, int col) {
+    const unsigned off = (unsigned)((col >> 4) - w.jbase);
+    if (off >= (unsigned)w.span) return -1;
+    int s;
+    if (w.use_map) {
+        s = (int)w.map[map_swz(off)];
+        if (s >= w.S) return -1;
+    } else {
+        s = lower_bound_dev(w.scol, w.S, col >> 4);
+        if (s >= w.S || w.scol[s] != (col >> 4)) return -1;
+    }
+    const unsigned wd = w.word[s];
+    const int c = col & 15;
+    if (!((wd >> (TILE - 1 - c)) & 1u)) return -1;
+    const int p = rank_in_row(wd, c);
+    return p < w.nacc ? acc_swz(p) : -1;
+}
+
+// values (coalesced) and column indices of one row from its accumulator
+__device__ __forceinline__ void row_epilogue(const NumericArgs &g, const RowSmem &w, int i, long long Rb, int nnz_r,
+                                             int tid, int nthr)
+{
+    for (int p = tid; p < nnz_r; p += nthr) g.valC[Rb + p] = w.acc[acc_swz(p)];
     const int cshift = g.tr_coloff ? g.tr_coloff[i] : 0;
-    for (int s = lane; s < S; s += 32) {
-        const unsigned w = word[s];
-        unsigned mk = w & 0xffffu;
-        long long dst = Rb + (w >> 16);
-        const int jb = (use_map ? g.ccol[c0 + s] : scol[s]) * TILE - cshift;
+    const long long c0 = g.crp[i];
+    for (int s = tid; s < w.S; s += nthr) {
+        const unsigned wd = w.word[s];
+        unsigned mk = wd & 0xffffu;
+        long long dst = Rb + (wd >> 16);
+        const int jb = (w.use_map ? g.ccol[c0 + s] : w.scol[s]) * TILE - cshift;
         while (mk) {
             const int b = 31 - __clz(mk);   // highest bit = smallest local column
             g.colC[dst] = jb + (TILE - 1 - b);
@@ -415,174 +498,191 @@ k_numeric_rows(NumericArgs g, int mybin)
     }
 }
 
-// ---- rows too large for a shared-memory accumulator ----------------------
-
-// per row of a global-bin tile-row: column indices and zeroed values
-__global__ void __launch_bounds__(256)
-k_global_prep(NumericArgs g)
+// One single-warp CTA per row of row class ROW_S or ROW_M: the row's CSR
+// segment of values in shared memory, addressed by the slot map + the row's
+// packed words, then streamed out.  The class bounds the shared memory of
+// its launch, so short rows keep a high occupancy.
+__global__ void __launch_bounds__(32, 32)
+k_numeric_rows(NumericArgs g, int cls, bool packed)
 {
-    const int i = g.binlist[(long long)BIN_GLOBAL * g.blkm + blockIdx.x];
-    const int cshift = g.tr_coloff ? g.tr_coloff[i] : 0;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int r0 = i * TILE, rows = min(TILE, g.m - r0);
-    const long long c0 = g.crp[i];
-    const int S = (int)(g.crp[i + 1] - c0);
-    for (int r = warp; r < rows; r += 8) {
-        const long long Rb = g.rowptrC[r0 + r];
-        long long run = 0;
-        for (int sb = 0; sb < S; sb += 32) {
-            const int s = sb + lane;
-            unsigned mk = (s < S) ? (unsigned)g.cmask[c0 * TILE + (long long)r * S + s] : 0u;
-            const int c = __popc(mk);
-            const int incl = warp_incl_scan(c, lane);
-            long long dst = Rb + run + incl - c;
-            const int jb = (s < S) ? g.ccol[c0 + s] * TILE - cshift : 0;
-            while (mk) {
-                const int b = 31 - __clz(mk);
-                g.colC[dst] = jb + (TILE - 1 - b);
-                g.valC[dst] = 0.0;
-                ++dst;
-                mk &= ~(1u << b);
-            }
-            run += __shfl_sync(0xffffffffu, incl, 31);
-        }
-    }
+    extern __shared__ __align__(16) unsigned char s_raw[];
+    const int R = g.rowlist[(long long)cls * g.m + blockIdx.x];
+    const int i = R >> 4, r = R & (TILE - 1);
+    const int lane = threadIdx.x;
+    const long long Rb = g.rowptrC[R];
+    const int nnz_r = (int)(g.rowptrC[R + 1] - Rb);
+    const RowSmem w = row_smem_build(g, s_raw, i, r, nnz_r, lane, 32, nullptr);
+    TileRowSmem t{w.scol, w.word, w.map, w.acc, w.S, w.jbase, w.span, w.nacc};
+    if (packed) row_walk_packed(g, R, lane, w.acc, [&](int col) -> long long { return row_pos(w, col); });
+    else if (w.use_map) numeric_row_prefetch<true>(g, t, R, lane);
+    else numeric_row_prefetch<false>(g, t, R, lane);
+    __syncwarp();
+    row_epilogue(g, w, i, Rb, nnz_r, lane, 32);
 }
 
-constexpr int WIDE_W = 4096;   // tile columns per window of the wide-row kernel
-
-// One single-warp CTA per C row of a global-bin tile-row; the values
-// accumulate in place in C (zeroed by k_global_prep).  The row's tile
-// columns are walked in windows of WIDE_W tile columns: for a window the
-// CTA tabulates, by tile column, the row's mask and the offset of its
-// segment in the row (shared memory, 24 KB), then applies A's row in order,
-// each A entry's B row restricted to the window's columns (found by a warp
-// search, then scanned until it leaves the window).  Per output the
-// products still come in A's row order.
-template <bool DUPSAFE>
-__global__ void __launch_bounds__(32, 16)
-k_numeric_wide(NumericArgs g)
+// One CTA of ROW_WARPS warps per row of class ROW_L (accumulator up to
+// SMEM_LARGE): the row's entries are split into ROW_WARPS column ranges of
+// about equal size, and warp w applies, in A's row order, only the products
+// whose column falls in its range -- disjoint outputs per warp, so the
+// order per output is unchanged.
+__global__ void __launch_bounds__(ROW_WARPS * 32, 1)
+k_numeric_rows_split(NumericArgs g, bool packed)
 {
-    __shared__ unsigned s_off[WIDE_W];
-    __shared__ unsigned short s_msk[WIDE_W];
-    const int i = g.binlist[(long long)BIN_GLOBAL * g.blkm + (blockIdx.x >> 4)];
-    const int r = blockIdx.x & (TILE - 1);
-    const int R = i * TILE + r;
-    if (R >= g.m) return;
-    const int lane = threadIdx.x;
+    extern __shared__ __align__(16) unsigned char s_raw[];
+    __shared__ int s_part[ROW_WARPS];
+    const int R = g.rowlist[(long long)ROW_L * g.m + blockIdx.x];
+    const int i = R >> 4, r = R & (TILE - 1);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const long long Rb = g.rowptrC[R];
+    const int nnz_r = (int)(g.rowptrC[R + 1] - Rb);
+    const RowSmem w = row_smem_build(g, s_raw, i, r, nnz_r, tid, ROW_WARPS * 32, s_part);
+    // warp's range: the slots whose row offset lies in [e_lo, e_hi)
+    auto first_slot = [&](int e) {
+        int lo = 0, hi = w.S;
+        while (lo < hi) { const int md = (lo + hi) >> 1; if ((int)(w.word[md] >> 16) < e) lo = md + 1; else hi = md; }
+        return lo;
+    };
+    const long long c0 = g.crp[i];
+    auto slot_col = [&](int s) { return (w.use_map ? g.ccol[c0 + s] : w.scol[s]) * TILE; };
+    const int sa = first_slot((int)((long long)nnz_r * warp / ROW_WARPS));
+    const int sb = warp + 1 < ROW_WARPS ? first_slot((int)((long long)nnz_r * (warp + 1) / ROW_WARPS)) : w.S;
+    const int lo = warp == 0 ? INT_MIN : (sa < w.S ? slot_col(sa) : INT_MAX);
+    const int hi = sb < w.S ? slot_col(sb) : INT_MAX;
+    if (lo < hi) {
+        if (packed)
+            row_walk_packed(g, R, lane, w.acc, [&](int col) -> long long {
+                return (col >= lo && col < hi) ? row_pos(w, col) : -2ll; });
+        else
+            row_walk_range(g, R, lane, lo, hi, w.acc, [&](int col) -> long long { return row_pos(w, col); });
+    }
+    __syncthreads();
+    row_epilogue(g, w, i, Rb, nnz_r, tid, ROW_WARPS * 32);
+}
+
+// ---- rows too large for a shared-memory accumulator (ROW_WIDE) -------------
+
+// per wide row (one warp each): column indices and zeroed values
+__global__ void __launch_bounds__(256)
+k_global_prep(NumericArgs g, long long nrows)
+{
+    const long long k = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+    if (k >= nrows) return;
+    const int lane = threadIdx.x & 31;
+    const int R = g.rowlist[(long long)ROW_WIDE * g.m + k];
+    const int i = R >> 4, r = R & (TILE - 1);
+    const int cshift = g.tr_coloff ? g.tr_coloff[i] : 0;
     const long long c0 = g.crp[i];
     const int S = (int)(g.crp[i + 1] - c0);
     const long long Rb = g.rowptrC[R];
-    if (g.rowptrC[R + 1] == Rb) return;
-    for (int t = lane; t < WIDE_W; t += 32) s_msk[t] = 0;
-    __syncwarp();
+    long long run = 0;
+    for (int sb = 0; sb < S; sb += 32) {
+        const int s = sb + lane;
+        unsigned mk = (s < S) ? (unsigned)g.cmask[c0 * TILE + (long long)r * S + s] : 0u;
+        const int c = __popc(mk);
+        const int incl = warp_incl_scan(c, lane);
+        long long dst = Rb + run + incl - c;
+        const int jb = (s < S) ? g.ccol[c0 + s] * TILE - cshift : 0;
+        while (mk) {
+            const int b = 31 - __clz(mk);
+            g.colC[dst] = jb + (TILE - 1 - b);
+            g.valC[dst] = 0.0;
+            ++dst;
+            mk &= ~(1u << b);
+        }
+        run += __shfl_sync(0xffffffffu, incl, 31);
+    }
+}
+
+constexpr int WIDE_W = 2048;   // tile columns per window of the wide-row kernel
+constexpr size_t WIDE_SMEM = (size_t)ROW_WARPS * WIDE_W * (4 + 2);
+
+// One CTA of ROW_WARPS warps per wide row; the values accumulate in place in
+// C (zeroed, and columns written, by k_global_prep).  The row's entries are
+// split into ROW_WARPS column ranges of about equal size (read off C's
+// column indices), and warp w walks its range in windows of at most WIDE_W
+// tile columns: for a window it tabulates, by tile column, the row's mask
+// and the offset of its segment in the row (the warp's own 12 KB of shared
+// memory), then applies A's row in order, each A entry's B row restricted
+// to the window.  Ranges and windows are disjoint in columns, so per output
+// the products still come in A's row order.
+__global__ void __launch_bounds__(ROW_WARPS * 32, 2)
+k_numeric_wide(NumericArgs g, bool packed)
+{
+    extern __shared__ __align__(16) unsigned char s_raw[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    unsigned *s_off = reinterpret_cast<unsigned *>(s_raw) + warp * WIDE_W;
+    unsigned short *s_msk = reinterpret_cast<unsigned short *>(s_raw + (size_t)ROW_WARPS * WIDE_W * 4) + warp * WIDE_W;
+    const int R = g.rowlist[(long long)ROW_WIDE * g.m + blockIdx.x];
+    const int i = R >> 4, r = R & (TILE - 1);
+    const long long c0 = g.crp[i];
+    const int S = (int)(g.crp[i + 1] - c0);
+    const long long Rb = g.rowptrC[R];
+    const int nnz_r = (int)(g.rowptrC[R + 1] - Rb);
     const uint16_t *mrow = g.cmask + c0 * TILE + (long long)r * S;
     const int *tcol = g.ccol + c0;
-    const int pa0 = (int)g.rpA[R], pa1 = (int)g.rpA[R + 1];
-    unsigned run = 0;     // entries of the row before tile slot s
-    bool bad = false;
-    int s = 0;
-    while (s < S) {
-        // the window starts at the row's next tile with entries
-        {
-            int f = -1;
-            while (s < S) {
-                const int ss = s + lane;
-                const unsigned nz = __ballot_sync(0xffffffffu, ss < S && mrow[ss] != 0);
-                if (nz) { f = __ffs(nz) - 1; break; }
-                s += 32;
-            }
-            if (f < 0) break;
-            s += f;
-        }
-        const int j0 = tcol[s];
-        int se = s;
-        for (;;) {
-            const int ss = se + lane;
-            const bool in = ss < S && tcol[ss] < j0 + WIDE_W;
-            const unsigned mk = in ? (unsigned)mrow[ss] : 0u;
+    const int cshift = g.tr_coloff ? g.tr_coloff[i] : 0;
+    // this warp's entries [e0, e1) and their tile columns [t0, t1)
+    const int e0 = (int)((long long)nnz_r * warp / ROW_WARPS), e1 = (int)((long long)nnz_r * (warp + 1) / ROW_WARPS);
+    if (e0 >= e1) return;
+    const int t0 = (g.colC[Rb + e0] + cshift) >> 4;
+    const int t1 = e1 < nnz_r ? (g.colC[Rb + e1] + cshift) >> 4 : INT_MAX;
+    if (t0 >= t1) return;   // the range starts inside the previous warp's last tile column
+    for (int t = lane; t < WIDE_W; t += 32) s_msk[t] = 0;
+    __syncwarp();
+    int sa = warp_lower_bound(tcol, 0, S, t0, lane);
+    while (sa < S && tcol[sa] < t1) {
+        const int j0 = tcol[sa];
+        const int jend = (int)min((long long)t1, (long long)j0 + WIDE_W);
+        const int sb = warp_lower_bound(tcol, sa, S, jend, lane);
+        // offset of the window's first entry in the row, from C's columns
+        unsigned run = (unsigned)warp_lower_bound(g.colC + Rb, 0, nnz_r, j0 * TILE - cshift, lane);
+        for (int s = sa; s < sb; s += 32) {
+            const int ss = s + lane;
+            const unsigned mk = ss < sb ? (unsigned)mrow[ss] : 0u;
             const int c = __popc(mk);
             const int incl = warp_incl_scan(c, lane);
             if (mk) { const int t = tcol[ss] - j0; s_off[t] = run + incl - c; s_msk[t] = (unsigned short)mk; }
             run += __shfl_sync(0xffffffffu, incl, 31);
-            const int cnt = __popc(__ballot_sync(0xffffffffu, in));   // in-window slots are a prefix
-            se += cnt;
-            if (cnt < 32) break;
         }
         __syncwarp();
-        const int lo = j0 * TILE, hi = (j0 + WIDE_W) * TILE;
-        for (int pb = pa0; pb < pa1; pb += 32) {
-            const int na = min(32, pa1 - pb);
-            int bs = 0, be = 0;
-            double av = 0.0;
-            if (lane < na) {
-                const int k = g.colA[pb + lane];
-                av = g.valA[pb + lane];
-                bs = (int)g.rpB[k];
-                be = (int)g.rpB[k + 1];
-            }
-            for (int q = 0; q < na; ++q) {
-                const double a = __shfl_sync(0xffffffffu, av, q);
-                const int b1 = __shfl_sync(0xffffffffu, be, q);
-                const int b0 = warp_lower_bound(g.colB, __shfl_sync(0xffffffffu, bs, q), b1, lo, lane);
-                for (int eb = b0; eb < b1; eb += 32) {
-                    const int e = eb + lane;
-                    const int col = e < b1 ? g.colB[e] : INT_MAX;
-                    const bool ok = col < hi;
-                    long long pos = -1;
-                    double b = 0.0;
-                    if (ok) {
-                        b = g.valB[e];
-                        const int t = (col >> 4) - j0, cc = col & 15;
-                        const unsigned mk = s_msk[t];
-                        if ((mk >> (TILE - 1 - cc)) & 1u) pos = Rb + s_off[t] + __popc(mk >> (TILE - cc));
-                        else bad = true;
-                    }
-                    if (!DUPSAFE) {
-                        if (pos >= 0) g.valC[pos] = fma(a, b, g.valC[pos]);
-                    } else {
-                        const unsigned act = __activemask();
-                        const unsigned peers = __match_any_sync(act, pos >= 0 ? pos : -1 - lane);
-                        const int rank = __popc(peers & lanemask_lt());
-                        const int rounds = __reduce_max_sync(act, __popc(peers));
-                        for (int q2 = 0; q2 < rounds; ++q2) {
-                            if (q2 == rank && pos >= 0) g.valC[pos] = fma(a, b, g.valC[pos]);
-                            __syncwarp(act);
-                        }
-                    }
-                    if (__ballot_sync(0xffffffffu, !ok)) break;   // the rest of B's row is past the window
-                }
-                __syncwarp();
-            }
-        }
-        for (int ss = s + lane; ss < se; ss += 32) s_msk[tcol[ss] - j0] = 0;
+        const int lo = j0 * TILE, hi = jend * TILE;
+        auto pos_of = [&](int col) -> long long {
+            const int t = (col >> 4) - j0, cc = col & 15;
+            const unsigned mk = s_msk[t];
+            return ((mk >> (TILE - 1 - cc)) & 1u) ? Rb + s_off[t] + __popc(mk >> (TILE - cc)) : -1ll;
+        };
+        if (packed)
+            row_walk_packed(g, R, lane, g.valC, [&](int col) -> long long {
+                return (col >= lo && col < hi) ? pos_of(col) : -2ll; });
+        else
+            row_walk_range(g, R, lane, lo, hi, g.valC, pos_of);
+        for (int ss = sa + lane; ss < sb; ss += 32) s_msk[tcol[ss] - j0] = 0;
         __syncwarp();
-        s = se;
+        sa = sb;
     }
-    if (bad) set_flag(g.flags, FLAG_INTERNAL);
 }
 
-template <int NT, bool DENSE, bool DUPSAFE>
+template <int NT, bool DENSE, bool PACKED>
 cudaError_t set_smem_attr() {
-    cudaError_t e = cudaFuncSetAttribute(k_numeric_smem<NT, DENSE, DUPSAFE>,
+    cudaError_t e = cudaFuncSetAttribute(k_numeric_smem<NT, DENSE, PACKED>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_LARGE);
     // the whole unified L1 as shared memory, so occupancy is set by the
     // tile-row's actual request, not by a smaller carveout
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_numeric_smem<NT, DENSE, DUPSAFE>, cudaFuncAttributePreferredSharedMemoryCarveout,
+        e = cudaFuncSetAttribute(k_numeric_smem<NT, DENSE, PACKED>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                  (int)cudaSharedmemCarveoutMaxShared);
     return e;
 }
 
 template <int NT>
-cudaError_t launch_smem(const NumericArgs &a, int bin, long long nrows, long long smem, bool dense, bool dup,
+cudaError_t launch_smem(const NumericArgs &a, int bin, long long nrows, long long smem, bool dense, bool packed,
                         cudaStream_t s) {
     const unsigned grid = (unsigned)nrows;
     if (dense) {
-        if (dup) { k_numeric_smem<NT, true, true><<<grid, NT, smem, s>>>(a, bin); ::tsg::count_launch(); }
+        if (packed) { k_numeric_smem<NT, true, true><<<grid, NT, smem, s>>>(a, bin); ::tsg::count_launch(); }
         else { k_numeric_smem<NT, true, false><<<grid, NT, smem, s>>>(a, bin); ::tsg::count_launch(); }
     } else {
-        if (dup) { k_numeric_smem<NT, false, true><<<grid, NT, smem, s>>>(a, bin); ::tsg::count_launch(); }
+        if (packed) { k_numeric_smem<NT, false, true><<<grid, NT, smem, s>>>(a, bin); ::tsg::count_launch(); }
         else { k_numeric_smem<NT, false, false><<<grid, NT, smem, s>>>(a, bin); ::tsg::count_launch(); }
     }
     return cudaGetLastError();
@@ -602,41 +702,42 @@ cudaError_t numeric_init_attributes()
     TSG_SET(256)
     TSG_SET(512)
 #undef TSG_SET
-    for (int d = 0; d < 2 && e == cudaSuccess; ++d) {
-        const void *f = d ? (const void *)k_numeric_rows<true> : (const void *)k_numeric_rows<false>;
-        e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_LARGE);
+    const void *fs[3] = {(const void *)k_numeric_rows, (const void *)k_numeric_rows_split, (const void *)k_numeric_wide};
+    for (const void *f : fs) {
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_LARGE);
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
     }
     return e;
 }
 
-cudaError_t numeric_run(Pool &pool, const NumericArgs &a, const long long *counts, const long long *req,
-                        bool dupsafe, int threads)
+cudaError_t numeric_run(Pool &pool, const NumericArgs &a, const long long *binstat, bool packed, int threads)
 {
+    const long long *counts = binstat, *req = binstat + NBIN;
     cudaStream_t s = pool.stream;
     cudaError_t e = cudaSuccess;
     for (int b = BIN_SPARSE_S; b <= BIN_DENSE_L && e == cudaSuccess; ++b) {
         if (counts[b] == 0) continue;
         const bool dense = (b == BIN_DENSE_S || b == BIN_DENSE_L);
         const long long smem = req[b];
-        if (threads == 128) e = launch_smem<128>(a, b, counts[b], smem, dense, dupsafe, s);
-        else if (threads == 512) e = launch_smem<512>(a, b, counts[b], smem, dense, dupsafe, s);
-        else e = launch_smem<256>(a, b, counts[b], smem, dense, dupsafe, s);
+        if (threads == 128) e = launch_smem<128>(a, b, counts[b], smem, dense, packed, s);
+        else if (threads == 512) e = launch_smem<512>(a, b, counts[b], smem, dense, packed, s);
+        else e = launch_smem<256>(a, b, counts[b], smem, dense, packed, s);
     }
-    for (int b = BIN_ROWS_S; b <= BIN_ROWS_L && e == cudaSuccess; ++b) {
-        if (counts[b] == 0) continue;
-        const unsigned g = (unsigned)(counts[b] * TILE);
-        const size_t smem = (size_t)req[b];
-        if (dupsafe) { k_numeric_rows<true><<<g, 32, smem, s>>>(a, b); ::tsg::count_launch(); }
-        else { k_numeric_rows<false><<<g, 32, smem, s>>>(a, b); ::tsg::count_launch(); }
+    const long long *rcnt = binstat + BS_ROWCNT, *rreq = binstat + BS_ROWREQ;
+    for (int c = ROW_S; c <= ROW_M && e == cudaSuccess; ++c) {
+        if (rcnt[c] == 0) continue;
+        { k_numeric_rows<<<(unsigned)rcnt[c], 32, (size_t)rreq[c], s>>>(a, c, packed); ::tsg::count_launch(); }
         e = cudaGetLastError();
     }
-    if (e == cudaSuccess && counts[BIN_GLOBAL] > 0) {
-        { k_global_prep<<<(unsigned)counts[BIN_GLOBAL], 256, 0, s>>>(a); ::tsg::count_launch(); }
-        const unsigned g = (unsigned)(counts[BIN_GLOBAL] * TILE);
-        if (dupsafe) { k_numeric_wide<true><<<g, 32, 0, s>>>(a); ::tsg::count_launch(); }
-        else { k_numeric_wide<false><<<g, 32, 0, s>>>(a); ::tsg::count_launch(); }
+    if (e == cudaSuccess && rcnt[ROW_L] > 0) {
+        { k_numeric_rows_split<<<(unsigned)rcnt[ROW_L], ROW_WARPS * 32, (size_t)rreq[ROW_L], s>>>(a, packed); ::tsg::count_launch(); }
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess && rcnt[ROW_WIDE] > 0) {
+        const long long n = rcnt[ROW_WIDE];
+        { k_global_prep<<<(unsigned)((n * 32 + 255) / 256), 256, 0, s>>>(a, n); ::tsg::count_launch(); }
+        { k_numeric_wide<<<(unsigned)n, ROW_WARPS * 32, WIDE_SMEM, s>>>(a, packed); ::tsg::count_launch(); }
         e = cudaGetLastError();
     }
     return e;

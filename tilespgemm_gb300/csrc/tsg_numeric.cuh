@@ -14,12 +14,21 @@ enum NumericBin : int {
     BIN_SPARSE_L = 2,   // same, <= SMEM_LARGE bytes (one CTA per SM)
     BIN_DENSE_S = 3,    // dense 16x16 tile accumulators in shared memory, <= SMEM_SMALL
     BIN_DENSE_L = 4,    // same, <= SMEM_LARGE
-    BIN_ROWS_S = 5,     // one warp (CTA) per C row, the row's accumulator in shared memory, <= ROWS_SMALL bytes
-    BIN_ROWS_M = 6,     // same, <= ROWS_MEDIUM bytes
-    BIN_ROWS_L = 7,     // same, <= SMEM_LARGE bytes
-    BIN_GLOBAL = 8,     // accumulator in C's value array (any size)
-    NBIN = 9
+    BIN_ROWS = 5,       // too large for one CTA: each of its rows is classed on its own (RowClass)
+    NBIN = 6
 };
+
+// Classes of the rows of BIN_ROWS tile-rows; each class is one launch over a
+// list of rows, so a few long rows set neither the shared memory nor the
+// duration of the rest.
+enum RowClass : int {
+    ROW_S = 0,          // single-warp CTA, row accumulator in shared memory, <= ROWS_SMALL bytes
+    ROW_M = 1,          // same, <= ROWS_MEDIUM bytes
+    ROW_L = 2,          // ROW_WARPS warps per row, each a column range of it, <= SMEM_LARGE bytes
+    ROW_WIDE = 3,       // accumulator in C's value array, ROW_WARPS warps over column windows
+    NROWCLS = 4
+};
+constexpr int ROW_WARPS = 8;
 
 // C tile-rows whose masks the fused warp kernel builds (step 1 fill + step 2
 // in one warp): tile-column window at most FUSED_MAX_SPAN, at most
@@ -33,8 +42,7 @@ __host__ __device__ inline bool fused_handles(long long span, long long S) {
 constexpr long long SMEM_SMALL = 48 * 1024;
 constexpr long long SMEM_LARGE = 200 * 1024;
 constexpr long long MAP_MAX = 8192;   // direct tile-column -> slot map when the window is this narrow
-// size classes of the one-row-per-CTA kernel (each class is one launch, so a
-// few large rows do not set the shared memory, and the occupancy, of all)
+// size classes of the row kernels
 constexpr long long ROWS_SMALL = 24 * 1024;
 constexpr long long ROWS_MEDIUM = 64 * 1024;
 
@@ -67,10 +75,10 @@ __host__ __device__ inline long long numeric_row_smem_bytes(long long S, long lo
     return align16(S * 4) + (span <= MAP_MAX ? map_bytes(span) : align16(S * 4)) + ((row_nnz + 15) & ~15ll) * 8;
 }
 
-// Bin of a C tile-row from its tile count S, entries nnz_tr, tile-column
-// window span and largest row max_row; req = its shared-memory bytes.
+// Bin of a C tile-row from its tile count S, entries nnz_tr and tile-column
+// window span; req = its shared-memory bytes.
 __host__ __device__ inline void numeric_classify(const NumericBinParams &bp, long long S, long long nnz_tr, long long span,
-                                                 long long max_row, int &bin, long long &req) {
+                                                 int &bin, long long &req) {
     req = 0;
     if (nnz_tr == 0) { bin = BIN_EMPTY; return; }
     const long long dreq = numeric_smem_bytes(S, nnz_tr, span, true);
@@ -81,13 +89,48 @@ __host__ __device__ inline void numeric_classify(const NumericBinParams &bp, lon
     } else if (nnz_tr <= bp.smem_acc_max && sreq <= SMEM_LARGE && nnz_tr < 65536) {
         bin = sreq <= SMEM_SMALL ? BIN_SPARSE_S : BIN_SPARSE_L;
         req = sreq;
-    } else if (max_row <= bp.row_acc_max && numeric_row_smem_bytes(S, max_row, span) <= SMEM_LARGE &&
-               max_row < 65536) {
-        req = numeric_row_smem_bytes(S, max_row, span);
-        bin = req <= ROWS_SMALL ? BIN_ROWS_S : (req <= ROWS_MEDIUM ? BIN_ROWS_M : BIN_ROWS_L);
     } else {
-        bin = BIN_GLOBAL;
+        bin = BIN_ROWS;
     }
+}
+
+// Class of one row of a BIN_ROWS tile-row; req = its shared-memory bytes.
+__host__ __device__ inline int numeric_row_class(const NumericBinParams &bp, long long S, long long row_nnz,
+                                                 long long span, long long &req) {
+    req = numeric_row_smem_bytes(S, row_nnz, span);
+    if (row_nnz <= bp.row_acc_max && row_nnz < 65536) {
+        if (req <= ROWS_SMALL) return ROW_S;
+        if (req <= ROWS_MEDIUM) return ROW_M;
+        if (req <= SMEM_LARGE) return ROW_L;
+    }
+    req = 0;
+    return ROW_WIDE;
+}
+
+// Layout of the per-call bin statistics (device, then copied to the host):
+// [0, NBIN) tile-rows per bin, [NBIN, 2 NBIN) largest shared memory per bin,
+// then rows per row class and largest shared memory per row class.
+constexpr int BS_ROWCNT = 2 * NBIN;
+constexpr int BS_ROWREQ = 2 * NBIN + NROWCLS;
+constexpr int BS_SLOTS = 2 * NBIN + 2 * NROWCLS;
+
+// Step 2's record of a tile-row's bin (one thread): counts, shared-memory
+// maximum and the bin's work list.
+__device__ __forceinline__ void record_bin(int b, long long req, int i, int blkm, long long *binstat, int *binlist) {
+    const unsigned long long pos = atomicAdd((unsigned long long *)&binstat[b], 1ull);
+    binlist[(long long)b * blkm + (long long)pos] = i;
+    atomicMax((long long *)&binstat[NBIN + b], req);
+}
+
+// ...and of one row R of a BIN_ROWS tile-row (one thread per row).
+__device__ __forceinline__ void record_row(const NumericBinParams &bp, long long S, long long row_nnz, long long span,
+                                           int R, int m, long long *binstat, int *rowlist) {
+    if (row_nnz == 0) return;
+    long long req;
+    const int c = numeric_row_class(bp, S, row_nnz, span, req);
+    const unsigned long long pos = atomicAdd((unsigned long long *)&binstat[BS_ROWCNT + c], 1ull);
+    rowlist[(long long)c * m + (long long)pos] = R;
+    if (req) atomicMax((long long *)&binstat[BS_ROWREQ + c], req);
 }
 
 struct NumericArgs {
@@ -98,6 +141,8 @@ struct NumericArgs {
     const long long *rowptrC; int *colC; double *valC;
     const unsigned char *bin;
     const int *binlist;   // tile-rows of bin b at binlist[b * blkm + 0 .. counts[b])
+    const int *rowlist;   // rows of row class c at rowlist[c * m + 0 .. rowcounts[c])
+    bool b_sorted;        // B's rows have strictly increasing columns (column-range searches allowed)
     const int *tr_coloff; // per tile-row, subtracted from the column indices written (batched products); may be null
     int *flags;
 };
@@ -105,17 +150,17 @@ struct NumericArgs {
 cudaError_t step2_masks(Pool &pool, const TileCSR &A, const TileCSR &B, int m, int blkm, const long long *crp,
                         const int *ccol, uint16_t *cmask, int *rowcnt, int max_tiles_per_row, int max_span,
                         const NumericBinParams &bp, unsigned char *bin, long long *binstat, int *binlist,
-                        int *flags, const int *defer_list, int ndefer, const long long *erpB, const int *ecolB);
+                        int *rowlist, int *flags, const int *defer_list, int ndefer, const long long *erpB,
+                        const int *ecolB);
 
-// Launch the numeric kernels of every non-empty bin.  counts/req are the
-// per-bin tile-row counts and maximum shared-memory sizes from step 2.
-cudaError_t numeric_run(Pool &pool, const NumericArgs &a, const long long *counts, const long long *req,
-                        bool dupsafe, int threads);
+// Launch the numeric kernels of every non-empty bin and row class.
+// binstat is step 2's statistics (layout above), copied to the host.
+cudaError_t numeric_run(Pool &pool, const NumericArgs &a, const long long *binstat, bool packed, int threads);
 
 cudaError_t symbolic_fill_fused(Pool &pool, const TileCSR &A, const TileCSR &B, int m, const long long *crp,
                                 int *ccol, uint16_t *cmask, int *rowcnt, unsigned char *bin,
-                                const NumericBinParams &bp, long long *binstat, int *binlist, int *cnt, int *wide,
-                                int *flags, const long long *erpB, const int *ecolB);
+                                const NumericBinParams &bp, long long *binstat, int *binlist, int *rowlist, int *cnt,
+                                int *wide, int *flags, const long long *erpB, const int *ecolB);
 cudaError_t masks_to_tile_major_i32(Pool &pool, int blkm, const int *rowptr, const uint16_t *src, uint16_t *dst);
 cudaError_t masks_to_tile_major_i64(Pool &pool, int blkm, const long long *rowptr, const uint16_t *src, uint16_t *dst);
 

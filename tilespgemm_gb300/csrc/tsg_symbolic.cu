@@ -50,6 +50,11 @@ __device__ __forceinline__ unsigned or_rows(unsigned ma, const uint16_t *__restr
 
 constexpr int STG = 64;   // B tiles staged per warp at a time
 
+// OR `bits` into 16-bit mask idx of a uint16 array in shared memory (word atomics)
+__device__ __forceinline__ void smask_or(unsigned short *m, int idx, unsigned bits) {
+    atomicOr(reinterpret_cast<unsigned *>(m) + (idx >> 1), bits << ((idx & 1) * 16));
+}
+
 // slot of tile column j in C's tile-row: direct map over the row's window
 // when it is narrow, binary search otherwise; -1 if j is not one of its tiles
 __device__ __forceinline__ int c_slot(int j, int jbase, int span, const unsigned short *map, const int *scol, int S) {
@@ -59,21 +64,19 @@ __device__ __forceinline__ int c_slot(int j, int jbase, int span, const unsigned
     return (s < S && scol[s] == j) ? s : -1;
 }
 
-// GLOBAL = false: masks accumulate in shared memory (tile-rows with at most
-// `smax` tiles); GLOBAL = true: in cmask with global atomics (the rest).
+// Masks accumulate in shared memory (tile-rows with at most `smax` tiles).
 // Work split: a warp takes one A tile (i,k) at a time and its lanes the B
 // tiles of B's tile-row k.  The A tile is transposed once (16 ballots give,
 // for every local column c, the set of rows that use it); then for each c,
 // uniformly across the warp, every lane ORs its B tile's row c into the
 // rows of that set -- one shared atomicOr per A entry and B tile, no search,
 // no per-element branching on the B side.
-template <bool GLOBAL>
 __global__ void __launch_bounds__(S2_THREADS)
 k_step2(int blkm, int m, const int *__restrict__ arp, const int *__restrict__ acol,
         const uint16_t *__restrict__ amask, const int *__restrict__ brp, const int *__restrict__ bcol,
         const uint16_t *__restrict__ bmask, const long long *__restrict__ crp, const int *__restrict__ ccol,
         uint16_t *cmask, int *rowcnt, int smax, int map_cap, NumericBinParams bp, unsigned char *bin,
-        long long *binstat, int *binlist, int *flags, const int *__restrict__ rows_list,
+        long long *binstat, int *binlist, int *rowlist, int *flags, const int *__restrict__ rows_list,
         const long long *__restrict__ erpB, const int *__restrict__ ecolB)
 {
     extern __shared__ __align__(16) unsigned char s_raw[];
@@ -82,28 +85,26 @@ k_step2(int blkm, int m, const int *__restrict__ arp, const int *__restrict__ ac
     if (i >= blkm) return;
     const long long c0 = crp[i];
     const int S = (int)(crp[i + 1] - c0);
-    if (GLOBAL ? (S <= smax) : (S > smax)) return;
+    if (S > smax) return;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int jbase = S > 0 ? ccol[c0] : 0;
     const int span = S > 0 ? ccol[c0 + S - 1] - jbase + 1 : 0;
     if (fused_handles(span, S)) return;     // done by the fused warp kernel
-    unsigned *smask = reinterpret_cast<unsigned *>(s_raw);                        // [16][S] (shared path)
-    int *wcol = reinterpret_cast<int *>(s_raw + (GLOBAL ? 0 : align16((long long)S * TILE * 4)));
+    unsigned short *smask = reinterpret_cast<unsigned short *>(s_raw);          // [16][S]
+    int *wcol = reinterpret_cast<int *>(s_raw + align16((long long)S * TILE * 2));
     unsigned short *map = nullptr;
-    if (!GLOBAL && span <= map_cap)
-        map = reinterpret_cast<unsigned short *>(s_raw + align16((long long)S * TILE * 4) + align16((long long)S * 4));
-    const int *scol = GLOBAL ? (ccol + c0) : wcol;
-    if (!GLOBAL) {
-        for (int t = tid; t < S * TILE; t += S2_THREADS) smask[t] = 0u;
+    if (span <= map_cap)
+        map = reinterpret_cast<unsigned short *>(s_raw + align16((long long)S * TILE * 2) + align16((long long)S * 4));
+    const int *scol = wcol;
+    {
+        unsigned *z = reinterpret_cast<unsigned *>(smask);
+        for (int t = tid; t < (S * TILE + 1) / 2; t += S2_THREADS) z[t] = 0u;
         for (int t = tid; t < S; t += S2_THREADS) wcol[t] = ccol[c0 + t];
         if (map) {
             for (int t = tid; t < span; t += S2_THREADS) map[t] = 0xffffu;
             __syncthreads();
             for (int t = tid; t < S; t += S2_THREADS) map[ccol[c0 + t] - jbase] = (unsigned short)t;
         }
-    } else {
-        unsigned *mw = reinterpret_cast<unsigned *>(cmask) + c0 * 8;
-        for (long long t = tid; t < (long long)S * 8; t += S2_THREADS) mw[t] = 0u;
     }
     if (tid < TILE) s_rowtot[tid] = 0;
     __syncthreads();
@@ -138,8 +139,7 @@ k_step2(int blkm, int m, const int *__restrict__ arp, const int *__restrict__ ac
                     const unsigned bit = 0x8000u >> (col & 15);
                     for (unsigned rs = rowsc; rs; rs &= rs - 1) {
                         const int r = __ffs(rs) - 1;
-                        if (GLOBAL) atomic_or_mask16(cmask, c0 * TILE + (long long)r * S + sl, bit);
-                        else atomicOr(&smask[r * S + sl], bit);
+                        smask_or(smask, r * S + sl, bit);
                     }
                 }
             }
@@ -165,26 +165,21 @@ k_step2(int blkm, int m, const int *__restrict__ arp, const int *__restrict__ ac
                     const int r = __ffs(rowsc) - 1;
                     rowsc &= rowsc - 1;
                     if (!b) continue;
-                    if (GLOBAL) atomic_or_mask16(cmask, c0 * TILE + (long long)r * S + sl, b);
-                    else atomicOr(&smask[r * S + sl], b);
+                    smask_or(smask, r * S + sl, b);
                 }
             }
         }
     }
     if (bad) set_flag(flags, FLAG_INTERNAL);
     __syncthreads();
-    if (GLOBAL) __threadfence();
 
     const int rows = min(TILE, m - i * TILE);
-    if (!GLOBAL) {
-        // both smask and cmask are row-major ([r][s]) within the tile-row
-        for (int t = tid; t < S * TILE; t += S2_THREADS) cmask[c0 * TILE + t] = (uint16_t)smask[t];
-    }
+    // both smask and cmask are row-major ([r][s]) within the tile-row
+    for (int t = tid; t < S * TILE; t += S2_THREADS) cmask[c0 * TILE + t] = smask[t];
     for (int r = warp; r < TILE; r += S2_WARPS) {
         int c = 0;
         for (int s = lane; s < S; s += 32) {
-            unsigned mk = GLOBAL ? (unsigned)__ldcg(cmask + c0 * TILE + (long long)r * S + s) : smask[r * S + s];
-            c += __popc(mk & 0xffffu);
+            c += __popc((unsigned)smask[r * S + s]);
         }
         c = warp_sum_int(c);
         if (lane == 0) {
@@ -193,17 +188,19 @@ k_step2(int blkm, int m, const int *__restrict__ arp, const int *__restrict__ ac
         }
     }
     __syncthreads();
+    __shared__ int s_bin;
     if (tid == 0) {
-        long long nnz_tr = 0, max_row = 0;
-        for (int r = 0; r < TILE; ++r) { nnz_tr += s_rowtot[r]; max_row = max(max_row, s_rowtot[r]); }
+        long long nnz_tr = 0;
+        for (int r = 0; r < TILE; ++r) nnz_tr += s_rowtot[r];
         int b;
         long long req = 0;
-        numeric_classify(bp, S, nnz_tr, span, max_row, b, req);
+        numeric_classify(bp, S, nnz_tr, span, b, req);
         bin[i] = (unsigned char)b;
-        const unsigned long long pos = atomicAdd((unsigned long long *)&binstat[b], 1ull);
-        binlist[(long long)b * blkm + (long long)pos] = i;
-        atomicMax((long long *)&binstat[NBIN + b], req);
+        record_bin(b, req, i, blkm, binstat, binlist);
+        s_bin = b;
     }
+    __syncthreads();
+    if (s_bin == BIN_ROWS && tid < rows) record_row(bp, S, s_rowtot[tid], span, i * TILE + tid, m, binstat, rowlist);
 }
 
 // Tile-rows with more than `smax` C tiles: the tile slots are taken in
@@ -217,7 +214,7 @@ k_step2_win(int blkm, int m, const int *__restrict__ arp, const int *__restrict_
             const uint16_t *__restrict__ amask, const int *__restrict__ brp, const int *__restrict__ bcol,
             const uint16_t *__restrict__ bmask, const long long *__restrict__ crp, const int *__restrict__ ccol,
             uint16_t *cmask, int *rowcnt, int smax, NumericBinParams bp, unsigned char *bin,
-            long long *binstat, int *binlist, int *flags, const int *__restrict__ rows_list,
+            long long *binstat, int *binlist, int *rowlist, int *flags, const int *__restrict__ rows_list,
             const long long *__restrict__ erpB, const int *__restrict__ ecolB)
 {
     extern __shared__ __align__(16) unsigned char s_raw[];
@@ -229,16 +226,19 @@ k_step2_win(int blkm, int m, const int *__restrict__ arp, const int *__restrict_
     if (S <= smax) return;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int span = ccol[c0 + S - 1] - ccol[c0] + 1;
-    unsigned *smask = reinterpret_cast<unsigned *>(s_raw);                                   // [16][smax]
-    int *wcol = reinterpret_cast<int *>(s_raw + align16((long long)smax * TILE * 4));        // [smax]
-    unsigned short *map = reinterpret_cast<unsigned short *>(s_raw + align16((long long)smax * TILE * 4) +
+    unsigned short *smask = reinterpret_cast<unsigned short *>(s_raw);                       // [16][smax]
+    int *wcol = reinterpret_cast<int *>(s_raw + align16((long long)smax * TILE * 2));        // [smax]
+    unsigned short *map = reinterpret_cast<unsigned short *>(s_raw + align16((long long)smax * TILE * 2) +
                                                               align16((long long)smax * 4));  // [MAP_MAX]
     if (tid < TILE) s_rowtot[tid] = 0;
     const int a0 = arp[i], a1 = arp[i + 1], na = a1 - a0;
     bool bad = false;
     for (int s0 = 0; s0 < S; s0 += smax) {
         const int SW = min(smax, S - s0);
-        for (int t = tid; t < SW * TILE; t += S2_THREADS) smask[t] = 0u;
+        {
+            unsigned *z = reinterpret_cast<unsigned *>(smask);
+            for (int t = tid; t < (SW * TILE + 1) / 2; t += S2_THREADS) z[t] = 0u;
+        }
         for (int t = tid; t < SW; t += S2_THREADS) wcol[t] = ccol[c0 + s0 + t];
         __syncthreads();
         const int jlo = wcol[0], jhi = wcol[SW - 1];
@@ -273,7 +273,7 @@ k_step2_win(int blkm, int m, const int *__restrict__ arp, const int *__restrict_
                             if (sl < 0) bad = true;
                             else {
                                 const unsigned bit = 0x8000u >> (col & 15);
-                                for (unsigned rs = rowsc; rs; rs &= rs - 1) atomicOr(&smask[(__ffs(rs) - 1) * SW + sl], bit);
+                                for (unsigned rs = rowsc; rs; rs &= rs - 1) smask_or(smask, (__ffs(rs) - 1) * SW + sl, bit);
                             }
                         }
                         if (__ballot_sync(0xffffffffu, !ok)) break;
@@ -305,7 +305,7 @@ k_step2_win(int blkm, int m, const int *__restrict__ arp, const int *__restrict_
                     while (rowsc) {
                         const int r = __ffs(rowsc) - 1;
                         rowsc &= rowsc - 1;
-                        if (b) atomicOr(&smask[r * SW + sl], b);
+                        if (b) smask_or(smask, r * SW + sl, b);
                     }
                 }
                 if (__ballot_sync(0xffffffffu, !ok)) break;
@@ -314,11 +314,11 @@ k_step2_win(int blkm, int m, const int *__restrict__ arp, const int *__restrict_
         __syncthreads();
         for (int t = tid; t < SW * TILE; t += S2_THREADS) {
             const int r = t / SW, sl = t - r * SW;
-            cmask[c0 * TILE + (long long)r * S + s0 + sl] = (uint16_t)smask[t];
+            cmask[c0 * TILE + (long long)r * S + s0 + sl] = smask[t];
         }
         for (int r = warp; r < TILE; r += S2_WARPS) {
             int c = 0;
-            for (int sl = lane; sl < SW; sl += 32) c += __popc(smask[r * SW + sl] & 0xffffu);
+            for (int sl = lane; sl < SW; sl += 32) c += __popc((unsigned)smask[r * SW + sl]);
             c = warp_sum_int(c);
             if (lane == 0) s_rowtot[r] += c;
         }
@@ -326,33 +326,34 @@ k_step2_win(int blkm, int m, const int *__restrict__ arp, const int *__restrict_
     }
     if (bad) set_flag(flags, FLAG_INTERNAL);
     const int rows = min(TILE, m - i * TILE);
+    __shared__ int s_bin;
     if (tid == 0) {
-        long long nnz_tr = 0, max_row = 0;
+        long long nnz_tr = 0;
         for (int r = 0; r < TILE; ++r) {
             if (r < rows) rowcnt[i * TILE + r] = (int)s_rowtot[r];
             nnz_tr += s_rowtot[r];
-            max_row = max(max_row, s_rowtot[r]);
         }
         int b;
         long long req = 0;
-        numeric_classify(bp, S, nnz_tr, span, max_row, b, req);
+        numeric_classify(bp, S, nnz_tr, span, b, req);
         bin[i] = (unsigned char)b;
-        const unsigned long long pos = atomicAdd((unsigned long long *)&binstat[b], 1ull);
-        binlist[(long long)b * blkm + (long long)pos] = i;
-        atomicMax((long long *)&binstat[NBIN + b], req);
+        record_bin(b, req, i, blkm, binstat, binlist);
+        s_bin = b;
     }
+    __syncthreads();
+    if (s_bin == BIN_ROWS && tid < rows) record_row(bp, S, s_rowtot[tid], span, i * TILE + tid, m, binstat, rowlist);
 }
 
 }  // namespace
 
-constexpr int S2_SMAX = 2048;   // tiles per tile-row handled with shared-memory masks
+constexpr int S2_SMAX = 4096;   // tiles per tile-row (or window) handled with shared-memory masks
 
 cudaError_t symbolic_init_attributes()
 {
-    const int smem = (int)(align16(S2_SMAX * TILE * 4) + align16(S2_SMAX * 4) + align16(MAP_MAX * 2));
-    cudaError_t e = cudaFuncSetAttribute(k_step2<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    const int smem = (int)(align16(S2_SMAX * TILE * 2) + align16(S2_SMAX * 4) + align16(MAP_MAX * 2));
+    cudaError_t e = cudaFuncSetAttribute(k_step2, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_step2<false>, cudaFuncAttributePreferredSharedMemoryCarveout,
+        e = cudaFuncSetAttribute(k_step2, cudaFuncAttributePreferredSharedMemoryCarveout,
                                  (int)cudaSharedmemCarveoutMaxShared);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_step2_win, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e == cudaSuccess)
@@ -364,20 +365,21 @@ cudaError_t symbolic_init_attributes()
 cudaError_t step2_masks(Pool &pool, const TileCSR &A, const TileCSR &B, int m, int blkm, const long long *crp,
                         const int *ccol, uint16_t *cmask, int *rowcnt, int max_tiles_per_row, int max_span,
                         const NumericBinParams &bp, unsigned char *bin, long long *binstat, int *binlist,
-                        int *flags, const int *defer_list, int ndefer, const long long *erpB, const int *ecolB)
+                        int *rowlist, int *flags, const int *defer_list, int ndefer, const long long *erpB,
+                        const int *ecolB)
 {
     cudaStream_t s = pool.stream;
     if (blkm <= 0 || ndefer <= 0) return cudaSuccess;
     const int s_used = max_tiles_per_row < S2_SMAX ? max_tiles_per_row : S2_SMAX;
     const int map_cap = max_span < (int)MAP_MAX ? max_span : (int)MAP_MAX;
-    const size_t smem = (size_t)(align16((long long)s_used * TILE * 4) + align16((long long)s_used * 4) + align16((long long)map_cap * 2));
-    { k_step2<false><<<ndefer, S2_THREADS, smem, s>>>(blkm, m, A.trp, A.tcol, A.mask, B.trp, B.tcol, B.mask, crp, ccol,
-                                                   cmask, rowcnt, S2_SMAX, map_cap, bp, bin, binstat, binlist, flags, defer_list,
+    const size_t smem = (size_t)(align16((long long)s_used * TILE * 2) + align16((long long)s_used * 4) + align16((long long)map_cap * 2));
+    { k_step2<<<ndefer, S2_THREADS, smem, s>>>(blkm, m, A.trp, A.tcol, A.mask, B.trp, B.tcol, B.mask, crp, ccol,
+                                                   cmask, rowcnt, S2_SMAX, map_cap, bp, bin, binstat, binlist, rowlist, flags, defer_list,
                                                    erpB, ecolB); ::tsg::count_launch(); }
     if (max_tiles_per_row > S2_SMAX) {
-        const size_t wsmem = (size_t)(align16(S2_SMAX * TILE * 4) + align16(S2_SMAX * 4) + align16(MAP_MAX * 2));
+        const size_t wsmem = (size_t)(align16(S2_SMAX * TILE * 2) + align16(S2_SMAX * 4) + align16(MAP_MAX * 2));
         { k_step2_win<<<ndefer, S2_THREADS, wsmem, s>>>(blkm, m, A.trp, A.tcol, A.mask, B.trp, B.tcol, B.mask, crp, ccol,
-                                                      cmask, rowcnt, S2_SMAX, bp, bin, binstat, binlist, flags, defer_list,
+                                                      cmask, rowcnt, S2_SMAX, bp, bin, binstat, binlist, rowlist, flags, defer_list,
                                                       erpB, ecolB); ::tsg::count_launch(); }
     }
     return cudaGetLastError();

@@ -24,6 +24,7 @@
 // (count pass, fill pass) and writes 36 bytes per tile.
 #include "tsg_internal.cuh"
 #include "tsg_numeric.cuh"
+#include <algorithm>
 #include <climits>
 
 namespace tsg {
@@ -59,13 +60,23 @@ struct CsrKeys {
             }
         }
     }
+    __device__ void or_bits(unsigned *bm, int kbase, int lane) const {
+        each(lane, 32, [&](int key, int, int) {
+            const int o = key - kbase;
+            atomicOr(&bm[o >> 5], 1u << (o & 31));
+        });
+    }
 };
 
 // Tile columns of C's tile-row i: union over A's tiles (i,k) of B's tile-row k.
 struct UnionKeys {
-    struct Params { const int *arp; const int *acol; const int *brp; const int *bcol; };
-    const int *arp, *acol, *brp, *bcol; int i;
-    __device__ UnionKeys(const Params &p, int row) : arp(p.arp), acol(p.acol), brp(p.brp), bcol(p.bcol), i(row) {}
+    struct Params {
+        const int *arp; const int *acol; const int *brp; const int *bcol;
+        const long long *bmoff = nullptr; const unsigned *bmw = nullptr;   // B's tile-row bitmaps, if built
+    };
+    const int *arp, *acol, *brp, *bcol; const long long *bmoff; const unsigned *bmw; int i;
+    __device__ UnionKeys(const Params &p, int row)
+        : arp(p.arp), acol(p.acol), brp(p.brp), bcol(p.bcol), bmoff(p.bmoff), bmw(p.bmw), i(row) {}
     __device__ void bounds(int start, int stride, int &kmin, int &kmax) const {
         for (int a = arp[i] + start; a < arp[i + 1]; a += stride) {
             int k = acol[a];
@@ -80,6 +91,40 @@ struct UnionKeys {
             for (int q = brp[k] + start; q < q1; q += stride) f(bcol[q], 0, 0);
         }
     }
+    // OR the keys into a warp's bitmap bm whose bit o stands for key kbase+o
+    // (kbase a multiple of 32): per A tile, B's tile-row bitmap word by word
+    // when it has fewer words than keys, else key by key.  The A tiles' B
+    // tile-row descriptors are fetched 32 at a time, one per lane.
+    __device__ void or_bits(unsigned *bm, int kbase, int lane) const {
+        const int a0 = arp[i], a1 = arp[i + 1];
+        for (int ab = a0; ab < a1; ab += 32) {
+            const int nac = min(32, a1 - ab);
+            int q0 = 0, q1 = 0, d = 0;
+            long long w0 = 0, w1 = 0;
+            if (lane < nac) {
+                const int k = acol[ab + lane];
+                q0 = brp[k]; q1 = brp[k + 1];
+                if (bmoff) { w0 = bmoff[k]; w1 = bmoff[k + 1]; }
+                if (q1 > q0) d = ((bcol[q0] & ~31) - kbase) >> 5;
+            }
+            for (int t = 0; t < nac; ++t) {
+                const int tq0 = __shfl_sync(0xffffffffu, q0, t), tq1 = __shfl_sync(0xffffffffu, q1, t);
+                const long long tw0 = __shfl_sync(0xffffffffu, w0, t), tw1 = __shfl_sync(0xffffffffu, w1, t);
+                if (tw1 > tw0 && tw1 - tw0 < tq1 - tq0) {
+                    const int td = __shfl_sync(0xffffffffu, d, t);
+                    for (long long w = tw0 + lane; w < tw1; w += 32) {
+                        const unsigned x = bmw[w];
+                        if (x) atomicOr(&bm[td + (int)(w - tw0)], x);
+                    }
+                } else {
+                    for (int q = tq0 + lane; q < tq1; q += 32) {
+                        const int o = bcol[q] - kbase;
+                        atomicOr(&bm[o >> 5], 1u << (o & 31));
+                    }
+                }
+            }
+        }
+    }
 };
 
 // ---- narrow path: one warp per tile-row ----------------------------------
@@ -89,7 +134,7 @@ __global__ void __launch_bounds__(WPC * 32)
 k_union_count(typename KS::Params P, int nrows, int *cnt, int *wide_list, int *wide_n, int *stat, int *defer_list,
               int *defer_n, int defer_S)
 {
-    __shared__ unsigned s_bm[WPC][NW];
+    __shared__ unsigned s_bm[WPC][NW + 1];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int row = blockIdx.x * WPC + warp;
     if (row >= nrows) return;
@@ -110,13 +155,11 @@ k_union_count(typename KS::Params P, int nrows, int *cnt, int *wide_list, int *w
         return;
     }
     unsigned *bm = s_bm[warp];
-    const int nwords = (int)((span + 31) >> 5);
+    const int kbase = kmin & ~31;
+    const int nwords = ((kmax - kbase) >> 5) + 1;     // at most NW + 1
     for (int w = lane; w < nwords; w += 32) bm[w] = 0;
     __syncwarp();
-    ks.each(lane, 32, [&](int key, int, int) {
-        int o = key - kmin;
-        atomicOr(&bm[o >> 5], 1u << (o & 31));
-    });
+    ks.or_bits(bm, kbase, lane);
     __syncwarp();
     int c = 0;
     for (int w = lane; w < nwords; w += 32) c += __popc(bm[w]);
@@ -203,11 +246,11 @@ static_assert(NW * 32 == FUSED_MAX_SPAN, "fused window");
 __global__ void __launch_bounds__(FWPC * 32)
 k_sym_fused(UnionKeys::Params P, int blkm, int m, const long long *__restrict__ crp, int *ccol,
             const uint16_t *__restrict__ amask, const uint16_t *__restrict__ bmask, uint16_t *cmask, int *rowcnt,
-            unsigned char *bin, NumericBinParams bp, long long *binstat, int *binlist, int *flags,
+            unsigned char *bin, NumericBinParams bp, long long *binstat, int *binlist, int *rowlist, int *flags,
             const long long *__restrict__ erpB, const int *__restrict__ ecolB)
 {
-    __shared__ unsigned s_bm[FWPC][NW];
-    __shared__ unsigned short s_pref[FWPC][NW];
+    __shared__ unsigned s_bm[FWPC][NW + 1];
+    __shared__ unsigned short s_pref[FWPC][NW + 1];
     __shared__ unsigned short s_msk[FWPC][TILE * FSW];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int row = blockIdx.x * FWPC + warp;
@@ -225,15 +268,15 @@ k_sym_fused(UnionKeys::Params P, int blkm, int m, const long long *__restrict__ 
     unsigned *bm = s_bm[warp];
     unsigned short *pref = s_pref[warp];
     unsigned short *msk = s_msk[warp];
-    const int nwords = (int)((span + 31) >> 5);
+    // bit o of bm stands for tile column kbase + o (kbase a multiple of 32)
+    const int kbase = kmin & ~31;
+    const int nwords = ((kmax - kbase) >> 5) + 1;     // at most NW + 1
+    const int wbits = nwords * 32;
     for (int w = lane; w < nwords; w += 32) bm[w] = 0;
     if (S <= FSW)
         for (int t = lane; t < S * TILE; t += 32) msk[t] = 0;
     __syncwarp();
-    ks.each(lane, 32, [&](int key, int, int) {
-        int o = key - kmin;
-        atomicOr(&bm[o >> 5], 1u << (o & 31));
-    });
+    ks.or_bits(bm, kbase, lane);
     __syncwarp();
     {   // sorted tile columns + per-word ranks
         const int wpl = (nwords + 31) >> 5;
@@ -247,7 +290,7 @@ k_sym_fused(UnionKeys::Params P, int blkm, int m, const long long *__restrict__ 
             pref[w] = (unsigned short)run;
             while (x) {
                 const int b = __ffs(x) - 1;
-                ccol[c0 + run] = kmin + w * 32 + b;
+                ccol[c0 + run] = kbase + w * 32 + b;
                 ++run;
                 x &= x - 1;
             }
@@ -289,9 +332,9 @@ k_sym_fused(UnionKeys::Params P, int blkm, int m, const long long *__restrict__ 
                     const int e0 = __shfl_sync(0xffffffffu, eb0, c), e1 = __shfl_sync(0xffffffffu, eb1, c);
                     const unsigned rowsc = __ballot_sync(0xffffffffu, (ma >> (TILE - 1 - c)) & 1u) & 0xffffu;
                     for (int e = e0 + lane; e < e1; e += 32) {
-                        const int o = (ecolB[e] >> 4) - kmin;
+                        const int o = (ecolB[e] >> 4) - kbase;
                         int slot = -1;
-                        if (o >= 0 && o < span) {
+                        if (o >= 0 && o < wbits) {
                             const int w = o >> 5;
                             slot = pref[w] + __popc(bm[w] & ((1u << (o & 31)) - 1u));
                         }
@@ -311,8 +354,8 @@ k_sym_fused(UnionKeys::Params P, int blkm, int m, const long long *__restrict__ 
                 const int q = qb + lane;
                 int slot = -1;
                 if (q < nq) {
-                    const int o = P.bcol[q0 + q] - kmin;
-                    if (o >= 0 && o < span) {
+                    const int o = P.bcol[q0 + q] - kbase;
+                    if (o >= 0 && o < wbits) {
                         const int w = o >> 5;
                         slot = pref[w] + __popc(bm[w] & ((1u << (o & 31)) - 1u));
                     }
@@ -339,25 +382,25 @@ k_sym_fused(UnionKeys::Params P, int blkm, int m, const long long *__restrict__ 
     __syncwarp();
     for (int t = lane; t < S * TILE; t += 32) cmask[c0 * TILE + t] = msk[t];
     long long nnz_tr = 0;
-    int max_row = 0;
+    int mycnt = 0;
     for (int r = 0; r < TILE; ++r) {
         int c = 0;
         for (int sl = lane; sl < S; sl += 32) c += __popc((unsigned)msk[r * S + sl]);
         c = warp_sum_int(c);
         if (lane == 0 && r < rows) rowcnt[row * TILE + r] = c;
+        if (lane == r) mycnt = c;
         nnz_tr += c;
-        max_row = max(max_row, c);
     }
     if (bad) set_flag(flags, FLAG_INTERNAL);
+    int b = 0;
     if (lane == 0) {
-        int b;
         long long req = 0;
-        numeric_classify(bp, S, nnz_tr, span, max_row, b, req);
+        numeric_classify(bp, S, nnz_tr, span, b, req);
         bin[row] = (unsigned char)b;
-        const unsigned long long pos = atomicAdd((unsigned long long *)&binstat[b], 1ull);
-        binlist[(long long)b * blkm + (long long)pos] = row;
-        atomicMax((long long *)&binstat[NBIN + b], req);
+        record_bin(b, req, row, blkm, binstat, binlist);
     }
+    b = __shfl_sync(0xffffffffu, b, 0);
+    if (b == BIN_ROWS && lane < rows) record_row(bp, S, mycnt, span, row * TILE + lane, m, binstat, rowlist);
 }
 
 // Row-major masks of each tile-row -> 16 consecutive masks per tile (the
@@ -743,10 +786,63 @@ cudaError_t csr_to_tile_structure(Pool &pool, const long long *rp, const int *co
 // defer (blkm+1 ints, count pass only): the tile-rows the fused warp kernel
 // leaves to the CTA step-2 kernel (too wide, or more than FUSED_MAX_TILES
 // tiles), then their number; the caller zeroes defer[blkm] first.
+namespace {
+
+// Words of each tile-row's bitmap (0 for tile-rows wider than the narrow
+// window, which never take the bitmap path).
+__global__ void k_bitmap_words(const int *__restrict__ trp, const int *__restrict__ tcol, int blk, long long *nw)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= blk) return;
+    const int t0 = trp[k], t1 = trp[k + 1];
+    long long w = 0;
+    if (t1 > t0) {
+        const int lo = tcol[t0] & ~31, hi = tcol[t1 - 1];
+        if (hi - lo < NW * 32) w = ((hi - lo) >> 5) + 1;
+    }
+    nw[k] = w;
+}
+
+// one warp per tile-row: set the bits of its tile columns (words zeroed before)
+__global__ void k_bitmap_fill(const int *__restrict__ trp, const int *__restrict__ tcol, int blk,
+                              const long long *__restrict__ bmoff, unsigned *bmw)
+{
+    const int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (k >= blk) return;
+    const long long w0 = bmoff[k];
+    if (bmoff[k + 1] == w0) return;
+    const int t0 = trp[k], t1 = trp[k + 1];
+    const int lo = tcol[t0] & ~31;
+    for (int t = t0 + lane; t < t1; t += 32) {
+        const int o = tcol[t] - lo;
+        atomicOr(&bmw[w0 + (o >> 5)], 1u << (o & 31));
+    }
+}
+
+}  // namespace
+
+long long tile_bitmap_words_bound(const TileCSR &T)
+{
+    const long long per = std::min<long long>(NW + 1, (long long)T.blkn / 32 + 2);
+    return (long long)T.blkm * per + 1;
+}
+
+cudaError_t tile_bitmaps(Pool &pool, TileCSR &T, long long *wcount, int *flags)
+{
+    cudaStream_t s = pool.stream;
+    if (T.blkm <= 0) return cudaSuccess;
+    { k_bitmap_words<<<(unsigned)((T.blkm + 255) / 256), 256, 0, s>>>(T.trp, T.tcol, T.blkm, wcount); ::tsg::count_launch(); }
+    cudaError_t e = scan_i64_to_i64(pool, wcount, T.bmoff, T.blkm, flags);
+    if (e == cudaSuccess) e = cudaMemsetAsync(T.bmw, 0, sizeof(unsigned) * (size_t)tile_bitmap_words_bound(T), s);
+    if (e == cudaSuccess) { k_bitmap_fill<<<(unsigned)((T.blkm * 32LL + 255) / 256), 256, 0, s>>>(T.trp, T.tcol, T.blkm, T.bmoff, T.bmw); ::tsg::count_launch(); }
+    if (e == cudaSuccess) e = cudaGetLastError();
+    return e;
+}
+
 cudaError_t tile_symbolic(Pool &pool, const TileCSR &A, const TileCSR &B, long long *crp, int *ccol, int *cnt,
                           int *wide, int *flags, int *stat, bool count_pass, int *defer)
 {
-    UnionKeys::Params P{A.trp, A.tcol, B.trp, B.tcol};
+    UnionKeys::Params P{A.trp, A.tcol, B.trp, B.tcol, B.bmoff, B.bmw};
     return union_structure<UnionKeys, long long>(pool, P, A.blkm, cnt, wide, crp, ccol, nullptr, flags, stat,
                                                  scan_i32_to_i64, count_pass, !count_pass, defer, FUSED_MAX_TILES);
 }
@@ -756,14 +852,14 @@ cudaError_t tile_symbolic(Pool &pool, const TileCSR &A, const TileCSR &B, long l
 // come from step2_masks's CTA kernel).
 cudaError_t symbolic_fill_fused(Pool &pool, const TileCSR &A, const TileCSR &B, int m, const long long *crp,
                                 int *ccol, uint16_t *cmask, int *rowcnt, unsigned char *bin,
-                                const NumericBinParams &bp, long long *binstat, int *binlist, int *cnt, int *wide,
-                                int *flags, const long long *erpB, const int *ecolB)
+                                const NumericBinParams &bp, long long *binstat, int *binlist, int *rowlist, int *cnt,
+                                int *wide, int *flags, const long long *erpB, const int *ecolB)
 {
     cudaStream_t s = pool.stream;
     if (A.blkm <= 0) return cudaSuccess;
-    UnionKeys::Params P{A.trp, A.tcol, B.trp, B.tcol};
+    UnionKeys::Params P{A.trp, A.tcol, B.trp, B.tcol, B.bmoff, B.bmw};
     { k_sym_fused<<<(unsigned)((A.blkm + FWPC - 1) / FWPC), FWPC * 32, 0, s>>>(P, A.blkm, m, crp, ccol, A.mask, B.mask,
-                                                                         cmask, rowcnt, bin, bp, binstat, binlist, flags,
+                                                                         cmask, rowcnt, bin, bp, binstat, binlist, rowlist, flags,
                                                                          erpB, ecolB); ::tsg::count_launch(); }
     (void)cnt;
     { k_union_wide<UnionKeys, true, false, long long><<<304, WIDE_THREADS, WIDE_SMEM, s>>>(
