@@ -48,8 +48,10 @@ def make_workload(name: str):
         return M.stencil_27(side, seed=1), "AA", f"3D 27-point stencil {side}^3, values U[0.5,1.5], diagonal = row sum, C = A*A"
     if name == "lap256":
         return M.laplacian_2d(256), "AA", "2D 5-point Laplacian 256x256 (n=65,536), diag 4, off -1, C = A*A"
-    if name == "rmat16-aat":
-        return M.rmat(16, 16, seed=1), "AAT", "R-MAT 2^16 x 16/row (0.57,0.19,0.19,0.05), values U[-1,1], C = A*A^T"
+    if name.startswith("rmat") and name.endswith("-aat") and name[4:-4].isdigit():
+        scale = int(name[4:-4])
+        return (M.rmat(scale, 16, seed=1), "AAT",
+                f"R-MAT 2^{scale} x 16/row (0.57,0.19,0.19,0.05), duplicates merged, values U[-1,1], C = A*A^T")
     raise SystemExit(f"unknown workload {name}")
 
 
@@ -437,7 +439,11 @@ def run_served(args) -> None:
     procs = max(1, min(16, (os.cpu_count() or 1)))
     reqs = make_stream(args.serve_requests, seed=1, rate=args.serve_rate,
                        rmat_scale=(12, args.serve_max_scale), procs=procs)
-    warm = make_stream(16, seed=99, rate=args.serve_rate, rmat_scale=(12, 13), lap_side=(32, 64))
+    # warm-up: another realization of the same stream (other pattern keys, so
+    # the timed run's plans are not cached), which also warms the pinned
+    # result buffers
+    warm = make_stream(max(16, args.serve_requests // 4), seed=2, rate=args.serve_rate,
+                       rmat_scale=(12, args.serve_max_scale), procs=procs, key_base=1 << 40)
     with Server(workers=args.serve_workers, budget_gb=64.0) as srv:
         run_stream(srv, warm, realtime=False, download=False)
         st = run_stream(srv, reqs, realtime=True, download=False)

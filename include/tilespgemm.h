@@ -86,8 +86,10 @@ typedef struct {
                                 16x16 accumulator (default 160; 257 = never) */
     int32_t smem_acc_max;    /* largest C tile-row (in entries) accumulated in shared memory (default 24576) */
     int32_t threads_numeric; /* threads per CTA of the numeric kernels: 128, 256 or 512 (default 256) */
-    int32_t row_acc_max;     /* larger tile-rows: largest C row (entries) accumulated in shared memory by the
-                                one-row-per-CTA kernel; longer rows accumulate in C's value array (default 65535) */
+    int32_t row_acc_max;     /* tile-rows too large for one CTA: rows of up to this many entries accumulate in
+                                shared memory (one CTA per row); longer rows -- and rows of 1,536+ entries with
+                                96+ per entry of A's row -- accumulate in C's value array, eight warps per row
+                                (default 65535) */
     int32_t numeric_walk;    /* 0 = auto; 1 = lanes over one B row per A entry; 2 = packed (lanes over the row's
                                 flattened (A entry, B entry) pairs).  Auto packs only when a B row repeats a
                                 column. */
@@ -270,8 +272,11 @@ tsg_status tsg_plan_tune(tsg_ctx *ctx, tsg_plan *plan, double *best_ms);
  * requests concurrently, taking up to max_batch at a time.  A request with a
  * nonzero pattern_key keeps its symbolic result (a plan) in its worker's
  * cache (plan_cache_bytes, least recently used first out): a later request
- * with the same key and new values runs only the numeric step.  Keyless
- * requests of one op taken together run as one batched product.
+ * with the same key and new values runs only the numeric step (a request
+ * whose op, shapes, row pointers or sampled column indices differ from the
+ * key's plan rebuilds it, so a reused key never runs another pattern's
+ * numeric step on these checks).  Keyless requests of one op taken together
+ * run as one batched product.
  * Operands are host memory and must stay valid until tsg_server_wait returns
  * the request.  Results are host CSRs (pinned); release them with
  * tsg_csr_free before destroying the server.
@@ -360,6 +365,11 @@ tsg_status tsg_tiles_to_csr_noalloc(tsg_ctx *ctx, const tsg_tiles *T, int64_t *r
                                     double *val);
 
 tsg_status tsg_tiles_free(tsg_ctx *ctx, tsg_tiles *T);
+
+/* y = T x on the tile form, without going back to CSR (the reference's
+ * tile-format consumer, the CCSB SpMV of ccsb_spmv.h:11-252).  x (T->n) and
+ * y (T->m) are device memory; waits for the result. */
+tsg_status tsg_tiles_spmv(tsg_ctx *ctx, const tsg_tiles *T, const double *x, double *y);
 
 /* Copy a tile matrix's arrays to caller-provided host buffers (sizes from T). */
 tsg_status tsg_tiles_download(tsg_ctx *ctx, const tsg_tiles *T, int64_t *blkrowptr, int32_t *blkcolidx,

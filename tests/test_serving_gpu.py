@@ -62,6 +62,20 @@ def test_repeats_run_numeric_only(built_lib):
     assert np.array_equal(C2.col, col) and np.array_equal(C2.val, val)
 
 
+def test_key_reused_for_another_pattern(built_lib):
+    """A key whose pattern changes rebuilds its plan (fingerprint check)."""
+    from tilespgemm_gb300 import matrices as M
+    from tilespgemm_gb300.serving import Server
+    A1 = M.rmat(9, 8, seed=4)
+    A2 = M.rmat(9, 8, seed=5)
+    with Server(workers=1) as srv:
+        srv.wait(srv.submit(A1, op="AA", key=5))
+        C2, info = srv.wait(srv.submit(A2, op="AA", key=5))
+    assert info["numeric_only"] == 0
+    rp, col, val = O.spgemm(A2, A2)
+    assert np.array_equal(C2.col, col) and np.array_equal(C2.val, val)
+
+
 def test_budget_refuses_oversized(built_lib):
     from tilespgemm_gb300 import TSGError
     from tilespgemm_gb300 import matrices as M

@@ -137,6 +137,7 @@ SIGNATURES = {
                                    C.POINTER(tsg_tiles), C.POINTER(tsg_stats)]),
     "tsg_tiles_to_csr": (C.c_int, [C.c_void_p, C.POINTER(tsg_tiles), C.POINTER(tsg_csr)]),
     "tsg_tiles_free": (C.c_int, [C.c_void_p, C.POINTER(tsg_tiles)]),
+    "tsg_tiles_spmv": (C.c_int, [C.c_void_p, C.POINTER(tsg_tiles), C.c_void_p, C.c_void_p]),
     "tsg_tiles_to_csr_noalloc": (C.c_int, [C.c_void_p, C.POINTER(tsg_tiles), C.c_void_p, C.c_void_p, C.c_void_p]),
     "tsg_tiles_download": (C.c_int, [C.c_void_p, C.POINTER(tsg_tiles), C.c_void_p, C.c_void_p, C.c_void_p,
                                      C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),

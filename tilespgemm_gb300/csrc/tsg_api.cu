@@ -12,6 +12,7 @@
 #include "tsg_internal.cuh"
 #include "tsg_numeric.cuh"
 
+#include <algorithm>
 #include <atomic>
 #include <chrono>
 #include <cstdarg>
@@ -37,7 +38,8 @@ cudaError_t aux_gather(Pool &pool, const int *perm, const double *src, double *d
 cudaError_t aux_nnzcub(Pool &pool, const long long *rpA, const int *colA, int m, const long long *rpB, int kB,
                        unsigned long long *out);
 cudaError_t aux_mask_popc(Pool &pool, const int *trp, int blkm, const uint16_t *mask, unsigned long long *out);
-cudaError_t aux_rows_increasing(Pool &pool, const long long *rp, const int *col, int m, unsigned long long *out);
+cudaError_t aux_rows_increasing(Pool &pool, const long long *rp, const int *col, int m, long long nnz,
+                                unsigned long long *out);
 cudaError_t aux_copy_scalars(Pool &pool, const long long *a, long long *da, const int *b, long long *db,
                              const int *c, long long *dc);
 cudaError_t aux_rowptr_narrow(Pool &pool, const long long *in, int *out, long long n);
@@ -57,6 +59,8 @@ cudaError_t csr_fill_from_tiles(cudaStream_t s, int m, const long long *brp, con
                                 const uint8_t *ptr, const uint8_t *lcol, const double *tval, const long long *rowptr,
                                 int *col, double *val);
 long long scan_status_words(long long n);
+cudaError_t tiles_spmv(cudaStream_t s, int m, int blkm, const long long *brp, const int *bcol, const long long *nnzb,
+                       const uint8_t *ptr, const uint8_t *lcol, const double *tval, const double *x, int n, double *y);
 cudaError_t scan_i32_to_i64_in(cudaStream_t s, const int *in, long long *out, long long n, int *flags,
                                unsigned *ticket, unsigned long long *status);
 }  // namespace tsg
@@ -440,7 +444,7 @@ tsg_status plan_symbolic(tsg_ctx *ctx, Pool &pool, Scratch &sc, tsg_op op, const
     CUDA_OK(aux_copy_scalars(pool, P.crp + P.blkm, ctx->dstat + ST_NUMBLKC, TA.trp + TA.blkm, ctx->dstat + ST_TILESA,
                              TB.trp + TB.blkm, ctx->dstat + ST_TILESB));
     CUDA_OK(aux_mask_popc(pool, TB.trp, TB.blkm, TB.mask, (unsigned long long *)(ctx->dstat + ST_POPCB)));
-    CUDA_OK(aux_rows_increasing(pool, P.rpB, P.colB, P.k, (unsigned long long *)(ctx->dstat + ST_BUNSORTED)));
+    CUDA_OK(aux_rows_increasing(pool, P.rpB, P.colB, P.k, P.nnzB, (unsigned long long *)(ctx->dstat + ST_BUNSORTED)));
     if (want_cub)
         CUDA_OK(aux_nnzcub(pool, P.rpA, P.colA, P.m, P.rpB, P.k, (unsigned long long *)(ctx->dstat + ST_NNZCUB)));
     r = host_wait(ctx, &P.nsync);
@@ -467,7 +471,7 @@ tsg_status plan_symbolic(tsg_ctx *ctx, Pool &pool, Scratch &sc, tsg_op op, const
     P.rowptrC = P.own<long long>(pool, P.m + 1);
     if (!P.ccol || !P.cmask || !rowcnt || !P.bin || !P.binlist || !P.rowlist || !P.rowptrC)
         return fail(TSG_ERR_OOM, "device pool allocation failed for C tiles");
-    NumericBinParams bp{ctx->opts.dense_tile_min, ctx->opts.smem_acc_max, ctx->opts.row_acc_max};
+    NumericBinParams bp{ctx->opts.dense_tile_min, ctx->opts.smem_acc_max, ctx->opts.row_acc_max, P.rpA};
     CUDA_OK(symbolic_fill_fused(pool, TA, TB, P.m, P.crp, P.ccol, P.cmask, rowcnt, P.bin, bp, ctx->dstat + ST_BINS,
                                 P.binlist, P.rowlist, cnt, wide, ctx->dflags, P.rpB, P.colB));
     tm.mark();  // 2
@@ -1207,7 +1211,10 @@ tsg_status pack_operands(tsg_ctx *ctx, Pool &pool, Scratch &sc, int count, const
         PackDesc *dd = sc.get<PackDesc>(count);
         if (!dd) return fail(TSG_ERR_OOM, "device pool allocation failed");
         CUDA_OK(cudaMemcpyAsync(dd, d.data(), sizeof(PackDesc) * (size_t)count, cudaMemcpyHostToDevice, ctx->stream));
-        CUDA_OK(batch_pack(pool, dd, count, rp, col, val, ctx->dflags));
+        long long most = 0;
+        for (int i = 0; i < count; ++i) most = std::max<long long>(most, std::max<long long>(M[i].nnz, d[i].rowpad));
+        const int per = (int)std::min<long long>(64, std::max<long long>(1, (most + 8191) / 8192));
+        CUDA_OK(batch_pack(pool, dd, count, per, rp, col, val, ctx->dflags));
         CUDA_OK(cudaMemcpyAsync(rp + rows_total, &nnz, sizeof(long long), cudaMemcpyHostToDevice, ctx->stream));
         CUDA_OK(cudaStreamSynchronize(ctx->stream));   // the descriptor and the end value are host stack memory
     }
@@ -1773,3 +1780,14 @@ tsg_status tsg_plan_tune(tsg_ctx *ctx, tsg_plan *plan, double *best_ms)
 }
 
 }  // extern "C"
+
+extern "C" tsg_status tsg_tiles_spmv(tsg_ctx *ctx, const tsg_tiles *T, const double *x, double *y)
+{
+    if (!ctx || !T || !x || !y) return fail(TSG_ERR_INVALID_ARG, "ctx/T/x/y is NULL");
+    if (T->m < 0 || T->n < 0 || T->blkm != (T->m + TILE - 1) / TILE) return fail(TSG_ERR_INVALID_ARG, "T is not a tile form");
+    CUDA_OK(cudaSetDevice(ctx->device));
+    CUDA_OK(tiles_spmv(ctx->stream, T->m, T->blkm, (const long long *)T->blkrowptr, T->blkcolidx,
+                       (const long long *)T->nnzb, T->ptr, T->col, T->val, x, T->n, y));
+    CUDA_OK(cudaStreamSynchronize(ctx->stream));
+    return TSG_OK;
+}

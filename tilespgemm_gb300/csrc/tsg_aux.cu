@@ -54,21 +54,28 @@ __global__ void k_mask_popc(const int *__restrict__ trp, int blkm, const uint16_
     if ((threadIdx.x & 31) == 0 && acc) atomicAdd(out, acc);
 }
 
-// rows whose columns are not strictly increasing (unsorted or repeated);
-// one warp per row, lanes compare neighbours
-__global__ void k_rows_increasing(const long long *__restrict__ rp, const int *__restrict__ col, int m,
-                                  unsigned long long *out)
+// Is every row's column sequence strictly increasing?  Pass 1 marks the
+// first entry of every non-empty row in a bitmap over the entries; pass 2
+// compares each entry with the next unless the next starts a row, and
+// counts the descents (coalesced over the entries).
+__global__ void k_mark_row_starts(const long long *__restrict__ rp, int m, unsigned *starts)
 {
-    const int lane = threadIdx.x & 31;
-    unsigned long long cnt = 0;
-    for (long long R = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5; R < m;
-         R += ((long long)gridDim.x * blockDim.x) >> 5) {
-        const long long p0 = rp[R], p1 = rp[R + 1];
-        bool bad = false;
-        for (long long q = p0 + lane; q + 1 < p1; q += 32) bad |= col[q] >= col[q + 1];
-        if (__any_sync(0xffffffffu, bad)) ++cnt;
+    for (long long R = blockIdx.x * (long long)blockDim.x + threadIdx.x; R < m; R += (long long)gridDim.x * blockDim.x) {
+        const long long p = rp[R];
+        if (rp[R + 1] > p) atomicOr(&starts[p >> 5], 1u << (p & 31));
     }
-    if (lane == 0 && cnt) atomicAdd(out, cnt);
+}
+
+__global__ void k_count_descents(const int *__restrict__ col, long long nnz, const unsigned *__restrict__ starts,
+                                 unsigned long long *out)
+{
+    unsigned long long cnt = 0;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q + 1 < nnz; q += (long long)gridDim.x * blockDim.x) {
+        const long long n1 = q + 1;
+        if (!((starts[n1 >> 5] >> (n1 & 31)) & 1u) && col[q] >= col[n1]) ++cnt;
+    }
+    cnt = (unsigned long long)warp_sum_ll((long long)cnt);
+    if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(out, cnt);
 }
 
 __global__ void k_copy_scalars(const long long *a, long long *da, const int *b, long long *db, const int *c, long long *dc)
@@ -213,6 +220,36 @@ __device__ __forceinline__ int tile_row_len(const uint8_t *ptr, const long long 
     return e > s ? e - s : 0;
 }
 
+// y = T x on the tile form (the consumer the reference's CCSB SpMV is,
+// ccsb_spmv.h:11-252): one warp per tile-row, a lane pair per row, each lane
+// of the pair taking every other entry of the row's segment in each tile;
+// the tile's 16 entries of x are staged in shared memory.
+__global__ void __launch_bounds__(256)
+k_tiles_spmv(int m, int blkm, const long long *__restrict__ brp, const int *__restrict__ bcol,
+             const long long *__restrict__ nnzb, const uint8_t *__restrict__ ptr, const uint8_t *__restrict__ lcol,
+             const double *__restrict__ tval, const double *__restrict__ x, int n, double *y)
+{
+    __shared__ double s_x[8][TILE];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int i = blockIdx.x * 8 + warp;
+    if (i >= blkm) return;
+    const int r = lane >> 1, half = lane & 1;
+    double sum = 0.0;
+    for (long long t = brp[i]; t < brp[i + 1]; ++t) {
+        const int jb = bcol[t] * TILE;
+        if (lane < TILE) s_x[warp][lane] = (jb + lane < n) ? x[jb + lane] : 0.0;
+        __syncwarp();
+        const long long base = nnzb[t];
+        const int s = ptr[t * TILE + r];
+        const int e = (r == TILE - 1) ? (int)(nnzb[t + 1] - base) : ptr[t * TILE + r + 1];
+        for (int q = s + half; q < e; q += 2) sum = fma(tval[base + q], s_x[warp][lcol[base + q] & 15], sum);
+        __syncwarp();
+    }
+    sum += __shfl_xor_sync(0xffffffffu, sum, 1);
+    const int R = i * TILE + r;
+    if (half == 0 && R < m) y[R] = sum;
+}
+
 __global__ void k_csr_rowcnt_from_tiles(int m, const long long *__restrict__ brp, const long long *__restrict__ nnzb,
                                         const uint8_t *__restrict__ ptr, int *rowcnt)
 {
@@ -271,14 +308,16 @@ __global__ void k_gather(const int *__restrict__ perm, const double *__restrict_
 
 // ---- batched products: block-diagonal packing -----------------------------
 
-// one CTA per instance: shifted row pointer (padding rows repeat the end),
-// shifted columns, copied values; row pointers and columns are validated
+// gridDim.y CTAs per instance (blockIdx.x): shifted row pointer (padding
+// rows repeat the end), shifted columns, copied values; row pointers and
+// columns are validated
 __global__ void __launch_bounds__(256)
 k_batch_pack(const PackDesc *__restrict__ descs, long long *rp, int *col, double *val, int *flags)
 {
     const PackDesc d = descs[blockIdx.x];
+    const long long t0 = (long long)blockIdx.y * blockDim.x + threadIdx.x, ts = (long long)gridDim.y * blockDim.x;
     bool bad = false;
-    for (long long r = threadIdx.x; r < d.rowpad; r += blockDim.x) {
+    for (long long r = t0; r < d.rowpad; r += ts) {
         long long v;
         if (r < d.m) {
             v = d.rp_bits == 64 ? ((const long long *)d.rp)[r] : (long long)((const int *)d.rp)[r];
@@ -290,11 +329,11 @@ k_batch_pack(const PackDesc *__restrict__ descs, long long *rp, int *col, double
         }
         rp[d.rowoff + r] = d.nnzoff + v;
     }
-    if (threadIdx.x == 0 && d.m > 0) {
+    if (t0 == 0 && d.m > 0) {
         const long long last = d.rp_bits == 64 ? ((const long long *)d.rp)[d.m] : (long long)((const int *)d.rp)[d.m];
         if (last != d.nnz) bad = true;
     }
-    for (long long q = threadIdx.x; q < d.nnz; q += blockDim.x) {
+    for (long long q = t0; q < d.nnz; q += ts) {
         int c = d.col[q];
         if ((unsigned)c >= (unsigned)d.n) { bad = true; c = 0; }
         col[d.nnzoff + q] = (int)(c + d.coloff);
@@ -359,13 +398,19 @@ cudaError_t aux_nnzcub(Pool &pool, const long long *rpA, const int *colA, int m,
     return cudaGetLastError();
 }
 
-cudaError_t aux_rows_increasing(Pool &pool, const long long *rp, const int *col, int m, unsigned long long *out)
+cudaError_t aux_rows_increasing(Pool &pool, const long long *rp, const int *col, int m, long long nnz,
+                                unsigned long long *out)
 {
-    if (m <= 0) return cudaSuccess;
-    long long g = ((long long)m * 32 + 255) / 256;
-    if (g > 152ll * 16) g = 152ll * 16;
-    { k_rows_increasing<<<(unsigned)g, 256, 0, pool.stream>>>(rp, col, m, out); ::tsg::count_launch(); }
-    return cudaGetLastError();
+    if (m <= 0 || nnz <= 1) return cudaSuccess;
+    const long long words = (nnz + 31) / 32 + 1;
+    unsigned *starts = pool.alloc_n<unsigned>(words);
+    if (!starts) return pool.err;
+    cudaError_t e = cudaMemsetAsync(starts, 0, sizeof(unsigned) * (size_t)words, pool.stream);
+    if (e == cudaSuccess) { k_mark_row_starts<<<g256(m), 256, 0, pool.stream>>>(rp, m, starts); ::tsg::count_launch(); }
+    if (e == cudaSuccess) { k_count_descents<<<g256(nnz), 256, 0, pool.stream>>>(col, nnz, starts, out); ::tsg::count_launch(); }
+    if (e == cudaSuccess) e = cudaGetLastError();
+    pool.free(starts);
+    return e;
 }
 
 cudaError_t aux_mask_popc(Pool &pool, const int *trp, int blkm, const uint16_t *mask, unsigned long long *out)
@@ -388,10 +433,12 @@ cudaError_t aux_gather(Pool &pool, const int *perm, const double *src, double *d
     return cudaGetLastError();
 }
 
-cudaError_t batch_pack(Pool &pool, const PackDesc *d_desc, int count, long long *rp, int *col, double *val, int *flags)
+cudaError_t batch_pack(Pool &pool, const PackDesc *d_desc, int count, int per, long long *rp, int *col, double *val,
+                       int *flags)
 {
     if (count <= 0) return cudaSuccess;
-    { k_batch_pack<<<count, 256, 0, pool.stream>>>(d_desc, rp, col, val, flags); ::tsg::count_launch(); }
+    const dim3 grid((unsigned)count, (unsigned)(per < 1 ? 1 : per));
+    { k_batch_pack<<<grid, 256, 0, pool.stream>>>(d_desc, rp, col, val, flags); ::tsg::count_launch(); }
     return cudaGetLastError();
 }
 
@@ -461,6 +508,13 @@ cudaError_t csr_fill_from_tiles(cudaStream_t s, int m, const long long *brp, con
                                 int *col, double *val)
 {
     if (m > 0) { k_csr_fill_from_tiles<<<(unsigned)((m + 7) / 8), 256, 0, s>>>(m, brp, bcol, nnzb, ptr, lcol, tval, rowptr, col, val); ::tsg::count_launch(); }
+    return cudaGetLastError();
+}
+
+cudaError_t tiles_spmv(cudaStream_t s, int m, int blkm, const long long *brp, const int *bcol, const long long *nnzb,
+                       const uint8_t *ptr, const uint8_t *lcol, const double *tval, const double *x, int n, double *y)
+{
+    if (blkm > 0) { k_tiles_spmv<<<(unsigned)((blkm + 7) / 8), 256, 0, s>>>(m, blkm, brp, bcol, nnzb, ptr, lcol, tval, x, n, y); ::tsg::count_launch(); }
     return cudaGetLastError();
 }
 

@@ -173,7 +173,9 @@ struct UnpackDesc {
     long long rpoff;         // first entry of C_i's row pointer in the output array
 };
 
-cudaError_t batch_pack(Pool &pool, const PackDesc *d_desc, int count, long long *rp, int *col, double *val, int *flags);
+// per = CTAs per instance (grid y)
+cudaError_t batch_pack(Pool &pool, const PackDesc *d_desc, int count, int per, long long *rp, int *col, double *val,
+                       int *flags);
 cudaError_t batch_unpack(Pool &pool, const UnpackDesc *d_desc, int count, const long long *rowptrC, void *rp_out,
                          int rp_bits, long long *ebase);
 

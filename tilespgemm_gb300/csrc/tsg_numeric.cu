@@ -196,8 +196,11 @@ __device__ __forceinline__ void row_walk_packed(const NumericArgs &g, int R, int
 
 // One warp applies row R's products whose column lies in [lo, hi), in A's
 // row order then B's (lanes over one B row; B rows without repeated
-// columns).  With sorted B rows the B row is entered by a warp search and
-// left at the first column >= hi; otherwise every entry is tested.
+// columns).  A's entries are taken 32 at a time, one per lane: with sorted
+// B rows each lane first cuts its B row to [lo, hi) by two binary searches
+// (all lanes at once), then the warp walks the (A entry, 32-entry chunk)
+// pairs in order with the next pair's loads issued before the current
+// pair's updates.  Without sorted B rows every entry is tested instead.
 template <class Acc, class PosFn>
 __device__ __forceinline__ void row_walk_range(const NumericArgs &g, int R, int lane, int lo, int hi, Acc *acc,
                                                PosFn pos_of)
@@ -213,23 +216,44 @@ __device__ __forceinline__ void row_walk_range(const NumericArgs &g, int R, int 
             av = g.valA[pb + lane];
             bs = (int)g.rpB[k];
             be = (int)g.rpB[k + 1];
+            if (g.b_sorted) {
+                int l = bs, h = be;
+                while (l < h) { const int md = (l + h) >> 1; if (g.colB[md] < lo) l = md + 1; else h = md; }
+                bs = l; h = be;
+                while (l < h) { const int md = (l + h) >> 1; if (g.colB[md] < hi) l = md + 1; else h = md; }
+                be = l;
+            }
         }
-        for (int q = 0; q < na; ++q) {
-            const double a = __shfl_sync(0xffffffffu, av, q);
-            const int b1 = __shfl_sync(0xffffffffu, be, q);
-            int b0 = __shfl_sync(0xffffffffu, bs, q);
-            if (g.b_sorted) b0 = warp_lower_bound(g.colB, b0, b1, lo, lane);
-            for (int eb = b0; eb < b1; eb += 32) {
-                const int e = eb + lane;
-                const int col = e < b1 ? g.colB[e] : INT_MAX;
-                if (col >= lo && col < hi) {
-                    const long long pos = pos_of(col);
-                    if (pos < 0) bad = true;
-                    else acc[pos] = fma(a, g.valB[e], acc[pos]);
-                }
-                if (g.b_sorted && __ballot_sync(0xffffffffu, col >= hi)) break;
+        // first non-empty pair
+        int q = 0, eb = __shfl_sync(0xffffffffu, bs, 0), ee = __shfl_sync(0xffffffffu, be, 0);
+        double a = __shfl_sync(0xffffffffu, av, 0);
+        while (eb >= ee && ++q < na) {
+            eb = __shfl_sync(0xffffffffu, bs, q);
+            ee = __shfl_sync(0xffffffffu, be, q);
+            a = __shfl_sync(0xffffffffu, av, q);
+        }
+        int col = INT_MAX;
+        double b = 0.0;
+        if (q < na && eb + lane < ee) { col = g.colB[eb + lane]; b = g.valB[eb + lane]; }
+        while (q < na) {
+            int nq = q, neb = eb + 32, nee = ee;
+            double na_ = a;
+            while (neb >= nee && ++nq < na) {
+                neb = __shfl_sync(0xffffffffu, bs, nq);
+                nee = __shfl_sync(0xffffffffu, be, nq);
+                na_ = __shfl_sync(0xffffffffu, av, nq);
+            }
+            int ncol = INT_MAX;
+            double nb = 0.0;
+            if (nq < na && neb + lane < nee) { ncol = g.colB[neb + lane]; nb = g.valB[neb + lane]; }
+            if (col >= lo && col < hi) {
+                const long long pos = pos_of(col);
+                if (pos < 0) bad = true;
+                else acc[pos] = fma(a, b, acc[pos]);
             }
             __syncwarp();
+            q = nq; eb = neb; ee = nee; a = na_;
+            col = ncol; b = nb;
         }
     }
     if (bad) set_flag(g.flags, FLAG_INTERNAL);

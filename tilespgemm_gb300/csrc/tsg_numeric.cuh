@@ -50,6 +50,7 @@ struct NumericBinParams {
     int dense_tile_min;   // mean C-tile nnz at which a tile-row uses dense accumulators
     int smem_acc_max;     // largest tile-row (entries) accumulated in shared memory
     int row_acc_max;      // largest row (entries) accumulated in shared memory by the row kernel
+    const long long *rpA; // A's row pointer (row classes weigh C's row against A's row)
 };
 
 __host__ __device__ inline long long align16(long long x) { return (x + 15) & ~15ll; }
@@ -94,11 +95,21 @@ __host__ __device__ inline void numeric_classify(const NumericBinParams &bp, lon
     }
 }
 
-// Class of one row of a BIN_ROWS tile-row; req = its shared-memory bytes.
+// Rows this long, with this many entries per entry of A's row (so B's rows
+// are long), go to the wide kernel: eight warps then share the row's
+// products, each over its column range, while one warp would walk long B
+// rows alone (measured faster on R-MAT A*A^T; rows of short B rows stay in
+// shared memory).
+constexpr long long WIDE_MIN_ROW = 1536;
+constexpr long long WIDE_MIN_RATIO = 96;
+
+// Class of one row of a BIN_ROWS tile-row (a_len: entries of A's row);
+// req = its shared-memory bytes.
 __host__ __device__ inline int numeric_row_class(const NumericBinParams &bp, long long S, long long row_nnz,
-                                                 long long span, long long &req) {
+                                                 long long span, long long a_len, long long &req) {
     req = numeric_row_smem_bytes(S, row_nnz, span);
-    if (row_nnz <= bp.row_acc_max && row_nnz < 65536) {
+    const bool long_b = row_nnz >= WIDE_MIN_ROW && row_nnz >= WIDE_MIN_RATIO * a_len;
+    if (row_nnz <= bp.row_acc_max && row_nnz < 65536 && !long_b) {
         if (req <= ROWS_SMALL) return ROW_S;
         if (req <= ROWS_MEDIUM) return ROW_M;
         if (req <= SMEM_LARGE) return ROW_L;
@@ -127,7 +138,7 @@ __device__ __forceinline__ void record_row(const NumericBinParams &bp, long long
                                            int R, int m, long long *binstat, int *rowlist) {
     if (row_nnz == 0) return;
     long long req;
-    const int c = numeric_row_class(bp, S, row_nnz, span, req);
+    const int c = numeric_row_class(bp, S, row_nnz, span, bp.rpA[R + 1] - bp.rpA[R], req);
     const unsigned long long pos = atomicAdd((unsigned long long *)&binstat[BS_ROWCNT + c], 1ull);
     rowlist[(long long)c * m + (long long)pos] = R;
     if (req) atomicMax((long long *)&binstat[BS_ROWREQ + c], req);

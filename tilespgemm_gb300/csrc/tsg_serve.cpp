@@ -60,6 +60,7 @@ struct Request {
 struct PlanEntry {
     tsg_plan *plan = nullptr;
     int64_t bytes = 0;
+    uint64_t fp = 0;                     // fingerprint of the pattern the plan was built for
     std::list<uint64_t>::iterator lru;
 };
 
@@ -75,6 +76,26 @@ struct Worker {
 int64_t rowptr_at(const tsg_csr &M, int64_t i)
 {
     return M.rowptr_bits == 64 ? ((const int64_t *)M.row_ptr)[i] : ((const int32_t *)M.row_ptr)[i];
+}
+
+// Fingerprint of a request's pattern: op, shapes, entry counts, the whole
+// row pointer and 64 evenly spaced column indices of each operand (FNV-1a).
+// A keyed request whose fingerprint differs from its key's plan rebuilds
+// the plan instead of running another pattern's numeric step.
+uint64_t fingerprint(tsg_op op, const tsg_csr &A, const tsg_csr *B)
+{
+    uint64_t h = 1469598103934665603ull;
+    auto mix = [&](uint64_t v) { for (int b = 0; b < 8; ++b) { h ^= (v >> (8 * b)) & 0xff; h *= 1099511628211ull; } };
+    auto one = [&](const tsg_csr &M) {
+        mix((uint64_t)M.m); mix((uint64_t)M.n); mix((uint64_t)M.nnz);
+        for (int64_t i = 0; i <= M.m; ++i) mix((uint64_t)rowptr_at(M, i));
+        if (M.nnz > 0)
+            for (int t = 0; t < 64; ++t) mix((uint64_t)(uint32_t)M.col[(M.nnz - 1) * t / 63]);
+    };
+    mix((uint64_t)op);
+    one(A);
+    if (B) one(*B);
+    return h;
 }
 
 // Device bytes a request may need: operands, C's upper bound (per row, the
@@ -166,7 +187,15 @@ void evict_plans(Worker &W, int64_t limit)
 
 void run_keyed(tsg_server *s, Worker &W, Request *r)
 {
+    const uint64_t fp = fingerprint(r->op, r->A, r->hasB ? &r->B : nullptr);
     auto it = W.plans.find(r->key);
+    if (it != W.plans.end() && it->second.fp != fp) {   // the key now names another pattern
+        W.lru.erase(it->second.lru);
+        W.plan_bytes -= it->second.bytes;
+        tsg_plan_destroy(W.ctx, it->second.plan);
+        W.plans.erase(it);
+        it = W.plans.end();
+    }
     tsg_plan *plan = nullptr;
     if (it != W.plans.end()) {
         plan = it->second.plan;
@@ -180,6 +209,7 @@ void run_keyed(tsg_server *s, Worker &W, Request *r)
         PlanEntry e;
         e.plan = plan;
         e.bytes = tsg_plan_device_bytes(plan);
+        e.fp = fp;
         W.lru.push_front(r->key);
         e.lru = W.lru.begin();
         W.plans[r->key] = e;

@@ -25,8 +25,6 @@ namespace tsg {
 
 namespace {
 
-constexpr int S2_THREADS = 256;
-constexpr int S2_WARPS = S2_THREADS / 32;
 
 __device__ __forceinline__ int lower_bound_i(const int *a, int n, int key) {
     int lo = 0, hi = n;
@@ -71,11 +69,12 @@ __device__ __forceinline__ int c_slot(int j, int jbase, int span, const unsigned
 // uniformly across the warp, every lane ORs its B tile's row c into the
 // rows of that set -- one shared atomicOr per A entry and B tile, no search,
 // no per-element branching on the B side.
-__global__ void __launch_bounds__(S2_THREADS)
+template <int NT>
+__global__ void __launch_bounds__(NT)
 k_step2(int blkm, int m, const int *__restrict__ arp, const int *__restrict__ acol,
         const uint16_t *__restrict__ amask, const int *__restrict__ brp, const int *__restrict__ bcol,
         const uint16_t *__restrict__ bmask, const long long *__restrict__ crp, const int *__restrict__ ccol,
-        uint16_t *cmask, int *rowcnt, int smax, int map_cap, NumericBinParams bp, unsigned char *bin,
+        uint16_t *cmask, int *rowcnt, int smin, int smax, int map_cap, NumericBinParams bp, unsigned char *bin,
         long long *binstat, int *binlist, int *rowlist, int *flags, const int *__restrict__ rows_list,
         const long long *__restrict__ erpB, const int *__restrict__ ecolB)
 {
@@ -85,7 +84,7 @@ k_step2(int blkm, int m, const int *__restrict__ arp, const int *__restrict__ ac
     if (i >= blkm) return;
     const long long c0 = crp[i];
     const int S = (int)(crp[i + 1] - c0);
-    if (S > smax) return;
+    if (S <= smin || S > smax) return;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int jbase = S > 0 ? ccol[c0] : 0;
     const int span = S > 0 ? ccol[c0 + S - 1] - jbase + 1 : 0;
@@ -98,12 +97,12 @@ k_step2(int blkm, int m, const int *__restrict__ arp, const int *__restrict__ ac
     const int *scol = wcol;
     {
         unsigned *z = reinterpret_cast<unsigned *>(smask);
-        for (int t = tid; t < (S * TILE + 1) / 2; t += S2_THREADS) z[t] = 0u;
-        for (int t = tid; t < S; t += S2_THREADS) wcol[t] = ccol[c0 + t];
+        for (int t = tid; t < (S * TILE + 1) / 2; t += NT) z[t] = 0u;
+        for (int t = tid; t < S; t += NT) wcol[t] = ccol[c0 + t];
         if (map) {
-            for (int t = tid; t < span; t += S2_THREADS) map[t] = 0xffffu;
+            for (int t = tid; t < span; t += NT) map[t] = 0xffffu;
             __syncthreads();
-            for (int t = tid; t < S; t += S2_THREADS) map[ccol[c0 + t] - jbase] = (unsigned short)t;
+            for (int t = tid; t < S; t += NT) map[ccol[c0 + t] - jbase] = (unsigned short)t;
         }
     }
     if (tid < TILE) s_rowtot[tid] = 0;
@@ -111,7 +110,7 @@ k_step2(int blkm, int m, const int *__restrict__ arp, const int *__restrict__ ac
 
     const int a0 = arp[i], a1 = arp[i + 1], na = a1 - a0;
     bool bad = false;
-    for (int a = a0 + warp; a < a1; a += S2_WARPS) {
+    for (int a = a0 + warp; a < a1; a += (NT / 32)) {
         const int kt = acol[a];
         const int q0 = brp[kt], nq = brp[kt + 1] - q0;
         // transpose the A tile: colrows[c] = rows r whose mask has local column c
@@ -175,8 +174,8 @@ k_step2(int blkm, int m, const int *__restrict__ arp, const int *__restrict__ ac
 
     const int rows = min(TILE, m - i * TILE);
     // both smask and cmask are row-major ([r][s]) within the tile-row
-    for (int t = tid; t < S * TILE; t += S2_THREADS) cmask[c0 * TILE + t] = smask[t];
-    for (int r = warp; r < TILE; r += S2_WARPS) {
+    for (int t = tid; t < S * TILE; t += NT) cmask[c0 * TILE + t] = smask[t];
+    for (int r = warp; r < TILE; r += (NT / 32)) {
         int c = 0;
         for (int s = lane; s < S; s += 32) {
             c += __popc((unsigned)smask[r * S + s]);
@@ -209,7 +208,8 @@ k_step2(int blkm, int m, const int *__restrict__ arp, const int *__restrict__ ac
 // walks the tile-row's A tiles again, with each B tile-row (tile path) or
 // B row (element path) restricted to the window's tile columns by a warp
 // search.
-__global__ void __launch_bounds__(S2_THREADS)
+template <int NT>
+__global__ void __launch_bounds__(NT)
 k_step2_win(int blkm, int m, const int *__restrict__ arp, const int *__restrict__ acol,
             const uint16_t *__restrict__ amask, const int *__restrict__ brp, const int *__restrict__ bcol,
             const uint16_t *__restrict__ bmask, const long long *__restrict__ crp, const int *__restrict__ ccol,
@@ -237,20 +237,20 @@ k_step2_win(int blkm, int m, const int *__restrict__ arp, const int *__restrict_
         const int SW = min(smax, S - s0);
         {
             unsigned *z = reinterpret_cast<unsigned *>(smask);
-            for (int t = tid; t < (SW * TILE + 1) / 2; t += S2_THREADS) z[t] = 0u;
+            for (int t = tid; t < (SW * TILE + 1) / 2; t += NT) z[t] = 0u;
         }
-        for (int t = tid; t < SW; t += S2_THREADS) wcol[t] = ccol[c0 + s0 + t];
+        for (int t = tid; t < SW; t += NT) wcol[t] = ccol[c0 + s0 + t];
         __syncthreads();
         const int jlo = wcol[0], jhi = wcol[SW - 1];
         const bool use_map = jhi - jlo + 1 <= (int)MAP_MAX;
         if (use_map) {
-            for (int t = tid; t < jhi - jlo + 1; t += S2_THREADS) map[t] = 0xffffu;
+            for (int t = tid; t < jhi - jlo + 1; t += NT) map[t] = 0xffffu;
             __syncthreads();
-            for (int t = tid; t < SW; t += S2_THREADS) map[wcol[t] - jlo] = (unsigned short)t;
+            for (int t = tid; t < SW; t += NT) map[wcol[t] - jlo] = (unsigned short)t;
         }
         __syncthreads();
         const int wspan = jhi - jlo + 1;
-        for (int a = a0 + warp; a < a1; a += S2_WARPS) {
+        for (int a = a0 + warp; a < a1; a += (NT / 32)) {
             const int kt = acol[a];
             const int q0 = brp[kt], nq = brp[kt + 1] - q0;
             const unsigned ma = (lane < TILE) ? (unsigned)amask[(long long)a0 * TILE + (long long)lane * na + (a - a0)] : 0u;
@@ -312,11 +312,11 @@ k_step2_win(int blkm, int m, const int *__restrict__ arp, const int *__restrict_
             }
         }
         __syncthreads();
-        for (int t = tid; t < SW * TILE; t += S2_THREADS) {
+        for (int t = tid; t < SW * TILE; t += NT) {
             const int r = t / SW, sl = t - r * SW;
             cmask[c0 * TILE + (long long)r * S + s0 + sl] = smask[t];
         }
-        for (int r = warp; r < TILE; r += S2_WARPS) {
+        for (int r = warp; r < TILE; r += (NT / 32)) {
             int c = 0;
             for (int sl = lane; sl < SW; sl += 32) c += __popc((unsigned)smask[r * SW + sl]);
             c = warp_sum_int(c);
@@ -348,20 +348,34 @@ k_step2_win(int blkm, int m, const int *__restrict__ arp, const int *__restrict_
 
 constexpr int S2_SMAX = 4096;   // tiles per tile-row (or window) handled with shared-memory masks
 
+constexpr int S2_SMALL = 1024;  // tile-rows of up to this many tiles: 256-thread CTAs with less shared memory
+
+namespace {
+size_t step2_smem(int slots, int map_cap) {
+    return (size_t)(align16((long long)slots * TILE * 2) + align16((long long)slots * 4) + align16((long long)map_cap * 2));
+}
+template <class K>
+cudaError_t step2_attr(K kern) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)step2_smem(S2_SMAX, MAP_MAX));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
+    return e;
+}
+}  // namespace
+
 cudaError_t symbolic_init_attributes()
 {
-    const int smem = (int)(align16(S2_SMAX * TILE * 2) + align16(S2_SMAX * 4) + align16(MAP_MAX * 2));
-    cudaError_t e = cudaFuncSetAttribute(k_step2, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_step2, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                 (int)cudaSharedmemCarveoutMaxShared);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_step2_win, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_step2_win, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                 (int)cudaSharedmemCarveoutMaxShared);
+    cudaError_t e = step2_attr(k_step2<256>);
+    if (e == cudaSuccess) e = step2_attr(k_step2<512>);
+    if (e == cudaSuccess) e = step2_attr(k_step2_win<512>);
     return e;
 }
 
+// The deferred tile-rows (too many tiles or too wide a window for the fused
+// warp kernel): up to S2_SMALL tiles in 256-thread CTAs, up to S2_SMAX in
+// 512-thread CTAs (one per SM at that shared memory, so more warps per
+// CTA), beyond that in windows.  Each launch walks the whole defer list and
+// skips the tile-rows of the other classes.
 cudaError_t step2_masks(Pool &pool, const TileCSR &A, const TileCSR &B, int m, int blkm, const long long *crp,
                         const int *ccol, uint16_t *cmask, int *rowcnt, int max_tiles_per_row, int max_span,
                         const NumericBinParams &bp, unsigned char *bin, long long *binstat, int *binlist,
@@ -370,15 +384,21 @@ cudaError_t step2_masks(Pool &pool, const TileCSR &A, const TileCSR &B, int m, i
 {
     cudaStream_t s = pool.stream;
     if (blkm <= 0 || ndefer <= 0) return cudaSuccess;
-    const int s_used = max_tiles_per_row < S2_SMAX ? max_tiles_per_row : S2_SMAX;
     const int map_cap = max_span < (int)MAP_MAX ? max_span : (int)MAP_MAX;
-    const size_t smem = (size_t)(align16((long long)s_used * TILE * 2) + align16((long long)s_used * 4) + align16((long long)map_cap * 2));
-    { k_step2<<<ndefer, S2_THREADS, smem, s>>>(blkm, m, A.trp, A.tcol, A.mask, B.trp, B.tcol, B.mask, crp, ccol,
-                                                   cmask, rowcnt, S2_SMAX, map_cap, bp, bin, binstat, binlist, rowlist, flags, defer_list,
+    {
+        const int slots = max_tiles_per_row < S2_SMALL ? max_tiles_per_row : S2_SMALL;
+        { k_step2<256><<<ndefer, 256, step2_smem(slots, map_cap), s>>>(blkm, m, A.trp, A.tcol, A.mask, B.trp, B.tcol, B.mask, crp, ccol,
+                                                   cmask, rowcnt, 0, S2_SMALL, map_cap, bp, bin, binstat, binlist, rowlist, flags, defer_list,
                                                    erpB, ecolB); ::tsg::count_launch(); }
+    }
+    if (max_tiles_per_row > S2_SMALL) {
+        const int slots = max_tiles_per_row < S2_SMAX ? max_tiles_per_row : S2_SMAX;
+        { k_step2<512><<<ndefer, 512, step2_smem(slots, map_cap), s>>>(blkm, m, A.trp, A.tcol, A.mask, B.trp, B.tcol, B.mask, crp, ccol,
+                                                   cmask, rowcnt, S2_SMALL, S2_SMAX, map_cap, bp, bin, binstat, binlist, rowlist, flags, defer_list,
+                                                   erpB, ecolB); ::tsg::count_launch(); }
+    }
     if (max_tiles_per_row > S2_SMAX) {
-        const size_t wsmem = (size_t)(align16(S2_SMAX * TILE * 2) + align16(S2_SMAX * 4) + align16(MAP_MAX * 2));
-        { k_step2_win<<<ndefer, S2_THREADS, wsmem, s>>>(blkm, m, A.trp, A.tcol, A.mask, B.trp, B.tcol, B.mask, crp, ccol,
+        { k_step2_win<512><<<ndefer, 512, step2_smem(S2_SMAX, MAP_MAX), s>>>(blkm, m, A.trp, A.tcol, A.mask, B.trp, B.tcol, B.mask, crp, ccol,
                                                       cmask, rowcnt, S2_SMAX, bp, bin, binstat, binlist, rowlist, flags, defer_list,
                                                       erpB, ecolB); ::tsg::count_launch(); }
     }

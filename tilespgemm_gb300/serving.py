@@ -91,7 +91,7 @@ def _build_request(spec: dict) -> CSR:
 
 
 def make_stream(n_requests: int, seed: int = 1, rate: float = 2000.0, repeat_frac: float = 0.3,
-                lap_side=(32, 512), rmat_scale=(12, 18), rmat_edge=(8, 32), procs: int = 0):
+                lap_side=(32, 512), rmat_scale=(12, 18), rmat_edge=(8, 32), procs: int = 0, key_base: int = 0):
     """The seeded request stream: list of dicts (t, A, op, key, kind).
 
     Arrival gaps are exponential (Poisson arrivals at `rate`/s).  With
@@ -99,7 +99,9 @@ def make_stream(n_requests: int, seed: int = 1, rate: float = 2000.0, repeat_fra
     (same key) with new values; otherwise it is a fresh 2D Laplacian or R-MAT
     operand, A*A or A*A^T with equal odds.  All draws are made first, in one
     sequential pass; the operands are then built, in `procs` spawned worker
-    processes when procs > 1 (start those before the first GPU call)."""
+    processes when procs > 1 (start those before the first GPU call).
+    Pattern keys are key_base + 1, key_base + 2, ... (streams sent to one
+    server must not share keys)."""
     rng = np.random.Generator(np.random.Philox(seed))
     t = 0.0
     specs = []
@@ -113,11 +115,11 @@ def make_stream(n_requests: int, seed: int = 1, rate: float = 2000.0, repeat_fra
         op = "AA" if rng.random() < 0.5 else "AAT"
         if rng.random() < 0.5:
             side = int(rng.integers(lap_side[0], lap_side[1] + 1))
-            specs.append(dict(t=t, vseed=vseed, op=op, key=i + 1, kind=f"lap{side}", side=side))
+            specs.append(dict(t=t, vseed=vseed, op=op, key=key_base + i + 1, kind=f"lap{side}", side=side))
         else:
             scale = int(rng.integers(rmat_scale[0], rmat_scale[1] + 1))
             ef = int(rng.integers(rmat_edge[0], rmat_edge[1] + 1))
-            specs.append(dict(t=t, vseed=vseed, op=op, key=i + 1, kind=f"rmat{scale}x{ef}", scale=scale, ef=ef,
+            specs.append(dict(t=t, vseed=vseed, op=op, key=key_base + i + 1, kind=f"rmat{scale}x{ef}", scale=scale, ef=ef,
                               mseed=int(rng.integers(1, 2 ** 31))))
     if procs > 1 and len(specs) > 1:
         import multiprocessing as mp
