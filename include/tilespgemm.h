@@ -93,6 +93,8 @@ typedef struct {
     int32_t numeric_walk;    /* 0 = auto; 1 = lanes over one B row per A entry; 2 = packed (lanes over the row's
                                 flattened (A entry, B entry) pairs).  Auto packs only when a B row repeats a
                                 column. */
+    int32_t rows_global;     /* 1: rows of tile-rows too large for one CTA that would accumulate in shared memory
+                                (one warp each) accumulate in C's value array instead, one warp each (default 0) */
 } tsg_opts;
 
 /* Per-call statistics.  Sizes are always filled; times only with phase_times. */

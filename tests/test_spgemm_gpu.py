@@ -143,7 +143,7 @@ def test_numeric_bins_agree(opts, built_lib):
                 assert C.rowptr.dtype == np.int64
 
 
-@pytest.mark.parametrize("opts", [dict(), dict(row_acc_max=0)])
+@pytest.mark.parametrize("opts", [dict(), dict(row_acc_max=0), dict(rows_global=1)])
 def test_long_rows(opts, built_lib):
     """C rows of ~3,900 and ~8,400 entries: the medium and large size classes
     of the one-row-per-CTA kernel (and, with row_acc_max=0, the global

@@ -471,7 +471,8 @@ tsg_status plan_symbolic(tsg_ctx *ctx, Pool &pool, Scratch &sc, tsg_op op, const
     P.rowptrC = P.own<long long>(pool, P.m + 1);
     if (!P.ccol || !P.cmask || !rowcnt || !P.bin || !P.binlist || !P.rowlist || !P.rowptrC)
         return fail(TSG_ERR_OOM, "device pool allocation failed for C tiles");
-    NumericBinParams bp{ctx->opts.dense_tile_min, ctx->opts.smem_acc_max, ctx->opts.row_acc_max, P.rpA};
+    NumericBinParams bp{ctx->opts.dense_tile_min, ctx->opts.smem_acc_max, ctx->opts.row_acc_max, P.rpA,
+                        ctx->opts.rows_global};
     CUDA_OK(symbolic_fill_fused(pool, TA, TB, P.m, P.crp, P.ccol, P.cmask, rowcnt, P.bin, bp, ctx->dstat + ST_BINS,
                                 P.binlist, P.rowlist, cnt, wide, ctx->dflags, P.rpB, P.colB));
     tm.mark();  // 2
@@ -621,6 +622,7 @@ void tsg_opts_default(tsg_opts *o)
     o->threads_numeric = 256;
     o->row_acc_max = 65535;
     o->numeric_walk = 0;
+    o->rows_global = 0;
 }
 
 const char *tsg_last_error(void) { return g_err.c_str(); }

@@ -587,12 +587,12 @@ k_numeric_rows_split(NumericArgs g, bool packed)
 
 // per wide row (one warp each): column indices and zeroed values
 __global__ void __launch_bounds__(256)
-k_global_prep(NumericArgs g, long long nrows)
+k_global_prep(NumericArgs g, int cls, long long nrows)
 {
     const long long k = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
     if (k >= nrows) return;
     const int lane = threadIdx.x & 31;
-    const int R = g.rowlist[(long long)ROW_WIDE * g.m + k];
+    const int R = g.rowlist[(long long)cls * g.m + k];
     const int i = R >> 4, r = R & (TILE - 1);
     const int cshift = g.tr_coloff ? g.tr_coloff[i] : 0;
     const long long c0 = g.crp[i];
@@ -617,7 +617,7 @@ k_global_prep(NumericArgs g, long long nrows)
     }
 }
 
-constexpr int WIDE_W = 2048;   // tile columns per window of the wide-row kernel
+constexpr int WIDE_W = 1024;   // tile columns per window of the wide-row kernel
 constexpr size_t WIDE_SMEM = (size_t)ROW_WARPS * WIDE_W * (4 + 2);
 
 // One CTA of ROW_WARPS warps per wide row; the values accumulate in place in
@@ -629,14 +629,20 @@ constexpr size_t WIDE_SMEM = (size_t)ROW_WARPS * WIDE_W * (4 + 2);
 // memory), then applies A's row in order, each A entry's B row restricted
 // to the window.  Ranges and windows are disjoint in columns, so per output
 // the products still come in A's row order.
-__global__ void __launch_bounds__(ROW_WARPS * 32, 2)
-k_numeric_wide(NumericArgs g, bool packed)
+template <int WPR>
+__global__ void __launch_bounds__(ROW_WARPS * 32, 4)
+k_numeric_wide(NumericArgs g, int cls, long long nrows, bool packed)
 {
     extern __shared__ __align__(16) unsigned char s_raw[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     unsigned *s_off = reinterpret_cast<unsigned *>(s_raw) + warp * WIDE_W;
     unsigned short *s_msk = reinterpret_cast<unsigned short *>(s_raw + (size_t)ROW_WARPS * WIDE_W * 4) + warp * WIDE_W;
-    const int R = g.rowlist[(long long)ROW_WIDE * g.m + blockIdx.x];
+    // WPR warps per row: ROW_WARPS (one row per CTA, the warps split its
+    // entries) or 1 (ROW_WARPS rows per CTA, one warp each)
+    const long long idx = WPR == 1 ? (long long)blockIdx.x * ROW_WARPS + warp : (long long)blockIdx.x;
+    if (idx >= nrows) return;
+    const int part = WPR == 1 ? 0 : warp;
+    const int R = g.rowlist[(long long)cls * g.m + idx];
     const int i = R >> 4, r = R & (TILE - 1);
     const long long c0 = g.crp[i];
     const int S = (int)(g.crp[i + 1] - c0);
@@ -646,7 +652,7 @@ k_numeric_wide(NumericArgs g, bool packed)
     const int *tcol = g.ccol + c0;
     const int cshift = g.tr_coloff ? g.tr_coloff[i] : 0;
     // this warp's entries [e0, e1) and their tile columns [t0, t1)
-    const int e0 = (int)((long long)nnz_r * warp / ROW_WARPS), e1 = (int)((long long)nnz_r * (warp + 1) / ROW_WARPS);
+    const int e0 = (int)((long long)nnz_r * part / WPR), e1 = (int)((long long)nnz_r * (part + 1) / WPR);
     if (e0 >= e1) return;
     const int t0 = (g.colC[Rb + e0] + cshift) >> 4;
     const int t1 = e1 < nnz_r ? (g.colC[Rb + e1] + cshift) >> 4 : INT_MAX;
@@ -726,7 +732,8 @@ cudaError_t numeric_init_attributes()
     TSG_SET(256)
     TSG_SET(512)
 #undef TSG_SET
-    const void *fs[3] = {(const void *)k_numeric_rows, (const void *)k_numeric_rows_split, (const void *)k_numeric_wide};
+    const void *fs[4] = {(const void *)k_numeric_rows, (const void *)k_numeric_rows_split,
+                         (const void *)k_numeric_wide<ROW_WARPS>, (const void *)k_numeric_wide<1>};
     for (const void *f : fs) {
         if (e == cudaSuccess) e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_LARGE);
         if (e == cudaSuccess)
@@ -758,10 +765,12 @@ cudaError_t numeric_run(Pool &pool, const NumericArgs &a, const long long *binst
         { k_numeric_rows_split<<<(unsigned)rcnt[ROW_L], ROW_WARPS * 32, (size_t)rreq[ROW_L], s>>>(a, packed); ::tsg::count_launch(); }
         e = cudaGetLastError();
     }
-    if (e == cudaSuccess && rcnt[ROW_WIDE] > 0) {
-        const long long n = rcnt[ROW_WIDE];
-        { k_global_prep<<<(unsigned)((n * 32 + 255) / 256), 256, 0, s>>>(a, n); ::tsg::count_launch(); }
-        { k_numeric_wide<<<(unsigned)n, ROW_WARPS * 32, WIDE_SMEM, s>>>(a, packed); ::tsg::count_launch(); }
+    for (int c = ROW_WIDE; c <= ROW_WIDE1 && e == cudaSuccess; ++c) {
+        const long long n = rcnt[c];
+        if (n == 0) continue;
+        { k_global_prep<<<(unsigned)((n * 32 + 255) / 256), 256, 0, s>>>(a, c, n); ::tsg::count_launch(); }
+        if (c == ROW_WIDE) { k_numeric_wide<ROW_WARPS><<<(unsigned)n, ROW_WARPS * 32, WIDE_SMEM, s>>>(a, c, n, packed); ::tsg::count_launch(); }
+        else { k_numeric_wide<1><<<(unsigned)((n + ROW_WARPS - 1) / ROW_WARPS), ROW_WARPS * 32, WIDE_SMEM, s>>>(a, c, n, packed); ::tsg::count_launch(); }
         e = cudaGetLastError();
     }
     return e;

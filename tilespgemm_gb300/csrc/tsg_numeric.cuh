@@ -26,7 +26,8 @@ enum RowClass : int {
     ROW_M = 1,          // same, <= ROWS_MEDIUM bytes
     ROW_L = 2,          // ROW_WARPS warps per row, each a column range of it, <= SMEM_LARGE bytes
     ROW_WIDE = 3,       // accumulator in C's value array, ROW_WARPS warps over column windows
-    NROWCLS = 4
+    ROW_WIDE1 = 4,      // accumulator in C's value array, one warp per row (rows_global)
+    NROWCLS = 5
 };
 constexpr int ROW_WARPS = 8;
 
@@ -51,6 +52,7 @@ struct NumericBinParams {
     int smem_acc_max;     // largest tile-row (entries) accumulated in shared memory
     int row_acc_max;      // largest row (entries) accumulated in shared memory by the row kernel
     const long long *rpA; // A's row pointer (row classes weigh C's row against A's row)
+    int rows_global;      // rows of the shared-memory row classes accumulate in C's values instead
 };
 
 __host__ __device__ inline long long align16(long long x) { return (x + 15) & ~15ll; }
@@ -110,8 +112,10 @@ __host__ __device__ inline int numeric_row_class(const NumericBinParams &bp, lon
     req = numeric_row_smem_bytes(S, row_nnz, span);
     const bool long_b = row_nnz >= WIDE_MIN_ROW && row_nnz >= WIDE_MIN_RATIO * a_len;
     if (row_nnz <= bp.row_acc_max && row_nnz < 65536 && !long_b) {
-        if (req <= ROWS_SMALL) return ROW_S;
-        if (req <= ROWS_MEDIUM) return ROW_M;
+        if (req <= ROWS_MEDIUM) {
+            if (bp.rows_global) { req = 0; return ROW_WIDE1; }
+            return req <= ROWS_SMALL ? ROW_S : ROW_M;
+        }
         if (req <= SMEM_LARGE) return ROW_L;
     }
     req = 0;
