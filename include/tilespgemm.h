@@ -95,6 +95,8 @@ typedef struct {
                                 column. */
     int32_t rows_global;     /* 1: rows of tile-rows too large for one CTA that would accumulate in shared memory
                                 (one warp each) accumulate in C's value array instead, one warp each (default 0) */
+    int32_t row_warps;       /* warps per row for those shared-memory rows: 1, 2 or 4, each warp a column range
+                                (default 4, measured fastest) */
 } tsg_opts;
 
 /* Per-call statistics.  Sizes are always filled; times only with phase_times. */

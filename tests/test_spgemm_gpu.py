@@ -122,7 +122,8 @@ def test_general_ab_rectangular(ctx):
 
 @pytest.mark.parametrize("opts", [dict(smem_acc_max=0), dict(smem_acc_max=0, row_acc_max=0), dict(dense_tile_min=1),
                                   dict(threads_numeric=128), dict(threads_numeric=512), dict(out_rowptr_bits=64),
-                                  dict(numeric_walk=1), dict(numeric_walk=2), dict(numeric_walk=2, dense_tile_min=1)])
+                                  dict(numeric_walk=1), dict(numeric_walk=2), dict(numeric_walk=2, dense_tile_min=1),
+                                  dict(smem_acc_max=0, row_warps=1), dict(smem_acc_max=0, numeric_walk=2)])
 def test_numeric_bins_agree(opts, built_lib):
     """Every accumulator path (shared sparse, shared dense, one row per CTA,
     global) gives the same bits."""
@@ -143,7 +144,7 @@ def test_numeric_bins_agree(opts, built_lib):
                 assert C.rowptr.dtype == np.int64
 
 
-@pytest.mark.parametrize("opts", [dict(), dict(row_acc_max=0), dict(rows_global=1)])
+@pytest.mark.parametrize("opts", [dict(), dict(row_warps=1), dict(row_warps=2), dict(row_acc_max=0), dict(rows_global=1)])
 def test_long_rows(opts, built_lib):
     """C rows of ~3,900 and ~8,400 entries: the medium and large size classes
     of the one-row-per-CTA kernel (and, with row_acc_max=0, the global

@@ -505,7 +505,7 @@ tsg_status plan_numeric(tsg_ctx *ctx, Pool &pool, PlanData &P, const double *val
     if (walk < 0) walk = ctx->opts.numeric_walk;
     if (threads <= 0) threads = ctx->opts.threads_numeric;
     const bool packed = P.dupsafe || walk == 2;
-    CUDA_OK(numeric_run(pool, na, P.bstat, packed, threads));
+    CUDA_OK(numeric_run(pool, na, P.bstat, packed, threads, ctx->opts.row_warps));
     return TSG_OK;
 }
 
@@ -623,6 +623,7 @@ void tsg_opts_default(tsg_opts *o)
     o->row_acc_max = 65535;
     o->numeric_walk = 0;
     o->rows_global = 0;
+    o->row_warps = 4;
 }
 
 const char *tsg_last_error(void) { return g_err.c_str(); }

@@ -544,22 +544,24 @@ k_numeric_rows(NumericArgs g, int cls, bool packed)
     row_epilogue(g, w, i, Rb, nnz_r, lane, 32);
 }
 
-// One CTA of ROW_WARPS warps per row of class ROW_L (accumulator up to
-// SMEM_LARGE): the row's entries are split into ROW_WARPS column ranges of
-// about equal size, and warp w applies, in A's row order, only the products
-// whose column falls in its range -- disjoint outputs per warp, so the
-// order per output is unchanged.
-__global__ void __launch_bounds__(ROW_WARPS * 32, 1)
-k_numeric_rows_split(NumericArgs g, bool packed)
+// One CTA of WPR warps per row of class `cls` (accumulator in shared
+// memory): the row's entries are split into WPR column ranges of about
+// equal size, and warp w applies, in A's row order, only the products whose
+// column falls in its range -- disjoint outputs per warp, so the order per
+// output is unchanged.  More warps per row means more warps per SM for the
+// same shared memory.
+template <int WPR>
+__global__ void __launch_bounds__(WPR * 32)
+k_numeric_rows_split(NumericArgs g, int cls, bool packed)
 {
     extern __shared__ __align__(16) unsigned char s_raw[];
-    __shared__ int s_part[ROW_WARPS];
-    const int R = g.rowlist[(long long)ROW_L * g.m + blockIdx.x];
+    __shared__ int s_part[WPR];
+    const int R = g.rowlist[(long long)cls * g.m + blockIdx.x];
     const int i = R >> 4, r = R & (TILE - 1);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const long long Rb = g.rowptrC[R];
     const int nnz_r = (int)(g.rowptrC[R + 1] - Rb);
-    const RowSmem w = row_smem_build(g, s_raw, i, r, nnz_r, tid, ROW_WARPS * 32, s_part);
+    const RowSmem w = row_smem_build(g, s_raw, i, r, nnz_r, tid, WPR * 32, s_part);
     // warp's range: the slots whose row offset lies in [e_lo, e_hi)
     auto first_slot = [&](int e) {
         int lo = 0, hi = w.S;
@@ -568,8 +570,8 @@ k_numeric_rows_split(NumericArgs g, bool packed)
     };
     const long long c0 = g.crp[i];
     auto slot_col = [&](int s) { return (w.use_map ? g.ccol[c0 + s] : w.scol[s]) * TILE; };
-    const int sa = first_slot((int)((long long)nnz_r * warp / ROW_WARPS));
-    const int sb = warp + 1 < ROW_WARPS ? first_slot((int)((long long)nnz_r * (warp + 1) / ROW_WARPS)) : w.S;
+    const int sa = first_slot((int)((long long)nnz_r * warp / WPR));
+    const int sb = warp + 1 < WPR ? first_slot((int)((long long)nnz_r * (warp + 1) / WPR)) : w.S;
     const int lo = warp == 0 ? INT_MIN : (sa < w.S ? slot_col(sa) : INT_MAX);
     const int hi = sb < w.S ? slot_col(sb) : INT_MAX;
     if (lo < hi) {
@@ -580,7 +582,7 @@ k_numeric_rows_split(NumericArgs g, bool packed)
             row_walk_range(g, R, lane, lo, hi, w.acc, [&](int col) -> long long { return row_pos(w, col); });
     }
     __syncthreads();
-    row_epilogue(g, w, i, Rb, nnz_r, tid, ROW_WARPS * 32);
+    row_epilogue(g, w, i, Rb, nnz_r, tid, WPR * 32);
 }
 
 // ---- rows too large for a shared-memory accumulator (ROW_WIDE) -------------
@@ -732,7 +734,8 @@ cudaError_t numeric_init_attributes()
     TSG_SET(256)
     TSG_SET(512)
 #undef TSG_SET
-    const void *fs[4] = {(const void *)k_numeric_rows, (const void *)k_numeric_rows_split,
+    const void *fs[6] = {(const void *)k_numeric_rows, (const void *)k_numeric_rows_split<ROW_WARPS>,
+                         (const void *)k_numeric_rows_split<4>, (const void *)k_numeric_rows_split<2>,
                          (const void *)k_numeric_wide<ROW_WARPS>, (const void *)k_numeric_wide<1>};
     for (const void *f : fs) {
         if (e == cudaSuccess) e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_LARGE);
@@ -742,7 +745,8 @@ cudaError_t numeric_init_attributes()
     return e;
 }
 
-cudaError_t numeric_run(Pool &pool, const NumericArgs &a, const long long *binstat, bool packed, int threads)
+cudaError_t numeric_run(Pool &pool, const NumericArgs &a, const long long *binstat, bool packed, int threads,
+                        int row_warps)
 {
     const long long *counts = binstat, *req = binstat + NBIN;
     cudaStream_t s = pool.stream;
@@ -758,11 +762,15 @@ cudaError_t numeric_run(Pool &pool, const NumericArgs &a, const long long *binst
     const long long *rcnt = binstat + BS_ROWCNT, *rreq = binstat + BS_ROWREQ;
     for (int c = ROW_S; c <= ROW_M && e == cudaSuccess; ++c) {
         if (rcnt[c] == 0) continue;
-        { k_numeric_rows<<<(unsigned)rcnt[c], 32, (size_t)rreq[c], s>>>(a, c, packed); ::tsg::count_launch(); }
+        const unsigned g = (unsigned)rcnt[c];
+        const size_t sm = (size_t)rreq[c];
+        if (row_warps >= 4) { k_numeric_rows_split<4><<<g, 128, sm, s>>>(a, c, packed); ::tsg::count_launch(); }
+        else if (row_warps == 2) { k_numeric_rows_split<2><<<g, 64, sm, s>>>(a, c, packed); ::tsg::count_launch(); }
+        else { k_numeric_rows<<<g, 32, sm, s>>>(a, c, packed); ::tsg::count_launch(); }
         e = cudaGetLastError();
     }
     if (e == cudaSuccess && rcnt[ROW_L] > 0) {
-        { k_numeric_rows_split<<<(unsigned)rcnt[ROW_L], ROW_WARPS * 32, (size_t)rreq[ROW_L], s>>>(a, packed); ::tsg::count_launch(); }
+        { k_numeric_rows_split<ROW_WARPS><<<(unsigned)rcnt[ROW_L], ROW_WARPS * 32, (size_t)rreq[ROW_L], s>>>(a, ROW_L, packed); ::tsg::count_launch(); }
         e = cudaGetLastError();
     }
     for (int c = ROW_WIDE; c <= ROW_WIDE1 && e == cudaSuccess; ++c) {

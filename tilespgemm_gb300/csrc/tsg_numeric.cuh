@@ -170,7 +170,9 @@ cudaError_t step2_masks(Pool &pool, const TileCSR &A, const TileCSR &B, int m, i
 
 // Launch the numeric kernels of every non-empty bin and row class.
 // binstat is step 2's statistics (layout above), copied to the host.
-cudaError_t numeric_run(Pool &pool, const NumericArgs &a, const long long *binstat, bool packed, int threads);
+// row_warps: warps per row for the shared-memory row classes ROW_S / ROW_M (1, 2 or 4)
+cudaError_t numeric_run(Pool &pool, const NumericArgs &a, const long long *binstat, bool packed, int threads,
+                        int row_warps);
 
 cudaError_t symbolic_fill_fused(Pool &pool, const TileCSR &A, const TileCSR &B, int m, const long long *crp,
                                 int *ccol, uint16_t *cmask, int *rowcnt, unsigned char *bin,
