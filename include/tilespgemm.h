@@ -91,8 +91,10 @@ typedef struct {
                                 96+ per entry of A's row -- accumulate in C's value array, eight warps per row
                                 (default 65535) */
     int32_t numeric_walk;    /* 0 = auto; 1 = lanes over one B row per A entry; 2 = packed (lanes over the row's
-                                flattened (A entry, B entry) pairs).  Auto packs only when a B row repeats a
-                                column. */
+                                flattened (A entry, B entry) pairs); 3 = as 1 with the next B row's loads issued
+                                one A entry ahead in the tile-row kernels.  Auto packs only when a B row repeats
+                                a column, and loads ahead when the mean row lengths put fewer than 3 products on
+                                an entry of C. */
     int32_t rows_global;     /* 1: rows of tile-rows too large for one CTA that would accumulate in shared memory
                                 (one warp each) accumulate in C's value array instead, one warp each (default 0) */
     int32_t row_warps;       /* warps per row for those shared-memory rows: 1, 2 or 4, each warp a column range

@@ -122,7 +122,8 @@ def test_general_ab_rectangular(ctx):
 
 @pytest.mark.parametrize("opts", [dict(smem_acc_max=0), dict(smem_acc_max=0, row_acc_max=0), dict(dense_tile_min=1),
                                   dict(threads_numeric=128), dict(threads_numeric=512), dict(out_rowptr_bits=64),
-                                  dict(numeric_walk=1), dict(numeric_walk=2), dict(numeric_walk=2, dense_tile_min=1),
+                                  dict(numeric_walk=1), dict(numeric_walk=2), dict(numeric_walk=3), dict(numeric_walk=2, dense_tile_min=1),
+                                  dict(numeric_walk=3, dense_tile_min=1),
                                   dict(smem_acc_max=0, row_warps=1), dict(smem_acc_max=0, numeric_walk=2)])
 def test_numeric_bins_agree(opts, built_lib):
     """Every accumulator path (shared sparse, shared dense, one row per CTA,

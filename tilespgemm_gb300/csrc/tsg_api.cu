@@ -504,8 +504,17 @@ tsg_status plan_numeric(tsg_ctx *ctx, Pool &pool, PlanData &P, const double *val
     na.bin = P.bin; na.binlist = P.binlist; na.rowlist = P.rowlist; na.b_sorted = P.b_increasing; na.tr_coloff = tr_coloff; na.flags = ctx->dflags;
     if (walk < 0) walk = ctx->opts.numeric_walk;
     if (threads <= 0) threads = ctx->opts.threads_numeric;
-    const bool packed = P.dupsafe || walk == 2;
-    CUDA_OK(numeric_run(pool, na, P.bstat, packed, threads, ctx->opts.row_warps));
+    // repeated B columns need the packed walk.  Auto otherwise loads B one
+    // step ahead when few products meet in one output (estimated from the
+    // mean row lengths: under 3 per entry of C), where the walk is bound by
+    // the latency of B's loads, and walks plainly (twice the warps per SM)
+    // when many do.
+    int kw = 0;
+    if (P.dupsafe || walk == 2) kw = 1;
+    else if (walk == 3) kw = 2;
+    else if (walk == 0 && P.nnzC > 0 && P.k > 0 &&
+             (double)P.nnzA * ((double)P.nnzB / P.k) < 3.0 * (double)P.nnzC) kw = 2;
+    CUDA_OK(numeric_run(pool, na, P.bstat, kw, threads, ctx->opts.row_warps));
     return TSG_OK;
 }
 
@@ -1751,12 +1760,12 @@ tsg_status tsg_plan_tune(tsg_ctx *ctx, tsg_plan *plan, double *best_ms)
     tsg_status r = plan_resident(plan, pool);
     if (r) return r;
     const int cand_threads[3] = {128, 256, 512};
-    const int cand_walk[2] = {1, 2};
+    const int cand_walk[3] = {1, 2, 3};
     float best = 1e30f;
     int bt = plan->threads, bw = plan->walk;
     for (int t : cand_threads) {
         for (int w : cand_walk) {
-            if (w == 1 && plan->P.dupsafe) continue;   // repeated B columns always take the packed walk
+            if (w != 2 && plan->P.dupsafe) continue;   // repeated B columns always take the packed walk
             float tot = 0.f;
             for (int rep = 0; rep < 4; ++rep) {
                 CUDA_OK(cudaEventRecord(ctx->ev[6], ctx->stream));

@@ -259,8 +259,70 @@ __device__ __forceinline__ void row_walk_range(const NumericArgs &g, int R, int 
     if (bad) set_flag(g.flags, FLAG_INTERNAL);
 }
 
-template <int NT, bool DENSE, bool PACKED>
-__global__ void __launch_bounds__(NT, (PACKED ? 1024 : 2048) / NT)
+// numeric_row with B's entries loaded one step ahead:
+// the warp walks the (A entry, 32-entry chunk of its B row) pairs in order
+// and issues the next pair's loads before the current pair's shared-memory
+// update, so the L2 latency of B overlaps the accumulator work.  Order of the
+// updates per output is unchanged (A's row order, then B's row order).
+template <bool DENSE, bool MAP>
+__device__ __forceinline__ void numeric_row_prefetch(const NumericArgs &g, const TileRowSmem &t, int r0, int r, int lane)
+{
+    const int R = r0 + r;
+    const unsigned *wrow = t.word + r * t.S;
+    const int pa0 = (int)g.rpA[R], pa1 = (int)g.rpA[R + 1];
+    double *acc = t.acc;
+    bool bad = false;
+    for (int pb = pa0; pb < pa1; pb += 32) {
+        const int na = min(32, pa1 - pb);
+        int bs = 0, be = 0;
+        double av = 0.0;
+        if (lane < na) {
+            const int k = g.colA[pb + lane];
+            av = g.valA[pb + lane];
+            bs = (int)g.rpB[k];
+            be = (int)g.rpB[k + 1];
+        }
+        // first non-empty pair
+        int q = 0, eb = __shfl_sync(0xffffffffu, bs, 0), ee = __shfl_sync(0xffffffffu, be, 0);
+        double a = __shfl_sync(0xffffffffu, av, 0);
+        while (eb >= ee && ++q < na) {
+            eb = __shfl_sync(0xffffffffu, bs, q);
+            ee = __shfl_sync(0xffffffffu, be, q);
+            a = __shfl_sync(0xffffffffu, av, q);
+        }
+        int col = 0;
+        double b = 0.0;
+        bool ok = false;
+        if (q < na && eb + lane < ee) { ok = true; col = g.colB[eb + lane]; b = g.valB[eb + lane]; }
+        while (q < na) {
+            // next pair (uniform across the warp)
+            int nq = q, neb = eb + 32, nee = ee;
+            double na_ = a;
+            while (neb >= nee && ++nq < na) {
+                neb = __shfl_sync(0xffffffffu, bs, nq);
+                nee = __shfl_sync(0xffffffffu, be, nq);
+                na_ = __shfl_sync(0xffffffffu, av, nq);
+            }
+            int ncol = 0;
+            double nb = 0.0;
+            bool nok = false;
+            if (nq < na && neb + lane < nee) { nok = true; ncol = g.colB[neb + lane]; nb = g.valB[neb + lane]; }
+            if (ok) {
+                const int pos = out_pos<DENSE, MAP>(t, wrow, r, col);
+                if (pos < 0) bad = true;
+                else acc[pos] = fma(a, b, acc[pos]);
+            }
+            q = nq; eb = neb; ee = nee; a = na_;
+            col = ncol; b = nb; ok = nok;
+        }
+    }
+    if (bad) set_flag(g.flags, FLAG_INTERNAL);
+}
+
+// WALK: 0 lanes over one B row per A entry, 1 packed (repeated B columns),
+// 2 as 0 with B's entries loaded one step ahead (more registers, fewer warps)
+template <int NT, bool DENSE, int WALK>
+__global__ void __launch_bounds__(NT, (WALK == 0 ? 2048 : 1024) / NT)
 k_numeric_smem(NumericArgs g, int mybin)
 {
     constexpr int NWARP = NT / 32;
@@ -317,12 +379,15 @@ k_numeric_smem(NumericArgs g, int mybin)
     // warp w owns rows w, w+NWARP, ...
     TileRowSmem t{scol, word, map, acc, S, jbase, span, nacc};
     for (int r = warp; r < rows; r += NWARP) {
-        if (PACKED) {
+        if (WALK == 1) {
             const unsigned *wrow = word + r * S;
             if (use_map)
                 row_walk_packed(g, r0 + r, lane, acc, [&](int col) -> long long { return out_pos<DENSE, true>(t, wrow, r, col); });
             else
                 row_walk_packed(g, r0 + r, lane, acc, [&](int col) -> long long { return out_pos<DENSE, false>(t, wrow, r, col); });
+        } else if (WALK == 2) {
+            if (use_map) numeric_row_prefetch<DENSE, true>(g, t, r0, r, lane);
+            else numeric_row_prefetch<DENSE, false>(g, t, r0, r, lane);
         } else if (use_map) {
             numeric_row<DENSE, true>(g, t, r0, r, lane);
         } else {
@@ -354,64 +419,6 @@ k_numeric_smem(NumericArgs g, int mybin)
     }
 }
 
-// numeric_row for the row kernel, with B's entries loaded one step ahead:
-// the warp walks the (A entry, 32-entry chunk of its B row) pairs in order
-// and issues the next pair's loads before the current pair's shared-memory
-// update, so the L2 latency of B overlaps the accumulator work.  Order of the
-// updates per output is unchanged (A's row order, then B's row order).
-template <bool MAP>
-__device__ __forceinline__ void numeric_row_prefetch(const NumericArgs &g, const TileRowSmem &t, int R, int lane)
-{
-    const unsigned *wrow = t.word;
-    const int pa0 = (int)g.rpA[R], pa1 = (int)g.rpA[R + 1];
-    double *acc = t.acc;
-    bool bad = false;
-    for (int pb = pa0; pb < pa1; pb += 32) {
-        const int na = min(32, pa1 - pb);
-        int bs = 0, be = 0;
-        double av = 0.0;
-        if (lane < na) {
-            const int k = g.colA[pb + lane];
-            av = g.valA[pb + lane];
-            bs = (int)g.rpB[k];
-            be = (int)g.rpB[k + 1];
-        }
-        // first non-empty pair
-        int q = 0, eb = __shfl_sync(0xffffffffu, bs, 0), ee = __shfl_sync(0xffffffffu, be, 0);
-        double a = __shfl_sync(0xffffffffu, av, 0);
-        while (eb >= ee && ++q < na) {
-            eb = __shfl_sync(0xffffffffu, bs, q);
-            ee = __shfl_sync(0xffffffffu, be, q);
-            a = __shfl_sync(0xffffffffu, av, q);
-        }
-        int col = 0;
-        double b = 0.0;
-        bool ok = false;
-        if (q < na && eb + lane < ee) { ok = true; col = g.colB[eb + lane]; b = g.valB[eb + lane]; }
-        while (q < na) {
-            // next pair (uniform across the warp)
-            int nq = q, neb = eb + 32, nee = ee;
-            double na_ = a;
-            while (neb >= nee && ++nq < na) {
-                neb = __shfl_sync(0xffffffffu, bs, nq);
-                nee = __shfl_sync(0xffffffffu, be, nq);
-                na_ = __shfl_sync(0xffffffffu, av, nq);
-            }
-            int ncol = 0;
-            double nb = 0.0;
-            bool nok = false;
-            if (nq < na && neb + lane < nee) { nok = true; ncol = g.colB[neb + lane]; nb = g.valB[neb + lane]; }
-            if (ok) {
-                const int pos = out_pos<false, MAP>(t, wrow, 0, col);
-                if (pos < 0) bad = true;
-                else acc[pos] = fma(a, b, acc[pos]);
-            }
-            q = nq; eb = neb; ee = nee; a = na_;
-            col = ncol; b = nb; ok = nok;
-        }
-    }
-    if (bad) set_flag(g.flags, FLAG_INTERNAL);
-}
 
 // ---- rows of tile-rows too large for one CTA (BIN_ROWS) --------------------
 
@@ -538,8 +545,8 @@ k_numeric_rows(NumericArgs g, int cls, bool packed)
     const RowSmem w = row_smem_build(g, s_raw, i, r, nnz_r, lane, 32, nullptr);
     TileRowSmem t{w.scol, w.word, w.map, w.acc, w.S, w.jbase, w.span, w.nacc};
     if (packed) row_walk_packed(g, R, lane, w.acc, [&](int col) -> long long { return row_pos(w, col); });
-    else if (w.use_map) numeric_row_prefetch<true>(g, t, R, lane);
-    else numeric_row_prefetch<false>(g, t, R, lane);
+    else if (w.use_map) numeric_row_prefetch<false, true>(g, t, R, 0, lane);
+    else numeric_row_prefetch<false, false>(g, t, R, 0, lane);
     __syncwarp();
     row_epilogue(g, w, i, Rb, nnz_r, lane, 32);
 }
@@ -694,29 +701,26 @@ k_numeric_wide(NumericArgs g, int cls, long long nrows, bool packed)
     }
 }
 
-template <int NT, bool DENSE, bool PACKED>
+template <int NT, bool DENSE, int WALK>
 cudaError_t set_smem_attr() {
-    cudaError_t e = cudaFuncSetAttribute(k_numeric_smem<NT, DENSE, PACKED>,
+    cudaError_t e = cudaFuncSetAttribute(k_numeric_smem<NT, DENSE, WALK>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_LARGE);
     // the whole unified L1 as shared memory, so occupancy is set by the
     // tile-row's actual request, not by a smaller carveout
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_numeric_smem<NT, DENSE, PACKED>, cudaFuncAttributePreferredSharedMemoryCarveout,
+        e = cudaFuncSetAttribute(k_numeric_smem<NT, DENSE, WALK>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                  (int)cudaSharedmemCarveoutMaxShared);
     return e;
 }
 
 template <int NT>
-cudaError_t launch_smem(const NumericArgs &a, int bin, long long nrows, long long smem, bool dense, bool packed,
+cudaError_t launch_smem(const NumericArgs &a, int bin, long long nrows, long long smem, bool dense, int walk,
                         cudaStream_t s) {
     const unsigned grid = (unsigned)nrows;
-    if (dense) {
-        if (packed) { k_numeric_smem<NT, true, true><<<grid, NT, smem, s>>>(a, bin); ::tsg::count_launch(); }
-        else { k_numeric_smem<NT, true, false><<<grid, NT, smem, s>>>(a, bin); ::tsg::count_launch(); }
-    } else {
-        if (packed) { k_numeric_smem<NT, false, true><<<grid, NT, smem, s>>>(a, bin); ::tsg::count_launch(); }
-        else { k_numeric_smem<NT, false, false><<<grid, NT, smem, s>>>(a, bin); ::tsg::count_launch(); }
-    }
+#define TSG_L(D, W) { k_numeric_smem<NT, D, W><<<grid, NT, smem, s>>>(a, bin); ::tsg::count_launch(); }
+    if (dense) { if (walk == 1) TSG_L(true, 1) else if (walk == 2) TSG_L(true, 2) else TSG_L(true, 0) }
+    else { if (walk == 1) TSG_L(false, 1) else if (walk == 2) TSG_L(false, 2) else TSG_L(false, 0) }
+#undef TSG_L
     return cudaGetLastError();
 }
 
@@ -726,10 +730,12 @@ cudaError_t numeric_init_attributes()
 {
     cudaError_t e = cudaSuccess;
 #define TSG_SET(NT)                                                    \
-    if (e == cudaSuccess) e = set_smem_attr<NT, false, false>();       \
-    if (e == cudaSuccess) e = set_smem_attr<NT, false, true>();        \
-    if (e == cudaSuccess) e = set_smem_attr<NT, true, false>();        \
-    if (e == cudaSuccess) e = set_smem_attr<NT, true, true>();
+    if (e == cudaSuccess) e = set_smem_attr<NT, false, 0>();           \
+    if (e == cudaSuccess) e = set_smem_attr<NT, false, 1>();           \
+    if (e == cudaSuccess) e = set_smem_attr<NT, false, 2>();           \
+    if (e == cudaSuccess) e = set_smem_attr<NT, true, 0>();            \
+    if (e == cudaSuccess) e = set_smem_attr<NT, true, 1>();            \
+    if (e == cudaSuccess) e = set_smem_attr<NT, true, 2>();
     TSG_SET(128)
     TSG_SET(256)
     TSG_SET(512)
@@ -745,9 +751,10 @@ cudaError_t numeric_init_attributes()
     return e;
 }
 
-cudaError_t numeric_run(Pool &pool, const NumericArgs &a, const long long *binstat, bool packed, int threads,
+cudaError_t numeric_run(Pool &pool, const NumericArgs &a, const long long *binstat, int walk, int threads,
                         int row_warps)
 {
+    const bool packed = walk == 1;
     const long long *counts = binstat, *req = binstat + NBIN;
     cudaStream_t s = pool.stream;
     cudaError_t e = cudaSuccess;
@@ -755,9 +762,9 @@ cudaError_t numeric_run(Pool &pool, const NumericArgs &a, const long long *binst
         if (counts[b] == 0) continue;
         const bool dense = (b == BIN_DENSE_S || b == BIN_DENSE_L);
         const long long smem = req[b];
-        if (threads == 128) e = launch_smem<128>(a, b, counts[b], smem, dense, packed, s);
-        else if (threads == 512) e = launch_smem<512>(a, b, counts[b], smem, dense, packed, s);
-        else e = launch_smem<256>(a, b, counts[b], smem, dense, packed, s);
+        if (threads == 128) e = launch_smem<128>(a, b, counts[b], smem, dense, walk, s);
+        else if (threads == 512) e = launch_smem<512>(a, b, counts[b], smem, dense, walk, s);
+        else e = launch_smem<256>(a, b, counts[b], smem, dense, walk, s);
     }
     const long long *rcnt = binstat + BS_ROWCNT, *rreq = binstat + BS_ROWREQ;
     for (int c = ROW_S; c <= ROW_M && e == cudaSuccess; ++c) {

@@ -170,8 +170,10 @@ cudaError_t step2_masks(Pool &pool, const TileCSR &A, const TileCSR &B, int m, i
 
 // Launch the numeric kernels of every non-empty bin and row class.
 // binstat is step 2's statistics (layout above), copied to the host.
-// row_warps: warps per row for the shared-memory row classes ROW_S / ROW_M (1, 2 or 4)
-cudaError_t numeric_run(Pool &pool, const NumericArgs &a, const long long *binstat, bool packed, int threads,
+// walk: 0 lanes over one B row per A entry, 1 packed (repeated B columns),
+// 2 as 0 with B loads one step ahead (tile-row kernels); row_warps: warps
+// per row for the shared-memory row classes ROW_S / ROW_M (1, 2 or 4)
+cudaError_t numeric_run(Pool &pool, const NumericArgs &a, const long long *binstat, int walk, int threads,
                         int row_warps);
 
 cudaError_t symbolic_fill_fused(Pool &pool, const TileCSR &A, const TileCSR &B, int m, const long long *crp,
