@@ -526,8 +526,8 @@ void fill_stats(const PlanData &P, tsg_stats *st)
     st->tiles_a = P.tilesA; st->tiles_b = P.tilesB; st->tiles_c = P.numblkC;
     st->n_syncs = P.nsync;
     st->bins[0] = (int)P.bstat[BIN_EMPTY];
-    st->bins[1] = (int)(P.bstat[BIN_SPARSE_S] + P.bstat[BIN_SPARSE_L]);
-    st->bins[2] = (int)(P.bstat[BIN_DENSE_S] + P.bstat[BIN_DENSE_L]);
+    st->bins[1] = (int)(P.bstat[BIN_SPARSE_S] + P.bstat[BIN_SPARSE_M] + P.bstat[BIN_SPARSE_L]);
+    st->bins[2] = (int)(P.bstat[BIN_DENSE_S] + P.bstat[BIN_DENSE_M] + P.bstat[BIN_DENSE_L]);
     st->bins[3] = (int)P.bstat[BIN_ROWS];
 }
 

@@ -37,6 +37,7 @@
 // 12 bytes per C entry written.
 #include "tsg_numeric.cuh"
 
+#include <algorithm>
 #include <climits>
 
 namespace tsg {
@@ -760,10 +761,12 @@ cudaError_t numeric_run(Pool &pool, const NumericArgs &a, const long long *binst
     cudaError_t e = cudaSuccess;
     for (int b = BIN_SPARSE_S; b <= BIN_DENSE_L && e == cudaSuccess; ++b) {
         if (counts[b] == 0) continue;
-        const bool dense = (b == BIN_DENSE_S || b == BIN_DENSE_L);
+        const bool dense = b >= BIN_DENSE_S;
         const long long smem = req[b];
-        if (threads == 128) e = launch_smem<128>(a, b, counts[b], smem, dense, walk, s);
-        else if (threads == 512) e = launch_smem<512>(a, b, counts[b], smem, dense, walk, s);
+        // bins whose shared memory leaves one or two CTAs per SM run 16 warps, one per row
+        const int nt = (b == BIN_SPARSE_S || b == BIN_DENSE_S) ? threads : std::max(threads, 512);
+        if (nt == 128) e = launch_smem<128>(a, b, counts[b], smem, dense, walk, s);
+        else if (nt == 512) e = launch_smem<512>(a, b, counts[b], smem, dense, walk, s);
         else e = launch_smem<256>(a, b, counts[b], smem, dense, walk, s);
     }
     const long long *rcnt = binstat + BS_ROWCNT, *rreq = binstat + BS_ROWREQ;
@@ -771,7 +774,8 @@ cudaError_t numeric_run(Pool &pool, const NumericArgs &a, const long long *binst
         if (rcnt[c] == 0) continue;
         const unsigned g = (unsigned)rcnt[c];
         const size_t sm = (size_t)rreq[c];
-        if (row_warps >= 4) { k_numeric_rows_split<4><<<g, 128, sm, s>>>(a, c, packed); ::tsg::count_launch(); }
+        if (row_warps >= 8) { k_numeric_rows_split<ROW_WARPS><<<g, ROW_WARPS * 32, sm, s>>>(a, c, packed); ::tsg::count_launch(); }
+        else if (row_warps >= 4) { k_numeric_rows_split<4><<<g, 128, sm, s>>>(a, c, packed); ::tsg::count_launch(); }
         else if (row_warps == 2) { k_numeric_rows_split<2><<<g, 64, sm, s>>>(a, c, packed); ::tsg::count_launch(); }
         else { k_numeric_rows<<<g, 32, sm, s>>>(a, c, packed); ::tsg::count_launch(); }
         e = cudaGetLastError();

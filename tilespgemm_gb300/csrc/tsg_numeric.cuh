@@ -11,11 +11,13 @@ namespace tsg {
 enum NumericBin : int {
     BIN_EMPTY = 0,      // no entries
     BIN_SPARSE_S = 1,   // mask-rank accumulator in shared memory, <= SMEM_SMALL bytes
-    BIN_SPARSE_L = 2,   // same, <= SMEM_LARGE bytes (one CTA per SM)
-    BIN_DENSE_S = 3,    // dense 16x16 tile accumulators in shared memory, <= SMEM_SMALL
-    BIN_DENSE_L = 4,    // same, <= SMEM_LARGE
-    BIN_ROWS = 5,       // too large for one CTA: each of its rows is classed on its own (RowClass)
-    NBIN = 6
+    BIN_SPARSE_M = 2,   // same, <= SMEM_MEDIUM bytes (two CTAs per SM)
+    BIN_SPARSE_L = 3,   // same, <= SMEM_LARGE bytes (one CTA per SM)
+    BIN_DENSE_S = 4,    // dense 16x16 tile accumulators in shared memory, <= SMEM_SMALL
+    BIN_DENSE_M = 5,    // same, <= SMEM_MEDIUM
+    BIN_DENSE_L = 6,    // same, <= SMEM_LARGE
+    BIN_ROWS = 7,       // too large for one CTA: each of its rows is classed on its own (RowClass)
+    NBIN = 8
 };
 
 // Classes of the rows of BIN_ROWS tile-rows; each class is one launch over a
@@ -41,6 +43,7 @@ __host__ __device__ inline bool fused_handles(long long span, long long S) {
 }
 
 constexpr long long SMEM_SMALL = 48 * 1024;
+constexpr long long SMEM_MEDIUM = 100 * 1024;
 constexpr long long SMEM_LARGE = 200 * 1024;
 constexpr long long MAP_MAX = 8192;   // direct tile-column -> slot map when the window is this narrow
 // size classes of the row kernels
@@ -87,10 +90,10 @@ __host__ __device__ inline void numeric_classify(const NumericBinParams &bp, lon
     const long long dreq = numeric_smem_bytes(S, nnz_tr, span, true);
     const long long sreq = numeric_smem_bytes(S, nnz_tr, span, false);
     if (nnz_tr >= (long long)bp.dense_tile_min * S && dreq <= SMEM_LARGE && nnz_tr < 65536) {
-        bin = dreq <= SMEM_SMALL ? BIN_DENSE_S : BIN_DENSE_L;
+        bin = dreq <= SMEM_SMALL ? BIN_DENSE_S : dreq <= SMEM_MEDIUM ? BIN_DENSE_M : BIN_DENSE_L;
         req = dreq;
     } else if (nnz_tr <= bp.smem_acc_max && sreq <= SMEM_LARGE && nnz_tr < 65536) {
-        bin = sreq <= SMEM_SMALL ? BIN_SPARSE_S : BIN_SPARSE_L;
+        bin = sreq <= SMEM_SMALL ? BIN_SPARSE_S : sreq <= SMEM_MEDIUM ? BIN_SPARSE_M : BIN_SPARSE_L;
         req = sreq;
     } else {
         bin = BIN_ROWS;
