@@ -112,6 +112,28 @@ def O_transpose_csr(A):
     return CSR(A.n, A.m, tp, tr, tv)
 
 
+def _mixed_b(k, n, seed):
+    """B with mostly 3-entry rows and every 37th row 200 entries long."""
+    from tilespgemm_gb300 import matrices as M
+    rng = np.random.default_rng(seed)
+    lens = np.where(np.arange(k) % 37 == 0, min(200, n), 3)
+    r = np.repeat(np.arange(k, dtype=np.int64), lens)
+    c = np.concatenate([rng.choice(n, size=int(L), replace=False) for L in lens])
+    return M._from_coo(k, n, r, c, rng.uniform(-1.0, 1.0, size=r.size), merge=True)
+
+
+@pytest.mark.parametrize("n", [900, 9000])
+def test_sparse_a_tiles_mixed_b_rows(ctx, n):
+    """A tiles of about one entry (the symbolic steps walk A by entry) times
+    B rows both shorter and longer than the entry walk takes (the long ones
+    go through B's tile masks); C tile-rows narrow (n=900) and wide (n=9000)."""
+    from tilespgemm_gb300 import matrices as M
+    A = M.random_sparse(2000, 3000, 4, seed=31)
+    B = _mixed_b(3000, n, seed=32)
+    C = ctx.spgemm(A, B, op="AB")
+    check_against_oracle(C, A, B)
+
+
 def test_general_ab_rectangular(ctx):
     from tilespgemm_gb300 import matrices as M
     A = M.random_sparse(300, 500, 9, seed=21)

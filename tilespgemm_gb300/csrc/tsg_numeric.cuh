@@ -169,7 +169,7 @@ cudaError_t step2_masks(Pool &pool, const TileCSR &A, const TileCSR &B, int m, i
                         const int *ccol, uint16_t *cmask, int *rowcnt, int max_tiles_per_row, int max_span,
                         const NumericBinParams &bp, unsigned char *bin, long long *binstat, int *binlist,
                         int *rowlist, int *flags, const int *defer_list, int ndefer, const long long *erpB,
-                        const int *ecolB);
+                        const int *ecolB, const long long *erpA, const int *ecolA);
 
 // Launch the numeric kernels of every non-empty bin and row class.
 // binstat is step 2's statistics (layout above), copied to the host.
@@ -182,7 +182,8 @@ cudaError_t numeric_run(Pool &pool, const NumericArgs &a, const long long *binst
 cudaError_t symbolic_fill_fused(Pool &pool, const TileCSR &A, const TileCSR &B, int m, const long long *crp,
                                 int *ccol, uint16_t *cmask, int *rowcnt, unsigned char *bin,
                                 const NumericBinParams &bp, long long *binstat, int *binlist, int *rowlist, int *cnt,
-                                int *wide, int *flags, const long long *erpB, const int *ecolB);
+                                int *wide, int *flags, const long long *erpB, const int *ecolB,
+                                const long long *erpA, const int *ecolA);
 cudaError_t masks_to_tile_major_i32(Pool &pool, int blkm, const int *rowptr, const uint16_t *src, uint16_t *dst);
 cudaError_t masks_to_tile_major_i64(Pool &pool, int blkm, const long long *rowptr, const uint16_t *src, uint16_t *dst);
 

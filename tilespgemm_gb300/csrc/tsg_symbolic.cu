@@ -47,6 +47,8 @@ __device__ __forceinline__ unsigned or_rows(unsigned ma, const uint16_t *__restr
 }
 
 constexpr int STG = 64;   // B tiles staged per warp at a time
+constexpr int ENTRY_WALK_MAX = 3;   // mean A entries per A tile up to which step 2 walks A's rows by entry
+constexpr int ENTRY_B_MAX = 64;     // ...taking there the B rows of at most this many entries
 
 // OR `bits` into 16-bit mask idx of a uint16 array in shared memory (word atomics)
 __device__ __forceinline__ void smask_or(unsigned short *m, int idx, unsigned bits) {
@@ -76,7 +78,8 @@ k_step2(int blkm, int m, const int *__restrict__ arp, const int *__restrict__ ac
         const uint16_t *__restrict__ bmask, const long long *__restrict__ crp, const int *__restrict__ ccol,
         uint16_t *cmask, int *rowcnt, int smin, int smax, int map_cap, NumericBinParams bp, unsigned char *bin,
         long long *binstat, int *binlist, int *rowlist, int *flags, const int *__restrict__ rows_list,
-        const long long *__restrict__ erpB, const int *__restrict__ ecolB)
+        const long long *__restrict__ erpB, const int *__restrict__ ecolB, const long long *__restrict__ erpA,
+        const int *__restrict__ ecolA)
 {
     extern __shared__ __align__(16) unsigned char s_raw[];
     __shared__ long long s_rowtot[TILE];
@@ -85,6 +88,7 @@ k_step2(int blkm, int m, const int *__restrict__ arp, const int *__restrict__ ac
     const long long c0 = crp[i];
     const int S = (int)(crp[i + 1] - c0);
     if (S <= smin || S > smax) return;
+    const int rows = min(TILE, m - i * TILE);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int jbase = S > 0 ? ccol[c0] : 0;
     const int span = S > 0 ? ccol[c0 + S - 1] - jbase + 1 : 0;
@@ -110,11 +114,55 @@ k_step2(int blkm, int m, const int *__restrict__ arp, const int *__restrict__ ac
 
     const int a0 = arp[i], a1 = arp[i + 1], na = a1 - a0;
     bool bad = false;
-    for (int a = a0 + warp; a < a1; a += (NT / 32)) {
+    // A tiles of a few entries each: walk A's rows entry by entry instead
+    // (warp w takes rows w, w + NT/32, ...; lanes take the B row of each
+    // entry), skipping the per-tile transpose.  Entries whose B row is
+    // longer than ENTRY_B_MAX are left to the tile walk below, which then
+    // takes only those (OR does not depend on order): there B's tile masks
+    // cover many of the row's entries per operation.
+    const long long nea = erpA[(long long)i * TILE + rows] - erpA[(long long)i * TILE];
+    const bool by_entry = nea <= (long long)ENTRY_WALK_MAX * na;
+    bool has_long = !by_entry;
+    if (by_entry) {
+        for (int r = warp; r < rows; r += (NT / 32)) {
+            const int p0 = (int)erpA[(long long)i * TILE + r], p1 = (int)erpA[(long long)i * TILE + r + 1];
+            for (int pb = p0; pb < p1; pb += 32) {
+                const int cnt = min(32, p1 - pb);
+                int bs = 0, be = 0;
+                if (lane < cnt) {
+                    const int k = ecolA[pb + lane];
+                    bs = (int)erpB[k];
+                    be = (int)erpB[k + 1];
+                }
+                if (be - bs > ENTRY_B_MAX) has_long = true;
+                for (int q = 0; q < cnt; ++q) {
+                    const int e0 = __shfl_sync(0xffffffffu, bs, q), e1 = __shfl_sync(0xffffffffu, be, q);
+                    if (e1 - e0 > ENTRY_B_MAX) continue;
+                    for (int e = e0 + lane; e < e1; e += 32) {
+                        const int col = ecolB[e];
+                        const int sl = c_slot(col >> 4, jbase, span, map, scol, S);
+                        if (sl < 0) { bad = true; continue; }
+                        smask_or(smask, r * S + sl, 0x8000u >> (col & 15));
+                    }
+                }
+            }
+        }
+    }
+    has_long = __syncthreads_or(has_long);
+    for (int a = a0 + warp; a < a1 && has_long; a += (NT / 32)) {
         const int kt = acol[a];
         const int q0 = brp[kt], nq = brp[kt + 1] - q0;
         // transpose the A tile: colrows[c] = rows r whose mask has local column c
-        const unsigned ma = (lane < TILE) ? (unsigned)amask[(long long)a0 * TILE + (long long)lane * na + (a - a0)] : 0u;
+        unsigned ma = (lane < TILE) ? (unsigned)amask[(long long)a0 * TILE + (long long)lane * na + (a - a0)] : 0u;
+        if (by_entry) {
+            // only the columns whose B rows the entry walk left (a used
+            // column names a row of B, so the row pointer reads stay in range)
+            const unsigned used = __brev(__reduce_or_sync(0xffffffffu, ma)) >> 16;
+            const bool lng = lane < TILE && ((used >> lane) & 1u) &&
+                             erpB[kt * TILE + lane + 1] - erpB[kt * TILE + lane] > ENTRY_B_MAX;
+            ma &= __brev(__ballot_sync(0xffffffffu, lng)) >> 16;
+            if (!__any_sync(0xffffffffu, ma != 0u)) continue;
+        }
         unsigned colrows[TILE];
 #pragma unroll
         for (int c = 0; c < TILE; ++c) colrows[c] = __ballot_sync(0xffffffffu, (ma >> (TILE - 1 - c)) & 1u) & 0xffffu;
@@ -172,7 +220,6 @@ k_step2(int blkm, int m, const int *__restrict__ arp, const int *__restrict__ ac
     if (bad) set_flag(flags, FLAG_INTERNAL);
     __syncthreads();
 
-    const int rows = min(TILE, m - i * TILE);
     // both smask and cmask are row-major ([r][s]) within the tile-row
     for (int t = tid; t < S * TILE; t += NT) cmask[c0 * TILE + t] = smask[t];
     for (int r = warp; r < TILE; r += (NT / 32)) {
@@ -380,7 +427,7 @@ cudaError_t step2_masks(Pool &pool, const TileCSR &A, const TileCSR &B, int m, i
                         const int *ccol, uint16_t *cmask, int *rowcnt, int max_tiles_per_row, int max_span,
                         const NumericBinParams &bp, unsigned char *bin, long long *binstat, int *binlist,
                         int *rowlist, int *flags, const int *defer_list, int ndefer, const long long *erpB,
-                        const int *ecolB)
+                        const int *ecolB, const long long *erpA, const int *ecolA)
 {
     cudaStream_t s = pool.stream;
     if (blkm <= 0 || ndefer <= 0) return cudaSuccess;
@@ -389,13 +436,13 @@ cudaError_t step2_masks(Pool &pool, const TileCSR &A, const TileCSR &B, int m, i
         const int slots = max_tiles_per_row < S2_SMALL ? max_tiles_per_row : S2_SMALL;
         { k_step2<256><<<ndefer, 256, step2_smem(slots, map_cap), s>>>(blkm, m, A.trp, A.tcol, A.mask, B.trp, B.tcol, B.mask, crp, ccol,
                                                    cmask, rowcnt, 0, S2_SMALL, map_cap, bp, bin, binstat, binlist, rowlist, flags, defer_list,
-                                                   erpB, ecolB); ::tsg::count_launch(); }
+                                                   erpB, ecolB, erpA, ecolA); ::tsg::count_launch(); }
     }
     if (max_tiles_per_row > S2_SMALL) {
         const int slots = max_tiles_per_row < S2_SMAX ? max_tiles_per_row : S2_SMAX;
         { k_step2<512><<<ndefer, 512, step2_smem(slots, map_cap), s>>>(blkm, m, A.trp, A.tcol, A.mask, B.trp, B.tcol, B.mask, crp, ccol,
                                                    cmask, rowcnt, S2_SMALL, S2_SMAX, map_cap, bp, bin, binstat, binlist, rowlist, flags, defer_list,
-                                                   erpB, ecolB); ::tsg::count_launch(); }
+                                                   erpB, ecolB, erpA, ecolA); ::tsg::count_launch(); }
     }
     if (max_tiles_per_row > S2_SMAX) {
         { k_step2_win<512><<<ndefer, 512, step2_smem(S2_SMAX, MAP_MAX), s>>>(blkm, m, A.trp, A.tcol, A.mask, B.trp, B.tcol, B.mask, crp, ccol,

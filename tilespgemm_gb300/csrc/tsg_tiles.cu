@@ -232,6 +232,8 @@ k_union_fill(typename KS::Params P, int nrows, const TP *rowptr, int *out, uint1
 // ---- fused step-1 fill + step 2 (narrow tile-rows) -------------------------
 
 constexpr int FWPC = 4;                 // warps per CTA
+constexpr int FUSED_ENTRY_WALK_MAX = 3; // mean A entries per A tile up to which A's rows are walked by entry,
+constexpr int FUSED_ENTRY_B_MAX = 64;   // ...taking there the B rows of at most this many entries
 constexpr int FSW = FUSED_MAX_TILES;    // most C tiles per tile-row handled here
 static_assert(NW * 32 == FUSED_MAX_SPAN, "fused window");
 
@@ -247,7 +249,8 @@ __global__ void __launch_bounds__(FWPC * 32)
 k_sym_fused(UnionKeys::Params P, int blkm, int m, const long long *__restrict__ crp, int *ccol,
             const uint16_t *__restrict__ amask, const uint16_t *__restrict__ bmask, uint16_t *cmask, int *rowcnt,
             unsigned char *bin, NumericBinParams bp, long long *binstat, int *binlist, int *rowlist, int *flags,
-            const long long *__restrict__ erpB, const int *__restrict__ ecolB)
+            const long long *__restrict__ erpB, const int *__restrict__ ecolB, const long long *__restrict__ erpA,
+            const int *__restrict__ ecolA)
 {
     __shared__ unsigned s_bm[FWPC][NW + 1];
     __shared__ unsigned short s_pref[FWPC][NW + 1];
@@ -300,7 +303,50 @@ k_sym_fused(UnionKeys::Params P, int blkm, int m, const long long *__restrict__ 
     if (S > FSW) return;          // masks and counts of this tile-row: CTA step-2 kernel
     const int a0 = P.arp[row], a1 = P.arp[row + 1], na = a1 - a0;
     bool bad = false;
-    for (int ab = a0; ab < a1; ab += 32) {
+    // A tiles of a few entries each: A's rows entry by entry, lanes over the
+    // B row of each entry (no per-tile transpose).  Entries whose B row is
+    // longer than FUSED_ENTRY_B_MAX are left to the tile walk, which then
+    // takes only those (OR does not depend on order).
+    const long long ea0 = erpA[(long long)row * TILE];
+    const bool by_entry = erpA[(long long)row * TILE + rows] - ea0 <= (long long)FUSED_ENTRY_WALK_MAX * na;
+    bool has_long = !by_entry;
+    if (by_entry) {
+        unsigned *mw = reinterpret_cast<unsigned *>(msk);
+        const int p0 = (int)ea0, p1 = (int)erpA[(long long)row * TILE + rows];
+        // lane l <= rows holds the start of row l; an entry's row is the
+        // number of row starts at or before it, less one
+        const int rstart = lane <= rows ? (int)erpA[(long long)row * TILE + lane] : INT_MAX;
+        for (int pb = p0; pb < p1; pb += 32) {
+            const int cnt = min(32, p1 - pb);
+            int bs = 0, be = 0;
+            if (lane < cnt) {
+                const int k = ecolA[pb + lane];
+                bs = (int)erpB[k];
+                be = (int)erpB[k + 1];
+            }
+            if (be - bs > FUSED_ENTRY_B_MAX) has_long = true;
+            for (int q = 0; q < cnt; ++q) {
+                const int r = __popc(__ballot_sync(0xffffffffu, rstart <= pb + q)) - 1;
+                const int e0 = __shfl_sync(0xffffffffu, bs, q), e1 = __shfl_sync(0xffffffffu, be, q);
+                if (e1 - e0 > FUSED_ENTRY_B_MAX) continue;
+                for (int e = e0 + lane; e < e1; e += 32) {
+                    const int col = ecolB[e];
+                    const int o = (col >> 4) - kbase;
+                    int slot = -1;
+                    if (o >= 0 && o < wbits) {
+                        const int w = o >> 5;
+                        slot = pref[w] + __popc(bm[w] & ((1u << (o & 31)) - 1u));
+                    }
+                    if (slot < 0 || slot >= S) { bad = true; continue; }
+                    const int idx = r * S + slot;
+                    atomicOr(mw + (idx >> 1), (0x8000u >> (col & 15)) << ((idx & 1) * 16));
+                }
+            }
+        }
+    }
+    __syncwarp();
+    has_long = __any_sync(0xffffffffu, has_long);
+    for (int ab = a0; ab < a1 && has_long; ab += 32) {
         // B tile-row of up to 32 A tiles, fetched by the lanes at once
         const int nac = min(32, a1 - ab);
         int q0l = 0, nql = 0;
@@ -312,7 +358,17 @@ k_sym_fused(UnionKeys::Params P, int blkm, int m, const long long *__restrict__ 
         for (int t = 0; t < nac; ++t) {
             const int q0 = __shfl_sync(0xffffffffu, q0l, t), nq = __shfl_sync(0xffffffffu, nql, t);
             const int a = ab + t;
-            const unsigned ma = (lane < TILE) ? (unsigned)amask[(long long)a0 * TILE + (long long)lane * na + (a - a0)] : 0u;
+            unsigned ma = (lane < TILE) ? (unsigned)amask[(long long)a0 * TILE + (long long)lane * na + (a - a0)] : 0u;
+            if (by_entry) {
+                // only the columns whose B rows the entry walk left (a used
+                // column names a row of B, so the row pointer reads stay in range)
+                const unsigned used = __brev(__reduce_or_sync(0xffffffffu, ma)) >> 16;
+                const int ktu = P.acol[a];
+                const bool lng = lane < TILE && ((used >> lane) & 1u) &&
+                                 erpB[ktu * TILE + lane + 1] - erpB[ktu * TILE + lane] > FUSED_ENTRY_B_MAX;
+                ma &= __brev(__ballot_sync(0xffffffffu, lng)) >> 16;
+                if (!__any_sync(0xffffffffu, ma != 0u)) continue;
+            }
             // transpose the A tile: colrows[c] = rows that use local column c (uniform)
             unsigned colrows[TILE];
 #pragma unroll
@@ -853,14 +909,15 @@ cudaError_t tile_symbolic(Pool &pool, const TileCSR &A, const TileCSR &B, long l
 cudaError_t symbolic_fill_fused(Pool &pool, const TileCSR &A, const TileCSR &B, int m, const long long *crp,
                                 int *ccol, uint16_t *cmask, int *rowcnt, unsigned char *bin,
                                 const NumericBinParams &bp, long long *binstat, int *binlist, int *rowlist, int *cnt,
-                                int *wide, int *flags, const long long *erpB, const int *ecolB)
+                                int *wide, int *flags, const long long *erpB, const int *ecolB,
+                                const long long *erpA, const int *ecolA)
 {
     cudaStream_t s = pool.stream;
     if (A.blkm <= 0) return cudaSuccess;
     UnionKeys::Params P{A.trp, A.tcol, B.trp, B.tcol, B.bmoff, B.bmw};
     { k_sym_fused<<<(unsigned)((A.blkm + FWPC - 1) / FWPC), FWPC * 32, 0, s>>>(P, A.blkm, m, crp, ccol, A.mask, B.mask,
                                                                          cmask, rowcnt, bin, bp, binstat, binlist, rowlist, flags,
-                                                                         erpB, ecolB); ::tsg::count_launch(); }
+                                                                         erpB, ecolB, erpA, ecolA); ::tsg::count_launch(); }
     (void)cnt;
     { k_union_wide<UnionKeys, true, false, long long><<<304, WIDE_THREADS, WIDE_SMEM, s>>>(
         P, wide, wide + A.blkm, nullptr, nullptr, crp, ccol, nullptr); ::tsg::count_launch(); }
