@@ -595,7 +595,8 @@ k_numeric_rows_split(NumericArgs g, int cls, bool packed)
 
 // ---- rows too large for a shared-memory accumulator (ROW_WIDE) -------------
 
-// per wide row (one warp each): column indices and zeroed values
+// per wide row (one warp each): column indices (the wide kernel zeroes the
+// values window by window)
 __global__ void __launch_bounds__(256)
 k_global_prep(NumericArgs g, int cls, long long nrows)
 {
@@ -619,7 +620,6 @@ k_global_prep(NumericArgs g, int cls, long long nrows)
         while (mk) {
             const int b = 31 - __clz(mk);
             g.colC[dst] = jb + (TILE - 1 - b);
-            g.valC[dst] = 0.0;
             ++dst;
             mk &= ~(1u << b);
         }
@@ -631,7 +631,7 @@ constexpr int WIDE_W = 1024;   // tile columns per window of the wide-row kernel
 constexpr size_t WIDE_SMEM = (size_t)ROW_WARPS * WIDE_W * (4 + 2);
 
 // One CTA of ROW_WARPS warps per wide row; the values accumulate in place in
-// C (zeroed, and columns written, by k_global_prep).  The row's entries are
+// C (columns written by k_global_prep, values zeroed per window here).  The row's entries are
 // split into ROW_WARPS column ranges of about equal size (read off C's
 // column indices), and warp w walks its range in windows of at most WIDE_W
 // tile columns: for a window it tabulates, by tile column, the row's mask
@@ -681,7 +681,15 @@ k_numeric_wide(NumericArgs g, int cls, long long nrows, bool packed)
             const unsigned mk = ss < sb ? (unsigned)mrow[ss] : 0u;
             const int c = __popc(mk);
             const int incl = warp_incl_scan(c, lane);
-            if (mk) { const int t = tcol[ss] - j0; s_off[t] = run + incl - c; s_msk[t] = (unsigned short)mk; }
+            if (mk) {
+                const int t = tcol[ss] - j0;
+                s_off[t] = run + incl - c;
+                s_msk[t] = (unsigned short)mk;
+                // the segment's values zeroed just before the walk updates
+                // them, so they are still in L2 then
+                const long long dst = Rb + run + incl - c;
+                for (int q = 0; q < c; ++q) g.valC[dst + q] = 0.0;
+            }
             run += __shfl_sync(0xffffffffu, incl, 31);
         }
         __syncwarp();
