@@ -48,7 +48,14 @@ __device__ __forceinline__ unsigned or_rows(unsigned ma, const uint16_t *__restr
 
 constexpr int STG = 64;   // B tiles staged per warp at a time
 constexpr int ENTRY_WALK_MAX = 3;   // mean A entries per A tile up to which step 2 walks A's rows by entry
-constexpr int ENTRY_B_MAX = 64;     // ...taking there the B rows of at most this many entries
+
+// Tile-row i's A tiles hold ENTRY_WALK_MAX entries or fewer on average: step
+// 2 then walks A's rows entry by entry (k_step2_entries) instead of tile by
+// tile, as the per-tile transpose would cost more than the entries.
+__device__ __forceinline__ bool entry_walk(const long long *erpA, const int *arp, int i, int rows) {
+    const long long nea = erpA[(long long)i * TILE + rows] - erpA[(long long)i * TILE];
+    return nea <= (long long)ENTRY_WALK_MAX * (arp[i + 1] - arp[i]);
+}
 
 // OR `bits` into 16-bit mask idx of a uint16 array in shared memory (word atomics)
 __device__ __forceinline__ void smask_or(unsigned short *m, int idx, unsigned bits) {
@@ -78,8 +85,7 @@ k_step2(int blkm, int m, const int *__restrict__ arp, const int *__restrict__ ac
         const uint16_t *__restrict__ bmask, const long long *__restrict__ crp, const int *__restrict__ ccol,
         uint16_t *cmask, int *rowcnt, int smin, int smax, int map_cap, NumericBinParams bp, unsigned char *bin,
         long long *binstat, int *binlist, int *rowlist, int *flags, const int *__restrict__ rows_list,
-        const long long *__restrict__ erpB, const int *__restrict__ ecolB, const long long *__restrict__ erpA,
-        const int *__restrict__ ecolA)
+        const long long *__restrict__ erpB, const int *__restrict__ ecolB, const long long *__restrict__ erpA)
 {
     extern __shared__ __align__(16) unsigned char s_raw[];
     __shared__ long long s_rowtot[TILE];
@@ -93,6 +99,7 @@ k_step2(int blkm, int m, const int *__restrict__ arp, const int *__restrict__ ac
     const int jbase = S > 0 ? ccol[c0] : 0;
     const int span = S > 0 ? ccol[c0 + S - 1] - jbase + 1 : 0;
     if (fused_handles(span, S)) return;     // done by the fused warp kernel
+    if (entry_walk(erpA, arp, i, rows)) return;   // sparse A tiles: k_step2_entries
     unsigned short *smask = reinterpret_cast<unsigned short *>(s_raw);          // [16][S]
     int *wcol = reinterpret_cast<int *>(s_raw + align16((long long)S * TILE * 2));
     unsigned short *map = nullptr;
@@ -114,55 +121,11 @@ k_step2(int blkm, int m, const int *__restrict__ arp, const int *__restrict__ ac
 
     const int a0 = arp[i], a1 = arp[i + 1], na = a1 - a0;
     bool bad = false;
-    // A tiles of a few entries each: walk A's rows entry by entry instead
-    // (warp w takes rows w, w + NT/32, ...; lanes take the B row of each
-    // entry), skipping the per-tile transpose.  Entries whose B row is
-    // longer than ENTRY_B_MAX are left to the tile walk below, which then
-    // takes only those (OR does not depend on order): there B's tile masks
-    // cover many of the row's entries per operation.
-    const long long nea = erpA[(long long)i * TILE + rows] - erpA[(long long)i * TILE];
-    const bool by_entry = nea <= (long long)ENTRY_WALK_MAX * na;
-    bool has_long = !by_entry;
-    if (by_entry) {
-        for (int r = warp; r < rows; r += (NT / 32)) {
-            const int p0 = (int)erpA[(long long)i * TILE + r], p1 = (int)erpA[(long long)i * TILE + r + 1];
-            for (int pb = p0; pb < p1; pb += 32) {
-                const int cnt = min(32, p1 - pb);
-                int bs = 0, be = 0;
-                if (lane < cnt) {
-                    const int k = ecolA[pb + lane];
-                    bs = (int)erpB[k];
-                    be = (int)erpB[k + 1];
-                }
-                if (be - bs > ENTRY_B_MAX) has_long = true;
-                for (int q = 0; q < cnt; ++q) {
-                    const int e0 = __shfl_sync(0xffffffffu, bs, q), e1 = __shfl_sync(0xffffffffu, be, q);
-                    if (e1 - e0 > ENTRY_B_MAX) continue;
-                    for (int e = e0 + lane; e < e1; e += 32) {
-                        const int col = ecolB[e];
-                        const int sl = c_slot(col >> 4, jbase, span, map, scol, S);
-                        if (sl < 0) { bad = true; continue; }
-                        smask_or(smask, r * S + sl, 0x8000u >> (col & 15));
-                    }
-                }
-            }
-        }
-    }
-    has_long = __syncthreads_or(has_long);
-    for (int a = a0 + warp; a < a1 && has_long; a += (NT / 32)) {
+    for (int a = a0 + warp; a < a1; a += (NT / 32)) {
         const int kt = acol[a];
         const int q0 = brp[kt], nq = brp[kt + 1] - q0;
         // transpose the A tile: colrows[c] = rows r whose mask has local column c
-        unsigned ma = (lane < TILE) ? (unsigned)amask[(long long)a0 * TILE + (long long)lane * na + (a - a0)] : 0u;
-        if (by_entry) {
-            // only the columns whose B rows the entry walk left (a used
-            // column names a row of B, so the row pointer reads stay in range)
-            const unsigned used = __brev(__reduce_or_sync(0xffffffffu, ma)) >> 16;
-            const bool lng = lane < TILE && ((used >> lane) & 1u) &&
-                             erpB[kt * TILE + lane + 1] - erpB[kt * TILE + lane] > ENTRY_B_MAX;
-            ma &= __brev(__ballot_sync(0xffffffffu, lng)) >> 16;
-            if (!__any_sync(0xffffffffu, ma != 0u)) continue;
-        }
+        const unsigned ma = (lane < TILE) ? (unsigned)amask[(long long)a0 * TILE + (long long)lane * na + (a - a0)] : 0u;
         unsigned colrows[TILE];
 #pragma unroll
         for (int c = 0; c < TILE; ++c) colrows[c] = __ballot_sync(0xffffffffu, (ma >> (TILE - 1 - c)) & 1u) & 0xffffu;
@@ -262,7 +225,7 @@ k_step2_win(int blkm, int m, const int *__restrict__ arp, const int *__restrict_
             const uint16_t *__restrict__ bmask, const long long *__restrict__ crp, const int *__restrict__ ccol,
             uint16_t *cmask, int *rowcnt, int smax, NumericBinParams bp, unsigned char *bin,
             long long *binstat, int *binlist, int *rowlist, int *flags, const int *__restrict__ rows_list,
-            const long long *__restrict__ erpB, const int *__restrict__ ecolB)
+            const long long *__restrict__ erpB, const int *__restrict__ ecolB, const long long *__restrict__ erpA)
 {
     extern __shared__ __align__(16) unsigned char s_raw[];
     __shared__ long long s_rowtot[TILE];
@@ -271,6 +234,8 @@ k_step2_win(int blkm, int m, const int *__restrict__ arp, const int *__restrict_
     const long long c0 = crp[i];
     const int S = (int)(crp[i + 1] - c0);
     if (S <= smax) return;
+    const int rows = min(TILE, m - i * TILE);
+    if (entry_walk(erpA, arp, i, rows)) return;   // sparse A tiles: k_step2_entries
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int span = ccol[c0 + S - 1] - ccol[c0] + 1;
     unsigned short *smask = reinterpret_cast<unsigned short *>(s_raw);                       // [16][smax]
@@ -372,8 +337,205 @@ k_step2_win(int blkm, int m, const int *__restrict__ arp, const int *__restrict_
         __syncthreads();
     }
     if (bad) set_flag(flags, FLAG_INTERNAL);
-    const int rows = min(TILE, m - i * TILE);
     __shared__ int s_bin;
+    if (tid == 0) {
+        long long nnz_tr = 0;
+        for (int r = 0; r < TILE; ++r) {
+            if (r < rows) rowcnt[i * TILE + r] = (int)s_rowtot[r];
+            nnz_tr += s_rowtot[r];
+        }
+        int b;
+        long long req = 0;
+        numeric_classify(bp, S, nnz_tr, span, b, req);
+        bin[i] = (unsigned char)b;
+        record_bin(b, req, i, blkm, binstat, binlist);
+        s_bin = b;
+    }
+    __syncthreads();
+    if (s_bin == BIN_ROWS && tid < rows) record_row(bp, S, s_rowtot[tid], span, i * TILE + tid, m, binstat, rowlist);
+}
+
+// ---- tile-rows of sparse A tiles: A's entries one by one -------------------
+//
+// An entry (r, k) of A's tile-row sets, for every entry (k, col) of B's row
+// k, bit 15-(col&15) of row r's mask in C's tile col>>4.  The tile-row's
+// entries are taken in batches of up to EB; work is spread over the CTA's
+// warps in units of 32 consecutive B entries of one A entry (a block scan
+// over the entries' unit counts gives each warp an equal share), so a few
+// long B rows do not hold the other warps at the CTA's barrier.  Tile-rows
+// with more tiles than one window of shared masks are taken in windows;
+// with sorted B rows each entry keeps a cursor into its B row from window
+// to window (when the batch holds the whole tile-row) and a galloping
+// search finds where its segment in the window ends.  Unsorted B rows are
+// tested entry by entry in every window.
+constexpr int EB = 1024;   // A entries per batch
+
+__device__ __forceinline__ int block_excl_scan(int *v, int n, int *s_wsum, int tid, int nt)
+{
+    const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+    __syncthreads();   // v was written under another thread mapping
+    const int per = (n + nt - 1) / nt;
+    const int b = min(n, tid * per), e = min(n, b + per);
+    int loc = 0;
+    for (int j = b; j < e; ++j) loc += v[j];
+    const int incl = warp_incl_scan(loc, lane);
+    if (lane == 31) s_wsum[warp] = incl;
+    __syncthreads();
+    int pre = 0, total = 0;
+    for (int w = 0; w < nw; ++w) {
+        const int x = s_wsum[w];
+        if (w < warp) pre += x;
+        total += x;
+    }
+    int run = pre + incl - loc;
+    for (int j = b; j < e; ++j) { const int x = v[j]; v[j] = run; run += x; }
+    if (tid == 0) v[n] = total;
+    __syncthreads();
+    return total;
+}
+
+// first e in [lo, hi) with col[e] >= key (col sorted on [lo, hi)), probing
+// lo, lo+1, lo+3, lo+7, ... before a binary search of the last gap
+__device__ __forceinline__ int gallop_lower_bound(const int *__restrict__ col, int lo, int hi, int key)
+{
+    int step = 1, a = lo, b = hi;
+    while (true) {
+        const int probe = a + step - 1;
+        if (probe >= hi) break;
+        if (col[probe] >= key) { b = probe; break; }
+        a = probe + 1;
+        step <<= 1;
+    }
+    while (a < b) {
+        const int md = (a + b) >> 1;
+        if (col[md] < key) a = md + 1; else b = md;
+    }
+    return a;
+}
+
+// shared memory of k_step2_entries: masks, tile columns, map, entry state
+__host__ __device__ inline size_t step2e_smem(int slots, int map_cap) {
+    return (size_t)(align16((long long)slots * TILE * 2) + align16((long long)slots * 4) +
+                    align16((long long)map_cap * 2) + 4ll * (4 * EB + 1) + EB);
+}
+
+template <int NT>
+__global__ void __launch_bounds__(NT)
+k_step2_entries(int blkm, int m, const int *__restrict__ arp, const long long *__restrict__ crp,
+                const int *__restrict__ ccol, uint16_t *cmask, int *rowcnt, int smin, int smax, int wslots, int map_cap,
+                NumericBinParams bp, unsigned char *bin, long long *binstat, int *binlist, int *rowlist, int *flags,
+                const int *__restrict__ rows_list, const long long *__restrict__ erpB, const int *__restrict__ ecolB,
+                const long long *__restrict__ erpA, const int *__restrict__ ecolA, int b_sorted)
+{
+    constexpr int NW = NT / 32;
+    extern __shared__ __align__(16) unsigned char s_raw[];
+    __shared__ long long s_rowtot[TILE];
+    __shared__ int s_wsum[NW];
+    __shared__ int s_rs[TILE + 1];
+    __shared__ int s_bin;
+    const int i = rows_list[blockIdx.x];
+    if (i >= blkm) return;
+    const long long c0 = crp[i];
+    const int S = (int)(crp[i + 1] - c0);
+    if (S <= smin || S > smax) return;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int span = ccol[c0 + S - 1] - ccol[c0] + 1;
+    if (fused_handles(span, S)) return;     // done by the fused warp kernel
+    const int rows = min(TILE, m - i * TILE);
+    if (!entry_walk(erpA, arp, i, rows)) return;   // dense A tiles: the tile kernels
+    const int SW = min(S, wslots);
+    unsigned short *smask = reinterpret_cast<unsigned short *>(s_raw);                      // [16][SW]
+    int *wcol = reinterpret_cast<int *>(s_raw + align16((long long)SW * TILE * 2));         // [SW]
+    unsigned short *map = reinterpret_cast<unsigned short *>(reinterpret_cast<unsigned char *>(wcol) +
+                                                             align16((long long)SW * 4));   // [map_cap]
+    int *e_cur = reinterpret_cast<int *>(reinterpret_cast<unsigned char *>(map) + align16((long long)map_cap * 2));
+    int *e_end = e_cur + EB, *e_wend = e_end + EB, *e_pre = e_wend + EB;                     // e_pre: EB + 1
+    unsigned char *e_row = reinterpret_cast<unsigned char *>(e_pre + EB + 1);
+    if (tid <= TILE) s_rs[tid] = (int)erpA[(long long)i * TILE + min(tid, rows)];
+    if (tid < TILE) s_rowtot[tid] = 0;
+    __syncthreads();
+    const int p0 = s_rs[0], p1 = s_rs[TILE];
+    const bool keep = p1 - p0 <= EB && b_sorted;   // cursors carried from window to window
+    bool bad = false;
+    for (int s0 = 0; s0 < S; s0 += SW) {
+        const int nsl = min(SW, S - s0);
+        {
+            unsigned *z = reinterpret_cast<unsigned *>(smask);
+            for (int t = tid; t < (nsl * TILE + 1) / 2; t += NT) z[t] = 0u;
+            for (int t = tid; t < nsl; t += NT) wcol[t] = ccol[c0 + s0 + t];
+        }
+        __syncthreads();
+        const int jlo = wcol[0], jhi = wcol[nsl - 1];
+        const int wspan = jhi - jlo + 1;
+        const bool use_map = wspan <= map_cap;
+        if (use_map) {
+            for (int t = tid; t < wspan; t += NT) map[t] = 0xffffu;
+            __syncthreads();
+            for (int t = tid; t < nsl; t += NT) map[wcol[t] - jlo] = (unsigned short)t;
+        }
+        const int cfirst = jlo * TILE, climit = (jhi + 1) * TILE;
+        const bool last = s0 + SW >= S;
+        for (int pb0 = p0; pb0 < p1; pb0 += EB) {
+            const int nb = min(EB, p1 - pb0);
+            for (int t = tid; t < nb; t += NT) {
+                const int p = pb0 + t;
+                int cur, end;
+                if (keep && s0 > 0) {
+                    cur = e_wend[t];
+                    end = e_end[t];
+                } else {
+                    const int k = ecolA[p];
+                    cur = (int)erpB[k];
+                    end = (int)erpB[k + 1];
+                    if (s0 > 0 && b_sorted) cur = gallop_lower_bound(ecolB, cur, end, cfirst);
+                    int r = 0;
+                    while (s_rs[r + 1] <= p) ++r;
+                    e_row[t] = (unsigned char)r;
+                }
+                const int wend = (b_sorted && !last) ? gallop_lower_bound(ecolB, cur, end, climit) : end;
+                e_cur[t] = cur;
+                e_end[t] = end;
+                e_wend[t] = wend;
+                e_pre[t] = (wend - cur + 31) >> 5;
+            }
+            // (the scan's first barrier also orders the map and state writes above)
+            const int U = block_excl_scan(e_pre, nb, s_wsum, tid, NT);
+            const int u0 = (int)((long long)U * warp / NW), u1 = (int)((long long)U * (warp + 1) / NW);
+            if (u0 < u1) {
+                int lo = 0, hi = nb - 1;   // last entry whose units start at or before u0
+                while (lo < hi) { const int md = (lo + hi + 1) >> 1; if (e_pre[md] <= u0) lo = md; else hi = md - 1; }
+                int t = lo;
+                for (int u = u0; u < u1; ++u) {
+                    while (e_pre[t + 1] <= u) ++t;
+                    const int e = e_cur[t] + ((u - e_pre[t]) << 5) + lane;
+                    if (e < e_wend[t]) {
+                        const int col = ecolB[e];
+                        if (col >= cfirst && col < climit) {
+                            const int sl = c_slot(col >> 4, jlo, wspan, use_map ? map : nullptr, wcol, nsl);
+                            if (sl < 0) bad = true;
+                            else smask_or(smask, (int)e_row[t] * nsl + sl, 0x8000u >> (col & 15));
+                        } else if (b_sorted) {
+                            bad = true;   // a sorted segment lies inside its window
+                        }
+                    }
+                }
+            }
+            __syncthreads();
+        }
+        // the window's masks out (row-major within the tile-row) and row counts
+        for (int r = warp; r < TILE; r += NW) {
+            int c = 0;
+            for (int sl = lane; sl < nsl; sl += 32) {
+                const unsigned short v = smask[r * nsl + sl];
+                cmask[c0 * TILE + (long long)r * S + s0 + sl] = v;
+                c += __popc((unsigned)v);
+            }
+            c = warp_sum_int(c);
+            if (lane == 0) s_rowtot[r] += c;
+        }
+        __syncthreads();
+    }
+    if (bad) set_flag(flags, FLAG_INTERNAL);
     if (tid == 0) {
         long long nnz_tr = 0;
         for (int r = 0; r < TILE; ++r) {
@@ -415,6 +577,12 @@ cudaError_t symbolic_init_attributes()
     cudaError_t e = step2_attr(k_step2<256>);
     if (e == cudaSuccess) e = step2_attr(k_step2<512>);
     if (e == cudaSuccess) e = step2_attr(k_step2_win<512>);
+    for (const void *f : {(const void *)k_step2_entries<256>, (const void *)k_step2_entries<512>}) {
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)step2e_smem(S2_SMAX, MAP_MAX));
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
+    }
     return e;
 }
 
@@ -427,7 +595,7 @@ cudaError_t step2_masks(Pool &pool, const TileCSR &A, const TileCSR &B, int m, i
                         const int *ccol, uint16_t *cmask, int *rowcnt, int max_tiles_per_row, int max_span,
                         const NumericBinParams &bp, unsigned char *bin, long long *binstat, int *binlist,
                         int *rowlist, int *flags, const int *defer_list, int ndefer, const long long *erpB,
-                        const int *ecolB, const long long *erpA, const int *ecolA)
+                        const int *ecolB, const long long *erpA, const int *ecolA, bool b_sorted)
 {
     cudaStream_t s = pool.stream;
     if (blkm <= 0 || ndefer <= 0) return cudaSuccess;
@@ -436,18 +604,26 @@ cudaError_t step2_masks(Pool &pool, const TileCSR &A, const TileCSR &B, int m, i
         const int slots = max_tiles_per_row < S2_SMALL ? max_tiles_per_row : S2_SMALL;
         { k_step2<256><<<ndefer, 256, step2_smem(slots, map_cap), s>>>(blkm, m, A.trp, A.tcol, A.mask, B.trp, B.tcol, B.mask, crp, ccol,
                                                    cmask, rowcnt, 0, S2_SMALL, map_cap, bp, bin, binstat, binlist, rowlist, flags, defer_list,
-                                                   erpB, ecolB, erpA, ecolA); ::tsg::count_launch(); }
+                                                   erpB, ecolB, erpA); ::tsg::count_launch(); }
+        { k_step2_entries<256><<<ndefer, 256, step2e_smem(slots, map_cap), s>>>(blkm, m, A.trp, crp, ccol, cmask, rowcnt, 0, S2_SMALL,
+                                                   S2_SMALL, map_cap, bp, bin, binstat, binlist, rowlist, flags, defer_list,
+                                                   erpB, ecolB, erpA, ecolA, b_sorted ? 1 : 0); ::tsg::count_launch(); }
     }
     if (max_tiles_per_row > S2_SMALL) {
         const int slots = max_tiles_per_row < S2_SMAX ? max_tiles_per_row : S2_SMAX;
         { k_step2<512><<<ndefer, 512, step2_smem(slots, map_cap), s>>>(blkm, m, A.trp, A.tcol, A.mask, B.trp, B.tcol, B.mask, crp, ccol,
                                                    cmask, rowcnt, S2_SMALL, S2_SMAX, map_cap, bp, bin, binstat, binlist, rowlist, flags, defer_list,
-                                                   erpB, ecolB, erpA, ecolA); ::tsg::count_launch(); }
+                                                   erpB, ecolB, erpA); ::tsg::count_launch(); }
+        const int wslots = max_tiles_per_row < S2_SMAX ? max_tiles_per_row : S2_SMAX;
+        const int wmap = max_tiles_per_row > S2_SMAX ? (int)MAP_MAX : map_cap;
+        { k_step2_entries<512><<<ndefer, 512, step2e_smem(wslots, wmap), s>>>(blkm, m, A.trp, crp, ccol, cmask, rowcnt, S2_SMALL, INT_MAX,
+                                                   S2_SMAX, wmap, bp, bin, binstat, binlist, rowlist, flags, defer_list,
+                                                   erpB, ecolB, erpA, ecolA, b_sorted ? 1 : 0); ::tsg::count_launch(); }
     }
     if (max_tiles_per_row > S2_SMAX) {
         { k_step2_win<512><<<ndefer, 512, step2_smem(S2_SMAX, MAP_MAX), s>>>(blkm, m, A.trp, A.tcol, A.mask, B.trp, B.tcol, B.mask, crp, ccol,
                                                       cmask, rowcnt, S2_SMAX, bp, bin, binstat, binlist, rowlist, flags, defer_list,
-                                                      erpB, ecolB); ::tsg::count_launch(); }
+                                                      erpB, ecolB, erpA); ::tsg::count_launch(); }
     }
     return cudaGetLastError();
 }
