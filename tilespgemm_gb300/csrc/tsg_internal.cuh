@@ -77,6 +77,25 @@ __device__ __forceinline__ void atomic_or_mask16(uint16_t *mask, long long idx, 
     atomicOr(w, bits << ((idx & 1) * 16));
 }
 
+// first e in [lo, hi) with col[e] >= key (col sorted on [lo, hi)), probing
+// lo, lo+1, lo+3, lo+7, ... before a binary search of the last gap
+__device__ __forceinline__ int gallop_lower_bound(const int *__restrict__ col, int lo, int hi, int key)
+{
+    int step = 1, a = lo, b = hi;
+    while (true) {
+        const int probe = a + step - 1;
+        if (probe >= hi) break;
+        if (col[probe] >= key) { b = probe; break; }
+        a = probe + 1;
+        step <<= 1;
+    }
+    while (a < b) {
+        const int md = (a + b) >> 1;
+        if (col[md] < key) a = md + 1; else b = md;
+    }
+    return a;
+}
+
 // First index in [lo, hi) whose value is >= key (hi if none), by a 32-way
 // search of the warp: each round every lane probes one point.
 __device__ __forceinline__ int warp_lower_bound(const int *__restrict__ a, int lo, int hi, int key, int lane)

@@ -394,25 +394,6 @@ __device__ __forceinline__ int block_excl_scan(int *v, int n, int *s_wsum, int t
     return total;
 }
 
-// first e in [lo, hi) with col[e] >= key (col sorted on [lo, hi)), probing
-// lo, lo+1, lo+3, lo+7, ... before a binary search of the last gap
-__device__ __forceinline__ int gallop_lower_bound(const int *__restrict__ col, int lo, int hi, int key)
-{
-    int step = 1, a = lo, b = hi;
-    while (true) {
-        const int probe = a + step - 1;
-        if (probe >= hi) break;
-        if (col[probe] >= key) { b = probe; break; }
-        a = probe + 1;
-        step <<= 1;
-    }
-    while (a < b) {
-        const int md = (a + b) >> 1;
-        if (col[md] < key) a = md + 1; else b = md;
-    }
-    return a;
-}
-
 // shared memory of k_step2_entries: masks, tile columns, map, entry state
 __host__ __device__ inline size_t step2e_smem(int slots, int map_cap) {
     return (size_t)(align16((long long)slots * TILE * 2) + align16((long long)slots * 4) +
