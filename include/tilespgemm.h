@@ -312,6 +312,10 @@ tsg_status tsg_server_submit(tsg_server *server, tsg_op op, const tsg_csr *A, co
                              int64_t *request_id);
 /* Blocks until the request is done; C receives the result. */
 tsg_status tsg_server_wait(tsg_server *server, int64_t request_id, tsg_csr *C, tsg_server_result *info);
+/* Any completed request, in completion order (its id in *request_id): a
+ * collector that frees results as they finish holds at most the requests in
+ * flight.  TSG_ERR_INVALID_ARG when no request is outstanding. */
+tsg_status tsg_server_wait_any(tsg_server *server, int64_t *request_id, tsg_csr *C, tsg_server_result *info);
 tsg_status tsg_server_destroy(tsg_server *server);
 
 /* ---- tile form (the reference's device format) --------------------------- */

@@ -85,3 +85,44 @@ def test_budget_refuses_oversized(built_lib):
         with pytest.raises(TSGError) as e:
             srv.submit(A, op="AA")
         assert e.value.status == 10
+
+
+def test_wait_any_returns_every_request_once(built_lib):
+    """Completion-order collection gives each submitted request exactly once,
+    with the same result as waiting for it by id; with nothing outstanding
+    it reports an invalid argument."""
+    from tilespgemm_gb300 import TSGError
+    from tilespgemm_gb300.serving import Server
+    reqs = _req_set()
+    with Server(workers=3, max_batch=8, budget_gb=4) as srv:
+        alone = [srv.wait(srv.submit(A, op=op, key=key))[0] for A, op, key in reqs]
+        ids = [srv.submit(A, op=op, key=key) for A, op, key in reqs]
+        got = {}
+        for _ in ids:
+            rid, C, info = srv.wait_any()
+            assert rid not in got
+            got[rid] = C
+        with pytest.raises(TSGError) as e:
+            srv.wait_any()
+        assert e.value.status == 1
+    assert sorted(got) == sorted(ids)
+    for rid, Ca in zip(ids, alone):
+        Cm = got[rid]
+        assert np.array_equal(Ca.rowptr, Cm.rowptr) and np.array_equal(Ca.col, Cm.col)
+        assert np.array_equal(Ca.val, Cm.val)
+
+
+def test_run_stream_collects_in_completion_order(built_lib):
+    from tilespgemm_gb300.serving import Server, make_stream, run_stream
+    reqs = make_stream(12, seed=3, rate=500.0, lap_side=(16, 48), rmat_scale=(8, 10))
+    with Server(workers=2, budget_gb=4) as srv:
+        st = run_stream(srv, reqs, realtime=True, download=True)
+    assert st["completed"] + st["refused"] == 12 and st["refused"] == 0
+    for r, res in zip(reqs, st["results"]):
+        C, info = res
+        A = r["A"]
+        from tilespgemm_gb300.api import CSR
+        B = A if r["op"] == "AA" else CSR(A.n, A.m, *O.transpose(A))
+        rp, col, val = O.spgemm(A, B)
+        assert np.array_equal(C.col, col) and np.array_equal(C.val, val)
+        assert info["latency_ms"] >= 0.0

@@ -132,6 +132,8 @@ SIGNATURES = {
     "tsg_server_submit": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(tsg_csr), C.POINTER(tsg_csr), C.c_uint64,
                                     C.POINTER(C.c_int64)]),
     "tsg_server_wait": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(tsg_csr), C.POINTER(tsg_server_result)]),
+    "tsg_server_wait_any": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(tsg_csr),
+                                      C.POINTER(tsg_server_result)]),
     "tsg_server_destroy": (C.c_int, [C.c_void_p]),
     "tsg_csr_to_tiles": (C.c_int, [C.c_void_p, C.POINTER(tsg_csr), C.POINTER(tsg_tiles)]),
     "tsg_spgemm_tiles": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(tsg_csr), C.POINTER(tsg_csr),

@@ -108,6 +108,7 @@ struct tsg_ctx {
     long long *hstat = nullptr;      // pinned mirror: 64 stat slots + FLAG_COUNT flags (as long long)
     std::mutex mu;
     std::multimap<size_t, void *> pinned_cache;
+    size_t pinned_cached = 0;        // bytes held by pinned_cache
     cudaEvent_t ev[8] = {};
 };
 
@@ -140,6 +141,7 @@ void *pinned_get(tsg_ctx *ctx, size_t bytes)
         auto it = ctx->pinned_cache.lower_bound(bytes);
         if (it != ctx->pinned_cache.end() && it->first <= bytes + bytes / 4 + (1 << 20)) {
             void *p = it->second;
+            ctx->pinned_cached -= it->first;
             ctx->pinned_cache.erase(it);
             return p;
         }
@@ -149,10 +151,27 @@ void *pinned_get(tsg_ctx *ctx, size_t bytes)
     return p;
 }
 
+// Pinned buffers a context keeps for reuse, at most this many bytes: beyond
+// it the largest cached buffers are freed (outputs of very different sizes
+// would otherwise pile up in host memory).
+constexpr size_t PINNED_CACHE_MAX = 4ull << 30;
+
 void pinned_put(tsg_ctx *ctx, void *p, size_t bytes)
 {
-    std::lock_guard<std::mutex> lk(ctx->mu);
-    ctx->pinned_cache.emplace(bytes == 0 ? 16 : bytes, p);
+    if (bytes == 0) bytes = 16;
+    std::vector<void *> drop;
+    {
+        std::lock_guard<std::mutex> lk(ctx->mu);
+        ctx->pinned_cache.emplace(bytes, p);
+        ctx->pinned_cached += bytes;
+        while (ctx->pinned_cached > PINNED_CACHE_MAX && !ctx->pinned_cache.empty()) {
+            auto last = std::prev(ctx->pinned_cache.end());
+            ctx->pinned_cached -= last->first;
+            drop.push_back(last->second);
+            ctx->pinned_cache.erase(last);
+        }
+    }
+    for (void *q : drop) cudaFreeHost(q);
 }
 
 // device-side view of a CSR operand (after upload and preparation)
@@ -706,6 +725,7 @@ tsg_status tsg_destroy(tsg_ctx *c)
     if (c->stream) cudaStreamSynchronize(c->stream);
     for (auto &kv : c->pinned_cache) cudaFreeHost(kv.second);
     c->pinned_cache.clear();
+    c->pinned_cached = 0;
     for (auto &e : c->ev) if (e) cudaEventDestroy(e);
     if (c->dflags) cudaFree(c->dflags);
     if (c->dstat) cudaFree(c->dstat);

@@ -140,6 +140,7 @@ struct tsg_server {
     std::condition_variable cv_work, cv_done;
     std::deque<Request *> pending;
     std::unordered_map<int64_t, Request *> reqs;
+    std::deque<int64_t> finished;      // completed request ids, in completion order
     int64_t inflight_bytes = 0;
     int64_t next_id = 1;
     int rr = 0;
@@ -275,6 +276,7 @@ void worker_main(tsg_server *s, int w)
                 r->t_done = t1;
                 r->done = true;
                 s->inflight_bytes -= r->est_bytes;
+                s->finished.push_back(r->id);
             }
             admit(s);
         }
@@ -353,18 +355,13 @@ tsg_status tsg_server_submit(tsg_server *s, tsg_op op, const tsg_csr *A, const t
     return TSG_OK;
 }
 
-tsg_status tsg_server_wait(tsg_server *s, int64_t request_id, tsg_csr *C, tsg_server_result *info)
+}  // extern "C"
+
+namespace {
+
+// hand a completed request (already removed from s->reqs) to the caller
+tsg_status finish_wait(Request *r, tsg_csr *C, tsg_server_result *info)
 {
-    if (!s || !C) { tsg::set_last_error("server/C is NULL"); return TSG_ERR_INVALID_ARG; }
-    Request *r = nullptr;
-    {
-        std::unique_lock<std::mutex> lk(s->mu);
-        auto it = s->reqs.find(request_id);
-        if (it == s->reqs.end()) { tsg::set_last_error("unknown request id"); return TSG_ERR_INVALID_ARG; }
-        r = it->second;
-        s->cv_done.wait(lk, [&] { return r->done; });
-        s->reqs.erase(it);
-    }
     const tsg_status st = r->status;
     if (info) {
         info->latency_ms = std::chrono::duration<double, std::milli>(r->t_done - r->t_submit).count();
@@ -378,6 +375,48 @@ tsg_status tsg_server_wait(tsg_server *s, int64_t request_id, tsg_csr *C, tsg_se
     else tsg::set_last_error(r->err.c_str());
     delete r;
     return st;
+}
+
+}  // namespace
+
+extern "C" {
+
+tsg_status tsg_server_wait(tsg_server *s, int64_t request_id, tsg_csr *C, tsg_server_result *info)
+{
+    if (!s || !C) { tsg::set_last_error("server/C is NULL"); return TSG_ERR_INVALID_ARG; }
+    Request *r = nullptr;
+    {
+        std::unique_lock<std::mutex> lk(s->mu);
+        auto it = s->reqs.find(request_id);
+        if (it == s->reqs.end()) { tsg::set_last_error("unknown request id"); return TSG_ERR_INVALID_ARG; }
+        r = it->second;
+        s->cv_done.wait(lk, [&] { return r->done; });
+        s->reqs.erase(it);
+    }
+    return finish_wait(r, C, info);
+}
+
+tsg_status tsg_server_wait_any(tsg_server *s, int64_t *request_id, tsg_csr *C, tsg_server_result *info)
+{
+    if (!s || !C || !request_id) { tsg::set_last_error("server/C/request_id is NULL"); return TSG_ERR_INVALID_ARG; }
+    Request *r = nullptr;
+    {
+        std::unique_lock<std::mutex> lk(s->mu);
+        for (;;) {
+            // ids already returned by tsg_server_wait are skipped
+            while (!s->finished.empty() && !s->reqs.count(s->finished.front())) s->finished.pop_front();
+            if (!s->finished.empty()) break;
+            if (s->reqs.empty()) { tsg::set_last_error("no outstanding requests"); return TSG_ERR_INVALID_ARG; }
+            s->cv_done.wait(lk);
+        }
+        const int64_t id = s->finished.front();
+        s->finished.pop_front();
+        auto it = s->reqs.find(id);
+        r = it->second;
+        s->reqs.erase(it);
+        *request_id = id;
+    }
+    return finish_wait(r, C, info);
 }
 
 tsg_status tsg_server_destroy(tsg_server *s)

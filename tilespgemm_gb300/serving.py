@@ -67,6 +67,22 @@ class Server:
         lib().tsg_csr_free(None, C.byref(c))
         return res, d
 
+    def wait_any(self, download: bool = True) -> tuple[int, CSR | None, dict]:
+        """The next request to complete (completion order): its id, result
+        (None with download=False) and timing record."""
+        c = _abi.tsg_csr()
+        info = _abi.tsg_server_result()
+        rid = C.c_int64()
+        st = lib().tsg_server_wait_any(self.handle, C.byref(rid), C.byref(c), C.byref(info))
+        check(st)
+        with self._lock:
+            self._keep.pop(rid.value, None)
+        d = info.as_dict()
+        d["nnz"] = int(c.nnz)
+        res = _download(None, c) if download else None
+        lib().tsg_csr_free(None, C.byref(c))
+        return rid.value, res, d
+
     def close(self) -> None:
         if self.handle:
             lib().tsg_server_destroy(self.handle)
@@ -138,16 +154,26 @@ def run_stream(srv: Server, reqs: list, realtime: bool = True, download: bool = 
     ids = [None] * len(reqs)
     results = [None] * len(reqs)
     errors: list = []
+    where: dict[int, int] = {}       # request id -> stream index, filled by the submitter
+    state = {"submitted": 0, "done": False}
     t0 = time.perf_counter()
 
     def collector():
+        # results are taken in completion order and released at once, so
+        # host memory holds only the requests in flight
         try:
-            for i in range(len(reqs)):
-                while ids[i] is None:
-                    time.sleep(0.0001)
-                if ids[i] < 0:
-                    continue
-                results[i] = srv.wait(ids[i], download=download)
+            got = 0
+            while True:
+                if got < state["submitted"]:
+                    rid, res, d = srv.wait_any(download=download)
+                    while rid not in where:          # its submit call is still returning
+                        time.sleep(0.0001)
+                    results[where[rid]] = (res, d)
+                    got += 1
+                elif state["done"]:
+                    break
+                else:
+                    time.sleep(0.0002)
         except BaseException as e:   # surfaced after join
             errors.append(e)
 
@@ -160,7 +186,10 @@ def run_stream(srv: Server, reqs: list, realtime: bool = True, download: bool = 
                 if dt > 0:
                     time.sleep(dt)
             try:
-                ids[i] = srv.submit(r["A"], op=r["op"], key=r["key"])
+                rid = srv.submit(r["A"], op=r["op"], key=r["key"])
+                ids[i] = rid
+                where[rid] = i
+                state["submitted"] += 1
             except TSGError as e:
                 if e.status != _abi.ERR_BUDGET:
                     raise
@@ -169,6 +198,7 @@ def run_stream(srv: Server, reqs: list, realtime: bool = True, download: bool = 
         for i in range(len(ids)):
             if ids[i] is None:
                 ids[i] = -1
+        state["done"] = True
         th.join()
     if errors:
         raise errors[0]
