@@ -627,8 +627,128 @@ k_global_prep(NumericArgs g, int cls, long long nrows)
     }
 }
 
-constexpr int WIDE_W = 1024;   // tile columns per window of the wide-row kernel
-constexpr size_t WIDE_SMEM = (size_t)ROW_WARPS * WIDE_W * (4 + 2);
+constexpr int WIDE_W = 1024;   // tile columns per window of the wide-row kernel (accumulator in C)
+constexpr int WIDE_WARP_BYTES = WIDE_W * (4 + 2);   // shared memory per warp
+constexpr size_t WIDE_SMEM = (size_t)ROW_WARPS * WIDE_WARP_BYTES;
+// windows with the accumulator in shared memory: tile columns and entries
+constexpr int WS_W = 512, WS_E = 512;
+static_assert(4 * WS_W + 8 * WS_E <= WIDE_WARP_BYTES, "shared-memory windows fit the warp's share");
+
+// A wide row's share [t0, t1) of tile columns, for A rows of up to 32
+// entries and sorted B rows: windows of at most WS_W tile columns and WS_E
+// entries, each with its mask/offset table and its values in the warp's
+// shared memory, written out to C in one coalesced pass.  Lane q keeps A
+// entry q and a cursor into its B row: one binary search for the share's
+// first column, then each window takes the B entries from the cursor on
+// while their columns stay below the window's end (one ballot per 32), so
+// no window searches the B rows.  A entries follow one another in order
+// (with a warp barrier between them), so per output the products come in
+// A's row order, then B's.  (Longer A rows keep the accumulator in C: with
+// small windows their B rows would be searched again for every window.)
+__device__ __noinline__ void wide_windows_smem(const NumericArgs &g, int R, int lane, unsigned char *wbase,
+                                               const uint16_t *mrow, const int *tcol, int S, long long Rb, int nnz_r,
+                                               int cshift, int t0, int t1, int pa0, int na)
+{
+    unsigned short *w_msk = reinterpret_cast<unsigned short *>(wbase);
+    unsigned short *w_off = w_msk + WS_W;
+    double *w_acc = reinterpret_cast<double *>(wbase + 4 * WS_W);
+    for (int t = lane; t < WS_W; t += 32) w_msk[t] = 0;
+    int cur = 0, bend = 0;
+    double av = 0.0;
+    if (lane < na) {
+        const int k = g.colA[pa0 + lane];
+        av = g.valA[pa0 + lane];
+        cur = (int)g.rpB[k];
+        bend = (int)g.rpB[k + 1];
+        const int key = t0 * TILE;
+        int h = bend;
+        while (cur < h) { const int md = (cur + h) >> 1; if (g.colB[md] < key) cur = md + 1; else h = md; }
+    }
+    __syncwarp();
+    bool bad = false;
+    int sa = warp_lower_bound(tcol, 0, S, t0, lane);
+    // C offset of the share's first entry; each window then starts where the last ended
+    long long wg = sa < S ? Rb + warp_lower_bound(g.colC + Rb, 0, nnz_r, tcol[sa] * TILE - cshift, lane) : Rb;
+    while (sa < S && tcol[sa] < t1) {
+        const int j0 = tcol[sa];
+        const int jlim = (int)min((long long)t1, (long long)j0 + WS_W);
+        // the window: slots from sa while the tile column is below jlim and
+        // the entries fit; tile columns and masks loaded 128 slots at a time
+        int nwin = 0, s = sa;
+        bool more = true;
+        while (more) {
+            int tcv[4];
+            unsigned mkv[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int ss = s + 32 * u + lane;
+                tcv[u] = ss < S ? tcol[ss] : INT_MAX;
+                mkv[u] = ss < S ? (unsigned)mrow[ss] : 0u;
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                if (more) {
+                    const bool inr = tcv[u] < jlim;
+                    const int c = inr ? __popc(mkv[u]) : 0;
+                    const int incl = warp_incl_scan(c, lane);
+                    const bool ok = inr && nwin + incl <= WS_E;
+                    const int nok = __popc(__ballot_sync(0xffffffffu, ok));
+                    if (ok && mkv[u]) {
+                        w_msk[tcv[u] - j0] = (unsigned short)mkv[u];
+                        w_off[tcv[u] - j0] = (unsigned short)(nwin + incl - c);
+                    }
+                    if (nok > 0) nwin += __shfl_sync(0xffffffffu, incl, nok - 1);
+                    s += nok;
+                    if (nok < 32) more = false;
+                }
+            }
+        }
+        const int sb = s;
+        // B columns from the next slot's tile column on belong to later windows
+        const int tnext = sb < S ? tcol[sb] : INT_MAX;
+        const int hi = (tnext < t1) ? tnext * TILE : (t1 == INT_MAX ? INT_MAX : t1 * TILE);
+        for (int t = lane; t < nwin; t += 32) w_acc[t] = 0.0;
+        __syncwarp();
+        // the B entries of one A entry from position c0 on, below hi
+        auto segment = [&](int c0, int bq, double a) -> int {
+            for (;;) {
+                const int e = c0 + lane;
+                int col = INT_MAX;
+                double b = 0.0;
+                if (e < bq) { col = g.colB[e]; b = g.valB[e]; }
+                const bool in = col < hi;
+                if (in) {
+                    const int t = (col >> 4) - j0, cc = col & 15;
+                    const unsigned mk = (unsigned)t < (unsigned)WS_W ? w_msk[t] : 0u;
+                    if ((mk >> (TILE - 1 - cc)) & 1u) {
+                        const int p = w_off[t] + __popc(mk >> (TILE - cc));
+                        w_acc[p] = fma(a, b, w_acc[p]);
+                    } else {
+                        bad = true;
+                    }
+                }
+                const int n = __popc(__ballot_sync(0xffffffffu, in));
+                c0 += n;
+                if (n < 32) return c0;
+            }
+        };
+        for (int q = 0; q < na; ++q) {
+            const int c1 = segment(__shfl_sync(0xffffffffu, cur, q), __shfl_sync(0xffffffffu, bend, q),
+                                   __shfl_sync(0xffffffffu, av, q));
+            if (lane == q) cur = c1;
+            __syncwarp();
+        }
+        for (int t = lane; t < nwin; t += 32) g.valC[wg + t] = w_acc[t];
+        wg += nwin;
+        for (int ss = sa + lane; ss < sb; ss += 32) {
+            const int tc = tcol[ss];
+            if (tc - j0 < WS_W) w_msk[tc - j0] = 0;
+        }
+        __syncwarp();
+        sa = sb;
+    }
+    if (bad) set_flag(g.flags, FLAG_INTERNAL);
+}
 
 // One CTA of ROW_WARPS warps per wide row; the values accumulate in place in
 // C (columns written by k_global_prep, values zeroed per window here).  The row's entries are
@@ -645,8 +765,9 @@ k_numeric_wide(NumericArgs g, int cls, long long nrows, bool packed)
 {
     extern __shared__ __align__(16) unsigned char s_raw[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    unsigned *s_off = reinterpret_cast<unsigned *>(s_raw) + warp * WIDE_W;
-    unsigned short *s_msk = reinterpret_cast<unsigned short *>(s_raw + (size_t)ROW_WARPS * WIDE_W * 4) + warp * WIDE_W;
+    unsigned char *wbase = s_raw + (size_t)warp * WIDE_WARP_BYTES;   // this warp's shared memory
+    unsigned *s_off = reinterpret_cast<unsigned *>(wbase);
+    unsigned short *s_msk = reinterpret_cast<unsigned short *>(wbase + (size_t)WIDE_W * 4);
     // WPR warps per row: ROW_WARPS (one row per CTA, the warps split its
     // entries) or 1 (ROW_WARPS rows per CTA, one warp each)
     const long long idx = WPR == 1 ? (long long)blockIdx.x * ROW_WARPS + warp : (long long)blockIdx.x;
@@ -667,6 +788,13 @@ k_numeric_wide(NumericArgs g, int cls, long long nrows, bool packed)
     const int t0 = (g.colC[Rb + e0] + cshift) >> 4;
     const int t1 = e1 < nnz_r ? (g.colC[Rb + e1] + cshift) >> 4 : INT_MAX;
     if (t0 >= t1) return;   // the range starts inside the previous warp's last tile column
+    {
+        const int pa0 = (int)g.rpA[R], pa1 = (int)g.rpA[R + 1];
+        if (!packed && g.b_sorted && pa1 - pa0 <= 32) {
+            wide_windows_smem(g, R, lane, wbase, mrow, tcol, S, Rb, nnz_r, cshift, t0, t1, pa0, pa1 - pa0);
+            return;
+        }
+    }
     for (int t = lane; t < WIDE_W; t += 32) s_msk[t] = 0;
     __syncwarp();
     int sa = warp_lower_bound(tcol, 0, S, t0, lane);
