@@ -181,6 +181,23 @@ def test_long_rows(opts, built_lib):
             check_against_oracle(C, X, X)
 
 
+@pytest.mark.parametrize("opts", [dict(smem_acc_max=0, row_acc_max=0), dict()])
+def test_hub_rows_in_parts(opts, built_lib):
+    """A rows of ~590 entries times B spread over 300,000 columns: with every
+    row sent to the wide class (smem_acc_max=0, row_acc_max=0) the rows of
+    long A rows are cut into parts walked anywhere on the GPU from a table
+    of B-row cut points; bit-exact against the oracle either way."""
+    from tilespgemm_gb300 import Context
+    from tilespgemm_gb300 import matrices as M
+    A = M.random_sparse(48, 2000, 700, seed=41)
+    B = M.random_sparse(2000, 300000, 20, seed=42)
+    assert int(np.diff(np.asarray(A.rowptr)).min()) > 512
+    with Context(0, **opts) as c:
+        C, st = c.spgemm(A, B, op="AB", stats=True)
+        assert st["bins"][3] > 0
+        check_against_oracle(C, A, B)
+
+
 def _runs_matrix(m, n, runs, seed):
     """Row k holds the column runs given by runs(k) -> list of (start, length),
     values uniform in [-1, 1]."""

@@ -522,6 +522,7 @@ tsg_status plan_numeric(tsg_ctx *ctx, Pool &pool, PlanData &P, const double *val
     na.crp = P.crp; na.ccol = P.ccol; na.cmask = P.cmask;
     na.rowptrC = P.rowptrC; na.colC = col; na.valC = val;
     na.bin = P.bin; na.binlist = P.binlist; na.rowlist = P.rowlist; na.b_sorted = P.b_increasing; na.tr_coloff = tr_coloff; na.flags = ctx->dflags;
+    na.nnzA = P.nnzA; na.n = P.n;
     if (walk < 0) walk = ctx->opts.numeric_walk;
     if (threads <= 0) threads = ctx->opts.threads_numeric;
     // repeated B columns need the packed walk.  Auto otherwise loads B one

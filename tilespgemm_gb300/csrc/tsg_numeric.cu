@@ -195,36 +195,15 @@ __device__ __forceinline__ void row_walk_packed(const NumericArgs &g, int R, int
     if (bad) set_flag(g.flags, FLAG_INTERNAL);
 }
 
-// One warp applies row R's products whose column lies in [lo, hi), in A's
-// row order then B's (lanes over one B row; B rows without repeated
-// columns).  A's entries are taken 32 at a time, one per lane: with sorted
-// B rows each lane first cuts its B row to [lo, hi) by two binary searches
-// (all lanes at once), then the warp walks the (A entry, 32-entry chunk)
-// pairs in order with the next pair's loads issued before the current
-// pair's updates.  Without sorted B rows every entry is tested instead.
+// The (A entry, 32-entry chunk) pairs of up to 32 A entries, lane q holding
+// entry q's value av and B segment [bs, be): walked in order, the next
+// pair's B loads issued before the current pair's update; only columns in
+// [lo, hi) are applied.
 template <class Acc, class PosFn>
-__device__ __forceinline__ void row_walk_range(const NumericArgs &g, int R, int lane, int lo, int hi, Acc *acc,
-                                               PosFn pos_of)
+__device__ __forceinline__ void walk_segments(const NumericArgs &g, int lane, int na, double av, int bs, int be,
+                                              int lo, int hi, Acc *acc, PosFn pos_of, bool &bad)
 {
-    const int pa0 = (int)g.rpA[R], pa1 = (int)g.rpA[R + 1];
-    bool bad = false;
-    for (int pb = pa0; pb < pa1; pb += 32) {
-        const int na = min(32, pa1 - pb);
-        int bs = 0, be = 0;
-        double av = 0.0;
-        if (lane < na) {
-            const int k = g.colA[pb + lane];
-            av = g.valA[pb + lane];
-            bs = (int)g.rpB[k];
-            be = (int)g.rpB[k + 1];
-            if (g.b_sorted) {
-                int l = bs, h = be;
-                while (l < h) { const int md = (l + h) >> 1; if (g.colB[md] < lo) l = md + 1; else h = md; }
-                bs = l; h = be;
-                while (l < h) { const int md = (l + h) >> 1; if (g.colB[md] < hi) l = md + 1; else h = md; }
-                be = l;
-            }
-        }
+    {
         // first non-empty pair
         int q = 0, eb = __shfl_sync(0xffffffffu, bs, 0), ee = __shfl_sync(0xffffffffu, be, 0);
         double a = __shfl_sync(0xffffffffu, av, 0);
@@ -256,6 +235,40 @@ __device__ __forceinline__ void row_walk_range(const NumericArgs &g, int R, int 
             q = nq; eb = neb; ee = nee; a = na_;
             col = ncol; b = nb;
         }
+    }
+}
+
+// One warp applies row R's products whose column lies in [lo, hi), in A's
+// row order then B's (lanes over one B row; B rows without repeated
+// columns).  A's entries are taken 32 at a time, one per lane: with sorted
+// B rows each lane first cuts its B row to [lo, hi) by two binary searches
+// (all lanes at once), then the warp walks the (A entry, 32-entry chunk)
+// pairs in order with the next pair's loads issued before the current
+// pair's updates.  Without sorted B rows every entry is tested instead.
+template <class Acc, class PosFn>
+__device__ __forceinline__ void row_walk_range(const NumericArgs &g, int R, int lane, int lo, int hi, Acc *acc,
+                                               PosFn pos_of)
+{
+    const int pa0 = (int)g.rpA[R], pa1 = (int)g.rpA[R + 1];
+    bool bad = false;
+    for (int pb = pa0; pb < pa1; pb += 32) {
+        const int na = min(32, pa1 - pb);
+        int bs = 0, be = 0;
+        double av = 0.0;
+        if (lane < na) {
+            const int k = g.colA[pb + lane];
+            av = g.valA[pb + lane];
+            bs = (int)g.rpB[k];
+            be = (int)g.rpB[k + 1];
+            if (g.b_sorted) {
+                int l = bs, h = be;
+                while (l < h) { const int md = (l + h) >> 1; if (g.colB[md] < lo) l = md + 1; else h = md; }
+                bs = l; h = be;
+                while (l < h) { const int md = (l + h) >> 1; if (g.colB[md] < hi) l = md + 1; else h = md; }
+                be = l;
+            }
+        }
+        walk_segments(g, lane, na, av, bs, be, lo, hi, acc, pos_of, bad);
     }
     if (bad) set_flag(g.flags, FLAG_INTERNAL);
 }
@@ -632,6 +645,13 @@ constexpr int WIDE_WARP_BYTES = WIDE_W * (4 + 2);   // shared memory per warp
 constexpr size_t WIDE_SMEM = (size_t)ROW_WARPS * WIDE_WARP_BYTES;
 // windows with the accumulator in shared memory: tile columns and entries
 constexpr int WS_W = 512, WS_E = 512;
+// Wide rows with more A entries than LONG_NA are cut into parts of at most
+// WIDE_W tile columns, each part one warp's work anywhere on the GPU
+// (k_long_walk); their B rows' cut points come from a table built once.
+constexpr int LONG_NA = 512;
+constexpr int LONG_MINP = 16;        // parts of such a row at least (more warps than the per-row kernel's 8)
+constexpr int LONG_GRID = 152 * 4;   // CTAs of the part walk: four per SM
+constexpr long long LONG_TAB_MAX = 1ll << 30;   // cut-table entries (4 GB) beyond which long rows stay per row
 static_assert(4 * WS_W + 8 * WS_E <= WIDE_WARP_BYTES, "shared-memory windows fit the warp's share");
 
 // A wide row's share [t0, t1) of tile columns, for A rows of up to 32
@@ -761,7 +781,7 @@ __device__ __noinline__ void wide_windows_smem(const NumericArgs &g, int R, int 
 // the products still come in A's row order.
 template <int WPR>
 __global__ void __launch_bounds__(ROW_WARPS * 32, 4)
-k_numeric_wide(NumericArgs g, int cls, long long nrows, bool packed)
+k_numeric_wide(NumericArgs g, int cls, long long nrows, bool packed, const unsigned char *handled)
 {
     extern __shared__ __align__(16) unsigned char s_raw[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -774,6 +794,7 @@ k_numeric_wide(NumericArgs g, int cls, long long nrows, bool packed)
     if (idx >= nrows) return;
     const int part = WPR == 1 ? 0 : warp;
     const int R = g.rowlist[(long long)cls * g.m + idx];
+    if (handled && handled[idx]) return;   // k_long_walk's row
     const int i = R >> 4, r = R & (TILE - 1);
     const long long c0 = g.crp[i];
     const int S = (int)(g.crp[i + 1] - c0);
@@ -838,6 +859,205 @@ k_numeric_wide(NumericArgs g, int cls, long long nrows, bool packed)
     }
 }
 
+// ---- wide rows of long A rows: parts and the cut table ---------------------
+//
+// A row's span of tile columns [T0, T1] (from C's first and last column) is
+// cut into P = max(ceil(span / WIDE_W), LONG_MINP) parts of Wp = ceil(span /
+// P) tile columns.  The cut table holds, for each A entry p of the row and each part
+// boundary j = 0..P, the first entry of B's row k_p whose column is at or
+// past the boundary (at [j * na + p], so a part reads its 32 A entries
+// coalesced).  A part is one warp's work anywhere on the GPU: a window of
+// the per-row kernel (mask/offset table by tile column, values accumulated
+// in C) whose B segments come straight from the table -- no search of B on
+// the walk's path, and a row with thousands of A entries spreads over many
+// warps instead of eight.  Parts hold disjoint columns and each walks A's
+// entries in order, so per output the products come in A's row order, then
+// B's.
+
+struct LongRow {
+    int na, pa0, P, T0, Wp, cshift, nnz_r;
+    long long Rb;
+};
+
+__device__ __forceinline__ LongRow long_row(const NumericArgs &g, int R)
+{
+    LongRow L;
+    L.pa0 = (int)g.rpA[R];
+    L.na = (int)g.rpA[R + 1] - L.pa0;
+    L.Rb = g.rowptrC[R];
+    L.nnz_r = (int)(g.rowptrC[R + 1] - L.Rb);
+    L.cshift = g.tr_coloff ? g.tr_coloff[R >> 4] : 0;
+    L.P = 0; L.T0 = 0; L.Wp = 1;
+    if (L.na > LONG_NA && L.nnz_r > 0) {
+        L.T0 = (g.colC[L.Rb] + L.cshift) >> 4;
+        const int span = ((g.colC[L.Rb + L.nnz_r - 1] + L.cshift) >> 4) - L.T0 + 1;
+        L.P = max((span + WIDE_W - 1) / WIDE_W, min(span, LONG_MINP));
+        L.Wp = (span + L.P - 1) / L.P;
+        L.P = (span + L.Wp - 1) / L.Wp;   // no empty trailing part
+    }
+    return L;
+}
+
+// per wide row: 1 when its A row is long enough for the parts path
+__global__ void __launch_bounds__(256)
+k_long_flag(NumericArgs g, int cls, long long nrows, int *flag)
+{
+    const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (idx >= nrows) return;
+    flag[idx] = long_row(g, g.rowlist[(long long)cls * g.m + idx]).P > 0 ? 1 : 0;
+}
+
+// the long rows in order (l = lpos[idx]): wide-row index, row, parts, A
+// entries and cut-table size; entries past the last long row stay zero
+__global__ void __launch_bounds__(256)
+k_long_list(NumericArgs g, int cls, long long nrows, const int *lpos, int *lidx, int *lrow, int *parts, int *nas,
+            long long *tabsz)
+{
+    const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (idx >= nrows || lpos[idx + 1] == lpos[idx]) return;
+    const int R = g.rowlist[(long long)cls * g.m + idx];
+    const LongRow L = long_row(g, R);
+    const int l = lpos[idx];
+    lidx[l] = (int)idx;
+    lrow[l] = R;
+    parts[l] = L.P;
+    nas[l] = L.na;
+    tabsz[l] = (long long)L.na * (L.P + 1);
+}
+
+// rows whose cut table fits the allocation take the parts path
+// (handled[idx] = 1); the others stay with k_numeric_wide
+__global__ void __launch_bounds__(256)
+k_long_fit(long long nrows, const int *lpos, const int *lidx, const long long *tab_off, long long cap,
+           unsigned char *handled, unsigned char *lfit)
+{
+    const long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (l >= nrows || l >= lpos[nrows]) return;
+    const bool fit = tab_off[l + 1] <= cap;
+    lfit[l] = fit ? 1 : 0;
+    handled[lidx[l]] = fit ? 1 : 0;
+}
+
+// last l in [0, n) with off[l] <= v (off nondecreasing, off[0] <= v)
+template <typename T>
+__device__ __forceinline__ long long last_le(const T *off, long long n, long long v)
+{
+    long long lo = 0, hi = n - 1;
+    while (lo < hi) { const long long md = (lo + hi + 1) >> 1; if ((long long)off[md] <= v) lo = md; else hi = md - 1; }
+    return lo;
+}
+
+// the cut table: each warp a contiguous run of the long rows' A entries
+// (na_off: prefix of their counts), lanes over an entry's boundaries
+__global__ void __launch_bounds__(256)
+k_long_cuts(NumericArgs g, long long nrows, const int *lrow, const unsigned char *lfit, const long long *na_off,
+            const long long *tab_off, int *tab)
+{
+    const int lane = threadIdx.x & 31;
+    const long long nw = (long long)gridDim.x * 8, w = blockIdx.x * 8LL + (threadIdx.x >> 5);
+    const long long total = na_off[nrows];
+    const long long ch = (total + nw - 1) / nw;
+    const long long e0 = w * ch, e1 = min(total, e0 + ch);
+    if (e0 >= e1) return;
+    long long l = last_le(na_off, nrows, e0);
+    int R = lrow[l];
+    LongRow L = long_row(g, R);
+    for (long long e = e0; e < e1; ++e) {
+        while (na_off[l + 1] <= e) { ++l; R = lrow[l]; L = long_row(g, R); }
+        if (!lfit[l]) continue;
+        const int p = (int)(e - na_off[l]);
+        const int k = g.colA[L.pa0 + p];
+        const int bs = (int)g.rpB[k], be = (int)g.rpB[k + 1];
+        int *t = tab + tab_off[l];
+        for (int j = lane; j <= L.P; j += 32) {
+            int v;
+            if (j == 0) v = bs;
+            else if (j == L.P) v = be;
+            else {
+                const int key = (L.T0 + j * L.Wp) * TILE;
+                int lo = bs, hi = be;
+                while (lo < hi) { const int md = (lo + hi) >> 1; if (g.colB[md] < key) lo = md + 1; else hi = md; }
+                v = lo;
+            }
+            t[(long long)j * L.na + p] = v;
+        }
+    }
+}
+
+// the walk: warps over parts (grid-stride, so a row's parts land on
+// different warps)
+__global__ void __launch_bounds__(ROW_WARPS * 32, 4)
+k_long_walk(NumericArgs g, long long nrows, const int *lrow, const unsigned char *lfit, const int *part_off,
+            const long long *tab_off, const int *tab)
+{
+    extern __shared__ __align__(16) unsigned char s_raw[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    unsigned char *wbase = s_raw + (size_t)warp * WIDE_WARP_BYTES;
+    unsigned *s_off = reinterpret_cast<unsigned *>(wbase);
+    unsigned short *s_msk = reinterpret_cast<unsigned short *>(wbase + (size_t)WIDE_W * 4);
+    for (int t = lane; t < WIDE_W; t += 32) s_msk[t] = 0;
+    __syncwarp();
+    const long long nparts = part_off[nrows];
+    bool bad = false;
+    for (long long gp = blockIdx.x * (long long)ROW_WARPS + warp; gp < nparts; gp += (long long)gridDim.x * ROW_WARPS) {
+        const long long l = last_le(part_off, nrows, gp);
+        if (!lfit[l]) continue;
+        const int R = lrow[l];
+        const LongRow L = long_row(g, R);
+        const int j = (int)(gp - part_off[l]);
+        const int i = R >> 4, r = R & (TILE - 1);
+        const long long c0 = g.crp[i];
+        const int S = (int)(g.crp[i + 1] - c0);
+        const uint16_t *mrow = g.cmask + c0 * TILE + (long long)r * S;
+        const int *tcol = g.ccol + c0;
+        const int wlo = L.T0 + j * L.Wp, whi = wlo + L.Wp;   // tile columns [wlo, whi)
+        const int sa = warp_lower_bound(tcol, 0, S, wlo, lane);
+        const int sb = warp_lower_bound(tcol, sa, S, whi, lane);
+        if (sa >= sb) continue;
+        unsigned run = (unsigned)warp_lower_bound(g.colC + L.Rb, 0, L.nnz_r, wlo * TILE - L.cshift, lane);
+        bool any = false;
+        for (int s = sa; s < sb; s += 32) {
+            const int ss = s + lane;
+            const unsigned mk = ss < sb ? (unsigned)mrow[ss] : 0u;
+            const int c = __popc(mk);
+            const int incl = warp_incl_scan(c, lane);
+            if (mk) {
+                const int t = tcol[ss] - wlo;
+                s_off[t] = run + incl - c;
+                s_msk[t] = (unsigned short)mk;
+                const long long dst = L.Rb + run + incl - c;
+                for (int q = 0; q < c; ++q) g.valC[dst + q] = 0.0;   // zeroed just before the walk
+                any = true;
+            }
+            run += __shfl_sync(0xffffffffu, incl, 31);
+        }
+        __syncwarp();
+        if (__any_sync(0xffffffffu, any)) {
+            const long long Rb = L.Rb;
+            auto pos_of = [&](int col) -> long long {
+                const int t = (col >> 4) - wlo, cc = col & 15;
+                const unsigned mk = s_msk[t];
+                return ((mk >> (TILE - 1 - cc)) & 1u) ? Rb + s_off[t] + __popc(mk >> (TILE - cc)) : -1ll;
+            };
+            const int *tb = tab + tab_off[l];
+            for (int pb = 0; pb < L.na; pb += 32) {
+                const int nb = min(32, L.na - pb);
+                int bs = 0, be = 0;
+                double av = 0.0;
+                if (lane < nb) {
+                    av = g.valA[L.pa0 + pb + lane];
+                    bs = tb[(long long)j * L.na + pb + lane];
+                    be = tb[(long long)(j + 1) * L.na + pb + lane];
+                }
+                walk_segments(g, lane, nb, av, bs, be, wlo * TILE, whi * TILE, g.valC, pos_of, bad);
+            }
+        }
+        for (int ss = sa + lane; ss < sb; ss += 32) s_msk[tcol[ss] - wlo] = 0;
+        __syncwarp();
+    }
+    if (bad) set_flag(g.flags, FLAG_INTERNAL);
+}
+
 template <int NT, bool DENSE, int WALK>
 cudaError_t set_smem_attr() {
     cudaError_t e = cudaFuncSetAttribute(k_numeric_smem<NT, DENSE, WALK>,
@@ -888,6 +1108,97 @@ cudaError_t numeric_init_attributes()
     return e;
 }
 
+namespace {
+
+// scratch of the parts path (pool memory, released after the walk)
+struct LongScratch {
+    int *flag = nullptr, *lpos = nullptr, *lidx = nullptr, *lrow = nullptr, *parts = nullptr, *nas = nullptr,
+        *part_off = nullptr;
+    long long *tabsz = nullptr, *na_off = nullptr, *tab_off = nullptr;
+    unsigned char *handled = nullptr, *lfit = nullptr;
+    int *tab = nullptr;
+};
+
+void long_release(Pool &pool, LongScratch &L)
+{
+    for (void *p : {(void *)L.flag, (void *)L.lpos, (void *)L.lidx, (void *)L.lrow, (void *)L.parts, (void *)L.nas,
+                    (void *)L.part_off, (void *)L.tabsz, (void *)L.na_off, (void *)L.tab_off, (void *)L.handled,
+                    (void *)L.lfit, (void *)L.tab})
+        pool.free(p);
+    L = LongScratch{};
+}
+
+// the long rows' list, part and A-entry prefixes, and the cut table
+cudaError_t long_prepare(Pool &pool, const NumericArgs &a, int cls, long long n, long long tab_bound, LongScratch &L)
+{
+    cudaStream_t s = pool.stream;
+    L.flag = pool.alloc_n<int>(n + 1);
+    L.lpos = pool.alloc_n<int>(n + 1);
+    L.lidx = pool.alloc_n<int>(n);
+    L.handled = pool.alloc_n<unsigned char>(n);
+    L.lfit = pool.alloc_n<unsigned char>(n);
+    L.lrow = pool.alloc_n<int>(n);
+    L.parts = pool.alloc_n<int>(n + 1);
+    L.nas = pool.alloc_n<int>(n + 1);
+    L.part_off = pool.alloc_n<int>(n + 1);
+    L.tabsz = pool.alloc_n<long long>(n + 1);
+    L.na_off = pool.alloc_n<long long>(n + 1);
+    L.tab_off = pool.alloc_n<long long>(n + 1);
+    if (!L.flag || !L.lpos || !L.lidx || !L.handled || !L.lfit || !L.lrow || !L.parts || !L.nas || !L.part_off ||
+        !L.tabsz || !L.na_off || !L.tab_off) {
+        const cudaError_t err = pool.err != cudaSuccess ? pool.err : cudaErrorMemoryAllocation;
+        long_release(pool, L);
+        return err;
+    }
+    cudaError_t e = cudaMemsetAsync(L.parts, 0, sizeof(int) * (size_t)n, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(L.handled, 0, (size_t)n, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(L.lfit, 0, (size_t)n, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(L.nas, 0, sizeof(int) * (size_t)n, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(L.tabsz, 0, sizeof(long long) * (size_t)n, s);
+    const unsigned gb = (unsigned)((n + 255) / 256);
+    if (e == cudaSuccess) { k_long_flag<<<gb, 256, 0, s>>>(a, cls, n, L.flag); ::tsg::count_launch(); e = cudaGetLastError(); }
+    if (e == cudaSuccess) e = scan_i32_to_i32(pool, L.flag, L.lpos, n, a.flags);
+    if (e == cudaSuccess) {
+        k_long_list<<<gb, 256, 0, s>>>(a, cls, n, L.lpos, L.lidx, L.lrow, L.parts, L.nas, L.tabsz);
+        ::tsg::count_launch();
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = scan_i32_to_i32(pool, L.parts, L.part_off, n, a.flags);
+    if (e == cudaSuccess) e = scan_i32_to_i64(pool, L.nas, L.na_off, n, a.flags);
+    if (e == cudaSuccess) e = scan_i64_to_i64(pool, L.tabsz, L.tab_off, n, a.flags);
+    // the cut table: its exact size when the stream can wait for it, else
+    // the bound (inside a graph capture)
+    long long cap = tab_bound;
+    if (e == cudaSuccess) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        e = cudaStreamIsCapturing(s, &cs);
+        if (e == cudaSuccess && cs == cudaStreamCaptureStatusNone) {
+            long long need = 0;
+            e = cudaMemcpyAsync(&need, L.tab_off + n, sizeof(long long), cudaMemcpyDeviceToHost, s);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+            cap = std::min(tab_bound, need);
+        }
+    }
+    if (e == cudaSuccess) {
+        L.tab = pool.alloc_n<int>(cap);
+        if (!L.tab) e = pool.err != cudaSuccess ? pool.err : cudaErrorMemoryAllocation;
+    }
+    if (e == cudaSuccess) {
+        k_long_fit<<<gb, 256, 0, s>>>(n, L.lpos, L.lidx, L.tab_off, cap, L.handled, L.lfit);
+        ::tsg::count_launch();
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) {
+        k_long_cuts<<<LONG_GRID * 2, 256, 0, s>>>(a, n, L.lrow, L.lfit, L.na_off, L.tab_off, L.tab);
+        ::tsg::count_launch();
+        e = cudaGetLastError();
+    }
+    if (e != cudaSuccess) long_release(pool, L);
+    return e;
+}
+
+}  // namespace
+
 cudaError_t numeric_run(Pool &pool, const NumericArgs &a, const long long *binstat, int walk, int threads,
                         int row_warps)
 {
@@ -924,8 +1235,25 @@ cudaError_t numeric_run(Pool &pool, const NumericArgs &a, const long long *binst
         const long long n = rcnt[c];
         if (n == 0) continue;
         { k_global_prep<<<(unsigned)((n * 32 + 255) / 256), 256, 0, s>>>(a, c, n); ::tsg::count_launch(); }
-        if (c == ROW_WIDE) { k_numeric_wide<ROW_WARPS><<<(unsigned)n, ROW_WARPS * 32, WIDE_SMEM, s>>>(a, c, n, packed); ::tsg::count_launch(); }
-        else { k_numeric_wide<1><<<(unsigned)((n + ROW_WARPS - 1) / ROW_WARPS), ROW_WARPS * 32, WIDE_SMEM, s>>>(a, c, n, packed); ::tsg::count_launch(); }
+        // rows of long A rows: parts over the whole GPU, when C is wide enough
+        // for rows to span LONG_MINP windows (measured: narrower products
+        // run faster per row); the cut table gets at most LONG_TAB_MAX
+        // entries (rows past it stay with k_numeric_wide)
+        const long long pmax = std::max<long long>(((long long)(a.n + TILE - 1) / TILE + WIDE_W - 1) / WIDE_W, LONG_MINP);
+        const long long tab_bound = std::min<long long>(LONG_TAB_MAX, a.nnzA * (pmax + 1));
+        const bool parts = c == ROW_WIDE && a.b_sorted && !packed &&
+                           ((long long)a.n + TILE - 1) / TILE >= (long long)LONG_MINP * WIDE_W;
+        LongScratch L{};
+        if (parts) {
+            e = long_prepare(pool, a, c, n, tab_bound, L);
+            if (e != cudaSuccess) return e;
+        }
+        if (c == ROW_WIDE) { k_numeric_wide<ROW_WARPS><<<(unsigned)n, ROW_WARPS * 32, WIDE_SMEM, s>>>(a, c, n, packed, L.handled); ::tsg::count_launch(); }
+        else { k_numeric_wide<1><<<(unsigned)((n + ROW_WARPS - 1) / ROW_WARPS), ROW_WARPS * 32, WIDE_SMEM, s>>>(a, c, n, packed, nullptr); ::tsg::count_launch(); }
+        if (parts) {
+            { k_long_walk<<<LONG_GRID, ROW_WARPS * 32, WIDE_SMEM, s>>>(a, n, L.lrow, L.lfit, L.part_off, L.tab_off, L.tab); ::tsg::count_launch(); }
+            long_release(pool, L);
+        }
         e = cudaGetLastError();
     }
     return e;

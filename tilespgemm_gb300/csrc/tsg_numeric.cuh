@@ -163,6 +163,8 @@ struct NumericArgs {
     bool b_sorted;        // B's rows have strictly increasing columns (column-range searches allowed)
     const int *tr_coloff; // per tile-row, subtracted from the column indices written (batched products); may be null
     int *flags;
+    long long nnzA;       // entries of A (bounds the wide rows' cut table)
+    int n;                // columns of C
 };
 
 cudaError_t step2_masks(Pool &pool, const TileCSR &A, const TileCSR &B, int m, int blkm, const long long *crp,
