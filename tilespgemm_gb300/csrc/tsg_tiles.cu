@@ -12,7 +12,7 @@
 // [min, max]; popc gives the count, a warp scan of per-word popc gives each
 // key its rank, so the list comes out sorted with no sort and no hash.  Rows
 // whose window exceeds 4096 keys go to a CTA-wide kernel that walks the
-// window in 262,144-key chunks (any width).
+// window in 65,536-key chunks (any width).
 //
 // Row masks are stored per tile-row in row-major order: the masks of the
 // tile-row whose tiles are t0..t1-1 occupy [16*t0, 16*t1), local row r of
@@ -33,7 +33,8 @@ namespace {
 
 constexpr int NW = 128;                 // narrow bitmap: 128 words = 4096 keys per warp
 constexpr int WPC = 8;                  // warps per CTA in the narrow kernels
-constexpr int WIDE_WORDS = 8192;        // wide bitmap chunk: 262,144 keys
+constexpr int WIDE_WORDS = 2048;        // wide bitmap chunk: 65,536 keys
+constexpr int WIDE_GRID = 1216;         // CTAs of the wide union (grid-stride over the wide tile-rows): 8 per SM
 constexpr int WIDE_THREADS = 256;
 constexpr int WIDE_SMEM = WIDE_WORDS * 4 * 2;  // bitmap + word prefix
 
@@ -767,7 +768,7 @@ cudaError_t union_structure(Pool &pool, typename KS::Params P, int nrows, int *c
         if (nrows > 0) {
             { k_union_count<KS><<<g, WPC * 32, 0, s>>>(P, nrows, cnt_scratch, wide, wide_n, stat, defer,
                                                       defer ? defer + nrows : nullptr, defer_S); ::tsg::count_launch(); }
-            { k_union_wide<KS, false, false, TP><<<304, WIDE_THREADS, WIDE_SMEM, s>>>(
+            { k_union_wide<KS, false, false, TP><<<WIDE_GRID, WIDE_THREADS, WIDE_SMEM, s>>>(
                 P, wide, wide_n, cnt_scratch, stat, nullptr, nullptr, nullptr); ::tsg::count_launch(); }
         }
         e = scan(pool, cnt_scratch, rowptr_out, nrows, flags);
@@ -775,11 +776,11 @@ cudaError_t union_structure(Pool &pool, typename KS::Params P, int nrows, int *c
     if (e == cudaSuccess && do_fill && nrows > 0 && out_cols) {
         if (mask) {
             { k_union_fill<KS, true, TP><<<g, WPC * 32, 0, s>>>(P, nrows, rowptr_out, out_cols, mask); ::tsg::count_launch(); }
-            { k_union_wide<KS, true, true, TP><<<304, WIDE_THREADS, WIDE_SMEM, s>>>(
+            { k_union_wide<KS, true, true, TP><<<WIDE_GRID, WIDE_THREADS, WIDE_SMEM, s>>>(
                 P, wide, wide_n, nullptr, nullptr, rowptr_out, out_cols, mask); ::tsg::count_launch(); }
         } else {
             { k_union_fill<KS, false, TP><<<g, WPC * 32, 0, s>>>(P, nrows, rowptr_out, out_cols, nullptr); ::tsg::count_launch(); }
-            { k_union_wide<KS, true, false, TP><<<304, WIDE_THREADS, WIDE_SMEM, s>>>(
+            { k_union_wide<KS, true, false, TP><<<WIDE_GRID, WIDE_THREADS, WIDE_SMEM, s>>>(
                 P, wide, wide_n, nullptr, nullptr, rowptr_out, out_cols, nullptr); ::tsg::count_launch(); }
         }
     }
@@ -919,7 +920,7 @@ cudaError_t symbolic_fill_fused(Pool &pool, const TileCSR &A, const TileCSR &B, 
                                                                          cmask, rowcnt, bin, bp, binstat, binlist, rowlist, flags,
                                                                          erpB, ecolB, erpA, ecolA); ::tsg::count_launch(); }
     (void)cnt;
-    { k_union_wide<UnionKeys, true, false, long long><<<304, WIDE_THREADS, WIDE_SMEM, s>>>(
+    { k_union_wide<UnionKeys, true, false, long long><<<WIDE_GRID, WIDE_THREADS, WIDE_SMEM, s>>>(
         P, wide, wide + A.blkm, nullptr, nullptr, crp, ccol, nullptr); ::tsg::count_launch(); }
     return cudaGetLastError();
 }
