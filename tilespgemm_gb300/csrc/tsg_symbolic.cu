@@ -539,6 +539,7 @@ k_step2_entries(int blkm, int m, const int *__restrict__ arp, const long long *_
 constexpr int S2_SMAX = 4096;   // tiles per tile-row (or window) handled with shared-memory masks
 
 constexpr int S2_SMALL = 1024;  // tile-rows of up to this many tiles: 256-thread CTAs with less shared memory
+constexpr int S2E_WIN = 2048;   // tiles per window of k_step2_entries (two CTAs per SM)
 
 namespace {
 size_t step2_smem(int slots, int map_cap) {
@@ -595,10 +596,10 @@ cudaError_t step2_masks(Pool &pool, const TileCSR &A, const TileCSR &B, int m, i
         { k_step2<512><<<ndefer, 512, step2_smem(slots, map_cap), s>>>(blkm, m, A.trp, A.tcol, A.mask, B.trp, B.tcol, B.mask, crp, ccol,
                                                    cmask, rowcnt, S2_SMALL, S2_SMAX, map_cap, bp, bin, binstat, binlist, rowlist, flags, defer_list,
                                                    erpB, ecolB, erpA); ::tsg::count_launch(); }
-        const int wslots = max_tiles_per_row < S2_SMAX ? max_tiles_per_row : S2_SMAX;
-        const int wmap = max_tiles_per_row > S2_SMAX ? (int)MAP_MAX : map_cap;
+        const int wslots = max_tiles_per_row < S2E_WIN ? max_tiles_per_row : S2E_WIN;
+        const int wmap = max_tiles_per_row > S2E_WIN ? (int)MAP_MAX : map_cap;
         { k_step2_entries<512><<<ndefer, 512, step2e_smem(wslots, wmap), s>>>(blkm, m, A.trp, crp, ccol, cmask, rowcnt, S2_SMALL, INT_MAX,
-                                                   S2_SMAX, wmap, bp, bin, binstat, binlist, rowlist, flags, defer_list,
+                                                   S2E_WIN, wmap, bp, bin, binstat, binlist, rowlist, flags, defer_list,
                                                    erpB, ecolB, erpA, ecolA, b_sorted ? 1 : 0); ::tsg::count_launch(); }
     }
     if (max_tiles_per_row > S2_SMAX) {
