@@ -212,7 +212,7 @@ k_step2(int blkm, int m, const int *__restrict__ arp, const int *__restrict__ ac
     if (s_bin == BIN_ROWS && tid < rows) record_row(bp, S, s_rowtot[tid], span, i * TILE + tid, m, binstat, rowlist);
 }
 
-// Tile-rows with more than `smax` C tiles: the tile slots are taken in
+// Tile-rows with more than `smin` C tiles: the tile slots are taken in
 // windows of `smax`; per window the row masks accumulate in shared memory
 // (OR does not depend on order) and are then written out.  Every window
 // walks the tile-row's A tiles again, with each B tile-row (tile path) or
@@ -223,7 +223,7 @@ __global__ void __launch_bounds__(NT)
 k_step2_win(int blkm, int m, const int *__restrict__ arp, const int *__restrict__ acol,
             const uint16_t *__restrict__ amask, const int *__restrict__ brp, const int *__restrict__ bcol,
             const uint16_t *__restrict__ bmask, const long long *__restrict__ crp, const int *__restrict__ ccol,
-            uint16_t *cmask, int *rowcnt, int smax, NumericBinParams bp, unsigned char *bin,
+            uint16_t *cmask, int *rowcnt, int smin, int smax, NumericBinParams bp, unsigned char *bin,
             long long *binstat, int *binlist, int *rowlist, int *flags, const int *__restrict__ rows_list,
             const long long *__restrict__ erpB, const int *__restrict__ ecolB, const long long *__restrict__ erpA)
 {
@@ -233,7 +233,7 @@ k_step2_win(int blkm, int m, const int *__restrict__ arp, const int *__restrict_
     if (i >= blkm) return;
     const long long c0 = crp[i];
     const int S = (int)(crp[i + 1] - c0);
-    if (S <= smax) return;
+    if (S <= smin) return;
     const int rows = min(TILE, m - i * TILE);
     if (entry_walk(erpA, arp, i, rows)) return;   // sparse A tiles: k_step2_entries
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -540,6 +540,7 @@ constexpr int S2_SMAX = 4096;   // tiles per tile-row (or window) handled with s
 
 constexpr int S2_SMALL = 1024;  // tile-rows of up to this many tiles: 256-thread CTAs with less shared memory
 constexpr int S2E_WIN = 2048;   // tiles per window of k_step2_entries (two CTAs per SM)
+constexpr int S2W_WIN = 4096;   // tiles per window of k_step2_win
 
 namespace {
 size_t step2_smem(int slots, int map_cap) {
@@ -603,8 +604,8 @@ cudaError_t step2_masks(Pool &pool, const TileCSR &A, const TileCSR &B, int m, i
                                                    erpB, ecolB, erpA, ecolA, b_sorted ? 1 : 0); ::tsg::count_launch(); }
     }
     if (max_tiles_per_row > S2_SMAX) {
-        { k_step2_win<512><<<ndefer, 512, step2_smem(S2_SMAX, MAP_MAX), s>>>(blkm, m, A.trp, A.tcol, A.mask, B.trp, B.tcol, B.mask, crp, ccol,
-                                                      cmask, rowcnt, S2_SMAX, bp, bin, binstat, binlist, rowlist, flags, defer_list,
+        { k_step2_win<512><<<ndefer, 512, step2_smem(S2W_WIN, MAP_MAX), s>>>(blkm, m, A.trp, A.tcol, A.mask, B.trp, B.tcol, B.mask, crp, ccol,
+                                                      cmask, rowcnt, S2_SMAX, S2W_WIN, bp, bin, binstat, binlist, rowlist, flags, defer_list,
                                                       erpB, ecolB, erpA); ::tsg::count_launch(); }
     }
     return cudaGetLastError();
