@@ -226,7 +226,7 @@ def run_ours(args) -> None:
     A, op, desc = make_workload(args.workload)
     B = operand_b(A, op)
     cub = nnzcub(A, B)
-    ctx = Context(local, phase_times=1)
+    ctx = Context(local, phase_times=1, count_products=0)   # nnzCub is counted on the host above
     lib = _abi.lib()
     stream = torch.cuda.ExternalStream(lib.tsg_get_stream(ctx.handle), device=torch.device("cuda", local))
 

@@ -99,6 +99,8 @@ typedef struct {
                                 (one warp each) accumulate in C's value array instead, one warp each (default 0) */
     int32_t row_warps;       /* warps per row for those shared-memory rows: 1, 2 or 4, each warp a column range
                                 (default 4, measured fastest) */
+    int32_t count_products;  /* 1: calls given a tsg_stats count the intermediate products (nnz_cub, one extra
+                                pass over A); 0: nnz_cub is reported as 0 (default 1) */
 } tsg_opts;
 
 /* Per-call statistics.  Sizes are always filled; times only with phase_times. */

@@ -53,7 +53,7 @@ class tsg_opts(C.Structure):
         ("validate", C.c_int32), ("phase_times", C.c_int32), ("out_rowptr_bits", C.c_int32),
         ("dense_tile_min", C.c_int32), ("smem_acc_max", C.c_int32), ("threads_numeric", C.c_int32),
         ("row_acc_max", C.c_int32), ("numeric_walk", C.c_int32),
-        ("rows_global", C.c_int32), ("row_warps", C.c_int32),
+        ("rows_global", C.c_int32), ("row_warps", C.c_int32), ("count_products", C.c_int32),
     ]
 
 

@@ -654,6 +654,7 @@ void tsg_opts_default(tsg_opts *o)
     o->numeric_walk = 0;
     o->rows_global = 0;
     o->row_warps = 4;
+    o->count_products = 1;
 }
 
 const char *tsg_last_error(void) { return g_err.c_str(); }
@@ -783,7 +784,7 @@ tsg_status tsg_spgemm(tsg_ctx *ctx, tsg_op op, const tsg_csr *A, const tsg_csr *
     tsg_status r;
     {
         Scratch sc(pool);
-        r = plan_symbolic(ctx, pool, sc, op, A, B, P, false, st != nullptr, tm);
+        r = plan_symbolic(ctx, pool, sc, op, A, B, P, false, st != nullptr && ctx->opts.count_products, tm);
         if (!r) {
             col = pool.alloc_n<int>(P.nnzC);
             val = pool.alloc_n<double>(P.nnzC);
@@ -1080,7 +1081,7 @@ tsg_status tsg_spgemm_tiles(tsg_ctx *ctx, tsg_op op, const tsg_csr *A, const tsg
     tsg_status r;
     {
         Scratch sc(pool);
-        r = plan_symbolic(ctx, pool, sc, op, A, B, P, false, st != nullptr, tm);
+        r = plan_symbolic(ctx, pool, sc, op, A, B, P, false, st != nullptr && ctx->opts.count_products, tm);
         if (!r) {
             col = pool.alloc_n<int>(P.nnzC);
             val = pool.alloc_n<double>(P.nnzC);
@@ -1303,7 +1304,7 @@ tsg_status tsg_spgemm_batched(tsg_ctx *ctx, tsg_op op, int32_t count, const tsg_
         r = pack_operands(ctx, pool, sc, count, A, roff, op == TSG_OP_AAT ? koff : (op == TSG_OP_AA ? roff : koff),
                           M, op == TSG_OP_AA ? M : K, pA);
         if (!r && op == TSG_OP_AB) r = pack_operands(ctx, pool, sc, count, B, koff, noff, K, N, pB);
-        if (!r) r = plan_symbolic(ctx, pool, sc, op, &pA, op == TSG_OP_AB ? &pB : nullptr, P, false, st != nullptr, tm,
+        if (!r) r = plan_symbolic(ctx, pool, sc, op, &pA, op == TSG_OP_AB ? &pB : nullptr, P, false, st != nullptr && ctx->opts.count_products, tm,
                                   false);
         // C's column offset of each packed tile-row's instance: the numeric
         // step writes C_i's columns already rebased
@@ -1630,7 +1631,7 @@ tsg_status tsg_plan_create_batched(tsg_ctx *ctx, tsg_op op, int32_t count, const
         r = pack_operands(ctx, pool, sc, count, A, roff, op == TSG_OP_AAT ? koff : (op == TSG_OP_AA ? roff : koff),
                           M, op == TSG_OP_AA ? M : K, pA);
         if (!r && op == TSG_OP_AB) r = pack_operands(ctx, pool, sc, count, B, koff, noff, K, N, pB);
-        if (!r) r = plan_symbolic(ctx, pool, sc, op, &pA, op == TSG_OP_AB ? &pB : nullptr, P, true, st != nullptr, tm,
+        if (!r) r = plan_symbolic(ctx, pool, sc, op, &pA, op == TSG_OP_AB ? &pB : nullptr, P, true, st != nullptr && ctx->opts.count_products, tm,
                                   false);
         if (!r) r = cudaStreamSynchronize(ctx->stream) == cudaSuccess ? TSG_OK : fail(TSG_ERR_CUDA, "plan build failed");
     }
