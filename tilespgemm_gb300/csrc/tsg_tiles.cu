@@ -370,10 +370,6 @@ k_sym_fused(UnionKeys::Params P, int blkm, int m, const long long *__restrict__ 
                 ma &= __brev(__ballot_sync(0xffffffffu, lng)) >> 16;
                 if (!__any_sync(0xffffffffu, ma != 0u)) continue;
             }
-            // transpose the A tile: colrows[c] = rows that use local column c (uniform)
-            unsigned colrows[TILE];
-#pragma unroll
-            for (int c = 0; c < TILE; ++c) colrows[c] = __ballot_sync(0xffffffffu, (ma >> (TILE - 1 - c)) & 1u) & 0xffffu;
             // A tiles with few entries: B's rows element by element (as in the
             // CTA step-2 kernel); lanes may then share a slot, so word atomics
             const unsigned acols = __brev(__reduce_or_sync(0xffffffffu, ma)) >> 16;
@@ -418,19 +414,28 @@ k_sym_fused(UnionKeys::Params P, int blkm, int m, const long long *__restrict__ 
                     }
                     if (slot < 0 || slot >= S) { bad = true; slot = -1; }
                 }
-                // the B tile's rows this A tile uses: independent loads, issued together
-                unsigned brow[TILE];
+                // half the A tile's columns at a time (fewer registers, more
+                // warps per SM): the rows that use local column c (a ballot,
+                // uniform), the B tile's rows c -- independent loads, issued
+                // together -- then the ORs
 #pragma unroll
-                for (int c = 0; c < TILE; ++c)
-                    brow[c] = (colrows[c] != 0u && slot >= 0) ? (unsigned)bq[c * nq + q] : 0u;
+                for (int h = 0; h < TILE; h += TILE / 2) {
+                    unsigned colrows[TILE / 2], brow[TILE / 2];
 #pragma unroll
-                for (int c = 0; c < TILE; ++c) {
-                    unsigned rws = colrows[c];
-                    const unsigned b = brow[c];
-                    while (rws) {
-                        const int r = __ffs(rws) - 1;
-                        rws &= rws - 1;
-                        if (b) msk[r * S + slot] |= (unsigned short)b;
+                    for (int c = 0; c < TILE / 2; ++c)
+                        colrows[c] = __ballot_sync(0xffffffffu, (ma >> (TILE - 1 - (h + c))) & 1u) & 0xffffu;
+#pragma unroll
+                    for (int c = 0; c < TILE / 2; ++c)
+                        brow[c] = (colrows[c] != 0u && slot >= 0) ? (unsigned)bq[(h + c) * nq + q] : 0u;
+#pragma unroll
+                    for (int c = 0; c < TILE / 2; ++c) {
+                        unsigned rws = colrows[c];
+                        const unsigned b = brow[c];
+                        while (rws) {
+                            const int r = __ffs(rws) - 1;
+                            rws &= rws - 1;
+                            if (b) msk[r * S + slot] |= (unsigned short)b;
+                        }
                     }
                 }
             }
