@@ -648,7 +648,7 @@ constexpr int WS_W = 512, WS_E = 512;
 // Wide rows with more A entries than LONG_NA are cut into parts of at most
 // WIDE_W tile columns, each part one warp's work anywhere on the GPU
 // (k_long_walk); their B rows' cut points come from a table built once.
-constexpr int LONG_NA = 512;
+constexpr int LONG_NA = 32;
 constexpr int LONG_MINP = 16;        // parts of such a row at least (more warps than the per-row kernel's 8)
 constexpr int LONG_GRID = 152 * 4;   // CTAs of the part walk: four per SM
 constexpr long long LONG_TAB_MAX = 1ll << 30;   // cut-table entries (4 GB) beyond which long rows stay per row
@@ -984,11 +984,12 @@ k_long_cuts(NumericArgs g, long long nrows, const int *lrow, const unsigned char
     }
 }
 
-// the walk: warps over parts (grid-stride, so a row's parts land on
-// different warps)
+// the walk: each warp takes the next part from a counter until none is
+// left (parts differ widely in cost, so a static share would leave warps
+// idle behind the hub rows' parts)
 __global__ void __launch_bounds__(ROW_WARPS * 32, 4)
 k_long_walk(NumericArgs g, long long nrows, const int *lrow, const unsigned char *lfit, const int *part_off,
-            const long long *tab_off, const int *tab)
+            const long long *tab_off, const int *tab, unsigned long long *next_part)
 {
     extern __shared__ __align__(16) unsigned char s_raw[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -999,7 +1000,11 @@ k_long_walk(NumericArgs g, long long nrows, const int *lrow, const unsigned char
     __syncwarp();
     const long long nparts = part_off[nrows];
     bool bad = false;
-    for (long long gp = blockIdx.x * (long long)ROW_WARPS + warp; gp < nparts; gp += (long long)gridDim.x * ROW_WARPS) {
+    for (;;) {
+        unsigned long long t = 0;
+        if (lane == 0) t = atomicAdd(next_part, 1ull);
+        const long long gp = (long long)__shfl_sync(0xffffffffu, t, 0);
+        if (gp >= nparts) break;
         const long long l = last_le(part_off, nrows, gp);
         if (!lfit[l]) continue;
         const int R = lrow[l];
@@ -1117,13 +1122,14 @@ struct LongScratch {
     long long *tabsz = nullptr, *na_off = nullptr, *tab_off = nullptr;
     unsigned char *handled = nullptr, *lfit = nullptr;
     int *tab = nullptr;
+    unsigned long long *next_part = nullptr;   // the walk's work counter
 };
 
 void long_release(Pool &pool, LongScratch &L)
 {
     for (void *p : {(void *)L.flag, (void *)L.lpos, (void *)L.lidx, (void *)L.lrow, (void *)L.parts, (void *)L.nas,
                     (void *)L.part_off, (void *)L.tabsz, (void *)L.na_off, (void *)L.tab_off, (void *)L.handled,
-                    (void *)L.lfit, (void *)L.tab})
+                    (void *)L.lfit, (void *)L.tab, (void *)L.next_part})
         pool.free(p);
     L = LongScratch{};
 }
@@ -1144,13 +1150,15 @@ cudaError_t long_prepare(Pool &pool, const NumericArgs &a, int cls, long long n,
     L.tabsz = pool.alloc_n<long long>(n + 1);
     L.na_off = pool.alloc_n<long long>(n + 1);
     L.tab_off = pool.alloc_n<long long>(n + 1);
+    L.next_part = pool.alloc_n<unsigned long long>(1);
     if (!L.flag || !L.lpos || !L.lidx || !L.handled || !L.lfit || !L.lrow || !L.parts || !L.nas || !L.part_off ||
-        !L.tabsz || !L.na_off || !L.tab_off) {
+        !L.tabsz || !L.na_off || !L.tab_off || !L.next_part) {
         const cudaError_t err = pool.err != cudaSuccess ? pool.err : cudaErrorMemoryAllocation;
         long_release(pool, L);
         return err;
     }
     cudaError_t e = cudaMemsetAsync(L.parts, 0, sizeof(int) * (size_t)n, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(L.next_part, 0, sizeof(unsigned long long), s);
     if (e == cudaSuccess) e = cudaMemsetAsync(L.handled, 0, (size_t)n, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(L.lfit, 0, (size_t)n, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(L.nas, 0, sizeof(int) * (size_t)n, s);
@@ -1235,14 +1243,14 @@ cudaError_t numeric_run(Pool &pool, const NumericArgs &a, const long long *binst
         const long long n = rcnt[c];
         if (n == 0) continue;
         { k_global_prep<<<(unsigned)((n * 32 + 255) / 256), 256, 0, s>>>(a, c, n); ::tsg::count_launch(); }
-        // rows of long A rows: parts over the whole GPU, when C is wide enough
-        // for rows to span LONG_MINP windows (measured: narrower products
-        // run faster per row); the cut table gets at most LONG_TAB_MAX
-        // entries (rows past it stay with k_numeric_wide)
+        // rows of long A rows: parts over the whole GPU (measured faster than
+        // eight warps per row from C widths of 1,024 tile columns on); the
+        // cut table gets at most LONG_TAB_MAX entries (rows past it stay
+        // with k_numeric_wide)
         const long long pmax = std::max<long long>(((long long)(a.n + TILE - 1) / TILE + WIDE_W - 1) / WIDE_W, LONG_MINP);
         const long long tab_bound = std::min<long long>(LONG_TAB_MAX, a.nnzA * (pmax + 1));
         const bool parts = c == ROW_WIDE && a.b_sorted && !packed &&
-                           ((long long)a.n + TILE - 1) / TILE >= (long long)LONG_MINP * WIDE_W;
+                           ((long long)a.n + TILE - 1) / TILE >= WIDE_W;
         LongScratch L{};
         if (parts) {
             e = long_prepare(pool, a, c, n, tab_bound, L);
@@ -1251,7 +1259,7 @@ cudaError_t numeric_run(Pool &pool, const NumericArgs &a, const long long *binst
         if (c == ROW_WIDE) { k_numeric_wide<ROW_WARPS><<<(unsigned)n, ROW_WARPS * 32, WIDE_SMEM, s>>>(a, c, n, packed, L.handled); ::tsg::count_launch(); }
         else { k_numeric_wide<1><<<(unsigned)((n + ROW_WARPS - 1) / ROW_WARPS), ROW_WARPS * 32, WIDE_SMEM, s>>>(a, c, n, packed, nullptr); ::tsg::count_launch(); }
         if (parts) {
-            { k_long_walk<<<LONG_GRID, ROW_WARPS * 32, WIDE_SMEM, s>>>(a, n, L.lrow, L.lfit, L.part_off, L.tab_off, L.tab); ::tsg::count_launch(); }
+            { k_long_walk<<<LONG_GRID, ROW_WARPS * 32, WIDE_SMEM, s>>>(a, n, L.lrow, L.lfit, L.part_off, L.tab_off, L.tab, L.next_part); ::tsg::count_launch(); }
             long_release(pool, L);
         }
         e = cudaGetLastError();
