@@ -645,11 +645,12 @@ constexpr int WIDE_WARP_BYTES = WIDE_W * (4 + 2);   // shared memory per warp
 constexpr size_t WIDE_SMEM = (size_t)ROW_WARPS * WIDE_WARP_BYTES;
 // windows with the accumulator in shared memory: tile columns and entries
 constexpr int WS_W = 512, WS_E = 512;
-// Wide rows with more A entries than LONG_NA are cut into parts of at most
-// WIDE_W tile columns, each part one warp's work anywhere on the GPU
-// (k_long_walk); their B rows' cut points come from a table built once.
-constexpr int LONG_NA = 32;
-constexpr int LONG_MINP = 16;        // parts of such a row at least (more warps than the per-row kernel's 8)
+// Wide rows with more A entries than LONG_NA (all of them, measured
+// fastest) are cut into parts of at most WIDE_W tile columns, each part one
+// warp's work anywhere on the GPU (k_long_walk); their B rows' cut points
+// come from a table built once.
+constexpr int LONG_NA = 0;
+constexpr int LONG_MINP = 32;        // parts of such a row at least (more warps than the per-row kernel's 8)
 constexpr int LONG_GRID = 152 * 4;   // CTAs of the part walk: four per SM
 constexpr long long LONG_TAB_MAX = 1ll << 30;   // cut-table entries (4 GB) beyond which long rows stay per row
 static_assert(4 * WS_W + 8 * WS_E <= WIDE_WARP_BYTES, "shared-memory windows fit the warp's share");
