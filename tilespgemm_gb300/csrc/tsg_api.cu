@@ -453,7 +453,7 @@ tsg_status plan_symbolic(tsg_ctx *ctx, Pool &pool, Scratch &sc, tsg_op op, const
     P.blkm = TA.blkm;
     P.crp = P.own<long long>(pool, P.blkm + 1);
     int *cnt = sc.get<int>(P.blkm + 1);
-    int *wide = sc.get<int>(P.blkm + 1);
+    int *wide = sc.get<int>(P.blkm + 2);
     int *defer = sc.get<int>(P.blkm + 1);
     if (!P.crp || !cnt || !wide || !defer) return fail(TSG_ERR_OOM, "device pool allocation failed (step 1)");
     CUDA_OK(cudaMemsetAsync(defer + P.blkm, 0, sizeof(int), ctx->stream));

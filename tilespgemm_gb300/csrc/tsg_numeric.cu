@@ -622,21 +622,32 @@ k_global_prep(NumericArgs g, int cls, long long nrows)
     const long long c0 = g.crp[i];
     const int S = (int)(g.crp[i + 1] - c0);
     const long long Rb = g.rowptrC[R];
+    const uint16_t *mrow = g.cmask + c0 * TILE + (long long)r * S;
     long long run = 0;
-    for (int sb = 0; sb < S; sb += 32) {
-        const int s = sb + lane;
-        unsigned mk = (s < S) ? (unsigned)g.cmask[c0 * TILE + (long long)r * S + s] : 0u;
-        const int c = __popc(mk);
-        const int incl = warp_incl_scan(c, lane);
-        long long dst = Rb + run + incl - c;
-        const int jb = (s < S) ? g.ccol[c0 + s] * TILE - cshift : 0;
-        while (mk) {
-            const int b = 31 - __clz(mk);
-            g.colC[dst] = jb + (TILE - 1 - b);
-            ++dst;
-            mk &= ~(1u << b);
+    // 128 slots per round: all their loads issued before any is used
+    for (int sb = 0; sb < S; sb += 128) {
+        unsigned mkv[4];
+        int jbv[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int s = sb + 32 * u + lane;
+            mkv[u] = s < S ? (unsigned)mrow[s] : 0u;
+            jbv[u] = s < S ? g.ccol[c0 + s] * TILE - cshift : 0;
         }
-        run += __shfl_sync(0xffffffffu, incl, 31);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            unsigned mk = mkv[u];
+            const int c = __popc(mk);
+            const int incl = warp_incl_scan(c, lane);
+            long long dst = Rb + run + incl - c;
+            while (mk) {
+                const int b = 31 - __clz(mk);
+                g.colC[dst] = jbv[u] + (TILE - 1 - b);
+                ++dst;
+                mk &= ~(1u << b);
+            }
+            run += __shfl_sync(0xffffffffu, incl, 31);
+        }
     }
 }
 

@@ -521,7 +521,7 @@ __device__ __forceinline__ long long block_reduce_sum_ll(long long v, long long 
 template <class KS, bool FILL, bool MASK, typename TP>
 __global__ void __launch_bounds__(WIDE_THREADS)
 k_union_wide(typename KS::Params P, const int *wide_list, const int *wide_n, int *cnt, int *stat_max,
-             const TP *rowptr, int *out, uint16_t *mask)
+             const TP *rowptr, int *out, uint16_t *mask, int *next)
 {
     extern __shared__ unsigned s_dyn[];
     unsigned *bm = s_dyn;
@@ -531,7 +531,13 @@ k_union_wide(typename KS::Params P, const int *wide_list, const int *wide_n, int
     __shared__ int s_wsum[WIDE_THREADS / 32];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int nw = *wide_n;
-    for (int wi = blockIdx.x; wi < nw; wi += gridDim.x) {
+    __shared__ int s_next;
+    // each CTA takes the next wide tile-row from a counter (their costs differ widely)
+    for (;;) {
+        if (tid == 0) s_next = atomicAdd(next, 1);
+        __syncthreads();
+        const int wi = s_next;
+        if (wi >= nw) break;
         const int row = wide_list[wi];
         KS ks(P, row);
         int kmin = INT_MAX, kmax = -1;
@@ -754,9 +760,26 @@ inline unsigned grid_for(long long n, int threads, long long cap = 152ll * 32) {
     return (unsigned)g;
 }
 
-// Count (+ scan into rowptr_out) and/or fill.  `wide` (nrows+1 ints: the
-// list of rows too wide for one warp, then its length) is written by the
-// count pass and read by the fill pass, so the two may be separate calls.
+// the wide kernel over the list; its work counter is the int after the
+// list's length (wide_n[1]), zeroed here
+template <class KS, bool FILL, bool MASK, typename TP>
+cudaError_t launch_union_wide(Pool &pool, typename KS::Params P, const int *wide, int *wide_n, int *cnt,
+                              int *stat, const TP *rowptr, int *out, uint16_t *mask)
+{
+    cudaError_t e = cudaMemsetAsync(wide_n + 1, 0, sizeof(int), pool.stream);
+    if (e == cudaSuccess) {
+        k_union_wide<KS, FILL, MASK, TP><<<WIDE_GRID, WIDE_THREADS, WIDE_SMEM, pool.stream>>>(P, wide, wide_n, cnt, stat,
+                                                                                          rowptr, out, mask, wide_n + 1);
+        ::tsg::count_launch();
+        e = cudaGetLastError();
+    }
+    return e;
+}
+
+// Count (+ scan into rowptr_out) and/or fill.  `wide` (nrows+2 ints: the
+// list of rows too wide for one warp, its length, and the wide kernel's work
+// counter) is written by the count pass and read by the fill pass, so the
+// two may be separate calls.
 template <class KS, typename TP>
 cudaError_t union_structure(Pool &pool, typename KS::Params P, int nrows, int *cnt_scratch, int *wide,
                             TP *rowptr_out, int *out_cols, uint16_t *mask, int *flags, int *stat,
@@ -773,20 +796,19 @@ cudaError_t union_structure(Pool &pool, typename KS::Params P, int nrows, int *c
         if (nrows > 0) {
             { k_union_count<KS><<<g, WPC * 32, 0, s>>>(P, nrows, cnt_scratch, wide, wide_n, stat, defer,
                                                       defer ? defer + nrows : nullptr, defer_S); ::tsg::count_launch(); }
-            { k_union_wide<KS, false, false, TP><<<WIDE_GRID, WIDE_THREADS, WIDE_SMEM, s>>>(
-                P, wide, wide_n, cnt_scratch, stat, nullptr, nullptr, nullptr); ::tsg::count_launch(); }
+            e = launch_union_wide<KS, false, false, TP>(pool, P, wide, wide_n, cnt_scratch, stat, nullptr, nullptr,
+                                                        nullptr);
         }
-        e = scan(pool, cnt_scratch, rowptr_out, nrows, flags);
+        if (e == cudaSuccess) e = scan(pool, cnt_scratch, rowptr_out, nrows, flags);
     }
     if (e == cudaSuccess && do_fill && nrows > 0 && out_cols) {
         if (mask) {
             { k_union_fill<KS, true, TP><<<g, WPC * 32, 0, s>>>(P, nrows, rowptr_out, out_cols, mask); ::tsg::count_launch(); }
-            { k_union_wide<KS, true, true, TP><<<WIDE_GRID, WIDE_THREADS, WIDE_SMEM, s>>>(
-                P, wide, wide_n, nullptr, nullptr, rowptr_out, out_cols, mask); ::tsg::count_launch(); }
+            e = launch_union_wide<KS, true, true, TP>(pool, P, wide, wide_n, nullptr, nullptr, rowptr_out, out_cols, mask);
         } else {
             { k_union_fill<KS, false, TP><<<g, WPC * 32, 0, s>>>(P, nrows, rowptr_out, out_cols, nullptr); ::tsg::count_launch(); }
-            { k_union_wide<KS, true, false, TP><<<WIDE_GRID, WIDE_THREADS, WIDE_SMEM, s>>>(
-                P, wide, wide_n, nullptr, nullptr, rowptr_out, out_cols, nullptr); ::tsg::count_launch(); }
+            e = launch_union_wide<KS, true, false, TP>(pool, P, wide, wide_n, nullptr, nullptr, rowptr_out, out_cols,
+                                                       nullptr);
         }
     }
     if (e == cudaSuccess) e = cudaGetLastError();
@@ -830,7 +852,7 @@ cudaError_t csr_to_tile_structure(Pool &pool, const long long *rp, const int *co
                                   int *flags, int *stat)
 {
     int *cnt = pool.alloc_n<int>(T.blkm + 1);
-    int *wide = pool.alloc_n<int>(T.blkm + 1);
+    int *wide = pool.alloc_n<int>(T.blkm + 2);
     cudaError_t e = (cnt && wide) ? cudaSuccess : pool.err;
     CsrKeys::Params P{rp, col, T.m, T.n};
     if (e == cudaSuccess)
@@ -842,7 +864,7 @@ cudaError_t csr_to_tile_structure(Pool &pool, const long long *rp, const int *co
 }
 
 // Step 1: C's tile-row pointer (crp, int64; count pass) and C's sorted tile
-// columns (fill pass, ccol).  cnt and wide (blkm+1 ints each) carry state
+// columns (fill pass, ccol).  cnt and wide (blkm+1 and blkm+2 ints) carry state
 // from the count pass to the fill pass; stat[0] gets the largest tile count
 // of a tile-row and stat[1] the widest tile-column window.
 // defer (blkm+1 ints, count pass only): the tile-rows the fused warp kernel
@@ -925,9 +947,11 @@ cudaError_t symbolic_fill_fused(Pool &pool, const TileCSR &A, const TileCSR &B, 
                                                                          cmask, rowcnt, bin, bp, binstat, binlist, rowlist, flags,
                                                                          erpB, ecolB, erpA, ecolA); ::tsg::count_launch(); }
     (void)cnt;
-    { k_union_wide<UnionKeys, true, false, long long><<<WIDE_GRID, WIDE_THREADS, WIDE_SMEM, s>>>(
-        P, wide, wide + A.blkm, nullptr, nullptr, crp, ccol, nullptr); ::tsg::count_launch(); }
-    return cudaGetLastError();
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess)
+        e = launch_union_wide<UnionKeys, true, false, long long>(pool, P, wide, wide + A.blkm, nullptr, nullptr, crp, ccol,
+                                                                 nullptr);
+    return e;
 }
 
 cudaError_t masks_to_tile_major_i32(Pool &pool, int blkm, const int *rowptr, const uint16_t *src, uint16_t *dst)
