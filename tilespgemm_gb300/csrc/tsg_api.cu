@@ -110,6 +110,8 @@ struct tsg_ctx {
     std::multimap<size_t, void *> pinned_cache;
     size_t pinned_cached = 0;        // bytes held by pinned_cache
     cudaEvent_t ev[8] = {};
+    cudaStream_t side = nullptr;     // second stream for kernels that overlap the main one's (fork/join by events)
+    cudaEvent_t fork = nullptr, join = nullptr;
 };
 
 namespace {
@@ -497,7 +499,7 @@ tsg_status plan_symbolic(tsg_ctx *ctx, Pool &pool, Scratch &sc, tsg_op op, const
     tm.mark();  // 2
     CUDA_OK(step2_masks(pool, TA, TB, P.m, P.blkm, P.crp, P.ccol, P.cmask, rowcnt, maxS, maxSpan, bp, P.bin,
                         ctx->dstat + ST_BINS, P.binlist, P.rowlist, ctx->dflags, defer, ndefer, P.rpB, P.colB,
-                        P.rpA, P.colA, P.b_increasing));
+                        P.rpA, P.colA, P.b_increasing, ctx->side, ctx->fork, ctx->join));
     CUDA_OK(scan_i32_to_i64(pool, rowcnt, P.rowptrC, P.m, ctx->dflags));
     CUDA_OK(cudaMemcpyAsync(ctx->dstat + ST_NNZC, P.rowptrC + P.m, sizeof(long long), cudaMemcpyDeviceToDevice,
                             ctx->stream));
@@ -695,8 +697,12 @@ tsg_status tsg_create(tsg_ctx **out, int device, const tsg_opts *opts)
     if (c->opts.threads_numeric != 128 && c->opts.threads_numeric != 256 && c->opts.threads_numeric != 512)
         c->opts.threads_numeric = 256;
     auto cleanup = [&](tsg_status st) { tsg_destroy(c); return st; };
-    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess)
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess)
         return cleanup(fail(TSG_ERR_CUDA, "cudaStreamCreate failed"));
+    if (cudaEventCreateWithFlags(&c->fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->join, cudaEventDisableTiming) != cudaSuccess)
+        return cleanup(fail(TSG_ERR_CUDA, "cudaEventCreate failed"));
     cudaMemPoolProps props{};
     props.allocType = cudaMemAllocationTypePinned;
     props.handleTypes = cudaMemHandleTypeNone;
@@ -729,6 +735,9 @@ tsg_status tsg_destroy(tsg_ctx *c)
     c->pinned_cache.clear();
     c->pinned_cached = 0;
     for (auto &e : c->ev) if (e) cudaEventDestroy(e);
+    if (c->fork) cudaEventDestroy(c->fork);
+    if (c->join) cudaEventDestroy(c->join);
+    if (c->side) { cudaStreamSynchronize(c->side); cudaStreamDestroy(c->side); }
     if (c->dflags) cudaFree(c->dflags);
     if (c->dstat) cudaFree(c->dstat);
     if (c->hstat) cudaFreeHost(c->hstat);

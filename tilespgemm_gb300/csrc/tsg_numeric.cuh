@@ -171,7 +171,8 @@ cudaError_t step2_masks(Pool &pool, const TileCSR &A, const TileCSR &B, int m, i
                         const int *ccol, uint16_t *cmask, int *rowcnt, int max_tiles_per_row, int max_span,
                         const NumericBinParams &bp, unsigned char *bin, long long *binstat, int *binlist,
                         int *rowlist, int *flags, const int *defer_list, int ndefer, const long long *erpB,
-                        const int *ecolB, const long long *erpA, const int *ecolA, bool b_sorted);
+                        const int *ecolB, const long long *erpA, const int *ecolA, bool b_sorted,
+                        cudaStream_t side, cudaEvent_t fork, cudaEvent_t join);
 
 // Launch the numeric kernels of every non-empty bin and row class.
 // binstat is step 2's statistics (layout above), copied to the host.

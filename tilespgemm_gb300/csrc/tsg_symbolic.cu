@@ -578,11 +578,29 @@ cudaError_t step2_masks(Pool &pool, const TileCSR &A, const TileCSR &B, int m, i
                         const int *ccol, uint16_t *cmask, int *rowcnt, int max_tiles_per_row, int max_span,
                         const NumericBinParams &bp, unsigned char *bin, long long *binstat, int *binlist,
                         int *rowlist, int *flags, const int *defer_list, int ndefer, const long long *erpB,
-                        const int *ecolB, const long long *erpA, const int *ecolA, bool b_sorted)
+                        const int *ecolB, const long long *erpA, const int *ecolA, bool b_sorted,
+                        cudaStream_t side, cudaEvent_t fork, cudaEvent_t join)
 {
     cudaStream_t s = pool.stream;
     if (blkm <= 0 || ndefer <= 0) return cudaSuccess;
     const int map_cap = max_span < (int)MAP_MAX ? max_span : (int)MAP_MAX;
+    // the windowed kernel takes few, long tile-rows: it runs on the side
+    // stream beside the other classes (disjoint tile-rows) and is joined at
+    // the end, so its CTAs do not leave the rest of the GPU idle
+    const bool win = max_tiles_per_row > S2_SMAX;
+    if (win) {
+        cudaError_t e = cudaEventRecord(fork, s);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(side, fork, 0);
+        if (e == cudaSuccess) {
+            k_step2_win<512><<<ndefer, 512, step2_smem(S2W_WIN, MAP_MAX), side>>>(blkm, m, A.trp, A.tcol, A.mask, B.trp, B.tcol,
+                                                      B.mask, crp, ccol, cmask, rowcnt, S2_SMAX, S2W_WIN, bp, bin, binstat, binlist,
+                                                      rowlist, flags, defer_list, erpB, ecolB, erpA);
+            ::tsg::count_launch();
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) e = cudaEventRecord(join, side);
+        if (e != cudaSuccess) return e;
+    }
     {
         const int slots = max_tiles_per_row < S2_SMALL ? max_tiles_per_row : S2_SMALL;
         { k_step2<256><<<ndefer, 256, step2_smem(slots, map_cap), s>>>(blkm, m, A.trp, A.tcol, A.mask, B.trp, B.tcol, B.mask, crp, ccol,
@@ -603,10 +621,9 @@ cudaError_t step2_masks(Pool &pool, const TileCSR &A, const TileCSR &B, int m, i
                                                    S2E_WIN, wmap, bp, bin, binstat, binlist, rowlist, flags, defer_list,
                                                    erpB, ecolB, erpA, ecolA, b_sorted ? 1 : 0); ::tsg::count_launch(); }
     }
-    if (max_tiles_per_row > S2_SMAX) {
-        { k_step2_win<512><<<ndefer, 512, step2_smem(S2W_WIN, MAP_MAX), s>>>(blkm, m, A.trp, A.tcol, A.mask, B.trp, B.tcol, B.mask, crp, ccol,
-                                                      cmask, rowcnt, S2_SMAX, S2W_WIN, bp, bin, binstat, binlist, rowlist, flags, defer_list,
-                                                      erpB, ecolB, erpA); ::tsg::count_launch(); }
+    if (win) {
+        const cudaError_t e = cudaStreamWaitEvent(s, join, 0);
+        if (e != cudaSuccess) return e;
     }
     return cudaGetLastError();
 }
