@@ -537,7 +537,7 @@ tsg_status plan_numeric(tsg_ctx *ctx, Pool &pool, PlanData &P, const double *val
     else if (walk == 3) kw = 2;
     else if (walk == 0 && P.nnzC > 0 && P.k > 0 &&
              (double)P.nnzA * ((double)P.nnzB / P.k) < 3.0 * (double)P.nnzC) kw = 2;
-    CUDA_OK(numeric_run(pool, na, P.bstat, kw, threads, ctx->opts.row_warps));
+    CUDA_OK(numeric_run(pool, na, P.bstat, kw, threads, ctx->opts.row_warps, ctx->side, ctx->fork, ctx->join));
     return TSG_OK;
 }
 

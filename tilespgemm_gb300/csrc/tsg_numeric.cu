@@ -1220,12 +1220,22 @@ cudaError_t long_prepare(Pool &pool, const NumericArgs &a, int cls, long long n,
 }  // namespace
 
 cudaError_t numeric_run(Pool &pool, const NumericArgs &a, const long long *binstat, int walk, int threads,
-                        int row_warps)
+                        int row_warps, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join)
 {
     const bool packed = walk == 1;
     const long long *counts = binstat, *req = binstat + NBIN;
-    cudaStream_t s = pool.stream;
+    const long long *rcnt = binstat + BS_ROWCNT, *rreq = binstat + BS_ROWREQ;
     cudaError_t e = cudaSuccess;
+    // with wide rows, the tile-row bins and the shared-memory row classes run
+    // on the side stream beside them (disjoint rows of C), joined at the end
+    const bool split = side && (rcnt[ROW_WIDE] > 0 || rcnt[ROW_WIDE1] > 0);
+    cudaStream_t s = pool.stream;
+    if (split) {
+        e = cudaEventRecord(fork, pool.stream);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(side, fork, 0);
+        if (e != cudaSuccess) return e;
+        s = side;
+    }
     for (int b = BIN_SPARSE_S; b <= BIN_DENSE_L && e == cudaSuccess; ++b) {
         if (counts[b] == 0) continue;
         const bool dense = b >= BIN_DENSE_S;
@@ -1236,7 +1246,6 @@ cudaError_t numeric_run(Pool &pool, const NumericArgs &a, const long long *binst
         else if (nt == 512) e = launch_smem<512>(a, b, counts[b], smem, dense, walk, s);
         else e = launch_smem<256>(a, b, counts[b], smem, dense, walk, s);
     }
-    const long long *rcnt = binstat + BS_ROWCNT, *rreq = binstat + BS_ROWREQ;
     for (int c = ROW_S; c <= ROW_M && e == cudaSuccess; ++c) {
         if (rcnt[c] == 0) continue;
         const unsigned g = (unsigned)rcnt[c];
@@ -1250,6 +1259,10 @@ cudaError_t numeric_run(Pool &pool, const NumericArgs &a, const long long *binst
     if (e == cudaSuccess && rcnt[ROW_L] > 0) {
         { k_numeric_rows_split<ROW_WARPS><<<(unsigned)rcnt[ROW_L], ROW_WARPS * 32, (size_t)rreq[ROW_L], s>>>(a, ROW_L, packed); ::tsg::count_launch(); }
         e = cudaGetLastError();
+    }
+    if (split) {
+        if (e == cudaSuccess) e = cudaEventRecord(join, side);
+        s = pool.stream;
     }
     for (int c = ROW_WIDE; c <= ROW_WIDE1 && e == cudaSuccess; ++c) {
         const long long n = rcnt[c];
@@ -1276,6 +1289,7 @@ cudaError_t numeric_run(Pool &pool, const NumericArgs &a, const long long *binst
         }
         e = cudaGetLastError();
     }
+    if (split && e == cudaSuccess) e = cudaStreamWaitEvent(pool.stream, join, 0);
     return e;
 }
 

@@ -179,8 +179,11 @@ cudaError_t step2_masks(Pool &pool, const TileCSR &A, const TileCSR &B, int m, i
 // walk: 0 lanes over one B row per A entry, 1 packed (repeated B columns),
 // 2 as 0 with B loads one step ahead (tile-row kernels); row_warps: warps
 // per row for the shared-memory row classes ROW_S / ROW_M (1, 2 or 4)
+// side/fork/join: a second stream and two events; with wide rows the other
+// classes run there concurrently (side may be null: one stream)
 cudaError_t numeric_run(Pool &pool, const NumericArgs &a, const long long *binstat, int walk, int threads,
-                        int row_warps);
+                        int row_warps, cudaStream_t side = nullptr, cudaEvent_t fork = nullptr,
+                        cudaEvent_t join = nullptr);
 
 cudaError_t symbolic_fill_fused(Pool &pool, const TileCSR &A, const TileCSR &B, int m, const long long *crp,
                                 int *ccol, uint16_t *cmask, int *rowcnt, unsigned char *bin,
