@@ -22,6 +22,7 @@
 #include <map>
 #include <mutex>
 #include <string>
+#include <unistd.h>
 #include <vector>
 
 namespace tsg {
@@ -107,9 +108,8 @@ struct tsg_ctx {
     long long *dstat = nullptr;      // 64 slots
     long long *hstat = nullptr;      // pinned mirror: 64 stat slots + FLAG_COUNT flags (as long long)
     std::mutex mu;
-    std::multimap<size_t, void *> pinned_cache;
-    size_t pinned_cached = 0;        // bytes held by pinned_cache
     cudaEvent_t ev[8] = {};
+    bool counted = false;            // entered in the pinned cache's count of live contexts
     cudaStream_t side = nullptr;     // second stream for kernels that overlap the main one's (fork/join by events)
     cudaEvent_t fork = nullptr, join = nullptr;
 };
@@ -135,16 +135,48 @@ struct OutOwner {
 };
 constexpr int OWN_MALLOC = 2;
 
+// Pinned host buffers (host outputs, staging) kept for reuse by all
+// contexts of the process: pinning fresh pages runs at about 13 GB/s on the
+// Grace host against ~190 GB/s for the copy itself, so a served stream of
+// large outputs is bound by pinning unless buffers come back.  At most
+// pinned_cap() bytes are kept (the largest are freed beyond it); the cache
+// is emptied when the last context is destroyed.
+struct PinnedCache {
+    std::mutex mu;
+    std::multimap<size_t, void *> bufs;
+    size_t bytes = 0;
+    int live_contexts = 0;
+};
+
+PinnedCache &pinned_cache()
+{
+    static PinnedCache c;
+    return c;
+}
+
+// min(48 GB, a quarter of the host's memory)
+size_t pinned_cap()
+{
+    static const size_t cap = [] {
+        const long pages = sysconf(_SC_PHYS_PAGES), psz = sysconf(_SC_PAGE_SIZE);
+        const size_t ram = (pages > 0 && psz > 0) ? (size_t)pages * (size_t)psz : (size_t)16 << 30;
+        return std::min<size_t>((size_t)48 << 30, ram / 4);
+    }();
+    return cap;
+}
+
 void *pinned_get(tsg_ctx *ctx, size_t bytes)
 {
+    (void)ctx;
     if (bytes == 0) bytes = 16;
+    PinnedCache &pc = pinned_cache();
     {
-        std::lock_guard<std::mutex> lk(ctx->mu);
-        auto it = ctx->pinned_cache.lower_bound(bytes);
-        if (it != ctx->pinned_cache.end() && it->first <= bytes + bytes / 4 + (1 << 20)) {
+        std::lock_guard<std::mutex> lk(pc.mu);
+        auto it = pc.bufs.lower_bound(bytes);
+        if (it != pc.bufs.end() && it->first <= bytes + bytes / 4 + (1 << 20)) {
             void *p = it->second;
-            ctx->pinned_cached -= it->first;
-            ctx->pinned_cache.erase(it);
+            pc.bytes -= it->first;
+            pc.bufs.erase(it);
             return p;
         }
     }
@@ -153,25 +185,48 @@ void *pinned_get(tsg_ctx *ctx, size_t bytes)
     return p;
 }
 
-// Pinned buffers a context keeps for reuse, at most this many bytes: beyond
-// it the largest cached buffers are freed (outputs of very different sizes
-// would otherwise pile up in host memory).
-constexpr size_t PINNED_CACHE_MAX = 4ull << 30;
-
 void pinned_put(tsg_ctx *ctx, void *p, size_t bytes)
 {
+    (void)ctx;
     if (bytes == 0) bytes = 16;
+    PinnedCache &pc = pinned_cache();
     std::vector<void *> drop;
     {
-        std::lock_guard<std::mutex> lk(ctx->mu);
-        ctx->pinned_cache.emplace(bytes, p);
-        ctx->pinned_cached += bytes;
-        while (ctx->pinned_cached > PINNED_CACHE_MAX && !ctx->pinned_cache.empty()) {
-            auto last = std::prev(ctx->pinned_cache.end());
-            ctx->pinned_cached -= last->first;
-            drop.push_back(last->second);
-            ctx->pinned_cache.erase(last);
+        std::lock_guard<std::mutex> lk(pc.mu);
+        if (pc.live_contexts <= 0) {   // freed after the last context: nothing left to reuse it
+            drop.push_back(p);
+            p = nullptr;
+        } else {
+            pc.bufs.emplace(bytes, p);
+            pc.bytes += bytes;
         }
+        while (pc.bytes > pinned_cap() && !pc.bufs.empty()) {
+            auto last = std::prev(pc.bufs.end());
+            pc.bytes -= last->first;
+            drop.push_back(last->second);
+            pc.bufs.erase(last);
+        }
+    }
+    for (void *q : drop) cudaFreeHost(q);
+}
+
+void pinned_context_enter()
+{
+    PinnedCache &pc = pinned_cache();
+    std::lock_guard<std::mutex> lk(pc.mu);
+    ++pc.live_contexts;
+}
+
+void pinned_context_leave()
+{
+    PinnedCache &pc = pinned_cache();
+    std::vector<void *> drop;
+    {
+        std::lock_guard<std::mutex> lk(pc.mu);
+        if (--pc.live_contexts > 0) return;
+        for (auto &kv : pc.bufs) drop.push_back(kv.second);
+        pc.bufs.clear();
+        pc.bytes = 0;
     }
     for (void *q : drop) cudaFreeHost(q);
 }
@@ -692,6 +747,8 @@ tsg_status tsg_create(tsg_ctx **out, int device, const tsg_opts *opts)
         return fail(TSG_ERR_NOT_SUPPORTED, "device %d is sm_%d%d; this library is built for sm_103a (GB300) only", device, major, minor);
     tsg_ctx *c = new tsg_ctx();
     c->device = device;
+    pinned_context_enter();
+    c->counted = true;
     tsg_opts_default(&c->opts);
     if (opts) c->opts = *opts;
     if (c->opts.threads_numeric != 128 && c->opts.threads_numeric != 256 && c->opts.threads_numeric != 512)
@@ -731,9 +788,7 @@ tsg_status tsg_destroy(tsg_ctx *c)
     if (!c) return TSG_OK;
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
-    for (auto &kv : c->pinned_cache) cudaFreeHost(kv.second);
-    c->pinned_cache.clear();
-    c->pinned_cached = 0;
+    if (c->counted) pinned_context_leave();
     for (auto &e : c->ev) if (e) cudaEventDestroy(e);
     if (c->fork) cudaEventDestroy(c->fork);
     if (c->join) cudaEventDestroy(c->join);
