@@ -651,19 +651,20 @@ k_global_prep(NumericArgs g, int cls, long long nrows)
     }
 }
 
-constexpr int WIDE_W = 1024;   // tile columns per window of the wide-row kernel (accumulator in C)
+constexpr int WIDE_W = 512;    // tile columns per window of the wide-row kernels (accumulator in C)
 constexpr int WIDE_WARP_BYTES = WIDE_W * (4 + 2);   // shared memory per warp
 constexpr size_t WIDE_SMEM = (size_t)ROW_WARPS * WIDE_WARP_BYTES;
 // windows with the accumulator in shared memory: tile columns and entries
-constexpr int WS_W = 512, WS_E = 512;
+constexpr int WS_W = 256, WS_E = 256;
 // Wide rows with more A entries than LONG_NA (all of them, measured
 // fastest) are cut into parts of at most WIDE_W tile columns, each part one
 // warp's work anywhere on the GPU (k_long_walk); their B rows' cut points
 // come from a table built once.
 constexpr int LONG_NA = 0;
 constexpr int LONG_MINP = 32;        // parts of such a row at least (more warps than the per-row kernel's 8)
-constexpr int LONG_GRID = 152 * 4;   // CTAs of the part walk: four per SM
-constexpr long long LONG_TAB_MAX = 1ll << 30;   // cut-table entries (4 GB) beyond which long rows stay per row
+constexpr int LONG_GRID = 152 * 5;   // CTAs of the part walk: five per SM
+constexpr int LONG_MIN_TILES = 1024; // C's tile columns from which wide rows take the parts path
+constexpr long long LONG_TAB_MAX = 1ll << 31;   // cut-table entries (8 GB) beyond which long rows stay per row
 static_assert(4 * WS_W + 8 * WS_E <= WIDE_WARP_BYTES, "shared-memory windows fit the warp's share");
 
 // A wide row's share [t0, t1) of tile columns, for A rows of up to 32
@@ -999,7 +1000,7 @@ k_long_cuts(NumericArgs g, long long nrows, const int *lrow, const unsigned char
 // the walk: each warp takes the next part from a counter until none is
 // left (parts differ widely in cost, so a static share would leave warps
 // idle behind the hub rows' parts)
-__global__ void __launch_bounds__(ROW_WARPS * 32, 4)
+__global__ void __launch_bounds__(ROW_WARPS * 32, 5)
 k_long_walk(NumericArgs g, long long nrows, const int *lrow, const unsigned char *lfit, const int *part_off,
             const long long *tab_off, const int *tab, unsigned long long *next_part)
 {
@@ -1273,9 +1274,13 @@ cudaError_t numeric_run(Pool &pool, const NumericArgs &a, const long long *binst
         // cut table gets at most LONG_TAB_MAX entries (rows past it stay
         // with k_numeric_wide)
         const long long pmax = std::max<long long>(((long long)(a.n + TILE - 1) / TILE + WIDE_W - 1) / WIDE_W, LONG_MINP);
-        const long long tab_bound = std::min<long long>(LONG_TAB_MAX, a.nnzA * (pmax + 1));
+        // ... and at most a quarter of the device's free memory
+        size_t free_b = 0, total_b = 0;
+        long long tab_cap = LONG_TAB_MAX;
+        if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess) tab_cap = std::min<long long>(tab_cap, (long long)(free_b / 16));
+        const long long tab_bound = std::min<long long>(tab_cap, a.nnzA * (pmax + 1));
         const bool parts = c == ROW_WIDE && a.b_sorted && !packed &&
-                           ((long long)a.n + TILE - 1) / TILE >= WIDE_W;
+                           ((long long)a.n + TILE - 1) / TILE >= LONG_MIN_TILES;
         LongScratch L{};
         if (parts) {
             e = long_prepare(pool, a, c, n, tab_bound, L);
