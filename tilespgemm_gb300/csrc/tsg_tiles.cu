@@ -42,6 +42,7 @@ constexpr int WIDE_SMEM = WIDE_WORDS * 4 * 2;  // bitmap + word prefix
 
 // Tile columns of the entries of one tile-row of a CSR matrix.
 struct CsrKeys {
+    static constexpr bool kHasOrRange = false;
     struct Params { const long long *rp; const int *col; int m, n; };
     const long long *rp; const int *col; int n, r0, r1;
     __device__ CsrKeys(const Params &p, int row)
@@ -71,6 +72,7 @@ struct CsrKeys {
 
 // Tile columns of C's tile-row i: union over A's tiles (i,k) of B's tile-row k.
 struct UnionKeys {
+    static constexpr bool kHasOrRange = true;
     struct Params {
         const int *arp; const int *acol; const int *brp; const int *bcol;
         const long long *bmoff = nullptr; const unsigned *bmw = nullptr;   // B's tile-row bitmaps, if built
@@ -90,6 +92,34 @@ struct UnionKeys {
             int k = acol[a];
             const int q1 = brp[k + 1];
             for (int q = brp[k] + start; q < q1; q += stride) f(bcol[q], 0, 0);
+        }
+    }
+    // CTA-wide: OR the keys in [c0, c0 + span) (c0 a multiple of 32) into bm
+    // (bit o stands for key c0 + o); warps take A tiles, and per A tile B's
+    // tile-row bitmap goes in word by word when it has fewer words than keys
+    __device__ void or_range(unsigned *bm, long long c0, long long span, int warp, int nwarps, int lane) const {
+        const int a0 = arp[i], a1 = arp[i + 1];
+        for (int a = a0 + warp; a < a1; a += nwarps) {
+            const int k = acol[a];
+            const int q0 = brp[k], q1 = brp[k + 1];
+            if (q1 <= q0) continue;
+            long long w0 = 0, w1 = 0;
+            if (bmoff) { w0 = bmoff[k]; w1 = bmoff[k + 1]; }
+            if (w1 > w0 && w1 - w0 < q1 - q0) {
+                const long long base = (long long)(bcol[q0] & ~31) - c0;   // bit 0 of word w0, relative to c0
+                for (long long w = w0 + lane; w < w1; w += 32) {
+                    const long long o = base + ((w - w0) << 5);
+                    if (o >= 0 && o < span) {
+                        const unsigned x = bmw[w];
+                        if (x) atomicOr(&bm[o >> 5], x);
+                    }
+                }
+            } else {
+                for (int q = q0 + lane; q < q1; q += 32) {
+                    const long long o = (long long)bcol[q] - c0;
+                    if (o >= 0 && o < span) atomicOr(&bm[o >> 5], 1u << (o & 31));
+                }
+            }
         }
     }
     // OR the keys into a warp's bitmap bm whose bit o stands for key kbase+o
@@ -555,15 +585,20 @@ k_union_wide(typename KS::Params P, const int *wide_list, const int *wide_n, int
             }
         }
         long long run = 0;
-        for (long long c0 = kmin; c0 <= kmax; c0 += (long long)WIDE_WORDS * 32) {
+        // chunks start on a multiple of 32 so that B's bitmap words align
+        for (long long c0 = kmin & ~31ll; c0 <= kmax; c0 += (long long)WIDE_WORDS * 32) {
             const long long span = min((long long)WIDE_WORDS * 32, (long long)kmax - c0 + 1);
             const int nwords = (int)((span + 31) >> 5);
             for (int w = tid; w < nwords; w += WIDE_THREADS) bm[w] = 0;
             __syncthreads();
-            ks.each(tid, WIDE_THREADS, [&](int key, int, int) {
-                long long o = (long long)key - c0;
-                if (o >= 0 && o < span) atomicOr(&bm[o >> 5], 1u << (o & 31));
-            });
+            if constexpr (KS::kHasOrRange) {
+                ks.or_range(bm, c0, span, warp, WIDE_THREADS / 32, lane);
+            } else {
+                ks.each(tid, WIDE_THREADS, [&](int key, int, int) {
+                    long long o = (long long)key - c0;
+                    if (o >= 0 && o < span) atomicOr(&bm[o >> 5], 1u << (o & 31));
+                });
+            }
             __syncthreads();
             const int wpt = (nwords + WIDE_THREADS - 1) / WIDE_THREADS;
             const int w0 = min(nwords, tid * wpt), w1 = min(nwords, w0 + wpt);
