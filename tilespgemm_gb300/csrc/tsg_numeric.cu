@@ -1227,9 +1227,14 @@ cudaError_t numeric_run(Pool &pool, const NumericArgs &a, const long long *binst
     const long long *counts = binstat, *req = binstat + NBIN;
     const long long *rcnt = binstat + BS_ROWCNT, *rreq = binstat + BS_ROWREQ;
     cudaError_t e = cudaSuccess;
-    // with wide rows, the tile-row bins and the shared-memory row classes run
-    // on the side stream beside them (disjoint rows of C), joined at the end
-    const bool split = side && (rcnt[ROW_WIDE] > 0 || rcnt[ROW_WIDE1] > 0);
+    // two streams when there are rows besides the tile-row bins' (disjoint
+    // rows of C, joined at the end): the bins -- and, with wide rows, the
+    // shared-memory row classes -- run on the side stream
+    const bool wide = rcnt[ROW_WIDE] > 0 || rcnt[ROW_WIDE1] > 0;
+    const bool rows = rcnt[ROW_S] > 0 || rcnt[ROW_M] > 0 || rcnt[ROW_L] > 0;
+    bool bins = false;
+    for (int b = BIN_SPARSE_S; b <= BIN_DENSE_L; ++b) bins = bins || counts[b] > 0;
+    const bool split = side && (wide || (rows && bins));
     cudaStream_t s = pool.stream;
     if (split) {
         e = cudaEventRecord(fork, pool.stream);
@@ -1247,6 +1252,10 @@ cudaError_t numeric_run(Pool &pool, const NumericArgs &a, const long long *binst
         else if (nt == 512) e = launch_smem<512>(a, b, counts[b], smem, dense, walk, s);
         else e = launch_smem<256>(a, b, counts[b], smem, dense, walk, s);
     }
+    if (split && !wide) {   // the row classes on the main stream beside the bins
+        if (e == cudaSuccess) e = cudaEventRecord(join, side);
+        s = pool.stream;
+    }
     for (int c = ROW_S; c <= ROW_M && e == cudaSuccess; ++c) {
         if (rcnt[c] == 0) continue;
         const unsigned g = (unsigned)rcnt[c];
@@ -1261,7 +1270,7 @@ cudaError_t numeric_run(Pool &pool, const NumericArgs &a, const long long *binst
         { k_numeric_rows_split<ROW_WARPS><<<(unsigned)rcnt[ROW_L], ROW_WARPS * 32, (size_t)rreq[ROW_L], s>>>(a, ROW_L, packed); ::tsg::count_launch(); }
         e = cudaGetLastError();
     }
-    if (split) {
+    if (split && wide) {
         if (e == cudaSuccess) e = cudaEventRecord(join, side);
         s = pool.stream;
     }
