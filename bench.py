@@ -115,6 +115,11 @@ class ClockSampler:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
                                           "--format=csv,noheader,nounits", "-lms", "20"],
                                          stdout=self.f, stderr=subprocess.DEVNULL)
+            # nvidia-smi takes a while to start: wait (2 s at most) for its
+            # first sample, so that short timed regions are sampled too
+            t0 = time.perf_counter()
+            while time.perf_counter() - t0 < 2.0 and self.proc.poll() is None and os.path.getsize(self.f.name) == 0:
+                time.sleep(0.01)
         except Exception:
             self.proc = None
         return self
