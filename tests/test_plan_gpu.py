@@ -124,3 +124,25 @@ def test_plain_plan_replay(ctx):
     got = plan.result(0)
     assert np.array_equal(got.col, ref.col) and np.array_equal(got.val, ref.val)
     plan.close()
+
+
+def test_plan_replay_of_wide_rows_in_parts(built_lib):
+    """Every row forced to the wide class (smem_acc_max=0, row_acc_max=0) in
+    a C 20,000 columns wide: the parts path -- cut table, part walk -- runs
+    inside the plan's captured graph (its table sized by the bound there)."""
+    from tilespgemm_gb300 import Context
+    from tilespgemm_gb300 import matrices as M
+    A = M.random_sparse(600, 2000, 40, seed=51)
+    B = M.random_sparse(2000, 20000, 20, seed=52)
+    with Context(0, smem_acc_max=0, row_acc_max=0) as c:
+        plan = c.plan(A, B, op="AB")
+        for rnd in range(2):
+            va, vb = _newvals(A, 10 + rnd), _newvals(B, 20 + rnd)
+            plan.set_values(va, vb)
+            plan.replay()
+            got = plan.result(0)
+            ref = c.spgemm(_with(A, va), _with(B, vb), op="AB")
+            assert np.array_equal(got.col, ref.col) and np.array_equal(got.val, ref.val)
+            rp, col, val = O.spgemm(_with(A, va), _with(B, vb))
+            assert np.array_equal(got.col, col) and np.array_equal(got.val, val)
+        plan.close()
