@@ -112,6 +112,11 @@ struct tsg_ctx {
     bool counted = false;            // entered in the pinned cache's count of live contexts
     cudaStream_t side = nullptr;     // second stream for kernels that overlap the main one's (fork/join by events)
     cudaEvent_t fork = nullptr, join = nullptr;
+    // host-link copies beside the kernels: operand values up during the
+    // symbolic phase, C's row pointers and column indices down during the
+    // numeric step
+    cudaStream_t copy = nullptr;
+    cudaEvent_t cfork = nullptr, vals_ev = nullptr, cols_ev = nullptr, copy_done = nullptr;
 };
 
 namespace {
@@ -376,7 +381,13 @@ struct PlanData {
     bool dupsafe = false;
     bool b_increasing = true;                      // every B row's columns strictly increase
     int nsync = 0;
+    cudaEvent_t vals_ev = nullptr;                 // set while operand values are still on their way up (copy stream)
     std::vector<void *> owned;
+    // the main stream waits for the values' upload (before their first use,
+    // and before any buffer of the plan is freed)
+    void wait_values(cudaStream_t s) {
+        if (vals_ev) { cudaStreamWaitEvent(s, vals_ev, 0); vals_ev = nullptr; }
+    }
     template <class T> T *own(Pool &pool, long long n) {
         T *p = pool.alloc_n<T>(n);
         if (p) owned.push_back(p);
@@ -386,6 +397,7 @@ struct PlanData {
         for (auto &q : owned) if (q == p) q = nullptr;
     }
     void release(Pool &pool) {
+        wait_values(pool.stream);
         for (void *p : owned) pool.free(p);
         owned.clear();
     }
@@ -431,7 +443,17 @@ tsg_status stage_into_plan(tsg_ctx *ctx, Pool &pool, PlanData &P, const tsg_csr 
         CUDA_OK(cudaMemcpyAsync(drp, rp, rpb, kind, ctx->stream));
         if (M->nnz > 0) {
             CUDA_OK(cudaMemcpyAsync(dcol, c, sizeof(int) * (size_t)M->nnz, kind, ctx->stream));
-            if (v) CUDA_OK(cudaMemcpyAsync(dval, v, sizeof(double) * (size_t)M->nnz, kind, ctx->stream));
+            if (v && M->where == TSG_MEM_HOST && !copy) {
+                // host values of a single call go up on the copy stream while
+                // the symbolic phase runs (PlanData::wait_values joins them)
+                CUDA_OK(cudaEventRecord(ctx->cfork, ctx->stream));
+                CUDA_OK(cudaStreamWaitEvent(ctx->copy, ctx->cfork, 0));
+                CUDA_OK(cudaMemcpyAsync(dval, v, sizeof(double) * (size_t)M->nnz, kind, ctx->copy));
+                CUDA_OK(cudaEventRecord(ctx->vals_ev, ctx->copy));
+                P.vals_ev = ctx->vals_ev;
+            } else if (v) {
+                CUDA_OK(cudaMemcpyAsync(dval, v, sizeof(double) * (size_t)M->nnz, kind, ctx->stream));
+            }
         }
         rp = drp; c = dcol; v = dval;
         valbuf = dval;
@@ -478,6 +500,7 @@ tsg_status plan_symbolic(tsg_ctx *ctx, Pool &pool, Scratch &sc, tsg_op op, const
         double *tv = P.own<double>(pool, P.nnzA);
         P.perm = P.own<int>(pool, P.nnzA);
         if (!tp || !tc || !tv || !P.perm) return fail(TSG_ERR_OOM, "device pool allocation failed for A^T");
+        P.wait_values(ctx->stream);
         CUDA_OK(csr_transpose(pool, P.rpA, P.colA, P.valA, P.m, P.k, P.nnzA, tp, tc, tv, P.perm, ctx->dflags));
         P.rpB = tp; P.colB = tc; P.valB = tv; P.valB_buf = tv;
     }
@@ -569,8 +592,8 @@ tsg_status plan_symbolic(tsg_ctx *ctx, Pool &pool, Scratch &sc, tsg_op op, const
 }
 
 // Numeric phase into caller-provided col/val (nnzC each).
-tsg_status plan_numeric(tsg_ctx *ctx, Pool &pool, PlanData &P, const double *valA, const double *valB, int *col,
-                        double *val, const int *tr_coloff = nullptr, int threads = 0, int walk = -1)
+NumericArgs numeric_args(tsg_ctx *ctx, const PlanData &P, const double *valA, const double *valB, int *col,
+                         double *val, const int *tr_coloff)
 {
     NumericArgs na{};
     na.m = P.m; na.blkm = P.blkm;
@@ -580,6 +603,17 @@ tsg_status plan_numeric(tsg_ctx *ctx, Pool &pool, PlanData &P, const double *val
     na.rowptrC = P.rowptrC; na.colC = col; na.valC = val;
     na.bin = P.bin; na.binlist = P.binlist; na.rowlist = P.rowlist; na.b_sorted = P.b_increasing; na.tr_coloff = tr_coloff; na.flags = ctx->dflags;
     na.nnzA = P.nnzA; na.n = P.n;
+    return na;
+}
+
+// cols_done: C's column indices were written before (numeric_cols)
+tsg_status plan_numeric(tsg_ctx *ctx, Pool &pool, PlanData &P, const double *valA, const double *valB, int *col,
+                        double *val, const int *tr_coloff = nullptr, int threads = 0, int walk = -1,
+                        bool cols_done = false)
+{
+    NumericArgs na = numeric_args(ctx, P, valA, valB, col, val, tr_coloff);
+    na.cols_done = cols_done;
+    P.wait_values(ctx->stream);
     if (walk < 0) walk = ctx->opts.numeric_walk;
     if (threads <= 0) threads = ctx->opts.threads_numeric;
     // repeated B columns need the packed walk.  Auto otherwise loads B one
@@ -609,13 +643,109 @@ void fill_stats(const PlanData &P, tsg_stats *st)
     st->bins[3] = (int)P.bstat[BIN_ROWS];
 }
 
-// Hand C (rowptr copied/narrowed from `rowptr`, col/val adopted) to the
-// caller per C->where; frees col/val on failure.
-tsg_status emit_output(tsg_ctx *ctx, Pool &pool, int m, int n, long long nnzC, const long long *rowptr, int *col,
-                       double *val, tsg_csr *C, tsg_stats *st)
+// C's row pointers for the caller (int64 copied, or narrowed to int32), on
+// the main stream
+cudaError_t output_rowptr(tsg_ctx *ctx, Pool &pool, int m, int bits, const long long *rowptr, void *&rp_dev)
 {
-    int bits = ctx->opts.out_rowptr_bits;
-    if (bits == 0) bits = nnzC < (1ll << 31) ? 32 : 64;
+    if (bits == 32) {
+        int *rp32 = pool.alloc_n<int>(m + 1);
+        rp_dev = rp32;
+        return rp32 ? aux_rowptr_narrow(pool, rowptr, rp32, m + 1) : cudaErrorMemoryAllocation;
+    }
+    long long *rp64 = pool.alloc_n<long long>(m + 1);
+    rp_dev = rp64;
+    return rp64 ? cudaMemcpyAsync(rp64, rowptr, sizeof(long long) * (size_t)(m + 1), cudaMemcpyDeviceToDevice, ctx->stream)
+                : cudaErrorMemoryAllocation;
+}
+
+int output_bits(const tsg_ctx *ctx, long long nnzC)
+{
+    const int bits = ctx->opts.out_rowptr_bits;
+    return bits ? bits : (nnzC < (1ll << 31) ? 32 : 64);
+}
+
+// Host output started before the numeric step: C's row pointers and its
+// column indices (numeric_cols, from the masks) go down on the copy stream
+// while the numeric kernels run; the values follow in emit_output.
+struct EarlyOut {
+    bool on = false;
+    int bits = 0;
+    void *rp_dev = nullptr;
+    void *hrp = nullptr, *hcol = nullptr, *hval = nullptr;
+    size_t rpb = 0, cb = 0, vb = 0;
+    double ms = 0;               // host time spent here (part of the d2h phase)
+};
+
+tsg_status early_out_begin(tsg_ctx *ctx, Pool &pool, PlanData &P, int *col, double *val, EarlyOut &eo)
+{
+    auto t0 = std::chrono::steady_clock::now();
+    eo.bits = output_bits(ctx, P.nnzC);
+    if (eo.bits == 32 && P.nnzC >= (1ll << 31)) return TSG_OK;   // emit_output reports it
+    eo.rpb = (size_t)(P.m + 1) * (eo.bits == 64 ? 8 : 4);
+    eo.cb = sizeof(int) * (size_t)P.nnzC;
+    eo.vb = sizeof(double) * (size_t)P.nnzC;
+    eo.hrp = pinned_get(ctx, eo.rpb);
+    eo.hcol = pinned_get(ctx, eo.cb);
+    eo.hval = pinned_get(ctx, eo.vb);
+    if (!eo.hrp || !eo.hcol || !eo.hval) return fail(TSG_ERR_OOM, "pinned host memory for C");
+    eo.on = true;
+    CUDA_OK(output_rowptr(ctx, pool, P.m, eo.bits, P.rowptrC, eo.rp_dev));
+    NumericArgs na = numeric_args(ctx, P, P.valA, P.valB, col, val, nullptr);
+    CUDA_OK(numeric_cols(pool, na));
+    CUDA_OK(cudaEventRecord(ctx->cols_ev, ctx->stream));
+    CUDA_OK(cudaStreamWaitEvent(ctx->copy, ctx->cols_ev, 0));
+    CUDA_OK(cudaMemcpyAsync(eo.hrp, eo.rp_dev, eo.rpb, cudaMemcpyDeviceToHost, ctx->copy));
+    CUDA_OK(cudaMemcpyAsync(eo.hcol, col, eo.cb, cudaMemcpyDeviceToHost, ctx->copy));
+    CUDA_OK(cudaEventRecord(ctx->copy_done, ctx->copy));
+    eo.ms = ms_since(t0);
+    return TSG_OK;
+}
+
+// Undo early_out_begin after a failure: the copy stream is drained before
+// anything is freed; the pinned buffers go back to the cache.
+void early_out_abort(tsg_ctx *ctx, Pool &pool, EarlyOut &eo)
+{
+    cudaStreamSynchronize(ctx->copy);
+    pool.free(eo.rp_dev);
+    cudaStreamSynchronize(ctx->stream);
+    if (eo.hrp) pinned_put(ctx, eo.hrp, eo.rpb);
+    if (eo.hcol) pinned_put(ctx, eo.hcol, eo.cb);
+    if (eo.hval) pinned_put(ctx, eo.hval, eo.vb);
+    eo = EarlyOut{};
+}
+
+// Hand C (rowptr copied/narrowed from `rowptr`, col/val adopted) to the
+// caller per C->where; frees col/val on failure.  With `eo` (host output
+// begun by early_out_begin) only the values remain to be copied.
+tsg_status emit_output(tsg_ctx *ctx, Pool &pool, int m, int n, long long nnzC, const long long *rowptr, int *col,
+                       double *val, tsg_csr *C, tsg_stats *st, EarlyOut *eo = nullptr)
+{
+    if (eo && eo->on) {
+        auto t_d2h = std::chrono::steady_clock::now();
+        OutOwner *o = new OutOwner();
+        o->ctx = ctx;
+        o->where = C->where;
+        C->m = m; C->n = n; C->nnz = nnzC; C->rowptr_bits = eo->bits;
+        cudaError_t e = cudaMemcpyAsync(eo->hval, val, eo->vb, cudaMemcpyDeviceToHost, ctx->stream);
+        cudaStreamWaitEvent(ctx->stream, ctx->copy_done, 0);
+        pool.free(eo->rp_dev); pool.free(col); pool.free(val);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        o->blocks.push_back({eo->hrp, eo->rpb});
+        o->blocks.push_back({eo->hcol, eo->cb});
+        o->blocks.push_back({eo->hval, eo->vb});
+        C->row_ptr = eo->hrp; C->col = (int *)eo->hcol; C->val = (double *)eo->hval;
+        C->owner = o;
+        if (st) st->ms_d2h = eo->ms + ms_since(t_d2h);
+        *eo = EarlyOut{};
+        if (e == cudaSuccess) e = cudaGetLastError();
+        if (e != cudaSuccess) {
+            tsg_csr_free(ctx, C);
+            cudaGetLastError();
+            return fail(TSG_ERR_CUDA, "output: %s", cudaGetErrorString(e));
+        }
+        return TSG_OK;
+    }
+    const int bits = output_bits(ctx, nnzC);
     if (bits == 32 && nnzC >= (1ll << 31)) {
         pool.free(col); pool.free(val);
         cudaStreamSynchronize(ctx->stream);
@@ -625,19 +755,8 @@ tsg_status emit_output(tsg_ctx *ctx, Pool &pool, int m, int n, long long nnzC, c
     o->ctx = ctx;
     o->where = C->where;
     C->m = m; C->n = n; C->nnz = nnzC; C->rowptr_bits = bits;
-    cudaError_t e = cudaSuccess;
     void *rp_dev = nullptr;
-    if (bits == 32) {
-        int *rp32 = pool.alloc_n<int>(m + 1);
-        if (!rp32) e = cudaErrorMemoryAllocation;
-        else e = aux_rowptr_narrow(pool, rowptr, rp32, m + 1);
-        rp_dev = rp32;
-    } else {
-        long long *rp64 = pool.alloc_n<long long>(m + 1);
-        if (!rp64) e = cudaErrorMemoryAllocation;
-        else e = cudaMemcpyAsync(rp64, rowptr, sizeof(long long) * (size_t)(m + 1), cudaMemcpyDeviceToDevice, ctx->stream);
-        rp_dev = rp64;
-    }
+    cudaError_t e = output_rowptr(ctx, pool, m, bits, rowptr, rp_dev);
     if (C->where == TSG_MEM_DEVICE) {
         o->blocks.push_back({rp_dev, 0});
         o->blocks.push_back({col, 0});
@@ -755,10 +874,15 @@ tsg_status tsg_create(tsg_ctx **out, int device, const tsg_opts *opts)
         c->opts.threads_numeric = 256;
     auto cleanup = [&](tsg_status st) { tsg_destroy(c); return st; };
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess)
+        cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&c->copy, cudaStreamNonBlocking) != cudaSuccess)
         return cleanup(fail(TSG_ERR_CUDA, "cudaStreamCreate failed"));
     if (cudaEventCreateWithFlags(&c->fork, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&c->join, cudaEventDisableTiming) != cudaSuccess)
+        cudaEventCreateWithFlags(&c->join, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->cfork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->vals_ev, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->cols_ev, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->copy_done, cudaEventDisableTiming) != cudaSuccess)
         return cleanup(fail(TSG_ERR_CUDA, "cudaEventCreate failed"));
     cudaMemPoolProps props{};
     props.allocType = cudaMemAllocationTypePinned;
@@ -793,6 +917,8 @@ tsg_status tsg_destroy(tsg_ctx *c)
     if (c->fork) cudaEventDestroy(c->fork);
     if (c->join) cudaEventDestroy(c->join);
     if (c->side) { cudaStreamSynchronize(c->side); cudaStreamDestroy(c->side); }
+    if (c->copy) { cudaStreamSynchronize(c->copy); cudaStreamDestroy(c->copy); }
+    for (cudaEvent_t e : {c->cfork, c->vals_ev, c->cols_ev, c->copy_done}) if (e) cudaEventDestroy(e);
     if (c->dflags) cudaFree(c->dflags);
     if (c->dstat) cudaFree(c->dstat);
     if (c->hstat) cudaFreeHost(c->hstat);
@@ -845,6 +971,7 @@ tsg_status tsg_spgemm(tsg_ctx *ctx, tsg_op op, const tsg_csr *A, const tsg_csr *
     PhaseTimer tm(ctx, st && ctx->opts.phase_times);
     int *col = nullptr;
     double *val = nullptr;
+    EarlyOut eo;
     tsg_status r;
     {
         Scratch sc(pool);
@@ -854,10 +981,17 @@ tsg_status tsg_spgemm(tsg_ctx *ctx, tsg_op op, const tsg_csr *A, const tsg_csr *
             val = pool.alloc_n<double>(P.nnzC);
             if (!col || !val) r = fail(TSG_ERR_OOM, "device pool allocation failed for C (%lld entries)", P.nnzC);
         }
-        if (!r) r = plan_numeric(ctx, pool, P, P.valA, P.valB, col, val);
+        // host output: column indices down while the numeric step runs, for
+        // C tiles of 8 entries or more on average (FP64-bound numeric
+        // kernels; with sparser tiles the kernels wait on B's rows in L2,
+        // which the concurrent copy slows by about as much as it saves)
+        if (!r && C->where == TSG_MEM_HOST && P.nnzC > 0 && P.nnzC >= 8 * P.numblkC)
+            r = early_out_begin(ctx, pool, P, col, val, eo);
+        if (!r) r = plan_numeric(ctx, pool, P, P.valA, P.valB, col, val, nullptr, 0, -1, eo.on);
         tm.mark();  // 4
     }
     if (r) {
+        early_out_abort(ctx, pool, eo);
         pool.free(col); pool.free(val);
         P.release(pool);
         cudaStreamSynchronize(ctx->stream);
@@ -865,7 +999,7 @@ tsg_status tsg_spgemm(tsg_ctx *ctx, tsg_op op, const tsg_csr *A, const tsg_csr *
         return r;
     }
     fill_stats(P, st);
-    r = emit_output(ctx, pool, P.m, P.n, P.nnzC, P.rowptrC, col, val, C, st);
+    r = emit_output(ctx, pool, P.m, P.n, P.nnzC, P.rowptrC, col, val, C, st, &eo);
     P.release(pool);
     if (r) return r;
     if (st) {

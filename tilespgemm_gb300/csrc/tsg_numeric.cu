@@ -424,7 +424,7 @@ k_numeric_smem(NumericArgs g, int mybin)
             while (mk) {
                 const int b = 31 - __clz(mk);   // highest bit = smallest local column
                 const int c = TILE - 1 - b;
-                g.colC[dst] = jb + c;
+                if (!g.cols_done) g.colC[dst] = jb + c;
                 if (DENSE) g.valC[dst] = acc[(r * S + s) * DPAD + c];
                 ++dst;
                 mk &= ~(1u << b);
@@ -527,6 +527,7 @@ __device__ __forceinline__ void row_epilogue(const NumericArgs &g, const RowSmem
                                              int tid, int nthr)
 {
     for (int p = tid; p < nnz_r; p += nthr) g.valC[Rb + p] = w.acc[acc_swz(p)];
+    if (g.cols_done) return;
     const int cshift = g.tr_coloff ? g.tr_coloff[i] : 0;
     const long long c0 = g.crp[i];
     for (int s = tid; s < w.S; s += nthr) {
@@ -608,15 +609,14 @@ k_numeric_rows_split(NumericArgs g, int cls, bool packed)
 
 // ---- rows too large for a shared-memory accumulator (ROW_WIDE) -------------
 
-// per wide row (one warp each): column indices (the wide kernel zeroes the
-// values window by window)
-__global__ void __launch_bounds__(256)
-k_global_prep(NumericArgs g, int cls, long long nrows)
+// column indices of row R of C (one warp) from its masks.  COALESCE: tile
+// rows of more than four entries are written one output position per lane
+// (coalesced stores; more shuffles per entry), which pays when many warps
+// share the GPU; a lone long row is bound by the length of its warp's chain
+// and writes a tile row per lane.
+template <bool COALESCE>
+__device__ __forceinline__ void row_cols(const NumericArgs &g, int R, int lane)
 {
-    const long long k = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
-    if (k >= nrows) return;
-    const int lane = threadIdx.x & 31;
-    const int R = g.rowlist[(long long)cls * g.m + k];
     const int i = R >> 4, r = R & (TILE - 1);
     const int cshift = g.tr_coloff ? g.tr_coloff[i] : 0;
     const long long c0 = g.crp[i];
@@ -636,18 +636,118 @@ k_global_prep(NumericArgs g, int cls, long long nrows)
         }
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
-            unsigned mk = mkv[u];
-            const int c = __popc(mk);
-            const int incl = warp_incl_scan(c, lane);
-            long long dst = Rb + run + incl - c;
-            while (mk) {
-                const int b = 31 - __clz(mk);
-                g.colC[dst] = jbv[u] + (TILE - 1 - b);
-                ++dst;
-                mk &= ~(1u << b);
+            const unsigned mk = mkv[u];
+            const int cnt = __popc(mk);
+            const int incl = warp_incl_scan(cnt, lane);
+            const int excl = incl - cnt;
+            const int total = __shfl_sync(0xffffffffu, incl, 31);
+            if (!COALESCE || __reduce_max_sync(0xffffffffu, (unsigned)cnt) <= 4) {
+                // few entries per tile row: each lane writes its own (a store
+                // per entry, consecutive lanes at consecutive positions)
+                unsigned m = mk;
+                long long dst = Rb + run + excl;
+                while (m) {
+                    const int b = 31 - __clz(m);   // highest bit = smallest local column
+                    g.colC[dst++] = jbv[u] + (TILE - 1 - b);
+                    m &= ~(1u << b);
+                }
+                run += total;
+                continue;
             }
-            run += __shfl_sync(0xffffffffu, incl, 31);
+            // one output position per lane (coalesced stores): its slot t is
+            // the first lane whose inclusive count exceeds it, its column the
+            // k-th set column of that slot's mask
+            for (int p0 = 0; p0 < total; p0 += 32) {
+                const int p = p0 + lane;
+                int t = 0;
+#pragma unroll
+                for (int step = 16; step; step >>= 1)
+                    if (__shfl_sync(0xffffffffu, incl, t + step - 1) <= p) t += step;
+                const unsigned mt = __shfl_sync(0xffffffffu, mk, t);
+                const int jt = __shfl_sync(0xffffffffu, jbv[u], t);
+                const int k = p - __shfl_sync(0xffffffffu, excl, t);
+                int x = 0;   // the largest x with popc(columns < x) <= k
+#pragma unroll
+                for (int step = 8; step; step >>= 1)
+                    if (__popc(mt >> (TILE - (x + step))) <= k) x += step;
+                if (p < total) g.colC[Rb + run + p] = jt + x;
+            }
+            run += total;
         }
+    }
+}
+
+// per wide row (one warp each): column indices (the wide kernel zeroes the
+// values window by window)
+__global__ void __launch_bounds__(256)
+k_global_prep(NumericArgs g, int cls, long long nrows)
+{
+    const long long k = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+    if (k >= nrows) return;
+    row_cols<false>(g, g.rowlist[(long long)cls * g.m + k], threadIdx.x & 31);
+}
+
+// Column indices of every row of C before the numeric kernels.  One CTA per
+// tile-row; a tile-row of at most COLS_NARROW C tiles gets a half-warp per
+// row, which expands one tile at a time with lane = column in the tile, so
+// each store instruction writes one contiguous run of the row.  Wider
+// tile-rows are listed for k_cols_wide (a warp per row).
+constexpr int COLS_NARROW = 32;
+constexpr int COLS_WIDE_GRID = 152 * 8;
+
+__global__ void __launch_bounds__(256)
+k_cols_tr(NumericArgs g, int *wide_list, int *wide_n)
+{
+    const int i = blockIdx.x;
+    const long long c0 = g.crp[i];
+    const int S = (int)(g.crp[i + 1] - c0);
+    if (S == 0) return;
+    const int tid = threadIdx.x;
+    if (S > COLS_NARROW) {
+        if (tid == 0) wide_list[atomicAdd(wide_n, 1)] = i;
+        return;
+    }
+    const int hl = tid & 15, r = tid >> 4;
+    const int R = i * TILE + r;
+    if (R >= g.m) return;                       // whole half-warps leave together
+    const unsigned hmask = 0xffffu << (tid & 16);
+    const int cshift = g.tr_coloff ? g.tr_coloff[i] : 0;
+    const long long Rb = g.rowptrC[R];
+    const uint16_t *mrow = g.cmask + c0 * TILE + (long long)r * S;
+    int run = 0;
+    for (int sb = 0; sb < S; sb += 16) {
+        const int sl = sb + hl;
+        const unsigned mk = sl < S ? (unsigned)mrow[sl] : 0u;
+        const int jb = sl < S ? g.ccol[c0 + sl] * TILE - cshift : 0;
+        const int cnt = __popc(mk);
+        int incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 16; o <<= 1) {
+            const int t = __shfl_up_sync(hmask, incl, o, 16);
+            if (hl >= o) incl += t;
+        }
+        const int excl = incl - cnt;
+        const int nt = min(16, S - sb);
+        for (int t = 0; t < nt; ++t) {
+            const unsigned mt = __shfl_sync(hmask, mk, t, 16);
+            const int jt = __shfl_sync(hmask, jb, t, 16);
+            const int et = __shfl_sync(hmask, excl, t, 16);
+            if ((mt >> (TILE - 1 - hl)) & 1u)   // local column hl is bit 15 - hl
+                g.colC[Rb + run + et + __popc(mt >> (TILE - hl))] = jt + hl;
+        }
+        run += __shfl_sync(hmask, incl, 15, 16);
+    }
+}
+
+// rows of the tile-rows k_cols_tr listed: a warp per row over the whole GPU
+__global__ void __launch_bounds__(256)
+k_cols_wide(NumericArgs g, const int *wide_list, const int *wide_n)
+{
+    const long long nrows = (long long)(*wide_n) * TILE;
+    const long long nw = (long long)gridDim.x * (blockDim.x >> 5);
+    for (long long k = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5; k < nrows; k += nw) {
+        const int R = wide_list[k >> 4] * TILE + (int)(k & (TILE - 1));
+        if (R < g.m) row_cols<true>(g, R, threadIdx.x & 31);
     }
 }
 
@@ -1220,6 +1320,24 @@ cudaError_t long_prepare(Pool &pool, const NumericArgs &a, int cls, long long n,
 
 }  // namespace
 
+cudaError_t numeric_cols(Pool &pool, const NumericArgs &a)
+{
+    if (a.m <= 0 || a.blkm <= 0) return cudaSuccess;
+    int *wide = pool.alloc_n<int>((long long)a.blkm + 1);
+    if (!wide) return cudaErrorMemoryAllocation;
+    int *wide_n = wide + a.blkm;
+    cudaError_t e = cudaMemsetAsync(wide_n, 0, sizeof(int), pool.stream);
+    if (e == cudaSuccess) {
+        k_cols_tr<<<(unsigned)a.blkm, 256, 0, pool.stream>>>(a, wide, wide_n);
+        ::tsg::count_launch();
+        k_cols_wide<<<COLS_WIDE_GRID, 256, 0, pool.stream>>>(a, wide, wide_n);
+        ::tsg::count_launch();
+        e = cudaGetLastError();
+    }
+    pool.free(wide);
+    return e;
+}
+
 cudaError_t numeric_run(Pool &pool, const NumericArgs &a, const long long *binstat, int walk, int threads,
                         int row_warps, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join)
 {
@@ -1277,7 +1395,7 @@ cudaError_t numeric_run(Pool &pool, const NumericArgs &a, const long long *binst
     for (int c = ROW_WIDE; c <= ROW_WIDE1 && e == cudaSuccess; ++c) {
         const long long n = rcnt[c];
         if (n == 0) continue;
-        { k_global_prep<<<(unsigned)((n * 32 + 255) / 256), 256, 0, s>>>(a, c, n); ::tsg::count_launch(); }
+        if (!a.cols_done) { k_global_prep<<<(unsigned)((n * 32 + 255) / 256), 256, 0, s>>>(a, c, n); ::tsg::count_launch(); }
         // rows of long A rows: parts over the whole GPU (measured faster than
         // eight warps per row from C widths of 1,024 tile columns on); the
         // cut table gets at most LONG_TAB_MAX entries (rows past it stay

@@ -165,6 +165,7 @@ struct NumericArgs {
     int *flags;
     long long nnzA;       // entries of A (bounds the wide rows' cut table)
     int n;                // columns of C
+    bool cols_done;       // colC already written (numeric_cols): the kernels write values only
 };
 
 cudaError_t step2_masks(Pool &pool, const TileCSR &A, const TileCSR &B, int m, int blkm, const long long *crp,
@@ -181,6 +182,11 @@ cudaError_t step2_masks(Pool &pool, const TileCSR &A, const TileCSR &B, int m, i
 // per row for the shared-memory row classes ROW_S / ROW_M (1, 2 or 4)
 // side/fork/join: a second stream and two events; with wide rows the other
 // classes run there concurrently (side may be null: one stream)
+// Column indices of every row of C from the masks (one warp per row), so
+// that they can leave the device while the numeric kernels run; the numeric
+// step then runs with a.cols_done set.
+cudaError_t numeric_cols(Pool &pool, const NumericArgs &a);
+
 cudaError_t numeric_run(Pool &pool, const NumericArgs &a, const long long *binstat, int walk, int threads,
                         int row_warps, cudaStream_t side = nullptr, cudaEvent_t fork = nullptr,
                         cudaEvent_t join = nullptr);
