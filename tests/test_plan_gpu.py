@@ -41,6 +41,30 @@ def test_plan_matches_full_call(ctx, op):
     plan.close()
 
 
+@pytest.mark.parametrize("op", ["AA", "AAT"])
+def test_plan_host_output_dense_tiles(ctx, op):
+    """C tiles of 8+ entries: a plan's host output writes C's column indices
+    before the numeric step and copies them down beside it; the same bits
+    as the full call and the oracle."""
+    from tilespgemm_gb300 import matrices as M
+    A = M.laplacian_2d(64) if op == "AA" else M.stencil_27(9, seed=4)
+    plan = ctx.plan(A, op=op)
+    for seed in range(2):
+        v = _newvals(A, 40 + seed)
+        Av = _with(A, v)
+        C1 = plan.execute(v)
+        C2 = ctx.spgemm(Av, op=op)
+        assert np.array_equal(C1.rowptr, C2.rowptr) and np.array_equal(C1.col, C2.col)
+        assert np.array_equal(C1.val, C2.val)
+        tp, tr, tv = O.transpose(Av)
+        from tilespgemm_gb300.api import CSR
+        B = Av if op == "AA" else CSR(A.n, A.m, tp, tr, tv)
+        rp, col, val = O.spgemm(Av, B)
+        assert np.array_equal(np.asarray(C1.rowptr, np.int64), rp) and np.array_equal(C1.col, col)
+        assert np.array_equal(C1.val, val)
+    plan.close()
+
+
 def test_plan_ab_and_device_values(ctx):
     import torch
     from tilespgemm_gb300 import matrices as M

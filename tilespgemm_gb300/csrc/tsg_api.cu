@@ -687,6 +687,15 @@ struct EarlyOut {
     double ms = 0;               // host time spent here (part of the d2h phase)
 };
 
+// Host output with C tiles of 8 entries or more on average: there the
+// numeric kernels are bound by FP64 issue and the copy beside them is
+// nearly free; with sparser tiles they wait on B's rows in L2, which the
+// concurrent copy slows by about as much as it hides.
+bool early_out_pays(const PlanData &P, const tsg_csr *C)
+{
+    return C->where == TSG_MEM_HOST && P.nnzC > 0 && P.nnzC >= 8 * P.numblkC;
+}
+
 tsg_status early_out_begin(tsg_ctx *ctx, Pool &pool, PlanData &P, int *col, double *val, EarlyOut &eo)
 {
     auto t0 = std::chrono::steady_clock::now();
@@ -989,12 +998,7 @@ tsg_status tsg_spgemm(tsg_ctx *ctx, tsg_op op, const tsg_csr *A, const tsg_csr *
             val = pool.alloc_n<double>(P.nnzC);
             if (!col || !val) r = fail(TSG_ERR_OOM, "device pool allocation failed for C (%lld entries)", P.nnzC);
         }
-        // host output: column indices down while the numeric step runs, for
-        // C tiles of 8 entries or more on average (FP64-bound numeric
-        // kernels; with sparser tiles the kernels wait on B's rows in L2,
-        // which the concurrent copy slows by about as much as it saves)
-        if (!r && C->where == TSG_MEM_HOST && P.nnzC > 0 && P.nnzC >= 8 * P.numblkC)
-            r = early_out_begin(ctx, pool, P, col, val, eo);
+        if (!r && early_out_pays(P, C)) r = early_out_begin(ctx, pool, P, col, val, eo);
         if (!r) r = plan_numeric(ctx, pool, P, P.valA, P.valB, col, val, nullptr, 0, -1, eo.on);
         tm.mark();  // 4
     }
@@ -1113,10 +1117,20 @@ tsg_status tsg_plan_execute(tsg_ctx *ctx, tsg_plan *plan, const double *valA, co
         pool.free(col); pool.free(val);
         return fail(TSG_ERR_OOM, "device pool allocation failed for C (%lld entries)", P.nnzC);
     }
-    tsg_status r = plan_numeric(ctx, pool, P, va, vb, col, val);
-    if (r) { pool.free(col); pool.free(val); cudaStreamSynchronize(ctx->stream); return r; }
+    // host output of dense enough C tiles: column indices down during the
+    // numeric step (as in tsg_spgemm)
+    EarlyOut eo;
+    tsg_status r = TSG_OK;
+    if (early_out_pays(P, C)) r = early_out_begin(ctx, pool, P, col, val, eo);
+    if (!r) r = plan_numeric(ctx, pool, P, va, vb, col, val, nullptr, 0, -1, eo.on);
+    if (r) {
+        early_out_abort(ctx, pool, eo);
+        pool.free(col); pool.free(val);
+        cudaStreamSynchronize(ctx->stream);
+        return r;
+    }
     fill_stats(P, st);
-    r = emit_output(ctx, pool, P.m, P.n, P.nnzC, P.rowptrC, col, val, C, st);
+    r = emit_output(ctx, pool, P.m, P.n, P.nnzC, P.rowptrC, col, val, C, st, &eo);
     if (r) return r;
     // numeric kernels report an internal bound failure through the flags
     int hflags[FLAG_COUNT];
