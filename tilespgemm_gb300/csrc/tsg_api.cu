@@ -1335,9 +1335,10 @@ tsg_status tsg_spgemm_tiles(tsg_ctx *ctx, tsg_op op, const tsg_csr *A, const tsg
         fill_stats(P, st);
     }
     pool.free(col); pool.free(val);
-    P.release(pool);
-    if (r) { tsg_tiles_free(ctx, C); cudaGetLastError(); }
-    else cudaStreamSynchronize(ctx->stream);
+    P.release(pool);   // after the values' upload, if it is still running
+    if (r) tsg_tiles_free(ctx, C);
+    cudaStreamSynchronize(ctx->stream);
+    cudaGetLastError();
     return r;
 }
 
