@@ -144,6 +144,13 @@ const char *tsg_version(void);
  * FMA throughput in GFLOP/s (2 FLOP per FMA), measured by a short kernel. */
 int64_t tsg_launch_count(void);
 void *tsg_get_stream(tsg_ctx *ctx);
+
+/* Bytes of pinned host memory the process-wide cache of host output buffers
+ * keeps for reuse (no counterpart in the reference): min(96 GB, 3/8 of the
+ * host's memory), or the environment variable TSG_PINNED_CACHE_BYTES read at
+ * the first use (a decimal byte count, at most half the host's memory; 0
+ * keeps nothing, so every host result is pinned afresh). */
+int64_t tsg_pinned_cache_cap(void);
 tsg_status tsg_measure_fp64_peak(tsg_ctx *ctx, double *gflops);
 
 /* ---- matrix market load path ------------------------------------------- */

@@ -58,3 +58,33 @@ def test_no_gpu_means_an_error_not_a_fallback(built_lib):
     st = _abi.lib().tsg_create(C.byref(h), 0, None)
     assert st in (_abi.ERR_CUDA, _abi.ERR_INVALID_ARG, _abi.ERR_NOT_SUPPORTED)
     assert not h.value
+
+
+def _cache_cap(env):
+    """tsg_pinned_cache_cap in a fresh process (the cap is read once)."""
+    import os
+    import subprocess
+    import sys
+    code = ("import sys; sys.path.insert(0, '.'); from tilespgemm_gb300 import _abi; "
+            "print(_abi.lib().tsg_pinned_cache_cap())")
+    e = dict(os.environ)
+    e.pop("TSG_PINNED_CACHE_BYTES", None)
+    e.update(env)
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    out = subprocess.run([sys.executable, "-c", code], cwd=root, env=e, capture_output=True, text=True, check=True)
+    return int(out.stdout.strip())
+
+
+def test_pinned_cache_cap(built_lib):
+    """The host-output buffer cache keeps min(96 GB, 3/8 of host memory), or
+    TSG_PINNED_CACHE_BYTES (at most half of host memory; malformed values
+    fall back to the default)."""
+    import os
+    ram = os.sysconf("SC_PHYS_PAGES") * os.sysconf("SC_PAGE_SIZE")
+    default = min(96 << 30, ram // 8 * 3)
+    assert _cache_cap({}) == default
+    assert _cache_cap({"TSG_PINNED_CACHE_BYTES": "0"}) == 0
+    assert _cache_cap({"TSG_PINNED_CACHE_BYTES": str(3 << 30)}) == min(3 << 30, ram // 2)
+    assert _cache_cap({"TSG_PINNED_CACHE_BYTES": str(ram * 4)}) == ram // 2
+    assert _cache_cap({"TSG_PINNED_CACHE_BYTES": "12GB"}) == default
+    assert _cache_cap({"TSG_PINNED_CACHE_BYTES": "-5"}) == default

@@ -161,14 +161,20 @@ PinnedCache &pinned_cache()
     return c;
 }
 
-// min(96 GB, 3/8 of the host's memory).  On the served stream (4 workers,
-// outputs up to ~15 GB) a quarter of a 199 GB host gave 28-33 requests/s,
-// 3/8 of it 37-39.
+// min(96 GB, 3/8 of the host's memory), or the environment's
+// TSG_PINNED_CACHE_BYTES (a decimal byte count, at most half the host's
+// memory; 0 keeps nothing).  On the served stream (4 workers, outputs up to
+// ~15 GB) a quarter of a 199 GB host gave 28-33 requests/s, 3/8 of it 37-39.
 size_t pinned_cap()
 {
     static const size_t cap = [] {
         const long pages = sysconf(_SC_PHYS_PAGES), psz = sysconf(_SC_PAGE_SIZE);
         const size_t ram = (pages > 0 && psz > 0) ? (size_t)pages * (size_t)psz : (size_t)16 << 30;
+        if (const char *env = getenv("TSG_PINNED_CACHE_BYTES")) {
+            char *end = nullptr;
+            const long long v = strtoll(env, &end, 10);
+            if (end != env && *end == '\0' && v >= 0) return std::min<size_t>((size_t)v, ram / 2);
+        }
         return std::min<size_t>((size_t)96 << 30, ram / 8 * 3);
     }();
     return cap;
@@ -858,6 +864,8 @@ const char *tsg_last_error(void) { return g_err.c_str(); }
 const char *tsg_version(void) { return "tilespgemm-gb300 0.1 (sm_103a)"; }
 
 int64_t tsg_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
+
+int64_t tsg_pinned_cache_cap(void) { return (int64_t)pinned_cap(); }
 
 void *tsg_get_stream(tsg_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
 
