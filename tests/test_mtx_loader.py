@@ -82,3 +82,85 @@ def test_write_then_load_round_trip(built_lib, tmp_path):
     write_mtx(p, A, exact=True)
     B, _ = load_mtx(p)
     assert np.array_equal(B.val, A.val)
+
+
+@pytest.fixture
+def mtx_threads(monkeypatch):
+    """Set TSG_MTX_THREADS for the loader (read at every call)."""
+    def set_threads(n):
+        monkeypatch.setenv("TSG_MTX_THREADS", str(n))
+    return set_threads
+
+
+@pytest.mark.parametrize("stem", FILES)
+@pytest.mark.parametrize("threads", [1, 3, 8])
+def test_threads_match_reference(built_lib, mtx_threads, stem, threads):
+    """The line-parallel reader (tiny runs of lines here) and the token
+    reader give the reference loader's result, or its refusal."""
+    mtx_threads(threads)
+    test_load_matches_reference(built_lib, stem)
+
+
+def _load(path):
+    from tilespgemm_gb300 import TSGError, load_mtx
+    try:
+        A, sym = load_mtx(path)
+        return ("ok", A.m, A.n, int(sym), np.asarray(A.rowptr).tolist(), np.asarray(A.col).tolist(),
+                np.asarray(A.val).view(np.int64).tolist())
+    except TSGError as e:
+        return ("err", e.status, str(e))
+
+
+CASES = {
+    "blank_lines_crlf": "%%MatrixMarket matrix coordinate real general\r\n4 4 3\r\n\r\n1 2 1.5\r\n  \r\n3 1 -2e-3\r\n4 4 7\r\n",
+    "past_nz_ignored": "%%MatrixMarket matrix coordinate real general\n3 3 2\n1 1 1\n2 2 2\ngarbage here\n9 9 9\n",
+    "split_entry": "%%MatrixMarket matrix coordinate real general\n3 3 2\n1 1\n1.0\n2 2 2.0\n",
+    "extra_token": "%%MatrixMarket matrix coordinate real general\n3 3 2\n1 1 1.0 5\n2 2 2.0\n",
+    "size_line_tail": "%%MatrixMarket matrix coordinate real general\n3 3 2 1 1 1.0\n2 2 2.0\n",
+    "comment_in_data": "%%MatrixMarket matrix coordinate real general\n3 3 2\n1 1 1.0\n% note\n2 2 2.0\n",
+    "truncated": "%%MatrixMarket matrix coordinate real general\n3 3 3\n1 1 1.0\n2 2 2.0\n",
+    "truncated_value": "%%MatrixMarket matrix coordinate real general\n3 3 2\n1 1 1.0\n2 2\n",
+    "outside": "%%MatrixMarket matrix coordinate real general\n3 3 3\n1 1 1.0\n4 2 2.0\n3 3 3.0\n",
+    "outside_past_nz": "%%MatrixMarket matrix coordinate real general\n3 3 2\n1 1 1.0\n2 2 2.0\n4 4 4.0\n",
+    "symmetric": "%%MatrixMarket matrix coordinate real symmetric\n4 4 5\n1 1 1\n3 1 2\n4 2 3\n2 1 4\n4 4 5\n",
+    "integer": "%%MatrixMarket matrix coordinate integer general\n3 3 3\n1 1 3\n2 3 -4\n3 2 5000000000\n",
+    "pattern": "%%MatrixMarket matrix coordinate pattern general\n3 3 3\n1 1\n2 3\n3 2\n",
+    "complex": "%%MatrixMarket matrix coordinate complex hermitian\n3 3 2\n1 1 1.0 0.0\n3 1 2.5 -1.0\n",
+    "no_final_newline": "%%MatrixMarket matrix coordinate real general\n2 2 2\n1 1 1.0\n2 2 2.0",
+}
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_threads_agree_on_edge_cases(built_lib, mtx_threads, tmp_path, name):
+    """Line reader and token reader agree on blank lines, CRLF, lines past
+    NZ, entries split over lines, extra tokens, comments and truncation."""
+    p = tmp_path / f"{name}.mtx"
+    p.write_bytes(CASES[name].encode())
+    mtx_threads(1)
+    want = _load(p)
+    for t in (2, 3, 5, 16):
+        mtx_threads(t)
+        assert _load(p) == want, t
+
+
+@pytest.mark.parametrize("sym", ["general", "symmetric"])
+def test_threads_agree_on_a_large_file(built_lib, mtx_threads, tmp_path, sym):
+    """~200,000 entries with random spacing: every thread count gives the
+    token reader's CSR, bit for bit."""
+    rng = np.random.default_rng(5)
+    n, nz = 20000, 200000
+    i = rng.integers(1, n + 1, nz)
+    j = rng.integers(1, n + 1, nz)
+    if sym == "symmetric":
+        i, j = np.maximum(i, j), np.minimum(i, j)
+    v = rng.standard_normal(nz) * 10.0 ** rng.integers(-5, 5, nz)
+    sep = np.where(rng.random(nz) < 0.1, "  ", " ")
+    lines = [f"{a}{s}{b} {x!r}" for a, b, x, s in zip(i.tolist(), j.tolist(), v.tolist(), sep.tolist())]
+    p = tmp_path / "big.mtx"
+    p.write_text(f"%%MatrixMarket matrix coordinate real {sym}\n% generated\n{n} {n} {nz}\n" + "\n".join(lines) + "\n")
+    mtx_threads(1)
+    want = _load(p)
+    assert want[0] == "ok"
+    for t in (2, 7, 32):
+        mtx_threads(t)
+        assert _load(p) == want, t

@@ -16,14 +16,24 @@
 // Differences, all of which the reference turns into undefined behaviour:
 // 'array' files, indices outside [1,M]x[1,N], and truncated data lines are
 // rejected with TSG_ERR_BAD_MTX.
+//
+// The data lines of large files are parsed by several host threads, each
+// over a run of whole lines, when every data line holds exactly one entry;
+// otherwise (an entry split over lines, extra tokens, a malformed line) the
+// file is read again token by token, as the reference's fscanf does, so the
+// result and the error are the same either way.  TSG_MTX_THREADS sets the
+// thread count (1: token by token only); by default one thread per 4 MB of
+// data, at most the host's hardware threads.
 #include "tilespgemm.h"
 
+#include <algorithm>
 #include <cctype>
 #include <cerrno>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 namespace tsg {
@@ -37,6 +47,13 @@ bool read_file(const char *path, std::string &out)
 {
     FILE *f = fopen(path, "rb");
     if (!f) return false;
+    // one allocation when the size is known (a regular file), then chunks
+    // for whatever else arrives
+    if (fseek(f, 0, SEEK_END) == 0) {
+        const long sz = ftell(f);
+        if (sz > 0) out.reserve((size_t)sz + 1);
+        rewind(f);
+    }
     std::vector<char> buf(1 << 20);
     size_t got;
     while ((got = fread(buf.data(), 1, buf.size(), f)) > 0) out.append(buf.data(), got);
@@ -80,6 +97,126 @@ tsg_status bad(const char *msg)
     return TSG_ERR_BAD_MTX;
 }
 
+enum ValueKind { V_REAL, V_COMPLEX, V_INT, V_PATTERN };
+
+// The entries of the data lines in [p, end), one per line (blank lines
+// skipped), in file order, 0-based.  ok = false when a line is not exactly
+// one entry (the caller then reads the file token by token); first_bad = the
+// run's first entry outside the M x N matrix (stored as 0, 0), or -1.
+struct LineRun {
+    std::vector<int> i, j;
+    std::vector<double> v;
+    long long first_bad = -1;
+    bool ok = true;
+};
+
+inline bool blank(char c) { return c == ' ' || c == '\t' || c == '\r' || c == '\v' || c == '\f'; }
+
+void parse_lines(const char *p, const char *end, ValueKind kind, long long M, long long N, LineRun &out)
+{
+    // room for one entry per line, allocated once (threads growing vectors
+    // side by side spent their time in the kernel's page mapping)
+    const size_t lines = (size_t)std::count(p, end, '\n') + 1;
+    out.i.reserve(lines);
+    out.j.reserve(lines);
+    out.v.reserve(lines);
+    while (p < end) {
+        const char *e = (const char *)memchr(p, '\n', (size_t)(end - p));
+        if (!e) e = end;
+        const char *q = p;
+        auto tok_long = [&](long long &x) {
+            while (q < e && blank(*q)) ++q;
+            if (q >= e) return false;
+            char *t = nullptr;
+            errno = 0;
+            x = strtoll(q, &t, 10);
+            if (t == q || errno || t > e) return false;
+            q = t;
+            return true;
+        };
+        auto tok_double = [&](double &x) {
+            while (q < e && blank(*q)) ++q;
+            if (q >= e) return false;
+            char *t = nullptr;
+            x = strtod(q, &t);
+            if (t == q || t > e) return false;
+            q = t;
+            return true;
+        };
+        while (q < e && blank(*q)) ++q;
+        if (q < e) {
+            long long i = 0, j = 0;
+            double v = 1.0, vim = 0.0;
+            bool good = tok_long(i) && tok_long(j);
+            if (good && kind == V_REAL) good = tok_double(v);
+            else if (good && kind == V_COMPLEX) good = tok_double(v) && tok_double(vim);
+            else if (good && kind == V_INT) { long long iv = 0; good = tok_long(iv); v = (double)(int)iv; }
+            while (good && q < e && blank(*q)) ++q;
+            if (!good || q != e) { out.ok = false; return; }
+            if (i < 1 || i > M || j < 1 || j > N) {
+                if (out.first_bad < 0) out.first_bad = (long long)out.i.size();
+                i = j = 1;
+            }
+            out.i.push_back((int)(i - 1));
+            out.j.push_back((int)(j - 1));
+            out.v.push_back(v);
+        }
+        p = e + 1;
+    }
+}
+
+int mtx_threads(size_t data_bytes)
+{
+    if (const char *env = getenv("TSG_MTX_THREADS")) {
+        const long t = strtol(env, nullptr, 10);
+        if (t >= 1) return (int)std::min<long>(t, 256);
+    }
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    return (int)std::min<size_t>(hw, std::max<size_t>(1, data_bytes / (4u << 20)));
+}
+
+// Data lines [p, end) parsed by `nt` threads into ri/ci/vv (the first NZ
+// entries, checked like the token reader checks them).  Returns false when
+// a line is not one entry: nothing is decided then.
+bool parse_parallel(const char *p, const char *end, int nt, ValueKind kind, long long M, long long N, long long NZ,
+                    std::vector<int> &ri, std::vector<int> &ci, std::vector<double> &vv, tsg_status &st)
+{
+    std::vector<const char *> cut((size_t)nt + 1);
+    cut[0] = p;
+    cut[(size_t)nt] = end;
+    for (int k = 1; k < nt; ++k) {   // run k starts after the first newline at or past its even share
+        const char *c = p + (size_t)(end - p) * (size_t)k / (size_t)nt;
+        if (c < cut[(size_t)k - 1]) c = cut[(size_t)k - 1];
+        const char *nl = (const char *)memchr(c, '\n', (size_t)(end - c));
+        cut[(size_t)k] = nl ? nl + 1 : end;
+    }
+    std::vector<LineRun> run((size_t)nt);
+    std::vector<std::thread> th;
+    for (int k = 1; k < nt; ++k)
+        th.emplace_back(parse_lines, cut[(size_t)k], cut[(size_t)k + 1], kind, M, N, std::ref(run[(size_t)k]));
+    parse_lines(cut[0], cut[1], kind, M, N, run[0]);
+    for (auto &t : th) t.join();
+    // entries past the first NZ are never read by the token reader, so a
+    // malformed line after them does not matter; one before them does
+    long long have = 0;
+    for (int k = 0; k < nt && have < NZ; ++k) {
+        if (!run[(size_t)k].ok) return false;
+        have += (long long)run[(size_t)k].i.size();
+    }
+    long long t = 0;
+    for (int k = 0; k < nt && t < NZ; ++k) {
+        const LineRun &r = run[(size_t)k];
+        const long long take = std::min<long long>((long long)r.i.size(), NZ - t);
+        if (r.first_bad >= 0 && r.first_bad < take) { st = bad("entry index outside the matrix"); return true; }
+        std::copy(r.i.begin(), r.i.begin() + take, ri.begin() + t);
+        std::copy(r.j.begin(), r.j.begin() + take, ci.begin() + t);
+        std::copy(r.v.begin(), r.v.begin() + take, vv.begin() + t);
+        t += take;
+    }
+    st = t < NZ ? bad("truncated data line") : TSG_OK;
+    return true;
+}
+
 }  // namespace
 
 extern "C" tsg_status tsg_load_mtx(const char *path, tsg_csr *out, int32_t *is_symmetric)
@@ -121,7 +258,16 @@ extern "C" tsg_status tsg_load_mtx(const char *path, tsg_csr *out, int32_t *is_s
     if (M < 0 || N < 0 || NZ < 0 || M > INT32_MAX - 1 || N > INT32_MAX - 1 || NZ > INT32_MAX) return bad("sizes out of range");
     std::vector<int> ri((size_t)NZ), ci((size_t)NZ);
     std::vector<double> vv((size_t)NZ);
-    for (long long t = 0; t < NZ; ++t) {
+    const ValueKind kind = is_real ? V_REAL : is_complex ? V_COMPLEX : is_int ? V_INT : V_PATTERN;
+    const int nt = NZ > 0 ? mtx_threads((size_t)(end - cur.p)) : 1;
+    tsg_status pst = TSG_OK;
+    // the rest of the size line must be blank for the line reader
+    const char *dp = cur.p;
+    while (dp < end && blank(*dp)) ++dp;
+    const bool lines_ok = dp < end && *dp == '\n';
+    if (nt > 1 && lines_ok && parse_parallel(dp + 1, end, nt, kind, M, N, NZ, ri, ci, vv, pst)) {
+        if (pst != TSG_OK) return pst;
+    } else for (long long t = 0; t < NZ; ++t) {
         long long i = 0, j = 0;
         double v = 1.0, vim = 0.0;
         if (!cur.read_long(i) || !cur.read_long(j)) return bad("truncated data line");
@@ -133,15 +279,26 @@ extern "C" tsg_status tsg_load_mtx(const char *path, tsg_csr *out, int32_t *is_s
         ci[(size_t)t] = (int)(j - 1);
         vv[(size_t)t] = v;
     }
-    // counts, then fill in file order (mirrors right after their source)
+    // counts, then fill in file order (mirrors right after their source).
+    // With several threads, thread k owns the rows [M k / nt, M (k+1) / nt)
+    // and walks every entry in file order, so each row keeps file order.
+    auto by_rows = [&](auto &&fn) {
+        if (nt <= 1) { fn(0ll, M); return; }
+        std::vector<std::thread> th;
+        for (int k = 1; k < nt; ++k) th.emplace_back(fn, M * k / nt, M * (k + 1) / nt);
+        fn(0ll, M / nt);
+        for (auto &t : th) t.join();
+    };
+    for (long long t = 0; symm && t < NZ; ++t)
+        if (ri[(size_t)t] != ci[(size_t)t] && ci[(size_t)t] >= M) return bad("symmetric entry mirrored outside the matrix");
     std::vector<long long> cnt((size_t)M + 1, 0);
-    for (long long t = 0; t < NZ; ++t) {
-        cnt[(size_t)ri[(size_t)t]]++;
-        if (symm && ri[(size_t)t] != ci[(size_t)t]) {
-            if (ci[(size_t)t] >= M) return bad("symmetric entry mirrored outside the matrix");
-            cnt[(size_t)ci[(size_t)t]]++;
+    by_rows([&](long long r0, long long r1) {
+        for (long long t = 0; t < NZ; ++t) {
+            const long long i = ri[(size_t)t], j = ci[(size_t)t];
+            if (i >= r0 && i < r1) cnt[(size_t)i]++;
+            if (symm && i != j && j >= r0 && j < r1) cnt[(size_t)j]++;
         }
-    }
+    });
     long long total = 0;
     for (long long r = 0; r < M; ++r) { long long c = cnt[(size_t)r]; cnt[(size_t)r] = total; total += c; }
     cnt[(size_t)M] = total;
@@ -158,18 +315,21 @@ extern "C" tsg_status tsg_load_mtx(const char *path, tsg_csr *out, int32_t *is_s
         return TSG_ERR_OOM;
     }
     for (long long r = 0; r <= M; ++r) rp[r] = (int)cnt[(size_t)r];
-    std::vector<long long> pos(cnt.begin(), cnt.end() - 1);
-    for (long long t = 0; t < NZ; ++t) {
-        const int i = ri[(size_t)t], j = ci[(size_t)t];
-        long long d = pos[(size_t)i]++;
-        col[d] = j;
-        val[d] = vv[(size_t)t];
-        if (symm && i != j) {
-            d = pos[(size_t)j]++;
-            col[d] = i;
-            val[d] = vv[(size_t)t];
+    by_rows([&](long long r0, long long r1) {   // cnt[r] becomes row r's next free slot
+        for (long long t = 0; t < NZ; ++t) {
+            const int i = ri[(size_t)t], j = ci[(size_t)t];
+            if (i >= r0 && i < r1) {
+                const long long d = cnt[(size_t)i]++;
+                col[d] = j;
+                val[d] = vv[(size_t)t];
+            }
+            if (symm && i != j && j >= r0 && j < r1) {
+                const long long d = cnt[(size_t)j]++;
+                col[d] = i;
+                val[d] = vv[(size_t)t];
+            }
         }
-    }
+    });
     out->m = (int32_t)M;
     out->n = (int32_t)N;
     out->nnz = total;
