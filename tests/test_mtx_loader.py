@@ -164,3 +164,56 @@ def test_threads_agree_on_a_large_file(built_lib, mtx_threads, tmp_path, sym):
     for t in (2, 7, 32):
         mtx_threads(t)
         assert _load(p) == want, t
+
+
+@pytest.mark.parametrize("exact", [False, True])
+def test_writer_threads_write_the_same_bytes(built_lib, mtx_threads, tmp_path, exact):
+    """tsg_write_mtx formats waves of rows on several threads: the file is
+    byte for byte the one-thread file (empty rows, a long row, int64 row
+    pointers), and it loads back."""
+    from tilespgemm_gb300 import load_mtx, write_mtx
+    from tilespgemm_gb300 import matrices as M
+    from tilespgemm_gb300.api import CSR
+    A = M.random_sparse(3000, 2500, 9, seed=12, empty_rows=0.2)
+    rp = np.asarray(A.rowptr, np.int64)
+    long_row = np.arange(0, 2500, 2, dtype=np.int32)             # row 7 gets 1,250 entries
+    cols = [np.asarray(A.col[rp[r]:rp[r + 1]]) for r in range(A.m)]
+    vals = [np.asarray(A.val[rp[r]:rp[r + 1]]) for r in range(A.m)]
+    cols[7], vals[7] = long_row, np.linspace(-3.0, 3.0, long_row.size)
+    rp2 = np.concatenate([[0], np.cumsum([c.size for c in cols])]).astype(np.int64)
+    B = CSR(A.m, A.n, rp2, np.concatenate(cols), np.concatenate(vals))
+    for X in (A, B):
+        mtx_threads(1)
+        write_mtx(tmp_path / "one.mtx", X, exact=exact)
+        want = (tmp_path / "one.mtx").read_bytes()
+        for t in (2, 5, 16):
+            mtx_threads(t)
+            write_mtx(tmp_path / "many.mtx", X, exact=exact)
+            assert (tmp_path / "many.mtx").read_bytes() == want, t
+        Y, _ = load_mtx(tmp_path / "many.mtx")
+        assert np.array_equal(np.asarray(Y.rowptr, np.int64), np.asarray(X.rowptr, np.int64))
+        assert np.array_equal(Y.col, X.col)
+        if exact:
+            assert np.array_equal(Y.val, X.val)
+
+
+def test_writer_refuses_a_bad_row_pointer(built_lib, tmp_path):
+    from tilespgemm_gb300 import TSGError, write_mtx
+    from tilespgemm_gb300.api import CSR
+    X = CSR(3, 3, np.array([0, 2, 1, 3], np.int64), np.array([0, 1, 2], np.int32), np.ones(3))
+    with pytest.raises(TSGError):
+        write_mtx(tmp_path / "bad.mtx", X)
+
+
+def test_writer_waves(built_lib, mtx_threads, tmp_path):
+    """More entries than one wave (2^20 per thread): several waves, written
+    in order, give the one-thread bytes."""
+    from tilespgemm_gb300 import write_mtx
+    from tilespgemm_gb300 import matrices as M
+    A = M.random_sparse(150000, 150000, 16, seed=4)     # 2.4 M entries: three waves on one thread, two on two
+    assert A.nnz > 2 * (1 << 20)
+    mtx_threads(1)
+    write_mtx(tmp_path / "one.mtx", A)
+    mtx_threads(2)
+    write_mtx(tmp_path / "two.mtx", A)
+    assert (tmp_path / "one.mtx").read_bytes() == (tmp_path / "two.mtx").read_bytes()
