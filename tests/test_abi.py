@@ -65,8 +65,8 @@ def _cache_cap(env):
     import os
     import subprocess
     import sys
-    code = ("import sys; sys.path.insert(0, '.'); from tilespgemm_gb300 import _abi; "
-            "print(_abi.lib().tsg_pinned_cache_cap())")
+    code = ("import sys; sys.path.insert(0, '.'); import tilespgemm_gb300 as t; "
+            "print(t.pinned_cache_cap())")
     e = dict(os.environ)
     e.pop("TSG_PINNED_CACHE_BYTES", None)
     e.update(env)

@@ -478,4 +478,11 @@ def version() -> str:
     return lib().tsg_version().decode()
 
 
-__all__ = ["CSR", "Context", "OwnedCSR", "Plan", "Tiles", "TSGError", "load_mtx", "write_mtx", "version"]
+def pinned_cache_cap() -> int:
+    """Bytes of pinned host memory kept for reuse by host results
+    (TSG_PINNED_CACHE_BYTES, else min(96 GB, 3/8 of host memory))."""
+    return int(lib().tsg_pinned_cache_cap())
+
+
+__all__ = ["CSR", "Context", "OwnedCSR", "Plan", "Tiles", "TSGError", "load_mtx", "write_mtx", "version",
+           "pinned_cache_cap"]
