@@ -213,6 +213,38 @@ def run_reference(args) -> None:
     print(json.dumps(out))
 
 
+def measure_e2e(args, ctx, A, op, stream, nnz_c, barrier, dist):
+    """The same SpGEMM through the C ABI with host operands (pinned) and a
+    host C: the copies both ways are inside the timed region.  Returns
+    (ms per step, H2D bytes per step, D2H bytes per step)."""
+    import torch
+    from tilespgemm_gb300.api import CSR
+    Ah = CSR(A.m, A.n, torch.from_numpy(np.asarray(A.rowptr, np.int32)).pin_memory(),
+             torch.from_numpy(np.asarray(A.col, np.int32)).pin_memory(),
+             torch.from_numpy(np.asarray(A.val, np.float64)).pin_memory())
+    oc, _ = ctx.spgemm_raw(Ah, op=op, out="host")
+    c_rowptr_bytes = 4 * (A.m + 1) if oc.rowptr_bits == 32 else 8 * (A.m + 1)
+    oc.free()
+    barrier()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        oc, _ = ctx.spgemm_raw(Ah, op=op, out="host")
+        oc.free()
+    e1.record(stream)
+    e1.synchronize()
+    barrier()
+    ms_e2e = e0.elapsed_time(e1) / args.steps
+    if dist is not None:
+        t = torch.tensor([ms_e2e], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_e2e = float(t.item())
+    h2d = 4 * (A.m + 1) + 12 * A.nnz
+    d2h = c_rowptr_bytes + 12 * nnz_c
+    return ms_e2e, h2d, d2h
+
+
 def run_ours(args) -> None:
     import torch
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -271,29 +303,9 @@ def run_ours(args) -> None:
     value = world * 2.0 * cub / (ms * 1e6)
 
     # ---- e2e through the ABI with host operands ----
-    Ah = CSR(A.m, A.n, torch.from_numpy(np.asarray(A.rowptr, np.int32)).pin_memory(),
-             torch.from_numpy(np.asarray(A.col, np.int32)).pin_memory(),
-             torch.from_numpy(np.asarray(A.val, np.float64)).pin_memory())
-    oc, _ = ctx.spgemm_raw(Ah, op=op, out="host")
-    c_rowptr_bytes = 4 * (A.m + 1) if oc.rowptr_bits == 32 else 8 * (A.m + 1)
-    oc.free()
-    barrier()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(args.steps):
-        oc, _ = ctx.spgemm_raw(Ah, op=op, out="host")
-        oc.free()
-    e1.record(stream)
-    e1.synchronize()
-    barrier()
-    ms_e2e = e0.elapsed_time(e1) / args.steps
-    if dist is not None:
-        t = torch.tensor([ms_e2e], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_e2e = float(t.item())
-    h2d = 4 * (A.m + 1) + 12 * A.nnz
-    d2h = c_rowptr_bytes + 12 * nnz_c
+    ms_e2e, h2d, d2h = None, 0, 0
+    if not args.no_e2e:
+        ms_e2e, h2d, d2h = measure_e2e(args, ctx, A, op, stream, nnz_c, barrier, dist)
 
     if rank != 0:
         ctx.close()
@@ -347,8 +359,8 @@ def run_ours(args) -> None:
         "host_waits_per_step": phases[-1]["n_syncs"],
         "roofline": roofline,
         "cpu_baseline": cpu,
-        "e2e": {"value": world * 2.0 * cub / (ms_e2e * 1e6), "unit": UNIT, "ms_per_step": ms_e2e,
-                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "e2e": ({"value": world * 2.0 * cub / (ms_e2e * 1e6), "unit": UNIT, "ms_per_step": ms_e2e,
+                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h} if ms_e2e is not None else None),
         "gpu_launches": int(launches),
         "gpu_launches_per_step": launches / args.steps,
         "clocks": clk.summary(),
@@ -479,6 +491,7 @@ def main() -> None:
     ap.add_argument("--workload", default="st27-96")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-operand leg (C of R-MAT 2^20 is 116 GB)")
     ap.add_argument("--batch-count", type=int, default=4096)
     ap.add_argument("--batch-waves", type=int, default=8)
     ap.add_argument("--serve-requests", type=int, default=400)

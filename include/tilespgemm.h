@@ -153,6 +153,28 @@ void *tsg_get_stream(tsg_ctx *ctx);
 int64_t tsg_pinned_cache_cap(void);
 tsg_status tsg_measure_fp64_peak(tsg_ctx *ctx, double *gflops);
 
+/* Failure detection, tested without a GPU fault (no counterpart in the
+ * reference, which checks no CUDA return code, spins without bound in its
+ * look-back scan, utils_cuda_scan.h:167-170, and exits on an unknown bin,
+ * spgemm_nsparse_kernel.h:1299).
+ *
+ * tsg_inject_alloc_failure: the `countdown`-th allocation from now of the
+ *   given kind fails as if memory were exhausted -- kind 0: device memory
+ *   from a context's pool, kind 1: pinned host memory (host results and
+ *   staging).  Process-wide; countdown 0 disarms it.  The call that meets the
+ *   failure returns TSG_ERR_OOM, releases what it holds, and its context
+ *   stays usable.  tsg_alloc_failure_pending: allocations still to go before
+ *   the armed failure (0: none armed, or it has fired).
+ * tsg_check_bounded_wait: runs the library's single-pass device scan over n
+ *   ones with its look-back waits limited to spin_limit polls, set up so
+ *   that the first tile's sum is never published (no CTA takes tile 0).  The waits for it give up, the kernel finishes, and the
+ *   call returns TSG_ERR_DEVICE_TIMEOUT -- what every call returns when a
+ *   bounded device wait gives up -- with the context still usable.  TSG_OK
+ *   would mean a wait did not give up. */
+tsg_status tsg_inject_alloc_failure(int32_t kind, int64_t countdown);
+int64_t tsg_alloc_failure_pending(int32_t kind);
+tsg_status tsg_check_bounded_wait(tsg_ctx *ctx, int64_t n, int32_t spin_limit);
+
 /* ---- matrix market load path ------------------------------------------- */
 
 /*
@@ -371,13 +393,16 @@ tsg_status tsg_tiles_to_csr(tsg_ctx *ctx, const tsg_tiles *T, tsg_csr *C);
 /* tsg_tiles_to_csr for callers that cannot allocate: no counterpart in the
  * reference.  T is device tile form (from tsg_csr_to_tiles or
  * tsg_spgemm_tiles); row_ptr (m+1 int64), col and val (T->nnz each) are
- * caller-provided device memory of ctx's device, and the result is the one
+ * caller-provided device memory of ctx's device (device memory of another
+ * GPU is refused with TSG_ERR_INVALID_ARG), and the result is the one
  * tsg_tiles_to_csr gives.  The call allocates no device or pinned memory: its
  * scratch (row counts, scan look-back state, error flags) is one static
  * device array, cleared at the start of every call.  T->m above
  * TSG_NOALLOC_MAX_ROWS is refused with TSG_ERR_NOT_SUPPORTED.  The first call
- * on a device looks up the array's address (cudaGetSymbolAddress); make it
- * before any stream capture.  All contexts of a device share the array, so
+ * on a device after a context is created there looks up the array's address
+ * (cudaGetSymbolAddress; a device reset can move the array, and contexts do
+ * not survive one); make that call before any stream capture.  All contexts
+ * of a device share the array, so
  * calls that overlap in time (other threads or streams) race: serialize them.
  * Returns after the result is complete (it waits on ctx's stream). */
 tsg_status tsg_tiles_to_csr_noalloc(tsg_ctx *ctx, const tsg_tiles *T, int64_t *row_ptr, int32_t *col,
@@ -397,6 +422,16 @@ tsg_status tsg_tiles_download(tsg_ctx *ctx, const tsg_tiles *T, int64_t *blkrowp
 /* Copy a CSR's arrays (any location) to caller-provided host buffers.
  * row_ptr receives int64 values whatever the source width. */
 tsg_status tsg_csr_download(tsg_ctx *ctx, const tsg_csr *M, int64_t *row_ptr, int32_t *col, double *val);
+
+/* Rows [r0, r1) of a CSR (any location) into caller-provided host buffers,
+ * for checking or exporting part of a result too large to bring back whole
+ * (no counterpart in the reference, which discards C).  row_ptr receives the
+ * r1 - r0 + 1 row pointers of those rows as int64, as they are in M
+ * (offsets into M's entries); col and val (either may be NULL: then only
+ * the row pointers are copied) receive the entries
+ * [row_ptr[0], row_ptr[r1 - r0]) of M. */
+tsg_status tsg_csr_download_rows(tsg_ctx *ctx, const tsg_csr *M, int32_t r0, int32_t r1, int64_t *row_ptr,
+                                 int32_t *col, double *val);
 
 #ifdef __cplusplus
 }

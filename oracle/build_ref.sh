@@ -19,7 +19,7 @@ if [ ! -f "$REF/thmkl_dcsrmultcsr.c" ]; then
   exit 0
 fi
 mkdir -p "$OUT"
-gcc -O2 -fopenmp -fPIC -shared -w -Dmain=thmkl_ref_main -I"$REF" \
+gcc -O3 -fopenmp -fPIC -shared -w -Dmain=thmkl_ref_main -I"$REF" \
     "$REF/thmkl_dcsrmultcsr.c" -o "$OUT/libthmkl_ref.so"
 nvcc -O2 -w -Xcompiler -fPIC -shared -gencode arch=compute_103a,code=sm_103a \
     -Dmain=stir_ref_main -DcudaThreadSynchronize=cudaDeviceSynchronize -DclockRate=major \

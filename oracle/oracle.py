@@ -21,7 +21,7 @@ P = C.c_void_p
 
 
 def _build() -> None:
-    subprocess.run(["gcc", "-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", "-Wall",
+    subprocess.run(["gcc", "-O3", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", "-Wall",
                     str(HERE / "tsg_oracle.c"), "-o", str(LIB_PATH), "-lm"], check=True)
 
 
@@ -36,6 +36,8 @@ def lib() -> C.CDLL:
         L.orc_spgemm_rownnz.argtypes = [C.c_int, C.c_int, P, P, P, P, P]
         L.orc_spgemm_fill.restype = C.c_int
         L.orc_spgemm_fill.argtypes = [C.c_int, C.c_int, P, P, P, P, P, P, P, P, P, P]
+        L.orc_spgemm_rows.restype = C.c_int
+        L.orc_spgemm_rows.argtypes = [C.c_int, P, C.c_int, C.c_int, P, P, P, P, P, P, P, P, P, P]
         L.orc_thmkl_rows.restype = None
         L.orc_thmkl_rows.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, P, P, P, P, P, P, P, P, P]
         L.orc_transpose.restype = None
@@ -89,6 +91,28 @@ def spgemm(A, B, with_bound: bool = False):
                       _p(ccol), _p(cval), _p(bnd))
     out = (crp, ccol[:nnz], cval[:nnz])
     return out + (bnd[:nnz],) if with_bound else out
+
+
+def spgemm_rows(A, B, rows):
+    """Rows `rows` (any order, no repeats needed) of C = A*B, as spgemm()
+    computes them: (rowptr relative to the list, col, val, bound), the
+    bound being sum |a||b| per entry."""
+    L = lib()
+    arp, acol, aval = _csr64(A)
+    brp, bcol, bval = _csr64(B)
+    rows = np.ascontiguousarray(np.asarray(rows), dtype=np.int32)
+    nr = len(rows)
+    crp = np.zeros(nr + 1, dtype=np.int64)
+    if L.orc_spgemm_rows(nr, _p(rows), int(A.m), int(B.n), _p(arp), _p(acol), None, _p(brp), _p(bcol), None,
+                         _p(crp), None, None, None) != 0:
+        raise ValueError("row or column index out of range")
+    nnz = int(crp[-1])
+    ccol = np.empty(max(nnz, 1), dtype=np.int32)
+    cval = np.empty(max(nnz, 1), dtype=np.float64)
+    bnd = np.empty(max(nnz, 1), dtype=np.float64)
+    L.orc_spgemm_rows(nr, _p(rows), int(A.m), int(B.n), _p(arp), _p(acol), _p(aval), _p(brp), _p(bcol),
+                      _p(bval), _p(crp), _p(ccol), _p(cval), _p(bnd))
+    return crp, ccol[:nnz], cval[:nnz], bnd[:nnz]
 
 
 def transpose(A):

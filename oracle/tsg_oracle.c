@@ -144,6 +144,67 @@ int orc_spgemm_fill(int m, int n, const int64_t *arp, const int32_t *acol, const
 }
 
 /*
+ * Rows rows[0..nr) of C = A*B, computed exactly as orc_spgemm_rownnz and
+ * orc_spgemm_fill compute them (thmkl_dcsrmultcsr.c:12-41, :52-91), for
+ * checking a sample of rows of a product too large to compute whole on the
+ * CPU.  With ccol == NULL, crp[0..nr] receives the exclusive prefix of the
+ * listed rows' entry counts; otherwise row t's columns (ascending), values
+ * and sum |a||b| bounds go to ccol/cval/cbound from crp[t].  Rows are taken
+ * one at a time by the threads (a few hub rows can hold most of the work).
+ * Returns -1 when a listed row or a B column is out of range.
+ */
+int orc_spgemm_rows(int nr, const int32_t *rows, int m, int n, const int64_t *arp, const int32_t *acol,
+                    const double *aval, const int64_t *brp, const int32_t *bcol, const double *bval,
+                    int64_t *crp, int32_t *ccol, double *cval, double *cbound)
+{
+    int bad = 0;
+#pragma omp parallel reduction(|:bad)
+    {
+        int64_t *stamp = (int64_t *)malloc(sizeof(int64_t) * (size_t)(n > 0 ? n : 1));
+        double *acc = (double *)malloc(sizeof(double) * (size_t)(n > 0 ? n : 1));
+        double *bnd = (double *)malloc(sizeof(double) * (size_t)(n > 0 ? n : 1));
+        for (int j = 0; j < n; ++j) stamp[j] = -1;
+#pragma omp for schedule(dynamic, 1)
+        for (int t = 0; t < nr; ++t) {
+            const int i = rows[t];
+            if (i < 0 || i >= m) { bad = 1; continue; }
+            int64_t cnt = 0;
+            const int64_t base = ccol ? crp[t] : 0;
+            for (int64_t p = arp[i]; p < arp[i + 1]; ++p) {
+                const int k = acol[p];
+                const double a = aval ? aval[p] : 0.0;
+                for (int64_t q = brp[k]; q < brp[k + 1]; ++q) {
+                    const int j = bcol[q];
+                    if (j < 0 || j >= n) { bad = 1; continue; }
+                    if (stamp[j] != t) {
+                        stamp[j] = t;
+                        if (ccol) { acc[j] = 0.0; bnd[j] = 0.0; ccol[base + cnt] = j; }
+                        ++cnt;
+                    }
+                    if (ccol) {
+                        acc[j] = fma(a, bval[q], acc[j]);
+                        bnd[j] += fabs(a) * fabs(bval[q]);
+                    }
+                }
+            }
+            if (!ccol) { crp[t + 1] = cnt; continue; }
+            sort_int_asc(ccol + base, cnt);
+            for (int64_t u = 0; u < cnt; ++u) {
+                const int j = ccol[base + u];
+                cval[base + u] = acc[j];
+                if (cbound) cbound[base + u] = bnd[j];
+            }
+        }
+        free(stamp); free(acc); free(bnd);
+    }
+    if (!ccol) {
+        crp[0] = 0;
+        for (int t = 0; t < nr; ++t) crp[t + 1] += crp[t];
+    }
+    return bad ? -1 : 0;
+}
+
+/*
  * Faithful restatement of thmkl_dcsrmultcsr (thmkl_dcsrmultcsr.c:7-95), the
  * reference's OpenMP CPU SpGEMM, kept for TIMING as the CPU baseline: per row
  * it allocates and clears dense flag (and value) arrays of length k (the

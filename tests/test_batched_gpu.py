@@ -77,3 +77,35 @@ def test_batched_bad_instance_is_reported(ctx):
     with pytest.raises(TSGError) as e:
         ctx.spgemm_batched([good, bad], op="AA")
     assert e.value.status == 8
+
+
+def test_sibling_results_freed_from_many_threads(ctx):
+    """The results of one batched call share one allocation that goes with
+    the last of them.  Freed from eight threads at once, it is released
+    exactly once: results of later calls get buffers of their own (a buffer
+    released twice would be handed to two live results) and stay exact."""
+    import threading
+    As = _instances(64, 21)
+    for _ in range(4):
+        outs, _ = ctx.spgemm_batched_raw(As, op="AA", out="host")
+        gate = threading.Barrier(8)
+
+        def work(part):
+            gate.wait()
+            for o in part:
+                o.free()
+
+        ths = [threading.Thread(target=work, args=(outs[t::8],)) for t in range(8)]
+        for t in ths:
+            t.start()
+        for t in ths:
+            t.join()
+        assert all(not o.s.owner for o in outs)
+    first, _ = ctx.spgemm_batched_raw(As[:32], op="AA", out="host")
+    second, _ = ctx.spgemm_batched_raw(As[32:], op="AA", out="host")
+    try:
+        for A, oc in zip(As, first + second):
+            _check(oc.download(), A, A)
+    finally:
+        for oc in first + second:
+            oc.free()

@@ -97,3 +97,29 @@ def test_empty_and_row_limit(ctx):
         assert b"TSG_NOALLOC_MAX_ROWS" in _abi.lib().tsg_last_error()
     finally:
         _abi.lib().tsg_tiles_free(ctx.handle, C.byref(t))
+
+
+def test_refuses_buffers_off_the_device(ctx):
+    """Outputs must be memory the context's GPU writes: pinned host memory,
+    and device memory of another GPU where there is one, are refused with
+    TSG_ERR_INVALID_ARG before any device work."""
+    import torch
+    A = M.random_sparse(300, 300, 4, seed=5)
+    t = _tiles(ctx, A)
+    try:
+        dev = torch.device("cuda", 0)
+        rp_h = torch.zeros(A.m + 1, dtype=torch.int64).pin_memory()
+        col = torch.empty(A.nnz, dtype=torch.int32, device=dev)
+        val = torch.empty(A.nnz, dtype=torch.float64, device=dev)
+        st = _abi.lib().tsg_tiles_to_csr_noalloc(ctx.handle, C.byref(t), rp_h.data_ptr(), col.data_ptr(),
+                                                 val.data_ptr())
+        assert st == _abi.ERR_INVALID_ARG
+        assert rp_h.numpy().tolist() == [0] * (A.m + 1)
+        if torch.cuda.device_count() > 1:
+            other = torch.device("cuda", 1)
+            rp_o = torch.zeros(A.m + 1, dtype=torch.int64, device=other)
+            st = _abi.lib().tsg_tiles_to_csr_noalloc(ctx.handle, C.byref(t), rp_o.data_ptr(), col.data_ptr(),
+                                                     val.data_ptr())
+            assert st == _abi.ERR_INVALID_ARG
+    finally:
+        _abi.lib().tsg_tiles_free(ctx.handle, C.byref(t))

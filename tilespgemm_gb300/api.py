@@ -128,6 +128,26 @@ class OwnedCSR:
     def download(self) -> CSR:
         return _download(self._ctx.handle, self.s)
 
+    def rowptr(self) -> np.ndarray:
+        """The whole row pointer (int64), without the entries."""
+        rp = np.empty(self.s.m + 1, dtype=np.int64)
+        check(lib().tsg_csr_download_rows(self._ctx.handle, C.byref(self.s), 0, self.s.m, rp.ctypes.data,
+                                          None, None))
+        return rp
+
+    def rows(self, r0: int, r1: int) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+        """Rows [r0, r1): (row pointer relative to row r0, columns, values)."""
+        rp = np.empty(r1 - r0 + 1, dtype=np.int64)
+        lib_ = lib()
+        check(lib_.tsg_csr_download_rows(self._ctx.handle, C.byref(self.s), r0, r1, rp.ctypes.data, None, None))
+        cnt = int(rp[-1] - rp[0])
+        col = np.empty(cnt, dtype=np.int32)
+        val = np.empty(cnt, dtype=np.float64)
+        if cnt:
+            check(lib_.tsg_csr_download_rows(self._ctx.handle, C.byref(self.s), r0, r1, rp.ctypes.data,
+                                             col.ctypes.data, val.ctypes.data))
+        return rp - rp[0], col, val
+
     def free(self) -> None:
         if self.s.owner:
             lib().tsg_csr_free(self._ctx.handle, C.byref(self.s))

@@ -61,6 +61,7 @@ cudaError_t csr_fill_from_tiles(cudaStream_t s, int m, const long long *brp, con
                                 const uint8_t *ptr, const uint8_t *lcol, const double *tval, const long long *rowptr,
                                 int *col, double *val);
 long long scan_status_words(long long n);
+cudaError_t scan_unpublished_tile(Pool &pool, long long n, int spin_limit, int *flags);
 cudaError_t tiles_spmv(cudaStream_t s, int m, int blkm, const long long *brp, const int *bcol, const long long *nnzb,
                        const uint8_t *ptr, const uint8_t *lcol, const double *tval, const double *x, int n, double *y);
 cudaError_t scan_i32_to_i64_in(cudaStream_t s, const int *in, long long *out, long long n, int *flags,
@@ -74,8 +75,20 @@ static std::atomic<long long> g_launches{0};
 
 void tsg::count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
+// armed allocation failures per kind: the allocation that takes the count
+// from 1 to 0 fails; 0 (or below) = disarmed
+static std::atomic<long long> g_fail_alloc[2];
+
+bool tsg::alloc_should_fail(int kind)
+{
+    std::atomic<long long> &c = g_fail_alloc[kind & 1];
+    if (c.load(std::memory_order_relaxed) <= 0) return false;
+    return c.fetch_sub(1, std::memory_order_relaxed) == 1;
+}
+
 namespace tsg {
 void set_last_error(const char *msg) { g_err = msg; }
+void noalloc_forget(int device);
 void *make_malloc_owner(void *a, void *b, void *c);
 }
 
@@ -90,6 +103,9 @@ static tsg_status fail(tsg_status st, const char *fmt, ...)
     g_err = buf;
     return st;
 }
+
+// status of a failed CUDA call: out of memory is TSG_ERR_OOM, the rest TSG_ERR_CUDA
+static inline tsg_status cuda_status(cudaError_t e) { return e == cudaErrorMemoryAllocation ? TSG_ERR_OOM : TSG_ERR_CUDA; }
 
 #define CUDA_OK(call)                                                                                  \
     do {                                                                                               \
@@ -136,7 +152,9 @@ enum StatSlot {
 struct OutOwner {
     int where = TSG_MEM_DEVICE;   // TSG_MEM_DEVICE: pool memory; TSG_MEM_HOST: pinned; OWN_MALLOC: malloc
     tsg_ctx *ctx = nullptr;
-    int refs = 1;
+    // views still alive; batched results are freed from several threads, so
+    // the last decrement (and only it) releases the blocks
+    std::atomic<int> refs{1};
     std::vector<std::pair<void *, size_t>> blocks;
 };
 constexpr int OWN_MALLOC = 2;
@@ -184,6 +202,7 @@ void *pinned_get(tsg_ctx *ctx, size_t bytes)
 {
     (void)ctx;
     if (bytes == 0) bytes = 16;
+    if (alloc_should_fail(1)) return nullptr;
     PinnedCache &pc = pinned_cache();
     {
         std::lock_guard<std::mutex> lk(pc.mu);
@@ -767,7 +786,7 @@ tsg_status emit_output(tsg_ctx *ctx, Pool &pool, int m, int n, long long nnzC, c
         if (e != cudaSuccess) {
             tsg_csr_free(ctx, C);
             cudaGetLastError();
-            return fail(TSG_ERR_CUDA, "output: %s", cudaGetErrorString(e));
+            return fail(cuda_status(e), "output: %s", cudaGetErrorString(e));
         }
         return TSG_OK;
     }
@@ -869,6 +888,42 @@ int64_t tsg_pinned_cache_cap(void) { return (int64_t)pinned_cap(); }
 
 void *tsg_get_stream(tsg_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
 
+tsg_status tsg_inject_alloc_failure(int32_t kind, int64_t countdown)
+{
+    if (kind != 0 && kind != 1) return fail(TSG_ERR_INVALID_ARG, "kind must be 0 (device pool) or 1 (pinned host)");
+    if (countdown < 0) return fail(TSG_ERR_INVALID_ARG, "countdown must be >= 0");
+    g_fail_alloc[kind].store(countdown, std::memory_order_relaxed);
+    return TSG_OK;
+}
+
+int64_t tsg_alloc_failure_pending(int32_t kind)
+{
+    if (kind != 0 && kind != 1) return -1;
+    const long long c = g_fail_alloc[kind].load(std::memory_order_relaxed);
+    return c > 0 ? c : 0;
+}
+
+tsg_status tsg_check_bounded_wait(tsg_ctx *ctx, int64_t n, int32_t spin_limit)
+{
+    if (!ctx) return fail(TSG_ERR_INVALID_ARG, "ctx is NULL");
+    if (n < 1 || n > (1ll << 30) || spin_limit < 1)
+        return fail(TSG_ERR_INVALID_ARG, "n must be in [1, 2^30] and spin_limit >= 1");
+    CUDA_OK(cudaSetDevice(ctx->device));
+    CUDA_OK(cudaMemsetAsync(ctx->dflags, 0, sizeof(int) * FLAG_COUNT, ctx->stream));
+    Pool pool{ctx->pool, ctx->stream};
+    const cudaError_t e = scan_unpublished_tile(pool, n, spin_limit, ctx->dflags);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(e == cudaErrorMemoryAllocation ? TSG_ERR_OOM : TSG_ERR_CUDA, "bounded-wait check: %s",
+                    cudaGetErrorString(e));
+    }
+    const tsg_status r = host_wait(ctx, nullptr);
+    // the flags of this check are not carried into the context's next call
+    cudaMemsetAsync(ctx->dflags, 0, sizeof(int) * FLAG_COUNT, ctx->stream);
+    cudaStreamSynchronize(ctx->stream);
+    return r;
+}
+
 tsg_status tsg_measure_fp64_peak(tsg_ctx *ctx, double *gflops)
 {
     if (!ctx || !gflops) return fail(TSG_ERR_INVALID_ARG, "ctx/gflops is NULL");
@@ -931,6 +986,7 @@ tsg_status tsg_create(tsg_ctx **out, int device, const tsg_opts *opts)
     if (e == cudaSuccess) e = symbolic_init_attributes();
     if (e == cudaSuccess) e = numeric_init_attributes();
     if (e != cudaSuccess) return cleanup(fail(TSG_ERR_CUDA, "kernel attributes: %s", cudaGetErrorString(e)));
+    noalloc_forget(device);   // tsg_tiles_to_csr_noalloc resolves its scratch address again
     *out = c;
     return TSG_OK;
 }
@@ -960,7 +1016,7 @@ tsg_status tsg_csr_free(tsg_ctx *ctx, tsg_csr *M)
 {
     if (!M) return TSG_OK;
     OutOwner *o = static_cast<OutOwner *>(M->owner);
-    if (o && --o->refs <= 0) {
+    if (o && o->refs.fetch_sub(1, std::memory_order_acq_rel) == 1) {
         tsg_ctx *c = o->ctx ? o->ctx : ctx;
         if (o->where == TSG_MEM_DEVICE) {
             if (c) {
@@ -1001,6 +1057,8 @@ tsg_status tsg_spgemm(tsg_ctx *ctx, tsg_op op, const tsg_csr *A, const tsg_csr *
     {
         Scratch sc(pool);
         r = plan_symbolic(ctx, pool, sc, op, A, B, P, false, st != nullptr && ctx->opts.count_products, tm);
+        if (!r && output_bits(ctx, P.nnzC) == 32 && P.nnzC >= (1ll << 31))   // before any work on C
+            r = fail(TSG_ERR_INT32_OVERFLOW, "C has %lld entries; int32 row pointers cannot hold them", P.nnzC);
         if (!r) {
             col = pool.alloc_n<int>(P.nnzC);
             val = pool.alloc_n<double>(P.nnzC);
@@ -1203,6 +1261,45 @@ tsg_status tsg_csr_download(tsg_ctx *ctx, const tsg_csr *M, int64_t *row_ptr, in
 }
 
 
+tsg_status tsg_csr_download_rows(tsg_ctx *ctx, const tsg_csr *M, int32_t r0, int32_t r1, int64_t *row_ptr,
+                                 int32_t *col, double *val)
+{
+    if (!M || !row_ptr) return fail(TSG_ERR_INVALID_ARG, "M/row_ptr is NULL");
+    if (r0 < 0 || r1 < r0 || r1 > M->m) return fail(TSG_ERR_INVALID_ARG, "rows [%d, %d) are not inside [0, %d)", r0, r1, M->m);
+    if (M->rowptr_bits != 32 && M->rowptr_bits != 64) return fail(TSG_ERR_INVALID_ARG, "M.rowptr_bits must be 32 or 64");
+    const bool dev = M->where == TSG_MEM_DEVICE;
+    if (dev && !ctx) return fail(TSG_ERR_INVALID_ARG, "device matrix needs a context");
+    if (ctx) CUDA_OK(cudaSetDevice(ctx->device));
+    const int w = M->rowptr_bits == 64 ? 8 : 4;
+    const size_t n = (size_t)(r1 - r0) + 1;
+    const char *src = static_cast<const char *>(M->row_ptr) + (size_t)r0 * w;
+    if (w == 8) {
+        if (dev) CUDA_OK(cudaMemcpy(row_ptr, src, 8 * n, cudaMemcpyDeviceToHost));
+        else memcpy(row_ptr, src, 8 * n);
+    } else {
+        std::vector<int> tmp(n);
+        if (dev) CUDA_OK(cudaMemcpy(tmp.data(), src, 4 * n, cudaMemcpyDeviceToHost));
+        else memcpy(tmp.data(), src, 4 * n);
+        for (size_t i = 0; i < n; ++i) row_ptr[i] = tmp[i];
+    }
+    const long long e0 = row_ptr[0], e1 = row_ptr[n - 1];
+    if (e0 < 0 || e1 < e0 || e1 > M->nnz)
+        return fail(TSG_ERR_BAD_INPUT, "row pointers of rows [%d, %d) give entries [%lld, %lld) outside [0, %lld)", r0, r1,
+                    e0, e1, (long long)M->nnz);
+    const size_t cnt = (size_t)(e1 - e0);
+    if (cnt == 0) return TSG_OK;
+    if (col) {
+        if (dev) CUDA_OK(cudaMemcpy(col, M->col + e0, sizeof(int) * cnt, cudaMemcpyDeviceToHost));
+        else memcpy(col, M->col + e0, sizeof(int) * cnt);
+    }
+    if (val) {
+        if (dev) CUDA_OK(cudaMemcpy(val, M->val + e0, sizeof(double) * cnt, cudaMemcpyDeviceToHost));
+        else memcpy(val, M->val + e0, sizeof(double) * cnt);
+    }
+    return TSG_OK;
+}
+
+
 }  // extern "C"
 
 // ---- tile form --------------------------------------------------------------
@@ -1286,7 +1383,7 @@ tsg_status tsg_csr_to_tiles(tsg_ctx *ctx, const tsg_csr *A, tsg_tiles *T)
                 masks_to_tile_major_i32(pool, TA.blkm, TA.trp, TA.mask, T->mask);
                 cudaError_t e = tiles_payload_a(pool, dA.m, dA.n, dA.rp, dA.col, dA.val, TA, nb, (long long *)T->nnzb,
                                                 T->ptr, T->col, T->val, ctx->dflags);
-                if (e != cudaSuccess) r = fail(TSG_ERR_CUDA, "tile payload: %s", cudaGetErrorString(e));
+                if (e != cudaSuccess) r = fail(cuda_status(e), "tile payload: %s", cudaGetErrorString(e));
             }
             if (!r) r = host_wait(ctx, nullptr);
         }
@@ -1337,7 +1434,7 @@ tsg_status tsg_spgemm_tiles(tsg_ctx *ctx, tsg_op op, const tsg_csr *A, const tsg
         if (!r) {
             cudaError_t e = tiles_from_csr_c(pool, P.m, P.blkm, nb, P.crp, P.ccol, P.cmask, P.rowptrC, col, val,
                                              (long long *)C->nnzb, C->ptr, C->col, C->val, ctx->dflags);
-            if (e != cudaSuccess) r = fail(TSG_ERR_CUDA, "tile payload of C: %s", cudaGetErrorString(e));
+            if (e != cudaSuccess) r = fail(cuda_status(e), "tile payload of C: %s", cudaGetErrorString(e));
         }
         if (!r) r = host_wait(ctx, nullptr);
         fill_stats(P, st);
@@ -1461,7 +1558,7 @@ tsg_status pack_operands(tsg_ctx *ctx, Pool &pool, Scratch &sc, int count, const
         pinned_put(ctx, hrp, rpb);
         pinned_put(ctx, hcol, sizeof(int) * (size_t)(nnz > 0 ? nnz : 1));
         pinned_put(ctx, hval, sizeof(double) * (size_t)(nnz > 0 ? nnz : 1));
-        if (e != cudaSuccess) return fail(TSG_ERR_CUDA, "batch upload: %s", cudaGetErrorString(e));
+        if (e != cudaSuccess) return fail(cuda_status(e), "batch upload: %s", cudaGetErrorString(e));
         if (bad) return fail(TSG_ERR_BAD_INPUT, "an instance's row pointer or column index is out of range");
     } else {
         std::vector<PackDesc> d(count);
@@ -1614,7 +1711,7 @@ tsg_status tsg_spgemm_batched(tsg_ctx *ctx, tsg_op op, int32_t count, const tsg_
                     tsg_csr tmp{};
                     tmp.owner = o;
                     tsg_csr_free(ctx, &tmp);
-                    r = fail(TSG_ERR_CUDA, "batch output copy: %s", cudaGetErrorString(e));
+                    r = fail(cuda_status(e), "batch output copy: %s", cudaGetErrorString(e));
                 }
             }
             if (!r) {
@@ -1686,8 +1783,12 @@ static __device__ __align__(256) unsigned char tsg_noalloc_scratch[NA_SCRATCH_BY
 
 namespace {
 
-// Device address of the scratch array on `device` (current), resolved once
-// per device with cudaGetSymbolAddress and kept.
+// Device address of the scratch array on `device` (current), resolved with
+// cudaGetSymbolAddress at the first call on the device and kept.  Creating
+// a context on the device drops the kept address (noalloc_forget), so the
+// first call after it resolves it again: a context cannot outlive a reset
+// of its device (cudaDeviceReset ends its streams and pool), and after a
+// reset the module is loaded anew and the array may sit elsewhere.
 tsg_status noalloc_scratch(int device, char **out)
 {
     if (device < 0 || device >= NA_MAX_DEVICES) return fail(TSG_ERR_NOT_SUPPORTED, "device %d: no-alloc scratch covers devices 0-%d", device, NA_MAX_DEVICES - 1);
@@ -1706,11 +1807,27 @@ tsg_status noalloc_scratch(int device, char **out)
     return TSG_OK;
 }
 
-bool is_device_pointer(const void *p)
+// p is memory that kernels launched on `device` may write: device memory of
+// that device, or managed memory (reachable from every device).  Device
+// memory of another GPU is refused: without peer access the writes would
+// fault, with it they would land on the other GPU.
+}  // namespace
+
+void tsg::noalloc_forget(int device)
+{
+    if (device < 0 || device >= NA_MAX_DEVICES) return;
+    std::lock_guard<std::mutex> lk(g_na_mu);
+    g_na_addr[device] = nullptr;
+}
+
+namespace {
+
+bool is_device_pointer(const void *p, int device)
 {
     cudaPointerAttributes a{};
     if (cudaPointerGetAttributes(&a, p) != cudaSuccess) { cudaGetLastError(); return false; }
-    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+    if (a.type == cudaMemoryTypeDevice) return a.device == device;
+    return a.type == cudaMemoryTypeManaged;
 }
 
 }  // namespace
@@ -1730,8 +1847,9 @@ tsg_status tsg_tiles_to_csr_noalloc(tsg_ctx *ctx, const tsg_tiles *T, int64_t *r
     if (T->nnz > 0 && (!T->blkcolidx || !T->col || !T->val)) return fail(TSG_ERR_INVALID_ARG, "T's entry arrays are NULL");
     if (T->nnz > 0 && (!col || !val)) return fail(TSG_ERR_INVALID_ARG, "col/val is NULL for %lld entries", (long long)T->nnz);
     CUDA_OK(cudaSetDevice(ctx->device));
-    if (!is_device_pointer(row_ptr) || (T->nnz > 0 && (!is_device_pointer(col) || !is_device_pointer(val))))
-        return fail(TSG_ERR_INVALID_ARG, "row_ptr/col/val must be device memory");
+    const int dev = ctx->device;
+    if (!is_device_pointer(row_ptr, dev) || (T->nnz > 0 && (!is_device_pointer(col, dev) || !is_device_pointer(val, dev))))
+        return fail(TSG_ERR_INVALID_ARG, "row_ptr/col/val must be device memory of the context's device %d", dev);
     char *scr = nullptr;
     tsg_status r = noalloc_scratch(ctx->device, &scr);
     if (r) return r;

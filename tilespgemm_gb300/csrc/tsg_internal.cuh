@@ -127,6 +127,10 @@ namespace tsg {
 // tsg_launch_count), so benchmarks count launches instead of estimating them.
 void count_launch();
 
+// Fault injection (tsg_inject_alloc_failure): true when this allocation of
+// `kind` (0: device pool, 1: pinned host) is the one armed to fail.
+bool alloc_should_fail(int kind);
+
 // Stream-ordered allocations from the context's memory pool.  The pool keeps
 // freed memory cached (release threshold = max), so steady-state calls do no
 // cudaMalloc.  alloc() returns nullptr and sets `err` on failure.
@@ -136,6 +140,7 @@ struct Pool {
     cudaError_t err = cudaSuccess;
     void *alloc(size_t bytes) {
         if (bytes == 0) bytes = 16;
+        if (alloc_should_fail(0)) { err = cudaErrorMemoryAllocation; return nullptr; }
         void *p = nullptr;
         cudaError_t e = cudaMallocFromPoolAsync(&p, bytes, pool, stream);
         if (e != cudaSuccess) { err = e; cudaGetLastError(); return nullptr; }

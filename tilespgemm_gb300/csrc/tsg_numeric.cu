@@ -1411,7 +1411,7 @@ cudaError_t numeric_run(Pool &pool, const NumericArgs &a, const long long *binst
         LongScratch L{};
         if (parts) {
             e = long_prepare(pool, a, c, n, tab_bound, L);
-            if (e != cudaSuccess) return e;
+            if (e != cudaSuccess) break;
         }
         if (c == ROW_WIDE) { k_numeric_wide<ROW_WARPS><<<(unsigned)n, ROW_WARPS * 32, WIDE_SMEM, s>>>(a, c, n, packed, L.handled); ::tsg::count_launch(); }
         else { k_numeric_wide<1><<<(unsigned)((n + ROW_WARPS - 1) / ROW_WARPS), ROW_WARPS * 32, WIDE_SMEM, s>>>(a, c, n, packed, nullptr); ::tsg::count_launch(); }
@@ -1421,7 +1421,13 @@ cudaError_t numeric_run(Pool &pool, const NumericArgs &a, const long long *binst
         }
         e = cudaGetLastError();
     }
-    if (split && e == cudaSuccess) e = cudaStreamWaitEvent(pool.stream, join, 0);
+    if (split) {
+        // joined after a failure too, so that nothing the caller frees on the
+        // main stream is still in use by the side stream's kernels
+        cudaError_t e2 = cudaEventRecord(join, side);
+        if (e2 == cudaSuccess) e2 = cudaStreamWaitEvent(pool.stream, join, 0);
+        if (e == cudaSuccess) e = e2;
+    }
     return e;
 }
 

@@ -28,7 +28,7 @@ constexpr unsigned long long ST_VAL = (1ull << 62) - 1;
 template <typename Tin, typename Tout>
 __global__ void __launch_bounds__(SCAN_THREADS)
 k_scan(const Tin *__restrict__ in, Tout *__restrict__ out, long long n,
-       unsigned long long *status, unsigned *ticket, int *flags)
+       unsigned long long *status, unsigned *ticket, int *flags, int spin_limit)
 {
     __shared__ int s_tile;
     __shared__ long long s_warp[SCAN_THREADS / 32];
@@ -84,7 +84,7 @@ k_scan(const Tin *__restrict__ in, Tout *__restrict__ out, long long n,
                     int spins = 0;
                     st = vst[look];
                     while ((st >> 62) == 0) {
-                        if (++spins > SPIN_LIMIT) { set_flag(flags, FLAG_TIMEOUT); st = ST_INC; break; }
+                        if (++spins > spin_limit) { set_flag(flags, FLAG_TIMEOUT); st = ST_INC; break; }
                         __nanosleep(64);
                         st = vst[look];
                     }
@@ -121,6 +121,12 @@ k_scan(const Tin *__restrict__ in, Tout *__restrict__ out, long long n,
 template <typename Tout>
 __global__ void k_scan_empty(Tout *out) { out[0] = 0; }
 
+__global__ void k_fill_ones(int *a, long long n)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) a[i] = 1;
+}
+
 template <typename Tin, typename Tout>
 cudaError_t scan_impl(Pool &pool, const Tin *in, Tout *out, long long n, int *flags)
 {
@@ -137,7 +143,7 @@ cudaError_t scan_impl(Pool &pool, const Tin *in, Tout *out, long long n, int *fl
     unsigned long long *status = reinterpret_cast<unsigned long long *>(scratch + 16);
     cudaError_t e = cudaMemsetAsync(scratch, 0, bytes, pool.stream);
     if (e != cudaSuccess) { pool.free(scratch); return e; }
-    { k_scan<Tin, Tout><<<(unsigned)tiles, SCAN_THREADS, 0, pool.stream>>>(in, out, n, status, ticket, flags); ::tsg::count_launch(); }
+    { k_scan<Tin, Tout><<<(unsigned)tiles, SCAN_THREADS, 0, pool.stream>>>(in, out, n, status, ticket, flags, SPIN_LIMIT); ::tsg::count_launch(); }
     e = cudaGetLastError();
     pool.free(scratch);
     return e;
@@ -166,8 +172,41 @@ cudaError_t scan_i32_to_i64_in(cudaStream_t s, const int *in, long long *out, lo
     }
     const long long tiles = scan_status_words(n);
     if (tiles > (1ll << 30)) return cudaErrorInvalidValue;
-    { k_scan<int, long long><<<(unsigned)tiles, SCAN_THREADS, 0, s>>>(in, out, n, status, ticket, flags); ::tsg::count_launch(); }
+    { k_scan<int, long long><<<(unsigned)tiles, SCAN_THREADS, 0, s>>>(in, out, n, status, ticket, flags, SPIN_LIMIT); ::tsg::count_launch(); }
     return cudaGetLastError();
+}
+
+// The bounded-wait check behind tsg_check_bounded_wait: the scan of n ones
+// with the ticket starting at 1, so that no CTA takes tile 0 and tile 0's
+// sum is never published.  Tile 1 (and every tile whose look-back reaches
+// tile 0) waits for it until spin_limit polls, then sets FLAG_TIMEOUT and
+// finishes.  Bounds: the grid has `tiles` CTAs, which take tiles 1..tiles,
+// so `status` needs tiles + 1 words (the last CTA's tile publishes into word
+// `tiles`; its items all lie past n and are neither read nor written).
+cudaError_t scan_unpublished_tile(Pool &pool, long long n, int spin_limit, int *flags)
+{
+    if (n <= 0 || spin_limit < 1) return cudaErrorInvalidValue;
+    const long long tiles = scan_status_words(n);
+    if (tiles > (1ll << 20)) return cudaErrorInvalidValue;
+    int *in = pool.alloc_n<int>(n);
+    long long *out = pool.alloc_n<long long>(n + 1);
+    char *scratch = static_cast<char *>(pool.alloc(16 + sizeof(unsigned long long) * (size_t)(tiles + 1)));
+    cudaError_t e = (in && out && scratch) ? cudaSuccess : cudaErrorMemoryAllocation;
+    if (e == cudaSuccess) e = cudaMemsetAsync(scratch, 0, 16 + sizeof(unsigned long long) * (size_t)(tiles + 1), pool.stream);
+    if (e == cudaSuccess) { k_fill_ones<<<(unsigned)((n + 255) / 256), 256, 0, pool.stream>>>(in, n); ::tsg::count_launch(); }
+    if (e == cudaSuccess) e = cudaGetLastError();
+    unsigned *ticket = reinterpret_cast<unsigned *>(scratch);
+    unsigned long long *status = reinterpret_cast<unsigned long long *>(scratch + 16);
+    const unsigned one = 1;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(ticket, &one, sizeof(one), cudaMemcpyHostToDevice, pool.stream);
+    if (e == cudaSuccess) {
+        k_scan<int, long long><<<(unsigned)tiles, SCAN_THREADS, 0, pool.stream>>>(in, out, n, status, ticket, flags, spin_limit);
+        ::tsg::count_launch();
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(pool.stream);   // `one` is host stack memory
+    pool.free(in); pool.free(out); pool.free(scratch);
+    return e;
 }
 
 }  // namespace tsg
