@@ -423,6 +423,13 @@ tsg_status tsg_tiles_download(tsg_ctx *ctx, const tsg_tiles *T, int64_t *blkrowp
  * row_ptr receives int64 values whatever the source width. */
 tsg_status tsg_csr_download(tsg_ctx *ctx, const tsg_csr *M, int64_t *row_ptr, int32_t *col, double *val);
 
+/* Copy a CSR (host or device, either row-pointer width) into device memory
+ * of the context's device that the library owns (tsg_csr_free releases
+ * it), so that one operand can be multiplied many times without the
+ * upload.  The reference's driver does the same: its 20 timed runs start
+ * from tile arrays already on the device (main_spgemm-col.cu:4448-4503). */
+tsg_status tsg_csr_to_device(tsg_ctx *ctx, const tsg_csr *H, tsg_csr *D);
+
 /* Rows [r0, r1) of a CSR (any location) into caller-provided host buffers,
  * for checking or exporting part of a result too large to bring back whole
  * (no counterpart in the reference, which discards C).  row_ptr receives the

@@ -149,6 +149,7 @@ SIGNATURES = {
     "tsg_inject_alloc_failure": (C.c_int, [C.c_int32, C.c_int64]),
     "tsg_alloc_failure_pending": (C.c_int64, [C.c_int32]),
     "tsg_check_bounded_wait": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32]),
+    "tsg_csr_to_device": (C.c_int, [C.c_void_p, C.POINTER(tsg_csr), C.POINTER(tsg_csr)]),
     "tsg_csr_download_rows": (C.c_int, [C.c_void_p, C.POINTER(tsg_csr), C.c_int32, C.c_int32, C.c_void_p,
                                         C.c_void_p, C.c_void_p]),
 }

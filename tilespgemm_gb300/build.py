@@ -5,6 +5,9 @@ process in parallel, for exactly one target: ``-gencode
 arch=compute_103a,code=sm_103a`` (GB300).  The CUDA runtime is linked
 statically so the library loads without a toolkit on the library path.
 
+The command-line front end (``cli/tsg.c``, plain C) is linked against it
+as ``_lib/tsg``.
+
 The oracle (``oracle/tsg_oracle.c``) is test infrastructure; it is built
 beside it as ``oracle/liboracle.so`` so that tests and the CPU-baseline leg
 of ``bench.py`` can load it.  When a reference checkout is present, the
@@ -82,6 +85,23 @@ def build_library(verbose: bool = False, jobs: int | None = None) -> Path:
     return LIB
 
 
+CLI_SRC = PKG / "cli" / "tsg.c"
+CLI = LIBDIR / "tsg"
+
+
+def build_cli() -> Path:
+    """The command-line front end (plain C99 against include/tilespgemm.h),
+    linked to libtilespgemm.so beside it."""
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        raise RuntimeError("gcc not found")
+    if _stale(CLI, [CLI_SRC, LIB, ROOT / "include" / "tilespgemm.h"]):
+        _run([cc, "-std=c99", "-D_POSIX_C_SOURCE=200809L", "-O2", "-Wall", "-Wextra", "-Werror",
+              f"-I{ROOT / 'include'}", str(CLI_SRC), f"-L{LIBDIR}", "-ltilespgemm", "-Wl,-rpath,$ORIGIN",
+              "-o", str(CLI)])
+    return CLI
+
+
 def build_oracle() -> Path:
     cc = shutil.which("gcc") or shutil.which("cc")
     if cc is None:
@@ -105,6 +125,7 @@ def build_reference() -> bool:
 
 def build_all(verbose: bool = False) -> None:
     build_library(verbose=verbose)
+    build_cli()
     build_oracle()
     build_reference()
 

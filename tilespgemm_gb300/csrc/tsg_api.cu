@@ -1261,6 +1261,39 @@ tsg_status tsg_csr_download(tsg_ctx *ctx, const tsg_csr *M, int64_t *row_ptr, in
 }
 
 
+tsg_status tsg_csr_to_device(tsg_ctx *ctx, const tsg_csr *H, tsg_csr *D)
+{
+    if (!ctx || !D) return fail(TSG_ERR_INVALID_ARG, "ctx/D is NULL");
+    tsg_status r = check_csr(H, "H");
+    if (r) return r;
+    CUDA_OK(cudaSetDevice(ctx->device));
+    const cudaMemcpyKind kind = H->where == TSG_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+    const size_t rpb = (size_t)(H->m + 1) * (H->rowptr_bits == 64 ? 8 : 4);
+    const size_t cb = sizeof(int) * (size_t)H->nnz, vb = sizeof(double) * (size_t)H->nnz;
+    Pool pool{ctx->pool, ctx->stream};
+    void *rp = pool.alloc(rpb);
+    int *col = static_cast<int *>(pool.alloc(cb));
+    double *val = static_cast<double *>(pool.alloc(vb));
+    cudaError_t e = (rp && col && val) ? cudaSuccess : cudaErrorMemoryAllocation;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(rp, H->row_ptr, rpb, kind, ctx->stream);
+    if (e == cudaSuccess && H->nnz > 0) e = cudaMemcpyAsync(col, H->col, cb, kind, ctx->stream);
+    if (e == cudaSuccess && H->nnz > 0) e = cudaMemcpyAsync(val, H->val, vb, kind, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) {
+        pool.free(rp); pool.free(col); pool.free(val);
+        cudaStreamSynchronize(ctx->stream);
+        cudaGetLastError();
+        return fail(cuda_status(e), "tsg_csr_to_device: %s", cudaGetErrorString(e));
+    }
+    OutOwner *o = new OutOwner();
+    o->ctx = ctx;
+    o->where = TSG_MEM_DEVICE;
+    o->blocks = {{rp, 0}, {col, 0}, {val, 0}};
+    D->m = H->m; D->n = H->n; D->nnz = H->nnz; D->rowptr_bits = H->rowptr_bits; D->where = TSG_MEM_DEVICE;
+    D->row_ptr = rp; D->col = col; D->val = val; D->owner = o;
+    return TSG_OK;
+}
+
 tsg_status tsg_csr_download_rows(tsg_ctx *ctx, const tsg_csr *M, int32_t r0, int32_t r1, int64_t *row_ptr,
                                  int32_t *col, double *val)
 {
