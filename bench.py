@@ -3,7 +3,8 @@
 project is measured on), through the library's C ABI.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload st27-96|lap256|rmat16-aat] [--cpu-seconds S]
+                    [--workload st27-96|st27-<side>|lap256|rmat<s>-aat|batched|served]
+                    [--cpu-seconds S] [--no-e2e] [--no-extras]
 
 One step = one full SpGEMM: CSR A in device memory -> tile conversion ->
 step 1 -> step 2 -> numeric -> CSR C in device memory (C is freed after the
@@ -12,6 +13,14 @@ the library's stream; `e2e` repeats the step through the same C ABI with
 host operands (pinned) and a host C, the copies inside the timed region.
 Under torchrun each rank runs its own replica of the workload (weak scaling)
 and rank 0 prints one JSON line with the max time over ranks.
+
+The default line (st27-96, one GPU) also carries the benchmark's other
+workloads, each run in a child process after the headline's timing:
+`configs` (2D Laplacian 256^2 A*A and R-MAT 2^20 A*A^T, device-resident),
+`batched` (4,096 instances in waves, against one call per instance and
+numeric-only graph replays) and `served` (the Poisson stream at 2,000
+requests/s offered, then at 0.5x and 0.9x of the measured capacity, with
+the host link's share of wall time).  `--no-extras` leaves them out.
 
 --impl reference times the reference's own CPU algorithm for the path
 (thmkl_dcsrmultcsr, restated in oracle/tsg_oracle.c) on the host cores, on a
@@ -365,8 +374,16 @@ def run_ours(args) -> None:
         "gpu_launches_per_step": launches / args.steps,
         "clocks": clk.summary(),
     }
-    print(json.dumps(out))
+    if out["e2e"] is not None:
+        # the host link's share: the bytes each way at the link's measured
+        # bandwidth, as if nothing overlapped them
+        link = link_gbs()
+        floor = h2d / (link["h2d"] * 1e6) + d2h / (link["d2h"] * 1e6)
+        out["e2e"].update({"host_link_gbs": link, "link_floor_ms": floor, "beyond_link_floor_ms": ms_e2e - floor})
     ctx.close()
+    if world == 1 and not args.no_extras and args.workload == "st27-96":
+        out.update(sub_benchmarks(args))
+    print(json.dumps(out))
     if dist is not None:
         dist.destroy_process_group()
 
@@ -450,36 +467,140 @@ def run_batched(args) -> None:
     ctx.close()
 
 
+def link_gbs() -> dict:
+    """Host-link bandwidth of this machine: one 2 GiB pinned copy each way, three
+    times, CUDA events (the link bounds every host-memory result)."""
+    import torch
+    n = 1 << 31
+    h = torch.empty(n, dtype=torch.uint8).pin_memory()
+    d = torch.empty(n, dtype=torch.uint8, device="cuda")
+    out = {}
+    for name, dst, src in (("h2d", d, h), ("d2h", h, d)):
+        dst.copy_(src, non_blocking=True)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(3):
+            dst.copy_(src, non_blocking=True)
+        e1.record()
+        e1.synchronize()
+        out[name] = 3 * n / (e0.elapsed_time(e1) * 1e6)
+    del h, d
+    return out
+
+
 def run_served(args) -> None:
-    """Served stream: p50/p99 latency and throughput (tsg_server_*)."""
+    """Served streams through tsg_server_*: p50/p99 latency and throughput.
+
+    1. The configured stream (Poisson, 2,000 requests/s offered) after a
+       warm-up on another realization: far above what the GPU and the host
+       link complete, so its latencies are the time the backlog takes to
+       drain; its completion rate is the capacity.
+    2. Streams of the same kind offered at 0.5x and 0.9x of that capacity
+       (other seeds and keys), where latency is per-request time, not
+       backlog.
+    For each: completed requests/s, p50/p99/mean latency, refusals, and the
+    share of wall time the host link needed for the results (C's bytes at
+    the measured device-to-host bandwidth)."""
     from tilespgemm_gb300.serving import Server, make_stream, run_stream
     procs = max(1, min(16, (os.cpu_count() or 1)))
-    reqs = make_stream(args.serve_requests, seed=1, rate=args.serve_rate,
-                       rmat_scale=(12, args.serve_max_scale), procs=procs)
-    # warm-up: another realization of the same stream (other pattern keys, so
-    # the timed run's plans are not cached), which also warms the pinned
-    # result buffers
-    warm = make_stream(max(16, args.serve_requests // 4), seed=2, rate=args.serve_rate,
-                       rmat_scale=(12, args.serve_max_scale), procs=procs, key_base=1 << 40)
+    scale = (12, args.serve_max_scale)
+    reqs = make_stream(args.serve_requests, seed=1, rate=args.serve_rate, rmat_scale=scale, procs=procs)
+    warm = make_stream(max(16, args.serve_requests // 4), seed=2, rate=args.serve_rate, rmat_scale=scale,
+                       procs=procs, key_base=1 << 40)
+    n_sub = max(40, args.serve_requests // 3)
+    sub = [make_stream(n_sub, seed=3 + j, rate=1.0, rmat_scale=scale, procs=procs, key_base=(2 + j) << 40)
+           for j in range(2)]
+    link = link_gbs()
+
+    def summary(st, offered):
+        done = [r for r in st["results"] if r is not None]
+        lat = [r[1]["latency_ms"] for r in done]
+        link_s = sum(12 * r[1]["nnz"] for r in done) / (link["d2h"] * 1e9)
+        return {"offered_rps": offered, "requests": st["n"], "completed": st["completed"],
+                "throughput_rps": st["throughput_rps"], "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"],
+                "mean_ms": st["mean_ms"], "max_ms": float(max(lat)) if lat else None,
+                "refused_over_budget": st["refused"], "numeric_only_requests": st["numeric_only"],
+                "wall_s": st["wall_s"], "c_entries_returned": int(sum(r[1]["nnz"] for r in done)),
+                "host_link_s": link_s, "host_link_frac_of_wall": link_s / st["wall_s"] if st["wall_s"] else None}
+
     with Server(workers=args.serve_workers, budget_gb=64.0) as srv:
         run_stream(srv, warm, realtime=False, download=False)
-        st = run_stream(srv, reqs, realtime=True, download=False)
-    done = [r for r in st["results"] if r is not None]
-    lat = [r[1]["latency_ms"] for r in done]
-    out_nnz = sum(r[1]["nnz"] for r in done)
+        with ClockSampler(0) as clk:
+            st = run_stream(srv, reqs, realtime=True, download=False)
+        top = summary(st, args.serve_rate)
+        cap = top["throughput_rps"]
+        below = []
+        for frac, rq in zip((0.5, 0.9), sub):
+            rate = frac * cap
+            for r in rq:                 # the drawn stream re-timed: gaps scale as 1/rate
+                r["t"] = r["t"] / rate
+            with ClockSampler(0) as clk2:
+                s2 = run_stream(srv, rq, realtime=True, download=False)
+            d = summary(s2, rate)
+            d["fraction_of_capacity"] = frac
+            d["clocks"] = clk2.summary()
+            below.append(d)
     out = {
-        "metric": "served SpGEMM requests/s with p50/p99 latency", "value": st["throughput_rps"], "unit": "requests/s",
-        "n_gpus": 1, "steps": 1, "warmup": 1, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64", "data": "synthetic (seeded Poisson stream)",
+        "metric": "served SpGEMM requests/s with p50/p99 latency", "value": top["throughput_rps"],
+        "unit": "requests/s", "n_gpus": 1, "steps": 1, "warmup": 1, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Poisson stream)",
         "config": {"workload": f"served: {len(reqs)} requests, Poisson {args.serve_rate:.0f}/s, 50/50 Laplacian "
                                f"(side 32-512) / R-MAT (2^12-2^{args.serve_max_scale}, 8-32/row), 50/50 A*A / A*A^T, "
                                "30% numeric-only repeats, 64 GB budget", "workers": args.serve_workers},
-        "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "mean_ms": st["mean_ms"],
-        "max_ms": float(max(lat)) if lat else None, "completed": st["completed"],
-        "refused_over_budget": st["refused"], "numeric_only_requests": st["numeric_only"],
-        "c_entries_returned": int(out_nnz), "wall_s": st["wall_s"],
+        **{k: v for k, v in top.items() if k != "offered_rps"},
+        "note": "offered far above capacity: these latencies measure the backlog's drain; see below_capacity",
+        "below_capacity": below,
+        "host_link_gbs": link,
+        "clocks": clk.summary(),
     }
     print(json.dumps(out))
+
+
+def run_sub(args, workload: str, extra: list) -> dict:
+    """One more workload in a child process (its memory -- R-MAT 2^20's
+    116 GB C, the served stream's pinned buffers -- goes with it): its JSON
+    line, or the reason it has none."""
+    cmd = [sys.executable, str(ROOT / "bench.py"), "--workload", workload, "--no-cpu-baseline", "--no-e2e",
+           "--no-extras", *extra]
+    t0 = time.perf_counter()
+    try:
+        res = subprocess.run(cmd, capture_output=True, text=True, timeout=args.sub_timeout)
+    except subprocess.TimeoutExpired:
+        return {"workload": workload, "error": f"timed out after {args.sub_timeout} s"}
+    lines = [x for x in res.stdout.splitlines() if x.startswith("{")]
+    if res.returncode != 0 or not lines:
+        return {"workload": workload, "error": f"exit {res.returncode}: {res.stderr.strip()[-400:]}"}
+    d = json.loads(lines[-1])
+    d.setdefault("wall_s", time.perf_counter() - t0)
+    return d
+
+
+def sub_benchmarks(args) -> dict:
+    """The benchmark's other workloads, each measured on its own (device-
+    resident operands and results, CUDA events, their own clock records),
+    reported beside the headline and outside its timing."""
+    out = {"configs": {}}
+    for w, steps in (("lap256", 20), ("rmat20-aat", 3)):
+        d = run_sub(args, w, ["--steps", str(steps), "--warmup", "3"])
+        if "error" in d:
+            out["configs"][w] = d
+            continue
+        out["configs"][w] = {"workload": d["config"]["workload"], "value": d["value"], "unit": d["unit"],
+                             "ms_per_step": d["ms_per_step"], "phases_ms": d["phases_ms"],
+                             "nnz_a": d["config"]["nnz_a"], "nnz_cub": d["config"]["nnz_cub"],
+                             "nnz_c": d["config"]["nnz_c"], "host_waits_per_step": d["host_waits_per_step"],
+                             "gpu_launches_per_step": d["gpu_launches_per_step"],
+                             "whole_step_hbm_frac": d["roofline"]["whole_step"]["frac"],
+                             "numeric_fp64_frac": d["roofline"]["fp64"]["frac"], "clocks": d["clocks"]}
+    b = run_sub(args, "batched", ["--steps", "5", "--warmup", "3"])
+    out["batched"] = b if "error" in b else {k: b[k] for k in (
+        "metric", "value", "unit", "ms_per_step", "config", "one_at_a_time", "speedup_vs_one_at_a_time",
+        "numeric_replay", "gflops_batched", "gpu_launches_per_step", "tuned", "clocks") if k in b}
+    s_ = run_sub(args, "served", [])
+    out["served"] = s_ if "error" in s_ else {k: v for k, v in s_.items() if k not in (
+        "n_gpus", "steps", "warmup", "higher_is_better", "scaling", "vs_baseline", "dtype", "data")}
+    return out
 
 
 def main() -> None:
@@ -492,6 +613,9 @@ def main() -> None:
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-operand leg (C of R-MAT 2^20 is 116 GB)")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="leave the other workloads (lap256, rmat20-aat, batched, served) out of the headline line")
+    ap.add_argument("--sub-timeout", type=float, default=600.0)
     ap.add_argument("--batch-count", type=int, default=4096)
     ap.add_argument("--batch-waves", type=int, default=8)
     ap.add_argument("--serve-requests", type=int, default=400)
