@@ -608,13 +608,14 @@ tsg_status plan_symbolic(tsg_ctx *ctx, Pool &pool, Scratch &sc, tsg_op op, const
         return fail(TSG_ERR_OOM, "device pool allocation failed for C tiles");
     NumericBinParams bp{ctx->opts.dense_tile_min, ctx->opts.smem_acc_max, ctx->opts.row_acc_max, P.rpA,
                         ctx->opts.rows_global};
-    CUDA_OK(symbolic_fill_fused(pool, TA, TB, P.m, P.crp, P.ccol, P.cmask, rowcnt, P.bin, bp, ctx->dstat + ST_BINS,
-                                P.binlist, P.rowlist, cnt, wide, ctx->dflags, P.rpB, P.colB, P.rpA, P.colA));
+    CUDA_OK(symbolic_fill_fused(pool, TA, TB, P.m, P.crp, P.ccol, P.cmask, rowcnt, cnt, wide, ctx->dflags, P.rpB,
+                                P.colB, P.rpA, P.colA));
     tm.mark();  // 2
-    CUDA_OK(step2_masks(pool, TA, TB, P.m, P.blkm, P.crp, P.ccol, P.cmask, rowcnt, maxS, maxSpan, bp, P.bin,
-                        ctx->dstat + ST_BINS, P.binlist, P.rowlist, ctx->dflags, defer, ndefer, P.rpB, P.colB,
-                        P.rpA, P.colA, P.b_increasing, ctx->side, ctx->fork, ctx->join));
+    CUDA_OK(step2_masks(pool, TA, TB, P.m, P.blkm, P.crp, P.ccol, P.cmask, rowcnt, maxS, maxSpan, ctx->dflags, defer,
+                        ndefer, P.rpB, P.colB, P.rpA, P.colA, P.b_increasing, ctx->side, ctx->fork, ctx->join));
     CUDA_OK(scan_i32_to_i64(pool, rowcnt, P.rowptrC, P.m, ctx->dflags));
+    CUDA_OK(bin_tilerows(pool, P.blkm, P.m, P.crp, P.ccol, P.rowptrC, bp, P.bin, ctx->dstat + ST_BINS, P.binlist,
+                         P.rowlist));
     CUDA_OK(cudaMemcpyAsync(ctx->dstat + ST_NNZC, P.rowptrC + P.m, sizeof(long long), cudaMemcpyDeviceToDevice,
                             ctx->stream));
     r = host_wait(ctx, &P.nsync);

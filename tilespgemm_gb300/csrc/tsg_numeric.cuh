@@ -132,15 +132,7 @@ constexpr int BS_ROWCNT = 2 * NBIN;
 constexpr int BS_ROWREQ = 2 * NBIN + NROWCLS;
 constexpr int BS_SLOTS = 2 * NBIN + 2 * NROWCLS;
 
-// Step 2's record of a tile-row's bin (one thread): counts, shared-memory
-// maximum and the bin's work list.
-__device__ __forceinline__ void record_bin(int b, long long req, int i, int blkm, long long *binstat, int *binlist) {
-    const unsigned long long pos = atomicAdd((unsigned long long *)&binstat[b], 1ull);
-    binlist[(long long)b * blkm + (long long)pos] = i;
-    atomicMax((long long *)&binstat[NBIN + b], req);
-}
-
-// ...and of one row R of a BIN_ROWS tile-row (one thread per row).
+// The record of one row R of a BIN_ROWS tile-row (one thread per row).
 __device__ __forceinline__ void record_row(const NumericBinParams &bp, long long S, long long row_nnz, long long span,
                                            int R, int m, long long *binstat, int *rowlist) {
     if (row_nnz == 0) return;
@@ -170,8 +162,7 @@ struct NumericArgs {
 
 cudaError_t step2_masks(Pool &pool, const TileCSR &A, const TileCSR &B, int m, int blkm, const long long *crp,
                         const int *ccol, uint16_t *cmask, int *rowcnt, int max_tiles_per_row, int max_span,
-                        const NumericBinParams &bp, unsigned char *bin, long long *binstat, int *binlist,
-                        int *rowlist, int *flags, const int *defer_list, int ndefer, const long long *erpB,
+                        int *flags, const int *defer_list, int ndefer, const long long *erpB,
                         const int *ecolB, const long long *erpA, const int *ecolA, bool b_sorted,
                         cudaStream_t side, cudaEvent_t fork, cudaEvent_t join);
 
@@ -192,10 +183,14 @@ cudaError_t numeric_run(Pool &pool, const NumericArgs &a, const long long *binst
                         cudaEvent_t join = nullptr);
 
 cudaError_t symbolic_fill_fused(Pool &pool, const TileCSR &A, const TileCSR &B, int m, const long long *crp,
-                                int *ccol, uint16_t *cmask, int *rowcnt, unsigned char *bin,
-                                const NumericBinParams &bp, long long *binstat, int *binlist, int *rowlist, int *cnt,
-                                int *wide, int *flags, const long long *erpB, const int *ecolB,
-                                const long long *erpA, const int *ecolA);
+                                int *ccol, uint16_t *cmask, int *rowcnt, int *cnt, int *wide, int *flags,
+                                const long long *erpB, const int *ecolB, const long long *erpA, const int *ecolA);
+
+// Numeric bins of C's tile-rows (bin[blkm], per-bin work lists and
+// statistics in binstat, row classes of BIN_ROWS tile-rows in rowlist), from
+// C's tile structure and row pointer once step 2 and its scan are done.
+cudaError_t bin_tilerows(Pool &pool, int blkm, int m, const long long *crp, const int *ccol, const long long *rowptrC,
+                         const NumericBinParams &bp, unsigned char *bin, long long *binstat, int *binlist, int *rowlist);
 cudaError_t masks_to_tile_major_i32(Pool &pool, int blkm, const int *rowptr, const uint16_t *src, uint16_t *dst);
 cudaError_t masks_to_tile_major_i64(Pool &pool, int blkm, const long long *rowptr, const uint16_t *src, uint16_t *dst);
 

@@ -202,12 +202,17 @@ k_union_count(typename KS::Params P, int nrows, int *cnt, int *wide_list, int *w
     }
 }
 
+// tile-rows of up to this many tiles build their masks in shared memory
+// (the warp's 16 x FILL_SMEM_TILES row masks), the rest with global atomics
+constexpr int FILL_SMEM_TILES = 64;
+
 template <class KS, bool MASK, typename TP>
 __global__ void __launch_bounds__(WPC * 32)
 k_union_fill(typename KS::Params P, int nrows, const TP *rowptr, int *out, uint16_t *mask)
 {
     __shared__ unsigned s_bm[WPC][NW];
     __shared__ unsigned short s_pref[WPC][NW];
+    __shared__ unsigned s_mw[MASK ? WPC : 1][MASK ? FILL_SMEM_TILES * TILE / 2 : 1];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int row = blockIdx.x * WPC + warp;
     if (row >= nrows) return;
@@ -248,15 +253,30 @@ k_union_fill(typename KS::Params P, int nrows, const TP *rowptr, int *out, uint1
         }
     }
     if (MASK) {
-        // zero this tile-row's masks, then OR the entries in
         unsigned *mw = reinterpret_cast<unsigned *>(mask) + base * 8;
-        for (int t = lane; t < total * 8; t += 32) mw[t] = 0u;
-        __syncwarp();
-        ks.each(lane, 32, [&](int key, int r, int c) {
-            int o = key - kmin, w = o >> 5;
-            int slot = pref[w] + __popc(bm[w] & ((1u << (o & 31)) - 1u));
-            atomic_or_mask16(mask, base * TILE + (long long)r * total + slot, 1u << (TILE - 1 - c));
-        });
+        if (total <= FILL_SMEM_TILES) {
+            // the row masks in shared memory (16 x total halfwords, row-major),
+            // written out once: no global atomics
+            unsigned *sw = s_mw[warp];
+            for (int t = lane; t < total * 8; t += 32) sw[t] = 0u;
+            __syncwarp();
+            ks.each(lane, 32, [&](int key, int r, int c) {
+                const int o = key - kmin, w = o >> 5;
+                const int idx = r * total + pref[w] + __popc(bm[w] & ((1u << (o & 31)) - 1u));
+                atomicOr(&sw[idx >> 1], (1u << (TILE - 1 - c)) << ((idx & 1) * 16));
+            });
+            __syncwarp();
+            for (int t = lane; t < total * 8; t += 32) mw[t] = sw[t];
+        } else {
+            // zero this tile-row's masks, then OR the entries in
+            for (int t = lane; t < total * 8; t += 32) mw[t] = 0u;
+            __syncwarp();
+            ks.each(lane, 32, [&](int key, int r, int c) {
+                int o = key - kmin, w = o >> 5;
+                int slot = pref[w] + __popc(bm[w] & ((1u << (o & 31)) - 1u));
+                atomic_or_mask16(mask, base * TILE + (long long)r * total + slot, 1u << (TILE - 1 - c));
+            });
+        }
     }
 }
 
@@ -278,8 +298,8 @@ static_assert(NW * 32 == FUSED_MAX_SPAN, "fused window");
 // Then per-row popcounts give C's row counts and the numeric bin.
 __global__ void __launch_bounds__(FWPC * 32)
 k_sym_fused(UnionKeys::Params P, int blkm, int m, const long long *__restrict__ crp, int *ccol,
-            const uint16_t *__restrict__ amask, const uint16_t *__restrict__ bmask, uint16_t *cmask, int *rowcnt,
-            unsigned char *bin, NumericBinParams bp, long long *binstat, int *binlist, int *rowlist, int *flags,
+            const uint16_t *__restrict__ amaskT, const uint16_t *__restrict__ bmaskT, uint16_t *cmask, int *rowcnt,
+            int *flags,
             const long long *__restrict__ erpB, const int *__restrict__ ecolB, const long long *__restrict__ erpA,
             const int *__restrict__ ecolA)
 {
@@ -378,36 +398,49 @@ k_sym_fused(UnionKeys::Params P, int blkm, int m, const long long *__restrict__ 
     __syncwarp();
     has_long = __any_sync(0xffffffffu, has_long);
     for (int ab = a0; ab < a1 && has_long; ab += 32) {
-        // B tile-row of up to 32 A tiles, fetched by the lanes at once
+        // up to 32 A tiles at once, one per lane: B's tile-row, the columns
+        // the A tile uses (bit c: local column c; with the entry walk only
+        // those whose B row it left), and what the element path would cost
+        // over those columns (32-entry chunks of their B rows)
         const int nac = min(32, a1 - ab);
-        int q0l = 0, nql = 0;
+        int q0l = 0, nql = 0, ktl = 0, eitl = 0;
+        unsigned colsl = 0u;
         if (lane < nac) {
-            const int kt = P.acol[ab + lane];
-            q0l = P.brp[kt];
-            nql = P.brp[kt + 1] - q0l;
+            const int a = ab + lane;
+            ktl = P.acol[a];
+            q0l = P.brp[ktl];
+            nql = P.brp[ktl + 1] - q0l;
+            const uint4 *at = reinterpret_cast<const uint4 *>(amaskT + (long long)a * TILE);
+            const uint4 x0 = at[0], x1 = at[1];
+            unsigned u = x0.x | x0.y | x0.z | x0.w | x1.x | x1.y | x1.z | x1.w;
+            u = (u | (u >> 16)) & 0xffffu;               // bit 15-c: column c used
+            colsl = __brev(u) >> 16;                      // bit c: column c used
+            for (unsigned cs = colsl; cs; cs &= cs - 1) {
+                const int c = __ffs(cs) - 1;
+                const long long len = erpB[(long long)ktl * TILE + c + 1] - erpB[(long long)ktl * TILE + c];
+                if (by_entry && len <= FUSED_ENTRY_B_MAX) colsl &= ~(1u << c);   // the entry walk did it
+                else eitl += (int)((len + 31) >> 5);
+            }
         }
+        // the next A tile's row masks are loaded while the current one is walked
+        unsigned ma_next = (lane < TILE) ? (unsigned)amaskT[(long long)ab * TILE + lane] : 0u;
         for (int t = 0; t < nac; ++t) {
             const int q0 = __shfl_sync(0xffffffffu, q0l, t), nq = __shfl_sync(0xffffffffu, nql, t);
-            const int a = ab + t;
-            unsigned ma = (lane < TILE) ? (unsigned)amask[(long long)a0 * TILE + (long long)lane * na + (a - a0)] : 0u;
-            if (by_entry) {
-                // only the columns whose B rows the entry walk left (a used
-                // column names a row of B, so the row pointer reads stay in range)
-                const unsigned used = __brev(__reduce_or_sync(0xffffffffu, ma)) >> 16;
-                const int ktu = P.acol[a];
-                const bool lng = lane < TILE && ((used >> lane) & 1u) &&
-                                 erpB[ktu * TILE + lane + 1] - erpB[ktu * TILE + lane] > FUSED_ENTRY_B_MAX;
-                ma &= __brev(__ballot_sync(0xffffffffu, lng)) >> 16;
-                if (!__any_sync(0xffffffffu, ma != 0u)) continue;
-            }
+            const int kt = __shfl_sync(0xffffffffu, ktl, t);
+            const unsigned acols = __shfl_sync(0xffffffffu, colsl, t);
+            const int elem_iters = __shfl_sync(0xffffffffu, eitl, t);
+            unsigned ma = ma_next;
+            if (t + 1 < nac) ma_next = (lane < TILE) ? (unsigned)amaskT[(long long)(ab + t + 1) * TILE + lane] : 0u;
+            if (!acols) continue;
+            ma &= __brev(acols) >> 16;                    // row masks restricted to those columns
             // A tiles with few entries: B's rows element by element (as in the
             // CTA step-2 kernel); lanes may then share a slot, so word atomics
-            const unsigned acols = __brev(__reduce_or_sync(0xffffffffu, ma)) >> 16;
-            const int kt = P.acol[a];
-            int eb0 = 0, eb1 = 0;   // operands hold < 2^31 entries
-            if (lane < TILE && ((acols >> lane) & 1u)) { eb0 = (int)erpB[kt * TILE + lane]; eb1 = (int)erpB[kt * TILE + lane + 1]; }
-            const int elem_iters = warp_sum_int((eb1 - eb0 + 31) >> 5);
             if (elem_iters <= 3 * ((nq + 31) >> 5)) {
+                int eb0 = 0, eb1 = 0;   // operands hold < 2^31 entries
+                if (lane < TILE && ((acols >> lane) & 1u)) {
+                    eb0 = (int)erpB[(long long)kt * TILE + lane];
+                    eb1 = (int)erpB[(long long)kt * TILE + lane + 1];
+                }
                 unsigned *mw = reinterpret_cast<unsigned *>(msk);
                 __syncwarp();
                 for (unsigned cs = acols; cs; cs &= cs - 1) {
@@ -432,7 +465,16 @@ k_sym_fused(UnionKeys::Params P, int blkm, int m, const long long *__restrict__ 
                 __syncwarp();
                 continue;
             }
-            const uint16_t *bq = bmask + (long long)q0 * TILE;
+            // tile path: lanes take B's tiles (k,j) -- the bitmap rank of j
+            // is the slot of C tile (i,j) -- and load each tile's 16 row
+            // masks at once (tile-major copy: two 16-byte loads); then per
+            // column c of the A tile the rows of A that use it (a ballot,
+            // uniform) get B's row c OR'ed in.  Lanes hold distinct slots,
+            // so the shared-memory updates need no atomics.
+            unsigned colrows[TILE];
+#pragma unroll
+            for (int c = 0; c < TILE; ++c)
+                colrows[c] = ((acols >> c) & 1u) ? __ballot_sync(0xffffffffu, (ma >> (TILE - 1 - c)) & 1u) & 0xffffu : 0u;
             for (int qb = 0; qb < nq; qb += 32) {
                 const int q = qb + lane;
                 int slot = -1;
@@ -444,28 +486,20 @@ k_sym_fused(UnionKeys::Params P, int blkm, int m, const long long *__restrict__ 
                     }
                     if (slot < 0 || slot >= S) { bad = true; slot = -1; }
                 }
-                // half the A tile's columns at a time (fewer registers, more
-                // warps per SM): the rows that use local column c (a ballot,
-                // uniform), the B tile's rows c -- independent loads, issued
-                // together -- then the ORs
+                uint4 lo = make_uint4(0u, 0u, 0u, 0u), hi = lo;
+                if (slot >= 0) {
+                    const uint4 *bt = reinterpret_cast<const uint4 *>(bmaskT + (long long)(q0 + q) * TILE);
+                    lo = bt[0];
+                    hi = bt[1];
+                }
+                const unsigned bw[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
 #pragma unroll
-                for (int h = 0; h < TILE; h += TILE / 2) {
-                    unsigned colrows[TILE / 2], brow[TILE / 2];
-#pragma unroll
-                    for (int c = 0; c < TILE / 2; ++c)
-                        colrows[c] = __ballot_sync(0xffffffffu, (ma >> (TILE - 1 - (h + c))) & 1u) & 0xffffu;
-#pragma unroll
-                    for (int c = 0; c < TILE / 2; ++c)
-                        brow[c] = (colrows[c] != 0u && slot >= 0) ? (unsigned)bq[(h + c) * nq + q] : 0u;
-#pragma unroll
-                    for (int c = 0; c < TILE / 2; ++c) {
-                        unsigned rws = colrows[c];
-                        const unsigned b = brow[c];
-                        while (rws) {
-                            const int r = __ffs(rws) - 1;
-                            rws &= rws - 1;
-                            if (b) msk[r * S + slot] |= (unsigned short)b;
-                        }
+                for (int c = 0; c < TILE; ++c) {
+                    const unsigned b = (bw[c >> 1] >> ((c & 1) * 16)) & 0xffffu;
+                    if (!b) continue;
+                    for (unsigned rws = colrows[c]; rws; rws &= rws - 1) {
+                        const int r = __ffs(rws) - 1;
+                        msk[r * S + slot] |= (unsigned short)b;
                     }
                 }
             }
@@ -473,26 +507,13 @@ k_sym_fused(UnionKeys::Params P, int blkm, int m, const long long *__restrict__ 
     }
     __syncwarp();
     for (int t = lane; t < S * TILE; t += 32) cmask[c0 * TILE + t] = msk[t];
-    long long nnz_tr = 0;
-    int mycnt = 0;
-    for (int r = 0; r < TILE; ++r) {
+    for (int r = 0; r < rows; ++r) {
         int c = 0;
         for (int sl = lane; sl < S; sl += 32) c += __popc((unsigned)msk[r * S + sl]);
         c = warp_sum_int(c);
-        if (lane == 0 && r < rows) rowcnt[row * TILE + r] = c;
-        if (lane == r) mycnt = c;
-        nnz_tr += c;
+        if (lane == 0) rowcnt[row * TILE + r] = c;
     }
     if (bad) set_flag(flags, FLAG_INTERNAL);
-    int b = 0;
-    if (lane == 0) {
-        long long req = 0;
-        numeric_classify(bp, S, nnz_tr, span, b, req);
-        bin[row] = (unsigned char)b;
-        record_bin(b, req, row, blkm, binstat, binlist);
-    }
-    b = __shfl_sync(0xffffffffu, b, 0);
-    if (b == BIN_ROWS && lane < rows) record_row(bp, S, mycnt, span, row * TILE + lane, m, binstat, rowlist);
 }
 
 // Row-major masks of each tile-row -> 16 consecutive masks per tile (the
@@ -970,19 +991,28 @@ cudaError_t tile_symbolic(Pool &pool, const TileCSR &A, const TileCSR &B, long l
 // then the sorted tile columns of the wide tile-rows (their masks and counts
 // come from step2_masks's CTA kernel).
 cudaError_t symbolic_fill_fused(Pool &pool, const TileCSR &A, const TileCSR &B, int m, const long long *crp,
-                                int *ccol, uint16_t *cmask, int *rowcnt, unsigned char *bin,
-                                const NumericBinParams &bp, long long *binstat, int *binlist, int *rowlist, int *cnt,
-                                int *wide, int *flags, const long long *erpB, const int *ecolB,
-                                const long long *erpA, const int *ecolA)
+                                int *ccol, uint16_t *cmask, int *rowcnt, int *cnt, int *wide, int *flags,
+                                const long long *erpB, const int *ecolB, const long long *erpA, const int *ecolA)
 {
     cudaStream_t s = pool.stream;
     if (A.blkm <= 0) return cudaSuccess;
     UnionKeys::Params P{A.trp, A.tcol, B.trp, B.tcol, B.bmoff, B.bmw};
-    { k_sym_fused<<<(unsigned)((A.blkm + FWPC - 1) / FWPC), FWPC * 32, 0, s>>>(P, A.blkm, m, crp, ccol, A.mask, B.mask,
-                                                                         cmask, rowcnt, bin, bp, binstat, binlist, rowlist, flags,
-                                                                         erpB, ecolB, erpA, ecolA); ::tsg::count_launch(); }
+    // the kernel reads the 16 row masks of a tile at once: tile-major copies
+    // of A's and B's masks (one copy when B is A)
+    uint16_t *amT = pool.alloc_n<uint16_t>(A.cap * TILE + 16);
+    uint16_t *bmT = (A.mask == B.mask) ? amT : pool.alloc_n<uint16_t>(B.cap * TILE + 16);
+    cudaError_t e = (amT && bmT) ? cudaSuccess : cudaErrorMemoryAllocation;
+    if (e == cudaSuccess) e = masks_to_tile_major_i32(pool, A.blkm, A.trp, A.mask, amT);
+    if (e == cudaSuccess && bmT != amT) e = masks_to_tile_major_i32(pool, B.blkm, B.trp, B.mask, bmT);
+    if (e == cudaSuccess) {
+        k_sym_fused<<<(unsigned)((A.blkm + FWPC - 1) / FWPC), FWPC * 32, 0, s>>>(P, A.blkm, m, crp, ccol, amT, bmT,
+                                                                           cmask, rowcnt, flags, erpB, ecolB, erpA, ecolA);
+        ::tsg::count_launch();
+        e = cudaGetLastError();
+    }
+    if (bmT && bmT != amT) pool.free(bmT);
+    pool.free(amT);
     (void)cnt;
-    cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess)
         e = launch_union_wide<UnionKeys, true, false, long long>(pool, P, wide, wide + A.blkm, nullptr, nullptr, crp, ccol,
                                                                  nullptr);
