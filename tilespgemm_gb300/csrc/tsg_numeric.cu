@@ -97,8 +97,24 @@ __device__ __forceinline__ int out_pos(const TileRowSmem &t, const unsigned *wro
     return (unsigned)p < (unsigned)t.nacc ? p : -1;
 }
 
+// out_pos for the map layout without early exits: every read uses an index
+// clamped into its array, and the checks combine into one predicate, so the
+// compiler selects instead of branching (a product costs about 80 warp
+// instructions with the branches, 13 of them branches).  -1: not in C.
+template <bool DENSE>
+__device__ __forceinline__ int out_pos_map(const TileRowSmem &t, const unsigned *wrow, int r, int col) {
+    const unsigned off = (unsigned)((col >> 4) - t.jbase);
+    const bool in = off < (unsigned)t.span;
+    const int s = (int)t.map[map_swz(in ? off : 0u)];   // 0xffff marks a column with no C tile
+    const bool sok = in && (unsigned)s < (unsigned)t.S;
+    const int c = col & 15;
+    const int p = DENSE ? (r * t.S + s) * DPAD + c : acc_swz(rank_in_row(wrow[sok ? s : 0], c));
+    return sok && (unsigned)p < (unsigned)t.nacc ? p : -1;
+}
+
 // One C row: the warp walks A's row in order; for each A entry its lanes
-// take the B row's entries (distinct columns, so distinct outputs).
+// take the B row's entries (distinct columns, so distinct outputs).  B rows
+// of up to 32 entries (one per lane) take a path without a loop.
 template <bool DENSE, bool MAP>
 __device__ __forceinline__ void numeric_row(const NumericArgs &g, const TileRowSmem &t, int r0, int r, int lane)
 {
@@ -121,6 +137,20 @@ __device__ __forceinline__ void numeric_row(const NumericArgs &g, const TileRowS
             const double a = __shfl_sync(0xffffffffu, av, q);
             const int b0 = __shfl_sync(0xffffffffu, bs, q);
             const int b1 = __shfl_sync(0xffffffffu, be, q);
+            if (MAP && b1 - b0 <= 32) {   // uniform
+                if (b1 <= b0) continue;
+                // every lane loads and updates: idle lanes re-read the row's
+                // last entry and update the spare slot acc[nacc]
+                const bool live = b0 + lane < b1;
+                const int e = live ? b0 + lane : b1 - 1;
+                const int col = g.colB[e];
+                const double b = g.valB[e];
+                const int pos = out_pos_map<DENSE>(t, wrow, r, col);
+                bad |= live && pos < 0;
+                const int pi = (live && pos >= 0) ? pos : t.nacc;
+                acc[pi] = fma(a, b, acc[pi]);
+                continue;
+            }
             for (int e = b0 + lane; e < b1; e += 32) {
                 const int col = g.colB[e];
                 const double b = g.valB[e];

@@ -68,10 +68,11 @@ __host__ __device__ inline long long map_bytes(long long span) { return align16(
 //   int   scol[S]       C tile columns
 //   u32   word[S*16]    (offset of the tile's row segment inside the tile-row << 16) | row mask
 //   u16   map[span64]   tile column - scol[0] -> slot, swizzled (only when span <= MAP_MAX)
-//   f64   acc[...]      nnz_tr entries rounded to 16, swizzled (sparse) or S*16*17 (dense, rows padded to 17)
+//   f64   acc[...]      nnz_tr entries rounded to 16, swizzled (sparse) or S*16*17 (dense, rows padded to 17),
+//                       then 16 more: the first of them takes the updates of idle lanes
 __host__ __device__ inline long long numeric_smem_bytes(long long S, long long nnz_tr, long long span, bool dense) {
     long long b = align16(S * 4) + align16(S * TILE * 4) + (span <= MAP_MAX ? map_bytes(span) : 0);
-    return b + (dense ? S * TILE * 17 * 8 : ((nnz_tr + 15) & ~15ll) * 8);
+    return b + (dense ? S * TILE * 17 * 8 : ((nnz_tr + 15) & ~15ll) * 8) + TILE * 8;
 }
 
 // Shared-memory layout of one C row in the row kernel: word[S] (the row's
