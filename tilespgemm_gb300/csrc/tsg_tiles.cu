@@ -522,13 +522,21 @@ template <typename TP>
 __global__ void k_masks_to_tile_major(int blkm, const TP *__restrict__ rowptr, const uint16_t *__restrict__ src,
                                       uint16_t *dst)
 {
+    // lanes take tiles: each gathers its tile's 16 row masks (loads of one
+    // row of the tile-row are coalesced across the lanes) and writes them as
+    // two 16-byte stores (32 contiguous bytes per tile; dst is 32-byte aligned)
     const int row = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
     if (row >= blkm) return;
     const long long b = (long long)rowptr[row];
     const long long nt = (long long)rowptr[row + 1] - b;
-    for (long long t = lane; t < nt * TILE; t += 32) {
-        const long long r = t / nt, sl = t - r * nt;
-        dst[(b + sl) * TILE + r] = src[b * TILE + t];
+    for (long long t = lane; t < nt; t += 32) {
+        unsigned w[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+            w[k] = (unsigned)src[b * TILE + (2 * k) * nt + t] | ((unsigned)src[b * TILE + (2 * k + 1) * nt + t] << 16);
+        uint4 *d = reinterpret_cast<uint4 *>(dst + (b + t) * TILE);
+        d[0] = make_uint4(w[0], w[1], w[2], w[3]);
+        d[1] = make_uint4(w[4], w[5], w[6], w[7]);
     }
 }
 
