@@ -33,7 +33,7 @@ cudaError_t prepare_csr(Pool &pool, const void *rp, int rp_bits, const int *col,
 cudaError_t csr_to_tile_structure(Pool &pool, const long long *rp, const int *col, TileCSR &T, bool masks,
                                   int *flags, int *stat_max);
 cudaError_t tile_symbolic(Pool &pool, const TileCSR &A, const TileCSR &B, long long *crp, int *ccol, int *cnt,
-                          int *wide, int *flags, int *stat, bool count_pass, int *defer);
+                          int *wide, int *flags, int *stat, bool count_pass, int *defer, unsigned *wbm, long long wpr);
 cudaError_t csr_transpose(Pool &pool, const long long *rp, const int *col, const double *val, int m, int n,
                           long long nnz, long long *tp, int *tcol, double *tval, int *perm, int *flags);
 cudaError_t aux_gather(Pool &pool, const int *perm, const double *src, double *dst, long long n);
@@ -573,8 +573,20 @@ tsg_status plan_symbolic(tsg_ctx *ctx, Pool &pool, Scratch &sc, tsg_op op, const
     int *defer = sc.get<int>(P.blkm + 1);
     if (!P.crp || !cnt || !wide || !defer) return fail(TSG_ERR_OOM, "device pool allocation failed (step 1)");
     CUDA_OK(cudaMemsetAsync(defer + P.blkm, 0, sizeof(int), ctx->stream));
+    // the wide tile-rows' window bitmaps, kept from step 1's count pass for
+    // its fill pass, when they take at most 2 GB and an eighth of the free
+    // device memory (else the fill takes the union again)
+    unsigned *wbm = nullptr;
+    const long long wpr = (long long)ceil_div_i(TB.n, TILE) / 32 + 2;
+    {
+        size_t free_b = 0, total_b = 0;
+        const long long bytes = 4ll * wpr * P.blkm;
+        if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess && bytes <= (2ll << 30) && bytes <= (long long)(free_b / 8))
+            wbm = sc.get<unsigned>(wpr * P.blkm);
+        cudaGetLastError();
+    }
     CUDA_OK(tile_symbolic(pool, TA, TB, P.crp, nullptr, cnt, wide, ctx->dflags, (int *)(ctx->dstat + ST_MAXS), true,
-                          defer));
+                          defer, wbm, wpr));
     CUDA_OK(cudaMemcpyAsync(ctx->dstat + ST_NDEFER, defer + P.blkm, sizeof(int), cudaMemcpyDeviceToDevice, ctx->stream));
     CUDA_OK(aux_copy_scalars(pool, P.crp + P.blkm, ctx->dstat + ST_NUMBLKC, TA.trp + TA.blkm, ctx->dstat + ST_TILESA,
                              TB.trp + TB.blkm, ctx->dstat + ST_TILESB));
@@ -609,7 +621,7 @@ tsg_status plan_symbolic(tsg_ctx *ctx, Pool &pool, Scratch &sc, tsg_op op, const
     NumericBinParams bp{ctx->opts.dense_tile_min, ctx->opts.smem_acc_max, ctx->opts.row_acc_max, P.rpA,
                         ctx->opts.rows_global};
     CUDA_OK(symbolic_fill_fused(pool, TA, TB, P.m, P.crp, P.ccol, P.cmask, rowcnt, cnt, wide, ctx->dflags, P.rpB,
-                                P.colB, P.rpA, P.colA));
+                                P.colB, P.rpA, P.colA, wbm, wpr));
     tm.mark();  // 2
     CUDA_OK(step2_masks(pool, TA, TB, P.m, P.blkm, P.crp, P.ccol, P.cmask, rowcnt, maxS, maxSpan, ctx->dflags, defer,
                         ndefer, P.rpB, P.colB, P.rpA, P.colA, P.b_increasing, ctx->side, ctx->fork, ctx->join));

@@ -185,7 +185,8 @@ cudaError_t numeric_run(Pool &pool, const NumericArgs &a, const long long *binst
 
 cudaError_t symbolic_fill_fused(Pool &pool, const TileCSR &A, const TileCSR &B, int m, const long long *crp,
                                 int *ccol, uint16_t *cmask, int *rowcnt, int *cnt, int *wide, int *flags,
-                                const long long *erpB, const int *ecolB, const long long *erpA, const int *ecolA);
+                                const long long *erpB, const int *ecolB, const long long *erpA, const int *ecolA,
+                                unsigned *wbm, long long wpr);
 
 // Numeric bins of C's tile-rows (bin[blkm], per-bin work lists and
 // statistics in binstat, row classes of BIN_ROWS tile-rows in rowlist), from

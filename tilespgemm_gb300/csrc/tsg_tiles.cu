@@ -76,6 +76,9 @@ struct UnionKeys {
     struct Params {
         const int *arp; const int *acol; const int *brp; const int *bcol;
         const long long *bmoff = nullptr; const unsigned *bmw = nullptr;   // B's tile-row bitmaps, if built
+        // the wide tile-rows' window bitmaps, kept by the count pass for the
+        // fill pass (wpr words per entry of the wide list), if there is room
+        unsigned *wbm = nullptr; long long wpr = 0;
     };
     const int *arp, *acol, *brp, *bcol; const long long *bmoff; const unsigned *bmw; int i;
     __device__ UnionKeys(const Params &p, int row)
@@ -618,17 +621,29 @@ k_union_wide(typename KS::Params P, const int *wide_list, const int *wide_n, int
         for (long long c0 = kmin & ~31ll; c0 <= kmax; c0 += (long long)WIDE_WORDS * 32) {
             const long long span = min((long long)WIDE_WORDS * 32, (long long)kmax - c0 + 1);
             const int nwords = (int)((span + 31) >> 5);
-            for (int w = tid; w < nwords; w += WIDE_THREADS) bm[w] = 0;
-            __syncthreads();
-            if constexpr (KS::kHasOrRange) {
-                ks.or_range(bm, c0, span, warp, WIDE_THREADS / 32, lane);
+            // the window's bitmap in global memory (count pass: stored, fill
+            // pass: loaded instead of taking the union again)
+            unsigned *gbm = nullptr;
+            if constexpr (KS::kHasOrRange)
+                if (P.wbm) gbm = P.wbm + (long long)wi * P.wpr + ((c0 - (kmin & ~31ll)) >> 5);
+            if (FILL && gbm) {
+                for (int w = tid; w < nwords; w += WIDE_THREADS) bm[w] = gbm[w];
+                __syncthreads();
             } else {
-                ks.each(tid, WIDE_THREADS, [&](int key, int, int) {
-                    long long o = (long long)key - c0;
-                    if (o >= 0 && o < span) atomicOr(&bm[o >> 5], 1u << (o & 31));
-                });
+                for (int w = tid; w < nwords; w += WIDE_THREADS) bm[w] = 0;
+                __syncthreads();
+                if constexpr (KS::kHasOrRange) {
+                    ks.or_range(bm, c0, span, warp, WIDE_THREADS / 32, lane);
+                } else {
+                    ks.each(tid, WIDE_THREADS, [&](int key, int, int) {
+                        long long o = (long long)key - c0;
+                        if (o >= 0 && o < span) atomicOr(&bm[o >> 5], 1u << (o & 31));
+                    });
+                }
+                __syncthreads();
+                if (!FILL && gbm)
+                    for (int w = tid; w < nwords; w += WIDE_THREADS) gbm[w] = bm[w];
             }
-            __syncthreads();
             const int wpt = (nwords + WIDE_THREADS - 1) / WIDE_THREADS;
             const int w0 = min(nwords, tid * wpt), w1 = min(nwords, w0 + wpt);
             int lc = 0;
@@ -988,9 +1003,9 @@ cudaError_t tile_bitmaps(Pool &pool, TileCSR &T, long long *wcount, int *flags)
 }
 
 cudaError_t tile_symbolic(Pool &pool, const TileCSR &A, const TileCSR &B, long long *crp, int *ccol, int *cnt,
-                          int *wide, int *flags, int *stat, bool count_pass, int *defer)
+                          int *wide, int *flags, int *stat, bool count_pass, int *defer, unsigned *wbm, long long wpr)
 {
-    UnionKeys::Params P{A.trp, A.tcol, B.trp, B.tcol, B.bmoff, B.bmw};
+    UnionKeys::Params P{A.trp, A.tcol, B.trp, B.tcol, B.bmoff, B.bmw, wbm, wpr};
     return union_structure<UnionKeys, long long>(pool, P, A.blkm, cnt, wide, crp, ccol, nullptr, flags, stat,
                                                  scan_i32_to_i64, count_pass, !count_pass, defer, FUSED_MAX_TILES);
 }
@@ -1000,11 +1015,12 @@ cudaError_t tile_symbolic(Pool &pool, const TileCSR &A, const TileCSR &B, long l
 // come from step2_masks's CTA kernel).
 cudaError_t symbolic_fill_fused(Pool &pool, const TileCSR &A, const TileCSR &B, int m, const long long *crp,
                                 int *ccol, uint16_t *cmask, int *rowcnt, int *cnt, int *wide, int *flags,
-                                const long long *erpB, const int *ecolB, const long long *erpA, const int *ecolA)
+                                const long long *erpB, const int *ecolB, const long long *erpA, const int *ecolA,
+                                unsigned *wbm, long long wpr)
 {
     cudaStream_t s = pool.stream;
     if (A.blkm <= 0) return cudaSuccess;
-    UnionKeys::Params P{A.trp, A.tcol, B.trp, B.tcol, B.bmoff, B.bmw};
+    UnionKeys::Params P{A.trp, A.tcol, B.trp, B.tcol, B.bmoff, B.bmw, wbm, wpr};
     // the kernel reads the 16 row masks of a tile at once: tile-major copies
     // of A's and B's masks (one copy when B is A)
     uint16_t *amT = pool.alloc_n<uint16_t>(A.cap * TILE + 16);
