@@ -55,9 +55,12 @@ def test_bounded_wait_gives_up_and_context_survives(fresh):
 
 def _sweep(kind, call, after):
     """Arm the k-th allocation of `kind` to fail for k = 1, 2, ... until a call
-    makes fewer allocations than k.  Every armed failure must surface as
-    TSG_ERR_OOM, and after each one `after()` (an exact product on the same
-    context) must pass.  Returns the number of failures seen."""
+    makes fewer allocations than k.  An armed failure either surfaces as
+    TSG_ERR_OOM or hits an optional buffer the call can do without (step 1
+    keeps wide tile-rows' bitmaps only when there is room), in which case the
+    call must still succeed with the exact result (`call` checks it); after
+    each one `after()` (an exact product on the same context) must pass.
+    Returns the number of failures reported."""
     from tilespgemm_gb300 import TSGError, _abi
     L = _abi.lib()
     fails = 0
@@ -71,10 +74,9 @@ def _sweep(kind, call, after):
             fired = True
         pending = L.tsg_alloc_failure_pending(kind)
         L.tsg_inject_alloc_failure(kind, 0)
-        if not fired:
-            assert pending > 0, f"allocation {k} of kind {kind} failed but the call succeeded"
-            return fails
-        fails += 1
+        if not fired and pending > 0:
+            return fails          # the call made fewer than k allocations
+        fails += int(fired)
         after()
     raise AssertionError("the call made more than 400 allocations")
 
@@ -85,8 +87,19 @@ def test_every_pool_allocation_failure_is_reported(fresh, op, out):
     A = M.random_sparse(900, 900, 9, seed=31, empty_rows=0.1) if op == "AA" else M.rmat(10, 12, seed=9)
 
     def call():
+        from tilespgemm_gb300.api import CSR
         oc, _ = fresh.spgemm_raw(A, op=op, out=out)
-        oc.free()
+        try:
+            C = oc.download()
+        finally:
+            oc.free()
+        B = A
+        if op == "AAT":
+            tp, tr, tv = O.transpose(A)
+            B = CSR(A.n, A.m, tp, tr, tv)
+        rp, col, val = O.spgemm(A, B)
+        assert np.array_equal(np.asarray(C.rowptr, np.int64), rp) and np.array_equal(C.col, col)
+        assert np.array_equal(C.val, val)
 
     n = _sweep(0, call, lambda: _exact(fresh, A, op))
     assert n >= 10   # the call allocates at every stage: staging, tiles, step 1, step 2, numeric, output
