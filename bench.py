@@ -440,9 +440,11 @@ def run_batched(args) -> None:
     # numeric-only repeats: one batched plan per wave (symbolic once, tuned),
     # then graph replays of the numeric step on resident values
     ms_r, launches_r = 0.0, 0
+    tuned = []
     for grp in groups:
         plan = ctx.plan_batched(grp, op="AA")
         plan.tune()
+        tuned.append(plan.settings())
         plan.replay()
         l0 = lib.tsg_launch_count()
         ms_r += timed(plan.replay, args.steps)
@@ -459,6 +461,7 @@ def run_batched(args) -> None:
         "speedup_vs_one_at_a_time": ms_s / ms_b,
         "numeric_replay": {"instances_per_s": count / (ms_r / 1e3), "ms": ms_r, "graph_kernels": launches_r,
                            "note": "same instances, new values: batched plan per wave, tuned, one CUDA graph each"},
+        "tuned": tuned,
         "gflops_batched": 2.0 * cub / (ms_b * 1e6),
         "gpu_launches_per_step": launches_b,
         "clocks": clk.summary(),

@@ -286,9 +286,17 @@ tsg_status tsg_plan_destroy(tsg_ctx *ctx, tsg_plan *plan);
  * tsg_plan_result: waits for the stream and returns a device view of
  *   instance `instance` of the resident C (int64 row pointer; owner NULL:
  *   the memory stays the plan's until the next replay or its destruction).
- * tsg_plan_tune: times the numeric step's variants (threads per tile-row
- *   CTA, row walk) on the resident values and keeps the fastest for later
- *   replays; every variant gives the same bits.
+ * tsg_plan_tune: the autotuner (no counterpart in the reference, whose bin
+ *   thresholds are constants: main_spgemm-col.cu:26-29 and
+ *   spgemm_nsparse_kernel.h:4-14).  On the resident values it times the
+ *   numeric step's variants -- threads per tile-row CTA and row walk, then,
+ *   with the best of those, the bin thresholds that choose each tile-row's
+ *   accumulator (dense_tile_min, smem_acc_max, row_acc_max of tsg_opts; the
+ *   plan's tile-rows are binned again for each candidate) -- and keeps the
+ *   fastest for later replays; every variant gives the same bits.
+ * tsg_plan_settings: the numeric settings and bin thresholds the plan runs
+ *   with (the context's until tsg_plan_tune picks others); any pointer may
+ *   be NULL.
  */
 tsg_status tsg_plan_create_batched(tsg_ctx *ctx, tsg_op op, int32_t count, const tsg_csr *A, const tsg_csr *B,
                                    tsg_plan **plan, tsg_stats *stats);
@@ -298,6 +306,8 @@ tsg_status tsg_plan_set_values(tsg_ctx *ctx, tsg_plan *plan, const double *valA,
 tsg_status tsg_plan_replay(tsg_ctx *ctx, tsg_plan *plan);
 tsg_status tsg_plan_result(tsg_ctx *ctx, tsg_plan *plan, int32_t instance, tsg_csr *C);
 tsg_status tsg_plan_tune(tsg_ctx *ctx, tsg_plan *plan, double *best_ms);
+tsg_status tsg_plan_settings(const tsg_plan *plan, int32_t *threads, int32_t *walk, int32_t *dense_tile_min,
+                             int32_t *smem_acc_max, int32_t *row_acc_max);
 
 /* ---- serving: continuous batching of requests ------------------------------ */
 

@@ -123,7 +123,14 @@ def test_batched_plan_replay(ctx, op):
         vb = np.concatenate([_newvals(B, 200 * rnd + i) for i, B in enumerate(Bs)]) if Bs else None
         plan.set_values(va, vb)
         if rnd == 1:
+            before = plan.settings()
+            assert before["dense_tile_min"] == 160 and before["smem_acc_max"] == 24576
             assert plan.tune() > 0.0
+            st = plan.settings()   # the tuner's pick: any of its candidates, same bits
+            assert st["threads"] in (128, 256, 512) and st["walk"] in (1, 2, 3)
+            assert (st["dense_tile_min"], st["smem_acc_max"], st["row_acc_max"]) in {
+                (160, 24576, 65535), (96, 24576, 65535), (257, 24576, 65535), (160, 12288, 65535),
+                (160, 65535, 65535), (160, 24576, 16384)}
         plan.replay()
         plan.replay()   # idempotent on the same values
         for i, A in enumerate(As):

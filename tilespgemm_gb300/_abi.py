@@ -146,6 +146,7 @@ SIGNATURES = {
     "tsg_tiles_download": (C.c_int, [C.c_void_p, C.POINTER(tsg_tiles), C.c_void_p, C.c_void_p, C.c_void_p,
                                      C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "tsg_csr_download": (C.c_int, [C.c_void_p, C.POINTER(tsg_csr), C.c_void_p, C.c_void_p, C.c_void_p]),
+    "tsg_plan_settings": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "tsg_inject_alloc_failure": (C.c_int, [C.c_int32, C.c_int64]),
     "tsg_alloc_failure_pending": (C.c_int64, [C.c_int32]),
     "tsg_check_bounded_wait": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32]),

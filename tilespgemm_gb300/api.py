@@ -258,10 +258,17 @@ class Plan:
         check(lib().tsg_plan_replay(self._ctx.handle, self.handle))
 
     def tune(self) -> float:
-        """Pick the fastest numeric variant for this plan; returns its time in ms."""
+        """Pick the fastest numeric variant and bin thresholds for this plan;
+        returns its time in ms."""
         ms = C.c_double()
         check(lib().tsg_plan_tune(self._ctx.handle, self.handle, C.byref(ms)))
         return ms.value
+
+    def settings(self) -> dict:
+        """Numeric settings and bin thresholds the plan runs with."""
+        v = [C.c_int32() for _ in range(5)]
+        check(lib().tsg_plan_settings(self.handle, *[C.byref(x) for x in v]))
+        return dict(zip(("threads", "walk", "dense_tile_min", "smem_acc_max", "row_acc_max"), (x.value for x in v)))
 
     def result(self, instance: int = 0) -> CSR:
         """Host copy of instance `instance` of the resident C (after replay)."""

@@ -1123,6 +1123,9 @@ struct tsg_plan {
     cudaGraphExec_t gexec = nullptr;
     long long glaunches = 0;             // kernel launches in the graph
     int threads = 0, walk = -1;          // numeric settings picked by tsg_plan_tune (0 / -1: the context's)
+    // bin thresholds the plan's bins were chosen with (the context's, or
+    // tsg_plan_tune's pick)
+    int dense_tile_min = 0, smem_acc_max = 0, row_acc_max = 0;
 };
 
 extern "C" {
@@ -1945,6 +1948,27 @@ namespace {
 
 // the numeric step of a plan on its resident values into its resident C;
 // stream-ordered, no allocation and no host wait (so it can be captured)
+// Bin the plan's C tile-rows again with other thresholds (the structure is
+// kept; only the bins, their work lists and statistics change).  One host
+// wait: the numeric launches need the bins' sizes on the host.
+tsg_status plan_rebin(tsg_ctx *ctx, Pool &pool, tsg_plan *pl, int dense_tile_min, int smem_acc_max, int row_acc_max)
+{
+    PlanData &P = pl->P;
+    NumericBinParams bp{dense_tile_min, smem_acc_max, row_acc_max, P.rpA, ctx->opts.rows_global};
+    CUDA_OK(cudaMemsetAsync(ctx->dstat + ST_BINS, 0, sizeof(long long) * BS_SLOTS, ctx->stream));
+    CUDA_OK(bin_tilerows(pool, P.blkm, P.m, P.crp, P.ccol, P.rowptrC, bp, P.bin, ctx->dstat + ST_BINS, P.binlist,
+                         P.rowlist));
+    CUDA_OK(cudaMemcpyAsync(ctx->hstat + ST_BINS, ctx->dstat + ST_BINS, sizeof(long long) * BS_SLOTS,
+                            cudaMemcpyDeviceToHost, ctx->stream));
+    CUDA_OK(cudaStreamSynchronize(ctx->stream));
+    for (int b = 0; b < BS_SLOTS; ++b) P.bstat[b] = ctx->hstat[ST_BINS + b];
+    pl->dense_tile_min = dense_tile_min;
+    pl->smem_acc_max = smem_acc_max;
+    pl->row_acc_max = row_acc_max;
+    if (pl->gexec) { cudaGraphExecDestroy(pl->gexec); pl->gexec = nullptr; }
+    return TSG_OK;
+}
+
 tsg_status plan_enqueue_numeric(tsg_ctx *ctx, Pool &pool, tsg_plan *pl, int threads, int walk)
 {
     PlanData &P = pl->P;
@@ -2175,6 +2199,28 @@ tsg_status tsg_plan_tune(tsg_ctx *ctx, tsg_plan *plan, double *best_ms)
     Pool pool{ctx->pool, ctx->stream};
     tsg_status r = plan_resident(plan, pool);
     if (r) return r;
+    if (!plan->dense_tile_min) {   // bins as built: the context's thresholds
+        plan->dense_tile_min = ctx->opts.dense_tile_min;
+        plan->smem_acc_max = ctx->opts.smem_acc_max;
+        plan->row_acc_max = ctx->opts.row_acc_max;
+    }
+    // mean of three timed runs after one warm-up run
+    auto time_numeric = [&](int t, int w, float &ms_out) -> tsg_status {
+        float tot = 0.f;
+        for (int rep = 0; rep < 4; ++rep) {
+            CUDA_OK(cudaEventRecord(ctx->ev[6], ctx->stream));
+            tsg_status rr = plan_enqueue_numeric(ctx, pool, plan, t, w);
+            if (rr) return rr;
+            CUDA_OK(cudaEventRecord(ctx->ev[7], ctx->stream));
+            CUDA_OK(cudaEventSynchronize(ctx->ev[7]));
+            float ms = 0.f;
+            CUDA_OK(cudaEventElapsedTime(&ms, ctx->ev[6], ctx->ev[7]));
+            if (rep > 0) tot += ms;
+        }
+        ms_out = tot / 3;
+        return TSG_OK;
+    };
+    // 1. threads per tile-row CTA and row walk, on the plan's bins
     const int cand_threads[3] = {128, 256, 512};
     const int cand_walk[3] = {1, 2, 3};
     float best = 1e30f;
@@ -2182,28 +2228,50 @@ tsg_status tsg_plan_tune(tsg_ctx *ctx, tsg_plan *plan, double *best_ms)
     for (int t : cand_threads) {
         for (int w : cand_walk) {
             if (w != 2 && plan->P.dupsafe) continue;   // repeated B columns always take the packed walk
-            float tot = 0.f;
-            for (int rep = 0; rep < 4; ++rep) {
-                CUDA_OK(cudaEventRecord(ctx->ev[6], ctx->stream));
-                r = plan_enqueue_numeric(ctx, pool, plan, t, w);
-                if (r) return r;
-                CUDA_OK(cudaEventRecord(ctx->ev[7], ctx->stream));
-                CUDA_OK(cudaEventSynchronize(ctx->ev[7]));
-                float ms = 0.f;
-                CUDA_OK(cudaEventElapsedTime(&ms, ctx->ev[6], ctx->ev[7]));
-                if (rep > 0) tot += ms;   // the first run warms up
-            }
-            if (tot / 3 < best) { best = tot / 3; bt = t; bw = w; }
+            float ms = 0.f;
+            r = time_numeric(t, w, ms);
+            if (r) return r;
+            if (ms < best) { best = ms; bt = t; bw = w; }
         }
     }
+    // 2. the bin thresholds -- which tile-rows take the dense accumulator,
+    // which the shared-memory sparse one, which rows the row kernels -- with
+    // those settings: every candidate bins the plan again and is timed
+    struct Th { int dense, smem, row; };
+    const Th base{plan->dense_tile_min, plan->smem_acc_max, plan->row_acc_max};
+    const Th cand_th[5] = {{96, base.smem, base.row}, {257, base.smem, base.row}, {base.dense, 12288, base.row},
+                           {base.dense, 65535, base.row}, {base.dense, base.smem, 16384}};
+    Th bth = base;
+    for (const Th &c : cand_th) {
+        if (c.dense == base.dense && c.smem == base.smem && c.row == base.row) continue;
+        r = plan_rebin(ctx, pool, plan, c.dense, c.smem, c.row);
+        if (r) return r;
+        float ms = 0.f;
+        r = time_numeric(bt, bw, ms);
+        if (r) return r;
+        if (ms < best * 0.98f) { best = ms; bth = c; }
+    }
+    r = plan_rebin(ctx, pool, plan, bth.dense, bth.smem, bth.row);
+    if (r) return r;
     r = plan_check_flags(ctx);
     if (r) return r;
-    if (bt != plan->threads || bw != plan->walk) {
-        plan->threads = bt;
-        plan->walk = bw;
-        if (plan->gexec) { cudaGraphExecDestroy(plan->gexec); plan->gexec = nullptr; }
-    }
+    plan->threads = bt;
+    plan->walk = bw;
+    if (plan->gexec) { cudaGraphExecDestroy(plan->gexec); plan->gexec = nullptr; }
     if (best_ms) *best_ms = best;
+    return TSG_OK;
+}
+
+tsg_status tsg_plan_settings(const tsg_plan *plan, int32_t *threads, int32_t *walk, int32_t *dense_tile_min,
+                             int32_t *smem_acc_max, int32_t *row_acc_max)
+{
+    if (!plan) return fail(TSG_ERR_INVALID_ARG, "plan is NULL");
+    const tsg_opts &o = plan->ctx->opts;
+    if (threads) *threads = plan->threads > 0 ? plan->threads : o.threads_numeric;
+    if (walk) *walk = plan->walk >= 0 ? plan->walk : o.numeric_walk;
+    if (dense_tile_min) *dense_tile_min = plan->dense_tile_min ? plan->dense_tile_min : o.dense_tile_min;
+    if (smem_acc_max) *smem_acc_max = plan->smem_acc_max ? plan->smem_acc_max : o.smem_acc_max;
+    if (row_acc_max) *row_acc_max = plan->row_acc_max ? plan->row_acc_max : o.row_acc_max;
     return TSG_OK;
 }
 
