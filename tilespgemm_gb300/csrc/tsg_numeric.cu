@@ -787,7 +787,7 @@ constexpr size_t WIDE_SMEM = (size_t)ROW_WARPS * WIDE_WARP_BYTES;
 // windows with the accumulator in shared memory: tile columns and entries
 constexpr int WS_W = 256, WS_E = 256;
 // Wide rows with more A entries than LONG_NA (all of them, measured
-// fastest) are cut into parts of at most WIDE_W tile columns, each part one
+// fastest) are cut into parts of at most LONG_W tile columns, each part one
 // warp's work anywhere on the GPU (k_long_walk); their B rows' cut points
 // come from a table built once.
 constexpr int LONG_NA = 0;
@@ -795,6 +795,11 @@ constexpr int LONG_MINP = 32;        // parts of such a row at least (more warps
 constexpr int LONG_GRID = 152 * 5;   // CTAs of the part walk: five per SM
 constexpr int LONG_MIN_TILES = 1024; // C's tile columns from which wide rows take the parts path
 constexpr long long LONG_TAB_MAX = 1ll << 31;   // cut-table entries (8 GB) beyond which long rows stay per row
+constexpr int LONG_W = 512;     // tile columns per part at most
+constexpr int LONG_ACC = 128;   // a part's entries up to which its accumulators sit in the warp's shared memory
+constexpr int LONG_WARP_BYTES = LONG_W * 4 + LONG_ACC * 8;
+static_assert(LONG_W * TILE <= 65536, "a part's offsets fit 16 bits");
+constexpr size_t LONG_SMEM = (size_t)ROW_WARPS * LONG_WARP_BYTES;
 static_assert(4 * WS_W + 8 * WS_E <= WIDE_WARP_BYTES, "shared-memory windows fit the warp's share");
 
 // A wide row's share [t0, t1) of tile columns, for A rows of up to 32
@@ -1005,7 +1010,7 @@ k_numeric_wide(NumericArgs g, int cls, long long nrows, bool packed, const unsig
 // ---- wide rows of long A rows: parts and the cut table ---------------------
 //
 // A row's span of tile columns [T0, T1] (from C's first and last column) is
-// cut into P = max(ceil(span / WIDE_W), LONG_MINP) parts of Wp = ceil(span /
+// cut into P = max(ceil(span / LONG_W), LONG_MINP) parts of Wp = ceil(span /
 // P) tile columns.  The cut table holds, for each A entry p of the row and each part
 // boundary j = 0..P, the first entry of B's row k_p whose column is at or
 // past the boundary (at [j * na + p], so a part reads its 32 A entries
@@ -1034,7 +1039,7 @@ __device__ __forceinline__ LongRow long_row(const NumericArgs &g, int R)
     if (L.na > LONG_NA && L.nnz_r > 0) {
         L.T0 = (g.colC[L.Rb] + L.cshift) >> 4;
         const int span = ((g.colC[L.Rb + L.nnz_r - 1] + L.cshift) >> 4) - L.T0 + 1;
-        L.P = max((span + WIDE_W - 1) / WIDE_W, min(span, LONG_MINP));
+        L.P = max((span + LONG_W - 1) / LONG_W, min(span, LONG_MINP));
         L.Wp = (span + L.P - 1) / L.P;
         L.P = (span + L.Wp - 1) / L.Wp;   // no empty trailing part
     }
@@ -1136,10 +1141,11 @@ k_long_walk(NumericArgs g, long long nrows, const int *lrow, const unsigned char
 {
     extern __shared__ __align__(16) unsigned char s_raw[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    unsigned char *wbase = s_raw + (size_t)warp * WIDE_WARP_BYTES;
-    unsigned *s_off = reinterpret_cast<unsigned *>(wbase);
-    unsigned short *s_msk = reinterpret_cast<unsigned short *>(wbase + (size_t)WIDE_W * 4);
-    for (int t = lane; t < WIDE_W; t += 32) s_msk[t] = 0;
+    unsigned char *wbase = s_raw + (size_t)warp * LONG_WARP_BYTES;
+    unsigned short *s_off = reinterpret_cast<unsigned short *>(wbase);   // < LONG_W * TILE
+    unsigned short *s_msk = reinterpret_cast<unsigned short *>(wbase + (size_t)LONG_W * 2);
+    double *s_acc = reinterpret_cast<double *>(wbase + (size_t)LONG_W * 4);
+    for (int t = lane; t < LONG_W; t += 32) s_msk[t] = 0;
     __syncwarp();
     const long long nparts = part_off[nrows];
     bool bad = false;
@@ -1162,8 +1168,10 @@ k_long_walk(NumericArgs g, long long nrows, const int *lrow, const unsigned char
         const int sa = warp_lower_bound(tcol, 0, S, wlo, lane);
         const int sb = warp_lower_bound(tcol, sa, S, whi, lane);
         if (sa >= sb) continue;
-        unsigned run = (unsigned)warp_lower_bound(g.colC + L.Rb, 0, L.nnz_r, wlo * TILE - L.cshift, lane);
-        bool any = false;
+        // the part's entries of C: [Rb + first, Rb + first + E); s_off
+        // holds each tile's offset among them
+        const unsigned first = (unsigned)warp_lower_bound(g.colC + L.Rb, 0, L.nnz_r, wlo * TILE - L.cshift, lane);
+        unsigned run = 0;
         for (int s = sa; s < sb; s += 32) {
             const int ss = s + lane;
             const unsigned mk = ss < sb ? (unsigned)mrow[ss] : 0u;
@@ -1171,21 +1179,26 @@ k_long_walk(NumericArgs g, long long nrows, const int *lrow, const unsigned char
             const int incl = warp_incl_scan(c, lane);
             if (mk) {
                 const int t = tcol[ss] - wlo;
-                s_off[t] = run + incl - c;
+                s_off[t] = (unsigned short)(run + incl - c);
                 s_msk[t] = (unsigned short)mk;
-                const long long dst = L.Rb + run + incl - c;
-                for (int q = 0; q < c; ++q) g.valC[dst + q] = 0.0;   // zeroed just before the walk
-                any = true;
             }
             run += __shfl_sync(0xffffffffu, incl, 31);
         }
+        const int E = (int)run;
+        double *gacc = g.valC + L.Rb + first;
+        // accumulators zeroed just before the walk: in the warp's shared
+        // memory when the part's entries fit there (written out after it),
+        // else in C's values
+        const bool sm = E <= LONG_ACC;
+        for (int q = lane; q < E; q += 32) {
+            if (sm) s_acc[q] = 0.0; else gacc[q] = 0.0;
+        }
         __syncwarp();
-        if (__any_sync(0xffffffffu, any)) {
-            const long long Rb = L.Rb;
-            auto pos_of = [&](int col) -> long long {
+        if (E > 0) {
+            auto pos_of = [&](int col) -> int {
                 const int t = (col >> 4) - wlo, cc = col & 15;
                 const unsigned mk = s_msk[t];
-                return ((mk >> (TILE - 1 - cc)) & 1u) ? Rb + s_off[t] + __popc(mk >> (TILE - cc)) : -1ll;
+                return ((mk >> (TILE - 1 - cc)) & 1u) ? (int)s_off[t] + __popc(mk >> (TILE - cc)) : -1;
             };
             const int *tb = tab + tab_off[l];
             for (int pb = 0; pb < L.na; pb += 32) {
@@ -1197,7 +1210,12 @@ k_long_walk(NumericArgs g, long long nrows, const int *lrow, const unsigned char
                     bs = tb[(long long)j * L.na + pb + lane];
                     be = tb[(long long)(j + 1) * L.na + pb + lane];
                 }
-                walk_segments(g, lane, nb, av, bs, be, wlo * TILE, whi * TILE, g.valC, pos_of, bad);
+                if (sm) walk_segments(g, lane, nb, av, bs, be, wlo * TILE, whi * TILE, s_acc, pos_of, bad);
+                else walk_segments(g, lane, nb, av, bs, be, wlo * TILE, whi * TILE, gacc, pos_of, bad);
+            }
+            if (sm) {
+                __syncwarp();
+                for (int q = lane; q < E; q += 32) gacc[q] = s_acc[q];
             }
         }
         for (int ss = sa + lane; ss < sb; ss += 32) s_msk[tcol[ss] - wlo] = 0;
@@ -1430,7 +1448,7 @@ cudaError_t numeric_run(Pool &pool, const NumericArgs &a, const long long *binst
         // eight warps per row from C widths of 1,024 tile columns on); the
         // cut table gets at most LONG_TAB_MAX entries (rows past it stay
         // with k_numeric_wide)
-        const long long pmax = std::max<long long>(((long long)(a.n + TILE - 1) / TILE + WIDE_W - 1) / WIDE_W, LONG_MINP);
+        const long long pmax = std::max<long long>(((long long)(a.n + TILE - 1) / TILE + LONG_W - 1) / LONG_W, LONG_MINP);
         // ... and at most a quarter of the device's free memory
         size_t free_b = 0, total_b = 0;
         long long tab_cap = LONG_TAB_MAX;
@@ -1446,7 +1464,7 @@ cudaError_t numeric_run(Pool &pool, const NumericArgs &a, const long long *binst
         if (c == ROW_WIDE) { k_numeric_wide<ROW_WARPS><<<(unsigned)n, ROW_WARPS * 32, WIDE_SMEM, s>>>(a, c, n, packed, L.handled); ::tsg::count_launch(); }
         else { k_numeric_wide<1><<<(unsigned)((n + ROW_WARPS - 1) / ROW_WARPS), ROW_WARPS * 32, WIDE_SMEM, s>>>(a, c, n, packed, nullptr); ::tsg::count_launch(); }
         if (parts) {
-            { k_long_walk<<<LONG_GRID, ROW_WARPS * 32, WIDE_SMEM, s>>>(a, n, L.lrow, L.lfit, L.part_off, L.tab_off, L.tab, L.next_part); ::tsg::count_launch(); }
+            { k_long_walk<<<LONG_GRID, ROW_WARPS * 32, LONG_SMEM, s>>>(a, n, L.lrow, L.lfit, L.part_off, L.tab_off, L.tab, L.next_part); ::tsg::count_launch(); }
             long_release(pool, L);
         }
         e = cudaGetLastError();
