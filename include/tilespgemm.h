@@ -101,6 +101,10 @@ typedef struct {
                                 (default 4, measured fastest) */
     int32_t count_products;  /* 1: calls given a tsg_stats count the intermediate products (nnz_cub, one extra
                                 pass over A); 0: nnz_cub is reported as 0 (default 1) */
+    int32_t small_path;      /* 1: tsg_spgemm runs A*B and A*A whose every row of A meets at most 128 entries of B
+                                (A and B of at most 4 M entries) row by row, one warp per row of C, instead of
+                                the tiled pipeline -- the same C, values included; a repeated shape waits on the
+                                device once per call; 0: always the tiled pipeline (default 1) */
 } tsg_opts;
 
 /* Per-call statistics.  Sizes are always filled; times only with phase_times. */
@@ -116,6 +120,7 @@ typedef struct {
     double ms_h2d, ms_d2h;     /* host <-> device copies (host operands only) */
     int32_t n_syncs;           /* host waits on the device inside the call */
     int32_t bins[4];           /* C tile-rows per numeric bin: empty, shared sparse, shared dense, per-row or global */
+    int32_t small_path;        /* 1: the small-product path ran (tiles_*, bins and phase times are 0) */
 } tsg_stats;
 
 typedef struct tsg_ctx tsg_ctx;

@@ -56,7 +56,10 @@ def built_lib():
 
 @pytest.fixture(scope="session")
 def ctx(built_lib):
+    """A context on the tiled pipeline (the small-product path off, so that
+    small test matrices exercise the tiled kernels; tests/test_small_gpu.py
+    covers that path)."""
     from tilespgemm_gb300 import Context
-    c = Context(0)
+    c = Context(0, small_path=0)
     yield c
     c.close()

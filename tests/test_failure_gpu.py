@@ -22,7 +22,7 @@ pytestmark = pytest.mark.gpu
 @pytest.fixture()
 def fresh():
     from tilespgemm_gb300 import Context, _abi
-    c = Context(0)
+    c = Context(0, small_path=0)
     yield c
     _abi.lib().tsg_inject_alloc_failure(0, 0)
     _abi.lib().tsg_inject_alloc_failure(1, 0)

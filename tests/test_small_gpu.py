@@ -1,0 +1,223 @@
+"""The small-product path of tsg_spgemm (tsg_opts.small_path, default on):
+A*B and A*A whose every row of A meets at most 128 entries of B run row by
+row, one warp per row of C.  Its C must equal the oracle's and the tiled
+pipeline's bit for bit (row pointer, columns, values: both accumulate each
+entry as fma over A's row order, then B's); a repeated shape waits on the
+device once per call; rows over the limit and A*A^T take the tiled path."""
+import numpy as np
+import pytest
+
+from conftest import golden_names, load_case
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def sctx(built_lib):
+    from tilespgemm_gb300 import Context
+    c = Context(0, small_path=1)
+    yield c
+    c.close()
+
+
+def _same(C, D):
+    assert C.m == D.m and C.n == D.n
+    assert np.array_equal(np.asarray(C.rowptr, np.int64), np.asarray(D.rowptr, np.int64))
+    assert np.array_equal(C.col, D.col)
+    assert np.array_equal(C.val, D.val)
+
+
+def _oracle(C, A, B):
+    rp, col, val = O.spgemm(A, B)
+    assert np.array_equal(np.asarray(C.rowptr, np.int64), rp)
+    assert np.array_equal(C.col, col)
+    assert np.array_equal(C.val, val)
+
+
+def _banded_and_spread(m, k, seed):
+    """Two m x m matrices with k entries in every row (the same shape): a
+    band (C rows of about 2k entries) and random columns (about k^2)."""
+    from tilespgemm_gb300.api import CSR
+    rng = np.random.default_rng(seed)
+    rp = np.arange(0, m * k + 1, k, dtype=np.int64)
+    band = (np.arange(m)[:, None] + np.arange(k)[None, :]) % m
+    band.sort(axis=1)
+    spread = np.stack([np.sort(rng.choice(m, size=k, replace=False)) for _ in range(m)])
+    vals = rng.uniform(-1.0, 1.0, size=m * k)
+    return (CSR(m, m, rp, band.reshape(-1).astype(np.int32), vals),
+            CSR(m, m, rp.copy(), spread.reshape(-1).astype(np.int32), vals.copy()))
+
+
+def _cases():
+    from tilespgemm_gb300 import matrices as M
+    return {
+        "lap64": (M.laplacian_2d(64), None, "AA"),
+        "lap256": (M.laplacian_2d(256), None, "AA"),
+        "rand5000": (M.random_sparse(5000, 5000, 10, seed=12), None, "AA"),
+        "dups_unsorted": (M.random_sparse(1000, 1000, 8, seed=15, dup=True, unsorted=True), None, "AA"),
+        "empty_rows": (M.random_sparse(3000, 3000, 6, seed=16, empty_rows=0.5), None, "AA"),
+        "rect_ab": (M.random_sparse(300, 500, 9, seed=21), M.random_sparse(500, 170, 7, seed=22), "AB"),
+        "far_columns": (M.random_sparse(200, 100000, 8, seed=5), M.random_sparse(100000, 90000, 8, seed=6), "AB"),
+        "full_rows": (M.random_sparse(64, 64, 11, seed=7), None, "AA"),
+    }
+
+
+@pytest.mark.parametrize("key", list(_cases().keys()))
+def test_small_path_matches_oracle_and_tiled(sctx, ctx, key):
+    A, B, op = _cases()[key]
+    C, st = sctx.spgemm(A, B, op=op, stats=True)
+    assert st["small_path"] == 1
+    _oracle(C, A, B if B is not None else A)
+    T, st2 = ctx.spgemm(A, B, op=op, stats=True)
+    assert st2["small_path"] == 0
+    _same(C, T)
+    assert st["nnz_c"] == C.nnz and st["nnz_cub"] == O.nnzcub(A, B if B is not None else A)
+
+
+@pytest.mark.parametrize("name", [n for n in golden_names() if load_case(n)["op"] != "AAT"])
+def test_small_path_golden(sctx, name):
+    d = load_case(name)
+    C, st = sctx.spgemm(d["A"], op=d["op"], stats=True)
+    assert np.array_equal(np.asarray(C.rowptr, np.int64), d["c_rowptr"])
+    assert np.array_equal(C.col, d["c_col"])
+    _oracle(C, d["A"], d["B"])
+
+
+def test_repeated_shape_waits_once(built_lib):
+    """The second call of a shape sizes C from the first and waits once; a
+    larger C of the same shape is found at that wait and filled again."""
+    from tilespgemm_gb300 import Context
+    band, spread = _banded_and_spread(3000, 8, seed=3)
+    with Context(0) as c:
+        Ad = band.to_device(0)
+        for i in range(3):
+            oc, st = c.spgemm_raw(Ad, op="AA", out="device", stats=True)
+            C = oc.download()
+            oc.free()
+            _oracle(C, band, band)
+            assert st["small_path"] == 1
+            assert st["n_syncs"] == (2 if i == 0 else 1)
+        Sd = spread.to_device(0)                 # same shape, C about 4x larger
+        oc, st = c.spgemm_raw(Sd, op="AA", out="device", stats=True)
+        C = oc.download()
+        oc.free()
+        _oracle(C, spread, spread)
+        assert st["small_path"] == 1 and st["n_syncs"] == 2
+        oc, st = c.spgemm_raw(Ad, op="AA", out="device", stats=True)   # back to the band
+        C = oc.download()
+        oc.free()
+        _oracle(C, band, band)
+        assert st["n_syncs"] == 1
+
+
+def test_rows_over_the_limit_take_the_tiled_path(sctx):
+    from tilespgemm_gb300 import matrices as M
+    A = M.random_sparse(500, 500, 12, seed=40)      # 144 products per row
+    for _ in range(2):
+        C, st = sctx.spgemm(A, op="AA", stats=True)
+        assert st["small_path"] == 0
+        _oracle(C, A, A)
+    R = M.rmat(9, 8, seed=2)
+    C, st = sctx.spgemm(R, op="AAT", stats=True)
+    assert st["small_path"] == 0
+
+
+@pytest.mark.parametrize("op", ["AA", "AB"])
+def test_pinned_host_operands_and_output(sctx, op):
+    import torch
+    from tilespgemm_gb300 import matrices as M
+    from tilespgemm_gb300.api import CSR
+
+    def pinned(X):
+        return CSR(X.m, X.n, torch.from_numpy(np.asarray(X.rowptr, np.int64)).pin_memory(),
+                   torch.from_numpy(np.asarray(X.col, np.int32)).pin_memory(),
+                   torch.from_numpy(np.asarray(X.val, np.float64)).pin_memory())
+
+    A = M.random_sparse(4000, 3000, 7, seed=50, empty_rows=0.1)
+    B = M.random_sparse(3000, 2500, 9, seed=51) if op == "AB" else None
+    if op == "AA":
+        A = M.random_sparse(4000, 4000, 7, seed=50, empty_rows=0.1)
+    for _ in range(2):
+        oc, st = sctx.spgemm_raw(pinned(A), pinned(B) if B is not None else None, op=op, out="host", stats=True)
+        assert oc.where == "host" and st["small_path"] == 1
+        C = oc.download()
+        oc.free()
+        _oracle(C, A, B if B is not None else A)
+
+
+def test_int64_row_pointers_and_tiny(built_lib):
+    from tilespgemm_gb300 import Context
+    from tilespgemm_gb300 import matrices as M
+    from tilespgemm_gb300.api import CSR
+    A = M.laplacian_2d(40)
+    with Context(0, out_rowptr_bits=64) as c:
+        oc, st = c.spgemm_raw(A.to_device(0), op="AA", out="device", stats=True)
+        assert oc.rowptr_bits == 64 and st["small_path"] == 1
+        C = oc.download()
+        oc.free()
+        _oracle(C, A, A)
+        Z = CSR(40, 40, np.zeros(41, np.int64), np.zeros(0, np.int32), np.zeros(0))
+        C = c.spgemm(Z, op="AA")
+        assert C.nnz == 0 and np.all(np.asarray(C.rowptr) == 0)
+        one = CSR(1, 1, np.array([0, 1]), np.array([0], np.int32), np.array([3.0]))
+        C = c.spgemm(one, op="AA")
+        assert C.nnz == 1 and C.val[0] == 9.0
+        E = CSR(0, 0, np.zeros(1, np.int64), np.zeros(0, np.int32), np.zeros(0))
+        C = c.spgemm(E, op="AA")
+        assert C.m == 0 and C.nnz == 0
+
+
+def test_invalid_inputs_are_reported(sctx):
+    """The same statuses as the tiled path, on a first call of a shape and on
+    a repeated one; the context stays usable."""
+    from tilespgemm_gb300 import TSGError
+    from tilespgemm_gb300.api import CSR
+    good = CSR(3, 3, np.array([0, 1, 2, 3]), np.array([0, 2, 1], np.int32), np.ones(3))
+    bad_col = CSR(3, 3, np.array([0, 1, 2, 3]), np.array([0, 5, 1], np.int32), np.ones(3))
+    bad_rp = CSR(3, 3, np.array([0, 2, 1, 3]), np.array([0, 1, 2], np.int32), np.ones(3))
+    for first in (True, False):
+        if not first:
+            sctx.spgemm(good, op="AA")      # the shape is known now
+        for bad in (bad_col, bad_rp):
+            with pytest.raises(TSGError) as e:
+                sctx.spgemm(bad, op="AA")
+            assert e.value.status == 8
+    rect = CSR(2, 3, np.array([0, 1, 2]), np.array([0, 2], np.int32), np.ones(2))
+    with pytest.raises(TSGError) as e:
+        sctx.spgemm(rect, op="AA")
+    assert e.value.status == 7
+    ok = CSR(2, 2, np.array([0, 1, 2]), np.array([1, 0], np.int32), np.array([2.0, 3.0]))
+    C = sctx.spgemm(ok, op="AA")
+    assert np.array_equal(C.val, [6.0, 6.0])
+
+
+def test_allocation_failures_are_reported(built_lib):
+    """Every device-pool allocation of a small-path call, on a first call of
+    the shape and on a repeated one, fails in turn: TSG_ERR_OOM, and the next
+    call is exact."""
+    from tilespgemm_gb300 import Context, _abi
+    from tilespgemm_gb300 import matrices as M
+    from test_failure_gpu import _sweep
+    A = M.random_sparse(900, 900, 9, seed=31, empty_rows=0.1)
+
+    def first_call():                      # a new context: the shape is not known yet
+        with Context(0, small_path=1) as c2:
+            C, st = c2.spgemm(A, op="AA", stats=True)
+            assert st["small_path"] == 1
+            _oracle(C, A, A)
+
+    c = Context(0, small_path=1)
+    try:
+        def call():
+            C, st = c.spgemm(A, op="AA", stats=True)
+            assert st["small_path"] == 1
+            _oracle(C, A, A)
+
+        assert _sweep(0, first_call, first_call) >= 5
+        assert _sweep(0, call, call) >= 5  # the shape is known after the first successful call
+        assert _sweep(1, lambda: c.spgemm(A, op="AA"), call) >= 3   # pinned host buffers of C
+    finally:
+        _abi.lib().tsg_inject_alloc_failure(0, 0)
+        _abi.lib().tsg_inject_alloc_failure(1, 0)
+        c.close()

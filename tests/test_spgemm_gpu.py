@@ -155,7 +155,7 @@ def test_numeric_bins_agree(opts, built_lib):
     A = M.stencil_27(12, seed=4)
     B2 = M.random_sparse(2000, 2000, 15, seed=23, dup=True)
     B3 = M.random_sparse(3000, 3000, 12, seed=25, band=24)   # few C tiles per tile-row
-    with Context(0, **opts) as c:
+    with Context(0, small_path=0, **opts) as c:
         for X in (A, B2, B3):
             C, st = c.spgemm(X, op="AA", stats=True)
             check_against_oracle(C, X, X)
@@ -174,7 +174,7 @@ def test_long_rows(opts, built_lib):
     accumulator), bit-exact against the oracle."""
     from tilespgemm_gb300 import Context
     from tilespgemm_gb300 import matrices as M
-    with Context(0, **opts) as c:
+    with Context(0, small_path=0, **opts) as c:
         for X in (M.random_sparse(6000, 6000, 80, seed=31), M.random_sparse(12000, 12000, 120, seed=32)):
             C, st = c.spgemm(X, op="AA", stats=True)
             assert st["bins"][3] > 0
@@ -192,7 +192,7 @@ def test_hub_rows_in_parts(opts, built_lib):
     A = M.random_sparse(48, 2000, 700, seed=41)
     B = M.random_sparse(2000, 300000, 20, seed=42)
     assert int(np.diff(np.asarray(A.rowptr)).min()) > 512
-    with Context(0, **opts) as c:
+    with Context(0, small_path=0, **opts) as c:
         C, st = c.spgemm(A, B, op="AB", stats=True)
         assert st["bins"][3] > 0
         check_against_oracle(C, A, B)
@@ -221,7 +221,7 @@ def test_wide_tile_rows(ctx, opts, built_lib):
     A = _runs_matrix(32, 120, lambda k: [(0, 120)], seed=41)                       # dense rows
     B1 = _runs_matrix(120, 120000, lambda k: [(k * 1000, 300)], seed=42)            # dense tiles
     B2 = _runs_matrix(120, 120000, lambda k: [(k * 997 + 16 * t, 1) for t in range(300)], seed=43)  # 1 per tile
-    with Context(0, **opts) as c:
+    with Context(0, small_path=0, **opts) as c:
         for B in (B1, B2):
             C, st = c.spgemm(A, B, op="AB", stats=True)
             assert st["bins"][3] > 0
@@ -384,6 +384,6 @@ def test_long_rows_unsorted_and_repeated(kind, built_lib):
     from tilespgemm_gb300 import Context
     from tilespgemm_gb300 import matrices as M
     X = M.random_sparse(5000, 5000, 60, seed=33, unsorted=(kind == "unsorted"), dup=(kind == "dup"))
-    with Context(0, row_acc_max=0) as c:
+    with Context(0, small_path=0, row_acc_max=0) as c:
         C = c.spgemm(X, op="AA")
         check_against_oracle(C, X, X)

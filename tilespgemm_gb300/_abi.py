@@ -54,6 +54,7 @@ class tsg_opts(C.Structure):
         ("dense_tile_min", C.c_int32), ("smem_acc_max", C.c_int32), ("threads_numeric", C.c_int32),
         ("row_acc_max", C.c_int32), ("numeric_walk", C.c_int32),
         ("rows_global", C.c_int32), ("row_warps", C.c_int32), ("count_products", C.c_int32),
+        ("small_path", C.c_int32),
     ]
 
 
@@ -63,7 +64,7 @@ class tsg_stats(C.Structure):
         ("tiles_a", C.c_int64), ("tiles_b", C.c_int64), ("tiles_c", C.c_int64),
         ("ms_total", C.c_double), ("ms_convert", C.c_double), ("ms_step1", C.c_double),
         ("ms_step2", C.c_double), ("ms_step3", C.c_double), ("ms_h2d", C.c_double), ("ms_d2h", C.c_double),
-        ("n_syncs", C.c_int32), ("bins", C.c_int32 * 4),
+        ("n_syncs", C.c_int32), ("bins", C.c_int32 * 4), ("small_path", C.c_int32),
     ]
 
     def as_dict(self) -> dict:

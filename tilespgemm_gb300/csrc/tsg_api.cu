@@ -116,6 +116,16 @@ static inline tsg_status cuda_status(cudaError_t e) { return e == cudaErrorMemor
         }                                                                                              \
     } while (0)
 
+// A product shape the small-product path has seen on a context: the next
+// call of that shape sizes C's buffers from nnzc and waits on the device
+// only at the end; small = false: its rows exceed the path's limit (the
+// tiled path takes it without trying).
+struct SmallShape {
+    int op = 0, m = 0, k = 0, n = 0;
+    long long nnz_a = 0, nnz_b = 0, nnzc = 0;
+    bool small = true;
+};
+
 struct tsg_ctx {
     int device = 0;
     tsg_opts opts{};
@@ -134,6 +144,7 @@ struct tsg_ctx {
     // numeric step
     cudaStream_t copy = nullptr;
     cudaEvent_t cfork = nullptr, vals_ev = nullptr, cols_ev = nullptr, copy_done = nullptr;
+    std::vector<SmallShape> small_shapes;   // the last SMALL_SHAPES shapes, newest last
 };
 
 namespace {
@@ -143,6 +154,7 @@ enum StatSlot {
     ST_NDEFER = 7,               // tile-rows left to the CTA step-2 kernel
     ST_BINS = 8,                 // step 2's bin statistics, BS_SLOTS slots (tsg_numeric.cuh)
     ST_BUNSORTED = 36,           // B rows whose columns are not strictly increasing
+    ST_SMALL = 37,               // small-product path: rows over its limit, products (2 slots)
     ST_HFLAGS = 40,              // host mirror only: device flags
     ST_SLOTS = 64
 };
@@ -365,7 +377,8 @@ tsg_status host_wait(tsg_ctx *ctx, int *nsync)
 {
     CUDA_OK(cudaMemcpyAsync(ctx->hstat, ctx->dstat, sizeof(long long) * ST_HFLAGS, cudaMemcpyDeviceToHost, ctx->stream));
     static_assert(FLAG_COUNT <= ST_SLOTS - ST_HFLAGS, "flag mirror");
-    static_assert(ST_BINS + BS_SLOTS <= ST_BUNSORTED && ST_BUNSORTED < ST_HFLAGS, "statistics slots");
+    static_assert(ST_BINS + BS_SLOTS <= ST_BUNSORTED && ST_BUNSORTED < ST_SMALL && ST_SMALL + 2 <= ST_HFLAGS,
+                  "statistics slots");
     int hflags[FLAG_COUNT];
     CUDA_OK(cudaMemcpyAsync(ctx->hstat + ST_HFLAGS + 16, ctx->dflags, sizeof(int) * FLAG_COUNT, cudaMemcpyDeviceToHost, ctx->stream));
     CUDA_OK(cudaStreamSynchronize(ctx->stream));
@@ -859,6 +872,157 @@ void phase_times(tsg_ctx *ctx, tsg_stats *st, const PhaseTimer &tm)
     st->ms_convert = a; st->ms_step1 = b; st->ms_step2 = c1; st->ms_step3 = d;
 }
 
+
+// ---- the small-product path ---------------------------------------------------
+
+constexpr long long SMALL_NNZ_MAX = 1ll << 22;   // entries of A and of B at most
+constexpr size_t SMALL_SHAPES = 32;
+
+SmallShape *small_shape_find(tsg_ctx *ctx, const SmallShape &k)
+{
+    for (auto &s : ctx->small_shapes)
+        if (s.op == k.op && s.m == k.m && s.k == k.k && s.n == k.n && s.nnz_a == k.nnz_a && s.nnz_b == k.nnz_b)
+            return &s;
+    return nullptr;
+}
+
+void small_shape_record(tsg_ctx *ctx, const SmallShape &k)
+{
+    if (SmallShape *s = small_shape_find(ctx, k)) { *s = k; return; }
+    if (ctx->small_shapes.size() >= SMALL_SHAPES) ctx->small_shapes.erase(ctx->small_shapes.begin());
+    ctx->small_shapes.push_back(k);
+}
+
+// tsg_spgemm for products whose every row of A meets at most
+// SMALL_MAX_PRODUCTS entries of B (A*B and A*A, operands of at most
+// SMALL_NNZ_MAX entries): one warp per row of C (tsg_small.cu), row counts,
+// scan, fill.  The first call of a shape reads C's size back before the fill
+// (two host waits); later calls of the shape size C's buffers from it and
+// wait once, at the end (a larger C is found there and the fill run again).
+// taken = false: nothing was returned to the caller -- the product is not
+// small, or turned out not to be -- and the tiled path runs instead.
+tsg_status small_spgemm(tsg_ctx *ctx, tsg_op op, const tsg_csr *A, const tsg_csr *B, tsg_csr *C, tsg_stats *st,
+                        bool &taken)
+{
+    taken = false;
+    if (!ctx->opts.small_path || op == TSG_OP_AAT) return TSG_OK;
+    if (check_op(op, A, B) != TSG_OK) { g_err.clear(); return TSG_OK; }   // the tiled path reports it
+    const tsg_csr *Bm = op == TSG_OP_AB ? B : A;
+    if (A->nnz > SMALL_NNZ_MAX || Bm->nnz > SMALL_NNZ_MAX) return TSG_OK;
+    SmallShape key;
+    key.op = (int)op; key.m = A->m; key.k = A->n; key.n = Bm->n; key.nnz_a = A->nnz; key.nnz_b = Bm->nnz;
+    const SmallShape *seen = small_shape_find(ctx, key);
+    if (seen && !seen->small) return TSG_OK;
+    const long long hint = seen ? seen->nnzc : -1;
+    taken = true;
+    auto t0 = std::chrono::steady_clock::now();
+    Pool pool{ctx->pool, ctx->stream};
+    PlanData P;
+    int *col = nullptr;
+    double *val = nullptr;
+    void *rp_dev = nullptr;
+    // undo everything before a return (the stream drained first)
+    auto release = [&]() {
+        P.wait_values(ctx->stream);
+        pool.free(col); pool.free(val); pool.free(rp_dev);
+        col = nullptr; val = nullptr; rp_dev = nullptr;
+        P.release(pool);
+        cudaStreamSynchronize(ctx->stream);
+    };
+    auto give_up = [&](tsg_status r) { release(); cudaGetLastError(); return r; };
+    const bool validate = ctx->opts.validate != 0;
+    unsigned long long *sstat = reinterpret_cast<unsigned long long *>(ctx->dstat + ST_SMALL);
+    cudaError_t e = cudaMemsetAsync(ctx->dflags, 0, sizeof(int) * FLAG_COUNT, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(ctx->dstat, 0, sizeof(long long) * ST_SLOTS, ctx->stream);
+    if (e != cudaSuccess) return give_up(fail(cuda_status(e), "small path: %s", cudaGetErrorString(e)));
+    P.op = op; P.m = A->m; P.k = A->n; P.nnzA = A->nnz;
+    tsg_status r = stage_into_plan(ctx, pool, P, A, validate, false, P.rpA, P.colA, P.valA, P.valA_buf);
+    if (r) return give_up(r);
+    if (op == TSG_OP_AB) {
+        P.n = B->n; P.nnzB = B->nnz;
+        r = stage_into_plan(ctx, pool, P, B, validate, false, P.rpB, P.colB, P.valB, P.valB_buf);
+        if (r) return give_up(r);
+    } else {
+        P.n = A->n; P.nnzB = A->nnz;
+        P.rpB = P.rpA; P.colB = P.colA; P.valB = P.valA;
+    }
+    int *rowcnt = P.own<int>(pool, (long long)P.m + 1);
+    P.rowptrC = P.own<long long>(pool, (long long)P.m + 1);
+    if (!rowcnt || !P.rowptrC) return give_up(fail(TSG_ERR_OOM, "device pool allocation failed (small path)"));
+    e = small_count(pool, P.rpA, P.colA, P.k, P.rpB, P.colB, P.n, P.m, rowcnt, sstat);
+    if (e == cudaSuccess) e = scan_i32_to_i64(pool, rowcnt, P.rowptrC, P.m, ctx->dflags);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(ctx->dstat + ST_NNZC, P.rowptrC + P.m, sizeof(long long), cudaMemcpyDeviceToDevice, ctx->stream);
+    if (e != cudaSuccess) return give_up(fail(cuda_status(e), "small path: %s", cudaGetErrorString(e)));
+    // rows over the limit: the tiled path, now and for later calls of the shape
+    auto not_small = [&]() {
+        release();
+        cudaGetLastError();
+        key.small = false;
+        small_shape_record(ctx, key);
+        taken = false;
+        return TSG_OK;
+    };
+    long long cap = hint >= 0 ? hint + hint / 8 + 64 : -1;
+    if (cap < 0) {
+        r = host_wait(ctx, &P.nsync);
+        if (r) return give_up(r);
+        if (ctx->hstat[ST_SMALL] > 0) return not_small();
+        cap = ctx->hstat[ST_NNZC];
+    }
+    const bool dev_out = C->where == TSG_MEM_DEVICE;
+    const int bits = ctx->opts.out_rowptr_bits ? ctx->opts.out_rowptr_bits : (cap < (1ll << 31) ? 32 : 64);
+    if (bits == 32 && cap >= (1ll << 31)) return not_small();   // not reached: far past the path's sizes
+    for (int pass = 0; pass < 2; ++pass) {
+        col = pool.alloc_n<int>(std::max(cap, 1ll));
+        val = pool.alloc_n<double>(std::max(cap, 1ll));
+        if (!col || !val) return give_up(fail(TSG_ERR_OOM, "device pool allocation failed for C (%lld entries)", cap));
+        P.wait_values(ctx->stream);
+        e = small_fill(pool, P.rpA, P.colA, P.valA, P.k, P.rpB, P.colB, P.valB, P.n, P.m, P.rowptrC, cap, col, val,
+                       ctx->dflags);
+        if (e == cudaSuccess && dev_out && !rp_dev) e = output_rowptr(ctx, pool, P.m, bits, P.rowptrC, rp_dev);
+        if (e != cudaSuccess) return give_up(fail(cuda_status(e), "small path: %s", cudaGetErrorString(e)));
+        r = host_wait(ctx, &P.nsync);
+        if (r) return give_up(r);
+        if (ctx->hstat[ST_SMALL] > 0) return not_small();
+        if (ctx->hstat[ST_NNZC] <= cap) break;
+        // C outgrew the buffers sized from the shape's last call
+        pool.free(col); pool.free(val);
+        col = nullptr; val = nullptr;
+        cap = ctx->hstat[ST_NNZC];
+    }
+    const long long nnzC = ctx->hstat[ST_NNZC];
+    const long long products = ctx->hstat[ST_SMALL + 1];
+    key.nnzc = nnzC;
+    small_shape_record(ctx, key);
+    if (st) {
+        st->nnz_a = P.nnzA; st->nnz_b = P.nnzB; st->nnz_c = nnzC;
+        st->nnz_cub = ctx->opts.count_products ? products : 0;
+        st->small_path = 1;
+    }
+    if (dev_out) {
+        OutOwner *o = new OutOwner();
+        o->ctx = ctx;
+        o->where = C->where;
+        o->blocks.push_back({rp_dev, 0});
+        o->blocks.push_back({col, 0});
+        o->blocks.push_back({val, 0});
+        C->m = P.m; C->n = P.n; C->nnz = nnzC; C->rowptr_bits = bits;
+        C->row_ptr = rp_dev; C->col = col; C->val = val;
+        C->owner = o;
+        P.release(pool);
+    } else {
+        r = emit_output(ctx, pool, P.m, P.n, nnzC, P.rowptrC, col, val, C, st);   // frees col and val
+        P.release(pool);
+        if (r) { cudaStreamSynchronize(ctx->stream); return r; }
+        if (st) st->n_syncs = 1;
+    }
+    if (st) {
+        st->n_syncs += P.nsync;
+        st->ms_total = ms_since(t0);
+    }
+    return TSG_OK;
+}
 }  // namespace
 
 void *tsg::make_malloc_owner(void *a, void *b, void *c)
@@ -889,6 +1053,7 @@ void tsg_opts_default(tsg_opts *o)
     o->rows_global = 0;
     o->row_warps = 4;
     o->count_products = 1;
+    o->small_path = 1;
 }
 
 const char *tsg_last_error(void) { return g_err.c_str(); }
@@ -1060,6 +1225,11 @@ tsg_status tsg_spgemm(tsg_ctx *ctx, tsg_op op, const tsg_csr *A, const tsg_csr *
     auto t0 = std::chrono::steady_clock::now();
     CUDA_OK(cudaSetDevice(ctx->device));
     if (st) memset(st, 0, sizeof(*st));
+    {
+        bool taken = false;
+        const tsg_status rs = small_spgemm(ctx, op, A, B, C, st, taken);
+        if (taken) return rs;
+    }
     Pool pool{ctx->pool, ctx->stream};
     PlanData P;
     PhaseTimer tm(ctx, st && ctx->opts.phase_times);

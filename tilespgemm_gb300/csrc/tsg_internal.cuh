@@ -176,6 +176,19 @@ cudaError_t scan_i64_to_i64(Pool &pool, const long long *in, long long *out, lon
 
 inline int ceil_div_i(long long a, long long b) { return (int)((a + b - 1) / b); }
 
+// The small-product path (tsg_small.cu): rows of A that meet at most
+// SMALL_MAX_PRODUCTS entries of B, one warp per row of C.  small_count
+// writes each row's entry count (0 for rows over the limit) and adds the
+// rows over the limit to stat[0], the products to stat[1]; small_fill
+// writes C's columns and values at rowptrC (nothing when rowptrC[m] > cap).
+// ka = A's columns (= B's rows), nb = B's columns.
+constexpr int SMALL_MAX_PRODUCTS = 128;
+cudaError_t small_count(Pool &pool, const long long *rpA, const int *colA, int ka, const long long *rpB,
+                        const int *colB, int nb, int m, int *rowcnt, unsigned long long *stat);
+cudaError_t small_fill(Pool &pool, const long long *rpA, const int *colA, const double *valA, int ka,
+                       const long long *rpB, const int *colB, const double *valB, int nb, int m,
+                       const long long *rowptrC, long long cap, int *colC, double *valC, int *flags);
+
 // One instance of a batched product, as the pack/unpack kernels see it.
 struct PackDesc {
     const void *rp;          // instance row pointer (int32 or int64), device

@@ -1,0 +1,346 @@
+// tsg_small.cu -- the small-product path of tsg_spgemm: C = A*B row by row,
+// one warp per row of C, the row kept in a shared-memory hash table (or, for
+// rows of at most 32 products, in the warp's registers).
+//
+// The tiled pipeline (conversion, two symbolic steps, binned numeric step)
+// costs some 27 launches and three host waits per call, which is most of
+// the time of a product of a few million intermediate products (a 2D
+// Laplacian on a 256x256 grid: 1.6 M products).  Products whose every row of
+// A meets at most SMALL_MAX_PRODUCTS entries of B take this path instead:
+//   k_small_count  per row, the distinct columns among its products (hash
+//                  insertions) -> rowcnt; rows over the limit are counted in
+//                  stat[0] (the caller then takes the tiled path), the
+//                  products in stat[1]
+//   (the look-back scan of rowcnt gives C's row pointer)
+//   k_small_fill   per row, the same walk accumulating values, then the row's
+//                  entries written in column order.
+// The row's products are dealt 32 at a time in A's order then B's (lane =
+// position in the concatenation of the B rows of up to 32 A entries); lanes
+// of one round that meet in one output apply in lane order, so every entry
+// of C sees exactly the sequence fma(a_ik, b_kj, c) over k in A's row order,
+// as in the tiled path and the oracle: the two paths give identical values.
+// The reference has no such path; its per-call setup is the overhead
+// (main_spgemm-col.cu:4529-4774) that this path removes for small products.
+#include "tsg_internal.cuh"
+
+namespace tsg {
+
+namespace {
+
+constexpr int SH_WARPS = 8;                    // rows per CTA (one warp each)
+constexpr int SH_BITS = 8;
+constexpr int SH_CAP = 1 << SH_BITS;           // hash slots per warp
+static_assert(SMALL_MAX_PRODUCTS * 2 <= SH_CAP, "the table stays at most half full");
+
+__device__ __forceinline__ int sh_hash(int col) { return (int)(((unsigned)col * 2654435761u) >> (32 - SH_BITS)); }
+
+// slot of `col` in the warp's table, inserting it if absent (fresh: it was);
+// -1 if the table is full (not reached: at most SMALL_MAX_PRODUCTS keys)
+__device__ __forceinline__ int sh_insert(int *key, int col, bool &fresh)
+{
+    int h = sh_hash(col);
+    fresh = false;
+    for (int probe = 0; probe < SH_CAP; ++probe) {
+        const int old = atomicCAS(key + h, -1, col);
+        if (old == -1) { fresh = true; return h; }
+        if (old == col) return h;
+        h = (h + 1) & (SH_CAP - 1);
+    }
+    return -1;
+}
+
+// Up to 32 A entries of row r, lane q < na holding entry q's B row
+// [bs, bs + len) (len clamped to SMALL_MAX_PRODUCTS + 1, empty for an
+// out-of-range column of A).
+struct Batch {
+    long long bs = 0;
+    int len = 0;
+};
+
+__device__ __forceinline__ Batch load_batch(const long long *rpA, const int *colA, int ka, const long long *rpB,
+                                            long long p, int na, int lane, int &k)
+{
+    Batch b;
+    k = -1;
+    if (lane < na) {
+        k = colA[p + lane];
+        if ((unsigned)k < (unsigned)ka) {
+            b.bs = rpB[k];
+            const long long l = rpB[k + 1] - b.bs;
+            b.len = (int)(l < 0 ? 0 : (l > SMALL_MAX_PRODUCTS + 1 ? SMALL_MAX_PRODUCTS + 1 : l));
+        } else {
+            k = -1;
+        }
+    }
+    return b;
+}
+
+// the lane whose B row holds position f of the concatenation (last lane
+// whose exclusive offset is at or before f)
+__device__ __forceinline__ int owner_lane(int off, int f)
+{
+    int q = 0;
+#pragma unroll
+    for (int step = 16; step > 0; step >>= 1) {
+        const int oc = __shfl_sync(0xffffffffu, off, q + step);
+        if (oc <= f) q += step;
+    }
+    return q;
+}
+
+// Rows whose products fit one round (at most 32, from at most 32 A
+// entries) skip the table: the 32 lanes' keys are sorted across the warp
+// (bitonic network on shuffles), equal columns then sit in adjacent lanes
+// in product order, and the first lane of each run of equal columns starts
+// an entry of C.
+template <typename K>
+__device__ __forceinline__ K warp_sort_up(K key, int lane)
+{
+#pragma unroll
+    for (int k = 2; k <= 32; k <<= 1) {
+#pragma unroll
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            const K other = __shfl_xor_sync(0xffffffffu, key, j);
+            const bool keep_min = ((lane & j) == 0) == ((lane & k) == 0);
+            key = keep_min ? (other < key ? other : key) : (other > key ? other : key);
+        }
+    }
+    return key;
+}
+
+__global__ void __launch_bounds__(SH_WARPS * 32)
+k_small_count(const long long *__restrict__ rpA, const int *__restrict__ colA, int ka,
+              const long long *__restrict__ rpB, const int *__restrict__ colB, int nb, int m, int *rowcnt,
+              unsigned long long *stat)
+{
+    __shared__ int s_key[SH_WARPS][SH_CAP];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int r = blockIdx.x * SH_WARPS + warp;
+    if (r >= m) return;
+    int *key = s_key[warp];
+    bool table = false;      // the hash table is set up on the first batch that needs it
+    const long long a0 = rpA[r], a1 = rpA[r + 1];
+    int cnt = 0, P = 0;
+    bool over = false;
+    for (long long pb = a0; pb < a1; pb += 32) {
+        const int na = (int)min(32ll, a1 - pb);
+        int k;
+        const Batch b = load_batch(rpA, colA, ka, rpB, pb, na, lane, k);
+        const int incl = warp_incl_scan(b.len, lane);
+        const int T = __shfl_sync(0xffffffffu, incl, 31);
+        P += T;
+        if (P > SMALL_MAX_PRODUCTS) { over = true; break; }
+        const int off = incl - b.len;
+        if (a1 - a0 <= 32 && T <= 32) {
+            // one round: sort the columns, count the runs
+            const int q = owner_lane(off, lane);
+            const long long e = __shfl_sync(0xffffffffu, b.bs, q) + (lane - __shfl_sync(0xffffffffu, off, q));
+            unsigned key = 0xffffffffu;
+            if (lane < T) {
+                const int col = colB[e];
+                if ((unsigned)col < (unsigned)nb) key = (unsigned)col;
+            }
+            key = warp_sort_up(key, lane);
+            const unsigned prev = __shfl_up_sync(0xffffffffu, key, 1);
+            const bool head = key != 0xffffffffu && (lane == 0 || prev != key);
+            const unsigned heads = __ballot_sync(0xffffffffu, head);   // every lane takes part
+            cnt = lane == 0 ? __popc(heads) : 0;
+            break;
+        }
+        if (!table) {
+            for (int t = lane; t < SH_CAP; t += 32) key[t] = -1;
+            __syncwarp();
+            table = true;
+        }
+        for (int base = 0; base < T; base += 32) {
+            const int f = base + lane;
+            const int q = owner_lane(off, f);
+            const long long e = __shfl_sync(0xffffffffu, b.bs, q) + (f - __shfl_sync(0xffffffffu, off, q));
+            if (f < T) {
+                const int col = colB[e];
+                if ((unsigned)col < (unsigned)nb) {
+                    bool fresh;
+                    sh_insert(key, col, fresh);
+                    cnt += fresh ? 1 : 0;
+                }
+            }
+        }
+    }
+    cnt = warp_sum_int(cnt);
+    if (lane == 0) {
+        rowcnt[r] = over ? 0 : cnt;
+        if (over) atomicAdd(stat, 1ull);
+        else if (P) atomicAdd(stat + 1, (unsigned long long)P);
+    }
+}
+
+__global__ void __launch_bounds__(SH_WARPS * 32)
+k_small_fill(const long long *__restrict__ rpA, const int *__restrict__ colA, const double *__restrict__ valA, int ka,
+             const long long *__restrict__ rpB, const int *__restrict__ colB, const double *__restrict__ valB, int nb,
+             int m, const long long *__restrict__ rowptrC, long long cap, int *colC, double *valC, int *flags)
+{
+    __shared__ int s_key[SH_WARPS][SH_CAP];
+    __shared__ double s_val[SH_WARPS][SH_CAP];
+    __shared__ int s_ck[SH_WARPS][SMALL_MAX_PRODUCTS];
+    __shared__ double s_cv[SH_WARPS][SMALL_MAX_PRODUCTS];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int r = blockIdx.x * SH_WARPS + warp;
+    if (r >= m) return;
+    const long long Rb = rowptrC[r], Re = rowptrC[r + 1];
+    // C larger than the buffers: nothing is written (the caller sees nnzC
+    // and runs this pass again into buffers of that size)
+    if (rowptrC[m] > cap) return;
+    const long long a0 = rpA[r], a1 = rpA[r + 1];
+    if (a1 - a0 <= 32) {
+        const int na = (int)(a1 - a0);
+        int k;
+        const Batch b = load_batch(rpA, colA, ka, rpB, a0, na, lane, k);
+        const int incl = warp_incl_scan(b.len, lane);
+        const int T = __shfl_sync(0xffffffffu, incl, 31);
+        if (T <= 32) {
+            // one round: lane f holds product f (A's order, then B's); the
+            // keys (column, f) sorted across the warp put each column's
+            // products in adjacent lanes in product order, and the run's
+            // first lane applies them in that order
+            const double av = (lane < na && k >= 0) ? valA[a0 + lane] : 0.0;
+            const int off = incl - b.len;
+            const int q = owner_lane(off, lane);
+            const long long e = __shfl_sync(0xffffffffu, b.bs, q) + (lane - __shfl_sync(0xffffffffu, off, q));
+            const double a = __shfl_sync(0xffffffffu, av, q);
+            unsigned long long key = ~0ull;
+            double bv = 0.0;
+            if (lane < T) {
+                const int col = colB[e];
+                if ((unsigned)col < (unsigned)nb) {
+                    key = ((unsigned long long)(unsigned)col << 5) | (unsigned)lane;
+                    bv = valB[e];
+                }
+            }
+            key = warp_sort_up(key, lane);
+            const bool live = key != ~0ull;
+            const int src = (int)(key & 31u);
+            const int col = (int)(key >> 5);
+            const double sa = __shfl_sync(0xffffffffu, a, src), sb = __shfl_sync(0xffffffffu, bv, src);
+            const int pcol = __shfl_up_sync(0xffffffffu, col, 1);
+            const bool head = live && (lane == 0 || pcol != col);
+            const unsigned heads = __ballot_sync(0xffffffffu, head);
+            const int n = __popc(heads);
+            if ((long long)n != Re - Rb) {
+                if (lane == 0) set_flag(flags, FLAG_INTERNAL);
+                return;
+            }
+            // run of lane i: lanes i, i+1, ... while the column stays col
+            double acc = 0.0;
+            bool more = head;
+            for (int j = 0; __any_sync(0xffffffffu, more); ++j) {
+                const int cj = __shfl_down_sync(0xffffffffu, col, j);
+                const bool lj = __shfl_down_sync(0xffffffffu, live ? 1 : 0, j) != 0;
+                const double aj = __shfl_down_sync(0xffffffffu, sa, j), bj = __shfl_down_sync(0xffffffffu, sb, j);
+                more = more && lane + j < 32 && lj && cj == col;
+                if (more) acc = fma(aj, bj, acc);
+            }
+            if (head) {
+                const int rank = __popc(heads & lanemask_lt());
+                colC[Rb + rank] = col;
+                valC[Rb + rank] = acc;
+            }
+            return;
+        }
+    }
+    int *key = s_key[warp];
+    double *val = s_val[warp];
+    for (int t = lane; t < SH_CAP; t += 32) { key[t] = -1; val[t] = 0.0; }
+    __syncwarp();
+    int P = 0;
+    for (long long pb = a0; pb < a1; pb += 32) {
+        const int na = (int)min(32ll, a1 - pb);
+        int k;
+        const Batch b = load_batch(rpA, colA, ka, rpB, pb, na, lane, k);
+        const double av = (lane < na && k >= 0) ? valA[pb + lane] : 0.0;
+        const int incl = warp_incl_scan(b.len, lane);
+        const int T = __shfl_sync(0xffffffffu, incl, 31);
+        P += T;
+        if (P > SMALL_MAX_PRODUCTS) return;   // counted as over the limit: the row is empty here
+        const int off = incl - b.len;
+        for (int base = 0; base < T; base += 32) {
+            const int f = base + lane;
+            const int q = owner_lane(off, f);
+            const long long e = __shfl_sync(0xffffffffu, b.bs, q) + (f - __shfl_sync(0xffffffffu, off, q));
+            const double a = __shfl_sync(0xffffffffu, av, q);
+            int slot = -1;
+            double bv = 0.0;
+            if (f < T) {
+                const int col = colB[e];
+                if ((unsigned)col < (unsigned)nb) {
+                    bool fresh;
+                    slot = sh_insert(key, col, fresh);
+                    bv = valB[e];
+                }
+            }
+            // lanes on one output apply in lane order (A's order, then B's)
+            const unsigned peers = __match_any_sync(0xffffffffu, slot >= 0 ? slot : -2 - lane);
+            const int rank = __popc(peers & lanemask_lt());
+            if (!__any_sync(0xffffffffu, rank > 0)) {
+                if (slot >= 0) val[slot] = fma(a, bv, val[slot]);
+            } else {
+                const int rounds = __reduce_max_sync(0xffffffffu, (unsigned)__popc(peers));
+                for (int q2 = 0; q2 < rounds; ++q2) {
+                    if (q2 == rank && slot >= 0) val[slot] = fma(a, bv, val[slot]);
+                    __syncwarp();
+                }
+            }
+            __syncwarp();
+        }
+    }
+    // the row's entries, compacted in slot order, then each to its rank by column
+    int *ck = s_ck[warp];
+    double *cv = s_cv[warp];
+    int n = 0;
+    for (int t0 = 0; t0 < SH_CAP; t0 += 32) {
+        const int t = t0 + lane;
+        const int kk = key[t];
+        const unsigned bal = __ballot_sync(0xffffffffu, kk >= 0);
+        if (kk >= 0) {
+            const int p = n + __popc(bal & lanemask_lt());
+            if (p < SMALL_MAX_PRODUCTS) { ck[p] = kk; cv[p] = val[t]; }
+        }
+        n += __popc(bal);
+    }
+    __syncwarp();
+    if ((long long)n != Re - Rb || n > SMALL_MAX_PRODUCTS) {
+        if (lane == 0) set_flag(flags, FLAG_INTERNAL);
+        return;
+    }
+    for (int p = lane; p < n; p += 32) {
+        const int c = ck[p];
+        int rank = 0;
+        for (int j = 0; j < n; ++j) rank += ck[j] < c ? 1 : 0;
+        colC[Rb + rank] = c;
+        valC[Rb + rank] = cv[p];
+    }
+}
+
+}  // namespace
+
+cudaError_t small_count(Pool &pool, const long long *rpA, const int *colA, int ka, const long long *rpB,
+                        const int *colB, int nb, int m, int *rowcnt, unsigned long long *stat)
+{
+    if (m <= 0) return cudaSuccess;
+    k_small_count<<<(unsigned)((m + SH_WARPS - 1) / SH_WARPS), SH_WARPS * 32, 0, pool.stream>>>(rpA, colA, ka, rpB, colB,
+                                                                                                 nb, m, rowcnt, stat);
+    ::tsg::count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t small_fill(Pool &pool, const long long *rpA, const int *colA, const double *valA, int ka,
+                       const long long *rpB, const int *colB, const double *valB, int nb, int m,
+                       const long long *rowptrC, long long cap, int *colC, double *valC, int *flags)
+{
+    if (m <= 0) return cudaSuccess;
+    k_small_fill<<<(unsigned)((m + SH_WARPS - 1) / SH_WARPS), SH_WARPS * 32, 0, pool.stream>>>(
+        rpA, colA, valA, ka, rpB, colB, valB, nb, m, rowptrC, cap, colC, valC, flags);
+    ::tsg::count_launch();
+    return cudaGetLastError();
+}
+
+}  // namespace tsg
