@@ -85,30 +85,32 @@ def test_small_path_golden(sctx, name):
 
 
 def test_repeated_shape_waits_once(built_lib):
-    """The second call of a shape sizes C from the first and waits once; a
-    larger C of the same shape is found at that wait and filled again."""
+    """A shape's first call counts, scans, reads C's size back and fills (two
+    waits); a repeat with the same structure fills at the kept row pointer
+    and waits once; a matrix of the same shape but another structure is
+    caught there (every row is counted again), counted and filled into
+    buffers sized from the last call -- and filled once more when C
+    outgrew them -- with the exact result every time."""
     from tilespgemm_gb300 import Context
     band, spread = _banded_and_spread(3000, 8, seed=3)
+
+    def run(c, X, Xd, syncs):
+        oc, st = c.spgemm_raw(Xd, op="AA", out="device", stats=True)
+        C = oc.download()
+        oc.free()
+        _oracle(C, X, X)
+        assert st["small_path"] == 1 and st["n_syncs"] == syncs, st["n_syncs"]
+        assert st["nnz_cub"] == O.nnzcub(X, X)
+
     with Context(0) as c:
-        Ad = band.to_device(0)
-        for i in range(3):
-            oc, st = c.spgemm_raw(Ad, op="AA", out="device", stats=True)
-            C = oc.download()
-            oc.free()
-            _oracle(C, band, band)
-            assert st["small_path"] == 1
-            assert st["n_syncs"] == (2 if i == 0 else 1)
-        Sd = spread.to_device(0)                 # same shape, C about 4x larger
-        oc, st = c.spgemm_raw(Sd, op="AA", out="device", stats=True)
-        C = oc.download()
-        oc.free()
-        _oracle(C, spread, spread)
-        assert st["small_path"] == 1 and st["n_syncs"] == 2
-        oc, st = c.spgemm_raw(Ad, op="AA", out="device", stats=True)   # back to the band
-        C = oc.download()
-        oc.free()
-        _oracle(C, band, band)
-        assert st["n_syncs"] == 1
+        Ad, Sd = band.to_device(0), spread.to_device(0)
+        run(c, band, Ad, 2)
+        run(c, band, Ad, 1)
+        run(c, band, Ad, 1)
+        run(c, spread, Sd, 3)      # kept fill, count + fill, fill again (C about 4x larger)
+        run(c, spread, Sd, 1)
+        run(c, band, Ad, 2)        # kept fill, count + fill (the buffers are large enough)
+        run(c, band, Ad, 1)
 
 
 def test_rows_over_the_limit_take_the_tiled_path(sctx):

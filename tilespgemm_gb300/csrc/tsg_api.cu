@@ -124,6 +124,7 @@ struct SmallShape {
     int op = 0, m = 0, k = 0, n = 0;
     long long nnz_a = 0, nnz_b = 0, nnzc = 0;
     bool small = true;
+    long long *rowptr = nullptr;   // C's row pointer of the last call (device, m+1; the context's pool)
 };
 
 struct tsg_ctx {
@@ -886,19 +887,34 @@ SmallShape *small_shape_find(tsg_ctx *ctx, const SmallShape &k)
     return nullptr;
 }
 
-void small_shape_record(tsg_ctx *ctx, const SmallShape &k)
+// the shape's entry, updated or added (the oldest dropped past SMALL_SHAPES)
+SmallShape *small_shape_record(tsg_ctx *ctx, const SmallShape &k)
 {
-    if (SmallShape *s = small_shape_find(ctx, k)) { *s = k; return; }
-    if (ctx->small_shapes.size() >= SMALL_SHAPES) ctx->small_shapes.erase(ctx->small_shapes.begin());
-    ctx->small_shapes.push_back(k);
+    SmallShape *s = small_shape_find(ctx, k);
+    if (!s) {
+        if (ctx->small_shapes.size() >= SMALL_SHAPES) {
+            if (ctx->small_shapes.front().rowptr) cudaFreeAsync(ctx->small_shapes.front().rowptr, ctx->stream);
+            ctx->small_shapes.erase(ctx->small_shapes.begin());
+        }
+        ctx->small_shapes.push_back(k);
+        s = &ctx->small_shapes.back();
+        s->rowptr = nullptr;
+    }
+    s->nnzc = k.nnzc;
+    s->small = k.small;
+    if (!s->small && s->rowptr) { cudaFreeAsync(s->rowptr, ctx->stream); s->rowptr = nullptr; }
+    return s;
 }
 
 // tsg_spgemm for products whose every row of A meets at most
 // SMALL_MAX_PRODUCTS entries of B (A*B and A*A, operands of at most
-// SMALL_NNZ_MAX entries): one warp per row of C (tsg_small.cu), row counts,
-// scan, fill.  The first call of a shape reads C's size back before the fill
-// (two host waits); later calls of the shape size C's buffers from it and
-// wait once, at the end (a larger C is found there and the fill run again).
+// SMALL_NNZ_MAX entries): one warp per row of C (tsg_small.cu).  A shape's
+// first call runs the count pass and scan, reads C's size back and fills
+// (two host waits).  Later calls of the shape run the fill alone at the row
+// pointer kept from the last call, counting every row again: when all counts
+// agree that row pointer is C's and the call waits once; otherwise the count
+// pass and scan run and the fill follows into buffers sized from the last
+// call (a larger C is found at the wait and the fill repeated).
 // taken = false: nothing was returned to the caller -- the product is not
 // small, or turned out not to be -- and the tiled path runs instead.
 tsg_status small_spgemm(tsg_ctx *ctx, tsg_op op, const tsg_csr *A, const tsg_csr *B, tsg_csr *C, tsg_stats *st,
@@ -911,9 +927,8 @@ tsg_status small_spgemm(tsg_ctx *ctx, tsg_op op, const tsg_csr *A, const tsg_csr
     if (A->nnz > SMALL_NNZ_MAX || Bm->nnz > SMALL_NNZ_MAX) return TSG_OK;
     SmallShape key;
     key.op = (int)op; key.m = A->m; key.k = A->n; key.n = Bm->n; key.nnz_a = A->nnz; key.nnz_b = Bm->nnz;
-    const SmallShape *seen = small_shape_find(ctx, key);
+    SmallShape *seen = small_shape_find(ctx, key);
     if (seen && !seen->small) return TSG_OK;
-    const long long hint = seen ? seen->nnzc : -1;
     taken = true;
     auto t0 = std::chrono::steady_clock::now();
     Pool pool{ctx->pool, ctx->stream};
@@ -921,20 +936,32 @@ tsg_status small_spgemm(tsg_ctx *ctx, tsg_op op, const tsg_csr *A, const tsg_csr
     int *col = nullptr;
     double *val = nullptr;
     void *rp_dev = nullptr;
-    // undo everything before a return (the stream drained first)
+    auto drop_cv = [&]() { pool.free(col); pool.free(val); col = nullptr; val = nullptr; };
+    // undo everything before a return (values' upload joined, the stream drained)
     auto release = [&]() {
         P.wait_values(ctx->stream);
-        pool.free(col); pool.free(val); pool.free(rp_dev);
-        col = nullptr; val = nullptr; rp_dev = nullptr;
+        drop_cv();
+        pool.free(rp_dev);
+        rp_dev = nullptr;
         P.release(pool);
         cudaStreamSynchronize(ctx->stream);
     };
     auto give_up = [&](tsg_status r) { release(); cudaGetLastError(); return r; };
+    auto cuda_fail = [&](cudaError_t e) { return give_up(fail(cuda_status(e), "small path: %s", cudaGetErrorString(e))); };
+    // rows over the limit: the tiled path, now and for later calls of the shape
+    auto not_small = [&]() {
+        release();
+        cudaGetLastError();
+        key.small = false;
+        small_shape_record(ctx, key);
+        taken = false;
+        return TSG_OK;
+    };
     const bool validate = ctx->opts.validate != 0;
     unsigned long long *sstat = reinterpret_cast<unsigned long long *>(ctx->dstat + ST_SMALL);
     cudaError_t e = cudaMemsetAsync(ctx->dflags, 0, sizeof(int) * FLAG_COUNT, ctx->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(ctx->dstat, 0, sizeof(long long) * ST_SLOTS, ctx->stream);
-    if (e != cudaSuccess) return give_up(fail(cuda_status(e), "small path: %s", cudaGetErrorString(e)));
+    if (e != cudaSuccess) return cuda_fail(e);
     P.op = op; P.m = A->m; P.k = A->n; P.nnzA = A->nnz;
     tsg_status r = stage_into_plan(ctx, pool, P, A, validate, false, P.rpA, P.colA, P.valA, P.valA_buf);
     if (r) return give_up(r);
@@ -946,55 +973,77 @@ tsg_status small_spgemm(tsg_ctx *ctx, tsg_op op, const tsg_csr *A, const tsg_csr
         P.n = A->n; P.nnzB = A->nnz;
         P.rpB = P.rpA; P.colB = P.colA; P.valB = P.valA;
     }
-    int *rowcnt = P.own<int>(pool, (long long)P.m + 1);
-    P.rowptrC = P.own<long long>(pool, (long long)P.m + 1);
-    if (!rowcnt || !P.rowptrC) return give_up(fail(TSG_ERR_OOM, "device pool allocation failed (small path)"));
-    e = small_count(pool, P.rpA, P.colA, P.k, P.rpB, P.colB, P.n, P.m, rowcnt, sstat);
-    if (e == cudaSuccess) e = scan_i32_to_i64(pool, rowcnt, P.rowptrC, P.m, ctx->dflags);
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(ctx->dstat + ST_NNZC, P.rowptrC + P.m, sizeof(long long), cudaMemcpyDeviceToDevice, ctx->stream);
-    if (e != cudaSuccess) return give_up(fail(cuda_status(e), "small path: %s", cudaGetErrorString(e)));
-    // rows over the limit: the tiled path, now and for later calls of the shape
-    auto not_small = [&]() {
-        release();
-        cudaGetLastError();
-        key.small = false;
-        small_shape_record(ctx, key);
-        taken = false;
-        return TSG_OK;
-    };
-    long long cap = hint >= 0 ? hint + hint / 8 + 64 : -1;
-    if (cap < 0) {
-        r = host_wait(ctx, &P.nsync);
-        if (r) return give_up(r);
-        if (ctx->hstat[ST_SMALL] > 0) return not_small();
-        cap = ctx->hstat[ST_NNZC];
-    }
     const bool dev_out = C->where == TSG_MEM_DEVICE;
-    const int bits = ctx->opts.out_rowptr_bits ? ctx->opts.out_rowptr_bits : (cap < (1ll << 31) ? 32 : 64);
-    if (bits == 32 && cap >= (1ll << 31)) return not_small();   // not reached: far past the path's sizes
-    for (int pass = 0; pass < 2; ++pass) {
-        col = pool.alloc_n<int>(std::max(cap, 1ll));
-        val = pool.alloc_n<double>(std::max(cap, 1ll));
-        if (!col || !val) return give_up(fail(TSG_ERR_OOM, "device pool allocation failed for C (%lld entries)", cap));
+    // C's row pointer type: 32-bit unless asked otherwise (C stays far below
+    // 2^31 entries on this path: at most SMALL_MAX_PRODUCTS per entry of A)
+    const int bits = ctx->opts.out_rowptr_bits ? ctx->opts.out_rowptr_bits : 32;
+    // buffers of `cap` entries, the fill at `rowptr` (kept: rows counted
+    // against it), the caller's row pointer for device output, the wait
+    auto fill = [&](const long long *rowptr, long long cap, bool kept) -> tsg_status {
+        col = pool.alloc_n<int>(cap);
+        val = pool.alloc_n<double>(cap);
+        if (!col || !val) return fail(TSG_ERR_OOM, "device pool allocation failed for C (%lld entries)", cap);
         P.wait_values(ctx->stream);
-        e = small_fill(pool, P.rpA, P.colA, P.valA, P.k, P.rpB, P.colB, P.valB, P.n, P.m, P.rowptrC, cap, col, val,
-                       ctx->dflags);
-        if (e == cudaSuccess && dev_out && !rp_dev) e = output_rowptr(ctx, pool, P.m, bits, P.rowptrC, rp_dev);
-        if (e != cudaSuccess) return give_up(fail(cuda_status(e), "small path: %s", cudaGetErrorString(e)));
-        r = host_wait(ctx, &P.nsync);
+        cudaError_t fe = small_fill(pool, P.rpA, P.colA, P.valA, P.k, P.rpB, P.colB, P.valB, P.n, P.m, rowptr, cap,
+                                    col, val, ctx->dflags, kept ? sstat : nullptr);
+        if (fe == cudaSuccess && dev_out && !rp_dev) fe = output_rowptr(ctx, pool, P.m, bits, rowptr, rp_dev);
+        if (fe != cudaSuccess) return fail(cuda_status(fe), "small path: %s", cudaGetErrorString(fe));
+        return host_wait(ctx, &P.nsync);
+    };
+    const long long *rowptr = nullptr;   // C's row pointer: the kept one, or this call's scan
+    long long nnzC = 0;
+    if (seen && seen->rowptr) {
+        r = fill(seen->rowptr, seen->nnzc, true);
         if (r) return give_up(r);
-        if (ctx->hstat[ST_SMALL] > 0) return not_small();
-        if (ctx->hstat[ST_NNZC] <= cap) break;
-        // C outgrew the buffers sized from the shape's last call
-        pool.free(col); pool.free(val);
-        col = nullptr; val = nullptr;
-        cap = ctx->hstat[ST_NNZC];
+        if (ctx->hstat[ST_SMALL] == 0) {
+            rowptr = seen->rowptr;
+            nnzC = seen->nnzc;
+        } else {   // a row differs from the kept pointer: the count pass decides
+            drop_cv();
+            pool.free(rp_dev);
+            rp_dev = nullptr;
+            e = cudaMemsetAsync(ctx->dstat + ST_SMALL, 0, 2 * sizeof(long long), ctx->stream);
+            if (e != cudaSuccess) return cuda_fail(e);
+        }
     }
-    const long long nnzC = ctx->hstat[ST_NNZC];
+    if (!rowptr) {
+        int *rowcnt = P.own<int>(pool, (long long)P.m + 1);
+        P.rowptrC = P.own<long long>(pool, (long long)P.m + 1);
+        if (!rowcnt || !P.rowptrC) return give_up(fail(TSG_ERR_OOM, "device pool allocation failed (small path)"));
+        e = small_count(pool, P.rpA, P.colA, P.k, P.rpB, P.colB, P.n, P.m, rowcnt, sstat);
+        if (e == cudaSuccess) e = scan_i32_to_i64(pool, rowcnt, P.rowptrC, P.m, ctx->dflags);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(ctx->dstat + ST_NNZC, P.rowptrC + P.m, sizeof(long long), cudaMemcpyDeviceToDevice,
+                                ctx->stream);
+        if (e != cudaSuccess) return cuda_fail(e);
+        long long cap = seen ? seen->nnzc + seen->nnzc / 8 + 64 : -1;
+        if (cap < 0) {   // a new shape: C's size first
+            r = host_wait(ctx, &P.nsync);
+            if (r) return give_up(r);
+            if (ctx->hstat[ST_SMALL] > 0) return not_small();
+            cap = ctx->hstat[ST_NNZC];
+        }
+        for (int pass = 0;; ++pass) {
+            r = fill(P.rowptrC, cap, false);
+            if (r) return give_up(r);
+            if (ctx->hstat[ST_SMALL] > 0) return not_small();
+            if (ctx->hstat[ST_NNZC] <= cap || pass > 0) break;
+            drop_cv();   // C outgrew the buffers sized from the shape's last call
+            cap = ctx->hstat[ST_NNZC];
+        }
+        rowptr = P.rowptrC;
+        nnzC = ctx->hstat[ST_NNZC];
+    }
     const long long products = ctx->hstat[ST_SMALL + 1];
     key.nnzc = nnzC;
-    small_shape_record(ctx, key);
+    seen = small_shape_record(ctx, key);
+    if (rowptr == P.rowptrC) {   // kept for the shape's next call (when memory allows)
+        if (!seen->rowptr) seen->rowptr = pool.alloc_n<long long>((long long)P.m + 1);
+        if (seen->rowptr)
+            cudaMemcpyAsync(seen->rowptr, P.rowptrC, sizeof(long long) * ((size_t)P.m + 1), cudaMemcpyDeviceToDevice,
+                            ctx->stream);
+        cudaGetLastError();
+    }
     if (st) {
         st->nnz_a = P.nnzA; st->nnz_b = P.nnzB; st->nnz_c = nnzC;
         st->nnz_cub = ctx->opts.count_products ? products : 0;
@@ -1012,7 +1061,7 @@ tsg_status small_spgemm(tsg_ctx *ctx, tsg_op op, const tsg_csr *A, const tsg_csr
         C->owner = o;
         P.release(pool);
     } else {
-        r = emit_output(ctx, pool, P.m, P.n, nnzC, P.rowptrC, col, val, C, st);   // frees col and val
+        r = emit_output(ctx, pool, P.m, P.n, nnzC, rowptr, col, val, C, st);   // frees col and val
         P.release(pool);
         if (r) { cudaStreamSynchronize(ctx->stream); return r; }
         if (st) st->n_syncs = 1;
@@ -1023,6 +1072,7 @@ tsg_status small_spgemm(tsg_ctx *ctx, tsg_op op, const tsg_csr *A, const tsg_csr
     }
     return TSG_OK;
 }
+
 }  // namespace
 
 void *tsg::make_malloc_owner(void *a, void *b, void *c)
@@ -1181,6 +1231,8 @@ tsg_status tsg_destroy(tsg_ctx *c)
     if (c->side) { cudaStreamSynchronize(c->side); cudaStreamDestroy(c->side); }
     if (c->copy) { cudaStreamSynchronize(c->copy); cudaStreamDestroy(c->copy); }
     for (cudaEvent_t e : {c->cfork, c->vals_ev, c->cols_ev, c->copy_done}) if (e) cudaEventDestroy(e);
+    for (auto &sh : c->small_shapes) if (sh.rowptr) cudaFreeAsync(sh.rowptr, c->stream);
+    if (c->stream) cudaStreamSynchronize(c->stream);
     if (c->dflags) cudaFree(c->dflags);
     if (c->dstat) cudaFree(c->dstat);
     if (c->hstat) cudaFreeHost(c->hstat);

@@ -13,7 +13,12 @@
 //                  products in stat[1]
 //   (the look-back scan of rowcnt gives C's row pointer)
 //   k_small_fill   per row, the same walk accumulating values, then the row's
-//                  entries written in column order.
+//                  entries written in column order.  With `kept` (C's row
+//                  pointer kept from the last call of the same shape, no
+//                  count pass before it) a row whose entries differ from the
+//                  kept count, or that is over the limit, adds 1 to kept[0]
+//                  (the caller then runs the count pass), the products go
+//                  to kept[1].
 // The row's products are dealt 32 at a time in A's order then B's (lane =
 // position in the concatenation of the B rows of up to 32 A entries); lanes
 // of one round that meet in one output apply in lane order, so every entry
@@ -177,7 +182,8 @@ k_small_count(const long long *__restrict__ rpA, const int *__restrict__ colA, i
 __global__ void __launch_bounds__(SH_WARPS * 32)
 k_small_fill(const long long *__restrict__ rpA, const int *__restrict__ colA, const double *__restrict__ valA, int ka,
              const long long *__restrict__ rpB, const int *__restrict__ colB, const double *__restrict__ valB, int nb,
-             int m, const long long *__restrict__ rowptrC, long long cap, int *colC, double *valC, int *flags)
+             int m, const long long *__restrict__ rowptrC, long long cap, int *colC, double *valC, int *flags,
+             unsigned long long *kept)
 {
     __shared__ int s_key[SH_WARPS][SH_CAP];
     __shared__ double s_val[SH_WARPS][SH_CAP];
@@ -226,9 +232,13 @@ k_small_fill(const long long *__restrict__ rpA, const int *__restrict__ colA, co
             const unsigned heads = __ballot_sync(0xffffffffu, head);
             const int n = __popc(heads);
             if ((long long)n != Re - Rb) {
-                if (lane == 0) set_flag(flags, FLAG_INTERNAL);
+                if (lane == 0) {
+                    if (kept) atomicAdd(kept, 1ull);
+                    else set_flag(flags, FLAG_INTERNAL);
+                }
                 return;
             }
+            if (kept && lane == 0 && T) atomicAdd(kept + 1, (unsigned long long)T);
             // run of lane i: lanes i, i+1, ... while the column stays col
             double acc = 0.0;
             bool more = head;
@@ -260,7 +270,10 @@ k_small_fill(const long long *__restrict__ rpA, const int *__restrict__ colA, co
         const int incl = warp_incl_scan(b.len, lane);
         const int T = __shfl_sync(0xffffffffu, incl, 31);
         P += T;
-        if (P > SMALL_MAX_PRODUCTS) return;   // counted as over the limit: the row is empty here
+        if (P > SMALL_MAX_PRODUCTS) {   // counted as over the limit: the row is empty here
+            if (kept && lane == 0) atomicAdd(kept, 1ull);
+            return;
+        }
         const int off = incl - b.len;
         for (int base = 0; base < T; base += 32) {
             const int f = base + lane;
@@ -308,9 +321,13 @@ k_small_fill(const long long *__restrict__ rpA, const int *__restrict__ colA, co
     }
     __syncwarp();
     if ((long long)n != Re - Rb || n > SMALL_MAX_PRODUCTS) {
-        if (lane == 0) set_flag(flags, FLAG_INTERNAL);
+        if (lane == 0) {
+            if (kept) atomicAdd(kept, 1ull);
+            else set_flag(flags, FLAG_INTERNAL);
+        }
         return;
     }
+    if (kept && lane == 0 && P) atomicAdd(kept + 1, (unsigned long long)P);
     for (int p = lane; p < n; p += 32) {
         const int c = ck[p];
         int rank = 0;
@@ -334,11 +351,12 @@ cudaError_t small_count(Pool &pool, const long long *rpA, const int *colA, int k
 
 cudaError_t small_fill(Pool &pool, const long long *rpA, const int *colA, const double *valA, int ka,
                        const long long *rpB, const int *colB, const double *valB, int nb, int m,
-                       const long long *rowptrC, long long cap, int *colC, double *valC, int *flags)
+                       const long long *rowptrC, long long cap, int *colC, double *valC, int *flags,
+                       unsigned long long *kept)
 {
     if (m <= 0) return cudaSuccess;
     k_small_fill<<<(unsigned)((m + SH_WARPS - 1) / SH_WARPS), SH_WARPS * 32, 0, pool.stream>>>(
-        rpA, colA, valA, ka, rpB, colB, valB, nb, m, rowptrC, cap, colC, valC, flags);
+        rpA, colA, valA, ka, rpB, colB, valB, nb, m, rowptrC, cap, colC, valC, flags, kept);
     ::tsg::count_launch();
     return cudaGetLastError();
 }
