@@ -254,6 +254,28 @@ def measure_e2e(args, ctx, A, op, stream, nnz_c, barrier, dist):
     return ms_e2e, h2d, d2h
 
 
+def cli_per_call(A, device: int, runs: int = 200) -> dict | None:
+    """Per-call time through the plain-C command line (tilespgemm_gb300/_lib/tsg,
+    the reference driver's interface over the C ABI): A resident on the
+    device, C on the device, the minimum of `runs` calls by the host clock
+    around each call -- the library's cost without the Python wrapper."""
+    from tilespgemm_gb300 import build
+    from tilespgemm_gb300.api import write_mtx
+    if not build.CLI.exists():
+        return None
+    with tempfile.TemporaryDirectory() as td:
+        path = os.path.join(td, "a.mtx")
+        write_mtx(path, A, exact=True)
+        res = subprocess.run([str(build.CLI), "-d", str(device), "--keep-values", "--repeat", str(runs),
+                              "--csv", os.path.join(td, "r.csv"), path], capture_output=True, text=True, timeout=300)
+    for line in res.stdout.splitlines():
+        if "min of" in line and " ms," in line:
+            ms = float(line.split("runs =")[1].split("ms")[0])
+            return {"ms_min": ms, "runs": runs,
+                    "via": "tsg CLI (plain C over the C ABI; A resident on the device, C on the device)"}
+    return None
+
+
 def run_ours(args) -> None:
     import torch
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -279,9 +301,12 @@ def run_ours(args) -> None:
     Ad = A.to_device(local)
     Ad.rowptr = Ad.rowptr.to(torch.int32)          # the reference's int row pointers
     for _ in range(args.warmup):
+        t_call = time.perf_counter()
         oc, st = ctx.spgemm_raw(Ad, op=op, out="device", stats=True)
         oc.free()
+        t_call = time.perf_counter() - t_call
     nnz_c = st["nnz_c"]
+    every = t_call >= 1e-3   # per-step statistics cost next to nothing against the call
 
     def barrier():
         if dist is not None:
@@ -296,9 +321,10 @@ def run_ours(args) -> None:
         ev0 = torch.cuda.Event(enable_timing=True)
         ev1 = torch.cuda.Event(enable_timing=True)
         ev0.record(stream)
-        for _ in range(args.steps):
-            oc, st = ctx.spgemm_raw(Ad, op=op, out="device", stats=True)
-            phases.append(st)
+        for i in range(args.steps):   # calls under a millisecond: statistics of the last step only
+            oc, st = ctx.spgemm_raw(Ad, op=op, out="device", stats=every or i == args.steps - 1)
+            if st is not None:
+                phases.append(st)
             oc.free()
         ev1.record(stream)
         ev1.synchronize()
@@ -327,17 +353,22 @@ def run_ours(args) -> None:
     import ctypes
     fp64 = ctypes.c_double(0.0)
     _abi.check(lib.tsg_measure_fp64_peak(ctx.handle, ctypes.byref(fp64)))
-    ms_num = statistics.mean(p["ms_step3"] for p in phases)
+    # the small-product path has no phase events: its dominant kernel
+    # (k_small_fill) is taken with the call's time and the call's bytes
+    small = bool(phases[-1].get("small_path", 0))
     ab = algorithmic_bytes(A, B, nnz_c)
-    achieved = ab["numeric"] / (ms_num * 1e6)
-    traffic = load_traffic(args.workload)
+    ms_num = ms if small else statistics.mean(p["ms_step3"] for p in phases)
+    kbytes = ab["total"] if small else ab["numeric"]
+    achieved = kbytes / (ms_num * 1e6)
+    traffic = None if small else load_traffic(args.workload)
     roofline = {
-        "kernel": "k_numeric_smem (step 3: FP64 accumulation + CSR write)",
+        "kernel": ("k_small_fill (small-product path, the whole call: count pass skipped on a repeated shape)"
+                   if small else "k_numeric_smem (step 3: FP64 accumulation + CSR write)"),
         "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
         "frac": (achieved / hbm_peak) if hbm_peak else None,
         "peak_source": "of measured (MEASURED_PEAKS.json hbm_gbs)" if hbm_peak else "of fallback 6800 GB/s",
         "traffic": traffic,
-        "algorithmic_bytes_per_launch": ab["numeric"], "ms_per_launch": ms_num,
+        "algorithmic_bytes_per_launch": kbytes, "ms_per_launch": ms_num,
         "fp64": {"achieved_gflops": 2.0 * cub / (ms_num * 1e6), "peak_gflops": fp64.value,
                  "frac": 2.0 * cub / (ms_num * 1e6) / fp64.value if fp64.value else None,
                  "peak_source": "measured live (tsg_measure_fp64_peak, DFMA-only kernel)"},
@@ -363,8 +394,10 @@ def run_ours(args) -> None:
                    "l2": "inputs larger than L2: A is %.0f MB and C %.0f MB against a 129 MB L2" % (
                        (12 * A.nnz + 4 * A.m) / 1e6, 12 * nnz_c / 1e6),
                    "parallelism": f"one replica per GPU ({world})"},
-        "phases_ms": {"convert": mean("ms_convert"), "step1": mean("ms_step1"), "step2": mean("ms_step2"),
-                      "step3": mean("ms_step3")},
+        "phases_ms": (None if small else
+                      {"convert": mean("ms_convert"), "step1": mean("ms_step1"), "step2": mean("ms_step2"),
+                       "step3": mean("ms_step3")}),
+        "path": "small-product (row by row)" if small else "tiled",
         "host_waits_per_step": phases[-1]["n_syncs"],
         "roofline": roofline,
         "cpu_baseline": cpu,
@@ -374,6 +407,8 @@ def run_ours(args) -> None:
         "gpu_launches_per_step": launches / args.steps,
         "clocks": clk.summary(),
     }
+    if world == 1 and args.workload == "lap256":
+        out["c_abi_per_call"] = cli_per_call(A, local)
     if out["e2e"] is not None:
         # the host link's share: the bytes each way at the link's measured
         # bandwidth, as if nothing overlapped them
@@ -590,7 +625,8 @@ def sub_benchmarks(args) -> dict:
             out["configs"][w] = d
             continue
         out["configs"][w] = {"workload": d["config"]["workload"], "value": d["value"], "unit": d["unit"],
-                             "ms_per_step": d["ms_per_step"], "phases_ms": d["phases_ms"],
+                             "ms_per_step": d["ms_per_step"], "path": d.get("path"),
+                             "c_abi_per_call": d.get("c_abi_per_call"), "phases_ms": d["phases_ms"],
                              "nnz_a": d["config"]["nnz_a"], "nnz_cub": d["config"]["nnz_cub"],
                              "nnz_c": d["config"]["nnz_c"], "host_waits_per_step": d["host_waits_per_step"],
                              "gpu_launches_per_step": d["gpu_launches_per_step"],

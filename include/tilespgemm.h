@@ -150,6 +150,13 @@ const char *tsg_version(void);
 int64_t tsg_launch_count(void);
 void *tsg_get_stream(tsg_ctx *ctx);
 
+/* Order the context's stream after the work already queued on `stream` (a
+ * cudaStream_t of the caller's, e.g. the one that wrote a device operand;
+ * NULL = the legacy default stream), without blocking the host: the next
+ * call's kernels start once that work is done.  No counterpart in the
+ * reference (its operands are copied synchronously). */
+tsg_status tsg_stream_wait(tsg_ctx *ctx, void *stream);
+
 /* Bytes of pinned host memory the process-wide cache of host output buffers
  * keeps for reuse (no counterpart in the reference): min(96 GB, 3/8 of the
  * host's memory), or the environment variable TSG_PINNED_CACHE_BYTES read at

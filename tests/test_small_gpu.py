@@ -113,6 +113,39 @@ def test_repeated_shape_waits_once(built_lib):
         run(c, band, Ad, 1)
 
 
+def test_one_round_shape_then_longer_rows(built_lib):
+    """A shape whose rows all fit one warp round (at most 32 products) runs
+    the register-only fill when repeated; the same shape with rows of more
+    products is caught there, counted again and filled by the general
+    kernel -- exact every time."""
+    from tilespgemm_gb300 import Context
+    from tilespgemm_gb300.api import CSR
+    rng = np.random.default_rng(61)
+
+    def rows(lens, n):
+        rp = np.zeros(len(lens) + 1, np.int64)
+        np.cumsum(lens, out=rp[1:])
+        col = np.concatenate([np.sort(rng.choice(n, size=int(L), replace=False)) for L in lens]).astype(np.int32)
+        return CSR(len(lens), n, rp, col, rng.uniform(-1.0, 1.0, size=col.size))
+
+    A = rows([5] * 2000, 1000)
+    B1 = rows([5] * 1000, 800)                               # 25 products per row of A
+    B2 = rows([20] * 10 + [5] * 840 + [4] * 150, 800)         # the same nnz; rows 0-9 of 20 entries
+    assert B1.nnz == B2.nnz
+    with Context(0) as c:
+        Ad, B1d, B2d = A.to_device(0), B1.to_device(0), B2.to_device(0)
+        for B, Bd, syncs in ((B1, B1d, 2), (B1, B1d, 1), (B2, B2d, None), (B2, B2d, 1), (B1, B1d, None)):
+            oc, st = c.spgemm_raw(Ad, Bd, op="AB", out="device", stats=True)
+            C = oc.download()
+            oc.free()
+            _oracle(C, A, B)
+            assert st["small_path"] == 1
+            if syncs is not None:
+                assert st["n_syncs"] == syncs
+            else:
+                assert st["n_syncs"] >= 2
+
+
 def test_rows_over_the_limit_take_the_tiled_path(sctx):
     from tilespgemm_gb300 import matrices as M
     A = M.random_sparse(500, 500, 12, seed=40)      # 144 products per row

@@ -106,6 +106,7 @@ SIGNATURES = {
     "tsg_launch_count": (C.c_int64, []),
     "tsg_pinned_cache_cap": (C.c_int64, []),
     "tsg_get_stream": (C.c_void_p, [C.c_void_p]),
+    "tsg_stream_wait": (C.c_int, [C.c_void_p, C.c_void_p]),
     "tsg_measure_fp64_peak": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "tsg_load_mtx": (C.c_int, [C.c_char_p, C.POINTER(tsg_csr), C.POINTER(C.c_int32)]),
     "tsg_csr_free": (C.c_int, [C.c_void_p, C.POINTER(tsg_csr)]),

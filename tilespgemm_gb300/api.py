@@ -65,8 +65,11 @@ class CSR:
         return CSR(self.m, self.n, torch.as_tensor(np.asarray(self.rowptr)).to(dev),
                    torch.as_tensor(np.asarray(self.col)).to(dev), torch.as_tensor(np.asarray(self.val)).to(dev))
 
-    def _tsg(self) -> tuple[_abi.tsg_csr, list]:
-        """tsg_csr view of this matrix plus the objects that must stay alive."""
+    def _tsg(self, ctx_handle=None) -> tuple[_abi.tsg_csr, list]:
+        """tsg_csr view of this matrix plus the objects that must stay alive.
+        Device tensors: the context's stream (ctx_handle) is ordered after
+        torch's current stream without blocking; without a context the host
+        waits for torch's stream."""
         s = _abi.tsg_csr()
         s.m, s.n = int(self.m), int(self.n)
         keep: list = []
@@ -81,7 +84,10 @@ class CSR:
             s.where = _abi.MEM_DEVICE
             s.row_ptr, s.col, s.val = rp.data_ptr(), col.data_ptr(), val.data_ptr()
             s.nnz = int(col.numel())
-            torch.cuda.current_stream(rp.device).synchronize()
+            if ctx_handle:
+                check(lib().tsg_stream_wait(ctx_handle, torch.cuda.current_stream(rp.device).cuda_stream))
+            else:
+                torch.cuda.current_stream(rp.device).synchronize()
         else:
             rp = np.asarray(self.rowptr)
             if rp.dtype not in (np.int32, np.int64):
@@ -368,11 +374,11 @@ class Context:
     def spgemm_raw(self, A: CSR, B: CSR | None = None, op: str = "AA", out: str = "host",
                    stats: bool = False) -> tuple[OwnedCSR, dict | None]:
         """C = op(A, B) left in library-owned memory (`out` = "host" pinned or "device")."""
-        a, keep_a = A._tsg()
+        a, keep_a = A._tsg(self.handle)
         b_ptr = None
         keep_b: list = []
         if B is not None:
-            b, keep_b = B._tsg()
+            b, keep_b = B._tsg(self.handle)
             b_ptr = C.byref(b)
         c = _abi.tsg_csr()
         c.where = _abi.MEM_DEVICE if out == "device" else _abi.MEM_HOST

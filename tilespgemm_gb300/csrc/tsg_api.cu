@@ -124,6 +124,7 @@ struct SmallShape {
     int op = 0, m = 0, k = 0, n = 0;
     long long nnz_a = 0, nnz_b = 0, nnzc = 0;
     bool small = true;
+    bool one_round = false;        // every row of the last call fit one warp round (32 products)
     long long *rowptr = nullptr;   // C's row pointer of the last call (device, m+1; the context's pool)
 };
 
@@ -132,7 +133,7 @@ struct tsg_ctx {
     tsg_opts opts{};
     cudaStream_t stream = nullptr;
     cudaMemPool_t pool = nullptr;
-    int *dflags = nullptr;           // FLAG_COUNT ints
+    int *dflags = nullptr;           // FLAG_COUNT ints, inside dstat (slots ST_HFLAGS on)
     long long *dstat = nullptr;      // 64 slots
     long long *hstat = nullptr;      // pinned mirror: 64 stat slots + FLAG_COUNT flags (as long long)
     std::mutex mu;
@@ -145,6 +146,7 @@ struct tsg_ctx {
     // numeric step
     cudaStream_t copy = nullptr;
     cudaEvent_t cfork = nullptr, vals_ev = nullptr, cols_ev = nullptr, copy_done = nullptr;
+    cudaEvent_t ext_ev = nullptr;            // tsg_stream_wait: the caller's stream's point to wait for
     std::vector<SmallShape> small_shapes;   // the last SMALL_SHAPES shapes, newest last
 };
 
@@ -155,8 +157,8 @@ enum StatSlot {
     ST_NDEFER = 7,               // tile-rows left to the CTA step-2 kernel
     ST_BINS = 8,                 // step 2's bin statistics, BS_SLOTS slots (tsg_numeric.cuh)
     ST_BUNSORTED = 36,           // B rows whose columns are not strictly increasing
-    ST_SMALL = 37,               // small-product path: rows over its limit, products (2 slots)
-    ST_HFLAGS = 40,              // host mirror only: device flags
+    ST_SMALL = 37,               // small-product path: rows over its limit, products, a row past one round (3 slots)
+    ST_HFLAGS = 40,              // device: the flags (FLAG_COUNT ints); host: their mirror as int64
     ST_SLOTS = 64
 };
 
@@ -376,14 +378,15 @@ tsg_status read_flags(tsg_ctx *ctx)
 // device -> pinned mirror of stats and flags, then wait
 tsg_status host_wait(tsg_ctx *ctx, int *nsync)
 {
-    CUDA_OK(cudaMemcpyAsync(ctx->hstat, ctx->dstat, sizeof(long long) * ST_HFLAGS, cudaMemcpyDeviceToHost, ctx->stream));
+    // the statistics and, behind them, the flags: one copy
+    CUDA_OK(cudaMemcpyAsync(ctx->hstat, ctx->dstat, sizeof(long long) * ST_HFLAGS + sizeof(int) * FLAG_COUNT,
+                            cudaMemcpyDeviceToHost, ctx->stream));
     static_assert(FLAG_COUNT <= ST_SLOTS - ST_HFLAGS, "flag mirror");
-    static_assert(ST_BINS + BS_SLOTS <= ST_BUNSORTED && ST_BUNSORTED < ST_SMALL && ST_SMALL + 2 <= ST_HFLAGS,
+    static_assert(ST_BINS + BS_SLOTS <= ST_BUNSORTED && ST_BUNSORTED < ST_SMALL && ST_SMALL + 3 <= ST_HFLAGS,
                   "statistics slots");
     int hflags[FLAG_COUNT];
-    CUDA_OK(cudaMemcpyAsync(ctx->hstat + ST_HFLAGS + 16, ctx->dflags, sizeof(int) * FLAG_COUNT, cudaMemcpyDeviceToHost, ctx->stream));
     CUDA_OK(cudaStreamSynchronize(ctx->stream));
-    memcpy(hflags, ctx->hstat + ST_HFLAGS + 16, sizeof(hflags));
+    memcpy(hflags, ctx->hstat + ST_HFLAGS, sizeof(hflags));
     for (int f = 0; f < FLAG_COUNT; ++f) ctx->hstat[ST_HFLAGS + f] = hflags[f];
     if (nsync) ++*nsync;
     return read_flags(ctx);
@@ -525,7 +528,7 @@ tsg_status plan_symbolic(tsg_ctx *ctx, Pool &pool, Scratch &sc, tsg_op op, const
     tsg_status r = check_op(op, A, B);
     if (r) return r;
     if (reset_flags) CUDA_OK(cudaMemsetAsync(ctx->dflags, 0, sizeof(int) * FLAG_COUNT, ctx->stream));
-    CUDA_OK(cudaMemsetAsync(ctx->dstat, 0, sizeof(long long) * ST_SLOTS, ctx->stream));
+    CUDA_OK(cudaMemsetAsync(ctx->dstat, 0, sizeof(long long) * ST_HFLAGS, ctx->stream));   // the flags stay
     tm.mark();  // 0
     P.op = op;
     P.m = A->m;
@@ -902,6 +905,7 @@ SmallShape *small_shape_record(tsg_ctx *ctx, const SmallShape &k)
     }
     s->nnzc = k.nnzc;
     s->small = k.small;
+    s->one_round = k.one_round;
     if (!s->small && s->rowptr) { cudaFreeAsync(s->rowptr, ctx->stream); s->rowptr = nullptr; }
     return s;
 }
@@ -959,8 +963,7 @@ tsg_status small_spgemm(tsg_ctx *ctx, tsg_op op, const tsg_csr *A, const tsg_csr
     };
     const bool validate = ctx->opts.validate != 0;
     unsigned long long *sstat = reinterpret_cast<unsigned long long *>(ctx->dstat + ST_SMALL);
-    cudaError_t e = cudaMemsetAsync(ctx->dflags, 0, sizeof(int) * FLAG_COUNT, ctx->stream);
-    if (e == cudaSuccess) e = cudaMemsetAsync(ctx->dstat, 0, sizeof(long long) * ST_SLOTS, ctx->stream);
+    cudaError_t e = cudaMemsetAsync(ctx->dstat, 0, sizeof(long long) * ST_SLOTS, ctx->stream);   // flags too
     if (e != cudaSuccess) return cuda_fail(e);
     P.op = op; P.m = A->m; P.k = A->n; P.nnzA = A->nnz;
     tsg_status r = stage_into_plan(ctx, pool, P, A, validate, false, P.rpA, P.colA, P.valA, P.valA_buf);
@@ -979,21 +982,24 @@ tsg_status small_spgemm(tsg_ctx *ctx, tsg_op op, const tsg_csr *A, const tsg_csr
     const int bits = ctx->opts.out_rowptr_bits ? ctx->opts.out_rowptr_bits : 32;
     // buffers of `cap` entries, the fill at `rowptr` (kept: rows counted
     // against it), the caller's row pointer for device output, the wait
-    auto fill = [&](const long long *rowptr, long long cap, bool kept) -> tsg_status {
+    auto fill = [&](const long long *rowptr, long long cap, bool kept, bool one_round) -> tsg_status {
         col = pool.alloc_n<int>(cap);
         val = pool.alloc_n<double>(cap);
-        if (!col || !val) return fail(TSG_ERR_OOM, "device pool allocation failed for C (%lld entries)", cap);
+        if (dev_out && !rp_dev) rp_dev = pool.alloc((size_t)(P.m + 1) * (bits == 64 ? 8 : 4));
+        if (!col || !val || (dev_out && !rp_dev))
+            return fail(TSG_ERR_OOM, "device pool allocation failed for C (%lld entries)", cap);
         P.wait_values(ctx->stream);
+        // the fill writes the caller's row pointer too (device output)
         cudaError_t fe = small_fill(pool, P.rpA, P.colA, P.valA, P.k, P.rpB, P.colB, P.valB, P.n, P.m, rowptr, cap,
-                                    col, val, ctx->dflags, kept ? sstat : nullptr);
-        if (fe == cudaSuccess && dev_out && !rp_dev) fe = output_rowptr(ctx, pool, P.m, bits, rowptr, rp_dev);
+                                    col, val, ctx->dflags, kept ? sstat : nullptr, dev_out ? rp_dev : nullptr, bits,
+                                    one_round);
         if (fe != cudaSuccess) return fail(cuda_status(fe), "small path: %s", cudaGetErrorString(fe));
         return host_wait(ctx, &P.nsync);
     };
     const long long *rowptr = nullptr;   // C's row pointer: the kept one, or this call's scan
     long long nnzC = 0;
     if (seen && seen->rowptr) {
-        r = fill(seen->rowptr, seen->nnzc, true);
+        r = fill(seen->rowptr, seen->nnzc, true, seen->one_round);
         if (r) return give_up(r);
         if (ctx->hstat[ST_SMALL] == 0) {
             rowptr = seen->rowptr;
@@ -1002,7 +1008,7 @@ tsg_status small_spgemm(tsg_ctx *ctx, tsg_op op, const tsg_csr *A, const tsg_csr
             drop_cv();
             pool.free(rp_dev);
             rp_dev = nullptr;
-            e = cudaMemsetAsync(ctx->dstat + ST_SMALL, 0, 2 * sizeof(long long), ctx->stream);
+            e = cudaMemsetAsync(ctx->dstat + ST_SMALL, 0, 3 * sizeof(long long), ctx->stream);
             if (e != cudaSuccess) return cuda_fail(e);
         }
     }
@@ -1024,7 +1030,7 @@ tsg_status small_spgemm(tsg_ctx *ctx, tsg_op op, const tsg_csr *A, const tsg_csr
             cap = ctx->hstat[ST_NNZC];
         }
         for (int pass = 0;; ++pass) {
-            r = fill(P.rowptrC, cap, false);
+            r = fill(P.rowptrC, cap, false, false);
             if (r) return give_up(r);
             if (ctx->hstat[ST_SMALL] > 0) return not_small();
             if (ctx->hstat[ST_NNZC] <= cap || pass > 0) break;
@@ -1036,6 +1042,8 @@ tsg_status small_spgemm(tsg_ctx *ctx, tsg_op op, const tsg_csr *A, const tsg_csr
     }
     const long long products = ctx->hstat[ST_SMALL + 1];
     key.nnzc = nnzC;
+    // this call's rows all fit one round (from the count pass; a kept shape keeps its flag)
+    key.one_round = rowptr == P.rowptrC ? ctx->hstat[ST_SMALL + 2] == 0 : seen->one_round;
     seen = small_shape_record(ctx, key);
     if (rowptr == P.rowptrC) {   // kept for the shape's next call (when memory allows)
         if (!seen->rowptr) seen->rowptr = pool.alloc_n<long long>((long long)P.m + 1);
@@ -1116,6 +1124,15 @@ int64_t tsg_pinned_cache_cap(void) { return (int64_t)pinned_cap(); }
 
 void *tsg_get_stream(tsg_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
 
+tsg_status tsg_stream_wait(tsg_ctx *ctx, void *stream)
+{
+    if (!ctx) return fail(TSG_ERR_INVALID_ARG, "ctx is NULL");
+    CUDA_OK(cudaSetDevice(ctx->device));
+    CUDA_OK(cudaEventRecord(ctx->ext_ev, static_cast<cudaStream_t>(stream)));
+    CUDA_OK(cudaStreamWaitEvent(ctx->stream, ctx->ext_ev, 0));
+    return TSG_OK;
+}
+
 tsg_status tsg_inject_alloc_failure(int32_t kind, int64_t countdown)
 {
     if (kind != 0 && kind != 1) return fail(TSG_ERR_INVALID_ARG, "kind must be 0 (device pool) or 1 (pinned host)");
@@ -1193,7 +1210,8 @@ tsg_status tsg_create(tsg_ctx **out, int device, const tsg_opts *opts)
         cudaEventCreateWithFlags(&c->cfork, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->vals_ev, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->cols_ev, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&c->copy_done, cudaEventDisableTiming) != cudaSuccess)
+        cudaEventCreateWithFlags(&c->copy_done, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ext_ev, cudaEventDisableTiming) != cudaSuccess)
         return cleanup(fail(TSG_ERR_CUDA, "cudaEventCreate failed"));
     cudaMemPoolProps props{};
     props.allocType = cudaMemAllocationTypePinned;
@@ -1204,10 +1222,12 @@ tsg_status tsg_create(tsg_ctx **out, int device, const tsg_opts *opts)
         return cleanup(fail(TSG_ERR_CUDA, "cudaMemPoolCreate failed"));
     unsigned long long thr = ~0ull;
     cudaMemPoolSetAttribute(c->pool, cudaMemPoolAttrReleaseThreshold, &thr);
-    if (cudaMalloc(&c->dflags, sizeof(int) * FLAG_COUNT) != cudaSuccess ||
-        cudaMalloc(&c->dstat, sizeof(long long) * ST_SLOTS) != cudaSuccess ||
+    if (cudaMalloc(&c->dstat, sizeof(long long) * ST_SLOTS) != cudaSuccess ||
         cudaMallocHost(&c->hstat, sizeof(long long) * ST_SLOTS) != cudaSuccess)
         return cleanup(fail(TSG_ERR_OOM, "context buffers"));
+    c->dflags = reinterpret_cast<int *>(c->dstat + ST_HFLAGS);   // the flags sit behind the statistics
+    if (cudaMemset(c->dstat, 0, sizeof(long long) * ST_SLOTS) != cudaSuccess)
+        return cleanup(fail(TSG_ERR_CUDA, "context buffers"));
     for (auto &e : c->ev)
         if (cudaEventCreate(&e) != cudaSuccess) return cleanup(fail(TSG_ERR_CUDA, "cudaEventCreate failed"));
     cudaError_t e = tiles_init_attributes();
@@ -1230,10 +1250,9 @@ tsg_status tsg_destroy(tsg_ctx *c)
     if (c->join) cudaEventDestroy(c->join);
     if (c->side) { cudaStreamSynchronize(c->side); cudaStreamDestroy(c->side); }
     if (c->copy) { cudaStreamSynchronize(c->copy); cudaStreamDestroy(c->copy); }
-    for (cudaEvent_t e : {c->cfork, c->vals_ev, c->cols_ev, c->copy_done}) if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : {c->cfork, c->vals_ev, c->cols_ev, c->copy_done, c->ext_ev}) if (e) cudaEventDestroy(e);
     for (auto &sh : c->small_shapes) if (sh.rowptr) cudaFreeAsync(sh.rowptr, c->stream);
     if (c->stream) cudaStreamSynchronize(c->stream);
-    if (c->dflags) cudaFree(c->dflags);
     if (c->dstat) cudaFree(c->dstat);
     if (c->hstat) cudaFreeHost(c->hstat);
     if (c->pool) cudaMemPoolDestroy(c->pool);
@@ -1583,8 +1602,7 @@ struct TilesOwner {
 
 void reset_dev_state(tsg_ctx *ctx)
 {
-    cudaMemsetAsync(ctx->dflags, 0, sizeof(int) * FLAG_COUNT, ctx->stream);
-    cudaMemsetAsync(ctx->dstat, 0, sizeof(long long) * ST_SLOTS, ctx->stream);
+    cudaMemsetAsync(ctx->dstat, 0, sizeof(long long) * ST_SLOTS, ctx->stream);   // the flags inside it too
 }
 
 __global__ void k_widen_i32(const int *in, long long *out, long long n)

@@ -179,10 +179,14 @@ inline int ceil_div_i(long long a, long long b) { return (int)((a + b - 1) / b);
 // The small-product path (tsg_small.cu): rows of A that meet at most
 // SMALL_MAX_PRODUCTS entries of B, one warp per row of C.  small_count
 // writes each row's entry count (0 for rows over the limit) and adds the
-// rows over the limit to stat[0], the products to stat[1]; small_fill
+// rows over the limit to stat[0], the products to stat[1], and sets stat[2]
+// when a row does not fit one warp round (32 products); small_fill
 // writes C's columns and values at rowptrC (nothing when rowptrC[m] > cap);
 // with `kept` non-null rowptrC is a row pointer kept from an earlier call:
-// rows that do not match it add 1 to kept[0] (products to kept[1]).
+// rows that do not match it add 1 to kept[0] (products to kept[1]);
+// rp_out (optional) gets rowptrC as the caller's int32 or int64 row pointer;
+// one_round (with `kept`): a variant without shared memory for shapes
+// whose rows all fit one round (a row that does not counts in kept[0]).
 // ka = A's columns (= B's rows), nb = B's columns.
 constexpr int SMALL_MAX_PRODUCTS = 128;
 cudaError_t small_count(Pool &pool, const long long *rpA, const int *colA, int ka, const long long *rpB,
@@ -190,7 +194,8 @@ cudaError_t small_count(Pool &pool, const long long *rpA, const int *colA, int k
 cudaError_t small_fill(Pool &pool, const long long *rpA, const int *colA, const double *valA, int ka,
                        const long long *rpB, const int *colB, const double *valB, int nb, int m,
                        const long long *rowptrC, long long cap, int *colC, double *valC, int *flags,
-                       unsigned long long *kept = nullptr);
+                       unsigned long long *kept = nullptr, void *rp_out = nullptr, int rp_bits = 32,
+                       bool one_round = false);
 
 // One instance of a batched product, as the pack/unpack kernels see it.
 struct PackDesc {

@@ -176,19 +176,21 @@ k_small_count(const long long *__restrict__ rpA, const int *__restrict__ colA, i
         rowcnt[r] = over ? 0 : cnt;
         if (over) atomicAdd(stat, 1ull);
         else if (P) atomicAdd(stat + 1, (unsigned long long)P);
+        // stat[2]: a row that does not fit one round (more than 32 products or A entries)
+        if (!over && (P > 32 || a1 - a0 > 32) && stat[2] == 0) atomicMax(stat + 2, 1ull);
     }
 }
 
-__global__ void __launch_bounds__(SH_WARPS * 32)
+// ONE: every row is expected to fit one round (a kept shape whose rows all
+// did): no hash tables, so no shared memory and more warps per SM; a row
+// that does not fit is reported through `kept` like a changed row.
+template <bool ONE>
+__global__ void __launch_bounds__(SH_WARPS * 32, ONE ? 8 : 1)
 k_small_fill(const long long *__restrict__ rpA, const int *__restrict__ colA, const double *__restrict__ valA, int ka,
              const long long *__restrict__ rpB, const int *__restrict__ colB, const double *__restrict__ valB, int nb,
              int m, const long long *__restrict__ rowptrC, long long cap, int *colC, double *valC, int *flags,
-             unsigned long long *kept)
+             unsigned long long *kept, void *rp_out, int rp_bits)
 {
-    __shared__ int s_key[SH_WARPS][SH_CAP];
-    __shared__ double s_val[SH_WARPS][SH_CAP];
-    __shared__ int s_ck[SH_WARPS][SMALL_MAX_PRODUCTS];
-    __shared__ double s_cv[SH_WARPS][SMALL_MAX_PRODUCTS];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int r = blockIdx.x * SH_WARPS + warp;
     if (r >= m) return;
@@ -196,6 +198,15 @@ k_small_fill(const long long *__restrict__ rpA, const int *__restrict__ colA, co
     // C larger than the buffers: nothing is written (the caller sees nnzC
     // and runs this pass again into buffers of that size)
     if (rowptrC[m] > cap) return;
+    if (rp_out && lane == 0) {   // the caller's row pointer, in its type
+        if (rp_bits == 64) {
+            static_cast<long long *>(rp_out)[r] = Rb;
+            if (r == m - 1) static_cast<long long *>(rp_out)[m] = Re;
+        } else {
+            static_cast<int *>(rp_out)[r] = (int)Rb;
+            if (r == m - 1) static_cast<int *>(rp_out)[m] = (int)Re;
+        }
+    }
     const long long a0 = rpA[r], a1 = rpA[r + 1];
     if (a1 - a0 <= 32) {
         const int na = (int)(a1 - a0);
@@ -257,6 +268,14 @@ k_small_fill(const long long *__restrict__ rpA, const int *__restrict__ colA, co
             return;
         }
     }
+    if constexpr (ONE) {
+        if (lane == 0) atomicAdd(kept, 1ull);   // not one round: the caller counts again
+        return;
+    } else {
+    __shared__ int s_key[SH_WARPS][SH_CAP];
+    __shared__ double s_val[SH_WARPS][SH_CAP];
+    __shared__ int s_ck[SH_WARPS][SMALL_MAX_PRODUCTS];
+    __shared__ double s_cv[SH_WARPS][SMALL_MAX_PRODUCTS];
     int *key = s_key[warp];
     double *val = s_val[warp];
     for (int t = lane; t < SH_CAP; t += 32) { key[t] = -1; val[t] = 0.0; }
@@ -335,6 +354,7 @@ k_small_fill(const long long *__restrict__ rpA, const int *__restrict__ colA, co
         colC[Rb + rank] = c;
         valC[Rb + rank] = cv[p];
     }
+    }
 }
 
 }  // namespace
@@ -352,11 +372,21 @@ cudaError_t small_count(Pool &pool, const long long *rpA, const int *colA, int k
 cudaError_t small_fill(Pool &pool, const long long *rpA, const int *colA, const double *valA, int ka,
                        const long long *rpB, const int *colB, const double *valB, int nb, int m,
                        const long long *rowptrC, long long cap, int *colC, double *valC, int *flags,
-                       unsigned long long *kept)
+                       unsigned long long *kept, void *rp_out, int rp_bits, bool one_round)
 {
-    if (m <= 0) return cudaSuccess;
-    k_small_fill<<<(unsigned)((m + SH_WARPS - 1) / SH_WARPS), SH_WARPS * 32, 0, pool.stream>>>(
-        rpA, colA, valA, ka, rpB, colB, valB, nb, m, rowptrC, cap, colC, valC, flags, kept);
+    if (m <= 0) {   // C's row pointer is the single 0
+        if (!rp_out) return cudaSuccess;
+        return cudaMemsetAsync(rp_out, 0, rp_bits == 64 ? 8 : 4, pool.stream);
+    }
+    const unsigned grid = (unsigned)((m + SH_WARPS - 1) / SH_WARPS);
+    if (one_round && kept)
+        k_small_fill<true><<<grid, SH_WARPS * 32, 0, pool.stream>>>(rpA, colA, valA, ka, rpB, colB, valB, nb, m,
+                                                                    rowptrC, cap, colC, valC, flags, kept, rp_out,
+                                                                    rp_bits);
+    else
+        k_small_fill<false><<<grid, SH_WARPS * 32, 0, pool.stream>>>(rpA, colA, valA, ka, rpB, colB, valB, nb, m,
+                                                                     rowptrC, cap, colC, valC, flags, kept, rp_out,
+                                                                     rp_bits);
     ::tsg::count_launch();
     return cudaGetLastError();
 }

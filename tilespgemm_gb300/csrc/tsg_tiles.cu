@@ -696,24 +696,25 @@ k_union_wide(typename KS::Params P, const int *wide_list, const int *wide_n, int
 
 // ---- preparation ----------------------------------------------------------
 
+// One launch: thread i <= m checks and copies row pointer i (clamped to
+// [0, nnz], int64); with `col` (validation on) the grid also strides over
+// the column indices, checking each against n.
 template <typename Tr>
-__global__ void k_prepare_rowptr(const Tr *__restrict__ rp, long long m, long long nnz, long long *out, int *flags)
+__global__ void k_prepare_rowptr(const Tr *__restrict__ rp, long long m, long long nnz, long long *out, int *flags,
+                                 const int *__restrict__ col, int n)
 {
-    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (i > m) return;
-    long long v = (long long)rp[i];
-    bool bad = (v < 0 || v > nnz) || (i == 0 && v != 0) || (i == m && v != nnz);
-    if (i < m && (long long)rp[i + 1] < v) bad = true;
-    if (bad) set_flag(flags, FLAG_BAD_INPUT);
-    out[i] = v < 0 ? 0 : (v > nnz ? nnz : v);
-}
-
-__global__ void k_check_cols(const int *__restrict__ col, long long nnz, int n, int *flags)
-{
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i <= m) {
+        const long long v = (long long)rp[i];
+        bool bad = (v < 0 || v > nnz) || (i == 0 && v != 0) || (i == m && v != nnz);
+        if (i < m && (long long)rp[i + 1] < v) bad = true;
+        if (bad) set_flag(flags, FLAG_BAD_INPUT);
+        out[i] = v < 0 ? 0 : (v > nnz ? nnz : v);
+    }
+    if (!col) return;
     bool bad = false;
-    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < nnz; q += (long long)gridDim.x * blockDim.x)
-        bad |= ((unsigned)col[q] >= (unsigned)n);
-    if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) set_flag(flags, FLAG_BAD_INPUT);
+    for (long long q = i; q < nnz; q += (long long)gridDim.x * blockDim.x) bad |= ((unsigned)col[q] >= (unsigned)n);
+    if (bad) set_flag(flags, FLAG_BAD_INPUT);
 }
 
 // ---- stable transpose (CSR of A^T), LSD radix sort of (column, position) --
@@ -917,10 +918,12 @@ cudaError_t prepare_csr(Pool &pool, const void *rp, int rp_bits, const int *col,
                         long long *rp_out, int *flags, bool check_cols)
 {
     cudaStream_t s = pool.stream;
-    unsigned g = (unsigned)((m + 1 + 255) / 256);
-    if (rp_bits == 64) { k_prepare_rowptr<long long><<<g, 256, 0, s>>>((const long long *)rp, m, nnz, rp_out, flags); ::tsg::count_launch(); }
-    else { k_prepare_rowptr<int><<<g, 256, 0, s>>>((const int *)rp, m, nnz, rp_out, flags); ::tsg::count_launch(); }
-    if (check_cols && nnz > 0) { k_check_cols<<<grid_for(nnz, 256), 256, 0, s>>>(col, nnz, n, flags); ::tsg::count_launch(); }
+    const int *cc = check_cols && nnz > 0 ? col : nullptr;
+    // threads for every row pointer, and up to one per column index
+    const unsigned g = std::max<unsigned>((unsigned)((m + 1 + 255) / 256), cc ? (unsigned)grid_for(nnz, 256) : 1u);
+    if (rp_bits == 64) k_prepare_rowptr<long long><<<g, 256, 0, s>>>((const long long *)rp, m, nnz, rp_out, flags, cc, n);
+    else k_prepare_rowptr<int><<<g, 256, 0, s>>>((const int *)rp, m, nnz, rp_out, flags, cc, n);
+    ::tsg::count_launch();
     return cudaGetLastError();
 }
 
