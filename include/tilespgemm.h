@@ -204,6 +204,18 @@ tsg_status tsg_check_bounded_wait(tsg_ctx *ctx, int64_t n, int32_t spin_limit);
  */
 tsg_status tsg_load_mtx(const char *path, tsg_csr *out, int32_t *is_symmetric);
 
+/* The same load with the data lines parsed on the device (no counterpart in
+ * the reference, whose mmio_allinone reads with fscanf): the file's bytes
+ * go up, one thread per line parses it, and the entries (mirrored for
+ * symmetric/hermitian files) are ordered into CSR on the device.  *A is a
+ * device CSR (int32 row pointers) equal to tsg_load_mtx's result, entry
+ * for entry; release it with tsg_csr_free(ctx, A).  Values the device does
+ * not convert exactly (more than 19 significant digits or beyond 2^53,
+ * decimal exponents outside [-22, 22], hex, inf, nan) and malformed lines
+ * are read by the host's line reader; files whose entries do not sit one
+ * per line are read by tsg_load_mtx and uploaded.  Errors as tsg_load_mtx. */
+tsg_status tsg_load_mtx_device(tsg_ctx *ctx, const char *path, tsg_csr *A, int32_t *is_symmetric);
+
 /* Write a host CSR (for example C) as a Matrix Market coordinate real
  * general file in the format of the reference's mm_write_mtx_crd
  * (mmio.h:780-850): 1-based "i j value" lines in CSR order, values as

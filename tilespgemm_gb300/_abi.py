@@ -109,6 +109,7 @@ SIGNATURES = {
     "tsg_stream_wait": (C.c_int, [C.c_void_p, C.c_void_p]),
     "tsg_measure_fp64_peak": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "tsg_load_mtx": (C.c_int, [C.c_char_p, C.POINTER(tsg_csr), C.POINTER(C.c_int32)]),
+    "tsg_load_mtx_device": (C.c_int, [C.c_void_p, C.c_char_p, C.POINTER(tsg_csr), C.POINTER(C.c_int32)]),
     "tsg_csr_free": (C.c_int, [C.c_void_p, C.POINTER(tsg_csr)]),
     "tsg_write_mtx": (C.c_int, [C.c_char_p, C.POINTER(tsg_csr), C.c_int32]),
     "tsg_spgemm": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(tsg_csr), C.POINTER(tsg_csr),

@@ -388,6 +388,14 @@ class Context:
         del keep_a, keep_b
         return OwnedCSR(self, c), (st.as_dict() if st is not None else None)
 
+    def load_mtx_device(self, path: str) -> tuple[OwnedCSR, bool]:
+        """Matrix Market file -> device CSR, the data lines parsed on the GPU
+        (tsg_load_mtx_device; the same matrix as load_mtx)."""
+        s = _abi.tsg_csr()
+        sym = C.c_int32(0)
+        check(lib().tsg_load_mtx_device(self.handle, str(path).encode(), C.byref(s), C.byref(sym)))
+        return OwnedCSR(self, s), bool(sym.value)
+
     def spgemm(self, A: CSR, B: CSR | None = None, op: str = "AA", stats: bool = False):
         """C = op(A, B) as a host CSR (numpy).  op: "AA", "AAT" or "AB"."""
         oc, st = self.spgemm_raw(A, B, op, out="host", stats=stats)

@@ -10,6 +10,7 @@
 // one stream.
 #include "tilespgemm.h"
 #include "tsg_internal.cuh"
+#include "tsg_mtx.h"
 #include "tsg_numeric.cuh"
 
 #include <algorithm>
@@ -23,6 +24,7 @@
 #include <unordered_map>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <unistd.h>
 #include <vector>
 
@@ -45,6 +47,21 @@ cudaError_t aux_rows_increasing(Pool &pool, const long long *rp, const int *col,
 cudaError_t aux_copy_scalars(Pool &pool, const long long *a, long long *da, const int *b, long long *db,
                              const int *c, long long *dc);
 cudaError_t aux_rowptr_narrow(Pool &pool, const long long *in, int *out, long long n);
+// the device Matrix Market reader (tsg_mtx_dev.cu)
+cudaError_t mtx_lines(Pool &pool, const char *text, long long n, long long *&ends, long long &lines, int *flags);
+cudaError_t mtx_parse(Pool &pool, const char *text, const long long *ends, long long lines, int kind, long long M,
+                      long long N, unsigned char *st, int *lri, int *lci, double *lvv);
+cudaError_t mtx_number_entries(Pool &pool, const unsigned char *st, long long lines, long long *tpos, int *flags);
+cudaError_t mtx_take(Pool &pool, const unsigned char *st, const long long *tpos, long long lines, long long NZ,
+                     long long M, bool symm, const int *lri, const int *lci, const double *lvv, int *ri, int *ci,
+                     double *vv, unsigned long long *hn, long long *ht, long long *hl, int *bad);
+cudaError_t mtx_patch(Pool &pool, long long n, const long long *ht, const int *hi, const int *hj, const double *hv,
+                      int *ri, int *ci, double *vv);
+cudaError_t mtx_emit(Pool &pool, const int *ri, const int *ci, const double *vv, long long NZ, bool symm, int *cnt,
+                     long long *eoff, int *flags);
+cudaError_t mtx_emit_fill(Pool &pool, const int *ri, const int *ci, const double *vv, long long NZ, bool symm,
+                          const long long *eoff, int *key, int *col, double *val);
+cudaError_t gather_i32(Pool &pool, const int *perm, const int *src, int *dst, long long n);
 cudaError_t tiles_from_csr_c(Pool &pool, int m, int blkm, long long numblk, const long long *crp, const int *ccol,
                              const uint16_t *cmask, const long long *rowptr, const int *col, const double *val,
                              long long *nnzb, uint8_t *ptr, uint8_t *lcol, double *tval, int *flags);
@@ -1548,6 +1565,186 @@ tsg_status tsg_csr_to_device(tsg_ctx *ctx, const tsg_csr *H, tsg_csr *D)
     o->blocks = {{rp, 0}, {col, 0}, {val, 0}};
     D->m = H->m; D->n = H->n; D->nnz = H->nnz; D->rowptr_bits = H->rowptr_bits; D->where = TSG_MEM_DEVICE;
     D->row_ptr = rp; D->col = col; D->val = val; D->owner = o;
+    return TSG_OK;
+}
+
+// Matrix Market file -> CSR on the device, the data lines parsed there
+// (tsg_mtx_dev.cu); the result equals tsg_load_mtx's, uploaded.
+tsg_status tsg_load_mtx_device(tsg_ctx *ctx, const char *path, tsg_csr *A, int32_t *is_symmetric)
+{
+    if (!ctx || !path || !A) return fail(TSG_ERR_INVALID_ARG, "ctx/path/A is NULL");
+    memset(A, 0, sizeof(*A));
+    CUDA_OK(cudaSetDevice(ctx->device));
+    std::string text;
+    if (!mtx_read_file(path, text)) return fail(TSG_ERR_BAD_MTX, "could not open the Matrix Market file");
+    MtxHeader h;
+    tsg_status r = mtx_header(text, h);
+    if (r) return r;
+    // files whose entries do not sit one per line: the host loader, uploaded
+    auto host_path = [&]() -> tsg_status {
+        tsg_csr H;
+        tsg_status rh = tsg_load_mtx(path, &H, is_symmetric);
+        if (rh) return rh;
+        rh = tsg_csr_to_device(ctx, &H, A);
+        tsg_csr_free(nullptr, &H);
+        return rh;
+    };
+    if (!h.lines) return host_path();
+    Pool pool{ctx->pool, ctx->stream};
+    std::vector<void *> tmp;   // device scratch, freed on every return
+    auto dalloc = [&](size_t bytes) -> void * {
+        void *p = pool.alloc(bytes);
+        if (p) tmp.push_back(p);
+        return p;
+    };
+    auto release = [&]() {
+        for (void *p : tmp) pool.free(p);
+        tmp.clear();
+        cudaStreamSynchronize(ctx->stream);
+        cudaGetLastError();
+    };
+    auto cuda_fail = [&](cudaError_t e) {
+        release();
+        return fail(e == cudaErrorMemoryAllocation ? TSG_ERR_OOM : cuda_status(e), "device Matrix Market load: %s",
+                    cudaGetErrorString(e));
+    };
+    auto mtx_fail = [&](const char *msg) { release(); return fail(TSG_ERR_BAD_MTX, "%s", msg); };
+    const long long M = h.M, N = h.N, NZ = h.NZ;
+    const char *data = text.data() + h.data;
+    const long long nb = (long long)(text.size() - h.data);
+    cudaError_t e = cudaMemsetAsync(ctx->dstat, 0, sizeof(long long) * ST_SLOTS, ctx->stream);   // flags too
+    char *dtext = static_cast<char *>(dalloc((size_t)((nb + 15) & ~15ll)));
+    if (!dtext) return cuda_fail(cudaErrorMemoryAllocation);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dtext, data, (size_t)nb, cudaMemcpyHostToDevice, ctx->stream);
+    long long *ends = nullptr, lines = 0;
+    if (e == cudaSuccess) e = mtx_lines(pool, dtext, nb, ends, lines, ctx->dflags);
+    if (ends) tmp.push_back(ends);
+    if (e != cudaSuccess) return cuda_fail(e);
+    // per line: what it holds; the entries' numbers in file order
+    const long long L1 = std::max(lines, 1ll);
+    unsigned char *st = static_cast<unsigned char *>(dalloc((size_t)L1));
+    int *lri = static_cast<int *>(dalloc(sizeof(int) * (size_t)L1));
+    int *lci = static_cast<int *>(dalloc(sizeof(int) * (size_t)L1));
+    double *lvv = static_cast<double *>(dalloc(sizeof(double) * (size_t)L1));
+    long long *tpos = static_cast<long long *>(dalloc(sizeof(long long) * (size_t)(lines + 1)));
+    const long long NZ1 = std::max(NZ, 1ll);
+    int *ri = static_cast<int *>(dalloc(sizeof(int) * (size_t)NZ1));
+    int *ci = static_cast<int *>(dalloc(sizeof(int) * (size_t)NZ1));
+    double *vv = static_cast<double *>(dalloc(sizeof(double) * (size_t)NZ1));
+    unsigned long long *hn = static_cast<unsigned long long *>(dalloc(sizeof(unsigned long long) + 2 * sizeof(int)));
+    long long *ht = static_cast<long long *>(dalloc(sizeof(long long) * (size_t)L1));
+    long long *hl = static_cast<long long *>(dalloc(sizeof(long long) * (size_t)L1));
+    if (!st || !lri || !lci || !lvv || !tpos || !ri || !ci || !vv || !hn || !ht || !hl)
+        return cuda_fail(cudaErrorMemoryAllocation);
+    int *bad = reinterpret_cast<int *>(hn + 1);
+    long long total = 0;
+    e = cudaMemsetAsync(hn, 0, sizeof(unsigned long long) + 2 * sizeof(int), ctx->stream);
+    if (e == cudaSuccess && lines > 0) e = mtx_parse(pool, dtext, ends, lines, h.kind, M, N, st, lri, lci, lvv);
+    if (e == cudaSuccess && lines > 0) e = mtx_number_entries(pool, st, lines, tpos, ctx->dflags);
+    if (e == cudaSuccess && lines > 0)
+        e = mtx_take(pool, st, tpos, lines, NZ, M, h.symm, lri, lci, lvv, ri, ci, vv, hn, ht, hl, bad);
+    unsigned long long hcount = 0;
+    int hbad[2] = {0, 0};
+    if (e == cudaSuccess && lines > 0) e = cudaMemcpyAsync(&total, tpos + lines, sizeof(long long), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&hcount, hn, sizeof(hcount), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hbad, bad, sizeof(hbad), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(e);
+    // lines the device left: the host loader's line reader, several threads
+    if (hcount > 0) {
+        std::vector<long long> hts(hcount), hls(hcount), endv((size_t)lines);
+        e = cudaMemcpyAsync(hts.data(), ht, sizeof(long long) * hcount, cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(hls.data(), hl, sizeof(long long) * hcount, cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(endv.data(), ends, sizeof(long long) * (size_t)lines, cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) return cuda_fail(e);
+        std::vector<int> hi(hcount), hj(hcount);
+        std::vector<double> hv(hcount);
+        std::atomic<int> malformed{0}, outside{0}, mirror{0};
+        auto work = [&](size_t a, size_t b) {
+            for (size_t k = a; k < b; ++k) {
+                const long long L = hls[k];
+                const char *q = data + (L == 0 ? 0 : endv[(size_t)L - 1] + 1), *qe = data + endv[(size_t)L];
+                while (q < qe && (*q == ' ' || *q == '\t' || *q == '\r' || *q == '\v' || *q == '\f')) ++q;
+                long long i = 0, j = 0;
+                double v = 1.0;
+                if (!mtx_line(q, qe, h.kind, i, j, v)) { malformed = 1; continue; }
+                if (i < 1 || i > M || j < 1 || j > N) { outside = 1; continue; }
+                if (h.symm && i != j && j - 1 >= M) mirror = 1;
+                hi[k] = (int)(i - 1);
+                hj[k] = (int)(j - 1);
+                hv[k] = v;
+            }
+        };
+        const size_t nt = std::min<size_t>(std::max(1u, std::thread::hardware_concurrency()),
+                                           std::max<size_t>(1, hcount / 65536));
+        std::vector<std::thread> th;
+        for (size_t k = 1; k < nt; ++k) th.emplace_back(work, hcount * k / nt, hcount * (k + 1) / nt);
+        work(0, hcount / nt);
+        for (auto &t : th) t.join();
+        if (malformed) { release(); return host_path(); }
+        if (outside) hbad[0] = 1;
+        if (mirror) hbad[1] = 1;
+        long long *dht = static_cast<long long *>(dalloc(sizeof(long long) * hcount));
+        int *dhi = static_cast<int *>(dalloc(sizeof(int) * hcount));
+        int *dhj = static_cast<int *>(dalloc(sizeof(int) * hcount));
+        double *dhv = static_cast<double *>(dalloc(sizeof(double) * hcount));
+        if (!dht || !dhi || !dhj || !dhv) return cuda_fail(cudaErrorMemoryAllocation);
+        e = cudaMemcpyAsync(dht, hts.data(), sizeof(long long) * hcount, cudaMemcpyHostToDevice, ctx->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(dhi, hi.data(), sizeof(int) * hcount, cudaMemcpyHostToDevice, ctx->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(dhj, hj.data(), sizeof(int) * hcount, cudaMemcpyHostToDevice, ctx->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(dhv, hv.data(), sizeof(double) * hcount, cudaMemcpyHostToDevice, ctx->stream);
+        if (e == cudaSuccess) e = mtx_patch(pool, (long long)hcount, dht, dhi, dhj, dhv, ri, ci, vv);
+        if (e != cudaSuccess) return cuda_fail(e);
+    }
+    // the host loader's checks, in its order
+    if (hbad[0]) return mtx_fail("entry index outside the matrix");
+    if (total < NZ) return mtx_fail("truncated data line");
+    if (hbad[1]) return mtx_fail("symmetric entry mirrored outside the matrix");
+    // the entries and their mirrors in file order -> stable sort by row
+    int *cnt = static_cast<int *>(dalloc(sizeof(int) * (size_t)NZ1));
+    long long *eoff = static_cast<long long *>(dalloc(sizeof(long long) * (size_t)(NZ + 1)));
+    if (!cnt || !eoff) return cuda_fail(cudaErrorMemoryAllocation);
+    long long E = 0;
+    e = mtx_emit(pool, ri, ci, vv, NZ, h.symm, cnt, eoff, ctx->dflags);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&E, eoff + NZ, sizeof(long long), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(e);
+    if (E > INT32_MAX) { release(); return fail(TSG_ERR_NOT_SUPPORTED, "more than 2^31-1 entries after mirroring"); }
+    const long long E1 = std::max(E, 1ll);
+    int *key = static_cast<int *>(dalloc(sizeof(int) * (size_t)E1));
+    int *ecol = static_cast<int *>(dalloc(sizeof(int) * (size_t)E1));
+    double *eval = static_cast<double *>(dalloc(sizeof(double) * (size_t)E1));
+    long long *rp1 = static_cast<long long *>(dalloc(2 * sizeof(long long)));
+    long long *tp = static_cast<long long *>(dalloc(sizeof(long long) * (size_t)(M + 1)));
+    int *tcol = static_cast<int *>(dalloc(sizeof(int) * (size_t)E1));
+    int *perm = static_cast<int *>(dalloc(sizeof(int) * (size_t)E1));
+    int *rp32 = static_cast<int *>(pool.alloc(sizeof(int) * (size_t)(M + 1)));
+    int *col = static_cast<int *>(pool.alloc(sizeof(int) * (size_t)E1));
+    double *val = static_cast<double *>(pool.alloc(sizeof(double) * (size_t)E1));
+    auto drop_out = [&]() { pool.free(rp32); pool.free(col); pool.free(val); };
+    if (!key || !ecol || !eval || !rp1 || !tp || !tcol || !perm || !rp32 || !col || !val) {
+        drop_out();
+        return cuda_fail(cudaErrorMemoryAllocation);
+    }
+    const long long rp1h[2] = {0, E};
+    e = mtx_emit_fill(pool, ri, ci, vv, NZ, h.symm, eoff, key, ecol, eval);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(rp1, rp1h, sizeof(rp1h), cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = csr_transpose(pool, rp1, key, eval, 1, (int)M, E, tp, tcol, val, perm, ctx->dflags);
+    if (e == cudaSuccess) e = gather_i32(pool, perm, ecol, col, E);
+    if (e == cudaSuccess) e = aux_rowptr_narrow(pool, tp, rp32, M + 1);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) { drop_out(); return cuda_fail(e); }
+    r = host_wait(ctx, nullptr);   // the scans' bounded waits
+    if (r) { drop_out(); release(); return r; }
+    release();
+    OutOwner *o = new OutOwner();
+    o->ctx = ctx;
+    o->where = TSG_MEM_DEVICE;
+    o->blocks = {{rp32, 0}, {col, 0}, {val, 0}};
+    A->m = (int32_t)M; A->n = (int32_t)N; A->nnz = E; A->rowptr_bits = 32; A->where = TSG_MEM_DEVICE;
+    A->row_ptr = rp32; A->col = col; A->val = val; A->owner = o;
+    if (is_symmetric) *is_symmetric = h.symm ? 1 : 0;
     return TSG_OK;
 }
 

@@ -40,6 +40,7 @@ namespace tsg {
 void set_last_error(const char *msg);
 void *make_malloc_owner(void *a, void *b, void *c);
 }
+#include "tsg_mtx.h"
 
 namespace {
 
@@ -98,6 +99,8 @@ tsg_status bad(const char *msg)
 }
 
 enum ValueKind { V_REAL, V_COMPLEX, V_INT, V_PATTERN };
+static_assert(V_REAL == tsg::MTX_REAL && V_COMPLEX == tsg::MTX_COMPLEX && V_INT == tsg::MTX_INTEGER &&
+              V_PATTERN == tsg::MTX_PATTERN, "value kinds");
 
 // The entries of the data lines in [p, end), one per line (blank lines
 // skipped), in file order, 0-based.  ok = false when a line is not exactly
@@ -112,6 +115,51 @@ struct LineRun {
 
 inline bool blank(char c) { return c == ' ' || c == '\t' || c == '\r' || c == '\v' || c == '\f'; }
 
+}  // namespace
+
+namespace tsg {
+
+// One data line [p, e) (no newline inside; the byte at e is not a digit):
+// false unless it is exactly one entry of the given value kind (i, j
+// 1-based as written; v: pattern 1.0, integer as (double)(int), complex the
+// real part).  Blank lines are the caller's.
+bool mtx_line(const char *p, const char *e, int kind, long long &i, long long &j, double &v)
+{
+    const char *q = p;
+    auto tok_long = [&](long long &x) {
+        while (q < e && blank(*q)) ++q;
+        if (q >= e) return false;
+        char *t = nullptr;
+        errno = 0;
+        x = strtoll(q, &t, 10);
+        if (t == q || errno || t > e) return false;
+        q = t;
+        return true;
+    };
+    auto tok_double = [&](double &x) {
+        while (q < e && blank(*q)) ++q;
+        if (q >= e) return false;
+        char *t = nullptr;
+        x = strtod(q, &t);
+        if (t == q || t > e) return false;
+        q = t;
+        return true;
+    };
+    i = j = 0;
+    v = 1.0;
+    double vim = 0.0;
+    bool good = tok_long(i) && tok_long(j);
+    if (good && kind == V_REAL) good = tok_double(v);
+    else if (good && kind == V_COMPLEX) good = tok_double(v) && tok_double(vim);
+    else if (good && kind == V_INT) { long long iv = 0; good = tok_long(iv); v = (double)(int)iv; }
+    while (good && q < e && blank(*q)) ++q;
+    return good && q == e;
+}
+
+}  // namespace tsg
+
+namespace {
+
 void parse_lines(const char *p, const char *end, ValueKind kind, long long M, long long N, LineRun &out)
 {
     // room for one entry per line, allocated once (threads growing vectors
@@ -124,35 +172,11 @@ void parse_lines(const char *p, const char *end, ValueKind kind, long long M, lo
         const char *e = (const char *)memchr(p, '\n', (size_t)(end - p));
         if (!e) e = end;
         const char *q = p;
-        auto tok_long = [&](long long &x) {
-            while (q < e && blank(*q)) ++q;
-            if (q >= e) return false;
-            char *t = nullptr;
-            errno = 0;
-            x = strtoll(q, &t, 10);
-            if (t == q || errno || t > e) return false;
-            q = t;
-            return true;
-        };
-        auto tok_double = [&](double &x) {
-            while (q < e && blank(*q)) ++q;
-            if (q >= e) return false;
-            char *t = nullptr;
-            x = strtod(q, &t);
-            if (t == q || t > e) return false;
-            q = t;
-            return true;
-        };
         while (q < e && blank(*q)) ++q;
         if (q < e) {
             long long i = 0, j = 0;
-            double v = 1.0, vim = 0.0;
-            bool good = tok_long(i) && tok_long(j);
-            if (good && kind == V_REAL) good = tok_double(v);
-            else if (good && kind == V_COMPLEX) good = tok_double(v) && tok_double(vim);
-            else if (good && kind == V_INT) { long long iv = 0; good = tok_long(iv); v = (double)(int)iv; }
-            while (good && q < e && blank(*q)) ++q;
-            if (!good || q != e) { out.ok = false; return; }
+            double v = 1.0;
+            if (!tsg::mtx_line(q, e, kind, i, j, v)) { out.ok = false; return; }
             if (i < 1 || i > M || j < 1 || j > N) {
                 if (out.first_bad < 0) out.first_bad = (long long)out.i.size();
                 i = j = 1;
@@ -219,17 +243,14 @@ bool parse_parallel(const char *p, const char *end, int nt, ValueKind kind, long
 
 }  // namespace
 
-extern "C" tsg_status tsg_load_mtx(const char *path, tsg_csr *out, int32_t *is_symmetric)
+namespace tsg {
+
+// The banner, comments and size line of a Matrix Market text (ending with
+// '\n'): sizes, value kind, symmetry; `cursor` = the offset just past the
+// size line's NZ, and, when the rest of that line is blank, `data` = the
+// offset of the first data line (lines = true).
+tsg_status mtx_header(const std::string &text, MtxHeader &h)
 {
-    if (!path || !out) {
-        tsg::set_last_error("path/out is NULL");
-        return TSG_ERR_INVALID_ARG;
-    }
-    memset(out, 0, sizeof(*out));
-    std::string text;
-    if (!read_file(path, text)) return bad("could not open the Matrix Market file");
-    // make sure strtod/strtoll stop at the end of the buffer
-    text.push_back('\n');
     const char *p = text.data(), *end = text.data() + text.size();
     // banner line
     const char *nl = (const char *)memchr(p, '\n', (size_t)(end - p));
@@ -244,8 +265,9 @@ extern "C" tsg_status tsg_load_mtx(const char *path, tsg_csr *out, int32_t *is_s
     if (crd != "coordinate") return bad("unsupported storage (not 'coordinate')");
     const bool is_real = type == "real", is_complex = type == "complex", is_int = type == "integer", is_pat = type == "pattern";
     if (!is_real && !is_complex && !is_int && !is_pat) return bad("unsupported data type");
-    const bool symm = (sym == "symmetric" || sym == "hermitian");
-    if (!symm && sym != "general" && sym != "skew-symmetric") return bad("unsupported symmetry");
+    h.symm = (sym == "symmetric" || sym == "hermitian");
+    if (!h.symm && sym != "general" && sym != "skew-symmetric") return bad("unsupported symmetry");
+    h.kind = is_real ? V_REAL : is_complex ? V_COMPLEX : is_int ? V_INT : V_PATTERN;
     p = nl ? nl + 1 : end;
     // skip comment lines, then blank lines, to the size line
     while (p < end && *p == '%') {
@@ -253,19 +275,50 @@ extern "C" tsg_status tsg_load_mtx(const char *path, tsg_csr *out, int32_t *is_s
         p = e ? e + 1 : end;
     }
     Cursor cur{p, end};
-    long long M = 0, N = 0, NZ = 0;
-    if (!cur.read_long(M) || !cur.read_long(N) || !cur.read_long(NZ)) return bad("bad size line");
-    if (M < 0 || N < 0 || NZ < 0 || M > INT32_MAX - 1 || N > INT32_MAX - 1 || NZ > INT32_MAX) return bad("sizes out of range");
-    std::vector<int> ri((size_t)NZ), ci((size_t)NZ);
-    std::vector<double> vv((size_t)NZ);
-    const ValueKind kind = is_real ? V_REAL : is_complex ? V_COMPLEX : is_int ? V_INT : V_PATTERN;
-    const int nt = NZ > 0 ? mtx_threads((size_t)(end - cur.p)) : 1;
-    tsg_status pst = TSG_OK;
-    // the rest of the size line must be blank for the line reader
+    if (!cur.read_long(h.M) || !cur.read_long(h.N) || !cur.read_long(h.NZ)) return bad("bad size line");
+    if (h.M < 0 || h.N < 0 || h.NZ < 0 || h.M > INT32_MAX - 1 || h.N > INT32_MAX - 1 || h.NZ > INT32_MAX)
+        return bad("sizes out of range");
+    h.cursor = (size_t)(cur.p - text.data());
+    // the rest of the size line must be blank for the line readers
     const char *dp = cur.p;
     while (dp < end && blank(*dp)) ++dp;
-    const bool lines_ok = dp < end && *dp == '\n';
-    if (nt > 1 && lines_ok && parse_parallel(dp + 1, end, nt, kind, M, N, NZ, ri, ci, vv, pst)) {
+    h.lines = dp < end && *dp == '\n';
+    h.data = h.lines ? (size_t)(dp + 1 - text.data()) : text.size();
+    return TSG_OK;
+}
+
+bool mtx_read_file(const char *path, std::string &out)
+{
+    if (!read_file(path, out)) return false;
+    out.push_back('\n');   // strtod/strtoll and the line readers stop at the end
+    return true;
+}
+
+}  // namespace tsg
+
+extern "C" tsg_status tsg_load_mtx(const char *path, tsg_csr *out, int32_t *is_symmetric)
+{
+    if (!path || !out) {
+        tsg::set_last_error("path/out is NULL");
+        return TSG_ERR_INVALID_ARG;
+    }
+    memset(out, 0, sizeof(*out));
+    std::string text;
+    if (!tsg::mtx_read_file(path, text)) return bad("could not open the Matrix Market file");
+    const char *end = text.data() + text.size();
+    tsg::MtxHeader h;
+    tsg_status hst = tsg::mtx_header(text, h);
+    if (hst != TSG_OK) return hst;
+    const long long M = h.M, N = h.N, NZ = h.NZ;
+    const bool symm = h.symm;
+    const ValueKind kind = (ValueKind)h.kind;
+    const bool is_real = kind == V_REAL, is_complex = kind == V_COMPLEX, is_int = kind == V_INT;
+    Cursor cur{text.data() + h.cursor, end};
+    std::vector<int> ri((size_t)NZ), ci((size_t)NZ);
+    std::vector<double> vv((size_t)NZ);
+    const int nt = NZ > 0 ? mtx_threads((size_t)(end - cur.p)) : 1;
+    tsg_status pst = TSG_OK;
+    if (nt > 1 && h.lines && parse_parallel(text.data() + h.data, end, nt, kind, M, N, NZ, ri, ci, vv, pst)) {
         if (pst != TSG_OK) return pst;
     } else for (long long t = 0; t < NZ; ++t) {
         long long i = 0, j = 0;
