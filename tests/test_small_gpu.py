@@ -146,6 +146,29 @@ def test_one_round_shape_then_longer_rows(built_lib):
                 assert st["n_syncs"] >= 2
 
 
+def test_wide_b_uses_long_sort_keys(sctx, ctx):
+    """B with more than 2^26 columns: the one-round sort keys (column, product
+    index) take 64 bits.  Columns drawn from a small shared pool spread over
+    80 M so that products meet; the result equals the tiled path's bit for
+    bit (both accumulate in A's order, then B's)."""
+    from tilespgemm_gb300.api import CSR
+    rng = np.random.default_rng(71)
+    pool = np.sort(rng.choice(80_000_000, size=300, replace=False))
+
+    def rows(m, n, per, choose):
+        rp = np.arange(0, m * per + 1, per, dtype=np.int64)
+        col = np.concatenate([np.sort(choose()) for _ in range(m)]).astype(np.int32)
+        return CSR(m, n, rp, col, rng.uniform(-1.0, 1.0, size=col.size))
+
+    A = rows(400, 1000, 4, lambda: rng.choice(1000, size=4, replace=False))
+    B = rows(1000, 80_000_000, 8, lambda: rng.choice(pool, size=8, replace=False))
+    C, st = sctx.spgemm(A, B, op="AB", stats=True)
+    assert st["small_path"] == 1
+    T = ctx.spgemm(A, B, op="AB")
+    _same(C, T)
+    assert C.nnz < 400 * 32   # products met
+
+
 def test_rows_over_the_limit_take_the_tiled_path(sctx):
     from tilespgemm_gb300 import matrices as M
     A = M.random_sparse(500, 500, 12, seed=40)      # 144 products per row

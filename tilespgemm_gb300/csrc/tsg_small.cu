@@ -113,6 +113,22 @@ __device__ __forceinline__ K warp_sort_up(K key, int lane)
     return key;
 }
 
+// One round's products sorted by (column, product index f = lane): lane
+// i gets the i-th smallest, its column, and the A and B values of the lane
+// that held it; live = false for the lanes past the products (c0 < 0).
+template <typename K>
+__device__ __forceinline__ void sort_products(int c0, double a, double bv, int lane, bool &live, int &col, double &sa,
+                                              double &sb)
+{
+    K key = c0 >= 0 ? (((K)(unsigned)c0 << 5) | (K)(unsigned)lane) : ~(K)0;
+    key = warp_sort_up(key, lane);
+    live = key != ~(K)0;
+    const int src = (int)(key & 31u);
+    col = (int)(key >> 5);
+    sa = __shfl_sync(0xffffffffu, a, src);
+    sb = __shfl_sync(0xffffffffu, bv, src);
+}
+
 __global__ void __launch_bounds__(SH_WARPS * 32)
 k_small_count(const long long *__restrict__ rpA, const int *__restrict__ colA, int ka,
               const long long *__restrict__ rpB, const int *__restrict__ colB, int nb, int m, int *rowcnt,
@@ -224,20 +240,21 @@ k_small_fill(const long long *__restrict__ rpA, const int *__restrict__ colA, co
             const int q = owner_lane(off, lane);
             const long long e = __shfl_sync(0xffffffffu, b.bs, q) + (lane - __shfl_sync(0xffffffffu, off, q));
             const double a = __shfl_sync(0xffffffffu, av, q);
-            unsigned long long key = ~0ull;
+            int c0 = -1;
             double bv = 0.0;
             if (lane < T) {
-                const int col = colB[e];
-                if ((unsigned)col < (unsigned)nb) {
-                    key = ((unsigned long long)(unsigned)col << 5) | (unsigned)lane;
+                const int cb = colB[e];
+                if ((unsigned)cb < (unsigned)nb) {
+                    c0 = cb;
                     bv = valB[e];
                 }
             }
-            key = warp_sort_up(key, lane);
-            const bool live = key != ~0ull;
-            const int src = (int)(key & 31u);
-            const int col = (int)(key >> 5);
-            const double sa = __shfl_sync(0xffffffffu, a, src), sb = __shfl_sync(0xffffffffu, bv, src);
+            // 32-bit keys when B's columns leave room for the 5 bits of f
+            bool live;
+            int col;
+            double sa, sb;
+            if (nb <= (1 << 26)) sort_products<unsigned>(c0, a, bv, lane, live, col, sa, sb);
+            else sort_products<unsigned long long>(c0, a, bv, lane, live, col, sa, sb);
             const int pcol = __shfl_up_sync(0xffffffffu, col, 1);
             const bool head = live && (lane == 0 || pcol != col);
             const unsigned heads = __ballot_sync(0xffffffffu, head);
