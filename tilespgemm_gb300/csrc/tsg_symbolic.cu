@@ -63,11 +63,17 @@ __device__ __forceinline__ void smask_or(unsigned short *m, int idx, unsigned bi
 }
 
 // slot of tile column j in C's tile-row: direct map over the row's window
-// when it is narrow, binary search otherwise; -1 if j is not one of its tiles
+// when it is narrow, binary search otherwise; -1 if j is not one of its
+// tiles.  The map holds, for every column of the window, its tile's slot or
+// 0xffff, so a mapped slot needs no check against the tile columns.
 __device__ __forceinline__ int c_slot(int j, int jbase, int span, const unsigned short *map, const int *scol, int S) {
     const unsigned off = (unsigned)(j - jbase);
     if (off >= (unsigned)span) return -1;
-    const int s = map ? (int)map[off] : lower_bound_i(scol, S, j);
+    if (map) {
+        const int s = (int)map[off];
+        return s < S ? s : -1;
+    }
+    const int s = lower_bound_i(scol, S, j);
     return (s < S && scol[s] == j) ? s : -1;
 }
 
