@@ -250,6 +250,31 @@ def test_invalid_inputs_are_reported(sctx):
     assert np.array_equal(C.val, [6.0, 6.0])
 
 
+def test_invalid_ab_operands_on_a_repeated_shape(sctx):
+    """A repeated A*B shape runs the fill alone on the operands as given and
+    validates them there: a column of B out of range in a row that A never
+    reaches, a B row pointer out of order, a column of A out of range --
+    each TSG_ERR_BAD_INPUT, as from the validation kernel -- and the
+    context stays exact."""
+    from tilespgemm_gb300 import TSGError
+    from tilespgemm_gb300.api import CSR
+    A = CSR(3, 3, np.array([0, 1, 2, 3]), np.array([0, 0, 1], np.int32), np.array([1.0, 2.0, 3.0]))
+    B = CSR(3, 4, np.array([0, 2, 3, 4]), np.array([0, 3, 1, 2], np.int32), np.array([1.0, 2.0, 3.0, 4.0]))
+    ref = O.spgemm(A, B)
+    for _ in range(2):
+        C = sctx.spgemm(A, B, op="AB")
+        assert np.array_equal(C.col, ref[1]) and np.array_equal(C.val, ref[2])
+    bad_b_col = CSR(3, 4, B.rowptr, np.array([0, 3, 1, 7], np.int32), B.val)      # row 2: A never reads it
+    bad_b_rp = CSR(3, 4, np.array([0, 3, 2, 4]), B.col, B.val)
+    bad_a_col = CSR(3, 3, A.rowptr, np.array([0, 5, 1], np.int32), A.val)
+    for a, b in ((A, bad_b_col), (A, bad_b_rp), (bad_a_col, B)):
+        with pytest.raises(TSGError) as e:
+            sctx.spgemm(a, b, op="AB")
+        assert e.value.status == 8
+    C = sctx.spgemm(A, B, op="AB")
+    assert np.array_equal(C.col, ref[1]) and np.array_equal(C.val, ref[2])
+
+
 def test_allocation_failures_are_reported(built_lib):
     """Every device-pool allocation of a small-path call, on a first call of
     the shape and on a repeated one, fails in turn: TSG_ERR_OOM, and the next

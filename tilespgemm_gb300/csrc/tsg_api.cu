@@ -927,6 +927,42 @@ SmallShape *small_shape_record(tsg_ctx *ctx, const SmallShape &k)
     return s;
 }
 
+// The small path's operands as the caller gave them: device arrays in
+// place, host arrays uploaded as they are (row pointers in their own type)
+// into buffers P owns.  Nothing is validated here.
+tsg_status small_raw_operands(tsg_ctx *ctx, Pool &pool, PlanData &P, bool aa, const tsg_csr *A, const tsg_csr *B,
+                              SmallOperands &o)
+{
+    auto view = [&](const tsg_csr *M, RowPtr &rp, const int *&col, const double *&val) -> tsg_status {
+        const void *r = M->row_ptr;
+        col = M->col;
+        val = M->val;
+        if (M->where == TSG_MEM_HOST) {
+            const size_t rpb = (size_t)(M->m + 1) * (M->rowptr_bits == 64 ? 8 : 4);
+            void *dr = P.own<char>(pool, (long long)rpb);
+            int *dc = P.own<int>(pool, M->nnz);
+            double *dv = P.own<double>(pool, M->nnz);
+            if (!dr || !dc || !dv) return fail(TSG_ERR_OOM, "device pool allocation failed for an operand");
+            CUDA_OK(cudaMemcpyAsync(dr, r, rpb, cudaMemcpyHostToDevice, ctx->stream));
+            if (M->nnz > 0) {
+                CUDA_OK(cudaMemcpyAsync(dc, col, sizeof(int) * (size_t)M->nnz, cudaMemcpyHostToDevice, ctx->stream));
+                CUDA_OK(cudaMemcpyAsync(dv, val, sizeof(double) * (size_t)M->nnz, cudaMemcpyHostToDevice, ctx->stream));
+            }
+            r = dr; col = dc; val = dv;
+        }
+        if (M->rowptr_bits == 64) rp.p64 = static_cast<const long long *>(r);
+        else rp.p32 = static_cast<const int *>(r);
+        return TSG_OK;
+    };
+    tsg_status st = view(A, o.rpA, o.colA, o.valA);
+    if (st) return st;
+    if (aa) { o.rpB = o.rpA; o.colB = o.colA; o.valB = o.valA; }
+    else if ((st = view(B, o.rpB, o.colB, o.valB))) return st;
+    o.m = A->m; o.ka = A->n; o.kb = B->m; o.nb = B->n; o.nnzA = A->nnz; o.nnzB = B->nnz;
+    o.b_is_a = aa;
+    return TSG_OK;
+}
+
 // tsg_spgemm for products whose every row of A meets at most
 // SMALL_MAX_PRODUCTS entries of B (A*B and A*A, operands of at most
 // SMALL_NNZ_MAX entries): one warp per row of C (tsg_small.cu).  A shape's
@@ -983,23 +1019,16 @@ tsg_status small_spgemm(tsg_ctx *ctx, tsg_op op, const tsg_csr *A, const tsg_csr
     cudaError_t e = cudaMemsetAsync(ctx->dstat, 0, sizeof(long long) * ST_SLOTS, ctx->stream);   // flags too
     if (e != cudaSuccess) return cuda_fail(e);
     P.op = op; P.m = A->m; P.k = A->n; P.nnzA = A->nnz;
-    tsg_status r = stage_into_plan(ctx, pool, P, A, validate, false, P.rpA, P.colA, P.valA, P.valA_buf);
-    if (r) return give_up(r);
-    if (op == TSG_OP_AB) {
-        P.n = B->n; P.nnzB = B->nnz;
-        r = stage_into_plan(ctx, pool, P, B, validate, false, P.rpB, P.colB, P.valB, P.valB_buf);
-        if (r) return give_up(r);
-    } else {
-        P.n = A->n; P.nnzB = A->nnz;
-        P.rpB = P.rpA; P.colB = P.colA; P.valB = P.valA;
-    }
+    P.n = Bm->n; P.nnzB = Bm->nnz;
+    tsg_status r = TSG_OK;
     const bool dev_out = C->where == TSG_MEM_DEVICE;
     // C's row pointer type: 32-bit unless asked otherwise (C stays far below
     // 2^31 entries on this path: at most SMALL_MAX_PRODUCTS per entry of A)
     const int bits = ctx->opts.out_rowptr_bits ? ctx->opts.out_rowptr_bits : 32;
     // buffers of `cap` entries, the fill at `rowptr` (kept: rows counted
     // against it), the caller's row pointer for device output, the wait
-    auto fill = [&](const long long *rowptr, long long cap, bool kept, bool one_round) -> tsg_status {
+    auto fill = [&](const SmallOperands &so, const long long *rowptr, long long cap, bool kept,
+                    bool one_round) -> tsg_status {
         col = pool.alloc_n<int>(cap);
         val = pool.alloc_n<double>(cap);
         if (dev_out && !rp_dev) rp_dev = pool.alloc((size_t)(P.m + 1) * (bits == 64 ? 8 : 4));
@@ -1007,16 +1036,21 @@ tsg_status small_spgemm(tsg_ctx *ctx, tsg_op op, const tsg_csr *A, const tsg_csr
             return fail(TSG_ERR_OOM, "device pool allocation failed for C (%lld entries)", cap);
         P.wait_values(ctx->stream);
         // the fill writes the caller's row pointer too (device output)
-        cudaError_t fe = small_fill(pool, P.rpA, P.colA, P.valA, P.k, P.rpB, P.colB, P.valB, P.n, P.m, rowptr, cap,
-                                    col, val, ctx->dflags, kept ? sstat : nullptr, dev_out ? rp_dev : nullptr, bits,
-                                    one_round);
+        cudaError_t fe = small_fill(pool, so, rowptr, cap, col, val, ctx->dflags, kept ? sstat : nullptr,
+                                    dev_out ? rp_dev : nullptr, bits, one_round);
         if (fe != cudaSuccess) return fail(cuda_status(fe), "small path: %s", cudaGetErrorString(fe));
         return host_wait(ctx, &P.nsync);
     };
     const long long *rowptr = nullptr;   // C's row pointer: the kept one, or this call's scan
     long long nnzC = 0;
-    if (seen && seen->rowptr) {
-        r = fill(seen->rowptr, seen->nnzc, true, seen->one_round);
+    if (seen && seen->rowptr && P.m > 0) {
+        // the fill alone at the kept row pointer, on the operands as they
+        // are (device) or as uploaded (host), which it validates itself
+        SmallOperands ro;
+        r = small_raw_operands(ctx, pool, P, op == TSG_OP_AA, A, Bm, ro);
+        if (r) return give_up(r);
+        ro.check = validate;
+        r = fill(ro, seen->rowptr, seen->nnzc, true, seen->one_round);
         if (r) return give_up(r);
         if (ctx->hstat[ST_SMALL] == 0) {
             rowptr = seen->rowptr;
@@ -1025,15 +1059,31 @@ tsg_status small_spgemm(tsg_ctx *ctx, tsg_op op, const tsg_csr *A, const tsg_csr
             drop_cv();
             pool.free(rp_dev);
             rp_dev = nullptr;
+            P.release(pool);
             e = cudaMemsetAsync(ctx->dstat + ST_SMALL, 0, 3 * sizeof(long long), ctx->stream);
             if (e != cudaSuccess) return cuda_fail(e);
         }
+    }
+    SmallOperands so;   // staged and validated operands (count pass)
+    if (!rowptr) {
+        r = stage_into_plan(ctx, pool, P, A, validate, false, P.rpA, P.colA, P.valA, P.valA_buf);
+        if (r) return give_up(r);
+        if (op == TSG_OP_AB) {
+            r = stage_into_plan(ctx, pool, P, B, validate, false, P.rpB, P.colB, P.valB, P.valB_buf);
+            if (r) return give_up(r);
+        } else {
+            P.rpB = P.rpA; P.colB = P.colA; P.valB = P.valA;
+        }
+        so.rpA.p64 = P.rpA; so.rpB.p64 = P.rpB;
+        so.colA = P.colA; so.colB = P.colB; so.valA = P.valA; so.valB = P.valB;
+        so.m = P.m; so.ka = P.k; so.kb = Bm->m; so.nb = P.n; so.nnzA = P.nnzA; so.nnzB = P.nnzB;
+        so.b_is_a = op == TSG_OP_AA;
     }
     if (!rowptr) {
         int *rowcnt = P.own<int>(pool, (long long)P.m + 1);
         P.rowptrC = P.own<long long>(pool, (long long)P.m + 1);
         if (!rowcnt || !P.rowptrC) return give_up(fail(TSG_ERR_OOM, "device pool allocation failed (small path)"));
-        e = small_count(pool, P.rpA, P.colA, P.k, P.rpB, P.colB, P.n, P.m, rowcnt, sstat);
+        e = small_count(pool, so, rowcnt, sstat);
         if (e == cudaSuccess) e = scan_i32_to_i64(pool, rowcnt, P.rowptrC, P.m, ctx->dflags);
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(ctx->dstat + ST_NNZC, P.rowptrC + P.m, sizeof(long long), cudaMemcpyDeviceToDevice,
@@ -1047,7 +1097,7 @@ tsg_status small_spgemm(tsg_ctx *ctx, tsg_op op, const tsg_csr *A, const tsg_csr
             cap = ctx->hstat[ST_NNZC];
         }
         for (int pass = 0;; ++pass) {
-            r = fill(P.rowptrC, cap, false, false);
+            r = fill(so, P.rowptrC, cap, false, false);
             if (r) return give_up(r);
             if (ctx->hstat[ST_SMALL] > 0) return not_small();
             if (ctx->hstat[ST_NNZC] <= cap || pass > 0) break;

@@ -176,6 +176,15 @@ cudaError_t scan_i64_to_i64(Pool &pool, const long long *in, long long *out, lon
 
 inline int ceil_div_i(long long a, long long b) { return (int)((a + b - 1) / b); }
 
+// A CSR row pointer as the caller gave it: int64 (p64) or int32 (p32).
+struct RowPtr {
+    const long long *p64 = nullptr;
+    const int *p32 = nullptr;
+    __host__ __device__ __forceinline__ long long operator[](long long i) const {
+        return p64 ? p64[i] : (long long)p32[i];
+    }
+};
+
 // The small-product path (tsg_small.cu): rows of A that meet at most
 // SMALL_MAX_PRODUCTS entries of B, one warp per row of C.  small_count
 // writes each row's entry count (0 for rows over the limit) and adds the
@@ -189,13 +198,22 @@ inline int ceil_div_i(long long a, long long b) { return (int)((a + b - 1) / b);
 // whose rows all fit one round (a row that does not counts in kept[0]).
 // ka = A's columns (= B's rows), nb = B's columns.
 constexpr int SMALL_MAX_PRODUCTS = 128;
-cudaError_t small_count(Pool &pool, const long long *rpA, const int *colA, int ka, const long long *rpB,
-                        const int *colB, int nb, int m, int *rowcnt, unsigned long long *stat);
-cudaError_t small_fill(Pool &pool, const long long *rpA, const int *colA, const double *valA, int ka,
-                       const long long *rpB, const int *colB, const double *valB, int nb, int m,
-                       const long long *rowptrC, long long cap, int *colC, double *valC, int *flags,
-                       unsigned long long *kept = nullptr, void *rp_out = nullptr, int rp_bits = 32,
-                       bool one_round = false);
+// The operands' row pointers are clamped into [0, nnz] where they are
+// read; with `check` (the kept-row-pointer fill on operands not validated
+// before) the fill also validates A's row pointer and columns as the
+// validation kernel does, and B's (kb rows) when B is not A.
+struct SmallOperands {
+    RowPtr rpA, rpB;
+    const int *colA = nullptr, *colB = nullptr;
+    const double *valA = nullptr, *valB = nullptr;
+    int m = 0, ka = 0, kb = 0, nb = 0;    // A: m x ka; B: kb x nb
+    long long nnzA = 0, nnzB = 0;
+    bool check = false, b_is_a = false;
+};
+cudaError_t small_count(Pool &pool, const SmallOperands &o, int *rowcnt, unsigned long long *stat);
+cudaError_t small_fill(Pool &pool, const SmallOperands &o, const long long *rowptrC, long long cap, int *colC,
+                       double *valC, int *flags, unsigned long long *kept = nullptr, void *rp_out = nullptr,
+                       int rp_bits = 32, bool one_round = false);
 
 // One instance of a batched product, as the pack/unpack kernels see it.
 struct PackDesc {

@@ -56,28 +56,47 @@ __device__ __forceinline__ int sh_insert(int *key, int col, bool &fresh)
 
 // Up to 32 A entries of row r, lane q < na holding entry q's B row
 // [bs, bs + len) (len clamped to SMALL_MAX_PRODUCTS + 1, empty for an
-// out-of-range column of A).
+// out-of-range column of A; B's row pointers clamped into [0, nnzB], so
+// that an unchecked row pointer reads nothing outside B).
 struct Batch {
     long long bs = 0;
     int len = 0;
 };
 
-__device__ __forceinline__ Batch load_batch(const long long *rpA, const int *colA, int ka, const long long *rpB,
-                                            long long p, int na, int lane, int &k)
+__device__ __forceinline__ Batch load_batch(const SmallOperands &o, long long p, int na, int lane, int *flags, int &k)
 {
     Batch b;
     k = -1;
     if (lane < na) {
-        k = colA[p + lane];
-        if ((unsigned)k < (unsigned)ka) {
-            b.bs = rpB[k];
-            const long long l = rpB[k + 1] - b.bs;
+        k = o.colA[p + lane];
+        if (o.check && (unsigned)k >= (unsigned)o.ka) set_flag(flags, FLAG_BAD_INPUT);
+        if ((unsigned)k < (unsigned)o.ka) {
+            const RowPtr rpB = o.rpB;
+            const long long nnzB = o.nnzB;
+            const long long s0 = rpB[k], s1 = rpB[k + 1];
+            b.bs = s0 < 0 ? 0 : (s0 > nnzB ? nnzB : s0);
+            const long long l = (s1 > nnzB ? nnzB : s1) - b.bs;
             b.len = (int)(l < 0 ? 0 : (l > SMALL_MAX_PRODUCTS + 1 ? SMALL_MAX_PRODUCTS + 1 : l));
         } else {
             k = -1;
         }
     }
     return b;
+}
+
+// Row r's entries [a0, a1) of A, clamped into [0, nnzA]; with `check` the
+// row pointer is validated as the validation kernel does (bounds, order,
+// first 0, last nnzA: lane 0 flags FLAG_BAD_INPUT).
+__device__ __forceinline__ void row_span(RowPtr rp, int r, int m, long long nnz, bool check, int lane, int *flags,
+                                         long long &a0, long long &a1)
+{
+    const long long v0 = rp[r], v1 = rp[r + 1];
+    if (check && lane == 0) {
+        const bool bad = v0 < 0 || v0 > nnz || v1 < v0 || v1 > nnz || (r == 0 && v0 != 0) || (r == m - 1 && v1 != nnz);
+        if (bad) set_flag(flags, FLAG_BAD_INPUT);
+    }
+    a0 = v0 < 0 ? 0 : (v0 > nnz ? nnz : v0);
+    a1 = v1 < a0 ? a0 : (v1 > nnz ? nnz : v1);
 }
 
 // the lane whose B row holds position f of the concatenation (last lane
@@ -130,23 +149,24 @@ __device__ __forceinline__ void sort_products(int c0, double a, double bv, int l
 }
 
 __global__ void __launch_bounds__(SH_WARPS * 32)
-k_small_count(const long long *__restrict__ rpA, const int *__restrict__ colA, int ka,
-              const long long *__restrict__ rpB, const int *__restrict__ colB, int nb, int m, int *rowcnt,
-              unsigned long long *stat)
+k_small_count(SmallOperands o, int *rowcnt, unsigned long long *stat)
 {
     __shared__ int s_key[SH_WARPS][SH_CAP];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int r = blockIdx.x * SH_WARPS + warp;
-    if (r >= m) return;
+    if (r >= o.m) return;
+    const int *__restrict__ colB = o.colB;
+    const int nb = o.nb;
     int *key = s_key[warp];
     bool table = false;      // the hash table is set up on the first batch that needs it
-    const long long a0 = rpA[r], a1 = rpA[r + 1];
+    long long a0, a1;
+    row_span(o.rpA, r, o.m, o.nnzA, false, lane, nullptr, a0, a1);
     int cnt = 0, P = 0;
     bool over = false;
     for (long long pb = a0; pb < a1; pb += 32) {
         const int na = (int)min(32ll, a1 - pb);
         int k;
-        const Batch b = load_batch(rpA, colA, ka, rpB, pb, na, lane, k);
+        const Batch b = load_batch(o, pb, na, lane, nullptr, k);
         const int incl = warp_incl_scan(b.len, lane);
         const int T = __shfl_sync(0xffffffffu, incl, 31);
         P += T;
@@ -201,15 +221,30 @@ k_small_count(const long long *__restrict__ rpA, const int *__restrict__ colA, i
 // did): no hash tables, so no shared memory and more warps per SM; a row
 // that does not fit is reported through `kept` like a changed row.
 template <bool ONE>
-__global__ void __launch_bounds__(SH_WARPS * 32, ONE ? 8 : 1)
-k_small_fill(const long long *__restrict__ rpA, const int *__restrict__ colA, const double *__restrict__ valA, int ka,
-             const long long *__restrict__ rpB, const int *__restrict__ colB, const double *__restrict__ valB, int nb,
-             int m, const long long *__restrict__ rowptrC, long long cap, int *colC, double *valC, int *flags,
-             unsigned long long *kept, void *rp_out, int rp_bits)
+__global__ void __launch_bounds__(SH_WARPS * 32, ONE ? 6 : 1)
+k_small_fill(SmallOperands o, const long long *__restrict__ rowptrC, long long cap, int *colC, double *valC,
+             int *flags, unsigned long long *kept, void *rp_out, int rp_bits)
 {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int r = blockIdx.x * SH_WARPS + warp;
+    if (o.check && !o.b_is_a) {
+        // B's row pointer and columns, checked across the whole grid
+        const long long stride = (long long)gridDim.x * blockDim.x;
+        const long long t0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+        bool bad = false;
+        for (long long i = t0; i <= o.kb; i += stride) {
+            const long long v = o.rpB[i];
+            bad |= v < 0 || v > o.nnzB || (i == 0 && v != 0) || (i == o.kb && v != o.nnzB) || (i < o.kb && o.rpB[i + 1] < v);
+        }
+        for (long long q = t0; q < o.nnzB; q += stride) bad |= (unsigned)o.colB[q] >= (unsigned)o.nb;
+        if (bad) set_flag(flags, FLAG_BAD_INPUT);
+    }
+    const int m = o.m;
     if (r >= m) return;
+    const int *__restrict__ colB = o.colB;
+    const double *__restrict__ valA = o.valA;
+    const double *__restrict__ valB = o.valB;
+    const int nb = o.nb;
     const long long Rb = rowptrC[r], Re = rowptrC[r + 1];
     // C larger than the buffers: nothing is written (the caller sees nnzC
     // and runs this pass again into buffers of that size)
@@ -223,11 +258,12 @@ k_small_fill(const long long *__restrict__ rpA, const int *__restrict__ colA, co
             if (r == m - 1) static_cast<int *>(rp_out)[m] = (int)Re;
         }
     }
-    const long long a0 = rpA[r], a1 = rpA[r + 1];
+    long long a0, a1;
+    row_span(o.rpA, r, m, o.nnzA, o.check, lane, flags, a0, a1);
     if (a1 - a0 <= 32) {
         const int na = (int)(a1 - a0);
         int k;
-        const Batch b = load_batch(rpA, colA, ka, rpB, a0, na, lane, k);
+        const Batch b = load_batch(o, a0, na, lane, flags, k);
         const int incl = warp_incl_scan(b.len, lane);
         const int T = __shfl_sync(0xffffffffu, incl, 31);
         if (T <= 32) {
@@ -301,7 +337,7 @@ k_small_fill(const long long *__restrict__ rpA, const int *__restrict__ colA, co
     for (long long pb = a0; pb < a1; pb += 32) {
         const int na = (int)min(32ll, a1 - pb);
         int k;
-        const Batch b = load_batch(rpA, colA, ka, rpB, pb, na, lane, k);
+        const Batch b = load_batch(o, pb, na, lane, flags, k);
         const double av = (lane < na && k >= 0) ? valA[pb + lane] : 0.0;
         const int incl = warp_incl_scan(b.len, lane);
         const int T = __shfl_sync(0xffffffffu, incl, 31);
@@ -376,33 +412,28 @@ k_small_fill(const long long *__restrict__ rpA, const int *__restrict__ colA, co
 
 }  // namespace
 
-cudaError_t small_count(Pool &pool, const long long *rpA, const int *colA, int ka, const long long *rpB,
-                        const int *colB, int nb, int m, int *rowcnt, unsigned long long *stat)
+cudaError_t small_count(Pool &pool, const SmallOperands &o, int *rowcnt, unsigned long long *stat)
 {
-    if (m <= 0) return cudaSuccess;
-    k_small_count<<<(unsigned)((m + SH_WARPS - 1) / SH_WARPS), SH_WARPS * 32, 0, pool.stream>>>(rpA, colA, ka, rpB, colB,
-                                                                                                 nb, m, rowcnt, stat);
+    if (o.m <= 0) return cudaSuccess;
+    k_small_count<<<(unsigned)((o.m + SH_WARPS - 1) / SH_WARPS), SH_WARPS * 32, 0, pool.stream>>>(o, rowcnt, stat);
     ::tsg::count_launch();
     return cudaGetLastError();
 }
 
-cudaError_t small_fill(Pool &pool, const long long *rpA, const int *colA, const double *valA, int ka,
-                       const long long *rpB, const int *colB, const double *valB, int nb, int m,
-                       const long long *rowptrC, long long cap, int *colC, double *valC, int *flags,
-                       unsigned long long *kept, void *rp_out, int rp_bits, bool one_round)
+cudaError_t small_fill(Pool &pool, const SmallOperands &o, const long long *rowptrC, long long cap, int *colC,
+                       double *valC, int *flags, unsigned long long *kept, void *rp_out, int rp_bits, bool one_round)
 {
+    const int m = o.m;
     if (m <= 0) {   // C's row pointer is the single 0
         if (!rp_out) return cudaSuccess;
         return cudaMemsetAsync(rp_out, 0, rp_bits == 64 ? 8 : 4, pool.stream);
     }
     const unsigned grid = (unsigned)((m + SH_WARPS - 1) / SH_WARPS);
     if (one_round && kept)
-        k_small_fill<true><<<grid, SH_WARPS * 32, 0, pool.stream>>>(rpA, colA, valA, ka, rpB, colB, valB, nb, m,
-                                                                    rowptrC, cap, colC, valC, flags, kept, rp_out,
+        k_small_fill<true><<<grid, SH_WARPS * 32, 0, pool.stream>>>(o, rowptrC, cap, colC, valC, flags, kept, rp_out,
                                                                     rp_bits);
     else
-        k_small_fill<false><<<grid, SH_WARPS * 32, 0, pool.stream>>>(rpA, colA, valA, ka, rpB, colB, valB, nb, m,
-                                                                     rowptrC, cap, colC, valC, flags, kept, rp_out,
+        k_small_fill<false><<<grid, SH_WARPS * 32, 0, pool.stream>>>(o, rowptrC, cap, colC, valC, flags, kept, rp_out,
                                                                      rp_bits);
     ::tsg::count_launch();
     return cudaGetLastError();
