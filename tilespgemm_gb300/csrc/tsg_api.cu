@@ -993,13 +993,16 @@ tsg_status small_spgemm(tsg_ctx *ctx, tsg_op op, const tsg_csr *A, const tsg_csr
     int *col = nullptr;
     double *val = nullptr;
     void *rp_dev = nullptr;
-    auto drop_cv = [&]() { pool.free(col); pool.free(val); col = nullptr; val = nullptr; };
+    void *cblock = nullptr;   // device output: C's columns, values and row pointer in one allocation
+    auto drop_cv = [&]() {
+        if (cblock) pool.free(cblock);
+        else { pool.free(col); pool.free(val); }
+        cblock = nullptr; col = nullptr; val = nullptr; rp_dev = nullptr;
+    };
     // undo everything before a return (values' upload joined, the stream drained)
     auto release = [&]() {
         P.wait_values(ctx->stream);
         drop_cv();
-        pool.free(rp_dev);
-        rp_dev = nullptr;
         P.release(pool);
         cudaStreamSynchronize(ctx->stream);
     };
@@ -1029,11 +1032,20 @@ tsg_status small_spgemm(tsg_ctx *ctx, tsg_op op, const tsg_csr *A, const tsg_csr
     // against it), the caller's row pointer for device output, the wait
     auto fill = [&](const SmallOperands &so, const long long *rowptr, long long cap, bool kept,
                     bool one_round) -> tsg_status {
-        col = pool.alloc_n<int>(cap);
-        val = pool.alloc_n<double>(cap);
-        if (dev_out && !rp_dev) rp_dev = pool.alloc((size_t)(P.m + 1) * (bits == 64 ? 8 : 4));
-        if (!col || !val || (dev_out && !rp_dev))
-            return fail(TSG_ERR_OOM, "device pool allocation failed for C (%lld entries)", cap);
+        if (dev_out) {
+            auto a256 = [](long long x) { return (size_t)((x + 255) & ~255ll); };
+            const size_t oc = a256(4 * std::max(cap, 1ll)), ov = a256(8 * std::max(cap, 1ll));
+            cblock = pool.alloc(oc + ov + (size_t)(P.m + 1) * (bits == 64 ? 8 : 4));
+            if (cblock) {
+                col = static_cast<int *>(cblock);
+                val = reinterpret_cast<double *>(static_cast<char *>(cblock) + oc);
+                rp_dev = static_cast<char *>(cblock) + oc + ov;
+            }
+        } else {
+            col = pool.alloc_n<int>(cap);
+            val = pool.alloc_n<double>(cap);
+        }
+        if (!col || !val) return fail(TSG_ERR_OOM, "device pool allocation failed for C (%lld entries)", cap);
         P.wait_values(ctx->stream);
         // the fill writes the caller's row pointer too (device output)
         cudaError_t fe = small_fill(pool, so, rowptr, cap, col, val, ctx->dflags, kept ? sstat : nullptr,
@@ -1057,8 +1069,6 @@ tsg_status small_spgemm(tsg_ctx *ctx, tsg_op op, const tsg_csr *A, const tsg_csr
             nnzC = seen->nnzc;
         } else {   // a row differs from the kept pointer: the count pass decides
             drop_cv();
-            pool.free(rp_dev);
-            rp_dev = nullptr;
             P.release(pool);
             e = cudaMemsetAsync(ctx->dstat + ST_SMALL, 0, 3 * sizeof(long long), ctx->stream);
             if (e != cudaSuccess) return cuda_fail(e);
@@ -1128,9 +1138,7 @@ tsg_status small_spgemm(tsg_ctx *ctx, tsg_op op, const tsg_csr *A, const tsg_csr
         OutOwner *o = new OutOwner();
         o->ctx = ctx;
         o->where = C->where;
-        o->blocks.push_back({rp_dev, 0});
-        o->blocks.push_back({col, 0});
-        o->blocks.push_back({val, 0});
+        o->blocks.push_back({cblock, 0});   // the three arrays
         C->m = P.m; C->n = P.n; C->nnz = nnzC; C->rowptr_bits = bits;
         C->row_ptr = rp_dev; C->col = col; C->val = val;
         C->owner = o;
