@@ -1027,6 +1027,20 @@ struct LongRow {
     long long Rb;
 };
 
+// A long row's walk data, computed once per call (k_long_list, k_long_fit)
+struct LongRowDesc {
+    long long Rb;        // the row's first entry of C
+    long long c0;        // its tile-row's first C tile
+    long long tab_off;   // its cut table
+    int R, pa0, na, T0, Wp, cshift, S, nnz_r;
+};
+// A part of a long row (k_long_parts): the row (l < 0: skipped), the part's
+// index j, its C tile slots [sa, sb) and its first entry of C in the row
+struct LongPart {
+    int l, j, sa, sb, first, pad0, pad1, pad2;
+};
+static_assert(sizeof(LongPart) == 32, "two 16-byte loads");
+
 __device__ __forceinline__ LongRow long_row(const NumericArgs &g, int R)
 {
     LongRow L;
@@ -1059,7 +1073,7 @@ k_long_flag(NumericArgs g, int cls, long long nrows, int *flag)
 // entries and cut-table size; entries past the last long row stay zero
 __global__ void __launch_bounds__(256)
 k_long_list(NumericArgs g, int cls, long long nrows, const int *lpos, int *lidx, int *lrow, int *parts, int *nas,
-            long long *tabsz)
+            long long *tabsz, LongRowDesc *rdesc)
 {
     const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (idx >= nrows || lpos[idx + 1] == lpos[idx]) return;
@@ -1071,19 +1085,71 @@ k_long_list(NumericArgs g, int cls, long long nrows, const int *lpos, int *lidx,
     parts[l] = L.P;
     nas[l] = L.na;
     tabsz[l] = (long long)L.na * (L.P + 1);
+    LongRowDesc d;
+    d.Rb = L.Rb;
+    d.c0 = g.crp[R >> 4];
+    d.tab_off = 0;   // set by k_long_fit
+    d.R = R; d.pa0 = L.pa0; d.na = L.na; d.T0 = L.T0; d.Wp = L.Wp; d.cshift = L.cshift;
+    d.S = (int)(g.crp[(R >> 4) + 1] - d.c0);
+    d.nnz_r = L.nnz_r;
+    rdesc[l] = d;
 }
 
 // rows whose cut table fits the allocation take the parts path
 // (handled[idx] = 1); the others stay with k_numeric_wide
 __global__ void __launch_bounds__(256)
 k_long_fit(long long nrows, const int *lpos, const int *lidx, const long long *tab_off, long long cap,
-           unsigned char *handled, unsigned char *lfit)
+           unsigned char *handled, unsigned char *lfit, LongRowDesc *rdesc)
 {
     const long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (l >= nrows || l >= lpos[nrows]) return;
     const bool fit = tab_off[l + 1] <= cap;
     lfit[l] = fit ? 1 : 0;
     handled[lidx[l]] = fit ? 1 : 0;
+    rdesc[l].tab_off = tab_off[l];
+}
+
+// first index in [lo, hi) whose value is >= key (one thread's binary search)
+__device__ __forceinline__ int lb_range(const int *__restrict__ a, int lo, int hi, int key)
+{
+    while (lo < hi) {
+        const int md = (lo + hi) >> 1;
+        if (a[md] < key) lo = md + 1; else hi = md;
+    }
+    return lo;
+}
+
+// Every part's walk data, so that a part of the walk starts from two loads:
+// one warp per long row, lanes over its parts -- the part's C tile slots
+// [sa, sb) of the tile-row and its first entry of C within the row (binary
+// searches of the tile columns and of the row's columns).  Parts of rows
+// whose cut table did not fit get l = -1 (the walk skips them).
+__global__ void __launch_bounds__(256)
+k_long_parts(NumericArgs g, long long nrows, const int *lpos, const unsigned char *lfit, const int *part_off,
+             const LongRowDesc *rdesc, LongPart *pdesc)
+{
+    const int lane = threadIdx.x & 31;
+    const long long nw = (long long)gridDim.x * 8, w0 = blockIdx.x * 8LL + (threadIdx.x >> 5);
+    const long long nl = lpos[nrows];
+    for (long long l = w0; l < nl; l += nw) {
+        const LongRowDesc d = rdesc[l];
+        const int p0 = part_off[l], np = part_off[l + 1] - p0;
+        const bool fit = lfit[l] != 0;
+        const int *tcol = g.ccol + d.c0;
+        for (int j = lane; j < np; j += 32) {
+            LongPart pt;
+            pt.l = fit ? (int)l : -1;
+            pt.j = j;
+            pt.sa = pt.sb = pt.first = 0;
+            if (fit) {
+                const int wlo = d.T0 + j * d.Wp;
+                pt.sa = lb_range(tcol, 0, d.S, wlo);
+                pt.sb = lb_range(tcol, pt.sa, d.S, wlo + d.Wp);
+                pt.first = lb_range(g.colC + d.Rb, 0, d.nnz_r, wlo * TILE - d.cshift);
+            }
+            pdesc[p0 + j] = pt;
+        }
+    }
 }
 
 // last l in [0, n) with off[l] <= v (off nondecreasing, off[0] <= v)
@@ -1136,8 +1202,8 @@ k_long_cuts(NumericArgs g, long long nrows, const int *lrow, const unsigned char
 // left (parts differ widely in cost, so a static share would leave warps
 // idle behind the hub rows' parts)
 __global__ void __launch_bounds__(ROW_WARPS * 32, 5)
-k_long_walk(NumericArgs g, long long nrows, const int *lrow, const unsigned char *lfit, const int *part_off,
-            const long long *tab_off, const int *tab, unsigned long long *next_part)
+k_long_walk(NumericArgs g, long long nrows, const int *part_off, const LongRowDesc *__restrict__ rdesc,
+            const LongPart *__restrict__ pdesc, const int *tab, unsigned long long *next_part)
 {
     extern __shared__ __align__(16) unsigned char s_raw[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1150,27 +1216,26 @@ k_long_walk(NumericArgs g, long long nrows, const int *lrow, const unsigned char
     const long long nparts = part_off[nrows];
     bool bad = false;
     for (;;) {
+        // one part per fetch (consecutive parts of a hub row are all heavy:
+        // taking several at a time left warps busy behind the rest)
         unsigned long long t = 0;
         if (lane == 0) t = atomicAdd(next_part, 1ull);
         const long long gp = (long long)__shfl_sync(0xffffffffu, t, 0);
         if (gp >= nparts) break;
-        const long long l = last_le(part_off, nrows, gp);
-        if (!lfit[l]) continue;
-        const int R = lrow[l];
-        const LongRow L = long_row(g, R);
-        const int j = (int)(gp - part_off[l]);
-        const int i = R >> 4, r = R & (TILE - 1);
-        const long long c0 = g.crp[i];
-        const int S = (int)(g.crp[i + 1] - c0);
-        const uint16_t *mrow = g.cmask + c0 * TILE + (long long)r * S;
-        const int *tcol = g.ccol + c0;
+        const LongPart pt = pdesc[gp];   // the part's long row, tile slots and first entry (k_long_parts)
+        if (pt.l < 0) continue;
+        const LongRowDesc L = rdesc[pt.l];
+        const int j = pt.j;
+        const int r = L.R & (TILE - 1);
+        const int S = L.S;
+        const uint16_t *mrow = g.cmask + L.c0 * TILE + (long long)r * S;
+        const int *tcol = g.ccol + L.c0;
         const int wlo = L.T0 + j * L.Wp, whi = wlo + L.Wp;   // tile columns [wlo, whi)
-        const int sa = warp_lower_bound(tcol, 0, S, wlo, lane);
-        const int sb = warp_lower_bound(tcol, sa, S, whi, lane);
+        const int sa = pt.sa, sb = pt.sb;
         if (sa >= sb) continue;
         // the part's entries of C: [Rb + first, Rb + first + E); s_off
         // holds each tile's offset among them
-        const unsigned first = (unsigned)warp_lower_bound(g.colC + L.Rb, 0, L.nnz_r, wlo * TILE - L.cshift, lane);
+        const unsigned first = (unsigned)pt.first;
         unsigned run = 0;
         for (int s = sa; s < sb; s += 32) {
             const int ss = s + lane;
@@ -1200,7 +1265,7 @@ k_long_walk(NumericArgs g, long long nrows, const int *lrow, const unsigned char
                 const unsigned mk = s_msk[t];
                 return ((mk >> (TILE - 1 - cc)) & 1u) ? (int)s_off[t] + __popc(mk >> (TILE - cc)) : -1;
             };
-            const int *tb = tab + tab_off[l];
+            const int *tb = tab + L.tab_off;
             for (int pb = 0; pb < L.na; pb += 32) {
                 const int nb = min(32, L.na - pb);
                 int bs = 0, be = 0;
@@ -1284,19 +1349,22 @@ struct LongScratch {
     unsigned char *handled = nullptr, *lfit = nullptr;
     int *tab = nullptr;
     unsigned long long *next_part = nullptr;   // the walk's work counter
+    LongRowDesc *rdesc = nullptr;              // per long row (n at most)
+    LongPart *pdesc = nullptr;                 // per part
 };
 
 void long_release(Pool &pool, LongScratch &L)
 {
     for (void *p : {(void *)L.flag, (void *)L.lpos, (void *)L.lidx, (void *)L.lrow, (void *)L.parts, (void *)L.nas,
                     (void *)L.part_off, (void *)L.tabsz, (void *)L.na_off, (void *)L.tab_off, (void *)L.handled,
-                    (void *)L.lfit, (void *)L.tab, (void *)L.next_part})
+                    (void *)L.lfit, (void *)L.tab, (void *)L.next_part, (void *)L.rdesc, (void *)L.pdesc})
         pool.free(p);
     L = LongScratch{};
 }
 
 // the long rows' list, part and A-entry prefixes, and the cut table
-cudaError_t long_prepare(Pool &pool, const NumericArgs &a, int cls, long long n, long long tab_bound, LongScratch &L)
+cudaError_t long_prepare(Pool &pool, const NumericArgs &a, int cls, long long n, long long tab_bound,
+                         long long parts_bound, LongScratch &L)
 {
     cudaStream_t s = pool.stream;
     L.flag = pool.alloc_n<int>(n + 1);
@@ -1312,8 +1380,9 @@ cudaError_t long_prepare(Pool &pool, const NumericArgs &a, int cls, long long n,
     L.na_off = pool.alloc_n<long long>(n + 1);
     L.tab_off = pool.alloc_n<long long>(n + 1);
     L.next_part = pool.alloc_n<unsigned long long>(1);
+    L.rdesc = pool.alloc_n<LongRowDesc>(n);
     if (!L.flag || !L.lpos || !L.lidx || !L.handled || !L.lfit || !L.lrow || !L.parts || !L.nas || !L.part_off ||
-        !L.tabsz || !L.na_off || !L.tab_off || !L.next_part) {
+        !L.tabsz || !L.na_off || !L.tab_off || !L.next_part || !L.rdesc) {
         const cudaError_t err = pool.err != cudaSuccess ? pool.err : cudaErrorMemoryAllocation;
         long_release(pool, L);
         return err;
@@ -1328,7 +1397,7 @@ cudaError_t long_prepare(Pool &pool, const NumericArgs &a, int cls, long long n,
     if (e == cudaSuccess) { k_long_flag<<<gb, 256, 0, s>>>(a, cls, n, L.flag); ::tsg::count_launch(); e = cudaGetLastError(); }
     if (e == cudaSuccess) e = scan_i32_to_i32(pool, L.flag, L.lpos, n, a.flags);
     if (e == cudaSuccess) {
-        k_long_list<<<gb, 256, 0, s>>>(a, cls, n, L.lpos, L.lidx, L.lrow, L.parts, L.nas, L.tabsz);
+        k_long_list<<<gb, 256, 0, s>>>(a, cls, n, L.lpos, L.lidx, L.lrow, L.parts, L.nas, L.tabsz, L.rdesc);
         ::tsg::count_launch();
         e = cudaGetLastError();
     }
@@ -1337,23 +1406,33 @@ cudaError_t long_prepare(Pool &pool, const NumericArgs &a, int cls, long long n,
     if (e == cudaSuccess) e = scan_i64_to_i64(pool, L.tabsz, L.tab_off, n, a.flags);
     // the cut table: its exact size when the stream can wait for it, else
     // the bound (inside a graph capture)
-    long long cap = tab_bound;
+    // (and the parts' descriptors: their exact count, or the bound)
+    long long cap = tab_bound, nparts = parts_bound;
     if (e == cudaSuccess) {
         cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
         e = cudaStreamIsCapturing(s, &cs);
         if (e == cudaSuccess && cs == cudaStreamCaptureStatusNone) {
             long long need = 0;
+            int np = 0;
             e = cudaMemcpyAsync(&need, L.tab_off + n, sizeof(long long), cudaMemcpyDeviceToHost, s);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(&np, L.part_off + n, sizeof(int), cudaMemcpyDeviceToHost, s);
             if (e == cudaSuccess) e = cudaStreamSynchronize(s);
             cap = std::min(tab_bound, need);
+            nparts = np;
         }
     }
     if (e == cudaSuccess) {
         L.tab = pool.alloc_n<int>(cap);
-        if (!L.tab) e = pool.err != cudaSuccess ? pool.err : cudaErrorMemoryAllocation;
+        L.pdesc = pool.alloc_n<LongPart>(nparts);
+        if (!L.tab || !L.pdesc) e = pool.err != cudaSuccess ? pool.err : cudaErrorMemoryAllocation;
     }
     if (e == cudaSuccess) {
-        k_long_fit<<<gb, 256, 0, s>>>(n, L.lpos, L.lidx, L.tab_off, cap, L.handled, L.lfit);
+        k_long_fit<<<gb, 256, 0, s>>>(n, L.lpos, L.lidx, L.tab_off, cap, L.handled, L.lfit, L.rdesc);
+        ::tsg::count_launch();
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) {
+        k_long_parts<<<LONG_GRID * 2, 256, 0, s>>>(a, n, L.lpos, L.lfit, L.part_off, L.rdesc, L.pdesc);
         ::tsg::count_launch();
         e = cudaGetLastError();
     }
@@ -1458,13 +1537,13 @@ cudaError_t numeric_run(Pool &pool, const NumericArgs &a, const long long *binst
                            ((long long)a.n + TILE - 1) / TILE >= LONG_MIN_TILES;
         LongScratch L{};
         if (parts) {
-            e = long_prepare(pool, a, c, n, tab_bound, L);
+            e = long_prepare(pool, a, c, n, tab_bound, n * pmax, L);
             if (e != cudaSuccess) break;
         }
         if (c == ROW_WIDE) { k_numeric_wide<ROW_WARPS><<<(unsigned)n, ROW_WARPS * 32, WIDE_SMEM, s>>>(a, c, n, packed, L.handled); ::tsg::count_launch(); }
         else { k_numeric_wide<1><<<(unsigned)((n + ROW_WARPS - 1) / ROW_WARPS), ROW_WARPS * 32, WIDE_SMEM, s>>>(a, c, n, packed, nullptr); ::tsg::count_launch(); }
         if (parts) {
-            { k_long_walk<<<LONG_GRID, ROW_WARPS * 32, LONG_SMEM, s>>>(a, n, L.lrow, L.lfit, L.part_off, L.tab_off, L.tab, L.next_part); ::tsg::count_launch(); }
+            { k_long_walk<<<LONG_GRID, ROW_WARPS * 32, LONG_SMEM, s>>>(a, n, L.part_off, L.rdesc, L.pdesc, L.tab, L.next_part); ::tsg::count_launch(); }
             long_release(pool, L);
         }
         e = cudaGetLastError();
