@@ -653,9 +653,12 @@ __device__ __forceinline__ void row_cols(const NumericArgs &g, int R, int lane)
     const int S = (int)(g.crp[i + 1] - c0);
     const long long Rb = g.rowptrC[R];
     const uint16_t *mrow = g.cmask + c0 * TILE + (long long)r * S;
+    const long long nnz_r = g.rowptrC[R + 1] - Rb;
     long long run = 0;
-    // 128 slots per round: all their loads issued before any is used
-    for (int sb = 0; sb < S; sb += 128) {
+    // 128 slots per round: all their loads issued before any is used; the
+    // walk ends with the row's last entry (the tile-row's later tiles, which
+    // other rows use, hold nothing of this row)
+    for (int sb = 0; sb < S && run < nnz_r; sb += 128) {
         unsigned mkv[4];
         int jbv[4];
 #pragma unroll
@@ -667,6 +670,7 @@ __device__ __forceinline__ void row_cols(const NumericArgs &g, int R, int lane)
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
             const unsigned mk = mkv[u];
+            if (!__ballot_sync(0xffffffffu, mk != 0u)) continue;   // 32 tiles without an entry of this row
             const int cnt = __popc(mk);
             const int incl = warp_incl_scan(cnt, lane);
             const int excl = incl - cnt;
