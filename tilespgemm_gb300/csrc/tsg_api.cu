@@ -62,6 +62,7 @@ cudaError_t mtx_emit(Pool &pool, const int *ri, const int *ci, const double *vv,
 cudaError_t mtx_emit_fill(Pool &pool, const int *ri, const int *ci, const double *vv, long long NZ, bool symm,
                           const long long *eoff, int *key, int *col, double *val);
 cudaError_t gather_i32(Pool &pool, const int *perm, const int *src, int *dst, long long n);
+cudaError_t mtx_host_spans(Pool &pool, long long n, const long long *hl, const long long *ends, long long *span);
 cudaError_t tiles_from_csr_c(Pool &pool, int m, int blkm, long long numblk, const long long *crp, const int *ccol,
                              const uint16_t *cmask, const long long *rowptr, const int *col, const double *val,
                              long long *nnzb, uint8_t *ptr, uint8_t *lcol, double *tval, int *flags);
@@ -898,6 +899,7 @@ void phase_times(tsg_ctx *ctx, tsg_stats *st, const PhaseTimer &tm)
 
 constexpr long long SMALL_NNZ_MAX = 1ll << 22;   // entries of A and of B at most
 constexpr size_t SMALL_SHAPES = 32;
+constexpr int SMALL_KEEP_ROWS = 1 << 22;   // C's row pointer is kept for shapes of up to this many rows (32 MB each)
 
 SmallShape *small_shape_find(tsg_ctx *ctx, const SmallShape &k)
 {
@@ -1122,7 +1124,7 @@ tsg_status small_spgemm(tsg_ctx *ctx, tsg_op op, const tsg_csr *A, const tsg_csr
     // this call's rows all fit one round (from the count pass; a kept shape keeps its flag)
     key.one_round = rowptr == P.rowptrC ? ctx->hstat[ST_SMALL + 2] == 0 : seen->one_round;
     seen = small_shape_record(ctx, key);
-    if (rowptr == P.rowptrC) {   // kept for the shape's next call (when memory allows)
+    if (rowptr == P.rowptrC && P.m <= SMALL_KEEP_ROWS) {   // kept for the shape's next call (when memory allows)
         if (!seen->rowptr) seen->rowptr = pool.alloc_n<long long>((long long)P.m + 1);
         if (seen->rowptr)
             cudaMemcpyAsync(seen->rowptr, P.rowptrC, sizeof(long long) * ((size_t)P.m + 1), cudaMemcpyDeviceToDevice,
@@ -1710,10 +1712,13 @@ tsg_status tsg_load_mtx_device(tsg_ctx *ctx, const char *path, tsg_csr *A, int32
     if (e != cudaSuccess) return cuda_fail(e);
     // lines the device left: the host loader's line reader, several threads
     if (hcount > 0) {
-        std::vector<long long> hts(hcount), hls(hcount), endv((size_t)lines);
-        e = cudaMemcpyAsync(hts.data(), ht, sizeof(long long) * hcount, cudaMemcpyDeviceToHost, ctx->stream);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(hls.data(), hl, sizeof(long long) * hcount, cudaMemcpyDeviceToHost, ctx->stream);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(endv.data(), ends, sizeof(long long) * (size_t)lines, cudaMemcpyDeviceToHost, ctx->stream);
+        // their entry numbers and byte spans (gathered on the device)
+        std::vector<long long> hts(hcount), spans(2 * hcount);
+        long long *dspan = static_cast<long long *>(dalloc(2 * sizeof(long long) * hcount));
+        if (!dspan) return cuda_fail(cudaErrorMemoryAllocation);
+        e = mtx_host_spans(pool, (long long)hcount, hl, ends, dspan);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(hts.data(), ht, sizeof(long long) * hcount, cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(spans.data(), dspan, 2 * sizeof(long long) * hcount, cudaMemcpyDeviceToHost, ctx->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
         if (e != cudaSuccess) return cuda_fail(e);
         std::vector<int> hi(hcount), hj(hcount);
@@ -1721,8 +1726,7 @@ tsg_status tsg_load_mtx_device(tsg_ctx *ctx, const char *path, tsg_csr *A, int32
         std::atomic<int> malformed{0}, outside{0}, mirror{0};
         auto work = [&](size_t a, size_t b) {
             for (size_t k = a; k < b; ++k) {
-                const long long L = hls[k];
-                const char *q = data + (L == 0 ? 0 : endv[(size_t)L - 1] + 1), *qe = data + endv[(size_t)L];
+                const char *q = data + spans[2 * k], *qe = data + spans[2 * k + 1];
                 while (q < qe && (*q == ' ' || *q == '\t' || *q == '\r' || *q == '\v' || *q == '\f')) ++q;
                 long long i = 0, j = 0;
                 double v = 1.0;

@@ -267,6 +267,17 @@ __global__ void k_emit(const int *__restrict__ ri, const int *__restrict__ ci, c
     }
 }
 
+// the byte spans [start, end) of the host's lines
+__global__ void k_host_spans(long long n, const long long *__restrict__ hl, const long long *__restrict__ ends,
+                             long long *span)
+{
+    const long long h = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (h >= n) return;
+    const long long L = hl[h];
+    span[2 * h] = L == 0 ? 0 : ends[L - 1] + 1;
+    span[2 * h + 1] = ends[L];
+}
+
 __global__ void k_gather_i32(const int *__restrict__ perm, const int *__restrict__ src, int *dst, long long n)
 {
     const long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -358,6 +369,14 @@ cudaError_t mtx_emit_fill(Pool &pool, const int *ri, const int *ci, const double
 {
     if (NZ <= 0) return cudaSuccess;
     k_emit<<<blocks_for(NZ, 256), 256, 0, pool.stream>>>(ri, ci, vv, NZ, symm, eoff, key, col, val);
+    ::tsg::count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t mtx_host_spans(Pool &pool, long long n, const long long *hl, const long long *ends, long long *span)
+{
+    if (n <= 0) return cudaSuccess;
+    k_host_spans<<<blocks_for(n, 256), 256, 0, pool.stream>>>(n, hl, ends, span);
     ::tsg::count_launch();
     return cudaGetLastError();
 }
