@@ -222,6 +222,23 @@ def run_reference(args) -> None:
     print(json.dumps(out))
 
 
+def max_over_ranks(x: float, dist, device: str = "cuda") -> float:
+    """The largest x over the ranks of the job (x itself with one rank):
+    the whole job takes as long as its slowest replica."""
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_gflops(world: int, cub_per_rank: int, ms: float) -> float:
+    """GFLOPS of the job: every rank does 2 * cub_per_rank flops in ms
+    (the slowest rank's time)."""
+    return world * 2.0 * cub_per_rank / (ms * 1e6)
+
+
 def measure_e2e(args, ctx, A, op, stream, nnz_c, barrier, dist):
     """The same SpGEMM through the C ABI with host operands (pinned) and a
     host C: the copies both ways are inside the timed region.  Returns
@@ -244,11 +261,7 @@ def measure_e2e(args, ctx, A, op, stream, nnz_c, barrier, dist):
     e1.record(stream)
     e1.synchronize()
     barrier()
-    ms_e2e = e0.elapsed_time(e1) / args.steps
-    if dist is not None:
-        t = torch.tensor([ms_e2e], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_e2e = float(t.item())
+    ms_e2e = max_over_ranks(e0.elapsed_time(e1) / args.steps, dist)
     h2d = 4 * (A.m + 1) + 12 * A.nnz
     d2h = c_rowptr_bytes + 12 * nnz_c
     return ms_e2e, h2d, d2h
@@ -330,12 +343,8 @@ def run_ours(args) -> None:
         ev1.synchronize()
     launches = lib.tsg_launch_count() - l0
     barrier()
-    ms = ev0.elapsed_time(ev1) / args.steps
-    if dist is not None:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * 2.0 * cub / (ms * 1e6)
+    ms = max_over_ranks(ev0.elapsed_time(ev1) / args.steps, dist)
+    value = whole_job_gflops(world, cub, ms)
 
     # ---- e2e through the ABI with host operands ----
     ms_e2e, h2d, d2h = None, 0, 0
@@ -401,7 +410,7 @@ def run_ours(args) -> None:
         "host_waits_per_step": phases[-1]["n_syncs"],
         "roofline": roofline,
         "cpu_baseline": cpu,
-        "e2e": ({"value": world * 2.0 * cub / (ms_e2e * 1e6), "unit": UNIT, "ms_per_step": ms_e2e,
+        "e2e": ({"value": whole_job_gflops(world, cub, ms_e2e), "unit": UNIT, "ms_per_step": ms_e2e,
                  "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h} if ms_e2e is not None else None),
         "gpu_launches": int(launches),
         "gpu_launches_per_step": launches / args.steps,
