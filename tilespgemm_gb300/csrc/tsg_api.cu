@@ -57,8 +57,8 @@ cudaError_t mtx_take(Pool &pool, const unsigned char *st, const long long *tpos,
                      double *vv, unsigned long long *hn, long long *ht, long long *hl, int *bad);
 cudaError_t mtx_patch(Pool &pool, long long n, const long long *ht, const int *hi, const int *hj, const double *hv,
                       int *ri, int *ci, double *vv);
-cudaError_t mtx_emit(Pool &pool, const int *ri, const int *ci, const double *vv, long long NZ, bool symm, int *cnt,
-                     long long *eoff, int *flags);
+cudaError_t mtx_emit(Pool &pool, const int *ri, const int *ci, long long NZ, bool symm, int *cnt, long long *eoff,
+                     int *flags);
 cudaError_t mtx_emit_fill(Pool &pool, const int *ri, const int *ci, const double *vv, long long NZ, bool symm,
                           const long long *eoff, int *key, int *col, double *val);
 cudaError_t gather_i32(Pool &pool, const int *perm, const int *src, int *dst, long long n);
@@ -1768,7 +1768,7 @@ tsg_status tsg_load_mtx_device(tsg_ctx *ctx, const char *path, tsg_csr *A, int32
     long long *eoff = static_cast<long long *>(dalloc(sizeof(long long) * (size_t)(NZ + 1)));
     if (!cnt || !eoff) return cuda_fail(cudaErrorMemoryAllocation);
     long long E = 0;
-    e = mtx_emit(pool, ri, ci, vv, NZ, h.symm, cnt, eoff, ctx->dflags);
+    e = mtx_emit(pool, ri, ci, NZ, h.symm, cnt, eoff, ctx->dflags);
     if (e == cudaSuccess) e = cudaMemcpyAsync(&E, eoff + NZ, sizeof(long long), cudaMemcpyDeviceToHost, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) return cuda_fail(e);

@@ -99,8 +99,8 @@ tsg_status bad(const char *msg)
 }
 
 enum ValueKind { V_REAL, V_COMPLEX, V_INT, V_PATTERN };
-static_assert(V_REAL == tsg::MTX_REAL && V_COMPLEX == tsg::MTX_COMPLEX && V_INT == tsg::MTX_INTEGER &&
-              V_PATTERN == tsg::MTX_PATTERN, "value kinds");
+static_assert((int)V_REAL == (int)tsg::MTX_REAL && (int)V_COMPLEX == (int)tsg::MTX_COMPLEX &&
+              (int)V_INT == (int)tsg::MTX_INTEGER && (int)V_PATTERN == (int)tsg::MTX_PATTERN, "value kinds");
 
 // The entries of the data lines in [p, end), one per line (blank lines
 // skipped), in file order, 0-based.  ok = false when a line is not exactly

@@ -353,8 +353,8 @@ cudaError_t mtx_patch(Pool &pool, long long n, const long long *ht, const int *h
     return cudaGetLastError();
 }
 
-cudaError_t mtx_emit(Pool &pool, const int *ri, const int *ci, const double *vv, long long NZ, bool symm, int *cnt,
-                     long long *eoff, int *flags)
+cudaError_t mtx_emit(Pool &pool, const int *ri, const int *ci, long long NZ, bool symm, int *cnt, long long *eoff,
+                     int *flags)
 {
     if (NZ <= 0) return cudaMemsetAsync(eoff, 0, sizeof(long long), pool.stream);
     k_emit_count<<<blocks_for(NZ, 256), 256, 0, pool.stream>>>(ri, ci, NZ, symm, cnt);

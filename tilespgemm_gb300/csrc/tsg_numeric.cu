@@ -675,36 +675,38 @@ __device__ __forceinline__ void row_cols(const NumericArgs &g, int R, int lane)
             const int incl = warp_incl_scan(cnt, lane);
             const int excl = incl - cnt;
             const int total = __shfl_sync(0xffffffffu, incl, 31);
-            if (!COALESCE || __reduce_max_sync(0xffffffffu, (unsigned)cnt) <= 4) {
-                // few entries per tile row: each lane writes its own (a store
-                // per entry, consecutive lanes at consecutive positions)
-                unsigned m = mk;
-                long long dst = Rb + run + excl;
-                while (m) {
-                    const int b = 31 - __clz(m);   // highest bit = smallest local column
-                    g.colC[dst++] = jbv[u] + (TILE - 1 - b);
-                    m &= ~(1u << b);
+            if constexpr (COALESCE) {
+                if (__reduce_max_sync(0xffffffffu, (unsigned)cnt) > 4) {
+                    // one output position per lane (coalesced stores): its
+                    // slot t is the first lane whose inclusive count exceeds
+                    // it, its column the k-th set column of that slot's mask
+                    for (int p0 = 0; p0 < total; p0 += 32) {
+                        const int p = p0 + lane;
+                        int t = 0;
+#pragma unroll
+                        for (int step = 16; step; step >>= 1)
+                            if (__shfl_sync(0xffffffffu, incl, t + step - 1) <= p) t += step;
+                        const unsigned mt = __shfl_sync(0xffffffffu, mk, t);
+                        const int jt = __shfl_sync(0xffffffffu, jbv[u], t);
+                        const int k = p - __shfl_sync(0xffffffffu, excl, t);
+                        int x = 0;   // the largest x with popc(columns < x) <= k
+#pragma unroll
+                        for (int step = 8; step; step >>= 1)
+                            if (__popc(mt >> (TILE - (x + step))) <= k) x += step;
+                        if (p < total) g.colC[Rb + run + p] = jt + x;
+                    }
+                    run += total;
+                    continue;
                 }
-                run += total;
-                continue;
             }
-            // one output position per lane (coalesced stores): its slot t is
-            // the first lane whose inclusive count exceeds it, its column the
-            // k-th set column of that slot's mask
-            for (int p0 = 0; p0 < total; p0 += 32) {
-                const int p = p0 + lane;
-                int t = 0;
-#pragma unroll
-                for (int step = 16; step; step >>= 1)
-                    if (__shfl_sync(0xffffffffu, incl, t + step - 1) <= p) t += step;
-                const unsigned mt = __shfl_sync(0xffffffffu, mk, t);
-                const int jt = __shfl_sync(0xffffffffu, jbv[u], t);
-                const int k = p - __shfl_sync(0xffffffffu, excl, t);
-                int x = 0;   // the largest x with popc(columns < x) <= k
-#pragma unroll
-                for (int step = 8; step; step >>= 1)
-                    if (__popc(mt >> (TILE - (x + step))) <= k) x += step;
-                if (p < total) g.colC[Rb + run + p] = jt + x;
+            // few entries per tile row: each lane writes its own (a store
+            // per entry, consecutive lanes at consecutive positions)
+            unsigned m = mk;
+            long long dst = Rb + run + excl;
+            while (m) {
+                const int b = 31 - __clz(m);   // highest bit = smallest local column
+                g.colC[dst++] = jbv[u] + (TILE - 1 - b);
+                m &= ~(1u << b);
             }
             run += total;
         }
