@@ -421,12 +421,6 @@ struct PhaseTimer {
     int n = 0;
     PhaseTimer(tsg_ctx *c, bool enable) : ctx(c), on(enable) {}
     void mark() { if (on && n < 8) cudaEventRecord(ctx->ev[n++], ctx->stream); }
-    double between(int a, int b) {
-        if (!on || b >= n) return 0.0;
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, ctx->ev[a], ctx->ev[b]);
-        return ms;
-    }
 };
 
 // Everything the numeric step needs for one op(A, B), produced by the

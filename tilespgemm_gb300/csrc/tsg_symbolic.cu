@@ -25,7 +25,6 @@ namespace tsg {
 
 namespace {
 
-
 __device__ __forceinline__ int lower_bound_i(const int *a, int n, int key) {
     int lo = 0, hi = n;
     while (lo < hi) {
@@ -35,18 +34,6 @@ __device__ __forceinline__ int lower_bound_i(const int *a, int n, int key) {
     return lo;
 }
 
-// OR over the set bits (15-c) of `ma` of B tile q's row c masks
-__device__ __forceinline__ unsigned or_rows(unsigned ma, const uint16_t *__restrict__ bmask, long long q) {
-    unsigned acc = 0;
-    while (ma) {
-        int b = __ffs(ma) - 1;      // bit b <-> local column 15-b
-        acc |= bmask[q * TILE + (TILE - 1 - b)];
-        ma &= ma - 1;
-    }
-    return acc;
-}
-
-constexpr int STG = 64;   // B tiles staged per warp at a time
 constexpr int ENTRY_WALK_MAX = 3;   // mean A entries per A tile up to which step 2 walks A's rows by entry
 
 // Tile-row i's A tiles hold ENTRY_WALK_MAX entries or fewer on average: step
@@ -227,7 +214,6 @@ k_step2_win(int blkm, int m, const int *__restrict__ arp, const int *__restrict_
     const int rows = min(TILE, m - i * TILE);
     if (entry_walk(erpA, arp, i, rows)) return;   // sparse A tiles: k_step2_entries
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int span = ccol[c0 + S - 1] - ccol[c0] + 1;
     unsigned short *smask = reinterpret_cast<unsigned short *>(s_raw);                       // [16][smax]
     int *wcol = reinterpret_cast<int *>(s_raw + align16((long long)smax * TILE * 2));        // [smax]
     unsigned short *map = reinterpret_cast<unsigned short *>(s_raw + align16((long long)smax * TILE * 2) +
@@ -460,12 +446,24 @@ k_step2_entries(int blkm, int m, const int *__restrict__ arp, const long long *_
             if (u0 < u1) {
                 int lo = 0, hi = nb - 1;   // last entry whose units start at or before u0
                 while (lo < hi) { const int md = (lo + hi + 1) >> 1; if (e_pre[md] <= u0) lo = md; else hi = md - 1; }
+                // unit u's B entry for this lane (its A entry tt; -1: past
+                // the segment's end); the next unit's column is loaded before
+                // the current unit's update (OR does not depend on order)
+                auto unit_entry = [&](int u, int &tt) -> int {
+                    while (e_pre[tt + 1] <= u) ++tt;
+                    const int e = e_cur[tt] + ((u - e_pre[tt]) << 5) + lane;
+                    return e < e_wend[tt] ? e : -1;
+                };
                 int t = lo;
+                int e = unit_entry(u0, t);
+                int col = e >= 0 ? ecolB[e] : 0;
                 for (int u = u0; u < u1; ++u) {
-                    while (e_pre[t + 1] <= u) ++t;
-                    const int e = e_cur[t] + ((u - e_pre[t]) << 5) + lane;
-                    if (e < e_wend[t]) {
-                        const int col = ecolB[e];
+                    int tn = t, en = -1, coln = 0;
+                    if (u + 1 < u1) {
+                        en = unit_entry(u + 1, tn);
+                        if (en >= 0) coln = ecolB[en];
+                    }
+                    if (e >= 0) {
                         if (col >= cfirst && col < climit) {
                             const int sl = c_slot(col >> 4, jlo, wspan, use_map ? map : nullptr, wcol, nsl);
                             if (sl < 0) bad = true;
@@ -474,6 +472,7 @@ k_step2_entries(int blkm, int m, const int *__restrict__ arp, const long long *_
                             bad = true;   // a sorted segment lies inside its window
                         }
                     }
+                    t = tn; e = en; col = coln;
                 }
             }
             __syncthreads();
