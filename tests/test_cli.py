@@ -84,6 +84,41 @@ def test_integration_snippet_compiles_and_links(snippet_bin):
     assert snippet_bin.exists()
 
 
+README_MAIN = r"""
+#include <stdint.h>
+#include "tilespgemm.h"
+
+int main(void)
+{
+    int32_t rowptr[3] = {0, 1, 2}, col[2] = {0, 1};
+    double val[2] = {1.0, 2.0};
+    int32_t m = 2, n = 2;
+    int64_t nnz = 2;
+    {
+%s
+    }
+    return 0;
+}
+"""
+
+
+def test_readme_c_example_compiles_and_links(built_lib, tmp_path):
+    """The C example of README.md, given a 2 x 2 CSR, compiles with gcc
+    -std=c99 -Wall -Werror against include/tilespgemm.h and links."""
+    from tilespgemm_gb300 import build
+    cc = shutil.which("gcc")
+    if cc is None:
+        pytest.skip("gcc not found")
+    blocks = re.findall(r"```c\n(.*?)```", (ROOT / "README.md").read_text(), flags=re.S)
+    assert blocks, "README.md has no C block"
+    src = tmp_path / "readme.c"
+    src.write_text(README_MAIN % blocks[0])
+    res = subprocess.run([cc, "-std=c99", "-Wall", "-Werror", f"-I{ROOT / 'include'}", str(src),
+                          f"-L{build.LIBDIR}", "-ltilespgemm", f"-Wl,-rpath,{build.LIBDIR}", "-o", str(tmp_path / "readme")],
+                         capture_output=True, text=True)
+    assert res.returncode == 0, res.stderr
+
+
 def test_cli_usage_and_refusals(cli, tmp_path):
     res = subprocess.run([str(cli)], capture_output=True, text=True)
     assert res.returncode == 2 and "-d 0" in res.stderr
