@@ -375,11 +375,15 @@ tsg_status tsg_server_create(const tsg_server_opts *opts, tsg_server **server);
 /* TSG_ERR_BUDGET: the request alone exceeds the budget. */
 tsg_status tsg_server_submit(tsg_server *server, tsg_op op, const tsg_csr *A, const tsg_csr *B, uint64_t pattern_key,
                              int64_t *request_id);
-/* Blocks until the request is done; C receives the result. */
+/* Blocks until the request is done; C receives the result.  Submit and the
+ * waits may be called from several threads; each request is returned once:
+ * waiting for a request another thread is already waiting for returns
+ * TSG_ERR_INVALID_ARG. */
 tsg_status tsg_server_wait(tsg_server *server, int64_t request_id, tsg_csr *C, tsg_server_result *info);
 /* Any completed request, in completion order (its id in *request_id): a
  * collector that frees results as they finish holds at most the requests in
- * flight.  TSG_ERR_INVALID_ARG when no request is outstanding. */
+ * flight.  Requests a tsg_server_wait is waiting for are left to it.
+ * TSG_ERR_INVALID_ARG when no request is outstanding. */
 tsg_status tsg_server_wait_any(tsg_server *server, int64_t *request_id, tsg_csr *C, tsg_server_result *info);
 tsg_status tsg_server_destroy(tsg_server *server);
 

@@ -53,6 +53,7 @@ struct Request {
     tsg_status status = TSG_OK;
     std::string err;
     bool done = false;
+    bool claimed = false;    // a tsg_server_wait is waiting for it (wait_any skips it)
     int numeric_only = 0;
     int batched_with = 1;
 };
@@ -141,6 +142,7 @@ struct tsg_server {
     std::deque<Request *> pending;
     std::unordered_map<int64_t, Request *> reqs;
     std::deque<int64_t> finished;      // completed request ids, in completion order
+    int64_t unclaimed = 0;             // outstanding requests no waiter has claimed
     int64_t inflight_bytes = 0;
     int64_t next_id = 1;
     int rr = 0;
@@ -348,6 +350,7 @@ tsg_status tsg_server_submit(tsg_server *s, tsg_op op, const tsg_csr *A, const t
         std::lock_guard<std::mutex> lk(s->mu);
         r->id = s->next_id++;
         s->reqs[r->id] = r;
+        ++s->unclaimed;
         s->pending.push_back(r);
         admit(s);
     }
@@ -390,8 +393,12 @@ tsg_status tsg_server_wait(tsg_server *s, int64_t request_id, tsg_csr *C, tsg_se
         auto it = s->reqs.find(request_id);
         if (it == s->reqs.end()) { tsg::set_last_error("unknown request id"); return TSG_ERR_INVALID_ARG; }
         r = it->second;
+        if (r->claimed) { tsg::set_last_error("another thread is waiting for this request"); return TSG_ERR_INVALID_ARG; }
+        // claimed: no other waiter takes it, so r stays valid while this one sleeps
+        r->claimed = true;
+        --s->unclaimed;
         s->cv_done.wait(lk, [&] { return r->done; });
-        s->reqs.erase(it);
+        s->reqs.erase(request_id);
     }
     return finish_wait(r, C, info);
 }
@@ -403,10 +410,14 @@ tsg_status tsg_server_wait_any(tsg_server *s, int64_t *request_id, tsg_csr *C, t
     {
         std::unique_lock<std::mutex> lk(s->mu);
         for (;;) {
-            // ids already returned by tsg_server_wait are skipped
-            while (!s->finished.empty() && !s->reqs.count(s->finished.front())) s->finished.pop_front();
+            // ids returned by tsg_server_wait, or claimed by a waiting one, are skipped
+            while (!s->finished.empty()) {
+                auto f = s->reqs.find(s->finished.front());
+                if (f != s->reqs.end() && !f->second->claimed) break;
+                s->finished.pop_front();
+            }
             if (!s->finished.empty()) break;
-            if (s->reqs.empty()) { tsg::set_last_error("no outstanding requests"); return TSG_ERR_INVALID_ARG; }
+            if (s->unclaimed == 0) { tsg::set_last_error("no outstanding requests"); return TSG_ERR_INVALID_ARG; }
             s->cv_done.wait(lk);
         }
         const int64_t id = s->finished.front();
@@ -414,6 +425,7 @@ tsg_status tsg_server_wait_any(tsg_server *s, int64_t *request_id, tsg_csr *C, t
         auto it = s->reqs.find(id);
         r = it->second;
         s->reqs.erase(it);
+        --s->unclaimed;
         *request_id = id;
     }
     return finish_wait(r, C, info);

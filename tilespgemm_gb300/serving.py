@@ -58,8 +58,9 @@ class Server:
         c = _abi.tsg_csr()
         info = _abi.tsg_server_result()
         st = lib().tsg_server_wait(self.handle, C.c_int64(rid), C.byref(c), C.byref(info))
-        with self._lock:
-            self._keep.pop(rid, None)
+        if st != _abi.ERR_INVALID_ARG:   # returned (invalid: unknown, or another thread waits for it)
+            with self._lock:
+                self._keep.pop(rid, None)
         check(st)
         d = info.as_dict()
         d["nnz"] = int(c.nnz)
