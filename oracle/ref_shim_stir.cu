@@ -11,6 +11,7 @@
  *   step1 / step2          main_spgemm-col.cu:122-188, :572-627  (C tile structure)
  *   step3 / step4          main_spgemm-col.cu:899-994, :4073-4179 (C tile nnz, payload)
  *   mmio_allinone          mmio_highlevel.h:593-759  (Matrix Market load path)
+ *   mm_write_mtx_crd       mmio.h:780-850  (Matrix Market writer; real general here)
  * The reference's main() is renamed by the build recipe and never runs.
  */
 #include "main_spgemm-col.cu"
@@ -42,4 +43,14 @@ void ref_step4(int *arp, int *aci, int blkmA, int blknA, int *nnzbA, int mA,
 int ref_mmio_allinone(int *m, int *n, int *nnz, int *isSym, int **rp, int **col, double **val, char *fn)
 { return mmio_allinone(m, n, nnz, isSym, rp, col, val, fn); }
 void ref_free(void *p) { free(p); }
+int ref_mm_write_mtx_crd(char *fn, int M, int N, int nz, int *I, int *J, double *val)
+{
+    MM_typecode code;
+    mm_initialize_typecode(&code);
+    mm_set_matrix(&code);
+    mm_set_coordinate(&code);
+    mm_set_real(&code);
+    mm_set_general(&code);
+    return mm_write_mtx_crd(fn, M, N, nz, I, J, val, code);
+}
 }

@@ -1,5 +1,6 @@
-"""The host Matrix Market loader (tsg_load_mtx) against the reference's own
-mmio_allinone (mmio_highlevel.h:593-759), called live on generated files.
+"""The host Matrix Market loader (tsg_load_mtx) and writer (tsg_write_mtx)
+against the reference's own mmio_allinone (mmio_highlevel.h:593-759) and
+mm_write_mtx_crd (mmio.h:780-850), called live on generated files.
 
 These are well-formed files of every value type and symmetry the loader
 takes.  Entries are in random order, with duplicates, explicit zeros,
@@ -113,3 +114,44 @@ def test_loader_matches_reference_live(built_lib, ref_loader, monkeypatch, tmp_p
             assert np.array_equal(np.asarray(A.rowptr, np.int64), rrp.astype(np.int64))
             assert np.array_equal(np.asarray(A.col), rcol)
             assert np.array_equal(np.asarray(A.val).view(np.int64), rval.view(np.int64))
+
+
+@pytest.fixture(scope="module")
+def ref_writer():
+    try:
+        st = C.CDLL(str(REF / "libstir_ref.so"))
+        f = st.ref_mm_write_mtx_crd
+    except (OSError, AttributeError) as e:
+        pytest.skip(f"the reference's writer is not built here ({e})")
+    f.restype = C.c_int
+
+    def write(path, A):
+        rp = np.asarray(A.rowptr, np.int64)
+        rows = np.repeat(np.arange(A.m, dtype=np.int32), np.diff(rp).astype(np.int64)) + 1
+        cols = np.ascontiguousarray(np.asarray(A.col, np.int32) + 1)
+        vals = np.ascontiguousarray(np.asarray(A.val, np.float64))
+        rc = f(str(path).encode(), A.m, A.n, int(A.nnz), rows.ctypes.data_as(C.c_void_p),
+               cols.ctypes.data_as(C.c_void_p), vals.ctypes.data_as(C.c_void_p))
+        assert rc == 0
+    return write
+
+
+@pytest.mark.parametrize("threads", [1, 8])
+def test_writer_matches_reference_live(built_lib, ref_writer, monkeypatch, tmp_path, threads):
+    """tsg_write_mtx (the reference's line format) gives the bytes of the
+    reference's mm_write_mtx_crd for the same entries in CSR order: varied
+    magnitudes, negative zeros, duplicate and unsorted columns, empty rows."""
+    from tilespgemm_gb300 import matrices as M
+    from tilespgemm_gb300 import write_mtx
+    from tilespgemm_gb300.api import CSR
+    monkeypatch.setenv("TSG_MTX_THREADS", str(threads))
+    rng = np.random.default_rng(77)
+    for t, (m, n, k) in enumerate([(1, 1, 1), (53, 41, 3), (700, 900, 9)]):
+        X = M.random_sparse(m, n, k, seed=200 + t, dup=True, unsorted=True, empty_rows=0.2)
+        v = rng.standard_normal(X.nnz) * 10.0 ** rng.integers(-300, 300, X.nnz)
+        v[rng.random(X.nnz) < 0.05] = -0.0
+        A = CSR(X.m, X.n, np.asarray(X.rowptr, np.int64), np.asarray(X.col, np.int32), v)
+        ours, theirs = tmp_path / f"ours{t}.mtx", tmp_path / f"ref{t}.mtx"
+        write_mtx(ours, A)
+        ref_writer(theirs, A)
+        assert ours.read_bytes() == theirs.read_bytes()

@@ -118,7 +118,8 @@ def build_reference() -> bool:
     sit and does nothing where there is none.  True when the libraries exist."""
     out = ROOT / "oracle" / "_ref"
     have = lambda: (out / "libthmkl_ref.so").exists() and (out / "libstir_ref.so").exists()  # noqa: E731
-    if not have():
+    recipe = [ROOT / "oracle" / "build_ref.sh", ROOT / "oracle" / "ref_shim_stir.cu"]
+    if not have() or _stale(out / "libstir_ref.so", recipe) or _stale(out / "libthmkl_ref.so", recipe):
         _run(["bash", str(ROOT / "oracle" / "build_ref.sh")])
     return have()
 
