@@ -90,3 +90,23 @@ def test_oracle_detects_planted_error():
     val = val.copy()
     val[7] += 1.0
     assert not np.array_equal(val, d["c_val"])
+
+
+@pytest.mark.parametrize("name", ["rand100_AA", "rect77x130_AAT", "dup_unsorted64_AA", "emptyrows90_AA", "rmat8_AAT"])
+def test_row_subset_oracle_matches_whole_product(name):
+    """orc_spgemm_rows, the checker of sampled rows at full size, gives
+    exactly the rows of the whole product (and of the reference's), for
+    rows in any order with repeats."""
+    d = load_case(name)
+    rp, col, val, bnd = O.spgemm(d["A"], d["B"], with_bound=True)
+    m = int(d["m"])
+    rng = np.random.default_rng(3)
+    rows = np.concatenate([rng.permutation(m)[: max(1, m // 3)], [0, m - 1, 0]])
+    srp, scol, sval, sbnd = O.spgemm_rows(d["A"], d["B"], rows)
+    assert srp[0] == 0 and srp.size == rows.size + 1
+    for t, r in enumerate(rows):
+        a, b = srp[t], srp[t + 1]
+        assert np.array_equal(scol[a:b], col[rp[r]:rp[r + 1]])
+        assert np.array_equal(sval[a:b].view(np.int64), val[rp[r]:rp[r + 1]].view(np.int64))
+        assert np.array_equal(sbnd[a:b], bnd[rp[r]:rp[r + 1]])
+        assert np.array_equal(scol[a:b], d["c_col"][d["c_rowptr"][r]:d["c_rowptr"][r + 1]])
